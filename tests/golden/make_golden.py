@@ -1,0 +1,189 @@
+"""Write golden fixtures by running the UNMODIFIED xreac reference (v0.10.0) in this container.
+
+Usage (needs the reference checkout; not run by the test suite):
+
+    python tests/golden/make_golden.py /root/reference
+
+The reference depends on HIPS ``autograd``, which is not installed here, so the
+torch-backed stand-in in ``tests/golden/shim`` goes first on ``sys.path``. With
+it, ``xreac.Calculator.evaluate`` runs unchanged: energies and charges come from
+numpy, forces from the reference's own derivative graph replayed by
+``torch.autograd``.
+
+For every case the script records the inputs, the reference's ``Evaluation``
+fields, its canonical neighbour list ``(i, j, S)`` and its per-edge corrected
+bond orders, into one compressed ``<case>.npz``. It also records the parsed
+parameter dicts of the bundled force fields (``forcefields.json``) so the parser
+can be checked without the reference present.
+
+Cases: the reference's own test geometries (imported from its ``examples/`` and
+``tests/``), small versions of the benchmark workloads generated with
+``xreac_gb300.workloads`` (the 192-atom water cluster is the full-size cluster
+workload), and a few request-stream samples.
+"""
+
+from __future__ import annotations
+
+import json
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+REPO = HERE.parents[1]
+
+
+def _setup(reference):
+    reference = Path(reference)
+    for p in (REPO, reference / "tests", reference / "examples", reference / "src", HERE / "shim"):
+        sys.path.insert(0, str(p))
+
+
+def reference_cases():
+    """Geometries of the reference's own tests (examples/*.py and tests/cases.py)."""
+    from cases import CASES  # tests/cases.py
+    from periodic_water import periodic_cases
+    from small_cells import small_cell_cases
+    from water_cluster import water_cases
+
+    out = {}
+    water = water_cases()
+    for name, (s, x) in water.items():
+        out["water_" + name] = ("ffield.reax.HO.2015", s, x, None, None, 0.0)
+    for name, (s, x, cell, pbc) in periodic_cases(include_bulk=True).items():
+        out["periodic_" + name] = ("ffield.reax.HO.2015", s, x, cell, pbc, 0.0)
+    for name, (ff, s, x, cell, pbc) in small_cell_cases().items():
+        out["small_" + name] = (ff, s, x, cell, pbc, 0.0)
+    for name, (s, x) in CASES.items():
+        out["zno_" + name] = ("ffield.reax.ZnOH.2010", s, np.asarray(x, dtype=float), None, None, 0.0)
+    methane = np.vstack(([0, 0, 0], 0.63 * np.array([[1, 1, 1], [1, -1, -1], [-1, 1, -1], [-1, -1, 1]])))
+    out["carbon_methane"] = ("ffield.reax.CHO.2008", ["C"] + ["H"] * 4, methane, None, None, 0.0)
+    out["carbon_monoxide"] = ("ffield.reax.CHO.2008", ["C", "O"], np.array([[0.0, 0, 0], [1.15, 0, 0]]), None, None, 0.0)
+    out["carbon_dimer"] = ("ffield.reax.CHO.2008", ["C", "C"], np.array([[0.0, 0, 0], [1.2, 0, 0]]), None, None, 0.0)
+    out["periodic_carbon_chain"] = (
+        "ffield.reax.CHO.2008",
+        ["C"] * 3,
+        np.array([[0.0, 0, 0], [1.5, 0.4, 0.2], [3.0, -0.2, 0.8]]),
+        np.diag([4.5, 12.0, 12.0]),
+        [True, False, False],
+        0.0,
+    )
+    s, x = water["monomer"]
+    out["charged_hydroxide"] = ("ffield.reax.HO.2015", s[:2], x[:2].copy(), None, None, -1.0)
+    out["charged_hydronium"] = ("ffield.reax.HO.2015", s + ["H"], np.vstack((x, [-0.3, -0.45, 0.85])), None, None, 1.0)
+    ff, s, x, cell, pbc = small_cell_cases()["water_4A"]
+    out["charged_water_4A"] = (ff, s, x, cell, pbc, -1.0)
+    return out
+
+
+def workload_cases():
+    """Seeded systems shaped like the benchmark workloads."""
+    from xreac_gb300 import workloads as w
+
+    out = {}
+
+    def add(name, sys_):
+        out[name] = (sys_.force_field, list(sys_.symbols), sys_.positions, sys_.cell, sys_.pbc, sys_.total_charge)
+
+    add("cluster_water_192", w.water_cluster())  # the full 64-H2O cluster workload
+    add("box_water_192", w.water_box(n_mol=64, box=12.42, seed=2))
+    add("box_cho_89", w.cho_mixture(counts=(8, 8, 8, 3), seed=3))
+    add("peroxide", w.hydrogen_peroxide())
+    add("anatase_water_288", w.anatase_slab_water(displacement=0.05))
+    stream = w.request_stream(n_requests=48, seed=4, periodic_fraction=0.2, charged_fraction=0.1)
+    picked = [r for r in stream if r.system.n <= 160][:8]
+    for r in picked:
+        add(f"stream_{r.index:02d}", r.system)
+    return out
+
+
+def _ff_to_json(ff):
+    def num(v):
+        return [float(t) for t in np.asarray(v).ravel()]
+
+    return dict(
+        checksum=ff.checksum,
+        citation=ff.citation,
+        general=num(ff.general),
+        atoms={s: {k: float(v) for k, v in a.items()} for s, a in ff.atoms.items()},
+        pairs={f"{s}|{t}": {k: float(v) for k, v in p.items()} for (s, t), p in ff.pairs.items()},
+        angles={"|".join(k): [num(r) for r in v] for k, v in ff.angles.items()},
+        torsions={"|".join(k): num(v) for k, v in ff.torsions.items()},
+        hydrogen_bonds={"|".join(k): num(v) for k, v in ff.hydrogen_bonds.items()},
+        vdw_type=ff.vdw_type,
+        elements=list(ff.elements),
+    )
+
+
+def run_case(name, ff_name, symbols, x, cell, pbc, charge, full_derivative=False):
+    import xreac
+    from xreac.energy import EnergyModel
+    from xreac.neighbors import replicated_neighbors
+
+    ff = xreac.ForceField.bundled(ff_name)
+    calc = xreac.Calculator(ff)
+    t0 = time.time()
+    res = calc.evaluate(symbols, x, cell=cell, pbc=pbc, total_charge=charge, full_derivative=full_derivative)
+    elapsed = time.time() - t0
+    # Per-edge quantities from the pure-numpy forward pass of the same model.
+    (nb, _) = replicated_neighbors(np.asarray(x, float), ff.general[12], cell, pbc)
+    model = EnergyModel(ff, symbols, nb, cell, pbc, total_charge=charge)
+    _, r = model.edges.geometry(np.asarray(x, float))
+    q = model.electrostatics(r)[0]
+    comps, _, (bo, total, nlp) = model.components(np.asarray(x, float), q, return_bond_state=True)
+    n = len(symbols)
+    nz = np.flatnonzero(bo)
+    data = dict(
+        ff=np.array(ff_name),
+        symbols=np.array(symbols),
+        positions=np.asarray(x, dtype=float),
+        cell=np.zeros((0, 3)) if cell is None else np.asarray(cell, dtype=float).reshape(-1, 3),
+        pbc=np.broadcast_to(np.asarray(pbc if pbc is not None else cell is not None, dtype=bool), (3,)).copy(),
+        total_charge=np.array(float(charge)),
+        full_derivative=np.array(bool(full_derivative)),
+        energy=np.array(res.energy),
+        energy_numpy=np.array(float(np.sum(comps))),
+        components=np.array([res.components[k] for k in xreac.energy.COMPONENTS]),
+        forces=res.forces,
+        charges=res.charges,
+        total_bond_orders=res.total_bond_orders,
+        lone_pairs=res.lone_pairs,
+        bond_counts=res.bond_counts,
+        dipole=res.dipole,
+        cell_repetitions=np.array(res.cell_repetitions),
+        edge_i=model.edges.i.astype(np.int32),
+        edge_j=model.edges.j.astype(np.int32),
+        edge_S=model.edges.shifts.astype(np.int8),
+        bo_index=nz.astype(np.int32),
+        bo_value=bo[nz],
+        seconds=np.array(elapsed),
+    )
+    if n <= 200:
+        data["bond_orders"] = res.bond_orders
+    np.savez_compressed(HERE / f"{name}.npz", **data)
+    return elapsed, len(model.edges.i)
+
+
+def main(reference):
+    _setup(reference)
+    import xreac
+
+    ffs = {}
+    for name in ("ffield.reax.HO.2015", "ffield.reax.CHO.2008", "ffield.reax.ZnOH.2010", "ffield.reax.TiOH.Kim2013"):
+        ffs[name] = _ff_to_json(xreac.ForceField.bundled(name))
+    (HERE / "forcefields.json").write_text(json.dumps(ffs, sort_keys=True))
+    cases = reference_cases()
+    cases.update(workload_cases())
+    for name, (ff_name, s, x, cell, pbc, charge) in cases.items():
+        dt, m = run_case(name, ff_name, list(s), x, cell, pbc, charge)
+        print(f"{name:28s} n={len(s):4d} edges={m:7d} {dt:6.2f} s", flush=True)
+    for name in ("water_distorted_dimer", "zno_cluster20", "small_water_4A", "carbon_methane"):
+        ff_name, s, x, cell, pbc, charge = cases[name]
+        run_case(name + "_full", ff_name, list(s), x, cell, pbc, charge, full_derivative=True)
+        print(f"{name + '_full':28s} (charge-response forces)", flush=True)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
