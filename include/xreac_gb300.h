@@ -1,0 +1,114 @@
+/*
+ * xreac_gb300 -- C ABI of the GB300 ReaxFF evaluator.
+ *
+ * The entry points replace the evaluation path behind hsulab/xreac's Python API:
+ *   ForceField.from_file / bundled          (src/xreac/forcefield.py:84-95, 120-315) -> xr_ff_create
+ *   Calculator(force_field)                  (src/xreac/calculator.py:69-74)          -> xr_ctx_create
+ *   Calculator.evaluate(symbols, positions, total_charge, cell, pbc, full_derivative)
+ *                                            (src/xreac/calculator.py:76-165)         -> xr_eval
+ *   one evaluate per request, batched        (no reference counterpart; serving)      -> xr_eval_batch
+ *   the ValueError raised by evaluate        (src/xreac/calculator.py:58-66, 149-154) -> return code + xr_last_error
+ *   Neighbors(i, j, S) of an evaluation      (src/xreac/neighbors.py:101-131)         -> xr_get_neighbors
+ *   Evaluation.bond_orders (sparse form)     (src/xreac/energy.py:167-178)            -> xr_get_bonds
+ *
+ * Plain pointers and sizes only. Units: Angstrom, kcal/mol, kcal/mol/Angstrom, elementary charge.
+ * All floating point is IEEE double. Arrays are C-contiguous.
+ */
+#ifndef XREAC_GB300_H
+#define XREAC_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Return codes. xr_last_error(ctx) gives the message, worded as xreac's ValueError texts. */
+enum xr_status {
+  XR_OK = 0,
+  XR_EINPUT = 1,        /* invalid arguments (shapes, types, cell) */
+  XR_ECOINCIDENT = 2,   /* "Coincident atoms are not supported" */
+  XR_ESINGULAR = 3,     /* "Singular QEq system; check the geometry and parameters" */
+  XR_ENONFINITE = 4,    /* "Non-finite energy, charges, or forces; check the geometry" */
+  XR_ECHARGE = 5,       /* "QEq charge constraint failed" */
+  XR_ECOLLINEAR = 6,    /* "Collinear atoms in an active torsion: ..." */
+  XR_ECAPACITY = 7,     /* a device list outgrew its limit (image shifts beyond +-255 cells) */
+  XR_EBADPARAM = 8,     /* "Invalid p_boc* mixing for an active bond-order correction" */
+  XR_ECUDA = 9,         /* CUDA runtime failure */
+  XR_EUNSUPPORTED = 10  /* requested option not available */
+};
+
+/* Evaluation flags. */
+#define XR_FLAG_FULL_DERIVATIVE 1u /* charge-response forces (xreac full_derivative=True) */
+#define XR_FLAG_DEVICE_IO 2u       /* positions and result arrays are device pointers */
+
+typedef struct xr_ff xr_ff;
+typedef struct xr_ctx xr_ctx;
+
+/* One system. positions: natoms x 3. cell: 9 doubles (three row vectors) or NULL when no
+ * direction is periodic. types: element numbers in parameter-file order. */
+typedef struct {
+  int natoms;
+  const int* types;
+  const double* positions;
+  const double* cell;
+  int pbc[3];
+  double total_charge;
+} xr_system;
+
+/* Results of one system. Any pointer may be NULL to skip that output.
+ * energy: 15 doubles = the 14 components in xreac's order (bond, atom, lone_pair, molecule, angle,
+ * penalty, angle_conjugation, hydrogen_bond, torsion, conjugation, vdw, coulomb, electric_field,
+ * qeq) followed by the total. */
+typedef struct {
+  double* energy;
+  double* forces;            /* natoms x 3 */
+  double* charges;           /* natoms */
+  double* total_bond_orders; /* natoms */
+  double* lone_pairs;        /* natoms */
+  int* bond_counts;          /* natoms */
+  double* dipole;            /* 3 */
+} xr_result;
+
+/* Force field: packed tables as produced by xreac_gb300.forcefield.ForceField.tables().
+ * general: 39; atom: ntypes x 24; pair: ntypes^2 x 28; is_carbon: ntypes;
+ * angle_index: ntypes^3 x 2 (first, count) into angle (nangle x 7);
+ * torsion_index: ntypes^4 (row or -1) into torsion (ntorsion x 5);
+ * hbond_index: ntypes^3 (row or -1) into hbond (nhbond x 4). vdw_type: 1, 2 or 3. */
+int xr_ff_create(const double* general, int ntypes, const double* atom, const double* pair, const int* is_carbon,
+                 int vdw_type, const int* angle_index, const double* angle, int nangle, const int* torsion_index,
+                 const double* torsion, int ntorsion, const int* hbond_index, const double* hbond, int nhbond,
+                 xr_ff** out);
+void xr_ff_destroy(xr_ff* ff);
+
+/* Context: device work buffers (grown on demand, reused across calls) and a CUDA stream.
+ * stream may be NULL (the context creates its own) or a cudaStream_t owned by the caller.
+ * A context is used by one host thread at a time. */
+int xr_ctx_create(int device, void* stream, xr_ctx** out);
+void xr_ctx_destroy(xr_ctx* ctx);
+const char* xr_last_error(const xr_ctx* ctx);
+
+/* Solver settings: QEq conjugate-gradient relative residual and iteration limit. */
+int xr_ctx_set_qeq(xr_ctx* ctx, double tolerance, int max_iterations);
+
+/* Evaluate one system (energy, fixed-charge forces, QEq charges, per-atom bond properties). */
+int xr_eval(xr_ctx* ctx, const xr_ff* ff, const xr_system* sys, unsigned flags, xr_result* out);
+
+/* Evaluate nsys independent systems in one ragged batch with per-system offsets. */
+int xr_eval_batch(xr_ctx* ctx, const xr_ff* ff, int nsys, const xr_system* sys, unsigned flags, xr_result* out);
+
+/* Neighbour list of the last evaluation of system `index` of the last batch, in canonical
+ * (i, j, Sx, Sy, Sz) order: i, j (capacity entries each), S (capacity x 3). *count receives the
+ * number of directed edges; nothing is written when capacity is too small. Host pointers. */
+int xr_get_neighbors(xr_ctx* ctx, int index, int* i, int* j, int* S, long long capacity, long long* count);
+
+/* Bond orders of the last evaluation of system `index`, one entry per bond-order candidate
+ * (unordered image pair within min(5 A, cutoff)): i, j, S (x3) and the corrected bond order.
+ * Host pointers; *count as for xr_get_neighbors. */
+int xr_get_bonds(xr_ctx* ctx, int index, int* i, int* j, int* S, double* bo, long long capacity, long long* count);
+
+/* Number of CUDA kernels the last xr_eval / xr_eval_batch call launched. */
+long long xr_last_launches(const xr_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* XREAC_GB300_H */

@@ -1,0 +1,178 @@
+"""ctypes bindings of the C ABI declared in include/xreac_gb300.h.
+
+The library is built in-tree (``python -m xreac_gb300.build``). There is no CPU fallback: when the
+library or a GPU is missing, loading fails with an error that says so.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from ctypes import POINTER, byref, c_char_p, c_double, c_int, c_longlong, c_uint, c_void_p
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libxreac_gb300.so"
+
+XR_OK = 0
+XR_EINPUT = 1
+XR_ECOINCIDENT = 2
+XR_ESINGULAR = 3
+XR_ENONFINITE = 4
+XR_ECHARGE = 5
+XR_ECOLLINEAR = 6
+XR_ECAPACITY = 7
+XR_EBADPARAM = 8
+XR_ECUDA = 9
+XR_EUNSUPPORTED = 10
+
+XR_FLAG_FULL_DERIVATIVE = 1
+XR_FLAG_DEVICE_IO = 2
+
+EXPORTED = (
+    "xr_ff_create",
+    "xr_ff_destroy",
+    "xr_ctx_create",
+    "xr_ctx_destroy",
+    "xr_last_error",
+    "xr_ctx_set_qeq",
+    "xr_eval",
+    "xr_eval_batch",
+    "xr_get_neighbors",
+    "xr_get_bonds",
+    "xr_last_launches",
+)
+
+
+class System(ctypes.Structure):
+    _fields_ = [
+        ("natoms", c_int),
+        ("types", POINTER(c_int)),
+        ("positions", POINTER(c_double)),
+        ("cell", POINTER(c_double)),
+        ("pbc", c_int * 3),
+        ("total_charge", c_double),
+    ]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [
+        ("energy", POINTER(c_double)),
+        ("forces", POINTER(c_double)),
+        ("charges", POINTER(c_double)),
+        ("total_bond_orders", POINTER(c_double)),
+        ("lone_pairs", POINTER(c_double)),
+        ("bond_counts", POINTER(c_int)),
+        ("dipole", POINTER(c_double)),
+    ]
+
+
+_LIB = None
+
+
+def load():
+    """Load the CUDA library; raises if it was not built (no CPU fallback exists)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not LIB_PATH.exists():
+        raise RuntimeError(
+            f"xreac_gb300 CUDA library not found at {LIB_PATH}; build it with `python -m xreac_gb300.build`"
+        )
+    lib = ctypes.CDLL(str(LIB_PATH))
+    lib.xr_ff_create.argtypes = [
+        POINTER(c_double), c_int, POINTER(c_double), POINTER(c_double), POINTER(c_int), c_int,
+        POINTER(c_int), POINTER(c_double), c_int, POINTER(c_int), POINTER(c_double), c_int,
+        POINTER(c_int), POINTER(c_double), c_int, POINTER(c_void_p),
+    ]
+    lib.xr_ff_create.restype = c_int
+    lib.xr_ff_destroy.argtypes = [c_void_p]
+    lib.xr_ff_destroy.restype = None
+    lib.xr_ctx_create.argtypes = [c_int, c_void_p, POINTER(c_void_p)]
+    lib.xr_ctx_create.restype = c_int
+    lib.xr_ctx_destroy.argtypes = [c_void_p]
+    lib.xr_ctx_destroy.restype = None
+    lib.xr_last_error.argtypes = [c_void_p]
+    lib.xr_last_error.restype = c_char_p
+    lib.xr_ctx_set_qeq.argtypes = [c_void_p, c_double, c_int]
+    lib.xr_ctx_set_qeq.restype = c_int
+    lib.xr_eval.argtypes = [c_void_p, c_void_p, POINTER(System), c_uint, POINTER(Result)]
+    lib.xr_eval.restype = c_int
+    lib.xr_eval_batch.argtypes = [c_void_p, c_void_p, c_int, POINTER(System), c_uint, POINTER(Result)]
+    lib.xr_eval_batch.restype = c_int
+    lib.xr_get_neighbors.argtypes = [c_void_p, c_int, POINTER(c_int), POINTER(c_int), POINTER(c_int), c_longlong,
+                                     POINTER(c_longlong)]
+    lib.xr_get_neighbors.restype = c_int
+    lib.xr_get_bonds.argtypes = [c_void_p, c_int, POINTER(c_int), POINTER(c_int), POINTER(c_int), POINTER(c_double),
+                                 c_longlong, POINTER(c_longlong)]
+    lib.xr_get_bonds.restype = c_int
+    lib.xr_last_launches.argtypes = [c_void_p]
+    lib.xr_last_launches.restype = c_longlong
+    _LIB = lib
+    return lib
+
+
+def ptr(a, ctype):
+    """Pointer to a C-contiguous numpy array (or NULL for None)."""
+    if a is None:
+        return None
+    return a.ctypes.data_as(POINTER(ctype))
+
+
+class ForceFieldHandle:
+    """Device copy of a force field's packed tables (``xr_ff``)."""
+
+    def __init__(self, tables, is_carbon, vdw_type):
+        lib = load()
+        self._lib = lib
+        t = tables
+        keep = dict(
+            general=np.ascontiguousarray(t["general"], dtype=np.float64),
+            atom=np.ascontiguousarray(t["atom"], dtype=np.float64),
+            pair=np.ascontiguousarray(t["pair"], dtype=np.float64),
+            is_carbon=np.ascontiguousarray(is_carbon, dtype=np.int32),
+            angle_index=np.ascontiguousarray(t["angle_index"], dtype=np.int32),
+            angle=np.ascontiguousarray(t["angle"], dtype=np.float64),
+            torsion_index=np.ascontiguousarray(t["torsion_index"], dtype=np.int32),
+            torsion=np.ascontiguousarray(t["torsion"], dtype=np.float64),
+            hbond_index=np.ascontiguousarray(t["hbond_index"], dtype=np.int32),
+            hbond=np.ascontiguousarray(t["hbond"], dtype=np.float64),
+        )
+        handle = c_void_p()
+        code = lib.xr_ff_create(
+            ptr(keep["general"], c_double), int(t["ntypes"]), ptr(keep["atom"], c_double), ptr(keep["pair"], c_double),
+            ptr(keep["is_carbon"], c_int), int(vdw_type), ptr(keep["angle_index"], c_int), ptr(keep["angle"], c_double),
+            len(keep["angle"]), ptr(keep["torsion_index"], c_int), ptr(keep["torsion"], c_double), len(keep["torsion"]),
+            ptr(keep["hbond_index"], c_int), ptr(keep["hbond"], c_double), len(keep["hbond"]), byref(handle),
+        )
+        if code != XR_OK:
+            raise RuntimeError(f"xr_ff_create failed with code {code}")
+        self.handle = handle
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value:
+            self._lib.xr_ff_destroy(h)
+            self.handle = None
+
+
+class Context:
+    """Device work buffers and stream of one host thread (``xr_ctx``)."""
+
+    def __init__(self, device=0, stream=None):
+        lib = load()
+        self._lib = lib
+        handle = c_void_p()
+        code = lib.xr_ctx_create(int(device), c_void_p(stream) if stream else None, byref(handle))
+        if code != XR_OK:
+            raise RuntimeError(f"xr_ctx_create failed with code {code} (is a CUDA GPU available?)")
+        self.handle = handle
+
+    def last_error(self):
+        return self._lib.xr_last_error(self.handle).decode()
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value:
+            self._lib.xr_ctx_destroy(h)
+            self.handle = None

@@ -1,0 +1,836 @@
+// Bond orders, bonded energy terms and their hand-written adjoints (FP64).
+//
+// Forward equations restate src/xreac/energy.py:105-370 (bond orders and corrections, bond,
+// lone-pair, over/under-coordination, C2 and triple-bond corrections, valence angle, penalty,
+// angle conjugation, torsion, four-body conjugation and hydrogen bonds). Forces are the exact
+// derivative of that energy at fixed charges, written by hand in reverse mode: every term kernel
+// adds its sensitivities to
+//   - per-bond accumulators  dE/d bo, dE/d pi, dE/d pp, dE/d sigma      (thresholded outputs)
+//   - per-atom accumulators  dE/d total, dE/d d, dE/d db, dE/d sbo2
+//   - atom gradients directly for the angular geometry,
+// and the chain kernels then carry those back through the per-atom sums, the bond-order
+// correction f1..f5 and the uncorrected bond orders to dE/dr per bond, which lands on the pair's
+// radial accumulator. The near-collinear angle rule -1/max(sin, 1e-5) of xreac's fixed-charge
+// forces (src/xreac/energy.py:49-55) is reproduced; thresholds are not differentiated, exactly as
+// xreac's getval() masks are not.
+//
+// Layout: bonds are half pairs (each unordered image pair once); dbrow lists, per atom, its
+// directed bond edges in canonical order as (bond id, +1 source / -1 target), so per-atom sums
+// are gathers in the reference's order and need no atomics.
+#include "xr_common.cuh"
+
+namespace {
+
+constexpr double THB_CUT = 0.001;
+constexpr double THB_PRODUCT_CUT = 0.00001;
+constexpr double HBOND_THRESHOLD = 0.01;
+
+struct Ctx {
+  XrWork w;
+  XrFF ff;
+};
+
+#define AFV(k, a) w.a_fwd[(size_t)(k) * w.A + (a)]
+#define AJV(k, a) w.a_adj[(size_t)(k) * w.A + (a)]
+#define AEV(k, a) w.a_e[(size_t)(k) * w.A + (a)]
+#define BFV(k, b) w.b_fwd[(size_t)(k) * w.cap_B + (b)]
+#define BJV(k, b) w.b_adj[(size_t)(k) * w.cap_B + (b)]
+#define BEV(k, b) w.b_e[(size_t)(k) * w.cap_B + (b)]
+
+__device__ inline double atom_prm(const XrFF& ff, int t, int col) { return __ldg(ff.atom + t * XR_NATOM_COLS + col); }
+__device__ inline double pair_prm(const XrFF& ff, int pt, int col) { return __ldg(ff.pair + pt * XR_NPAIR_COLS + col); }
+
+__device__ inline void atomic_add3(double* f, int a, double gx, double gy, double gz) {
+  atomicAdd(f + 3 * a + 0, gx);
+  atomicAdd(f + 3 * a + 1, gy);
+  atomicAdd(f + 3 * a + 2, gz);
+}
+
+// Vector from `atom` to the other end of bond b, for the bond-row entry direction `dir`.
+__device__ inline void bond_vec(const XrWork& w, int b, int dir, double v[3]) {
+  const double s = (double)dir;
+  v[0] = s * w.b_v[0 * w.cap_B + b];
+  v[1] = s * w.b_v[1 * w.cap_B + b];
+  v[2] = s * w.b_v[2 * w.cap_B + b];
+}
+__device__ inline int bond_other(const XrWork& w, int b, int dir) { return dir > 0 ? w.bond_j[b] : w.bond_i[b]; }
+// Image shift bits of the directed edge for a bond-row entry.
+__device__ inline uint32_t bond_shift(const XrWork& w, int b, int dir) {
+  const uint32_t c = (uint32_t)w.edge[w.pair_edge[w.bond_pair[b]]].y & XR_SHIFT_MASK;
+  return dir > 0 ? c : xr_neg_shift(c);
+}
+
+// ------------------------------------------------------------------ uncorrected bond orders
+// sigma' = (1+cut) exp(p_bo1 (r/r_s)^p_bo2), pi' = exp(p_bo3 (r/r_p)^p_bo4), pp' likewise;
+// raw = sum; active when raw >= cut; bo0 = raw - cut (src/xreac/energy.py:130-149).
+__global__ void k_bo1(XrWork w, XrFF ff) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= w.nB) return;
+  const int i = w.bond_i[b], j = w.bond_j[b];
+  const uint32_t code = (uint32_t)w.edge[w.pair_edge[w.bond_pair[b]]].y;
+  const XrSystem& S = w.sys[w.sys_of[i]];
+  const int sx = xr_sx(code), sy = xr_sy(code), sz = xr_sz(code);
+  const double4_32a xi = w.x[i], xj = w.x[j];
+  const double xa[3] = {xi.x, xi.y, xi.z}, xb[3] = {xj.x, xj.y, xj.z};
+  double v[3];
+  for (int c = 0; c < 3; ++c) {
+    const double off = __dadd_rn(__dadd_rn(__dmul_rn((double)sx, S.cell[c]), __dmul_rn((double)sy, S.cell[3 + c])),
+                                 __dmul_rn((double)sz, S.cell[6 + c]));
+    v[c] = __dadd_rn(__dsub_rn(xb[c], xa[c]), off);
+  }
+  const double r = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(v[0], v[0]), __dmul_rn(v[1], v[1])), __dmul_rn(v[2], v[2])));
+  w.b_r[b] = r;
+  w.b_v[0 * w.cap_B + b] = v[0];
+  w.b_v[1 * w.cap_B + b] = v[1];
+  w.b_v[2 * w.cap_B + b] = v[2];
+  const int ti = w.type[i], tj = w.type[j], T = ff.ntypes;
+  const int pt = ti * T + tj;
+  const double cut = 0.01 * ff.g[29];
+  const double lr = log(r);
+  double sig = 0, pi = 0, pp = 0, dsig = 0, dpi = 0, dpp = 0;
+  if (atom_prm(ff, ti, A_R_S) > 0 && atom_prm(ff, tj, A_R_S) > 0) {
+    const double p1 = pair_prm(ff, pt, P_BO1), p2 = pair_prm(ff, pt, P_BO2);
+    const double t = exp(p2 * (lr - __ldg(ff.pair_logr + 3 * pt + 0)));
+    sig = (1.0 + cut) * exp(p1 * t);
+    dsig = sig * p1 * p2 * t / r;
+  }
+  if (atom_prm(ff, ti, A_R_PI) > 0 && atom_prm(ff, tj, A_R_PI) > 0) {
+    const double p3 = pair_prm(ff, pt, P_BO3), p4 = pair_prm(ff, pt, P_BO4);
+    const double t = exp(p4 * (lr - __ldg(ff.pair_logr + 3 * pt + 1)));
+    pi = exp(p3 * t);
+    dpi = pi * p3 * p4 * t / r;
+  }
+  if (atom_prm(ff, ti, A_R_PI_PI) > 0 && atom_prm(ff, tj, A_R_PI_PI) > 0) {
+    const double p5 = pair_prm(ff, pt, P_BO5), p6 = pair_prm(ff, pt, P_BO6);
+    const double t = exp(p6 * (lr - __ldg(ff.pair_logr + 3 * pt + 2)));
+    pp = exp(p5 * t);
+    dpp = pp * p5 * p6 * t / r;
+  }
+  const double raw = sig + pi + pp;
+  const bool mask = raw >= cut;
+  BFV(BF_BO0, b) = mask ? raw - cut : 0.0;
+  BFV(BF_PI0, b) = mask ? pi : 0.0;
+  BFV(BF_PP0, b) = mask ? pp : 0.0;
+  BFV(BF_DSIG, b) = dsig;
+  BFV(BF_DPI, b) = dpi;
+  BFV(BF_DPP, b) = dpp;
+  BFV(BF_MASK, b) = mask ? 1.0 : 0.0;
+}
+
+// Delta'_a = sum of uncorrected bond orders over the atom's directed bond edges.
+__global__ void k_deltap(XrWork w) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= w.A) return;
+  const int L = w.A + 1;
+  double s = 0;
+  for (int k = w.cnt[3 * L + a]; k < w.cnt[3 * L + a + 1]; ++k) s += BFV(BF_BO0, w.dbrow[k].x);
+  AFV(AF_DELTAP, a) = s;
+}
+
+// Corrected bond orders (src/xreac/energy.py:150-165).
+__global__ void k_bo2(XrWork w, XrFF ff) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= w.nB) return;
+  const int i = w.bond_i[b], j = w.bond_j[b];
+  const int ti = w.type[i], tj = w.type[j], T = ff.ntypes, pt = ti * T + tj;
+  const double* g = ff.g;
+  const double bo0 = BFV(BF_BO0, b), pi0 = BFV(BF_PI0, b), pp0 = BFV(BF_PP0, b);
+  const bool mask = BFV(BF_MASK, b) != 0.0;
+  const double ovc = pair_prm(ff, pt, P_OVC), v13 = pair_prm(ff, pt, P_V13COR);
+  const bool corrected = mask && (ovc >= 0.001 || v13 >= 0.001);
+  double boc3 = pair_prm(ff, pt, P_BOC3), boc4 = pair_prm(ff, pt, P_BOC4), boc5 = pair_prm(ff, pt, P_BOC5);
+  if (corrected && (!isfinite(boc3) || !isfinite(boc4) || !isfinite(boc5))) atomicOr(w.status, XR_S_BOC_NAN);
+  if (!corrected) boc3 = boc4 = boc5 = 0.0;
+  const double vi = atom_prm(ff, ti, A_VALENCY), vj = atom_prm(ff, tj, A_VALENCY);
+  const double dpi_ = AFV(AF_DELTAP, i), dpj = AFV(AF_DELTAP, j);
+  const double di = dpi_ - vi, dj = dpj - vj;
+  const double dbi = dpi_ - atom_prm(ff, ti, A_VALENCY_VAL), dbj = dpj - atom_prm(ff, tj, A_VALENCY_VAL);
+  double f1 = 1.0, df1i = 0.0, df1j = 0.0;
+  if (ovc >= 0.001) {
+    const double e2i = exp(-g[0] * di), e2j = exp(-g[0] * dj);
+    const double f2 = e2i + e2j;
+    const double e3i = exp(-g[1] * di), e3j = exp(-g[1] * dj);
+    const double s3 = 0.5 * (e3i + e3j);
+    const double f3 = -log(s3) / g[1];
+    const double Ai = vi + f2, Bi = Ai + f3, Aj = vj + f2, Bj = Aj + f3;
+    f1 = 0.5 * (Ai / Bi + Aj / Bj);
+    const double df1_df2 = 0.5 * (f3 / (Bi * Bi) + f3 / (Bj * Bj));
+    const double df1_df3 = -0.5 * (Ai / (Bi * Bi) + Aj / (Bj * Bj));
+    df1i = df1_df2 * (-g[0] * e2i) + df1_df3 * (0.5 * e3i / s3);
+    df1j = df1_df2 * (-g[0] * e2j) + df1_df3 * (0.5 * e3j / s3);
+  }
+  const double f4 = 1.0 / (1.0 + exp(-(boc4 * bo0 * bo0 - dbi) * boc3 + boc5));
+  const double f5 = 1.0 / (1.0 + exp(-(boc4 * bo0 * bo0 - dbj) * boc3 + boc5));
+  const double f45 = v13 >= 0.001 ? f4 * f5 : 1.0;
+  const double corr = f1 * f45;
+  const double bo = bo0 * corr, pi = pi0 * corr * f1, pp = pp0 * corr * f1;
+  const double sig = bo - pi - pp;
+  BFV(BF_BO, b) = bo >= 1e-10 ? bo : 0.0;
+  BFV(BF_PI, b) = pi >= 1e-10 ? pi : 0.0;
+  BFV(BF_PP, b) = pp >= 1e-10 ? pp : 0.0;
+  BFV(BF_SIG, b) = sig >= 1e-10 ? sig : 0.0;
+  BFV(BF_F1, b) = f1;
+  BFV(BF_F4, b) = f4;
+  BFV(BF_F5, b) = f5;
+  BFV(BF_CORR, b) = corr;
+  BFV(BF_DF1I, b) = df1i;
+  BFV(BF_DF1J, b) = df1j;
+}
+
+// Per-atom sums of corrected bond orders and the lone-pair quantities
+// (src/xreac/energy.py:185-199, 295-296).
+__global__ void k_atom1(XrWork w, XrFF ff) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= w.A) return;
+  const int L = w.A + 1, T = ff.ntypes, ta = w.type[a];
+  const double* g = ff.g;
+  double total = 0, sumpi = 0, prodsum = 0, ov1 = 0, n30 = 0;
+  for (int k = w.cnt[3 * L + a]; k < w.cnt[3 * L + a + 1]; ++k) {
+    const int2 en = w.dbrow[k];
+    const int b = en.x;
+    const double bo = BFV(BF_BO, b);
+    total += bo;
+    sumpi += BFV(BF_PI, b) + BFV(BF_PP, b);
+    const double b2 = bo * bo, b4 = b2 * b2;
+    prodsum += b4 * b4;
+    const int pt = ta * T + w.type[bond_other(w, b, en.y)];
+    ov1 += pair_prm(ff, pt, P_OVUN1) * pair_prm(ff, pt, P_DE_S) * bo;
+    n30 += bo > 0.3 ? 1.0 : 0.0;
+  }
+  const double val = atom_prm(ff, ta, A_VALENCY), vale = atom_prm(ff, ta, A_VALENCY_E);
+  const double de = total - vale;
+  const double half = trunc(de / 2);
+  const double vlpex = de - 2 * half;
+  const double e15 = exp(-g[15] * (2 + vlpex) * (2 + vlpex));
+  const double nlp = e15 - half;
+  const double dlp = 0.5 * (vale - val) - nlp;
+  const double dlpt = atom_prm(ff, ta, A_MASS) > 21 ? 0.0 : dlp;
+  const double elp = exp(-75 * dlp);
+  const double s = 1.0 / (1.0 + elp);
+  const double plp2 = atom_prm(ff, ta, A_P_LP2);
+  AEV(0, a) = plp2 * dlp * s;
+  AJV(AJ_DLP, a) = plp2 * (s + 75.0 * dlp * elp * s * s);
+  AFV(AF_TOTAL, a) = total;
+  AFV(AF_NLP, a) = nlp;
+  AFV(AF_VLPEX, a) = vlpex;
+  AFV(AF_DLP, a) = dlp;
+  AFV(AF_DLPT, a) = dlpt;
+  AFV(AF_SUMPI, a) = sumpi;
+  AFV(AF_PROD, a) = exp(-prodsum);
+  AFV(AF_OV1, a) = ov1;
+  AFV(AF_COUNT30, a) = n30;
+  AFV(AF_E15, a) = e15;
+}
+
+__device__ inline double sbo2_of(double sbo, double p) {
+  if (sbo <= 0) return 0.0;
+  if (sbo <= 1) return exp(p * log(sbo));
+  if (sbo < 2) return 2.0 - exp(p * log(2.0 - sbo));
+  return 2.0;
+}
+__device__ inline double dsbo2_of(double sbo, double p) {
+  if (sbo <= 0) return 0.0;
+  if (sbo <= 1) return p * exp((p - 1) * log(sbo));
+  if (sbo < 2) return p * exp((p - 1) * log(2.0 - sbo));
+  return 0.0;
+}
+
+// Over/under-coordination and sbo (src/xreac/energy.py:201-212, 295-301), with their local adjoints.
+__global__ void k_atom2(XrWork w, XrFF ff) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= w.A) return;
+  const int L = w.A + 1, ta = w.type[a];
+  const double* g = ff.g;
+  const double dfvl = atom_prm(ff, ta, A_MASS) <= 21 ? 1.0 : 0.0;
+  double ov2 = 0;
+  for (int k = w.cnt[3 * L + a]; k < w.cnt[3 * L + a + 1]; ++k) {
+    const int2 en = w.dbrow[k];
+    const int b = en.x, j = bond_other(w, b, en.y);
+    const double dj = AFV(AF_TOTAL, j) - atom_prm(ff, w.type[j], A_VALENCY);
+    ov2 += (dj - dfvl * AFV(AF_DLPT, j)) * (BFV(BF_PI, b) + BFV(BF_PP, b));
+  }
+  const double total = AFV(AF_TOTAL, a), val = atom_prm(ff, ta, A_VALENCY);
+  const double d = total - val, db = total - atom_prm(ff, ta, A_VALENCY_BOC);
+  const double dlpt = AFV(AF_DLPT, a), ov1 = AFV(AF_OV1, a);
+  const double exov = exp(g[31] * ov2);
+  const double denc = 1.0 + g[32] * exov;
+  const double dc = d - dfvl * dlpt / denc;
+  const double po2 = atom_prm(ff, ta, A_P_OVUN2), p5 = atom_prm(ff, ta, A_P_OVUN5);
+  const double D1 = dc + val + 1e-8;
+  const double eo = exp(po2 * dc);
+  const double D2 = 1.0 + eo;
+  const double over = ov1 * dc / D1 / D2;
+  const double eu = exp(g[6] * dc), em = exp(-po2 * dc), e9 = exp(g[9] * ov2);
+  const double D3 = 1.0 + em, D4 = 1.0 + g[8] * e9;
+  const double under = -p5 * (1.0 - eu) / D3 / D4;
+  AEV(1, a) = over + under;
+  const double dover_ddc = ov1 * (1.0 / (D1 * D2) - dc / (D1 * D1 * D2) - dc * po2 * eo / (D1 * D2 * D2));
+  const double dunder_ddc = -p5 * (-g[6] * eu / (D3 * D4) + (1.0 - eu) * po2 * em / (D3 * D3 * D4));
+  const double dunder_dov2 = -under * g[8] * g[9] * e9 / D4;
+  const double A_dc = dover_ddc + dunder_ddc;
+  AJV(AJ_OV1, a) = dc / (D1 * D2);
+  AJV(AJ_OV2, a) = A_dc * dfvl * dlpt * g[32] * g[31] * exov / (denc * denc) + dunder_dov2;
+  AJV(AJ_D, a) += A_dc;
+  AJV(AJ_DLPT, a) = A_dc * (-dfvl / denc);
+  const double vlpex = AFV(AF_VLPEX, a), nlp = AFV(AF_NLP, a), prod = AFV(AF_PROD, a);
+  const double lpt = vlpex >= 0 ? 0.0 : nlp;
+  const double sbo = AFV(AF_SUMPI, a) + (1.0 - prod) * (-db - g[33] * lpt);
+  AFV(AF_OV2, a) = ov2;
+  AFV(AF_DC, a) = dc;
+  AFV(AF_SBO, a) = sbo;
+  AFV(AF_SBO2, a) = sbo2_of(sbo, g[16]);
+}
+
+// Bond energy, C2 correction and triple-bond stabilisation, per half bond
+// (src/xreac/energy.py:194-198, 231-246).
+__global__ void k_bond_energy(XrWork w, XrFF ff) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= w.nB) return;
+  const int i = w.bond_i[b], j = w.bond_j[b];
+  const int ti = w.type[i], tj = w.type[j], T = ff.ntypes, pt = ti * T + tj;
+  const double* g = ff.g;
+  const double bo = BFV(BF_BO, b), pi = BFV(BF_PI, b), pp = BFV(BF_PP, b), sig = BFV(BF_SIG, b);
+  const double Des = pair_prm(ff, pt, P_DE_S), Dep = pair_prm(ff, pt, P_DE_P), Depp = pair_prm(ff, pt, P_DE_PP);
+  const double be1 = pair_prm(ff, pt, P_BE1), be2 = pair_prm(ff, pt, P_BE2);
+  const double powv = sig > 0 ? exp(be2 * log(sig)) : 0.0;
+  const double ex = exp(be1 * (1.0 - powv));
+  double e_bond = -(Des * sig * ex + Dep * pi + Depp * pp);
+  BJV(BJ_SIG, b) = -Des * ex * (1.0 - be1 * be2 * powv);
+  BJV(BJ_PI, b) += -Dep;
+  BJV(BJ_PP, b) += -Depp;
+  double e_c2 = 0.0, dbo = 0.0;
+  if (g[5] > 0.001 && __ldg(ff.is_carbon + ti) && __ldg(ff.is_carbon + tj)) {
+    const int ends[2] = {i, j};
+    for (int s = 0; s < 2; ++s) {
+      const int src = ends[s];
+      const double d = AFV(AF_TOTAL, src) - atom_prm(ff, w.type[src], A_VALENCY);
+      const double d2 = d * d;
+      const double vov3 = bo - d - 0.040 * d2 * d2;
+      if (vov3 > 3) {
+        e_c2 += g[5] * (vov3 - 3) * (vov3 - 3);
+        dbo += 2 * g[5] * (vov3 - 3);
+        atomicAdd(&AJV(AJ_D, src), 2 * g[5] * (vov3 - 3) * (-1.0 - 0.16 * d2 * d));
+      }
+    }
+  }
+  const double mi = atom_prm(ff, ti, A_MASS), mj = atom_prm(ff, tj, A_MASS);
+  const bool co = (mi == 12.0 && mj == 15.999) || (mj == 12.0 && mi == 15.999);
+  const bool allowed = ((int)g[37] != 2) ? co : true;
+  if (allowed && bo >= 1.0) {
+    const double ti_ = AFV(AF_TOTAL, i), tj_ = AFV(AF_TOTAL, j);
+    const double di = ti_ - atom_prm(ff, ti, A_VALENCY), dj = tj_ - atom_prm(ff, tj, A_VALENCY);
+    const double e1 = exp(-g[7] * (bo - 2.5) * (bo - 2.5));
+    const double e4 = exp(g[4] * (di + dj));
+    const double D = 1.0 + 25.0 * e4;
+    const double ei = exp(-g[3] * (ti_ - bo)), ej = exp(-g[3] * (tj_ - bo));
+    const double stab = g[10] * e1 / D * (ei + ej);
+    e_bond += stab;
+    dbo += g[10] / D * (-2.0 * g[7] * (bo - 2.5) * e1 * (ei + ej) + e1 * g[3] * (ei + ej));
+    const double dd = -g[10] * e1 * (ei + ej) * 25.0 * g[4] * e4 / (D * D);
+    atomicAdd(&AJV(AJ_D, i), dd);
+    atomicAdd(&AJV(AJ_D, j), dd);
+    atomicAdd(&AJV(AJ_TOTAL, i), g[10] * e1 / D * (-g[3] * ei));
+    atomicAdd(&AJV(AJ_TOTAL, j), g[10] * e1 / D * (-g[3] * ej));
+  }
+  if (dbo != 0.0) atomicAdd(&BJV(BJ_BO, b), dbo);
+  BEV(0, b) = e_bond;
+  BEV(1, b) = e_c2;
+}
+
+// Valence angle, penalty and angle conjugation, one thread per centre atom
+// (src/xreac/energy.py:278-318).
+__global__ void k_angles(XrWork w, XrFF ff) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= w.A) return;
+  const int L = w.A + 1, T = ff.ntypes, tj = w.type[j];
+  const double* g = ff.g;
+  const int beg = w.cnt[3 * L + j], end = w.cnt[3 * L + j + 1];
+  const double total_j = AFV(AF_TOTAL, j);
+  const double d_j = total_j - atom_prm(ff, tj, A_VALENCY);
+  const double db_j = total_j - atom_prm(ff, tj, A_VALENCY_BOC);
+  const double sbo2 = AFV(AF_SBO2, j);
+  const double pv3 = atom_prm(ff, tj, A_P_VAL3), pv5 = atom_prm(ff, tj, A_P_VAL5);
+  const double valval = atom_prm(ff, tj, A_VALENCY_VAL);
+  const double k180 = 3.14159265 / 180;
+  const double e17 = exp(-g[17] * (2 - sbo2));
+  // penalty and conjugation factors that depend on the centre only
+  const double ex3 = exp(-g[20] * d_j), ex4 = exp(g[21] * d_j);
+  const double den34 = 1 + ex3 + ex4;
+  const double Fp = (2 + ex3) / den34;
+  const double dFp_dd = (-g[20] * ex3 * den34 - (2 + ex3) * (-g[20] * ex3 + g[21] * ex4)) / (den34 * den34);
+  const double e2 = exp(g[2] * (total_j - valval));
+  const double K1 = 1.0 / (1.0 + e2);
+  const double dK1_dt = -g[2] * e2 * K1 * K1;
+  double E_ang = 0, E_pen = 0, E_coa = 0;
+  double A_sbo2 = 0, A_db = 0, A_d = 0, A_tj = 0;
+  double gj[3] = {0, 0, 0};
+  const bool lammps = !w.full_derivative;
+  for (int a = beg; a < end; ++a) {
+    const int2 ea = w.dbrow[a];
+    const double bo_l = BFV(BF_BO, ea.x);
+    if (!(bo_l > THB_CUT)) continue;
+    const int i = bond_other(w, ea.x, ea.y);
+    double vl[3];
+    bond_vec(w, ea.x, ea.y, vl);
+    const double rl = w.b_r[ea.x];
+    const double total_i = AFV(AF_TOTAL, i);
+    const int ti = w.type[i];
+    double gl[3] = {0, 0, 0}, dbo_l = 0, dtot_i = 0;
+    for (int c = a + 1; c < end; ++c) {
+      const int2 ec = w.dbrow[c];
+      const double bo_r = BFV(BF_BO, ec.x);
+      if (!(bo_r > THB_CUT)) continue;
+      if (bo_l * bo_r <= THB_PRODUCT_CUT) continue;
+      const int k = bond_other(w, ec.x, ec.y);
+      const int key = (ti * T + tj) * T + w.type[k];
+      const int first = __ldg(ff.angle_index + 2 * key), count = __ldg(ff.angle_index + 2 * key + 1);
+      if (count == 0) continue;
+      double vr[3];
+      bond_vec(w, ec.x, ec.y, vr);
+      const double rr = w.b_r[ec.x];
+      const double total_k = AFV(AF_TOTAL, k);
+      const double cosv = (vl[0] * vr[0] + vl[1] * vr[1] + vl[2] * vr[2]) / (rl * rr);
+      double theta, dth_dcos;
+      if (lammps) {
+        const double cc = fmin(fmax(cosv, -1.0), 1.0);
+        theta = acos(cc);
+        dth_dcos = -1.0 / fmax(sin(theta), 1e-5);
+      } else {
+        const double lo = -1 + 1e-14, hi = 1 - 1e-14;
+        const double cc = fmin(fmax(cosv, lo), hi);
+        theta = acos(cc);
+        dth_dcos = (cosv > lo && cosv < hi) ? -1.0 / sqrt(1.0 - cc * cc) : 0.0;
+      }
+      const double bij = bo_l - THB_CUT, bjk = bo_r - THB_CUT;
+      const double lbij = log(bij), lbjk = log(bjk);
+      double dE_dcos = 0, dbij = 0, dbjk = 0, dtot_k = 0;
+      for (int q = 0; q < count; ++q) {
+        const double* prm = ff.angle + 7 * (first + q);
+        const double th00 = __ldg(prm + 0), v1 = __ldg(prm + 1), v2 = __ldg(prm + 2), coa1 = __ldg(prm + 3);
+        const double v7 = __ldg(prm + 4), pen1 = __ldg(prm + 5), v4 = __ldg(prm + 6);
+        if (!(fabs(v1) > 0.001)) continue;
+        const double theta0 = (180 - th00 * (1 - e17)) * k180;
+        const double dth0_dsbo2 = th00 * k180 * g[17] * e17;
+        const double pij = exp(v4 * lbij), pjk = exp(v4 * lbjk);
+        const double A1 = exp(-pv3 * pij), A2 = exp(-pv3 * pjk);
+        const double f7 = (1 - A1) * (1 - A2);
+        const double df7_dbij = pv3 * v4 * pij / bij * A1 * (1 - A2);
+        const double df7_dbjk = (1 - A1) * pv3 * v4 * pjk / bjk * A2;
+        const double ex6 = exp(g[14] * db_j), ex7 = exp(-v7 * db_j);
+        const double den8 = 1 + ex6 + ex7;
+        const double f8 = pv5 - (pv5 - 1) * (2 + ex6) / den8;
+        const double df8_ddb = -(pv5 - 1) * (g[14] * ex6 * den8 - (2 + ex6) * (g[14] * ex6 - v7 * ex7)) / (den8 * den8);
+        const double dt = theta0 - theta;
+        const double exang = exp(-v2 * dt * dt);
+        const double branch = v1 >= 0 ? 1 - exang : -exang;
+        E_ang += f7 * f8 * v1 * branch;
+        const double dE_ddt = f7 * f8 * v1 * 2 * v2 * dt * exang;
+        dE_dcos += -dE_ddt * dth_dcos;
+        A_sbo2 += dE_ddt * dth0_dsbo2;
+        dbij += f8 * v1 * branch * df7_dbij;
+        dbjk += f8 * v1 * branch * df7_dbjk;
+        A_db += f7 * v1 * branch * df8_ddb;
+        // penalty
+        const double Gp = exp(-g[19] * ((bij - 2) * (bij - 2) + (bjk - 2) * (bjk - 2)));
+        const double ep = pen1 * Fp * Gp;
+        E_pen += ep;
+        A_d += pen1 * dFp_dd * Gp;
+        dbij += ep * (-2 * g[19] * (bij - 2));
+        dbjk += ep * (-2 * g[19] * (bjk - 2));
+        // angle conjugation
+        const double ti_b = total_i - bij, tk_b = total_k - bjk;
+        const double K2 = exp(-g[38] * (ti_b * ti_b + tk_b * tk_b));
+        const double K3 = exp(-g[30] * ((bij - 1.5) * (bij - 1.5) + (bjk - 1.5) * (bjk - 1.5)));
+        const double ec = coa1 * K1 * K2 * K3;
+        E_coa += ec;
+        A_tj += coa1 * dK1_dt * K2 * K3;
+        dtot_i += ec * (-2 * g[38] * ti_b);
+        dtot_k += ec * (-2 * g[38] * tk_b);
+        dbij += ec * (2 * g[38] * ti_b) + ec * (-2 * g[30] * (bij - 1.5));
+        dbjk += ec * (2 * g[38] * tk_b) + ec * (-2 * g[30] * (bjk - 1.5));
+      }
+      if (dE_dcos != 0.0) {
+        const double inv = 1.0 / (rl * rr);
+        double gr[3];
+        for (int c3 = 0; c3 < 3; ++c3) {
+          const double g_l = dE_dcos * (vr[c3] * inv - cosv * vl[c3] / (rl * rl));
+          gr[c3] = dE_dcos * (vl[c3] * inv - cosv * vr[c3] / (rr * rr));
+          gl[c3] += g_l;
+          gj[c3] -= g_l + gr[c3];
+        }
+        atomic_add3(w.f, k, gr[0], gr[1], gr[2]);
+      }
+      dbo_l += dbij;
+      if (dbjk != 0.0) atomicAdd(&BJV(BJ_BO, ec.x), dbjk);
+      if (dtot_k != 0.0) atomicAdd(&AJV(AJ_TOTAL, k), dtot_k);
+    }
+    if (dbo_l != 0.0) atomicAdd(&BJV(BJ_BO, ea.x), dbo_l);
+    if (dtot_i != 0.0) atomicAdd(&AJV(AJ_TOTAL, i), dtot_i);
+    if (gl[0] != 0.0 || gl[1] != 0.0 || gl[2] != 0.0) atomic_add3(w.f, i, gl[0], gl[1], gl[2]);
+  }
+  AEV(2, j) = E_ang;
+  AEV(3, j) = E_pen;
+  AEV(4, j) = E_coa;
+  if (A_sbo2 != 0.0) atomicAdd(&AJV(AJ_SBO2, j), A_sbo2);
+  if (A_db != 0.0) atomicAdd(&AJV(AJ_DB, j), A_db);
+  if (A_d != 0.0) atomicAdd(&AJV(AJ_D, j), A_d);
+  if (A_tj != 0.0) atomicAdd(&AJV(AJ_TOTAL, j), A_tj);
+  if (gj[0] != 0.0 || gj[1] != 0.0 || gj[2] != 0.0) atomic_add3(w.f, j, gj[0], gj[1], gj[2]);
+}
+
+__device__ inline void cross3(const double a[3], const double b[3], double c[3]) {
+  c[0] = a[1] * b[2] - a[2] * b[1];
+  c[1] = a[2] * b[0] - a[0] * b[2];
+  c[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+// Torsion and four-body conjugation, one thread per middle bond j -> k (the half direction)
+// (src/xreac/energy.py:320-370).
+__global__ void k_torsions(XrWork w, XrFF ff) {
+  const int m = blockIdx.x * blockDim.x + threadIdx.x;
+  if (m >= w.nB) return;
+  const double bo_m = BFV(BF_BO, m);
+  if (!(bo_m > THB_CUT)) return;
+  const int L = w.A + 1, T = ff.ntypes;
+  const double* g = ff.g;
+  const int j = w.bond_i[m], k = w.bond_j[m];
+  const int tj = w.type[j], tk = w.type[k];
+  const uint32_t sm = (uint32_t)w.edge[w.pair_edge[w.bond_pair[m]]].y & XR_SHIFT_MASK;
+  double v[3];
+  bond_vec(w, m, 1, v);
+  const double rm = w.b_r[m];
+  const double pi_m = BFV(BF_PI, m);
+  const double db_j = AFV(AF_TOTAL, j) - atom_prm(ff, tj, A_VALENCY_BOC);
+  const double db_k = AFV(AF_TOTAL, k) - atom_prm(ff, tk, A_VALENCY_BOC);
+  const double ds = db_j + db_k;
+  const double ex3 = exp(-g[24] * ds), ex4 = exp(g[25] * ds);
+  const double den = 1 + ex3 + ex4;
+  const double f11 = (2 + ex3) / den;
+  const double df11_dds = (-g[24] * ex3 * den - (2 + ex3) * (-g[24] * ex3 + g[25] * ex4)) / (den * den);
+  const double b2 = bo_m - THB_CUT;
+  const double e2 = exp(-g[23] * b2);
+  double E_tor = 0, E_con = 0, A_bom = 0, A_pim = 0, A_ds = 0;
+  double g_j[3] = {0, 0, 0}, g_k[3] = {0, 0, 0};
+  for (int a = w.cnt[3 * L + j]; a < w.cnt[3 * L + j + 1]; ++a) {
+    const int2 el = w.dbrow[a];
+    if (el.x == m && el.y > 0) continue;  // left == middle
+    const double bo_l = BFV(BF_BO, el.x);
+    if (!(bo_l > THB_CUT)) continue;
+    const int i = bond_other(w, el.x, el.y);
+    const int ti = w.type[i];
+    const uint32_t sl = bond_shift(w, el.x, el.y);
+    double u[3];
+    bond_vec(w, el.x, el.y, u);
+    const double rl = w.b_r[el.x];
+    const double b1 = bo_l - THB_CUT;
+    const double e1 = exp(-g[23] * b1);
+    double A_bol = 0, g_i[3] = {0, 0, 0};
+    for (int c = w.cnt[3 * L + k]; c < w.cnt[3 * L + k + 1]; ++c) {
+      const int2 er = w.dbrow[c];
+      if (er.x == m && er.y < 0) continue;  // right == reverse(middle)
+      const double bo_r = BFV(BF_BO, er.x);
+      if (!(bo_r > THB_CUT)) continue;
+      const int l = bond_other(w, er.x, er.y);
+      const int row = __ldg(ff.torsion_index + ((ti * T + tj) * T + tk) * T + w.type[l]);
+      if (row < 0) continue;
+      if (bo_l * bo_m * bo_r <= THB_CUT) continue;
+      if (i == l) {
+        const uint32_t sr = bond_shift(w, er.x, er.y);
+        if (xr_sx(sl) == xr_sx(sm) + xr_sx(sr) && xr_sy(sl) == xr_sy(sm) + xr_sy(sr) &&
+            xr_sz(sl) == xr_sz(sm) + xr_sz(sr))
+          continue;
+      }
+      double wv[3];
+      bond_vec(w, er.x, er.y, wv);
+      const double rr = w.b_r[er.x];
+      double n1[3], n2[3];
+      cross3(u, v, n1);
+      cross3(wv, v, n2);
+      const double A1 = n1[0] * n1[0] + n1[1] * n1[1] + n1[2] * n1[2];
+      const double A2 = n2[0] * n2[0] + n2[1] * n2[1] + n2[2] * n2[2];
+      const double s1 = A1 / ((rl * rm) * (rl * rm));
+      const double s2 = A2 / ((rm * rr) * (rm * rr));
+      if (s1 < 1e-20 || s2 < 1e-20) {
+        atomicOr(w.status, XR_S_COLLINEAR);
+        continue;
+      }
+      const double sinprod = sqrt(s1 * s2);
+      const double sq = sqrt(A1 * A2);
+      const double P = n1[0] * n2[0] + n1[1] * n2[1] + n1[2] * n2[2];
+      const double cw = P / sq;
+      const double* prm = ff.torsion + 5 * row;
+      const double V1 = __ldg(prm + 0), V2 = __ldg(prm + 1), V3 = __ldg(prm + 2), tor1 = __ldg(prm + 3),
+                   cot1 = __ldg(prm + 4);
+      const double b3 = bo_r - THB_CUT;
+      const double e3 = exp(-g[23] * b3);
+      const double y = 2 - pi_m - f11;
+      const double ex1 = exp(tor1 * y * y);
+      const double fn10 = (1 - e1) * (1 - e2) * (1 - e3);
+      const double cv = 0.5 * (V1 * (1 + cw) + V2 * ex1 * (2 - 2 * cw * cw) + V3 * (1 + 4 * cw * cw * cw - 3 * cw));
+      E_tor += fn10 * sinprod * cv;
+      const double q1 = b1 - 1.5, q2 = b2 - 1.5, q3 = b3 - 1.5;
+      const double fn12 = exp(-g[27] * (q1 * q1 + q2 * q2 + q3 * q3));
+      const double conj = 1 + (cw * cw - 1) * sinprod;
+      E_con += cot1 * fn12 * conj;
+      const double dcv_dcw = 0.5 * (V1 - 4 * V2 * ex1 * cw + V3 * (12 * cw * cw - 3));
+      const double dE_dcw = fn10 * sinprod * dcv_dcw + cot1 * fn12 * 2 * cw * sinprod;
+      const double dE_dsp = fn10 * cv + cot1 * fn12 * (cw * cw - 1);
+      const double dE_dex1 = fn10 * sinprod * 0.5 * V2 * (2 - 2 * cw * cw);
+      const double dex1_dy = 2 * tor1 * y * ex1;
+      A_pim += -dE_dex1 * dex1_dy;
+      A_ds += -dE_dex1 * dex1_dy * df11_dds;
+      const double sc = sinprod * cv, cc = cot1 * conj;
+      A_bol += sc * g[23] * e1 * (1 - e2) * (1 - e3) + cc * fn12 * (-2 * g[27] * q1);
+      A_bom += sc * g[23] * e2 * (1 - e1) * (1 - e3) + cc * fn12 * (-2 * g[27] * q2);
+      const double A_bor = sc * g[23] * e3 * (1 - e1) * (1 - e2) + cc * fn12 * (-2 * g[27] * q3);
+      atomicAdd(&BJV(BJ_BO, er.x), A_bor);
+      // geometry: dE/dn1 = a, dE/dn2 = bb
+      double av[3], bv[3];
+      for (int c3 = 0; c3 < 3; ++c3) {
+        av[c3] = dE_dcw * (n2[c3] - (P / A1) * n1[c3]) / sq + dE_dsp * sinprod * n1[c3] / A1;
+        bv[c3] = dE_dcw * (n1[c3] - (P / A2) * n2[c3]) / sq + dE_dsp * sinprod * n2[c3] / A2;
+      }
+      double gu[3], gv[3], gw[3], t1[3], t2[3];
+      cross3(v, av, gu);
+      cross3(av, u, t1);
+      cross3(bv, wv, t2);
+      cross3(v, bv, gw);
+      for (int c3 = 0; c3 < 3; ++c3) {
+        gu[c3] += dE_dsp * (-sinprod) * u[c3] / (rl * rl);
+        gv[c3] = t1[c3] + t2[c3] + dE_dsp * (-2 * sinprod) * v[c3] / (rm * rm);
+        gw[c3] += dE_dsp * (-sinprod) * wv[c3] / (rr * rr);
+        g_i[c3] += gu[c3];
+        g_j[c3] += -gu[c3] - gv[c3];
+        g_k[c3] += gv[c3] - gw[c3];
+      }
+      atomic_add3(w.f, l, gw[0], gw[1], gw[2]);
+    }
+    if (A_bol != 0.0) atomicAdd(&BJV(BJ_BO, el.x), A_bol);
+    if (g_i[0] != 0.0 || g_i[1] != 0.0 || g_i[2] != 0.0) atomic_add3(w.f, i, g_i[0], g_i[1], g_i[2]);
+  }
+  BEV(2, m) = E_tor;
+  BEV(3, m) = E_con;
+  if (A_bom != 0.0) atomicAdd(&BJV(BJ_BO, m), A_bom);
+  if (A_pim != 0.0) atomicAdd(&BJV(BJ_PI, m), A_pim);
+  if (A_ds != 0.0) {
+    atomicAdd(&AJV(AJ_DB, j), A_ds);
+    atomicAdd(&AJV(AJ_DB, k), A_ds);
+  }
+  if (g_j[0] != 0.0 || g_j[1] != 0.0 || g_j[2] != 0.0) atomic_add3(w.f, j, g_j[0], g_j[1], g_j[2]);
+  if (g_k[0] != 0.0 || g_k[1] != 0.0 || g_k[2] != 0.0) atomic_add3(w.f, k, g_k[0], g_k[1], g_k[2]);
+}
+
+// Hydrogen bonds, one warp per hydrogen: lanes take acceptor edges of the hydrogen's full row
+// (heavy neighbour within min(7.5, cutoff)), each paired with every donor bond (heavy neighbour,
+// bo >= 0.01) other than the same edge (src/xreac/energy.py:248-276).
+__global__ void k_hbonds(XrWork w, XrFF ff) {
+  const int lane = threadIdx.x & 31;
+  const int h = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
+  if (h >= w.A) return;
+  const int th = w.type[h], T = ff.ntypes;
+  if ((int)atom_prm(ff, th, A_P_HBOND) != 1) {
+    if (lane == 0) AEV(5, h) = 0.0;
+    return;
+  }
+  const int L = w.A + 1;
+  const XrSystem& S = w.sys[w.sys_of[h]];
+  const double4_32a xh = w.x[h];
+  double E = 0;
+  double gh[3] = {0, 0, 0};
+  const int dbeg = w.cnt[3 * L + h], dend = w.cnt[3 * L + h + 1];
+  for (int e = w.cnt[0 * L + h] + lane; e < w.cnt[0 * L + h + 1]; e += 32) {
+    const int2 ed = w.edge[e];
+    const uint32_t code = (uint32_t)ed.y;
+    if (!(code & XR_CODE_HB)) continue;
+    const int ja = ed.x, ta = w.type[ja];
+    if ((int)atom_prm(ff, ta, A_P_HBOND) != 2) continue;
+    const uint32_t sa = code & XR_SHIFT_MASK;
+    double va[3];
+    {
+      const double4_32a xa = w.x[ja];
+      const int sx = xr_sx(sa), sy = xr_sy(sa), sz = xr_sz(sa);
+      const double p0[3] = {xh.x, xh.y, xh.z}, p1[3] = {xa.x, xa.y, xa.z};
+      for (int c = 0; c < 3; ++c) {
+        const double off = __dadd_rn(__dadd_rn(__dmul_rn((double)sx, S.cell[c]), __dmul_rn((double)sy, S.cell[3 + c])),
+                                     __dmul_rn((double)sz, S.cell[6 + c]));
+        va[c] = __dadd_rn(__dsub_rn(p1[c], p0[c]), off);
+      }
+    }
+    const double ra = sqrt(va[0] * va[0] + va[1] * va[1] + va[2] * va[2]);
+    double ga[3] = {0, 0, 0};
+    for (int k = dbeg; k < dend; ++k) {
+      const int2 en = w.dbrow[k];
+      const int jd = bond_other(w, en.x, en.y);
+      const int td = w.type[jd];
+      if ((int)atom_prm(ff, td, A_P_HBOND) != 2) continue;
+      const double bo_d = BFV(BF_BO, en.x);
+      if (!(bo_d >= HBOND_THRESHOLD)) continue;
+      if (jd == ja && bond_shift(w, en.x, en.y) == sa) continue;  // same edge
+      const int row = __ldg(ff.hbond_index + (td * T + th) * T + ta);
+      if (row < 0) continue;
+      const double* prm = ff.hbond + 4 * row;
+      const double r0 = __ldg(prm + 0), hb1 = __ldg(prm + 1), hb2 = __ldg(prm + 2), hb3 = __ldg(prm + 3);
+      if (!(r0 > 0)) continue;
+      double vd[3];
+      bond_vec(w, en.x, en.y, vd);
+      const double rd = w.b_r[en.x];
+      const double cosv = (vd[0] * va[0] + vd[1] * va[1] + vd[2] * va[2]) / (rd * ra);
+      const double cc = fmin(fmax(cosv, -1.0), 1.0);
+      const double sin4 = 0.25 * (1 - cc) * (1 - cc);
+      const double eb = exp(-hb2 * bo_d);
+      const double Fb = hb1 * (1 - eb);
+      const double E2 = exp(-hb3 * (r0 / ra + ra / r0 - 2));
+      E += Fb * E2 * sin4;
+      atomicAdd(&BJV(BJ_BO, en.x), hb1 * hb2 * eb * E2 * sin4);
+      const double dE_dr = Fb * E2 * sin4 * (-hb3) * (-r0 / (ra * ra) + 1 / r0);
+      const double dE_dcos = (cosv > -1.0 && cosv < 1.0) ? Fb * E2 * (-0.5) * (1 - cc) : 0.0;
+      const double inv = 1.0 / (rd * ra);
+      double gd[3];
+      for (int c = 0; c < 3; ++c) {
+        gd[c] = dE_dcos * (va[c] * inv - cosv * vd[c] / (rd * rd));
+        const double gac = dE_dcos * (vd[c] * inv - cosv * va[c] / (ra * ra)) + dE_dr * va[c] / ra;
+        ga[c] += gac;
+        gh[c] -= gd[c] + gac;
+      }
+      atomic_add3(w.f, jd, gd[0], gd[1], gd[2]);
+    }
+    if (ga[0] != 0.0 || ga[1] != 0.0 || ga[2] != 0.0) atomic_add3(w.f, ja, ga[0], ga[1], ga[2]);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    E += __shfl_down_sync(0xffffffffu, E, o);
+    gh[0] += __shfl_down_sync(0xffffffffu, gh[0], o);
+    gh[1] += __shfl_down_sync(0xffffffffu, gh[1], o);
+    gh[2] += __shfl_down_sync(0xffffffffu, gh[2], o);
+  }
+  if (lane == 0) {
+    AEV(5, h) = E;
+    if (gh[0] != 0.0 || gh[1] != 0.0 || gh[2] != 0.0) atomic_add3(w.f, h, gh[0], gh[1], gh[2]);
+  }
+}
+
+// Per-atom chain: neighbours' over-coordination cross terms, lone pair, sbo, then dE/d total.
+__global__ void k_chain_atom(XrWork w, XrFF ff) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= w.A) return;
+  const int L = w.A + 1, ta = w.type[a];
+  const double* g = ff.g;
+  double A_d = AJV(AJ_D, a), A_dlpt = AJV(AJ_DLPT, a);
+  for (int k = w.cnt[3 * L + a]; k < w.cnt[3 * L + a + 1]; ++k) {
+    const int2 en = w.dbrow[k];
+    const int j = bond_other(w, en.x, en.y);
+    const double P = BFV(BF_PI, en.x) + BFV(BF_PP, en.x);
+    if (P == 0.0) continue;
+    const double dfvl_j = atom_prm(ff, w.type[j], A_MASS) <= 21 ? 1.0 : 0.0;
+    const double aov2 = AJV(AJ_OV2, j);
+    A_d += aov2 * P;
+    A_dlpt -= aov2 * dfvl_j * P;
+  }
+  const double mass = atom_prm(ff, ta, A_MASS);
+  const double A_dlp = AJV(AJ_DLP, a) + (mass <= 21 ? A_dlpt : 0.0);
+  const double sbo = AFV(AF_SBO, a), prod = AFV(AF_PROD, a), vlpex = AFV(AF_VLPEX, a), nlp = AFV(AF_NLP, a);
+  const double db = AFV(AF_TOTAL, a) - atom_prm(ff, ta, A_VALENCY_BOC);
+  const double lpt = vlpex >= 0 ? 0.0 : nlp;
+  const double A_sbo = AJV(AJ_SBO2, a) * dsbo2_of(sbo, g[16]);
+  const double A_prod = A_sbo * (db + g[33] * lpt);
+  const double A_db = AJV(AJ_DB, a) - A_sbo * (1 - prod);
+  double A_nlp = -A_dlp;
+  if (vlpex < 0) A_nlp += -A_sbo * (1 - prod) * g[33];
+  const double A_vlpex = A_nlp * (-2 * g[15] * (2 + vlpex) * AFV(AF_E15, a));
+  AJV(AJ_SUMPI, a) = A_sbo;
+  AJV(AJ_PRODSUM, a) = -prod * A_prod;
+  AJV(AJ_TOTAL_ALL, a) = AJV(AJ_TOTAL, a) + A_d + A_db + A_vlpex;
+}
+
+// Per-bond chain: from the thresholded outputs back through f1, f4, f5 to the uncorrected orders.
+__global__ void k_chain_bond(XrWork w, XrFF ff) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= w.nB) return;
+  const int i = w.bond_i[b], j = w.bond_j[b];
+  const int ti = w.type[i], tj = w.type[j], T = ff.ntypes, pt = ti * T + tj;
+  const double bo = BFV(BF_BO, b), pi = BFV(BF_PI, b), pp = BFV(BF_PP, b), sig = BFV(BF_SIG, b);
+  const double b2 = bo * bo, b4 = b2 * b2, b7 = b4 * b2 * bo;
+  double A_bo = BJV(BJ_BO, b) + AJV(AJ_TOTAL_ALL, i) + AJV(AJ_TOTAL_ALL, j) +
+                (AJV(AJ_OV1, i) + AJV(AJ_OV1, j)) * pair_prm(ff, pt, P_OVUN1) * pair_prm(ff, pt, P_DE_S) +
+                (AJV(AJ_PRODSUM, i) + AJV(AJ_PRODSUM, j)) * 8.0 * b7;
+  const double di = AFV(AF_TOTAL, i) - atom_prm(ff, ti, A_VALENCY), dj = AFV(AF_TOTAL, j) - atom_prm(ff, tj, A_VALENCY);
+  const double dfi = atom_prm(ff, ti, A_MASS) <= 21 ? 1.0 : 0.0, dfj = atom_prm(ff, tj, A_MASS) <= 21 ? 1.0 : 0.0;
+  const double A_P = AJV(AJ_OV2, i) * (dj - dfi * AFV(AF_DLPT, j)) + AJV(AJ_OV2, j) * (di - dfj * AFV(AF_DLPT, i)) +
+                     AJV(AJ_SUMPI, i) + AJV(AJ_SUMPI, j);
+  const double A_pi = BJV(BJ_PI, b) + A_P, A_pp = BJV(BJ_PP, b) + A_P, A_sig = BJV(BJ_SIG, b);
+  const double gsig = sig != 0.0 ? A_sig : 0.0;
+  const double g_bo = (bo != 0.0 ? A_bo : 0.0) + gsig;
+  const double g_pi = (pi != 0.0 ? A_pi : 0.0) - gsig;
+  const double g_pp = (pp != 0.0 ? A_pp : 0.0) - gsig;
+  const double bo0 = BFV(BF_BO0, b), pi0 = BFV(BF_PI0, b), pp0 = BFV(BF_PP0, b);
+  const double f1 = BFV(BF_F1, b), f4 = BFV(BF_F4, b), f5 = BFV(BF_F5, b), corr = BFV(BF_CORR, b);
+  const double v13 = pair_prm(ff, pt, P_V13COR), ovc = pair_prm(ff, pt, P_OVC);
+  const bool mask = BFV(BF_MASK, b) != 0.0;
+  const bool corrected = mask && (ovc >= 0.001 || v13 >= 0.001);
+  const double boc3 = corrected ? pair_prm(ff, pt, P_BOC3) : 0.0, boc4 = corrected ? pair_prm(ff, pt, P_BOC4) : 0.0;
+  const double f45 = v13 >= 0.001 ? f4 * f5 : 1.0;
+  double d_bo0 = g_bo * corr;
+  const double d_pi0 = g_pi * corr * f1;
+  const double d_pp0 = g_pp * corr * f1;
+  const double d_corr = g_bo * bo0 + g_pi * pi0 * f1 + g_pp * pp0 * f1;
+  const double d_f1 = (g_pi * pi0 + g_pp * pp0) * corr + d_corr * f45;
+  double d_dbi = 0, d_dbj = 0;
+  if (v13 >= 0.001) {
+    const double d_f45 = d_corr * f1;
+    const double dz4 = d_f45 * f5 * (-f4 * (1 - f4));
+    const double dz5 = d_f45 * f4 * (-f5 * (1 - f5));
+    d_bo0 += (dz4 + dz5) * (-2 * boc3 * boc4 * bo0);
+    d_dbi = dz4 * boc3;
+    d_dbj = dz5 * boc3;
+  }
+  BJV(BJ_BO0, b) = d_bo0;
+  BJV(BJ_PI0, b) = d_pi0;
+  BJV(BJ_PP0, b) = d_pp0;
+  BJV(BJ_CI, b) = d_f1 * BFV(BF_DF1I, b) + d_dbi;
+  BJV(BJ_CJ, b) = d_f1 * BFV(BF_DF1J, b) + d_dbj;
+}
+
+__global__ void k_chain_deltap(XrWork w) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= w.A) return;
+  const int L = w.A + 1;
+  double s = 0;
+  for (int k = w.cnt[3 * L + a]; k < w.cnt[3 * L + a + 1]; ++k) {
+    const int2 en = w.dbrow[k];
+    s += en.y > 0 ? BJV(BJ_CI, en.x) : BJV(BJ_CJ, en.x);
+  }
+  AJV(AJ_DELTAP, a) = s;
+}
+
+// dE/dr of each bond from the uncorrected bond orders; added to the pair's radial accumulator.
+__global__ void k_chain_radial(XrWork w) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= w.nB) return;
+  if (BFV(BF_MASK, b) == 0.0) return;
+  const double d_bo0 = BJV(BJ_BO0, b) + AJV(AJ_DELTAP, w.bond_i[b]) + AJV(AJ_DELTAP, w.bond_j[b]);
+  const double G = d_bo0 * BFV(BF_DSIG, b) + (d_bo0 + BJV(BJ_PI0, b)) * BFV(BF_DPI, b) +
+                   (d_bo0 + BJV(BJ_PP0, b)) * BFV(BF_DPP, b);
+  w.p_g[w.bond_pair[b]] += G;
+}
+
+}  // namespace
+
+void xr_launch_bonded(const XrWork& w, const XrFF& ff, cudaStream_t st) {
+  const int tb = 128;
+  const int gA = (w.A + tb - 1) / tb;
+  const int gB = (w.nB + tb - 1) / tb;
+  if (w.nB > 0) k_bo1<<<gB, tb, 0, st>>>(w, ff);
+  k_deltap<<<gA, tb, 0, st>>>(w);
+  if (w.nB > 0) k_bo2<<<gB, tb, 0, st>>>(w, ff);
+  k_atom1<<<gA, tb, 0, st>>>(w, ff);
+  k_atom2<<<gA, tb, 0, st>>>(w, ff);
+  if (w.nB > 0) k_bond_energy<<<gB, tb, 0, st>>>(w, ff);
+  k_angles<<<gA, tb, 0, st>>>(w, ff);
+  if (w.nB > 0) k_torsions<<<gB, tb, 0, st>>>(w, ff);
+  k_hbonds<<<(w.A + 3) / 4, 128, 0, st>>>(w, ff);
+  k_chain_atom<<<gA, tb, 0, st>>>(w, ff);
+  if (w.nB > 0) {
+    k_chain_bond<<<gB, tb, 0, st>>>(w, ff);
+    k_chain_deltap<<<gA, tb, 0, st>>>(w);
+    k_chain_radial<<<gB, tb, 0, st>>>(w);
+  }
+}

@@ -1,0 +1,197 @@
+// Shared device-side definitions for the GB300 ReaxFF evaluator.
+//
+// Data model (one "batch" = one or more independent systems evaluated together):
+//   atoms      : concatenated over systems; system s owns atoms [atom_off, atom_off + natoms).
+//   edges      : full directed neighbour list within the nonbonded cutoff, CSR by source atom,
+//                rows in canonical (j, Sx, Sy, Sz) order -- the order of xreac's Neighbors
+//                (src/xreac/neighbors.py:65-98). Each edge is int2 {j, code}.
+//   pairs      : the "half" edges (i < j, or i == j with a lexicographically negative shift),
+//                one per unordered image pair; nonbonded energies and forces run over pairs.
+//   bonds      : pairs within min(5 A, cutoff) (bond-order candidates, src/xreac/energy.py:109).
+//   bond rows  : per atom, its directed bond edges in canonical order, as (bond id, direction).
+// Pairs and bonds are numbered in source-atom order, so every system owns contiguous ranges of
+// atoms, edges, pairs and bonds. All physics is FP64; FP32 is used only to pre-classify squared
+// distances that lie far from a threshold.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#define XR_NATOM_COLS 24
+#define XR_NPAIR_COLS 28
+#define XR_NGENERAL 39
+#define XR_NCOMP 14
+
+// Atom table columns (xreac_gb300/forcefield.py: ATOM_COLUMNS).
+enum AtomCol {
+  A_R_S = 0, A_VALENCY, A_MASS, A_R_VDW, A_EPSILON, A_GAMMA, A_R_PI, A_VALENCY_E, A_ALPHA, A_GAMMA_W,
+  A_VALENCY_BOC, A_P_OVUN5, A_CHI, A_ETA, A_P_HBOND, A_R_PI_PI, A_P_LP2, A_P_OVUN2, A_P_VAL3,
+  A_VALENCY_VAL, A_P_VAL5, A_RCORE, A_ECORE, A_ACORE
+};
+// Pair table columns (xreac_gb300/forcefield.py: PAIR_COLUMNS).
+enum PairCol {
+  P_DE_S = 0, P_DE_P, P_DE_PP, P_BE1, P_BE2, P_BO1, P_BO2, P_BO3, P_BO4, P_BO5, P_BO6, P_OVUN1, P_OVC,
+  P_V13COR, P_RS, P_RP, P_RPP, P_BOC3, P_BOC4, P_BOC5, P_D, P_ALPHA, P_GAMMA_W, P_RVDW, P_RCORE,
+  P_ECORE, P_ACORE, P_GAMMA
+};
+// Energy components, in xreac's order (src/xreac/energy.py:26-41).
+enum Comp {
+  C_BOND = 0, C_ATOM, C_LONE_PAIR, C_MOLECULE, C_ANGLE, C_PENALTY, C_ANGLE_CONJ, C_HBOND, C_TORSION,
+  C_CONJ, C_VDW, C_COULOMB, C_EFIELD, C_QEQ
+};
+
+// Status bits written by kernels instead of trapping; the host maps them to errors.
+enum XrStatusBits {
+  XR_S_CAPACITY = 1 << 0,     // a list outgrew its buffer: the host grows it and retries
+  XR_S_SHIFT_RANGE = 1 << 1,  // an image shift does not fit the packed edge code
+  XR_S_COLLINEAR = 1 << 2,    // collinear atoms in an active torsion
+  XR_S_BOC_NAN = 1 << 3,      // NaN p_boc mixing on an active bond-order correction
+  XR_S_CG = 1 << 4,           // QEq conjugate gradient hit its iteration limit
+  XR_S_NONFINITE = 1 << 5,    // non-finite energy, charge or force
+  XR_S_COINCIDENT = 1 << 6,   // two atoms closer than 1e-6 A
+  XR_S_NONSPD = 1 << 7,       // QEq matrix not positive definite along a CG direction
+  XR_S_BARRIER = 1 << 8,      // a grid barrier wait reached its iteration limit
+  XR_S_REVERSE = 1 << 9,      // an edge without its reverse (internal consistency check)
+};
+
+// Edge code: three 9-bit signed image shifts plus flags. Sx sits in the highest shift bits so the
+// integer order of the 27 shift bits is the lexicographic order of (Sx, Sy, Sz).
+#define XR_CODE_BOND (1u << 27)   // r <= min(5, cutoff): bond-order candidate
+#define XR_CODE_HB (1u << 28)     // r <= min(7.5, cutoff): hydrogen-bond acceptor range
+#define XR_CODE_HALF (1u << 29)   // canonical half edge (owns the pair)
+#define XR_SHIFT_MASK ((1u << 27) - 1u)
+#define XR_SHIFT_MAX 255
+
+__host__ __device__ inline uint32_t xr_pack_shift(int sx, int sy, int sz) {
+  return ((uint32_t)(sx + 256) << 18) | ((uint32_t)(sy + 256) << 9) | (uint32_t)(sz + 256);
+}
+__host__ __device__ inline int xr_sx(uint32_t c) { return (int)((c >> 18) & 511u) - 256; }
+__host__ __device__ inline int xr_sy(uint32_t c) { return (int)((c >> 9) & 511u) - 256; }
+__host__ __device__ inline int xr_sz(uint32_t c) { return (int)(c & 511u) - 256; }
+// Shift bits of the reverse edge (-S).
+__host__ __device__ inline uint32_t xr_neg_shift(uint32_t c) {
+  return xr_pack_shift(-xr_sx(c), -xr_sy(c), -xr_sz(c));
+}
+
+// Per-system description (host-filled, uploaded with the batch).
+struct XrSystem {
+  int atom_off;          // first atom of the system
+  int natoms;
+  int periodic[3];       // pbc flags
+  int reach[3];          // image scan half-width per direction (0 non-periodic, 0 for large cells)
+  double cell[9];        // row vectors (identity when non-periodic)
+  double inv[9];         // inverse of cell (row-vector convention: frac = x @ inv)
+  double origin[3];      // reference point subtracted before FP32 rounding
+  double total_charge;
+  double rc, rc2, bond_cut, hb_cut;     // cutoff, cutoff^2, min(5, rc), min(7.5, rc)
+  float cellf[9];
+  float margin;          // bound on |FP32 squared distance - FP64 squared distance| (A^2)
+  int pad;
+};
+
+// Force-field tables on the device (uploaded once per force field).
+struct XrFF {
+  int ntypes;
+  int vdw_type;
+  double g[XR_NGENERAL];
+  const double* atom;         // [T][XR_NATOM_COLS]
+  const double* pair;         // [T*T][XR_NPAIR_COLS]
+  const double* pair_gw;      // [T*T] (1/gamma_w)^g28 for shielded vdW
+  const double* pair_logr;    // [T*T][3] log(r_s), log(r_p), log(r_pp) (0 where unused)
+  const int* is_carbon;       // [T] label is "C" (case-insensitive): C2 correction applies
+  const int* angle_index;     // [T^3][2] first, count
+  const double* angle;        // [R][7]
+  const int* torsion_index;   // [T^4] row or -1 (rows with a nonzero V1, V2, V3 or V_conj)
+  const double* torsion;      // [Q][5]
+  const int* hbond_index;     // [T^3] row or -1
+  const double* hbond;        // [H][4]
+};
+
+// Device work state of one batch. Sizes: A atoms, E edges, P pairs, B bonds, D = 2B bond-row
+// entries, S systems. Capacities (cap_*) are the allocated lengths; counts live on the device.
+struct XrWork {
+  int A, S;
+  int nE, nP, nB, nD;         // list sizes (known on the host once the count pass has been scanned)
+  long long cap_E, cap_P, cap_B;
+  int full_derivative;
+  int cg_max_iter;
+  double cg_tol;
+  const XrSystem* sys;
+  int* status;                // one int of XR_S_* bits
+  int* counts;                // [4]: E, P, B, D totals (last entries of the scans)
+  // atoms
+  const double4_32a* x;           // positions (w unused)
+  const int* type;
+  const int* sys_of;
+  int4* wrap;                 // integer lattice wrap of each atom
+  float4* xw;                 // wrapped position minus origin, FP32
+  float4* fw;                 // wrapped fractional coordinates, FP32
+  int* cnt;                   // [4][A+1] counts, then exclusive scans in place:
+                              //   0: edges, 1: half edges (pairs), 2: half bonds, 3: bond rows
+  // edges
+  int2* edge;                 // {j, code}
+  int* edge_pair;             // pair id of every edge (its own or its reverse's)
+  int* edge_dbslot;           // bond-row slot of bond edges, -1 otherwise
+  double* hval;               // per edge: 14.4 * shield of its pair (QEq matrix row entries)
+  // pairs
+  int* pair_edge;             // half edge of each pair
+  int* pair_i;                // source atom of each pair
+  int* pair_bond;             // bond id or -1
+  double* p_r;                // pair distance
+  double* p_shield;           // shield(r)
+  double* p_dshield;          // d shield / d r
+  double* p_g;                // accumulated dE/dr on the pair (nonbonded, bonded and H-bond radial parts)
+  double* p_evdw;             // vdW energy of the pair (both directions)
+  double* p_ecoul;            // Coulomb energy of the pair
+  // bonds
+  int* bond_pair;
+  int* bond_i;
+  int* bond_j;
+  double* b_r;                // bond length
+  double* b_v;                // [3][B] bond vector from bond_i to bond_j's image
+  double* b_fwd;              // [BF_N][B] forward intermediates (structure of arrays)
+  double* b_adj;              // [BJ_N][B] adjoint accumulators
+  double* b_e;                // [4][B] energies: bond, lone-pair C2, torsion, conjugation
+  int2* dbrow;                // [D] {bond id, +1 if the atom is the bond's source else -1}
+  // per-atom forward intermediates [AF_N][A] and adjoints [AJ_N][A] (structure of arrays)
+  double* a_fwd;
+  double* a_adj;
+  double* a_e;                // [8][A] per-atom energies: lp, atom, angle, penalty, coa, hb, qeq, spare
+  // charges and forces
+  double* q;
+  double* f;                  // [A][3] gradient dE/dx accumulator (forces = -f)
+  double* qwork;              // [XR_QW_N][A] QEq solver vectors
+  double* red;                // reduction scratch for solvers
+  unsigned* barrier;          // [2] grid-barrier counter and generation
+  // outputs
+  double* energy;             // [S][16]: 14 components, total, pad
+  double* props;              // [S][4]: dipole xyz, pad
+};
+
+// Per-atom forward slots in a_fwd.
+enum AF { AF_DELTAP = 0, AF_TOTAL, AF_NLP, AF_VLPEX, AF_DLP, AF_DLPT, AF_SUMPI, AF_PROD, AF_OV1, AF_OV2, AF_DC,
+          AF_SBO, AF_SBO2, AF_COUNT30, AF_E15, AF_N };
+// Per-atom adjoint slots in a_adj. AJ_TOTAL, AJ_D, AJ_DB and AJ_SBO2 collect the direct
+// sensitivities of the energy terms to total, d = total - valency, db = total - valency_boc and
+// sbo2; the rest are filled by the chain kernels.
+enum AJ { AJ_TOTAL = 0, AJ_D, AJ_DB, AJ_SBO2, AJ_OV1, AJ_OV2, AJ_DLPT, AJ_DLP, AJ_SUMPI, AJ_PRODSUM,
+          AJ_TOTAL_ALL, AJ_DELTAP, AJ_N };
+// Per-bond forward slots in b_fwd.
+enum BF { BF_BO0 = 0, BF_PI0, BF_PP0, BF_DSIG, BF_DPI, BF_DPP, BF_BO, BF_PI, BF_PP, BF_SIG, BF_F1, BF_F4, BF_F5,
+          BF_CORR, BF_MASK, BF_DF1I, BF_DF1J, BF_N };
+// Per-bond adjoint slots in b_adj: direct sensitivities to the thresholded bo, pi, pp, sigma, then
+// the chain's partial derivatives with respect to the uncorrected bond orders and the two ends' Delta'.
+enum BJ { BJ_BO = 0, BJ_PI, BJ_PP, BJ_SIG, BJ_BO0, BJ_PI0, BJ_PP0, BJ_CI, BJ_CJ, BJ_N };
+
+#define XR_QW_N 12
+
+// Kernel launchers (defined in the .cu files, called by the engine).
+void xr_launch_topology(const XrWork& w, cudaStream_t st);
+void xr_launch_scan(const XrWork& w, cudaStream_t st);
+void xr_launch_topology_fill(const XrWork& w, cudaStream_t st);
+void xr_launch_pairs(const XrWork& w, const XrFF& ff, cudaStream_t st);
+int xr_launch_qeq(const XrWork& w, const XrFF& ff, cudaStream_t st, int coop_blocks);
+int xr_qeq_coop_blocks_per_sm();
+void xr_launch_coulomb(const XrWork& w, const XrFF& ff, cudaStream_t st);
+void xr_launch_bonded(const XrWork& w, const XrFF& ff, cudaStream_t st);
+void xr_launch_forces(const XrWork& w, const XrFF& ff, cudaStream_t st);
+void xr_launch_reduce(const XrWork& w, const XrFF& ff, cudaStream_t st);

@@ -1,0 +1,821 @@
+// C ABI and orchestration of one evaluation (or a ragged batch of them) on the device.
+//
+// Sequence per call: upload positions and system descriptors -> count neighbour rows -> scan ->
+// (grow buffers) -> fill rows, pairs, bonds, reverse map -> pair kernel (vdW, shield) -> QEq ->
+// Coulomb -> bond orders, bonded energies and adjoints -> force assembly -> per-system reductions
+// -> one copy of the packed per-atom results back to the host (or straight into device outputs).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "xr_common.cuh"
+#include "xreac_gb300.h"
+
+namespace {
+
+struct DevArena {
+  std::vector<std::pair<void**, size_t>> dummy;
+};
+
+template <class T>
+bool grow(T** p, size_t* cap, size_t need) {
+  if (*p && *cap >= need) return true;
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  *cap = 0;
+  size_t n = std::max<size_t>(need, 1);
+  n = n + n / 4 + 64;
+  if (cudaMalloc((void**)p, n * sizeof(T)) != cudaSuccess) {
+    *p = nullptr;
+    return false;
+  }
+  *cap = n;
+  return true;
+}
+
+void inverse3(const double m[9], double inv[9], double* det_out) {
+  const double a = m[0], b = m[1], c = m[2], d = m[3], e = m[4], f = m[5], g = m[6], h = m[7], i = m[8];
+  const double A = e * i - f * h, B = -(d * i - f * g), C = d * h - e * g;
+  const double det = a * A + b * B + c * C;
+  *det_out = det;
+  inv[0] = A / det;
+  inv[3] = B / det;
+  inv[6] = C / det;
+  inv[1] = -(b * i - c * h) / det;
+  inv[4] = (a * i - c * g) / det;
+  inv[7] = -(a * h - b * g) / det;
+  inv[2] = (b * f - c * e) / det;
+  inv[5] = -(a * f - c * d) / det;
+  inv[8] = (a * e - b * d) / det;
+}
+
+}  // namespace
+
+struct xr_ff {
+  XrFF d{};
+  std::vector<void*> allocs;
+  int device = 0;
+};
+
+struct xr_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::string err;
+  double cg_tol = 1e-13;
+  int cg_max = 2000;
+  int nsm = 0;
+  int coop_per_sm = 0;
+  long long launches = 0;
+  // last batch layout (host copies for export)
+  std::vector<XrSystem> host_sys;
+  std::vector<int> host_cnt;  // [4][A+1] scans of the last evaluation
+  int last_A = 0;
+  // atom-sized buffers
+  size_t capA = 0;
+  double4_32a* x = nullptr;
+  size_t cx = 0;
+  int* type = nullptr;
+  size_t ctype = 0;
+  int* sys_of = nullptr;
+  size_t csys_of = 0;
+  int4* wrap = nullptr;
+  size_t cwrap = 0;
+  float4* xw = nullptr;
+  size_t cxw = 0;
+  float4* fw = nullptr;
+  size_t cfw = 0;
+  int* cnt = nullptr;
+  size_t ccnt = 0;
+  double* a_fwd = nullptr;
+  size_t ca_fwd = 0;
+  double* a_adj = nullptr;
+  size_t ca_adj = 0;
+  double* a_e = nullptr;
+  size_t ca_e = 0;
+  double* q = nullptr;
+  size_t cq = 0;
+  double* f = nullptr;
+  size_t cf = 0;
+  double* qwork = nullptr;
+  size_t cqwork = 0;
+  double* outbuf = nullptr;
+  size_t coutbuf = 0;
+  // edge / pair / bond buffers
+  int2* edge = nullptr;
+  size_t cedge = 0;
+  int* edge_pair = nullptr;
+  size_t cedge_pair = 0;
+  int* edge_dbslot = nullptr;
+  size_t cedge_dbslot = 0;
+  double* hval = nullptr;
+  size_t chval = 0;
+  int *pair_edge = nullptr, *pair_i = nullptr, *pair_bond = nullptr;
+  size_t cpair_edge = 0, cpair_i = 0, cpair_bond = 0;
+  double *p_r = nullptr, *p_shield = nullptr, *p_dshield = nullptr, *p_g = nullptr, *p_evdw = nullptr, *p_ecoul = nullptr;
+  size_t cp_r = 0, cp_shield = 0, cp_dshield = 0, cp_g = 0, cp_evdw = 0, cp_ecoul = 0;
+  int *bond_pair = nullptr, *bond_i = nullptr, *bond_j = nullptr;
+  size_t cbond_pair = 0, cbond_i = 0, cbond_j = 0;
+  double *b_r = nullptr, *b_v = nullptr, *b_fwd = nullptr, *b_adj = nullptr, *b_e = nullptr;
+  size_t cb_r = 0, cb_v = 0, cb_fwd = 0, cb_adj = 0, cb_e = 0;
+  size_t capB = 0;
+  int2* dbrow = nullptr;
+  size_t cdbrow = 0;
+  // system-sized and misc
+  XrSystem* sys = nullptr;
+  size_t csys = 0;
+  double* energy = nullptr;
+  size_t cenergy = 0;
+  double* props = nullptr;
+  size_t cprops = 0;
+  int* status = nullptr;
+  int* counts = nullptr;
+  unsigned* barrier = nullptr;
+  double* red = nullptr;
+  size_t cred = 0;
+  // pinned host staging
+  double4_32a* h_x = nullptr;
+  size_t ch_x = 0;
+  double* h_out = nullptr;
+  size_t ch_out = 0;
+  int* h_small = nullptr;  // status + counts
+};
+
+namespace {
+
+bool set_err(xr_ctx* c, const std::string& m) {
+  c->err = m;
+  return false;
+}
+
+int cuda_fail(xr_ctx* c, cudaError_t e, const char* where) {
+  c->err = std::string("CUDA error in ") + where + ": " + cudaGetErrorString(e);
+  return XR_ECUDA;
+}
+
+template <class T>
+bool host_grow(T** p, size_t* cap, size_t need) {
+  if (*p && *cap >= need) return true;
+  if (*p) cudaFreeHost(*p);
+  *p = nullptr;
+  *cap = 0;
+  size_t n = std::max<size_t>(need, 1);
+  n = n + n / 4 + 64;
+  if (cudaMallocHost((void**)p, n * sizeof(T)) != cudaSuccess) {
+    *p = nullptr;
+    return false;
+  }
+  *cap = n;
+  return true;
+}
+
+// Per-system descriptor: cell inverse, image scan reach and the FP32 error band.
+int build_system(xr_ctx* c, const xr_system& in, int atom_off, double rc, XrSystem& S, double4_32a* xpack) {
+  std::memset(&S, 0, sizeof(S));
+  S.atom_off = atom_off;
+  S.natoms = in.natoms;
+  bool any = false;
+  for (int k = 0; k < 3; ++k) {
+    S.periodic[k] = in.pbc[k] ? 1 : 0;
+    any = any || S.periodic[k];
+  }
+  double cell[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+  if (any) {
+    if (!in.cell) {
+      c->err = "A cell is required when pbc is enabled";
+      return XR_EINPUT;
+    }
+    for (int k = 0; k < 9; ++k) cell[k] = in.cell[k];
+  }
+  double inv[9], det;
+  inverse3(cell, inv, &det);
+  if (!(std::fabs(det) > 0) || !std::isfinite(det)) {
+    c->err = "Periodic cells must be nonsingular and right-handed";
+    return XR_EINPUT;
+  }
+  for (int k = 0; k < 9; ++k) {
+    S.cell[k] = cell[k];
+    S.inv[k] = inv[k];
+    S.cellf[k] = (float)cell[k];
+  }
+  double heights[3], lens[3];
+  for (int k = 0; k < 3; ++k) {
+    heights[k] = 1.0 / std::sqrt(inv[k] * inv[k] + inv[3 + k] * inv[3 + k] + inv[6 + k] * inv[6 + k]);
+    lens[k] = std::sqrt(cell[3 * k] * cell[3 * k] + cell[3 * k + 1] * cell[3 * k + 1] + cell[3 * k + 2] * cell[3 * k + 2]);
+    S.reach[k] = 0;
+    if (S.periodic[k] && !(heights[k] > 2.0 * rc)) S.reach[k] = (int)std::floor(rc / heights[k] + 0.5) + 1;
+  }
+  // Wrapped positions (as the device computes them) bound the FP32 coordinate magnitudes.
+  double origin[3] = {0, 0, 0};
+  double ext = 0.0;
+  for (int a = 0; a < in.natoms; ++a) {
+    const double* p = in.positions + 3 * a;
+    for (int k = 0; k < 3; ++k)
+      if (!std::isfinite(p[k])) {
+        c->err = "positions must be a finite (N, 3) array in Angstrom";
+        return XR_EINPUT;
+      }
+    double wr[3];
+    for (int k = 0; k < 3; ++k) {
+      const double fk = p[0] * inv[k] + p[1] * inv[3 + k] + p[2] * inv[6 + k];
+      wr[k] = S.periodic[k] ? std::floor(fk) : 0.0;
+    }
+    double xw[3];
+    for (int q = 0; q < 3; ++q) xw[q] = p[q] - (wr[0] * cell[q] + wr[1] * cell[3 + q] + wr[2] * cell[6 + q]);
+    if (a == 0)
+      for (int q = 0; q < 3; ++q) origin[q] = xw[q];
+    for (int q = 0; q < 3; ++q) ext = std::max(ext, std::fabs(xw[q] - origin[q]));
+    xpack[a] = make_double4_32a(p[0], p[1], p[2], 0.0);
+  }
+  double img = 0.0;
+  for (int k = 0; k < 3; ++k)
+    if (S.periodic[k]) img += (S.reach[k] + 2) * lens[k];
+  const double C = 2.0 * ext + img + 1.0;
+  const double u = 1.0 / 16777216.0;  // 2^-24
+  const double delta = 8.0 * u * C;    // per-component bound on |FP32 v - FP64 v|
+  const double margin = 2.0 * std::sqrt(3.0) * (rc + 2.0 * delta) * delta + 3.0 * delta * delta + 8.0 * u * rc * rc;
+  S.margin = (float)(4.0 * margin + 1e-6);
+  for (int q = 0; q < 3; ++q) S.origin[q] = origin[q];
+  S.total_charge = in.total_charge;
+  S.rc = rc;
+  S.rc2 = rc * rc;
+  S.bond_cut = std::min(5.0, rc);
+  S.hb_cut = std::min(7.5, rc);
+  return XR_OK;
+}
+
+#define GROW(field, n)                                      \
+  do {                                                      \
+    if (!grow(&c->field, &c->c##field, (size_t)(n))) return false; \
+  } while (0)
+
+bool ensure_atoms(xr_ctx* c, int A, int S) {
+  GROW(x, A);
+  GROW(type, A);
+  GROW(sys_of, A);
+  GROW(wrap, A);
+  GROW(xw, A);
+  GROW(fw, A);
+  GROW(cnt, 4 * (size_t)(A + 1));
+  GROW(a_fwd, (size_t)AF_N * A);
+  GROW(a_adj, (size_t)AJ_N * A);
+  GROW(a_e, 8 * (size_t)A);
+  GROW(q, A);
+  GROW(f, 3 * (size_t)A);
+  GROW(qwork, (size_t)XR_QW_N * A);
+  GROW(outbuf, 8 * (size_t)A);
+  GROW(sys, S);
+  GROW(energy, 16 * (size_t)S);
+  GROW(props, 4 * (size_t)S);
+  const size_t scan_ints = 4 * ((size_t)(A + 1) / 4096 + 2);
+  const size_t red = std::max<size_t>(scan_ints / 2 + 8, (size_t)4 * 4 * 2048);
+  GROW(red, red);
+  return true;
+}
+
+bool ensure_lists(xr_ctx* c, long long E, long long P, long long B) {
+  GROW(edge, E);
+  GROW(edge_pair, E);
+  GROW(edge_dbslot, E);
+  GROW(hval, E);
+  GROW(pair_edge, P);
+  GROW(pair_i, P);
+  GROW(pair_bond, P);
+  GROW(p_r, P);
+  GROW(p_shield, P);
+  GROW(p_dshield, P);
+  GROW(p_g, P);
+  GROW(p_evdw, P);
+  GROW(p_ecoul, P);
+  // bond arrays are structures of arrays with stride capB
+  if (c->capB < (size_t)B || !c->b_fwd) {
+    size_t nb = std::max<size_t>((size_t)B, 1);
+    nb = nb + nb / 4 + 64;
+    cudaFree(c->bond_pair);
+    cudaFree(c->bond_i);
+    cudaFree(c->bond_j);
+    cudaFree(c->b_r);
+    cudaFree(c->b_v);
+    cudaFree(c->b_fwd);
+    cudaFree(c->b_adj);
+    cudaFree(c->b_e);
+    cudaFree(c->dbrow);
+    c->bond_pair = c->bond_i = c->bond_j = nullptr;
+    c->b_r = c->b_v = c->b_fwd = c->b_adj = c->b_e = nullptr;
+    c->dbrow = nullptr;
+    bool ok = cudaMalloc((void**)&c->bond_pair, nb * sizeof(int)) == cudaSuccess &&
+              cudaMalloc((void**)&c->bond_i, nb * sizeof(int)) == cudaSuccess &&
+              cudaMalloc((void**)&c->bond_j, nb * sizeof(int)) == cudaSuccess &&
+              cudaMalloc((void**)&c->b_r, nb * sizeof(double)) == cudaSuccess &&
+              cudaMalloc((void**)&c->b_v, 3 * nb * sizeof(double)) == cudaSuccess &&
+              cudaMalloc((void**)&c->b_fwd, (size_t)BF_N * nb * sizeof(double)) == cudaSuccess &&
+              cudaMalloc((void**)&c->b_adj, (size_t)BJ_N * nb * sizeof(double)) == cudaSuccess &&
+              cudaMalloc((void**)&c->b_e, 4 * nb * sizeof(double)) == cudaSuccess &&
+              cudaMalloc((void**)&c->dbrow, 2 * nb * sizeof(int2)) == cudaSuccess;
+    if (!ok) return false;
+    c->capB = nb;
+  }
+  return true;
+}
+
+void fill_work(xr_ctx* c, XrWork& w, int A, int S, unsigned flags) {
+  std::memset(&w, 0, sizeof(w));
+  w.A = A;
+  w.S = S;
+  w.full_derivative = (flags & XR_FLAG_FULL_DERIVATIVE) ? 1 : 0;
+  w.cg_max_iter = c->cg_max;
+  w.cg_tol = c->cg_tol;
+  w.sys = c->sys;
+  w.status = c->status;
+  w.counts = c->counts;
+  w.x = c->x;
+  w.type = c->type;
+  w.sys_of = c->sys_of;
+  w.wrap = c->wrap;
+  w.xw = c->xw;
+  w.fw = c->fw;
+  w.cnt = c->cnt;
+  w.a_fwd = c->a_fwd;
+  w.a_adj = c->a_adj;
+  w.a_e = c->a_e;
+  w.q = c->q;
+  w.f = c->f;
+  w.qwork = c->qwork;
+  w.red = c->red;
+  w.barrier = c->barrier;
+  w.energy = c->energy;
+  w.props = c->props;
+}
+
+void attach_lists(xr_ctx* c, XrWork& w) {
+  w.cap_E = (long long)c->cedge;
+  w.cap_P = (long long)c->cpair_edge;
+  w.cap_B = (long long)c->capB;
+  w.edge = c->edge;
+  w.edge_pair = c->edge_pair;
+  w.edge_dbslot = c->edge_dbslot;
+  w.hval = c->hval;
+  w.pair_edge = c->pair_edge;
+  w.pair_i = c->pair_i;
+  w.pair_bond = c->pair_bond;
+  w.p_r = c->p_r;
+  w.p_shield = c->p_shield;
+  w.p_dshield = c->p_dshield;
+  w.p_g = c->p_g;
+  w.p_evdw = c->p_evdw;
+  w.p_ecoul = c->p_ecoul;
+  w.bond_pair = c->bond_pair;
+  w.bond_i = c->bond_i;
+  w.bond_j = c->bond_j;
+  w.b_r = c->b_r;
+  w.b_v = c->b_v;
+  w.b_fwd = c->b_fwd;
+  w.b_adj = c->b_adj;
+  w.b_e = c->b_e;
+  w.dbrow = c->dbrow;
+}
+
+// Packs forces (-dE/dx), charges, total bond orders, lone pairs and bond counts per atom.
+__global__ void k_pack(XrWork w, double* out) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= w.A) return;
+  out[8 * a + 0] = -w.f[3 * a + 0];
+  out[8 * a + 1] = -w.f[3 * a + 1];
+  out[8 * a + 2] = -w.f[3 * a + 2];
+  out[8 * a + 3] = w.q[a];
+  out[8 * a + 4] = w.a_fwd[(size_t)AF_TOTAL * w.A + a];
+  out[8 * a + 5] = w.a_fwd[(size_t)AF_NLP * w.A + a];
+  out[8 * a + 6] = w.a_fwd[(size_t)AF_COUNT30 * w.A + a];
+  out[8 * a + 7] = 0.0;
+}
+
+// Device-output variant for a single system: writes straight into the caller's arrays.
+__global__ void k_unpack_device(XrWork w, double* forces, double* charges, double* tbo, double* nlp, int* counts) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= w.A) return;
+  if (forces) {
+    forces[3 * a + 0] = -w.f[3 * a + 0];
+    forces[3 * a + 1] = -w.f[3 * a + 1];
+    forces[3 * a + 2] = -w.f[3 * a + 2];
+  }
+  if (charges) charges[a] = w.q[a];
+  if (tbo) tbo[a] = w.a_fwd[(size_t)AF_TOTAL * w.A + a];
+  if (nlp) nlp[a] = w.a_fwd[(size_t)AF_NLP * w.A + a];
+  if (counts) counts[a] = (int)w.a_fwd[(size_t)AF_COUNT30 * w.A + a];
+}
+
+__global__ void k_positions_from_device(const double* pos, double4_32a* x, int n) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= n) return;
+  x[a] = make_double4_32a(pos[3 * a], pos[3 * a + 1], pos[3 * a + 2], 0.0);
+}
+
+int status_to_code(xr_ctx* c, int st) {
+  if (st & XR_S_COINCIDENT) {
+    c->err = "Coincident atoms are not supported";
+    return XR_ECOINCIDENT;
+  }
+  if (st & (XR_S_SHIFT_RANGE | XR_S_CAPACITY)) {
+    c->err = "An image shift exceeds the supported range of +-255 cells; wrap the positions into the cell";
+    return XR_ECAPACITY;
+  }
+  if (st & XR_S_REVERSE) {
+    c->err = "neighbors must include both directions: (i, j, S) and (j, i, -S)";
+    return XR_EINPUT;
+  }
+  if (st & XR_S_BOC_NAN) {
+    c->err = "Invalid p_boc mixing for an active bond-order correction";
+    return XR_EBADPARAM;
+  }
+  if (st & XR_S_COLLINEAR) {
+    c->err = "Collinear atoms in an active torsion: the dihedral derivative is undefined; perturb the geometry";
+    return XR_ECOLLINEAR;
+  }
+  if (st & (XR_S_CG | XR_S_NONSPD | XR_S_BARRIER)) {
+    c->err = "Singular QEq system; check the geometry and parameters";
+    return XR_ESINGULAR;
+  }
+  if (st & XR_S_NONFINITE) {
+    c->err = "Non-finite energy, charges, or forces; check the geometry";
+    return XR_ENONFINITE;
+  }
+  return XR_OK;
+}
+
+int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsigned flags, xr_result* out) {
+  if (!c || !ff || nsys < 1 || !sys) {
+    if (c) c->err = "invalid arguments";
+    return XR_EINPUT;
+  }
+  if (flags & XR_FLAG_FULL_DERIVATIVE) {
+    c->err = "full_derivative forces are not available in this build";
+    return XR_EUNSUPPORTED;
+  }
+  const bool dev_io = (flags & XR_FLAG_DEVICE_IO) != 0;
+  if (dev_io && nsys != 1) {
+    c->err = "device input/output is supported for single-system calls";
+    return XR_EINPUT;
+  }
+  cudaSetDevice(c->device);
+  const double rc = ff->d.g[12];
+  long long A64 = 0;
+  for (int s = 0; s < nsys; ++s) {
+    if (sys[s].natoms < 1 || !sys[s].types || !sys[s].positions) {
+      c->err = "A nonempty sequence of parameter-file atom labels is required";
+      return XR_EINPUT;
+    }
+    A64 += sys[s].natoms;
+  }
+  if (A64 > (1ll << 26)) {
+    c->err = "batch too large";
+    return XR_EINPUT;
+  }
+  const int A = (int)A64;
+  if (!ensure_atoms(c, A, nsys) || !host_grow(&c->h_x, &c->ch_x, (size_t)A) ||
+      !host_grow(&c->h_out, &c->ch_out, 8 * (size_t)A + 32 * (size_t)nsys + 8))
+    return cuda_fail(c, cudaErrorMemoryAllocation, "allocation");
+  c->host_sys.resize(nsys);
+  std::vector<int> types(A), sys_of(A);
+  int off = 0;
+  for (int s = 0; s < nsys; ++s) {
+    const xr_system& in = sys[s];
+    if (dev_io) {
+      // positions live on the device: descriptor from a host-side copy of the cell only
+      std::vector<double> hp(3 * (size_t)in.natoms);
+      cudaMemcpy(hp.data(), in.positions, hp.size() * sizeof(double), cudaMemcpyDeviceToHost);
+      xr_system tmp = in;
+      tmp.positions = hp.data();
+      int rcode = build_system(c, tmp, off, rc, c->host_sys[s], c->h_x + off);
+      if (rcode) return rcode;
+    } else {
+      int rcode = build_system(c, in, off, rc, c->host_sys[s], c->h_x + off);
+      if (rcode) return rcode;
+    }
+    for (int a = 0; a < in.natoms; ++a) {
+      const int t = in.types[a];
+      if (t < 0 || t >= ff->d.ntypes) {
+        c->err = "Atom types absent from the force field";
+        return XR_EINPUT;
+      }
+      types[off + a] = t;
+      sys_of[off + a] = s;
+    }
+    off += in.natoms;
+  }
+  cudaStream_t st = c->stream;
+  long long launches = 0;
+  cudaError_t e;
+  if (dev_io) {
+    k_positions_from_device<<<(A + 255) / 256, 256, 0, st>>>(sys[0].positions, c->x, A);
+    ++launches;
+  } else {
+    cudaMemcpyAsync(c->x, c->h_x, sizeof(double4_32a) * A, cudaMemcpyHostToDevice, st);
+  }
+  cudaMemcpyAsync(c->type, types.data(), sizeof(int) * A, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(c->sys_of, sys_of.data(), sizeof(int) * A, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(c->sys, c->host_sys.data(), sizeof(XrSystem) * nsys, cudaMemcpyHostToDevice, st);
+  cudaMemsetAsync(c->status, 0, sizeof(int), st);
+  cudaMemsetAsync(c->cnt, 0, sizeof(int) * 4 * (size_t)(A + 1), st);
+  XrWork w;
+  fill_work(c, w, A, nsys, flags);
+  attach_lists(c, w);
+  xr_launch_topology(w, st);
+  launches += 2;
+  xr_launch_scan(w, st);
+  launches += 3;
+  cudaMemcpyAsync(c->h_small, c->counts, 4 * sizeof(int), cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(c->h_small + 4, c->status, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(c, e, "neighbour count");
+  const int nE = c->h_small[0], nP = c->h_small[1], nB = c->h_small[2], nD = c->h_small[3];
+  if (int code = status_to_code(c, c->h_small[4])) return code;
+  if (!ensure_lists(c, nE, nP, nB)) return cuda_fail(c, cudaErrorMemoryAllocation, "list allocation");
+  attach_lists(c, w);
+  w.nE = nE;
+  w.nP = nP;
+  w.nB = nB;
+  w.nD = nD;
+  xr_launch_topology_fill(w, st);
+  launches += 2;
+  cudaMemsetAsync(c->a_adj, 0, sizeof(double) * (size_t)AJ_N * A, st);
+  cudaMemsetAsync(c->f, 0, sizeof(double) * 3 * (size_t)A, st);
+  cudaMemsetAsync(c->b_adj, 0, sizeof(double) * (size_t)BJ_N * c->capB, st);
+  cudaMemsetAsync(c->b_e, 0, sizeof(double) * 4 * c->capB, st);
+  xr_launch_pairs(w, ff->d, st);
+  launches += 2;
+  int coop = 0;
+  if (nsys == 1) {
+    const int rows_blocks = (A + 7) / 8;
+    coop = std::min(c->nsm * std::max(c->coop_per_sm, 1), rows_blocks);
+    coop = std::min(coop, 2048);
+    if (coop < 2) coop = 0;
+  }
+  if (int le = xr_launch_qeq(w, ff->d, st, coop)) return cuda_fail(c, (cudaError_t)le, "QEq launch");
+  launches += 1;
+  xr_launch_coulomb(w, ff->d, st);
+  launches += 1;
+  xr_launch_bonded(w, ff->d, st);
+  launches += 13;
+  xr_launch_forces(w, ff->d, st);
+  launches += 1;
+  xr_launch_reduce(w, ff->d, st);
+  launches += 1;
+  if (dev_io) {
+    const xr_result& r = out[0];
+    k_unpack_device<<<(A + 255) / 256, 256, 0, st>>>(w, r.forces, r.charges, r.total_bond_orders, r.lone_pairs,
+                                                    r.bond_counts);
+    ++launches;
+    cudaMemcpyAsync(c->h_out, c->energy, sizeof(double) * 16, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(c->h_out + 16, c->props, sizeof(double) * 4, cudaMemcpyDeviceToHost, st);
+  } else {
+    k_pack<<<(A + 255) / 256, 256, 0, st>>>(w, c->outbuf);
+    ++launches;
+    cudaMemcpyAsync(c->h_out, c->outbuf, sizeof(double) * 8 * A, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(c->h_out + 8 * (size_t)A, c->energy, sizeof(double) * 16 * nsys, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(c->h_out + 8 * (size_t)A + 16 * nsys, c->props, sizeof(double) * 4 * nsys, cudaMemcpyDeviceToHost, st);
+  }
+  cudaMemcpyAsync(c->h_small + 4, c->status, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(c, e, "evaluation");
+  if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(c, e, "kernel launch");
+  c->launches = launches;
+  c->last_A = A;
+  // keep the scans for export
+  c->host_cnt.resize(4 * (size_t)(A + 1));
+  cudaMemcpy(c->host_cnt.data(), c->cnt, sizeof(int) * 4 * (size_t)(A + 1), cudaMemcpyDeviceToHost);
+  if (int code = status_to_code(c, c->h_small[4])) return code;
+  if (dev_io) {
+    const xr_result& r = out[0];
+    if (r.energy) {
+      for (int k = 0; k < 14; ++k) r.energy[k] = c->h_out[k];
+      r.energy[14] = c->h_out[14];
+    }
+    if (r.dipole)
+      for (int k = 0; k < 3; ++k) r.dipole[k] = c->h_out[16 + k];
+    return XR_OK;
+  }
+  off = 0;
+  for (int s = 0; s < nsys; ++s) {
+    const xr_result& r = out[s];
+    const int n = sys[s].natoms;
+    const double* pa = c->h_out + 8 * (size_t)off;
+    const double* pe = c->h_out + 8 * (size_t)A + 16 * s;
+    const double* pp = c->h_out + 8 * (size_t)A + 16 * nsys + 4 * s;
+    if (r.energy)
+      for (int k = 0; k < 15; ++k) r.energy[k] = pe[k];
+    if (r.dipole)
+      for (int k = 0; k < 3; ++k) r.dipole[k] = pp[k];
+    for (int a = 0; a < n; ++a) {
+      const double* v = pa + 8 * a;
+      if (r.forces) {
+        r.forces[3 * a + 0] = v[0];
+        r.forces[3 * a + 1] = v[1];
+        r.forces[3 * a + 2] = v[2];
+      }
+      if (r.charges) r.charges[a] = v[3];
+      if (r.total_bond_orders) r.total_bond_orders[a] = v[4];
+      if (r.lone_pairs) r.lone_pairs[a] = v[5];
+      if (r.bond_counts) r.bond_counts[a] = (int)v[6];
+    }
+    // the charge constraint check of src/xreac/calculator.py:153-154
+    if (r.charges) {
+      double sq = 0;
+      for (int a = 0; a < n; ++a) sq += r.charges[a];
+      if (std::fabs(sq - sys[s].total_charge) > 1e-8) {
+        c->err = "QEq charge constraint failed";
+        return XR_ECHARGE;
+      }
+    }
+    off += n;
+  }
+  return XR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int xr_ff_create(const double* general, int ntypes, const double* atom, const double* pair, const int* is_carbon,
+                 int vdw_type, const int* angle_index, const double* angle, int nangle, const int* torsion_index,
+                 const double* torsion, int ntorsion, const int* hbond_index, const double* hbond, int nhbond,
+                 xr_ff** out) {
+  if (!out || !general || ntypes < 1 || !atom || !pair || !is_carbon || !angle_index || !torsion_index || !hbond_index)
+    return XR_EINPUT;
+  if (vdw_type < 1 || vdw_type > 3) return XR_EINPUT;
+  xr_ff* f = new xr_ff();
+  cudaGetDevice(&f->device);
+  const int T = ntypes;
+  XrFF& d = f->d;
+  d.ntypes = T;
+  d.vdw_type = vdw_type;
+  for (int k = 0; k < XR_NGENERAL; ++k) d.g[k] = general[k];
+  // derived per-pair constants
+  std::vector<double> gw(T * T), logr(3 * T * T);
+  for (int pt = 0; pt < T * T; ++pt) {
+    const double* p = pair + pt * XR_NPAIR_COLS;
+    gw[pt] = std::pow(1.0 / p[P_GAMMA_W], general[28]);
+    logr[3 * pt + 0] = p[P_RS] > 0 ? std::log(p[P_RS]) : 0.0;
+    logr[3 * pt + 1] = p[P_RP] > 0 ? std::log(p[P_RP]) : 0.0;
+    logr[3 * pt + 2] = p[P_RPP] > 0 ? std::log(p[P_RPP]) : 0.0;
+  }
+  auto up = [&](const void* src, size_t bytes) -> void* {
+    void* dst = nullptr;
+    if (cudaMalloc(&dst, std::max<size_t>(bytes, 16)) != cudaSuccess) return nullptr;
+    if (bytes) cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice);
+    f->allocs.push_back(dst);
+    return dst;
+  };
+  d.atom = (const double*)up(atom, sizeof(double) * T * XR_NATOM_COLS);
+  d.pair = (const double*)up(pair, sizeof(double) * T * T * XR_NPAIR_COLS);
+  d.pair_gw = (const double*)up(gw.data(), sizeof(double) * T * T);
+  d.pair_logr = (const double*)up(logr.data(), sizeof(double) * 3 * T * T);
+  d.is_carbon = (const int*)up(is_carbon, sizeof(int) * T);
+  d.angle_index = (const int*)up(angle_index, sizeof(int) * 2 * T * T * T);
+  d.angle = (const double*)up(angle, sizeof(double) * 7 * (size_t)nangle);
+  d.torsion_index = (const int*)up(torsion_index, sizeof(int) * (size_t)T * T * T * T);
+  d.torsion = (const double*)up(torsion, sizeof(double) * 5 * (size_t)ntorsion);
+  d.hbond_index = (const int*)up(hbond_index, sizeof(int) * T * T * T);
+  d.hbond = (const double*)up(hbond, sizeof(double) * 4 * (size_t)nhbond);
+  for (void* p : f->allocs)
+    if (!p) {
+      xr_ff_destroy(f);
+      return XR_ECUDA;
+    }
+  *out = f;
+  return XR_OK;
+}
+
+void xr_ff_destroy(xr_ff* ff) {
+  if (!ff) return;
+  for (void* p : ff->allocs)
+    if (p) cudaFree(p);
+  delete ff;
+}
+
+int xr_ctx_create(int device, void* stream, xr_ctx** out) {
+  if (!out) return XR_EINPUT;
+  xr_ctx* c = new xr_ctx();
+  c->device = device;
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) {
+    delete c;
+    return XR_ECUDA;
+  }
+  if (stream) {
+    c->stream = (cudaStream_t)stream;
+  } else {
+    cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    c->own_stream = true;
+  }
+  cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device);
+  c->coop_per_sm = xr_qeq_coop_blocks_per_sm();
+  int coop_ok = 0;
+  cudaDeviceGetAttribute(&coop_ok, cudaDevAttrCooperativeLaunch, device);
+  if (!coop_ok) c->coop_per_sm = 0;
+  bool ok = cudaMalloc((void**)&c->status, sizeof(int)) == cudaSuccess &&
+            cudaMalloc((void**)&c->counts, 4 * sizeof(int)) == cudaSuccess &&
+            cudaMalloc((void**)&c->barrier, 2 * sizeof(unsigned)) == cudaSuccess &&
+            cudaMallocHost((void**)&c->h_small, 16 * sizeof(int)) == cudaSuccess;
+  if (!ok) {
+    xr_ctx_destroy(c);
+    return XR_ECUDA;
+  }
+  *out = c;
+  return XR_OK;
+}
+
+void xr_ctx_destroy(xr_ctx* c) {
+  if (!c) return;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  void* bufs[] = {c->x, c->type, c->sys_of, c->wrap, c->xw, c->fw, c->cnt, c->a_fwd, c->a_adj, c->a_e, c->q, c->f,
+                  c->qwork, c->outbuf, c->edge, c->edge_pair, c->edge_dbslot, c->hval, c->pair_edge, c->pair_i,
+                  c->pair_bond, c->p_r, c->p_shield, c->p_dshield, c->p_g, c->p_evdw, c->p_ecoul, c->bond_pair,
+                  c->bond_i, c->bond_j, c->b_r, c->b_v, c->b_fwd, c->b_adj, c->b_e, c->dbrow, c->sys, c->energy,
+                  c->props, c->status, c->counts, c->barrier, c->red};
+  for (void* p : bufs)
+    if (p) cudaFree(p);
+  if (c->h_x) cudaFreeHost(c->h_x);
+  if (c->h_out) cudaFreeHost(c->h_out);
+  if (c->h_small) cudaFreeHost(c->h_small);
+  if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+}
+
+const char* xr_last_error(const xr_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int xr_ctx_set_qeq(xr_ctx* c, double tolerance, int max_iterations) {
+  if (!c || !(tolerance > 0) || max_iterations < 1) return XR_EINPUT;
+  c->cg_tol = tolerance;
+  c->cg_max = max_iterations;
+  return XR_OK;
+}
+
+int xr_eval(xr_ctx* c, const xr_ff* ff, const xr_system* sys, unsigned flags, xr_result* out) {
+  return run_batch(c, ff, 1, sys, flags, out);
+}
+
+int xr_eval_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsigned flags, xr_result* out) {
+  return run_batch(c, ff, nsys, sys, flags, out);
+}
+
+long long xr_last_launches(const xr_ctx* c) { return c ? c->launches : 0; }
+
+int xr_get_neighbors(xr_ctx* c, int index, int* i, int* j, int* S, long long capacity, long long* count) {
+  if (!c || index < 0 || index >= (int)c->host_sys.size() || !count) return XR_EINPUT;
+  const int L = c->last_A + 1;
+  const XrSystem& sy = c->host_sys[index];
+  const int a0 = sy.atom_off, a1 = sy.atom_off + sy.natoms;
+  const int e0 = c->host_cnt[a0], e1 = c->host_cnt[a1];
+  *count = e1 - e0;
+  if (capacity < e1 - e0 || !i || !j || !S) return XR_OK;
+  std::vector<int2> ed(e1 - e0);
+  cudaMemcpy(ed.data(), c->edge + e0, sizeof(int2) * (e1 - e0), cudaMemcpyDeviceToHost);
+  (void)L;
+  for (int a = a0; a < a1; ++a)
+    for (int e = c->host_cnt[a]; e < c->host_cnt[a + 1]; ++e) {
+      const int k = e - e0;
+      const uint32_t code = (uint32_t)ed[k].y;
+      i[k] = a - a0;
+      j[k] = ed[k].x - a0;
+      S[3 * k + 0] = xr_sx(code);
+      S[3 * k + 1] = xr_sy(code);
+      S[3 * k + 2] = xr_sz(code);
+    }
+  return XR_OK;
+}
+
+int xr_get_bonds(xr_ctx* c, int index, int* i, int* j, int* S, double* bo, long long capacity, long long* count) {
+  if (!c || index < 0 || index >= (int)c->host_sys.size() || !count) return XR_EINPUT;
+  const int L = c->last_A + 1;
+  const XrSystem& sy = c->host_sys[index];
+  const int a0 = sy.atom_off, a1 = sy.atom_off + sy.natoms;
+  const int b0 = c->host_cnt[2 * L + a0], b1 = c->host_cnt[2 * L + a1];
+  *count = b1 - b0;
+  if (capacity < b1 - b0 || !i || !j || !S || !bo) return XR_OK;
+  const int nb = b1 - b0;
+  const int p0 = c->host_cnt[1 * L + a0], p1 = c->host_cnt[1 * L + a1];
+  const int e0 = c->host_cnt[a0], e1 = c->host_cnt[a1];
+  std::vector<int> bi(nb), bj(nb), bp(nb), pe(std::max(p1 - p0, 1));
+  std::vector<int2> ed(std::max(e1 - e0, 1));
+  std::vector<double> v(nb);
+  cudaMemcpy(bi.data(), c->bond_i + b0, sizeof(int) * nb, cudaMemcpyDeviceToHost);
+  cudaMemcpy(bj.data(), c->bond_j + b0, sizeof(int) * nb, cudaMemcpyDeviceToHost);
+  cudaMemcpy(bp.data(), c->bond_pair + b0, sizeof(int) * nb, cudaMemcpyDeviceToHost);
+  cudaMemcpy(v.data(), c->b_fwd + (size_t)BF_BO * c->capB + b0, sizeof(double) * nb, cudaMemcpyDeviceToHost);
+  cudaMemcpy(pe.data(), c->pair_edge + p0, sizeof(int) * (p1 - p0), cudaMemcpyDeviceToHost);
+  cudaMemcpy(ed.data(), c->edge + e0, sizeof(int2) * (e1 - e0), cudaMemcpyDeviceToHost);
+  for (int k = 0; k < nb; ++k) {
+    const uint32_t code = (uint32_t)ed[pe[bp[k] - p0] - e0].y;
+    i[k] = bi[k] - a0;
+    j[k] = bj[k] - a0;
+    S[3 * k + 0] = xr_sx(code);
+    S[3 * k + 1] = xr_sy(code);
+    S[3 * k + 2] = xr_sz(code);
+    bo[k] = v[k];
+  }
+  return XR_OK;
+}
+
+}  // extern "C"

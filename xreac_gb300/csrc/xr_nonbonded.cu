@@ -1,0 +1,499 @@
+// Nonbonded pairs, QEq charges, Coulomb, force assembly and per-system reductions (FP64).
+//
+// - Taper, shielded Coulomb kernel and tapered vdW (shielding and/or inner core) restate
+//   src/xreac/energy.py:89-92 and 213-219; each unordered image pair is evaluated once and counts
+//   for both of xreac's directed edges.
+// - QEq restates the KKT system of src/xreac/energy.py:95-102 as the two symmetric positive-definite
+//   systems H s = -chi and H t = -1 (H = 14.4 * sum of shields + diag(eta), self images on the
+//   diagonal), solved together by Jacobi-preconditioned conjugate gradients, with
+//   q = s + ((Q - sum s) / sum t) t. Matrix rows are gathered from the full directed neighbour
+//   rows, so a matrix-vector product needs no atomics and is deterministic.
+// - A single large system runs the solver as one cooperative grid with a barrier whose every wait
+//   is bounded; batches of systems give each system one thread block.
+#include "xr_common.cuh"
+
+namespace {
+
+constexpr double C_ELE = 332.06371;
+constexpr double QEQ_COULOMB = 14.4;
+constexpr double SELF_CONVERSION = 23.02;
+
+#define AEV(k, a) w.a_e[(size_t)(k) * w.A + (a)]
+#define QW(k, a) w.qwork[(size_t)(k) * w.A + (a)]
+
+__device__ inline double pair_prm(const XrFF& ff, int pt, int col) { return __ldg(ff.pair + pt * XR_NPAIR_COLS + col); }
+__device__ inline double atom_prm(const XrFF& ff, int t, int col) { return __ldg(ff.atom + t * XR_NATOM_COLS + col); }
+
+__device__ inline void edge_vector(const XrSystem& S, const double4_32a& xi, const double4_32a& xj, uint32_t code, double v[3]) {
+  const int sx = xr_sx(code), sy = xr_sy(code), sz = xr_sz(code);
+  const double xa[3] = {xi.x, xi.y, xi.z}, xb[3] = {xj.x, xj.y, xj.z};
+  for (int c = 0; c < 3; ++c) {
+    const double off = __dadd_rn(__dadd_rn(__dmul_rn((double)sx, S.cell[c]), __dmul_rn((double)sy, S.cell[3 + c])),
+                                 __dmul_rn((double)sz, S.cell[6 + c]));
+    v[c] = __dadd_rn(__dsub_rn(xb[c], xa[c]), off);
+  }
+}
+
+// ------------------------------------------------------------------------------ pair kernel
+__global__ void k_pairs(XrWork w, XrFF ff) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= w.nP) return;
+  const int e = w.pair_edge[p], i = w.pair_i[p];
+  const int2 ed = w.edge[e];
+  const int j = ed.x;
+  const XrSystem& S = w.sys[w.sys_of[i]];
+  double v[3];
+  edge_vector(S, w.x[i], w.x[j], (uint32_t)ed.y, v);
+  const double r = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(v[0], v[0]), __dmul_rn(v[1], v[1])), __dmul_rn(v[2], v[2])));
+  const double rc = S.rc;
+  const int T = ff.ntypes, pt = w.type[i] * T + w.type[j];
+  double taper = 0.0, dtaper = 0.0;
+  if (r < rc) {
+    const double u = r / rc;
+    taper = 1 + u * u * u * u * (-35 + u * (84 + u * (-70 + 20 * u)));
+    const double um = u - 1;
+    dtaper = 140.0 / rc * u * u * u * um * um * um;
+  }
+  const double gam = pair_prm(ff, pt, P_GAMMA);
+  const double c = cbrt(r * r * r + gam);
+  const double shield = taper / c;
+  const double dshield = dtaper / c - taper * r * r / (c * c * c * c);
+  double f13 = r, df13 = 1.0;
+  if (ff.vdw_type == 1 || ff.vdw_type == 3) {
+    const double pw = ff.g[28];
+    const double rp = exp(pw * log(r));
+    const double sum = rp + __ldg(ff.pair_gw + pt);
+    f13 = exp(log(sum) / pw);
+    df13 = f13 * rp / (sum * r);
+  }
+  const double D = pair_prm(ff, pt, P_D), alpha = pair_prm(ff, pt, P_ALPHA), rvdw = pair_prm(ff, pt, P_RVDW);
+  const double ev = exp(0.5 * alpha * (1 - f13 / rvdw));
+  const double dev = ev * (-0.5 * alpha / rvdw) * df13;
+  double E = taper * D * (ev * ev - 2 * ev);
+  double G = dtaper * D * (ev * ev - 2 * ev) + taper * D * (2 * ev - 2) * dev;
+  if (ff.vdw_type == 2 || ff.vdw_type == 3) {
+    const double ecore = pair_prm(ff, pt, P_ECORE), acore = pair_prm(ff, pt, P_ACORE), rcore = pair_prm(ff, pt, P_RCORE);
+    const double ec = ecore * exp(acore * (1 - r / rcore));
+    E += taper * ec;
+    G += dtaper * ec + taper * ec * (-acore / rcore);
+  }
+  w.p_r[p] = r;
+  w.p_shield[p] = shield;
+  w.p_dshield[p] = dshield;
+  w.p_evdw[p] = E;
+  w.p_g[p] = G;
+}
+
+__global__ void k_hval(XrWork w) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= w.nE) return;
+  w.hval[e] = QEQ_COULOMB * w.p_shield[w.edge_pair[e]];
+}
+
+// ---------------------------------------------------------------------------------- QEq
+// Solver vectors (QW slots).
+enum { Q_S = 0, Q_T, Q_RS, Q_RT, Q_PS, Q_PT, Q_APS, Q_APT, Q_MINV, Q_ZS, Q_ZT };
+
+// Bounded grid barrier for a cooperative launch (all blocks co-resident). Returns false when the
+// wait ran out; the caller then leaves the solver and the host reports the status bit.
+__device__ bool grid_barrier(unsigned* bar, unsigned nblocks, int* status) {
+  __syncthreads();
+  __shared__ int ok;
+  if (threadIdx.x == 0) {
+    ok = 1;
+    volatile unsigned* gen = bar + 1;
+    const unsigned g0 = *gen;
+    __threadfence();
+    const unsigned arrived = atomicAdd(bar, 1u);
+    if (arrived == nblocks - 1) {
+      bar[0] = 0;
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      long long it = 0;
+      while (*gen == g0) {
+        if (++it > (1ll << 22) || (*(volatile int*)status & XR_S_BARRIER)) {
+          atomicOr(status, XR_S_BARRIER);
+          ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return ok;
+}
+
+// Row product for both right-hand sides: y = H x over atom a's full row.
+__device__ inline void row_matvec(const XrWork& w, const XrFF& ff, int a, int lane, const double* xs, const double* xt,
+                                  double* ys, double* yt) {
+  const int L = w.A + 1;
+  double ss = 0, st = 0;
+  for (int e = w.cnt[a] + lane; e < w.cnt[a + 1]; e += 32) {
+    const int j = w.edge[e].x;
+    const double h = w.hval[e];
+    ss += h * xs[j];
+    st += h * xt[j];
+  }
+  (void)L;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    ss += __shfl_down_sync(0xffffffffu, ss, o);
+    st += __shfl_down_sync(0xffffffffu, st, o);
+  }
+  if (lane == 0) {
+    const double eta = atom_prm(ff, w.type[a], A_ETA);
+    *ys = eta * xs[a] + ss;
+    *yt = eta * xt[a] + st;
+  }
+}
+
+// Block-wide sum of NV values; result broadcast to all threads.
+template <int NV>
+__device__ inline void block_sum(double* v, double* smem) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int k = 0; k < NV; ++k)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+  __syncthreads();
+  if (lane == 0)
+    for (int k = 0; k < NV; ++k) smem[k * 32 + wid] = v[k];
+  __syncthreads();
+  for (int k = 0; k < NV; ++k) {
+    double s = 0;
+    for (int q = 0; q < nw; ++q) s += smem[k * 32 + q];
+    v[k] = s;
+  }
+  __syncthreads();
+}
+
+// Team abstraction: either the whole cooperative grid working on one system, or one block.
+struct GridTeam {
+  unsigned nblocks;
+  __device__ int warp() const { return (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); }
+  __device__ int nwarps() const { return (int)((gridDim.x * blockDim.x) >> 5); }
+  __device__ int thread() const { return (int)(blockIdx.x * blockDim.x + threadIdx.x); }
+  __device__ int nthreads() const { return (int)(gridDim.x * blockDim.x); }
+  __device__ bool sync(const XrWork& w) const { return grid_barrier(w.barrier, nblocks, w.status); }
+  // Sum NV values over the team: block sums written to w.red, then every block adds them in order.
+  template <int NV>
+  __device__ bool sum(const XrWork& w, double* v, double* smem, int slot) const {
+    block_sum<NV>(v, smem);
+    double* red = w.red + (size_t)slot * NV * gridDim.x;
+    if (threadIdx.x == 0)
+      for (int k = 0; k < NV; ++k) red[k * gridDim.x + blockIdx.x] = v[k];
+    if (!sync(w)) return false;
+    for (int k = 0; k < NV; ++k) {
+      double s = 0;
+      for (unsigned q = 0; q < gridDim.x; ++q) s += ((volatile double*)red)[k * gridDim.x + q];
+      v[k] = s;
+    }
+    return true;
+  }
+};
+
+struct BlockTeam {
+  __device__ int warp() const { return (int)(threadIdx.x >> 5); }
+  __device__ int nwarps() const { return (int)(blockDim.x >> 5); }
+  __device__ int thread() const { return (int)threadIdx.x; }
+  __device__ int nthreads() const { return (int)blockDim.x; }
+  __device__ bool sync(const XrWork&) const {
+    __syncthreads();
+    return true;
+  }
+  template <int NV>
+  __device__ bool sum(const XrWork&, double* v, double* smem, int) const {
+    block_sum<NV>(v, smem);
+    return true;
+  }
+};
+
+// Preconditioned CG on both right-hand sides for the atoms [a0, a0 + n) of one system.
+template <class Team>
+__device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int a0, int n, double Q, double* smem) {
+  const int lane = threadIdx.x & 31;
+  double* xs = &QW(Q_S, 0);
+  double* xt = &QW(Q_T, 0);
+  double* ps = &QW(Q_PS, 0);
+  double* pt = &QW(Q_PT, 0);
+  // Jacobi preconditioner: diag(H) = eta + self-image shields.
+  for (int r = team.warp(); r < n; r += team.nwarps()) {
+    const int a = a0 + r;
+    double d = 0;
+    for (int e = w.cnt[a] + lane; e < w.cnt[a + 1]; e += 32)
+      if (w.edge[e].x == a) d += w.hval[e];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) d += __shfl_down_sync(0xffffffffu, d, o);
+    if (lane == 0) QW(Q_MINV, a) = 1.0 / (atom_prm(ff, w.type[a], A_ETA) + d);
+  }
+  if (!team.sync(w)) return;
+  double v[4] = {0, 0, 0, 0};
+  for (int r = team.thread(); r < n; r += team.nthreads()) {
+    const int a = a0 + r;
+    const double bs = -atom_prm(ff, w.type[a], A_CHI), bt = -1.0, m = QW(Q_MINV, a);
+    QW(Q_S, a) = 0.0;
+    QW(Q_T, a) = 0.0;
+    QW(Q_RS, a) = bs;
+    QW(Q_RT, a) = bt;
+    QW(Q_PS, a) = m * bs;
+    QW(Q_PT, a) = m * bt;
+    v[0] += bs * m * bs;
+    v[1] += bt * m * bt;
+    v[2] += bs * bs;
+    v[3] += bt * bt;
+  }
+  if (!team.template sum<4>(w, v, smem, 0)) return;
+  double rz_s = v[0], rz_t = v[1];
+  const double tol2 = w.cg_tol * w.cg_tol;
+  const double bb_s = v[2], bb_t = v[3];
+  bool done_s = v[2] <= tol2 * bb_s, done_t = v[3] <= tol2 * bb_t;
+  int it = 0;
+  int slot = 1;
+  while (!(done_s && done_t)) {
+    if (++it > w.cg_max_iter) {
+      if (team.thread() == 0) atomicOr(w.status, XR_S_CG);
+      break;
+    }
+    for (int r = team.warp(); r < n; r += team.nwarps()) {
+      const int a = a0 + r;
+      double ys, yt;
+      row_matvec(w, ff, a, lane, ps, pt, &ys, &yt);
+      if (lane == 0) {
+        QW(Q_APS, a) = ys;
+        QW(Q_APT, a) = yt;
+      }
+    }
+    if (!team.sync(w)) return;
+    double u[2] = {0, 0};
+    for (int r = team.thread(); r < n; r += team.nthreads()) {
+      const int a = a0 + r;
+      u[0] += QW(Q_PS, a) * QW(Q_APS, a);
+      u[1] += QW(Q_PT, a) * QW(Q_APT, a);
+    }
+    if (!team.template sum<2>(w, u, smem, slot)) return;
+    slot = slot == 1 ? 2 : 1;
+    if ((!done_s && !(u[0] > 0)) || (!done_t && !(u[1] > 0))) {
+      if (team.thread() == 0) atomicOr(w.status, XR_S_NONSPD);
+      break;
+    }
+    const double as = done_s ? 0.0 : rz_s / u[0], at = done_t ? 0.0 : rz_t / u[1];
+    double z[4] = {0, 0, 0, 0};
+    for (int r = team.thread(); r < n; r += team.nthreads()) {
+      const int a = a0 + r;
+      const double m = QW(Q_MINV, a);
+      QW(Q_S, a) += as * QW(Q_PS, a);
+      QW(Q_T, a) += at * QW(Q_PT, a);
+      const double rs = QW(Q_RS, a) - as * QW(Q_APS, a);
+      const double rt = QW(Q_RT, a) - at * QW(Q_APT, a);
+      QW(Q_RS, a) = rs;
+      QW(Q_RT, a) = rt;
+      z[0] += rs * m * rs;
+      z[1] += rt * m * rt;
+      z[2] += rs * rs;
+      z[3] += rt * rt;
+    }
+    if (!team.template sum<4>(w, z, smem, slot)) return;
+    slot = slot == 1 ? 2 : 1;
+    const double bs = done_s ? 0.0 : z[0] / rz_s, bt = done_t ? 0.0 : z[1] / rz_t;
+    rz_s = z[0];
+    rz_t = z[1];
+    done_s = done_s || z[2] <= tol2 * bb_s;
+    done_t = done_t || z[3] <= tol2 * bb_t;
+    for (int r = team.thread(); r < n; r += team.nthreads()) {
+      const int a = a0 + r;
+      const double m = QW(Q_MINV, a);
+      QW(Q_PS, a) = m * QW(Q_RS, a) + bs * QW(Q_PS, a);
+      QW(Q_PT, a) = m * QW(Q_RT, a) + bt * QW(Q_PT, a);
+    }
+    if (!team.sync(w)) return;
+  }
+  // q = s + mu t with mu = (Q - sum s) / sum t.
+  double sm[2] = {0, 0};
+  for (int r = team.thread(); r < n; r += team.nthreads()) {
+    sm[0] += xs[a0 + r];
+    sm[1] += xt[a0 + r];
+  }
+  if (!team.template sum<2>(w, sm, smem, 3)) return;
+  const double mu = (Q - sm[0]) / sm[1];
+  for (int r = team.thread(); r < n; r += team.nthreads()) {
+    const int a = a0 + r;
+    const double q = xs[a] + mu * xt[a];
+    w.q[a] = q;
+    const int t = w.type[a];
+    AEV(6, a) = SELF_CONVERSION * (atom_prm(ff, t, A_CHI) * q + 0.5 * atom_prm(ff, t, A_ETA) * q * q);
+  }
+}
+
+__global__ void k_qeq_grid(XrWork w, XrFF ff) {
+  __shared__ double smem[4 * 32];
+  const XrSystem& S = w.sys[0];
+  GridTeam team{gridDim.x};
+  qeq_solve(w, ff, team, S.atom_off, S.natoms, S.total_charge, smem);
+}
+
+__global__ void k_qeq_block(XrWork w, XrFF ff) {
+  __shared__ double smem[4 * 32];
+  const XrSystem& S = w.sys[blockIdx.x];
+  BlockTeam team;
+  qeq_solve(w, ff, team, S.atom_off, S.natoms, S.total_charge, smem);
+}
+
+// ------------------------------------------------------------------------------ Coulomb
+__global__ void k_coulomb(XrWork w) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= w.nP) return;
+  const int i = w.pair_i[p], j = w.edge[w.pair_edge[p]].x;
+  const double qq = C_ELE * w.q[i] * w.q[j];
+  w.p_ecoul[p] = qq * w.p_shield[p];
+  w.p_g[p] += qq * w.p_dshield[p];
+}
+
+// ------------------------------------------------------------------------ force assembly
+// Every radial sensitivity (vdW, Coulomb, bond-order chain) sits on its pair: dE/dx_j += G v/r,
+// dE/dx_i -= G v/r.
+__global__ void k_pair_forces(XrWork w) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= w.nP) return;
+  const double G = w.p_g[p];
+  if (G == 0.0) return;
+  const int i = w.pair_i[p];
+  const int2 ed = w.edge[w.pair_edge[p]];
+  const int j = ed.x;
+  if (i == j) return;  // a self-image pair moves both ends together: no net force
+  const XrSystem& S = w.sys[w.sys_of[i]];
+  double v[3];
+  edge_vector(S, w.x[i], w.x[j], (uint32_t)ed.y, v);
+  const double s = G / w.p_r[p];
+  for (int c = 0; c < 3; ++c) {
+    atomicAdd(w.f + 3 * j + c, s * v[c]);
+    atomicAdd(w.f + 3 * i + c, -s * v[c]);
+  }
+}
+
+// ------------------------------------------------------------------------ reductions
+// One block per system sums every energy array over the system's contiguous atom, bond and pair
+// ranges in a fixed order (deterministic), computes the dipole about the mass centre, and checks
+// that energies, charges and forces are finite.
+__global__ void k_reduce(XrWork w, XrFF ff) {
+  __shared__ double smem[16 * 32];
+  const int s = blockIdx.x;
+  const XrSystem& S = w.sys[s];
+  const int L = w.A + 1;
+  const int a0 = S.atom_off, a1 = S.atom_off + S.natoms;
+  const int p0 = w.cnt[1 * L + a0], p1 = w.cnt[1 * L + a1];
+  const int b0 = w.cnt[2 * L + a0], b1 = w.cnt[2 * L + a1];
+  double v[16];
+  for (int k = 0; k < 16; ++k) v[k] = 0;
+  bool finite = true;
+  for (int a = a0 + threadIdx.x; a < a1; a += blockDim.x) {
+    v[C_LONE_PAIR] += AEV(0, a);
+    v[C_ATOM] += AEV(1, a);
+    v[C_ANGLE] += AEV(2, a);
+    v[C_PENALTY] += AEV(3, a);
+    v[C_ANGLE_CONJ] += AEV(4, a);
+    v[C_HBOND] += AEV(5, a);
+    v[C_QEQ] += AEV(6, a);
+    const double m = atom_prm(ff, w.type[a], A_MASS);
+    const double4_32a x = w.x[a];
+    v[14] += m;
+    v[C_MOLECULE] += 0.0;
+    finite = finite && isfinite(w.q[a]) && isfinite(w.f[3 * a]) && isfinite(w.f[3 * a + 1]) && isfinite(w.f[3 * a + 2]);
+    (void)x;
+  }
+  for (int b = b0 + threadIdx.x; b < b1; b += blockDim.x) {
+    v[C_BOND] += w.b_e[0 * w.cap_B + b];
+    v[C_LONE_PAIR] += w.b_e[1 * w.cap_B + b];
+    v[C_TORSION] += w.b_e[2 * w.cap_B + b];
+    v[C_CONJ] += w.b_e[3 * w.cap_B + b];
+  }
+  for (int p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
+    v[C_VDW] += w.p_evdw[p];
+    v[C_COULOMB] += w.p_ecoul[p];
+  }
+  block_sum<15>(v, smem);
+  // Dipole about the force-field mass centre (src/xreac/energy.py:171-177).
+  double c[3] = {0, 0, 0};
+  for (int a = a0 + threadIdx.x; a < a1; a += blockDim.x) {
+    const double m = atom_prm(ff, w.type[a], A_MASS);
+    const double4_32a x = w.x[a];
+    c[0] += m * x.x;
+    c[1] += m * x.y;
+    c[2] += m * x.z;
+  }
+  block_sum<3>(c, smem);
+  const double mt = v[14];
+  double dp[3] = {0, 0, 0};
+  for (int a = a0 + threadIdx.x; a < a1; a += blockDim.x) {
+    const double4_32a x = w.x[a];
+    const double q = w.q[a];
+    dp[0] += (x.x - c[0] / mt) * q;
+    dp[1] += (x.y - c[1] / mt) * q;
+    dp[2] += (x.z - c[2] / mt) * q;
+  }
+  block_sum<3>(dp, smem);
+  __shared__ int fin;
+  if (threadIdx.x == 0) fin = 1;
+  __syncthreads();
+  if (!finite) fin = 0;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double total = 0;
+    for (int k = 0; k < XR_NCOMP; ++k) {
+      w.energy[16 * s + k] = v[k];
+      total += v[k];
+      if (!isfinite(v[k])) fin = 0;
+    }
+    w.energy[16 * s + 14] = total;
+    w.energy[16 * s + 15] = 0.0;
+    w.props[4 * s + 0] = dp[0];
+    w.props[4 * s + 1] = dp[1];
+    w.props[4 * s + 2] = dp[2];
+    w.props[4 * s + 3] = 0.0;
+    if (!fin) atomicOr(w.status, XR_S_NONFINITE);
+  }
+}
+
+}  // namespace
+
+void xr_launch_pairs(const XrWork& w, const XrFF& ff, cudaStream_t st) {
+  if (w.nP > 0) k_pairs<<<(w.nP + 127) / 128, 128, 0, st>>>(w, ff);
+  if (w.nE > 0) k_hval<<<(w.nE + 255) / 256, 256, 0, st>>>(w);
+}
+
+int xr_qeq_coop_blocks_per_sm() {
+  int nb = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_qeq_grid, 256, 0);
+  return nb;
+}
+
+// Returns 0 on success or a CUDA error code from the launch.
+int xr_launch_qeq(const XrWork& w, const XrFF& ff, cudaStream_t st, int coop_blocks) {
+  if (w.S == 1 && coop_blocks > 1) {
+    const XrSystem* unused = nullptr;
+    (void)unused;
+    int blocks = coop_blocks;
+    // No more blocks than the rows need (8 warps per block).
+    // The host passes coop_blocks already clamped to the co-resident maximum.
+    cudaMemsetAsync(w.barrier, 0, 2 * sizeof(unsigned), st);
+    void* args[] = {(void*)&w, (void*)&ff};
+    cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_qeq_grid, dim3(blocks), dim3(256), args, 0, st);
+    return (int)e;
+  }
+  k_qeq_block<<<w.S, 256, 0, st>>>(w, ff);
+  return (int)cudaGetLastError();
+}
+
+void xr_launch_coulomb(const XrWork& w, const XrFF& ff, cudaStream_t st) {
+  (void)ff;
+  if (w.nP > 0) k_coulomb<<<(w.nP + 255) / 256, 256, 0, st>>>(w);
+}
+
+void xr_launch_forces(const XrWork& w, const XrFF& ff, cudaStream_t st) {
+  (void)ff;
+  if (w.nP > 0) k_pair_forces<<<(w.nP + 255) / 256, 256, 0, st>>>(w);
+}
+
+void xr_launch_reduce(const XrWork& w, const XrFF& ff, cudaStream_t st) { k_reduce<<<w.S, 256, 0, st>>>(w, ff); }

@@ -1,0 +1,351 @@
+// Neighbour, pair and bond topology on the device.
+//
+// Restates the edge set of xreac's replicated_neighbors (src/xreac/neighbors.py:17-53): every image
+// (j, S) of every atom with |x_j - x_i + S @ cell|^2 <= cutoff^2, zero-shift self edges excluded,
+// in the canonical (i, j, Sx, Sy, Sz) order of Neighbors (src/xreac/neighbors.py:65-131).
+//
+// GB300 design: FP64 issues at 1/58 of the FP32 rate on this part, so the all-pairs scan runs in
+// FP32 on cell-wrapped coordinates and only candidates whose squared distance lies inside a
+// per-system error band of a threshold (cutoff, bond cutoff, hydrogen-bond cutoff) are re-tested
+// with the reference's exact FP64 expression ((x_j - x_i) + S @ cell, ((vx^2 + vy^2) + vz^2)).
+// A warp scans one source atom against 32 targets at a time in increasing j, and each lane visits
+// its images in lexicographic shift order, so rows come out in canonical order without a sort.
+#include "xr_common.cuh"
+
+namespace {
+
+constexpr int kHitBit = 1 << 30;
+
+__global__ void k_prep(XrWork w) {
+  int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= w.A) return;
+  const XrSystem& S = w.sys[w.sys_of[a]];
+  const double4_32a p = w.x[a];
+  const double xs[3] = {p.x, p.y, p.z};
+  double f[3];
+  int wr[3];
+  for (int k = 0; k < 3; ++k) {
+    f[k] = xs[0] * S.inv[0 * 3 + k] + xs[1] * S.inv[1 * 3 + k] + xs[2] * S.inv[2 * 3 + k];
+    double fl = S.periodic[k] ? floor(f[k]) : 0.0;
+    fl = fmin(fmax(fl, -1.0e6), 1.0e6);
+    wr[k] = (int)fl;
+    f[k] -= fl;
+  }
+  double xw[3];
+  for (int c = 0; c < 3; ++c)
+    xw[c] = xs[c] - (wr[0] * S.cell[0 * 3 + c] + wr[1] * S.cell[1 * 3 + c] + wr[2] * S.cell[2 * 3 + c]) - S.origin[c];
+  w.wrap[a] = make_int4(wr[0], wr[1], wr[2], 0);
+  w.xw[a] = make_float4((float)xw[0], (float)xw[1], (float)xw[2], 0.f);
+  w.fw[a] = make_float4((float)f[0], (float)f[1], (float)f[2], 0.f);
+}
+
+// Exact FP64 edge vector with the reference's association: (x_j - x_i) + S @ cell.
+__device__ inline void exact_vector(const XrSystem& S, const double4_32a& xi, const double4_32a& xj, int sx, int sy, int sz,
+                                    double v[3]) {
+  const double xa[3] = {xi.x, xi.y, xi.z}, xb[3] = {xj.x, xj.y, xj.z};
+  for (int c = 0; c < 3; ++c) {
+    double off = __dadd_rn(__dadd_rn(__dmul_rn((double)sx, S.cell[0 * 3 + c]), __dmul_rn((double)sy, S.cell[1 * 3 + c])),
+                           __dmul_rn((double)sz, S.cell[2 * 3 + c]));
+    v[c] = __dadd_rn(__dsub_rn(xb[c], xa[c]), off);
+  }
+}
+
+__device__ inline double exact_d2(const double v[3]) {
+  return __dadd_rn(__dadd_rn(__dmul_rn(v[0], v[0]), __dmul_rn(v[1], v[1])), __dmul_rn(v[2], v[2]));
+}
+
+// Classify one candidate image. Returns 0 (no edge) or kHitBit | code.
+__device__ inline int classify(const XrWork& w, const XrSystem& S, int i, int j, const float4& pi, const float4& pj,
+                               const int4& wi, const int4& wj, int s0, int s1, int s2, const double4_32a& xi) {
+  const float vx = pj.x - pi.x + ((float)s0 * S.cellf[0] + (float)s1 * S.cellf[3] + (float)s2 * S.cellf[6]);
+  const float vy = pj.y - pi.y + ((float)s0 * S.cellf[1] + (float)s1 * S.cellf[4] + (float)s2 * S.cellf[7]);
+  const float vz = pj.z - pi.z + ((float)s0 * S.cellf[2] + (float)s1 * S.cellf[5] + (float)s2 * S.cellf[8]);
+  const float r2 = vx * vx + vy * vy + vz * vz;
+  const float mg = S.margin;
+  const float rc2f = (float)S.rc2;
+  if (r2 > rc2f + mg) return 0;
+  const int sx = s0 - wj.x + wi.x, sy = s1 - wj.y + wi.y, sz = s2 - wj.z + wi.z;
+  if (j == i && sx == 0 && sy == 0 && sz == 0) return 0;
+  const float bc2f = (float)(S.bond_cut * S.bond_cut), hc2f = (float)(S.hb_cut * S.hb_cut);
+  bool bond, hb;
+  const bool exact = (r2 >= rc2f - mg) || (fabsf(r2 - bc2f) <= mg) || (fabsf(r2 - hc2f) <= mg) || (r2 < 1.0e-2f);
+  if (exact) {
+    double v[3];
+    exact_vector(S, xi, w.x[j], sx, sy, sz, v);
+    const double d2 = exact_d2(v);
+    if (!(d2 <= S.rc2)) return 0;
+    const double r = __dsqrt_rn(d2);
+    if (r < 1e-6) atomicOr(w.status, XR_S_COINCIDENT);
+    bond = r <= S.bond_cut;
+    hb = r <= S.hb_cut;
+  } else {
+    bond = r2 < bc2f;
+    hb = r2 < hc2f;
+  }
+  if (sx < -XR_SHIFT_MAX || sx > XR_SHIFT_MAX || sy < -XR_SHIFT_MAX || sy > XR_SHIFT_MAX || sz < -XR_SHIFT_MAX ||
+      sz > XR_SHIFT_MAX) {
+    atomicOr(w.status, XR_S_SHIFT_RANGE);
+    return 0;
+  }
+  const bool neg = sx < 0 || (sx == 0 && (sy < 0 || (sy == 0 && sz < 0)));
+  const bool half = (i < j) || (i == j && neg);
+  return kHitBit | (int)(xr_pack_shift(sx, sy, sz) | (bond ? XR_CODE_BOND : 0u) | (hb ? XR_CODE_HB : 0u) |
+                         (half ? XR_CODE_HALF : 0u));
+}
+
+__device__ inline int warp_excl_scan(int v, int lane, int* total) {
+  int x = v;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, x, d);
+    if (lane >= d) x += y;
+  }
+  *total = __shfl_sync(0xffffffffu, x, 31);
+  return x - v;
+}
+
+// One warp per source atom. FILL=false counts, FILL=true writes the rows.
+template <bool FILL>
+__global__ void k_neighbors(XrWork w) {
+  const int lane = threadIdx.x & 31;
+  const int i = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
+  if (i >= w.A) return;
+  const XrSystem& S = w.sys[w.sys_of[i]];
+  const float4 pi = w.xw[i], fi = w.fw[i];
+  const int4 wi = w.wrap[i];
+  const double4_32a xi = w.x[i];
+  const int L = w.A + 1;
+  int n_e = 0, n_h = 0, n_bh = 0, n_ba = 0;  // warp-uniform running totals
+  int be = 0, bp = 0, bb = 0, bd = 0;
+  if (FILL) {
+    be = w.cnt[0 * L + i];
+    bp = w.cnt[1 * L + i];
+    bb = w.cnt[2 * L + i];
+    bd = w.cnt[3 * L + i];
+  }
+  const int r0 = S.reach[0], r1 = S.reach[1], r2 = S.reach[2];
+  for (int jb = 0; jb < S.natoms; jb += 32) {
+    const int jl = jb + lane;
+    const bool valid = jl < S.natoms;
+    const int j = S.atom_off + (valid ? jl : 0);
+    const float4 pj = w.xw[j], fj = w.fw[j];
+    const int4 wj = w.wrap[j];
+    const int b0 = S.periodic[0] ? -__float2int_rn(fj.x - fi.x) : 0;
+    const int b1 = S.periodic[1] ? -__float2int_rn(fj.y - fi.y) : 0;
+    const int b2 = S.periodic[2] ? -__float2int_rn(fj.z - fi.z) : 0;
+    int c_e = 0, c_h = 0, c_bh = 0, c_ba = 0;
+    if (valid) {
+      for (int o0 = -r0; o0 <= r0; ++o0)
+        for (int o1 = -r1; o1 <= r1; ++o1)
+          for (int o2 = -r2; o2 <= r2; ++o2) {
+            const int code = classify(w, S, i, j, pi, pj, wi, wj, b0 + o0, b1 + o1, b2 + o2, xi);
+            if (code) {
+              ++c_e;
+              const bool half = code & XR_CODE_HALF, bond = code & XR_CODE_BOND;
+              c_h += half;
+              c_bh += half && bond;
+              c_ba += bond;
+            }
+          }
+    }
+    int t_e, t_h, t_bh, t_ba;
+    const int o_e = warp_excl_scan(c_e, lane, &t_e);
+    const int o_h = warp_excl_scan(c_h, lane, &t_h);
+    const int o_bh = warp_excl_scan(c_bh, lane, &t_bh);
+    const int o_ba = warp_excl_scan(c_ba, lane, &t_ba);
+    if (FILL && c_e) {
+      int k_e = 0, k_h = 0, k_bh = 0, k_ba = 0;
+      for (int o0 = -r0; o0 <= r0; ++o0)
+        for (int o1 = -r1; o1 <= r1; ++o1)
+          for (int o2 = -r2; o2 <= r2; ++o2) {
+            const int code = classify(w, S, i, j, pi, pj, wi, wj, b0 + o0, b1 + o1, b2 + o2, xi);
+            if (!code) continue;
+            const uint32_t c = (uint32_t)code & ~(uint32_t)kHitBit;
+            const bool half = c & XR_CODE_HALF, bond = c & XR_CODE_BOND;
+            const int e = be + n_e + o_e + k_e++;
+            w.edge[e] = make_int2(j, (int)c);
+            int slot = -1;
+            if (bond) slot = bd + n_ba + o_ba + k_ba++;
+            w.edge_dbslot[e] = slot;
+            if (half) {
+              const int p = bp + n_h + o_h + k_h++;
+              w.edge_pair[e] = p;
+              w.pair_edge[p] = e;
+              w.pair_i[p] = i;
+              if (bond) {
+                const int b = bb + n_bh + o_bh + k_bh++;
+                w.pair_bond[p] = b;
+                w.bond_pair[b] = p;
+                w.bond_i[b] = i;
+                w.bond_j[b] = j;
+                w.dbrow[slot] = make_int2(b, 1);
+              } else {
+                w.pair_bond[p] = -1;
+              }
+            } else {
+              w.edge_pair[e] = -1;
+              if (bond) w.dbrow[slot] = make_int2(-1, -1);
+            }
+          }
+    }
+    n_e += t_e;
+    n_h += t_h;
+    n_bh += t_bh;
+    n_ba += t_ba;
+  }
+  if (!FILL && lane == 0) {
+    w.cnt[0 * L + i] = n_e;
+    w.cnt[1 * L + i] = n_h;
+    w.cnt[2 * L + i] = n_bh;
+    w.cnt[3 * L + i] = n_ba;
+  }
+}
+
+// Reverse edges: a non-half edge (i -> j, S) takes the pair of (j -> i, -S), found by binary search
+// in row j (rows are sorted by (j, shift bits), which is the canonical order).
+__global__ void k_reverse(XrWork w) {
+  const int lane = threadIdx.x & 31;
+  const int i = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
+  if (i >= w.A) return;
+  const int L = w.A + 1;
+  const int beg = w.cnt[0 * L + i], end = w.cnt[0 * L + i + 1];
+  for (int e = beg + lane; e < end; e += 32) {
+    const int2 ed = w.edge[e];
+    const uint32_t code = (uint32_t)ed.y;
+    if (code & XR_CODE_HALF) continue;
+    const int j = ed.x;
+    const uint64_t key = ((uint64_t)(uint32_t)i << 27) | xr_neg_shift(code & XR_SHIFT_MASK);
+    int lo = w.cnt[0 * L + j], hi = w.cnt[0 * L + j + 1];
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      const int2 m = w.edge[mid];
+      const uint64_t k = ((uint64_t)(uint32_t)m.x << 27) | ((uint32_t)m.y & XR_SHIFT_MASK);
+      if (k < key)
+        lo = mid + 1;
+      else
+        hi = mid;
+    }
+    const int rowend = w.cnt[0 * L + j + 1];
+    bool ok = lo < rowend;
+    if (ok) {
+      const int2 m = w.edge[lo];
+      ok = m.x == i && (((uint32_t)m.y & XR_SHIFT_MASK) == xr_neg_shift(code & XR_SHIFT_MASK));
+    }
+    if (!ok) {
+      // Inconsistent list (cannot happen for lists built here): record it and keep every index valid.
+      atomicOr(w.status, XR_S_REVERSE);
+      w.edge_pair[e] = 0;
+      if (code & XR_CODE_BOND) w.dbrow[w.edge_dbslot[e]] = make_int2(0, -1);
+      continue;
+    }
+    const int p = w.edge_pair[lo];
+    w.edge_pair[e] = p;
+    if (code & XR_CODE_BOND) w.dbrow[w.edge_dbslot[e]] = make_int2(w.pair_bond[p], -1);
+  }
+}
+
+// ---------------------------------------------------------------- multi-array exclusive scan
+// Scans the four count arrays cnt[k][0..A] in place (the last slot of each holds 0 on entry and
+// the total on exit) and copies the totals to counts[0..3].
+constexpr int kScanThreads = 1024;
+constexpr int kScanPer = 4;
+constexpr int kScanTile = kScanThreads * kScanPer;
+
+__device__ inline int block_excl_scan(int v, int* smem, int* total) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int x = v;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, x, d);
+    if (lane >= d) x += y;
+  }
+  if (lane == 31) smem[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    int s = lane < (blockDim.x >> 5) ? smem[lane] : 0;
+    int t = s;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, t, d);
+      if (lane >= d) t += y;
+    }
+    smem[lane] = t - s;
+    if (lane == 31) smem[32] = t;
+  }
+  __syncthreads();
+  const int r = x - v + smem[wid];
+  *total = smem[32];
+  __syncthreads();
+  return r;
+}
+
+__global__ void k_scan_blocks(XrWork w, int* block_sums, int nblocks) {
+  __shared__ int smem[33];
+  const int k = blockIdx.y, L = w.A + 1;
+  int* a = w.cnt + (size_t)k * L;
+  const int base = blockIdx.x * kScanTile + threadIdx.x * kScanPer;
+  int s = 0;
+  for (int t = 0; t < kScanPer; ++t) s += (base + t < L) ? a[base + t] : 0;
+  int total;
+  block_excl_scan(s, smem, &total);
+  if (threadIdx.x == 0) block_sums[k * nblocks + blockIdx.x] = total;
+}
+
+__global__ void k_scan_sums(XrWork w, int* block_sums, int nblocks) {
+  __shared__ int smem[33];
+  const int k = blockIdx.x;
+  int carry = 0;
+  for (int base = 0; base < nblocks; base += kScanThreads) {
+    const int idx = base + threadIdx.x;
+    const int v = idx < nblocks ? block_sums[k * nblocks + idx] : 0;
+    int total;
+    const int ex = block_excl_scan(v, smem, &total);
+    if (idx < nblocks) block_sums[k * nblocks + idx] = ex + carry;
+    carry += total;
+  }
+  if (threadIdx.x == 0) w.counts[k] = carry;
+}
+
+__global__ void k_scan_apply(XrWork w, const int* block_sums, int nblocks) {
+  __shared__ int smem[33];
+  const int k = blockIdx.y, L = w.A + 1;
+  int* a = w.cnt + (size_t)k * L;
+  const int base = blockIdx.x * kScanTile + threadIdx.x * kScanPer;
+  int v[kScanPer];
+  int s = 0;
+  for (int t = 0; t < kScanPer; ++t) {
+    v[t] = (base + t < L) ? a[base + t] : 0;
+    s += v[t];
+  }
+  int total;
+  int ex = block_excl_scan(s, smem, &total) + block_sums[k * nblocks + blockIdx.x];
+  for (int t = 0; t < kScanPer; ++t) {
+    if (base + t < L) a[base + t] = ex;
+    ex += v[t];
+  }
+}
+
+}  // namespace
+
+void xr_launch_topology(const XrWork& w, cudaStream_t st) {
+  k_prep<<<(w.A + 255) / 256, 256, 0, st>>>(w);
+  const int warps_per_block = 8;
+  k_neighbors<false><<<(w.A + warps_per_block - 1) / warps_per_block, 32 * warps_per_block, 0, st>>>(w);
+}
+
+// Needs w.red to hold at least 4 * ceil((A+1)/4096) ints.
+void xr_launch_scan(const XrWork& w, cudaStream_t st) {
+  const int L = w.A + 1;
+  const int nblocks = (L + kScanTile - 1) / kScanTile;
+  int* sums = reinterpret_cast<int*>(w.red);
+  k_scan_blocks<<<dim3(nblocks, 4), kScanThreads, 0, st>>>(w, sums, nblocks);
+  k_scan_sums<<<4, kScanThreads, 0, st>>>(w, sums, nblocks);
+  k_scan_apply<<<dim3(nblocks, 4), kScanThreads, 0, st>>>(w, sums, nblocks);
+}
+
+void xr_launch_topology_fill(const XrWork& w, cudaStream_t st) {
+  const int warps_per_block = 8;
+  const int blocks = (w.A + warps_per_block - 1) / warps_per_block;
+  k_neighbors<true><<<blocks, 32 * warps_per_block, 0, st>>>(w);
+  k_reverse<<<blocks, 32 * warps_per_block, 0, st>>>(w);
+}
