@@ -100,13 +100,25 @@ int xr_eval_batch(xr_ctx* ctx, const xr_ff* ff, int nsys, const xr_system* sys, 
  * number of directed edges; nothing is written when capacity is too small. Host pointers. */
 int xr_get_neighbors(xr_ctx* ctx, int index, int* i, int* j, int* S, long long capacity, long long* count);
 
-/* Bond orders of the last evaluation of system `index`, one entry per bond-order candidate
- * (unordered image pair within min(5 A, cutoff)): i, j, S (x3) and the corrected bond order.
+/* Nonzero corrected bond orders of the last evaluation of system `index`, one entry per unordered
+ * image pair (i, j, S) in pair order; the directed pair (j, i, -S) carries the same value.
  * Host pointers; *count as for xr_get_neighbors. */
 int xr_get_bonds(xr_ctx* ctx, int index, int* i, int* j, int* S, double* bo, long long capacity, long long* count);
 
 /* Number of CUDA kernels the last xr_eval / xr_eval_batch call launched. */
 long long xr_last_launches(const xr_ctx* ctx);
+
+/* Host-to-device and device-to-host bytes the last call moved (no reference counterpart). */
+int xr_last_transfer_bytes(const xr_ctx* ctx, long long* h2d, long long* d2h);
+
+/* Per-stage device timing with CUDA events on the context stream (no reference counterpart;
+ * instrumentation). enable=1 resets the accumulators. Stages: 0 neighbour count + scan (including
+ * the host read of the list sizes), 1 row fill + reverse map, 2 pair kernel (vdW, shield) and QEq
+ * matrix rows, 3 QEq solve, 4 Coulomb, 5 bond orders + bonded terms + adjoint chain, 6 force
+ * assembly + reductions + result packing. ms receives the summed
+ * milliseconds of the first n stages over *calls evaluations. */
+int xr_ctx_set_profiling(xr_ctx* ctx, int enable);
+int xr_ctx_stage_times(const xr_ctx* ctx, double* ms, int n, long long* calls);
 
 #ifdef __cplusplus
 }

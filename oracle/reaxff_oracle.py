@@ -113,7 +113,8 @@ def neighbor_list(x, cutoff, cell=None, pbc=None, chunk=256):
     the distance test ``sum(v * v) <= cutoff**2`` on ``v = (x_j - x_i) + S @ cell``.
     Instead of replicating the cell, each pair scans the integer shifts around
     its nearest image, ``floor(cutoff / height) + 1`` cells each way, which
-    reaches every image within the cutoff. Returned in canonical order.
+    reaches every image within the cutoff (only the nearest image when every
+    periodic height exceeds twice the cutoff). Returned in canonical order.
     """
     x = np.asarray(x, dtype=float)
     flags, m = boundary(cell, pbc)
@@ -123,6 +124,10 @@ def neighbor_list(x, cutoff, cell=None, pbc=None, chunk=256):
         inv = np.linalg.inv(m)
         heights = 1.0 / np.linalg.norm(inv, axis=0)
         reach = np.where(flags, np.floor(cutoff / heights) + 1, 0).astype(int)
+        # When every periodic height exceeds twice the cutoff, an image within the cutoff has
+        # |fractional offset| < 1/2 in each periodic direction, so it is the nearest image.
+        if np.all(heights[flags] > 2 * cutoff * (1 + 1e-9)):
+            reach = np.zeros(3, dtype=int)
     else:
         reach = np.zeros(3, dtype=int)
     offsets = np.array(list(product(*[range(-r, r + 1) for r in reach])), dtype=np.int64)

@@ -24,6 +24,7 @@ workload), and a few request-stream samples.
 
 from __future__ import annotations
 
+import hashlib
 import json
 import sys
 import time
@@ -89,6 +90,8 @@ def workload_cases():
 
     add("cluster_water_192", w.water_cluster())  # the full 64-H2O cluster workload
     add("box_water_192", w.water_box(n_mol=64, box=12.42, seed=2))
+    # Periodic heights above twice the cutoff: only the nearest image of a pair can be in range.
+    add("box_water_1536", w.water_box(n_mol=512, box=24.82, seed=2))
     add("box_cho_89", w.cho_mixture(counts=(8, 8, 8, 3), seed=3))
     add("peroxide", w.hydrogen_peroxide())
     add("anatase_water_288", w.anatase_slab_water(displacement=0.05))
@@ -135,6 +138,7 @@ def run_case(name, ff_name, symbols, x, cell, pbc, charge, full_derivative=False
     comps, _, (bo, total, nlp) = model.components(np.asarray(x, float), q, return_bond_state=True)
     n = len(symbols)
     nz = np.flatnonzero(bo)
+    canon = np.column_stack((model.edges.i, model.edges.j, model.edges.shifts)).astype(np.int32)
     data = dict(
         ff=np.array(ff_name),
         symbols=np.array(symbols),
@@ -153,20 +157,22 @@ def run_case(name, ff_name, symbols, x, cell, pbc, charge, full_derivative=False
         bond_counts=res.bond_counts,
         dipole=res.dipole,
         cell_repetitions=np.array(res.cell_repetitions),
-        edge_i=model.edges.i.astype(np.int32),
-        edge_j=model.edges.j.astype(np.int32),
-        edge_S=model.edges.shifts.astype(np.int8),
-        bo_index=nz.astype(np.int32),
+        edge_count=np.array(len(canon)),
+        edge_sha256=np.array(hashlib.sha256(np.ascontiguousarray(canon).tobytes()).hexdigest()),
         bo_value=bo[nz],
         seconds=np.array(elapsed),
     )
+    if len(canon) <= 100_000:  # small lists are stored in full; large ones by count and hash
+        data.update(edge_i=canon[:, 0], edge_j=canon[:, 1], edge_S=canon[:, 2:].astype(np.int8), bo_index=nz.astype(np.int32))
+    else:
+        data.update(bo_i=canon[nz, 0], bo_j=canon[nz, 1], bo_S=canon[nz, 2:].astype(np.int8))
     if n <= 200:
         data["bond_orders"] = res.bond_orders
     np.savez_compressed(HERE / f"{name}.npz", **data)
     return elapsed, len(model.edges.i)
 
 
-def main(reference):
+def main(reference, only=None):
     _setup(reference)
     import xreac
 
@@ -177,13 +183,17 @@ def main(reference):
     cases = reference_cases()
     cases.update(workload_cases())
     for name, (ff_name, s, x, cell, pbc, charge) in cases.items():
+        if only and name not in only:
+            continue
         dt, m = run_case(name, ff_name, list(s), x, cell, pbc, charge)
         print(f"{name:28s} n={len(s):4d} edges={m:7d} {dt:6.2f} s", flush=True)
     for name in ("water_distorted_dimer", "zno_cluster20", "small_water_4A", "carbon_methane"):
+        if only and name + "_full" not in only:
+            continue
         ff_name, s, x, cell, pbc, charge = cases[name]
         run_case(name + "_full", ff_name, list(s), x, cell, pbc, charge, full_derivative=True)
         print(f"{name + '_full':28s} (charge-response forces)", flush=True)
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference", set(sys.argv[2:]) or None)

@@ -1,0 +1,235 @@
+"""Parity of the CUDA path (through the C ABI) with the reference and the CPU oracle.
+
+Tolerances: the reference's own strict backend-equivalence limits (xreac scripts/validate.py:122-146:
+energy and components per atom 1e-9, forces 2e-8, charges and bond orders 1e-10, counts exact,
+dipole 1e-9), the stated limits of the evaluation path (energy 1e-8 relative, forces 1e-6
+kcal/mol/A, charges 1e-8 e), and exact neighbour lists.
+"""
+
+import hashlib
+
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_golden
+
+pytestmark = pytest.mark.gpu
+
+COMP = ("bond atom lone_pair molecule angle penalty angle_conjugation hydrogen_bond torsion conjugation vdw coulomb "
+        "electric_field qeq").split()
+_CALCS = {}
+
+
+def calc(ff_name):
+    from xreac_gb300 import Calculator, ForceField
+
+    if ff_name not in _CALCS:
+        _CALCS[ff_name] = Calculator(ForceField.bundled(ff_name))
+    return _CALCS[ff_name]
+
+
+def check_strict(r, g, n):
+    E = float(g["energy"])
+    assert abs(r.energy - E) / n <= 1e-9
+    assert abs(r.energy - E) <= 1e-8 * max(1.0, abs(E))
+    comps = np.array([r.components[k] for k in COMP])
+    assert np.max(np.abs(comps - g["components"])) / n <= 1e-9
+    np.testing.assert_allclose(r.forces, g["forces"], atol=2e-8, rtol=0)
+    np.testing.assert_allclose(r.charges, g["charges"], atol=1e-10, rtol=0)
+    np.testing.assert_allclose(r.total_bond_orders, g["total_bond_orders"], atol=1e-10, rtol=0)
+    np.testing.assert_allclose(r.lone_pairs, g["lone_pairs"], atol=1e-10, rtol=0)
+    np.testing.assert_array_equal(r.bond_counts, g["bond_counts"])
+    np.testing.assert_allclose(r.dipole, g["dipole"], atol=1e-9, rtol=0)
+    assert tuple(r.cell_repetitions) == tuple(int(v) for v in g["cell_repetitions"])
+    assert abs(r.charges.sum() - g["total_charge"]) <= 1e-8
+
+
+def canonical_bonds(r):
+    i, j, S, bo = r.bonds
+    # both directions of every bond, in canonical (i, j, S) order, nonzero only
+    ii = np.concatenate((i, j))
+    jj = np.concatenate((j, i))
+    SS = np.concatenate((S, -S))
+    bb = np.concatenate((bo, bo))
+    keep = bb != 0
+    ii, jj, SS, bb = ii[keep], jj[keep], SS[keep], bb[keep]
+    order = np.lexsort((SS[:, 2], SS[:, 1], SS[:, 0], jj, ii))
+    return ii[order], jj[order], SS[order], bb[order]
+
+
+@pytest.mark.parametrize("name", [n for n in golden_names() if not n.endswith("_full")])
+def test_reference_fixture(name):
+    g = load_golden(name)
+    c = calc(g["ff"])
+    r = c.evaluate(g["symbols"], g["positions"], cell=g["cell"], pbc=g["pbc"], total_charge=g["total_charge"])
+    check_strict(r, g, len(g["symbols"]))
+    # neighbour list: the reference's canonical (i, j, S), exactly
+    i, j, S = c.neighbor_list()
+    canon = np.column_stack((i, j, S)).astype(np.int32)
+    assert len(canon) == int(g["edge_count"])
+    assert hashlib.sha256(np.ascontiguousarray(canon).tobytes()).hexdigest() == str(g["edge_sha256"])
+    # per-edge corrected bond orders
+    bi, bj, bS, bo = canonical_bonds(r)
+    np.testing.assert_allclose(bo, g["bo_value"], atol=1e-10, rtol=0)
+    if "bond_orders" in g:
+        np.testing.assert_allclose(r.bond_orders, g["bond_orders"], atol=1e-10, rtol=0)
+    assert c.last_launches > 0
+
+
+def test_release_known_answers():
+    """The reference's release check (.github/workflows/release.yml:77-87)."""
+    c = calc("ffield.reax.HO.2015")
+    r = c.evaluate(["O", "H", "H"], [[0, 0, 0], [0.97, 0, 0], [-0.243, 0.94, 0]])
+    assert abs(r.energy - (-248.34420920633704)) < 1e-8
+    assert np.isfinite(r.forces).all() and abs(r.charges.sum()) < 1e-12
+    ion = c.evaluate(["O", "H"], [[0, 0, 0], [0.97, 0, 0]], total_charge=-1)
+    assert abs(ion.charges.sum() + 1) < 1e-12
+
+
+@pytest.fixture(scope="module")
+def water_4608():
+    from xreac_gb300 import workloads
+
+    return workloads.water_box()
+
+
+def test_full_size_water_box_against_oracle(water_4608):
+    """The 1,536-H2O (4,608-atom) periodic water box against the CPU oracle."""
+    from oracle import evaluate as oracle_evaluate
+    from xreac_gb300 import ForceField
+
+    s = water_4608
+    c = calc(s.force_field)
+    r = c.evaluate(s.symbols, s.positions, cell=s.cell, pbc=s.pbc)
+    o = oracle_evaluate(ForceField.bundled(s.force_field), s.symbols, s.positions, cell=s.cell, pbc=s.pbc,
+                        dense_bond_orders=False)
+    n = len(s.symbols)
+    assert abs(r.energy - o["energy"]) <= 1e-8 * abs(o["energy"])
+    comps = np.array([r.components[k] for k in COMP])
+    ocomps = np.array([o["components"][k] for k in COMP])
+    assert np.max(np.abs(comps - ocomps)) / n <= 1e-9
+    np.testing.assert_allclose(r.forces, o["forces"], atol=1e-6, rtol=0)
+    np.testing.assert_allclose(r.charges, o["charges"], atol=1e-8, rtol=0)
+    np.testing.assert_allclose(r.total_bond_orders, o["total_bond_orders"], atol=1e-10, rtol=0)
+    np.testing.assert_array_equal(r.bond_counts, o["bond_counts"])
+    i, j, S = c.neighbor_list()
+    oi, oj, oS = o["neighbors"]
+    np.testing.assert_array_equal(i, oi)
+    np.testing.assert_array_equal(j, oj)
+    np.testing.assert_array_equal(S, oS)
+
+
+def test_full_size_properties(water_4608):
+    """Size-independent properties at full size: momentum, charge, determinism, invariances."""
+    s = water_4608
+    c = calc(s.force_field)
+    a = c.evaluate(s.symbols, s.positions, cell=s.cell, pbc=s.pbc)
+    b = c.evaluate(s.symbols, s.positions, cell=s.cell, pbc=s.pbc)
+    assert a.energy == b.energy  # deterministic reductions
+    np.testing.assert_array_equal(a.charges, b.charges)
+    np.testing.assert_allclose(a.forces, b.forces, atol=1e-12, rtol=0)
+    assert abs(a.charges.sum()) < 1e-10
+    np.testing.assert_allclose(a.forces.sum(axis=0), 0.0, atol=1e-8)
+    # periodic wrapping and translation leave the physics unchanged
+    rng = np.random.default_rng(900)
+    shift = rng.integers(-2, 3, s.positions.shape) @ s.cell
+    w = c.evaluate(s.symbols, s.positions + shift + [0.37, -1.1, 2.3], cell=s.cell, pbc=s.pbc)
+    assert w.energy == pytest.approx(a.energy, rel=1e-11)
+    np.testing.assert_allclose(w.forces, a.forces, atol=1e-8, rtol=0)
+    np.testing.assert_allclose(w.charges, a.charges, atol=1e-10, rtol=0)
+    # permutation
+    order = rng.permutation(len(s.symbols))
+    p = c.evaluate([s.symbols[k] for k in order], s.positions[order], cell=s.cell, pbc=s.pbc)
+    assert p.energy == pytest.approx(a.energy, rel=1e-11)
+    np.testing.assert_allclose(p.forces, a.forces[order], atol=1e-8, rtol=0)
+
+
+def test_cho_mixture_full_size():
+    """The 3,300-atom C/H/O mixture: all terms active, momentum and charge conservation, FD check."""
+    from xreac_gb300 import workloads
+
+    s = workloads.cho_mixture()
+    c = calc(s.force_field)
+    r = c.evaluate(s.symbols, s.positions, cell=s.cell, pbc=s.pbc)
+    for k in ("angle", "torsion", "hydrogen_bond", "bond", "lone_pair", "atom", "vdw", "coulomb"):
+        assert r.components[k] != 0.0, k
+    assert abs(r.charges.sum()) < 1e-10
+    np.testing.assert_allclose(r.forces.sum(axis=0), 0.0, atol=1e-7)
+
+
+def test_batch_matches_single_evaluations():
+    """A ragged batch gives each system the result it has alone."""
+    names = ["cluster_water_192", "periodic_partial_pbc_water", "charged_water_4A", "water_monomer", "stream_08",
+             "periodic_boundary_dimer"]
+    cases = [load_golden(n) for n in names]
+    c = calc("ffield.reax.HO.2015")
+    systems = [dict(symbols=g["symbols"], positions=g["positions"], cell=g["cell"], pbc=g["pbc"],
+                    total_charge=g["total_charge"]) for g in cases if g["ff"] == "ffield.reax.HO.2015"]
+    batch = c.evaluate_many(systems)
+    for s, rb in zip(systems, batch):
+        r1 = c.evaluate(**s)
+        assert rb.energy == pytest.approx(r1.energy, abs=1e-9 * len(s["symbols"]))
+        np.testing.assert_allclose(rb.forces, r1.forces, atol=1e-9, rtol=0)
+        np.testing.assert_allclose(rb.charges, r1.charges, atol=1e-11, rtol=0)
+
+
+def test_symmetries_cluster():
+    """Rotation, translation and permutation (tests/test_calculator.py:77-90 of the reference)."""
+    g = load_golden("zno_cluster20")
+    c = calc(g["ff"])
+    x = g["positions"]
+    sym = g["symbols"]
+    rot, _ = np.linalg.qr(np.random.default_rng(33).normal(size=(3, 3)))
+    r = c.evaluate(sym, x)
+    moved = c.evaluate(sym, x @ rot + [4.2, -3.1, 7])
+    assert moved.energy == pytest.approx(r.energy, abs=1e-10)
+    np.testing.assert_allclose(moved.forces, r.forces @ rot, atol=1e-9)
+    order = np.random.default_rng(33).permutation(len(x))
+    perm = c.evaluate([sym[k] for k in order], x[order])
+    assert perm.energy == pytest.approx(r.energy, abs=1e-10)
+    np.testing.assert_allclose(perm.charges, r.charges[order], atol=1e-12)
+    np.testing.assert_allclose(perm.forces, r.forces[order], atol=1e-9)
+
+
+@pytest.mark.parametrize(
+    "symbols,x,kwargs",
+    [
+        ([], [], {}),
+        (["He"], [[0, 0, 0]], {}),
+        (["He"], [[0, 0, 0]], {"cell": [4.0] * 3}),
+        (["Zn", "O"], [[0, 0, 0], [0, 0, 0]], {}),
+        (["Zn"], [[np.nan, 0, 0]], {}),
+        (["Zn"], [[0, 0]], {}),
+        (["Zn"], [[0, 0, 0]], {"total_charge": float("nan")}),
+        (["Zn"], [[0, 0, 0]], {"cell": np.eye(3)}),
+        (["Zn"], [[0, 0, 0]], {"full_derivative": "false"}),
+    ],
+)
+def test_invalid_input(symbols, x, kwargs):
+    """Invalid inputs raise ValueError (tests/test_calculator.py:93-109 of the reference)."""
+    c = calc("ffield.reax.ZnOH.2010")
+    with pytest.raises(ValueError):
+        c.evaluate(symbols, x, **kwargs)
+
+
+def test_coincident_atoms_in_periodic_image():
+    c = calc("ffield.reax.HO.2015")
+    with pytest.raises(ValueError, match="Coincident"):
+        c.evaluate(["O", "H"], [[0.0, 0, 0], [12.0, 0, 0]], cell=[12.0] * 3)
+
+
+def test_collinear_active_torsion():
+    """tests/test_general.py:545-562 of the reference."""
+    c = calc("ffield.reax.CHO.2008")
+    with pytest.raises(ValueError, match="Collinear atoms in an active torsion"):
+        c.evaluate(["C"] * 4, [[0, 0, 0], [1.5, 0, 0], [3, 0, 0], [4.5, 0.3, 0]])
+
+
+def test_small_cell_memory_limit():
+    """tests/test_small_cells.py:200-204 of the reference."""
+    from xreac_gb300 import Calculator, ForceField
+
+    g = load_golden("water_monomer")
+    with pytest.raises(ValueError, match="max_expanded_atoms"):
+        Calculator(ForceField.bundled("ffield.reax.HO.2015"), max_expanded_atoms=80).evaluate(
+            g["symbols"], g["positions"], cell=[4.0] * 3)

@@ -41,6 +41,9 @@ EXPORTED = (
     "xr_get_neighbors",
     "xr_get_bonds",
     "xr_last_launches",
+    "xr_ctx_set_profiling",
+    "xr_ctx_stage_times",
+    "xr_last_transfer_bytes",
 )
 
 
@@ -108,6 +111,12 @@ def load():
     lib.xr_get_bonds.restype = c_int
     lib.xr_last_launches.argtypes = [c_void_p]
     lib.xr_last_launches.restype = c_longlong
+    lib.xr_ctx_set_profiling.argtypes = [c_void_p, c_int]
+    lib.xr_ctx_set_profiling.restype = c_int
+    lib.xr_ctx_stage_times.argtypes = [c_void_p, POINTER(c_double), c_int, POINTER(c_longlong)]
+    lib.xr_ctx_stage_times.restype = c_int
+    lib.xr_last_transfer_bytes.argtypes = [c_void_p, POINTER(c_longlong), POINTER(c_longlong)]
+    lib.xr_last_transfer_bytes.restype = c_int
     _LIB = lib
     return lib
 

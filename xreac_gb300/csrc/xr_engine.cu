@@ -70,6 +70,7 @@ struct xr_ctx {
   int nsm = 0;
   int coop_per_sm = 0;
   long long launches = 0;
+  long long h2d_bytes = 0, d2h_bytes = 0;  // host<->device bytes moved by the last evaluation
   // last batch layout (host copies for export)
   std::vector<XrSystem> host_sys;
   std::vector<int> host_cnt;  // [4][A+1] scans of the last evaluation
@@ -136,6 +137,20 @@ struct xr_ctx {
   unsigned* barrier = nullptr;
   double* red = nullptr;
   size_t cred = 0;
+  // per-stage timing (CUDA events on the context stream), enabled by xr_ctx_set_profiling
+  bool profile = false;
+  static constexpr int kStages = 8;
+  cudaEvent_t ev[kStages + 1] = {};
+  double stage_ms[kStages] = {};
+  long long stage_calls = 0;
+  // compact export of nonzero bonds: {bond, i, j, code} and bo
+  int4* bx_meta = nullptr;
+  size_t cbx_meta = 0;
+  double* bx_bo = nullptr;
+  size_t cbx_bo = 0;
+  int* bx_count = nullptr;
+  std::vector<int4> h_bx_meta;
+  std::vector<double> h_bx_bo;
   // pinned host staging
   double4_32a* h_x = nullptr;
   size_t ch_x = 0;
@@ -206,7 +221,7 @@ int build_system(xr_ctx* c, const xr_system& in, int atom_off, double rc, XrSyst
     heights[k] = 1.0 / std::sqrt(inv[k] * inv[k] + inv[3 + k] * inv[3 + k] + inv[6 + k] * inv[6 + k]);
     lens[k] = std::sqrt(cell[3 * k] * cell[3 * k] + cell[3 * k + 1] * cell[3 * k + 1] + cell[3 * k + 2] * cell[3 * k + 2]);
     S.reach[k] = 0;
-    if (S.periodic[k] && !(heights[k] > 2.0 * rc)) S.reach[k] = (int)std::floor(rc / heights[k] + 0.5) + 1;
+    if (S.periodic[k] && !(heights[k] > 2.0 * rc * (1.0 + 1e-9))) S.reach[k] = (int)std::floor(rc / heights[k] + 0.5) + 1;
   }
   // Wrapped positions (as the device computes them) bound the FP32 coordinate magnitudes.
   double origin[3] = {0, 0, 0};
@@ -413,6 +428,27 @@ __global__ void k_positions_from_device(const double* pos, double4_32a* x, int n
   x[a] = make_double4_32a(pos[3 * a], pos[3 * a + 1], pos[3 * a + 2], 0.0);
 }
 
+// Nonzero corrected bond orders, compacted with warp-aggregated atomics; the host restores bond order.
+__global__ void k_bond_export(XrWork w, int4* meta, double* bo_out, int* counter) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const double bo = b < w.nB ? w.b_fwd[(size_t)BF_BO * w.cap_B + b] : 0.0;
+  const bool keep = b < w.nB && bo != 0.0;
+  const unsigned m = __ballot_sync(0xffffffffu, keep);
+  int base = 0;
+  if (lane == 0 && m) base = atomicAdd(counter, __popc(m));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (!keep) return;
+  const int slot = base + __popc(m & ((1u << lane) - 1u));
+  const int code = w.edge[w.pair_edge[w.bond_pair[b]]].y;
+  meta[slot] = make_int4(b, w.bond_i[b], w.bond_j[b], code);
+  bo_out[slot] = bo;
+}
+
+void stage(xr_ctx* c, int k, cudaStream_t st) {
+  if (c->profile) cudaEventRecord(c->ev[k], st);
+}
+
 int status_to_code(xr_ctx* c, int st) {
   if (st & XR_S_COINCIDENT) {
     c->err = "Coincident atoms are not supported";
@@ -507,27 +543,32 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
   }
   cudaStream_t st = c->stream;
   long long launches = 0;
+  long long h2d = 0, d2h = 0;
   cudaError_t e;
   if (dev_io) {
     k_positions_from_device<<<(A + 255) / 256, 256, 0, st>>>(sys[0].positions, c->x, A);
     ++launches;
   } else {
     cudaMemcpyAsync(c->x, c->h_x, sizeof(double4_32a) * A, cudaMemcpyHostToDevice, st);
+    h2d += sizeof(double4_32a) * (long long)A;
   }
   cudaMemcpyAsync(c->type, types.data(), sizeof(int) * A, cudaMemcpyHostToDevice, st);
   cudaMemcpyAsync(c->sys_of, sys_of.data(), sizeof(int) * A, cudaMemcpyHostToDevice, st);
   cudaMemcpyAsync(c->sys, c->host_sys.data(), sizeof(XrSystem) * nsys, cudaMemcpyHostToDevice, st);
+  h2d += 2 * sizeof(int) * (long long)A + sizeof(XrSystem) * (long long)nsys;
   cudaMemsetAsync(c->status, 0, sizeof(int), st);
   cudaMemsetAsync(c->cnt, 0, sizeof(int) * 4 * (size_t)(A + 1), st);
   XrWork w;
   fill_work(c, w, A, nsys, flags);
   attach_lists(c, w);
+  stage(c, 0, st);
   xr_launch_topology(w, st);
   launches += 2;
   xr_launch_scan(w, st);
   launches += 3;
   cudaMemcpyAsync(c->h_small, c->counts, 4 * sizeof(int), cudaMemcpyDeviceToHost, st);
   cudaMemcpyAsync(c->h_small + 4, c->status, sizeof(int), cudaMemcpyDeviceToHost, st);
+  d2h += 5 * sizeof(int);
   if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(c, e, "neighbour count");
   const int nE = c->h_small[0], nP = c->h_small[1], nB = c->h_small[2], nD = c->h_small[3];
   if (int code = status_to_code(c, c->h_small[4])) return code;
@@ -537,14 +578,17 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
   w.nP = nP;
   w.nB = nB;
   w.nD = nD;
+  stage(c, 1, st);
   xr_launch_topology_fill(w, st);
   launches += 2;
   cudaMemsetAsync(c->a_adj, 0, sizeof(double) * (size_t)AJ_N * A, st);
   cudaMemsetAsync(c->f, 0, sizeof(double) * 3 * (size_t)A, st);
   cudaMemsetAsync(c->b_adj, 0, sizeof(double) * (size_t)BJ_N * c->capB, st);
   cudaMemsetAsync(c->b_e, 0, sizeof(double) * 4 * c->capB, st);
+  stage(c, 2, st);
   xr_launch_pairs(w, ff->d, st);
   launches += 2;
+  stage(c, 3, st);
   int coop = 0;
   if (nsys == 1) {
     const int rows_blocks = (A + 7) / 8;
@@ -554,14 +598,26 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
   }
   if (int le = xr_launch_qeq(w, ff->d, st, coop)) return cuda_fail(c, (cudaError_t)le, "QEq launch");
   launches += 1;
+  stage(c, 4, st);
   xr_launch_coulomb(w, ff->d, st);
   launches += 1;
+  stage(c, 5, st);
   xr_launch_bonded(w, ff->d, st);
   launches += 13;
+  stage(c, 6, st);
   xr_launch_forces(w, ff->d, st);
   launches += 1;
   xr_launch_reduce(w, ff->d, st);
   launches += 1;
+  if (!grow(&c->bx_meta, &c->cbx_meta, (size_t)std::max(nB, 1)) || !grow(&c->bx_bo, &c->cbx_bo, (size_t)std::max(nB, 1)))
+    return cuda_fail(c, cudaErrorMemoryAllocation, "bond export");
+  cudaMemsetAsync(c->bx_count, 0, sizeof(int), st);
+  if (nB > 0) {
+    k_bond_export<<<(nB + 255) / 256, 256, 0, st>>>(w, c->bx_meta, c->bx_bo, c->bx_count);
+    ++launches;
+  }
+  cudaMemcpyAsync(c->h_small + 5, c->bx_count, sizeof(int), cudaMemcpyDeviceToHost, st);
+  d2h += 2 * sizeof(int);
   if (dev_io) {
     const xr_result& r = out[0];
     k_unpack_device<<<(A + 255) / 256, 256, 0, st>>>(w, r.forces, r.charges, r.total_bond_orders, r.lone_pairs,
@@ -569,17 +625,50 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
     ++launches;
     cudaMemcpyAsync(c->h_out, c->energy, sizeof(double) * 16, cudaMemcpyDeviceToHost, st);
     cudaMemcpyAsync(c->h_out + 16, c->props, sizeof(double) * 4, cudaMemcpyDeviceToHost, st);
+    d2h += 20 * sizeof(double);
   } else {
     k_pack<<<(A + 255) / 256, 256, 0, st>>>(w, c->outbuf);
     ++launches;
     cudaMemcpyAsync(c->h_out, c->outbuf, sizeof(double) * 8 * A, cudaMemcpyDeviceToHost, st);
     cudaMemcpyAsync(c->h_out + 8 * (size_t)A, c->energy, sizeof(double) * 16 * nsys, cudaMemcpyDeviceToHost, st);
     cudaMemcpyAsync(c->h_out + 8 * (size_t)A + 16 * nsys, c->props, sizeof(double) * 4 * nsys, cudaMemcpyDeviceToHost, st);
+    d2h += sizeof(double) * (8 * (long long)A + 20 * (long long)nsys);
   }
   cudaMemcpyAsync(c->h_small + 4, c->status, sizeof(int), cudaMemcpyDeviceToHost, st);
+  stage(c, 7, st);
   if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(c, e, "evaluation");
+  if (c->profile) {
+    for (int k = 0; k < 7; ++k) {
+      float ms = 0.f;
+      if (cudaEventElapsedTime(&ms, c->ev[k], c->ev[k + 1]) == cudaSuccess) c->stage_ms[k] += ms;
+    }
+    ++c->stage_calls;
+  }
+  {
+    const int nx = c->h_small[5];
+    c->h_bx_meta.resize(nx);
+    c->h_bx_bo.resize(nx);
+    d2h += (sizeof(int4) + sizeof(double)) * (long long)nx;
+    if (nx > 0) {
+      cudaMemcpy(c->h_bx_meta.data(), c->bx_meta, sizeof(int4) * nx, cudaMemcpyDeviceToHost);
+      cudaMemcpy(c->h_bx_bo.data(), c->bx_bo, sizeof(double) * nx, cudaMemcpyDeviceToHost);
+      std::vector<int> order(nx);
+      for (int k = 0; k < nx; ++k) order[k] = k;
+      std::sort(order.begin(), order.end(), [&](int a, int b) { return c->h_bx_meta[a].x < c->h_bx_meta[b].x; });
+      std::vector<int4> m2(nx);
+      std::vector<double> b2(nx);
+      for (int k = 0; k < nx; ++k) {
+        m2[k] = c->h_bx_meta[order[k]];
+        b2[k] = c->h_bx_bo[order[k]];
+      }
+      c->h_bx_meta.swap(m2);
+      c->h_bx_bo.swap(b2);
+    }
+  }
   if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(c, e, "kernel launch");
   c->launches = launches;
+  c->h2d_bytes = h2d;
+  c->d2h_bytes = d2h;
   c->last_A = A;
   // keep the scans for export
   c->host_cnt.resize(4 * (size_t)(A + 1));
@@ -716,6 +805,7 @@ int xr_ctx_create(int device, void* stream, xr_ctx** out) {
   bool ok = cudaMalloc((void**)&c->status, sizeof(int)) == cudaSuccess &&
             cudaMalloc((void**)&c->counts, 4 * sizeof(int)) == cudaSuccess &&
             cudaMalloc((void**)&c->barrier, 2 * sizeof(unsigned)) == cudaSuccess &&
+            cudaMalloc((void**)&c->bx_count, sizeof(int)) == cudaSuccess &&
             cudaMallocHost((void**)&c->h_small, 16 * sizeof(int)) == cudaSuccess;
   if (!ok) {
     xr_ctx_destroy(c);
@@ -733,12 +823,14 @@ void xr_ctx_destroy(xr_ctx* c) {
                   c->qwork, c->outbuf, c->edge, c->edge_pair, c->edge_dbslot, c->hval, c->pair_edge, c->pair_i,
                   c->pair_bond, c->p_r, c->p_shield, c->p_dshield, c->p_g, c->p_evdw, c->p_ecoul, c->bond_pair,
                   c->bond_i, c->bond_j, c->b_r, c->b_v, c->b_fwd, c->b_adj, c->b_e, c->dbrow, c->sys, c->energy,
-                  c->props, c->status, c->counts, c->barrier, c->red};
+                  c->props, c->status, c->counts, c->barrier, c->red, c->bx_meta, c->bx_bo, c->bx_count};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (c->h_x) cudaFreeHost(c->h_x);
   if (c->h_out) cudaFreeHost(c->h_out);
   if (c->h_small) cudaFreeHost(c->h_small);
+  for (int k = 0; k <= xr_ctx::kStages; ++k)
+    if (c->ev[k]) cudaEventDestroy(c->ev[k]);
   if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
   delete c;
 }
@@ -761,6 +853,13 @@ int xr_eval_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, un
 }
 
 long long xr_last_launches(const xr_ctx* c) { return c ? c->launches : 0; }
+
+int xr_last_transfer_bytes(const xr_ctx* c, long long* h2d, long long* d2h) {
+  if (!c) return XR_EINPUT;
+  if (h2d) *h2d = c->h2d_bytes;
+  if (d2h) *d2h = c->d2h_bytes;
+  return XR_OK;
+}
 
 int xr_get_neighbors(xr_ctx* c, int index, int* i, int* j, int* S, long long capacity, long long* count) {
   if (!c || index < 0 || index >= (int)c->host_sys.size() || !count) return XR_EINPUT;
@@ -792,29 +891,41 @@ int xr_get_bonds(xr_ctx* c, int index, int* i, int* j, int* S, double* bo, long 
   const XrSystem& sy = c->host_sys[index];
   const int a0 = sy.atom_off, a1 = sy.atom_off + sy.natoms;
   const int b0 = c->host_cnt[2 * L + a0], b1 = c->host_cnt[2 * L + a1];
-  *count = b1 - b0;
-  if (capacity < b1 - b0 || !i || !j || !S || !bo) return XR_OK;
-  const int nb = b1 - b0;
-  const int p0 = c->host_cnt[1 * L + a0], p1 = c->host_cnt[1 * L + a1];
-  const int e0 = c->host_cnt[a0], e1 = c->host_cnt[a1];
-  std::vector<int> bi(nb), bj(nb), bp(nb), pe(std::max(p1 - p0, 1));
-  std::vector<int2> ed(std::max(e1 - e0, 1));
-  std::vector<double> v(nb);
-  cudaMemcpy(bi.data(), c->bond_i + b0, sizeof(int) * nb, cudaMemcpyDeviceToHost);
-  cudaMemcpy(bj.data(), c->bond_j + b0, sizeof(int) * nb, cudaMemcpyDeviceToHost);
-  cudaMemcpy(bp.data(), c->bond_pair + b0, sizeof(int) * nb, cudaMemcpyDeviceToHost);
-  cudaMemcpy(v.data(), c->b_fwd + (size_t)BF_BO * c->capB + b0, sizeof(double) * nb, cudaMemcpyDeviceToHost);
-  cudaMemcpy(pe.data(), c->pair_edge + p0, sizeof(int) * (p1 - p0), cudaMemcpyDeviceToHost);
-  cudaMemcpy(ed.data(), c->edge + e0, sizeof(int2) * (e1 - e0), cudaMemcpyDeviceToHost);
-  for (int k = 0; k < nb; ++k) {
-    const uint32_t code = (uint32_t)ed[pe[bp[k] - p0] - e0].y;
-    i[k] = bi[k] - a0;
-    j[k] = bj[k] - a0;
+  // exported entries are sorted by bond id: the system's are one contiguous run
+  const auto& m = c->h_bx_meta;
+  const auto lo = std::lower_bound(m.begin(), m.end(), b0, [](const int4& v, int key) { return v.x < key; });
+  const auto hi = std::lower_bound(m.begin(), m.end(), b1, [](const int4& v, int key) { return v.x < key; });
+  const long long n = hi - lo;
+  *count = n;
+  if (capacity < n || !i || !j || !S || !bo) return XR_OK;
+  long long k = 0;
+  for (auto it = lo; it != hi; ++it, ++k) {
+    const uint32_t code = (uint32_t)it->w;
+    i[k] = it->y - a0;
+    j[k] = it->z - a0;
     S[3 * k + 0] = xr_sx(code);
     S[3 * k + 1] = xr_sy(code);
     S[3 * k + 2] = xr_sz(code);
-    bo[k] = v[k];
+    bo[k] = c->h_bx_bo[it - m.begin()];
   }
+  return XR_OK;
+}
+
+int xr_ctx_set_profiling(xr_ctx* c, int enable) {
+  if (!c) return XR_EINPUT;
+  cudaSetDevice(c->device);
+  if (enable && !c->ev[0])
+    for (int k = 0; k <= xr_ctx::kStages; ++k) cudaEventCreate(&c->ev[k]);
+  c->profile = enable != 0;
+  for (int k = 0; k < xr_ctx::kStages; ++k) c->stage_ms[k] = 0.0;
+  c->stage_calls = 0;
+  return XR_OK;
+}
+
+int xr_ctx_stage_times(const xr_ctx* c, double* ms, int n, long long* calls) {
+  if (!c || !ms) return XR_EINPUT;
+  for (int k = 0; k < n && k < xr_ctx::kStages; ++k) ms[k] = c->stage_ms[k];
+  if (calls) *calls = c->stage_calls;
   return XR_OK;
 }
 
