@@ -108,6 +108,10 @@ int xr_get_bonds(xr_ctx* ctx, int index, int* i, int* j, int* S, double* bo, lon
 /* Number of CUDA kernels the last xr_eval / xr_eval_batch call launched. */
 long long xr_last_launches(const xr_ctx* ctx);
 
+/* QEq conjugate-gradient iterations of the last call (largest over its systems; no reference
+ * counterpart: the reference solves the KKT system directly). */
+int xr_last_qeq_iterations(const xr_ctx* ctx);
+
 /* Host-to-device and device-to-host bytes the last call moved (no reference counterpart). */
 int xr_last_transfer_bytes(const xr_ctx* ctx, long long* h2d, long long* d2h);
 

@@ -44,6 +44,7 @@ EXPORTED = (
     "xr_ctx_set_profiling",
     "xr_ctx_stage_times",
     "xr_last_transfer_bytes",
+    "xr_last_qeq_iterations",
 )
 
 
@@ -117,6 +118,8 @@ def load():
     lib.xr_ctx_stage_times.restype = c_int
     lib.xr_last_transfer_bytes.argtypes = [c_void_p, POINTER(c_longlong), POINTER(c_longlong)]
     lib.xr_last_transfer_bytes.restype = c_int
+    lib.xr_last_qeq_iterations.argtypes = [c_void_p]
+    lib.xr_last_qeq_iterations.restype = c_int
     _LIB = lib
     return lib
 

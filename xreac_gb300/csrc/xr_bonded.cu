@@ -185,10 +185,13 @@ __global__ void k_atom1(XrWork w, XrFF ff) {
   const int L = w.A + 1, T = ff.ntypes, ta = w.type[a];
   const double* g = ff.g;
   double total = 0, sumpi = 0, prodsum = 0, ov1 = 0, n30 = 0;
-  for (int k = w.cnt[3 * L + a]; k < w.cnt[3 * L + a + 1]; ++k) {
+  const int beg = w.cnt[3 * L + a];
+  int nact = 0;
+  for (int k = beg; k < w.cnt[3 * L + a + 1]; ++k) {
     const int2 en = w.dbrow[k];
     const int b = en.x;
     const double bo = BFV(BF_BO, b);
+    if (bo > THB_CUT) w.arow[beg + nact++] = en;  // bonded rows of src/xreac/energy.py:220
     total += bo;
     sumpi += BFV(BF_PI, b) + BFV(BF_PP, b);
     const double b2 = bo * bo, b4 = b2 * b2;
@@ -220,6 +223,7 @@ __global__ void k_atom1(XrWork w, XrFF ff) {
   AFV(AF_OV1, a) = ov1;
   AFV(AF_COUNT30, a) = n30;
   AFV(AF_E15, a) = e15;
+  w.nact[a] = nact;
 }
 
 __device__ inline double sbo2_of(double sbo, double p) {
@@ -337,58 +341,55 @@ __global__ void k_bond_energy(XrWork w, XrFF ff) {
   BEV(1, b) = e_c2;
 }
 
-// Valence angle, penalty and angle conjugation, one thread per centre atom
-// (src/xreac/energy.py:278-318).
+// Valence angle, penalty and angle conjugation, one warp per centre atom; the lanes take the
+// pairs (left, right) of the centre's active bond-row entries, left before right in canonical
+// order (src/xreac/energy.py:278-318).
 __global__ void k_angles(XrWork w, XrFF ff) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int j = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
   if (j >= w.A) return;
   const int L = w.A + 1, T = ff.ntypes, tj = w.type[j];
   const double* g = ff.g;
-  const int beg = w.cnt[3 * L + j], end = w.cnt[3 * L + j + 1];
-  const double total_j = AFV(AF_TOTAL, j);
-  const double d_j = total_j - atom_prm(ff, tj, A_VALENCY);
-  const double db_j = total_j - atom_prm(ff, tj, A_VALENCY_BOC);
-  const double sbo2 = AFV(AF_SBO2, j);
-  const double pv3 = atom_prm(ff, tj, A_P_VAL3), pv5 = atom_prm(ff, tj, A_P_VAL5);
-  const double valval = atom_prm(ff, tj, A_VALENCY_VAL);
-  const double k180 = 3.14159265 / 180;
-  const double e17 = exp(-g[17] * (2 - sbo2));
-  // penalty and conjugation factors that depend on the centre only
-  const double ex3 = exp(-g[20] * d_j), ex4 = exp(g[21] * d_j);
-  const double den34 = 1 + ex3 + ex4;
-  const double Fp = (2 + ex3) / den34;
-  const double dFp_dd = (-g[20] * ex3 * den34 - (2 + ex3) * (-g[20] * ex3 + g[21] * ex4)) / (den34 * den34);
-  const double e2 = exp(g[2] * (total_j - valval));
-  const double K1 = 1.0 / (1.0 + e2);
-  const double dK1_dt = -g[2] * e2 * K1 * K1;
+  const int beg = w.cnt[3 * L + j], m = w.nact[j];
+  const int npairs = m * (m - 1) / 2;
   double E_ang = 0, E_pen = 0, E_coa = 0;
   double A_sbo2 = 0, A_db = 0, A_d = 0, A_tj = 0;
   double gj[3] = {0, 0, 0};
-  const bool lammps = !w.full_derivative;
-  for (int a = beg; a < end; ++a) {
-    const int2 ea = w.dbrow[a];
-    const double bo_l = BFV(BF_BO, ea.x);
-    if (!(bo_l > THB_CUT)) continue;
-    const int i = bond_other(w, ea.x, ea.y);
-    double vl[3];
-    bond_vec(w, ea.x, ea.y, vl);
-    const double rl = w.b_r[ea.x];
-    const double total_i = AFV(AF_TOTAL, i);
-    const int ti = w.type[i];
-    double gl[3] = {0, 0, 0}, dbo_l = 0, dtot_i = 0;
-    for (int c = a + 1; c < end; ++c) {
-      const int2 ec = w.dbrow[c];
-      const double bo_r = BFV(BF_BO, ec.x);
-      if (!(bo_r > THB_CUT)) continue;
+  if (npairs > 0) {
+    const double total_j = AFV(AF_TOTAL, j);
+    const double d_j = total_j - atom_prm(ff, tj, A_VALENCY);
+    const double db_j = total_j - atom_prm(ff, tj, A_VALENCY_BOC);
+    const double sbo2 = AFV(AF_SBO2, j);
+    const double pv3 = atom_prm(ff, tj, A_P_VAL3), pv5 = atom_prm(ff, tj, A_P_VAL5);
+    const double valval = atom_prm(ff, tj, A_VALENCY_VAL);
+    const double k180 = 3.14159265 / 180;
+    const double e17 = exp(-g[17] * (2 - sbo2));
+    const double ex3 = exp(-g[20] * d_j), ex4 = exp(g[21] * d_j);
+    const double den34 = 1 + ex3 + ex4;
+    const double Fp = (2 + ex3) / den34;
+    const double dFp_dd = (-g[20] * ex3 * den34 - (2 + ex3) * (-g[20] * ex3 + g[21] * ex4)) / (den34 * den34);
+    const double e2 = exp(g[2] * (total_j - valval));
+    const double K1 = 1.0 / (1.0 + e2);
+    const double dK1_dt = -g[2] * e2 * K1 * K1;
+    const bool lammps = !w.full_derivative;
+    for (int t = lane; t < npairs; t += 32) {
+      int a = 0, rem = t;
+      while (rem >= m - 1 - a) {
+        rem -= m - 1 - a;
+        ++a;
+      }
+      const int2 ea = w.arow[beg + a], ec = w.arow[beg + a + 1 + rem];
+      const double bo_l = BFV(BF_BO, ea.x), bo_r = BFV(BF_BO, ec.x);
       if (bo_l * bo_r <= THB_PRODUCT_CUT) continue;
-      const int k = bond_other(w, ec.x, ec.y);
-      const int key = (ti * T + tj) * T + w.type[k];
+      const int i = bond_other(w, ea.x, ea.y), k = bond_other(w, ec.x, ec.y);
+      const int key = (w.type[i] * T + tj) * T + w.type[k];
       const int first = __ldg(ff.angle_index + 2 * key), count = __ldg(ff.angle_index + 2 * key + 1);
       if (count == 0) continue;
-      double vr[3];
+      double vl[3], vr[3];
+      bond_vec(w, ea.x, ea.y, vl);
       bond_vec(w, ec.x, ec.y, vr);
-      const double rr = w.b_r[ec.x];
-      const double total_k = AFV(AF_TOTAL, k);
+      const double rl = w.b_r[ea.x], rr = w.b_r[ec.x];
+      const double total_i = AFV(AF_TOTAL, i), total_k = AFV(AF_TOTAL, k);
       const double cosv = (vl[0] * vr[0] + vl[1] * vr[1] + vl[2] * vr[2]) / (rl * rr);
       double theta, dth_dcos;
       if (lammps) {
@@ -403,7 +404,7 @@ __global__ void k_angles(XrWork w, XrFF ff) {
       }
       const double bij = bo_l - THB_CUT, bjk = bo_r - THB_CUT;
       const double lbij = log(bij), lbjk = log(bjk);
-      double dE_dcos = 0, dbij = 0, dbjk = 0, dtot_k = 0;
+      double dE_dcos = 0, dbij = 0, dbjk = 0, dtot_i = 0, dtot_k = 0;
       for (int q = 0; q < count; ++q) {
         const double* prm = ff.angle + 7 * (first + q);
         const double th00 = __ldg(prm + 0), v1 = __ldg(prm + 1), v2 = __ldg(prm + 2), coa1 = __ldg(prm + 3);
@@ -430,52 +431,63 @@ __global__ void k_angles(XrWork w, XrFF ff) {
         dbij += f8 * v1 * branch * df7_dbij;
         dbjk += f8 * v1 * branch * df7_dbjk;
         A_db += f7 * v1 * branch * df8_ddb;
-        // penalty
         const double Gp = exp(-g[19] * ((bij - 2) * (bij - 2) + (bjk - 2) * (bjk - 2)));
         const double ep = pen1 * Fp * Gp;
         E_pen += ep;
         A_d += pen1 * dFp_dd * Gp;
         dbij += ep * (-2 * g[19] * (bij - 2));
         dbjk += ep * (-2 * g[19] * (bjk - 2));
-        // angle conjugation
         const double ti_b = total_i - bij, tk_b = total_k - bjk;
         const double K2 = exp(-g[38] * (ti_b * ti_b + tk_b * tk_b));
         const double K3 = exp(-g[30] * ((bij - 1.5) * (bij - 1.5) + (bjk - 1.5) * (bjk - 1.5)));
-        const double ec = coa1 * K1 * K2 * K3;
-        E_coa += ec;
+        const double ec_ = coa1 * K1 * K2 * K3;
+        E_coa += ec_;
         A_tj += coa1 * dK1_dt * K2 * K3;
-        dtot_i += ec * (-2 * g[38] * ti_b);
-        dtot_k += ec * (-2 * g[38] * tk_b);
-        dbij += ec * (2 * g[38] * ti_b) + ec * (-2 * g[30] * (bij - 1.5));
-        dbjk += ec * (2 * g[38] * tk_b) + ec * (-2 * g[30] * (bjk - 1.5));
+        dtot_i += ec_ * (-2 * g[38] * ti_b);
+        dtot_k += ec_ * (-2 * g[38] * tk_b);
+        dbij += ec_ * (2 * g[38] * ti_b) + ec_ * (-2 * g[30] * (bij - 1.5));
+        dbjk += ec_ * (2 * g[38] * tk_b) + ec_ * (-2 * g[30] * (bjk - 1.5));
       }
       if (dE_dcos != 0.0) {
         const double inv = 1.0 / (rl * rr);
-        double gr[3];
+        double gl[3], gr[3];
         for (int c3 = 0; c3 < 3; ++c3) {
-          const double g_l = dE_dcos * (vr[c3] * inv - cosv * vl[c3] / (rl * rl));
+          gl[c3] = dE_dcos * (vr[c3] * inv - cosv * vl[c3] / (rl * rl));
           gr[c3] = dE_dcos * (vl[c3] * inv - cosv * vr[c3] / (rr * rr));
-          gl[c3] += g_l;
-          gj[c3] -= g_l + gr[c3];
+          gj[c3] -= gl[c3] + gr[c3];
         }
+        atomic_add3(w.f, i, gl[0], gl[1], gl[2]);
         atomic_add3(w.f, k, gr[0], gr[1], gr[2]);
       }
-      dbo_l += dbij;
+      if (dbij != 0.0) atomicAdd(&BJV(BJ_BO, ea.x), dbij);
       if (dbjk != 0.0) atomicAdd(&BJV(BJ_BO, ec.x), dbjk);
+      if (dtot_i != 0.0) atomicAdd(&AJV(AJ_TOTAL, i), dtot_i);
       if (dtot_k != 0.0) atomicAdd(&AJV(AJ_TOTAL, k), dtot_k);
     }
-    if (dbo_l != 0.0) atomicAdd(&BJV(BJ_BO, ea.x), dbo_l);
-    if (dtot_i != 0.0) atomicAdd(&AJV(AJ_TOTAL, i), dtot_i);
-    if (gl[0] != 0.0 || gl[1] != 0.0 || gl[2] != 0.0) atomic_add3(w.f, i, gl[0], gl[1], gl[2]);
   }
-  AEV(2, j) = E_ang;
-  AEV(3, j) = E_pen;
-  AEV(4, j) = E_coa;
-  if (A_sbo2 != 0.0) atomicAdd(&AJV(AJ_SBO2, j), A_sbo2);
-  if (A_db != 0.0) atomicAdd(&AJV(AJ_DB, j), A_db);
-  if (A_d != 0.0) atomicAdd(&AJV(AJ_D, j), A_d);
-  if (A_tj != 0.0) atomicAdd(&AJV(AJ_TOTAL, j), A_tj);
-  if (gj[0] != 0.0 || gj[1] != 0.0 || gj[2] != 0.0) atomic_add3(w.f, j, gj[0], gj[1], gj[2]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    E_ang += __shfl_xor_sync(0xffffffffu, E_ang, o);
+    E_pen += __shfl_xor_sync(0xffffffffu, E_pen, o);
+    E_coa += __shfl_xor_sync(0xffffffffu, E_coa, o);
+    A_sbo2 += __shfl_xor_sync(0xffffffffu, A_sbo2, o);
+    A_db += __shfl_xor_sync(0xffffffffu, A_db, o);
+    A_d += __shfl_xor_sync(0xffffffffu, A_d, o);
+    A_tj += __shfl_xor_sync(0xffffffffu, A_tj, o);
+    gj[0] += __shfl_xor_sync(0xffffffffu, gj[0], o);
+    gj[1] += __shfl_xor_sync(0xffffffffu, gj[1], o);
+    gj[2] += __shfl_xor_sync(0xffffffffu, gj[2], o);
+  }
+  if (lane == 0) {
+    AEV(2, j) = E_ang;
+    AEV(3, j) = E_pen;
+    AEV(4, j) = E_coa;
+    if (A_sbo2 != 0.0) atomicAdd(&AJV(AJ_SBO2, j), A_sbo2);
+    if (A_db != 0.0) atomicAdd(&AJV(AJ_DB, j), A_db);
+    if (A_d != 0.0) atomicAdd(&AJV(AJ_D, j), A_d);
+    if (A_tj != 0.0) atomicAdd(&AJV(AJ_TOTAL, j), A_tj);
+    if (gj[0] != 0.0 || gj[1] != 0.0 || gj[2] != 0.0) atomic_add3(w.f, j, gj[0], gj[1], gj[2]);
+  }
 }
 
 __device__ inline void cross3(const double a[3], const double b[3], double c[3]) {
@@ -490,7 +502,11 @@ __global__ void k_torsions(XrWork w, XrFF ff) {
   const int m = blockIdx.x * blockDim.x + threadIdx.x;
   if (m >= w.nB) return;
   const double bo_m = BFV(BF_BO, m);
-  if (!(bo_m > THB_CUT)) return;
+  if (!(bo_m > THB_CUT)) {
+    BEV(2, m) = 0.0;
+    BEV(3, m) = 0.0;
+    return;
+  }
   const int L = w.A + 1, T = ff.ntypes;
   const double* g = ff.g;
   const int j = w.bond_i[m], k = w.bond_j[m];
@@ -511,11 +527,12 @@ __global__ void k_torsions(XrWork w, XrFF ff) {
   const double e2 = exp(-g[23] * b2);
   double E_tor = 0, E_con = 0, A_bom = 0, A_pim = 0, A_ds = 0;
   double g_j[3] = {0, 0, 0}, g_k[3] = {0, 0, 0};
-  for (int a = w.cnt[3 * L + j]; a < w.cnt[3 * L + j + 1]; ++a) {
-    const int2 el = w.dbrow[a];
+  const int jb = w.cnt[3 * L + j], kb = w.cnt[3 * L + k];
+  const int jn = w.nact[j], kn = w.nact[k];
+  for (int a = jb; a < jb + jn; ++a) {
+    const int2 el = w.arow[a];
     if (el.x == m && el.y > 0) continue;  // left == middle
     const double bo_l = BFV(BF_BO, el.x);
-    if (!(bo_l > THB_CUT)) continue;
     const int i = bond_other(w, el.x, el.y);
     const int ti = w.type[i];
     const uint32_t sl = bond_shift(w, el.x, el.y);
@@ -525,11 +542,10 @@ __global__ void k_torsions(XrWork w, XrFF ff) {
     const double b1 = bo_l - THB_CUT;
     const double e1 = exp(-g[23] * b1);
     double A_bol = 0, g_i[3] = {0, 0, 0};
-    for (int c = w.cnt[3 * L + k]; c < w.cnt[3 * L + k + 1]; ++c) {
-      const int2 er = w.dbrow[c];
+    for (int c = kb; c < kb + kn; ++c) {
+      const int2 er = w.arow[c];
       if (er.x == m && er.y < 0) continue;  // right == reverse(middle)
       const double bo_r = BFV(BF_BO, er.x);
-      if (!(bo_r > THB_CUT)) continue;
       const int l = bond_other(w, er.x, er.y);
       const int row = __ldg(ff.torsion_index + ((ti * T + tj) * T + tk) * T + w.type[l]);
       if (row < 0) continue;
@@ -637,7 +653,7 @@ __global__ void k_hbonds(XrWork w, XrFF ff) {
   const double4_32a xh = w.x[h];
   double E = 0;
   double gh[3] = {0, 0, 0};
-  const int dbeg = w.cnt[3 * L + h], dend = w.cnt[3 * L + h + 1];
+  const int dbeg = w.cnt[3 * L + h], dend = dbeg + w.nact[h];
   for (int e = w.cnt[0 * L + h] + lane; e < w.cnt[0 * L + h + 1]; e += 32) {
     const int2 ed = w.edge[e];
     const uint32_t code = (uint32_t)ed.y;
@@ -659,7 +675,7 @@ __global__ void k_hbonds(XrWork w, XrFF ff) {
     const double ra = sqrt(va[0] * va[0] + va[1] * va[1] + va[2] * va[2]);
     double ga[3] = {0, 0, 0};
     for (int k = dbeg; k < dend; ++k) {
-      const int2 en = w.dbrow[k];
+      const int2 en = w.arow[k];
       const int jd = bond_other(w, en.x, en.y);
       const int td = w.type[jd];
       if ((int)atom_prm(ff, td, A_P_HBOND) != 2) continue;
@@ -824,7 +840,7 @@ void xr_launch_bonded(const XrWork& w, const XrFF& ff, cudaStream_t st) {
   k_atom1<<<gA, tb, 0, st>>>(w, ff);
   k_atom2<<<gA, tb, 0, st>>>(w, ff);
   if (w.nB > 0) k_bond_energy<<<gB, tb, 0, st>>>(w, ff);
-  k_angles<<<gA, tb, 0, st>>>(w, ff);
+  k_angles<<<(w.A + 3) / 4, 128, 0, st>>>(w, ff);
   if (w.nB > 0) k_torsions<<<gB, tb, 0, st>>>(w, ff);
   k_hbonds<<<(w.A + 3) / 4, 128, 0, st>>>(w, ff);
   k_chain_atom<<<gA, tb, 0, st>>>(w, ff);

@@ -152,6 +152,8 @@ struct XrWork {
   double* b_adj;              // [BJ_N][B] adjoint accumulators
   double* b_e;                // [4][B] energies: bond, lone-pair C2, torsion, conjugation
   int2* dbrow;                // [D] {bond id, +1 if the atom is the bond's source else -1}
+  int2* arow;                 // [D] active bond-row entries (bo > 0.001) at the start of each atom's range
+  int* nact;                  // [A] number of active entries per atom
   // per-atom forward intermediates [AF_N][A] and adjoints [AJ_N][A] (structure of arrays)
   double* a_fwd;
   double* a_adj;
@@ -165,6 +167,12 @@ struct XrWork {
   // outputs
   double* energy;             // [S][16]: 14 components, total, pad
   double* props;              // [S][4]: dipole xyz, pad
+  // deterministic per-system reductions: per-atom energy sums, then fixed atom chunks per system
+  double* esum;               // [XR_ESUM_N][A]
+  const int4* chunks;         // [nchunks] {system, first atom, end atom, 0}
+  const int2* sys_chunks;     // [S] {first chunk, end chunk}
+  double* chunk_part;         // [nchunks][XR_PART_N]
+  int nchunks;
 };
 
 // Per-atom forward slots in a_fwd.
@@ -183,6 +191,9 @@ enum BF { BF_BO0 = 0, BF_PI0, BF_PP0, BF_DSIG, BF_DPI, BF_DPP, BF_BO, BF_PI, BF_
 enum BJ { BJ_BO = 0, BJ_PI, BJ_PP, BJ_SIG, BJ_BO0, BJ_PI0, BJ_PP0, BJ_CI, BJ_CJ, BJ_N };
 
 #define XR_QW_N 12
+#define XR_ESUM_N 14
+#define XR_PART_N 24
+#define XR_CHUNK_ATOMS 1024
 
 // Kernel launchers (defined in the .cu files, called by the engine).
 void xr_launch_topology(const XrWork& w, cudaStream_t st);

@@ -71,6 +71,7 @@ struct xr_ctx {
   int coop_per_sm = 0;
   long long launches = 0;
   long long h2d_bytes = 0, d2h_bytes = 0;  // host<->device bytes moved by the last evaluation
+  int qeq_iterations = 0;                   // CG iterations of the last evaluation (largest system)
   // last batch layout (host copies for export)
   std::vector<XrSystem> host_sys;
   std::vector<int> host_cnt;  // [4][A+1] scans of the last evaluation
@@ -105,6 +106,18 @@ struct xr_ctx {
   size_t cqwork = 0;
   double* outbuf = nullptr;
   size_t coutbuf = 0;
+  double* esum = nullptr;
+  size_t cesum = 0;
+  int2* arow = nullptr;
+  size_t carow = 0;
+  int* nact = nullptr;
+  size_t cnact = 0;
+  int4* chunks = nullptr;
+  size_t cchunks = 0;
+  int2* sys_chunks = nullptr;
+  size_t csys_chunks = 0;
+  double* chunk_part = nullptr;
+  size_t cchunk_part = 0;
   // edge / pair / bond buffers
   int2* edge = nullptr;
   size_t cedge = 0;
@@ -282,6 +295,9 @@ bool ensure_atoms(xr_ctx* c, int A, int S) {
   GROW(f, 3 * (size_t)A);
   GROW(qwork, (size_t)XR_QW_N * A);
   GROW(outbuf, 8 * (size_t)A);
+  GROW(esum, (size_t)XR_ESUM_N * A);
+  GROW(nact, A);
+  GROW(sys_chunks, S);
   GROW(sys, S);
   GROW(energy, 16 * (size_t)S);
   GROW(props, 4 * (size_t)S);
@@ -318,6 +334,8 @@ bool ensure_lists(xr_ctx* c, long long E, long long P, long long B) {
     cudaFree(c->b_adj);
     cudaFree(c->b_e);
     cudaFree(c->dbrow);
+    cudaFree(c->arow);
+    c->arow = nullptr;
     c->bond_pair = c->bond_i = c->bond_j = nullptr;
     c->b_r = c->b_v = c->b_fwd = c->b_adj = c->b_e = nullptr;
     c->dbrow = nullptr;
@@ -329,7 +347,8 @@ bool ensure_lists(xr_ctx* c, long long E, long long P, long long B) {
               cudaMalloc((void**)&c->b_fwd, (size_t)BF_N * nb * sizeof(double)) == cudaSuccess &&
               cudaMalloc((void**)&c->b_adj, (size_t)BJ_N * nb * sizeof(double)) == cudaSuccess &&
               cudaMalloc((void**)&c->b_e, 4 * nb * sizeof(double)) == cudaSuccess &&
-              cudaMalloc((void**)&c->dbrow, 2 * nb * sizeof(int2)) == cudaSuccess;
+              cudaMalloc((void**)&c->dbrow, 2 * nb * sizeof(int2)) == cudaSuccess &&
+              cudaMalloc((void**)&c->arow, 2 * nb * sizeof(int2)) == cudaSuccess;
     if (!ok) return false;
     c->capB = nb;
   }
@@ -363,6 +382,11 @@ void fill_work(xr_ctx* c, XrWork& w, int A, int S, unsigned flags) {
   w.barrier = c->barrier;
   w.energy = c->energy;
   w.props = c->props;
+  w.esum = c->esum;
+  w.nact = c->nact;
+  w.chunks = c->chunks;
+  w.sys_chunks = c->sys_chunks;
+  w.chunk_part = c->chunk_part;
 }
 
 void attach_lists(xr_ctx* c, XrWork& w) {
@@ -391,6 +415,7 @@ void attach_lists(xr_ctx* c, XrWork& w) {
   w.b_adj = c->b_adj;
   w.b_e = c->b_e;
   w.dbrow = c->dbrow;
+  w.arow = c->arow;
 }
 
 // Packs forces (-dE/dx), charges, total bond orders, lone pairs and bond counts per atom.
@@ -541,6 +566,18 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
     }
     off += in.natoms;
   }
+  std::vector<int4> chunk_tab;
+  std::vector<int2> sys_chunk_tab(nsys);
+  for (int s = 0, a = 0; s < nsys; ++s) {
+    sys_chunk_tab[s].x = (int)chunk_tab.size();
+    for (int b = 0; b < sys[s].natoms; b += XR_CHUNK_ATOMS)
+      chunk_tab.push_back(make_int4(s, a + b, a + std::min(sys[s].natoms, b + XR_CHUNK_ATOMS), 0));
+    sys_chunk_tab[s].y = (int)chunk_tab.size();
+    a += sys[s].natoms;
+  }
+  if (!grow(&c->chunks, &c->cchunks, chunk_tab.size()) ||
+      !grow(&c->chunk_part, &c->cchunk_part, chunk_tab.size() * (size_t)XR_PART_N))
+    return cuda_fail(c, cudaErrorMemoryAllocation, "allocation");
   cudaStream_t st = c->stream;
   long long launches = 0;
   long long h2d = 0, d2h = 0;
@@ -555,11 +592,16 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
   cudaMemcpyAsync(c->type, types.data(), sizeof(int) * A, cudaMemcpyHostToDevice, st);
   cudaMemcpyAsync(c->sys_of, sys_of.data(), sizeof(int) * A, cudaMemcpyHostToDevice, st);
   cudaMemcpyAsync(c->sys, c->host_sys.data(), sizeof(XrSystem) * nsys, cudaMemcpyHostToDevice, st);
-  h2d += 2 * sizeof(int) * (long long)A + sizeof(XrSystem) * (long long)nsys;
+  cudaMemcpyAsync(c->chunks, chunk_tab.data(), sizeof(int4) * chunk_tab.size(), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(c->sys_chunks, sys_chunk_tab.data(), sizeof(int2) * nsys, cudaMemcpyHostToDevice, st);
+  h2d += 2 * sizeof(int) * (long long)A + sizeof(XrSystem) * (long long)nsys +
+         (long long)(sizeof(int4) * chunk_tab.size() + sizeof(int2) * nsys);
   cudaMemsetAsync(c->status, 0, sizeof(int), st);
+  cudaMemsetAsync(c->counts, 0, 8 * sizeof(int), st);
   cudaMemsetAsync(c->cnt, 0, sizeof(int) * 4 * (size_t)(A + 1), st);
   XrWork w;
   fill_work(c, w, A, nsys, flags);
+  w.nchunks = (int)chunk_tab.size();
   attach_lists(c, w);
   stage(c, 0, st);
   xr_launch_topology(w, st);
@@ -591,7 +633,7 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
   stage(c, 3, st);
   int coop = 0;
   if (nsys == 1) {
-    const int rows_blocks = (A + 7) / 8;
+    const int rows_blocks = (A + 31) / 32;  // 32 warps (rows) per 1024-thread block
     coop = std::min(c->nsm * std::max(c->coop_per_sm, 1), rows_blocks);
     coop = std::min(coop, 2048);
     if (coop < 2) coop = 0;
@@ -608,7 +650,7 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
   xr_launch_forces(w, ff->d, st);
   launches += 1;
   xr_launch_reduce(w, ff->d, st);
-  launches += 1;
+  launches += 3;
   if (!grow(&c->bx_meta, &c->cbx_meta, (size_t)std::max(nB, 1)) || !grow(&c->bx_bo, &c->cbx_bo, (size_t)std::max(nB, 1)))
     return cuda_fail(c, cudaErrorMemoryAllocation, "bond export");
   cudaMemsetAsync(c->bx_count, 0, sizeof(int), st);
@@ -617,7 +659,8 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
     ++launches;
   }
   cudaMemcpyAsync(c->h_small + 5, c->bx_count, sizeof(int), cudaMemcpyDeviceToHost, st);
-  d2h += 2 * sizeof(int);
+  cudaMemcpyAsync(c->h_small + 6, c->counts + 4, sizeof(int), cudaMemcpyDeviceToHost, st);
+  d2h += 3 * sizeof(int);
   if (dev_io) {
     const xr_result& r = out[0];
     k_unpack_device<<<(A + 255) / 256, 256, 0, st>>>(w, r.forces, r.charges, r.total_bond_orders, r.lone_pairs,
@@ -667,6 +710,7 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
   }
   if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(c, e, "kernel launch");
   c->launches = launches;
+  c->qeq_iterations = c->h_small[6];
   c->h2d_bytes = h2d;
   c->d2h_bytes = d2h;
   c->last_A = A;
@@ -803,7 +847,7 @@ int xr_ctx_create(int device, void* stream, xr_ctx** out) {
   cudaDeviceGetAttribute(&coop_ok, cudaDevAttrCooperativeLaunch, device);
   if (!coop_ok) c->coop_per_sm = 0;
   bool ok = cudaMalloc((void**)&c->status, sizeof(int)) == cudaSuccess &&
-            cudaMalloc((void**)&c->counts, 4 * sizeof(int)) == cudaSuccess &&
+            cudaMalloc((void**)&c->counts, 8 * sizeof(int)) == cudaSuccess &&
             cudaMalloc((void**)&c->barrier, 2 * sizeof(unsigned)) == cudaSuccess &&
             cudaMalloc((void**)&c->bx_count, sizeof(int)) == cudaSuccess &&
             cudaMallocHost((void**)&c->h_small, 16 * sizeof(int)) == cudaSuccess;
@@ -823,7 +867,8 @@ void xr_ctx_destroy(xr_ctx* c) {
                   c->qwork, c->outbuf, c->edge, c->edge_pair, c->edge_dbslot, c->hval, c->pair_edge, c->pair_i,
                   c->pair_bond, c->p_r, c->p_shield, c->p_dshield, c->p_g, c->p_evdw, c->p_ecoul, c->bond_pair,
                   c->bond_i, c->bond_j, c->b_r, c->b_v, c->b_fwd, c->b_adj, c->b_e, c->dbrow, c->sys, c->energy,
-                  c->props, c->status, c->counts, c->barrier, c->red, c->bx_meta, c->bx_bo, c->bx_count};
+                  c->props, c->status, c->counts, c->barrier, c->red, c->bx_meta, c->bx_bo, c->bx_count,
+                  c->esum, c->arow, c->nact, c->chunks, c->sys_chunks, c->chunk_part};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (c->h_x) cudaFreeHost(c->h_x);
@@ -853,6 +898,8 @@ int xr_eval_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, un
 }
 
 long long xr_last_launches(const xr_ctx* c) { return c ? c->launches : 0; }
+
+int xr_last_qeq_iterations(const xr_ctx* c) { return c ? c->qeq_iterations : 0; }
 
 int xr_last_transfer_bytes(const xr_ctx* c, long long* h2d, long long* d2h) {
   if (!c) return XR_EINPUT;

@@ -96,13 +96,18 @@ enum { Q_S = 0, Q_T, Q_RS, Q_RT, Q_PS, Q_PT, Q_APS, Q_APT, Q_MINV, Q_ZS, Q_ZT };
 
 // Bounded grid barrier for a cooperative launch (all blocks co-resident). Returns false when the
 // wait ran out; the caller then leaves the solver and the host reports the status bit.
+__device__ inline unsigned ld_acquire(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
 __device__ bool grid_barrier(unsigned* bar, unsigned nblocks, int* status) {
   __syncthreads();
   __shared__ int ok;
   if (threadIdx.x == 0) {
     ok = 1;
-    volatile unsigned* gen = bar + 1;
-    const unsigned g0 = *gen;
+    const unsigned g0 = ld_acquire(bar + 1);
     __threadfence();
     const unsigned arrived = atomicAdd(bar, 1u);
     if (arrived == nblocks - 1) {
@@ -111,13 +116,13 @@ __device__ bool grid_barrier(unsigned* bar, unsigned nblocks, int* status) {
       atomicAdd(bar + 1, 1u);
     } else {
       long long it = 0;
-      while (*gen == g0) {
-        if (++it > (1ll << 22) || (*(volatile int*)status & XR_S_BARRIER)) {
+      while (ld_acquire(bar + 1) == g0) {
+        if (++it > (1ll << 24) || (*(volatile int*)status & XR_S_BARRIER)) {
           atomicOr(status, XR_S_BARRIER);
           ok = 0;
           break;
         }
-        __nanosleep(64);
+        if (it > 64) __nanosleep(32);
       }
     }
     __threadfence();
@@ -134,8 +139,8 @@ __device__ inline void row_matvec(const XrWork& w, const XrFF& ff, int a, int la
   for (int e = w.cnt[a] + lane; e < w.cnt[a + 1]; e += 32) {
     const int j = w.edge[e].x;
     const double h = w.hval[e];
-    ss += h * xs[j];
-    st += h * xt[j];
+    ss += h * __ldcg(xs + j);
+    st += h * __ldcg(xt + j);
   }
   (void)L;
 #pragma unroll
@@ -145,8 +150,8 @@ __device__ inline void row_matvec(const XrWork& w, const XrFF& ff, int a, int la
   }
   if (lane == 0) {
     const double eta = atom_prm(ff, w.type[a], A_ETA);
-    *ys = eta * xs[a] + ss;
-    *yt = eta * xt[a] + st;
+    *ys = eta * __ldcg(xs + a) + ss;
+    *yt = eta * __ldcg(xt + a) + st;
   }
 }
 
@@ -186,11 +191,18 @@ struct GridTeam {
     if (threadIdx.x == 0)
       for (int k = 0; k < NV; ++k) red[k * gridDim.x + blockIdx.x] = v[k];
     if (!sync(w)) return false;
-    for (int k = 0; k < NV; ++k) {
-      double s = 0;
-      for (unsigned q = 0; q < gridDim.x; ++q) s += ((volatile double*)red)[k * gridDim.x + q];
-      v[k] = s;
+    if (threadIdx.x < 32) {
+      for (int k = 0; k < NV; ++k) {
+        double s = 0;
+        for (unsigned q = threadIdx.x; q < gridDim.x; q += 32) s += __ldcg(red + k * gridDim.x + q);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (threadIdx.x == 0) smem[k] = s;
+      }
     }
+    __syncthreads();
+    for (int k = 0; k < NV; ++k) v[k] = smem[k];
+    __syncthreads();
     return true;
   }
 };
@@ -310,6 +322,7 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
     }
     if (!team.sync(w)) return;
   }
+  if (team.thread() == 0) atomicMax(w.counts + 4, it);
   // q = s + mu t with mu = (Q - sum s) / sum t.
   double sm[2] = {0, 0};
   for (int r = team.thread(); r < n; r += team.nthreads()) {
@@ -327,7 +340,7 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
   }
 }
 
-__global__ void k_qeq_grid(XrWork w, XrFF ff) {
+__global__ void __launch_bounds__(1024, 1) k_qeq_grid(XrWork w, XrFF ff) {
   __shared__ double smem[4 * 32];
   const XrSystem& S = w.sys[0];
   GridTeam team{gridDim.x};
@@ -374,83 +387,122 @@ __global__ void k_pair_forces(XrWork w) {
 }
 
 // ------------------------------------------------------------------------ reductions
-// One block per system sums every energy array over the system's contiguous atom, bond and pair
-// ranges in a fixed order (deterministic), computes the dipole about the mass centre, and checks
-// that energies, charges and forces are finite.
-__global__ void k_reduce(XrWork w, XrFF ff) {
-  __shared__ double smem[16 * 32];
-  const int s = blockIdx.x;
-  const XrSystem& S = w.sys[s];
+// Energies land per item (pair, bond, atom). A warp per atom first folds its own pairs and half
+// bonds into per-atom component sums; fixed chunks of at most XR_CHUNK_ATOMS atoms of one system
+// are then summed by one block each, and one block per system adds its chunks in order. Every sum
+// has a fixed order, so energies, charges and dipoles are bitwise reproducible.
+#define ESUM(k, a) w.esum[(size_t)(k) * w.A + (a)]
+
+__global__ void k_energy_gather(XrWork w) {
+  const int lane = threadIdx.x & 31;
+  const int a = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
+  if (a >= w.A) return;
   const int L = w.A + 1;
-  const int a0 = S.atom_off, a1 = S.atom_off + S.natoms;
-  const int p0 = w.cnt[1 * L + a0], p1 = w.cnt[1 * L + a1];
-  const int b0 = w.cnt[2 * L + a0], b1 = w.cnt[2 * L + a1];
-  double v[16];
-  for (int k = 0; k < 16; ++k) v[k] = 0;
-  bool finite = true;
-  for (int a = a0 + threadIdx.x; a < a1; a += blockDim.x) {
-    v[C_LONE_PAIR] += AEV(0, a);
-    v[C_ATOM] += AEV(1, a);
-    v[C_ANGLE] += AEV(2, a);
-    v[C_PENALTY] += AEV(3, a);
-    v[C_ANGLE_CONJ] += AEV(4, a);
-    v[C_HBOND] += AEV(5, a);
-    v[C_QEQ] += AEV(6, a);
+  double ev = 0, ec = 0, eb = 0, ec2 = 0, et = 0, eco = 0;
+  for (int p = w.cnt[1 * L + a] + lane; p < w.cnt[1 * L + a + 1]; p += 32) {
+    ev += w.p_evdw[p];
+    ec += w.p_ecoul[p];
+  }
+  for (int b = w.cnt[2 * L + a] + lane; b < w.cnt[2 * L + a + 1]; b += 32) {
+    eb += w.b_e[0 * w.cap_B + b];
+    ec2 += w.b_e[1 * w.cap_B + b];
+    et += w.b_e[2 * w.cap_B + b];
+    eco += w.b_e[3 * w.cap_B + b];
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    ev += __shfl_xor_sync(0xffffffffu, ev, o);
+    ec += __shfl_xor_sync(0xffffffffu, ec, o);
+    eb += __shfl_xor_sync(0xffffffffu, eb, o);
+    ec2 += __shfl_xor_sync(0xffffffffu, ec2, o);
+    et += __shfl_xor_sync(0xffffffffu, et, o);
+    eco += __shfl_xor_sync(0xffffffffu, eco, o);
+  }
+  if (lane == 0) {
+    ESUM(C_BOND, a) = eb;
+    ESUM(C_ATOM, a) = AEV(1, a);
+    ESUM(C_LONE_PAIR, a) = AEV(0, a) + ec2;
+    ESUM(C_MOLECULE, a) = 0.0;
+    ESUM(C_ANGLE, a) = AEV(2, a);
+    ESUM(C_PENALTY, a) = AEV(3, a);
+    ESUM(C_ANGLE_CONJ, a) = AEV(4, a);
+    ESUM(C_HBOND, a) = AEV(5, a);
+    ESUM(C_TORSION, a) = et;
+    ESUM(C_CONJ, a) = eco;
+    ESUM(C_VDW, a) = ev;
+    ESUM(C_COULOMB, a) = ec;
+    ESUM(C_EFIELD, a) = 0.0;
+    ESUM(C_QEQ, a) = AEV(6, a);
+  }
+}
+
+// Partial slots: 0..13 components, 14 mass, 15..17 mass * x, 18 charge, 19..21 charge * x, 22 finite.
+__global__ void k_reduce_chunk(XrWork w, XrFF ff) {
+  __shared__ double smem[XR_PART_N * 32];
+  const int4 ch = w.chunks[blockIdx.x];
+  double v[XR_PART_N];
+  for (int k = 0; k < XR_PART_N; ++k) v[k] = 0.0;
+  double finite = 1.0;
+  for (int a = ch.y + threadIdx.x; a < ch.z; a += blockDim.x) {
+    for (int k = 0; k < XR_NCOMP; ++k) v[k] += ESUM(k, a);
     const double m = atom_prm(ff, w.type[a], A_MASS);
-    const double4_32a x = w.x[a];
-    v[14] += m;
-    v[C_MOLECULE] += 0.0;
-    finite = finite && isfinite(w.q[a]) && isfinite(w.f[3 * a]) && isfinite(w.f[3 * a + 1]) && isfinite(w.f[3 * a + 2]);
-    (void)x;
-  }
-  for (int b = b0 + threadIdx.x; b < b1; b += blockDim.x) {
-    v[C_BOND] += w.b_e[0 * w.cap_B + b];
-    v[C_LONE_PAIR] += w.b_e[1 * w.cap_B + b];
-    v[C_TORSION] += w.b_e[2 * w.cap_B + b];
-    v[C_CONJ] += w.b_e[3 * w.cap_B + b];
-  }
-  for (int p = p0 + threadIdx.x; p < p1; p += blockDim.x) {
-    v[C_VDW] += w.p_evdw[p];
-    v[C_COULOMB] += w.p_ecoul[p];
-  }
-  block_sum<15>(v, smem);
-  // Dipole about the force-field mass centre (src/xreac/energy.py:171-177).
-  double c[3] = {0, 0, 0};
-  for (int a = a0 + threadIdx.x; a < a1; a += blockDim.x) {
-    const double m = atom_prm(ff, w.type[a], A_MASS);
-    const double4_32a x = w.x[a];
-    c[0] += m * x.x;
-    c[1] += m * x.y;
-    c[2] += m * x.z;
-  }
-  block_sum<3>(c, smem);
-  const double mt = v[14];
-  double dp[3] = {0, 0, 0};
-  for (int a = a0 + threadIdx.x; a < a1; a += blockDim.x) {
     const double4_32a x = w.x[a];
     const double q = w.q[a];
-    dp[0] += (x.x - c[0] / mt) * q;
-    dp[1] += (x.y - c[1] / mt) * q;
-    dp[2] += (x.z - c[2] / mt) * q;
+    v[14] += m;
+    v[15] += m * x.x;
+    v[16] += m * x.y;
+    v[17] += m * x.z;
+    v[18] += q;
+    v[19] += q * x.x;
+    v[20] += q * x.y;
+    v[21] += q * x.z;
+    if (!(isfinite(q) && isfinite(w.f[3 * a]) && isfinite(w.f[3 * a + 1]) && isfinite(w.f[3 * a + 2]))) finite = 0.0;
   }
-  block_sum<3>(dp, smem);
-  __shared__ int fin;
-  if (threadIdx.x == 0) fin = 1;
+  v[22] = finite;
+  // block sum (finite combines by min)
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int k = 0; k < XR_PART_N; ++k)
+    for (int o = 16; o > 0; o >>= 1) {
+      const double y = __shfl_xor_sync(0xffffffffu, v[k], o);
+      v[k] = (k == 22) ? fmin(v[k], y) : v[k] + y;
+    }
+  if (lane == 0)
+    for (int k = 0; k < XR_PART_N; ++k) smem[k * 32 + wid] = v[k];
   __syncthreads();
-  if (!finite) fin = 0;
+  if (threadIdx.x < XR_PART_N) {
+    const int k = threadIdx.x;
+    double s = k == 22 ? 1.0 : 0.0;
+    for (int q = 0; q < nw; ++q) s = (k == 22) ? fmin(s, smem[k * 32 + q]) : s + smem[k * 32 + q];
+    w.chunk_part[(size_t)blockIdx.x * XR_PART_N + k] = s;
+  }
+}
+
+__global__ void k_reduce_final(XrWork w) {
+  const int s = blockIdx.x;
+  const int2 r = w.sys_chunks[s];
+  const int k = threadIdx.x;
+  __shared__ double tot[XR_PART_N];
+  if (k < XR_PART_N) {
+    double acc = k == 22 ? 1.0 : 0.0;
+    for (int c = r.x; c < r.y; ++c) {
+      const double v = w.chunk_part[(size_t)c * XR_PART_N + k];
+      acc = (k == 22) ? fmin(acc, v) : acc + v;
+    }
+    tot[k] = acc;
+  }
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (k == 0) {
     double total = 0;
-    for (int k = 0; k < XR_NCOMP; ++k) {
-      w.energy[16 * s + k] = v[k];
-      total += v[k];
-      if (!isfinite(v[k])) fin = 0;
+    bool fin = tot[22] > 0.5;
+    for (int c = 0; c < XR_NCOMP; ++c) {
+      w.energy[16 * s + c] = tot[c];
+      total += tot[c];
+      if (!isfinite(tot[c])) fin = false;
     }
     w.energy[16 * s + 14] = total;
     w.energy[16 * s + 15] = 0.0;
-    w.props[4 * s + 0] = dp[0];
-    w.props[4 * s + 1] = dp[1];
-    w.props[4 * s + 2] = dp[2];
+    // dipole about the mass centre: sum q (x - c) = sum q x - c sum q (src/xreac/energy.py:171-177)
+    for (int d = 0; d < 3; ++d) w.props[4 * s + d] = tot[19 + d] - tot[15 + d] / tot[14] * tot[18];
     w.props[4 * s + 3] = 0.0;
     if (!fin) atomicOr(w.status, XR_S_NONFINITE);
   }
@@ -465,21 +517,18 @@ void xr_launch_pairs(const XrWork& w, const XrFF& ff, cudaStream_t st) {
 
 int xr_qeq_coop_blocks_per_sm() {
   int nb = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_qeq_grid, 256, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_qeq_grid, 1024, 0);
   return nb;
 }
 
 // Returns 0 on success or a CUDA error code from the launch.
 int xr_launch_qeq(const XrWork& w, const XrFF& ff, cudaStream_t st, int coop_blocks) {
   if (w.S == 1 && coop_blocks > 1) {
-    const XrSystem* unused = nullptr;
-    (void)unused;
-    int blocks = coop_blocks;
-    // No more blocks than the rows need (8 warps per block).
-    // The host passes coop_blocks already clamped to the co-resident maximum.
+    // coop_blocks is already clamped by the host to the co-resident maximum and to the rows.
+    const int blocks = coop_blocks;
     cudaMemsetAsync(w.barrier, 0, 2 * sizeof(unsigned), st);
     void* args[] = {(void*)&w, (void*)&ff};
-    cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_qeq_grid, dim3(blocks), dim3(256), args, 0, st);
+    cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_qeq_grid, dim3(blocks), dim3(1024), args, 0, st);
     return (int)e;
   }
   k_qeq_block<<<w.S, 256, 0, st>>>(w, ff);
@@ -496,4 +545,8 @@ void xr_launch_forces(const XrWork& w, const XrFF& ff, cudaStream_t st) {
   if (w.nP > 0) k_pair_forces<<<(w.nP + 255) / 256, 256, 0, st>>>(w);
 }
 
-void xr_launch_reduce(const XrWork& w, const XrFF& ff, cudaStream_t st) { k_reduce<<<w.S, 256, 0, st>>>(w, ff); }
+void xr_launch_reduce(const XrWork& w, const XrFF& ff, cudaStream_t st) {
+  k_energy_gather<<<(w.A + 7) / 8, 256, 0, st>>>(w);
+  k_reduce_chunk<<<w.nchunks, 256, 0, st>>>(w, ff);
+  k_reduce_final<<<w.S, 32, 0, st>>>(w);
+}
