@@ -276,6 +276,7 @@ def main():
     stage_names = ["neighbour_count_scan", "neighbour_fill_reverse", "pairs_vdw_shield", "qeq_cg", "coulomb",
                    "bonded_and_adjoint", "forces_reduce_pack"]
     stages = {nm: stage_ms[k] / max(calls.value, 1) for k, nm in enumerate(stage_names)}
+    qeq_iterations = int(lib.xr_last_qeq_iterations(ctx.handle))
 
     # e2e: the public API with host arrays, every step copying inputs in and results out
     h2d = ctypes.c_longlong()
@@ -331,7 +332,7 @@ def main():
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic (seeded water box)",
-        "config": {"workload": WORKLOAD, "atoms": n, "directed_edges": 2 * m_half,
+        "config": {"workload": WORKLOAD, "atoms": n, "directed_edges": 2 * m_half, "qeq_cg_iterations": qeq_iterations,
                    "parallelism": "replicas" if world > 1 else "single",
                    "l2": "flushed before every step (256 MiB write, outside the timed events)"},
         "roofline": roofline,

@@ -94,8 +94,12 @@ class Calculator:
         self._ctx = nat.Context(device)
         self._lib = nat.load()
 
-    def set_qeq(self, tolerance=1e-13, max_iterations=2000):
-        """QEq conjugate-gradient relative residual and iteration limit."""
+    def set_qeq(self, tolerance=1e-11, max_iterations=2000):
+        """QEq solver tolerance and iteration limit.
+
+        ``tolerance`` bounds the preconditioned projected residual relative to its starting value;
+        the default 1e-11 keeps charges within about 5e-11 e of the exact KKT solution.
+        """
         if self._lib.xr_ctx_set_qeq(self._ctx.handle, float(tolerance), int(max_iterations)) != nat.XR_OK:
             raise ValueError("QEq tolerance must be positive and the iteration limit at least 1")
 

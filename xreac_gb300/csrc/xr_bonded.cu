@@ -496,69 +496,74 @@ __device__ inline void cross3(const double a[3], const double b[3], double c[3])
   c[2] = a[0] * b[1] - a[1] * b[0];
 }
 
-// Torsion and four-body conjugation, one thread per middle bond j -> k (the half direction)
-// (src/xreac/energy.py:320-370).
-__global__ void k_torsions(XrWork w, XrFF ff) {
-  const int m = blockIdx.x * blockDim.x + threadIdx.x;
-  if (m >= w.nB) return;
-  const double bo_m = BFV(BF_BO, m);
-  if (!(bo_m > THB_CUT)) {
-    BEV(2, m) = 0.0;
-    BEV(3, m) = 0.0;
-    return;
+// Bonds with bo > 0.001 (the middles of torsion chains), compacted with warp-aggregated atomics.
+__global__ void k_torsion_middles(XrWork w) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const bool keep = b < w.nB && BFV(BF_BO, b) > THB_CUT;
+  if (b < w.nB && !keep) {
+    BEV(2, b) = 0.0;
+    BEV(3, b) = 0.0;
   }
+  const unsigned msk = __ballot_sync(0xffffffffu, keep);
+  int base = 0;
+  if (lane == 0 && msk) base = atomicAdd(w.nmids, __popc(msk));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (keep) w.mids[base + __popc(msk & ((1u << lane) - 1u))] = b;
+}
+
+// Torsion and four-body conjugation, one warp per middle bond j -> k (the half direction); the lanes
+// take the (left, right) combinations of the two ends' active bond rows (src/xreac/energy.py:320-370).
+__global__ void k_torsions(XrWork w, XrFF ff) {
+  const int lane = threadIdx.x & 31;
+  const int warp = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
+  const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
   const int L = w.A + 1, T = ff.ntypes;
   const double* g = ff.g;
-  const int j = w.bond_i[m], k = w.bond_j[m];
-  const int tj = w.type[j], tk = w.type[k];
-  const uint32_t sm = (uint32_t)w.edge[w.pair_edge[w.bond_pair[m]]].y & XR_SHIFT_MASK;
-  double v[3];
-  bond_vec(w, m, 1, v);
-  const double rm = w.b_r[m];
-  const double pi_m = BFV(BF_PI, m);
-  const double db_j = AFV(AF_TOTAL, j) - atom_prm(ff, tj, A_VALENCY_BOC);
-  const double db_k = AFV(AF_TOTAL, k) - atom_prm(ff, tk, A_VALENCY_BOC);
-  const double ds = db_j + db_k;
-  const double ex3 = exp(-g[24] * ds), ex4 = exp(g[25] * ds);
-  const double den = 1 + ex3 + ex4;
-  const double f11 = (2 + ex3) / den;
-  const double df11_dds = (-g[24] * ex3 * den - (2 + ex3) * (-g[24] * ex3 + g[25] * ex4)) / (den * den);
-  const double b2 = bo_m - THB_CUT;
-  const double e2 = exp(-g[23] * b2);
-  double E_tor = 0, E_con = 0, A_bom = 0, A_pim = 0, A_ds = 0;
-  double g_j[3] = {0, 0, 0}, g_k[3] = {0, 0, 0};
-  const int jb = w.cnt[3 * L + j], kb = w.cnt[3 * L + k];
-  const int jn = w.nact[j], kn = w.nact[k];
-  for (int a = jb; a < jb + jn; ++a) {
-    const int2 el = w.arow[a];
-    if (el.x == m && el.y > 0) continue;  // left == middle
-    const double bo_l = BFV(BF_BO, el.x);
-    const int i = bond_other(w, el.x, el.y);
-    const int ti = w.type[i];
-    const uint32_t sl = bond_shift(w, el.x, el.y);
-    double u[3];
-    bond_vec(w, el.x, el.y, u);
-    const double rl = w.b_r[el.x];
-    const double b1 = bo_l - THB_CUT;
-    const double e1 = exp(-g[23] * b1);
-    double A_bol = 0, g_i[3] = {0, 0, 0};
-    for (int c = kb; c < kb + kn; ++c) {
-      const int2 er = w.arow[c];
+  const int nm = *w.nmids;
+  for (int q = warp; q < nm; q += nwarps) {
+    const int m = w.mids[q];
+    const double bo_m = BFV(BF_BO, m);
+    const int j = w.bond_i[m], k = w.bond_j[m];
+    const int tj = w.type[j], tk = w.type[k];
+    const uint32_t sm = (uint32_t)w.edge[w.pair_edge[w.bond_pair[m]]].y & XR_SHIFT_MASK;
+    double v[3];
+    bond_vec(w, m, 1, v);
+    const double rm = w.b_r[m];
+    const double pi_m = BFV(BF_PI, m);
+    const double db_j = AFV(AF_TOTAL, j) - atom_prm(ff, tj, A_VALENCY_BOC);
+    const double db_k = AFV(AF_TOTAL, k) - atom_prm(ff, tk, A_VALENCY_BOC);
+    const double ds = db_j + db_k;
+    const double ex3 = exp(-g[24] * ds), ex4 = exp(g[25] * ds);
+    const double den = 1 + ex3 + ex4;
+    const double f11 = (2 + ex3) / den;
+    const double df11_dds = (-g[24] * ex3 * den - (2 + ex3) * (-g[24] * ex3 + g[25] * ex4)) / (den * den);
+    const double b2 = bo_m - THB_CUT;
+    const double e2 = exp(-g[23] * b2);
+    const int jb = w.cnt[3 * L + j], kb = w.cnt[3 * L + k];
+    const int jn = w.nact[j], kn = w.nact[k];
+    double E_tor = 0, E_con = 0, A_bom = 0, A_pim = 0, A_ds = 0;
+    double g_j[3] = {0, 0, 0}, g_k[3] = {0, 0, 0};
+    for (int t = lane; t < jn * kn; t += 32) {
+      const int2 el = w.arow[jb + t / kn];
+      const int2 er = w.arow[kb + t % kn];
+      if (el.x == m && el.y > 0) continue;  // left == middle
       if (er.x == m && er.y < 0) continue;  // right == reverse(middle)
-      const double bo_r = BFV(BF_BO, er.x);
-      const int l = bond_other(w, er.x, er.y);
-      const int row = __ldg(ff.torsion_index + ((ti * T + tj) * T + tk) * T + w.type[l]);
+      const double bo_l = BFV(BF_BO, el.x), bo_r = BFV(BF_BO, er.x);
+      const int i = bond_other(w, el.x, el.y), l = bond_other(w, er.x, er.y);
+      const int row = __ldg(ff.torsion_index + ((w.type[i] * T + tj) * T + tk) * T + w.type[l]);
       if (row < 0) continue;
       if (bo_l * bo_m * bo_r <= THB_CUT) continue;
       if (i == l) {
-        const uint32_t sr = bond_shift(w, er.x, er.y);
+        const uint32_t sl = bond_shift(w, el.x, el.y), sr = bond_shift(w, er.x, er.y);
         if (xr_sx(sl) == xr_sx(sm) + xr_sx(sr) && xr_sy(sl) == xr_sy(sm) + xr_sy(sr) &&
             xr_sz(sl) == xr_sz(sm) + xr_sz(sr))
           continue;
       }
-      double wv[3];
+      double u[3], wv[3];
+      bond_vec(w, el.x, el.y, u);
       bond_vec(w, er.x, er.y, wv);
-      const double rr = w.b_r[er.x];
+      const double rl = w.b_r[el.x], rr = w.b_r[er.x];
       double n1[3], n2[3];
       cross3(u, v, n1);
       cross3(wv, v, n2);
@@ -577,8 +582,8 @@ __global__ void k_torsions(XrWork w, XrFF ff) {
       const double* prm = ff.torsion + 5 * row;
       const double V1 = __ldg(prm + 0), V2 = __ldg(prm + 1), V3 = __ldg(prm + 2), tor1 = __ldg(prm + 3),
                    cot1 = __ldg(prm + 4);
-      const double b3 = bo_r - THB_CUT;
-      const double e3 = exp(-g[23] * b3);
+      const double b1 = bo_l - THB_CUT, b3 = bo_r - THB_CUT;
+      const double e1 = exp(-g[23] * b1), e3 = exp(-g[23] * b3);
       const double y = 2 - pi_m - f11;
       const double ex1 = exp(tor1 * y * y);
       const double fn10 = (1 - e1) * (1 - e2) * (1 - e3);
@@ -596,11 +601,11 @@ __global__ void k_torsions(XrWork w, XrFF ff) {
       A_pim += -dE_dex1 * dex1_dy;
       A_ds += -dE_dex1 * dex1_dy * df11_dds;
       const double sc = sinprod * cv, cc = cot1 * conj;
-      A_bol += sc * g[23] * e1 * (1 - e2) * (1 - e3) + cc * fn12 * (-2 * g[27] * q1);
+      const double A_bol = sc * g[23] * e1 * (1 - e2) * (1 - e3) + cc * fn12 * (-2 * g[27] * q1);
       A_bom += sc * g[23] * e2 * (1 - e1) * (1 - e3) + cc * fn12 * (-2 * g[27] * q2);
       const double A_bor = sc * g[23] * e3 * (1 - e1) * (1 - e2) + cc * fn12 * (-2 * g[27] * q3);
+      atomicAdd(&BJV(BJ_BO, el.x), A_bol);
       atomicAdd(&BJV(BJ_BO, er.x), A_bor);
-      // geometry: dE/dn1 = a, dE/dn2 = bb
       double av[3], bv[3];
       for (int c3 = 0; c3 < 3; ++c3) {
         av[c3] = dE_dcw * (n2[c3] - (P / A1) * n1[c3]) / sq + dE_dsp * sinprod * n1[c3] / A1;
@@ -615,32 +620,55 @@ __global__ void k_torsions(XrWork w, XrFF ff) {
         gu[c3] += dE_dsp * (-sinprod) * u[c3] / (rl * rl);
         gv[c3] = t1[c3] + t2[c3] + dE_dsp * (-2 * sinprod) * v[c3] / (rm * rm);
         gw[c3] += dE_dsp * (-sinprod) * wv[c3] / (rr * rr);
-        g_i[c3] += gu[c3];
         g_j[c3] += -gu[c3] - gv[c3];
         g_k[c3] += gv[c3] - gw[c3];
       }
+      atomic_add3(w.f, i, gu[0], gu[1], gu[2]);
       atomic_add3(w.f, l, gw[0], gw[1], gw[2]);
     }
-    if (A_bol != 0.0) atomicAdd(&BJV(BJ_BO, el.x), A_bol);
-    if (g_i[0] != 0.0 || g_i[1] != 0.0 || g_i[2] != 0.0) atomic_add3(w.f, i, g_i[0], g_i[1], g_i[2]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      E_tor += __shfl_xor_sync(0xffffffffu, E_tor, o);
+      E_con += __shfl_xor_sync(0xffffffffu, E_con, o);
+      A_bom += __shfl_xor_sync(0xffffffffu, A_bom, o);
+      A_pim += __shfl_xor_sync(0xffffffffu, A_pim, o);
+      A_ds += __shfl_xor_sync(0xffffffffu, A_ds, o);
+      for (int c3 = 0; c3 < 3; ++c3) {
+        g_j[c3] += __shfl_xor_sync(0xffffffffu, g_j[c3], o);
+        g_k[c3] += __shfl_xor_sync(0xffffffffu, g_k[c3], o);
+      }
+    }
+    if (lane == 0) {
+      BEV(2, m) = E_tor;
+      BEV(3, m) = E_con;
+      if (A_bom != 0.0) atomicAdd(&BJV(BJ_BO, m), A_bom);
+      if (A_pim != 0.0) atomicAdd(&BJV(BJ_PI, m), A_pim);
+      if (A_ds != 0.0) {
+        atomicAdd(&AJV(AJ_DB, j), A_ds);
+        atomicAdd(&AJV(AJ_DB, k), A_ds);
+      }
+      if (g_j[0] != 0.0 || g_j[1] != 0.0 || g_j[2] != 0.0) atomic_add3(w.f, j, g_j[0], g_j[1], g_j[2]);
+      if (g_k[0] != 0.0 || g_k[1] != 0.0 || g_k[2] != 0.0) atomic_add3(w.f, k, g_k[0], g_k[1], g_k[2]);
+    }
   }
-  BEV(2, m) = E_tor;
-  BEV(3, m) = E_con;
-  if (A_bom != 0.0) atomicAdd(&BJV(BJ_BO, m), A_bom);
-  if (A_pim != 0.0) atomicAdd(&BJV(BJ_PI, m), A_pim);
-  if (A_ds != 0.0) {
-    atomicAdd(&AJV(AJ_DB, j), A_ds);
-    atomicAdd(&AJV(AJ_DB, k), A_ds);
-  }
-  if (g_j[0] != 0.0 || g_j[1] != 0.0 || g_j[2] != 0.0) atomic_add3(w.f, j, g_j[0], g_j[1], g_j[2]);
-  if (g_k[0] != 0.0 || g_k[1] != 0.0 || g_k[2] != 0.0) atomic_add3(w.f, k, g_k[0], g_k[1], g_k[2]);
 }
 
-// Hydrogen bonds, one warp per hydrogen: lanes take acceptor edges of the hydrogen's full row
-// (heavy neighbour within min(7.5, cutoff)), each paired with every donor bond (heavy neighbour,
-// bo >= 0.01) other than the same edge (src/xreac/energy.py:248-276).
+// Hydrogen bonds, one warp per hydrogen (src/xreac/energy.py:248-276). The hydrogen's donors
+// (active bonds to a heavy atom with bo >= 0.01) are gathered once into a per-warp shared list; the
+// lanes then take acceptor edges of its full row (heavy neighbour within min(7.5, cutoff)) and pair
+// each with every donor except the same edge. Donor sensitivities accumulate in shared memory.
+constexpr int kHbWarps = 4;
+constexpr int kHbDonors = 8;
+struct HbDonor {
+  double v[3];
+  double r, bo, dbo, g[3];
+  int b, jd, td;
+  uint32_t shift;
+};
+
 __global__ void k_hbonds(XrWork w, XrFF ff) {
-  const int lane = threadIdx.x & 31;
+  __shared__ HbDonor don[kHbWarps][kHbDonors];
+  const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
   const int h = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
   if (h >= w.A) return;
   const int th = w.type[h], T = ff.ntypes;
@@ -651,67 +679,101 @@ __global__ void k_hbonds(XrWork w, XrFF ff) {
   const int L = w.A + 1;
   const XrSystem& S = w.sys[w.sys_of[h]];
   const double4_32a xh = w.x[h];
+  const int abeg = w.cnt[3 * L + h], na = w.nact[h];
   double E = 0;
   double gh[3] = {0, 0, 0};
-  const int dbeg = w.cnt[3 * L + h], dend = dbeg + w.nact[h];
-  for (int e = w.cnt[0 * L + h] + lane; e < w.cnt[0 * L + h + 1]; e += 32) {
-    const int2 ed = w.edge[e];
-    const uint32_t code = (uint32_t)ed.y;
-    if (!(code & XR_CODE_HB)) continue;
-    const int ja = ed.x, ta = w.type[ja];
-    if ((int)atom_prm(ff, ta, A_P_HBOND) != 2) continue;
-    const uint32_t sa = code & XR_SHIFT_MASK;
-    double va[3];
-    {
-      const double4_32a xa = w.x[ja];
-      const int sx = xr_sx(sa), sy = xr_sy(sa), sz = xr_sz(sa);
-      const double p0[3] = {xh.x, xh.y, xh.z}, p1[3] = {xa.x, xa.y, xa.z};
-      for (int c = 0; c < 3; ++c) {
-        const double off = __dadd_rn(__dadd_rn(__dmul_rn((double)sx, S.cell[c]), __dmul_rn((double)sy, S.cell[3 + c])),
-                                     __dmul_rn((double)sz, S.cell[6 + c]));
-        va[c] = __dadd_rn(__dsub_rn(p1[c], p0[c]), off);
-      }
-    }
-    const double ra = sqrt(va[0] * va[0] + va[1] * va[1] + va[2] * va[2]);
-    double ga[3] = {0, 0, 0};
-    for (int k = dbeg; k < dend; ++k) {
-      const int2 en = w.arow[k];
+  // Donor batches of up to kHbDonors (normally one batch holds them all).
+  for (int dbase = 0; dbase < na; dbase += 32) {
+    const int t = dbase + lane;
+    bool is_donor = false;
+    int2 en = make_int2(0, 0);
+    if (t < na) {
+      en = w.arow[abeg + t];
       const int jd = bond_other(w, en.x, en.y);
-      const int td = w.type[jd];
-      if ((int)atom_prm(ff, td, A_P_HBOND) != 2) continue;
-      const double bo_d = BFV(BF_BO, en.x);
-      if (!(bo_d >= HBOND_THRESHOLD)) continue;
-      if (jd == ja && bond_shift(w, en.x, en.y) == sa) continue;  // same edge
-      const int row = __ldg(ff.hbond_index + (td * T + th) * T + ta);
-      if (row < 0) continue;
-      const double* prm = ff.hbond + 4 * row;
-      const double r0 = __ldg(prm + 0), hb1 = __ldg(prm + 1), hb2 = __ldg(prm + 2), hb3 = __ldg(prm + 3);
-      if (!(r0 > 0)) continue;
-      double vd[3];
-      bond_vec(w, en.x, en.y, vd);
-      const double rd = w.b_r[en.x];
-      const double cosv = (vd[0] * va[0] + vd[1] * va[1] + vd[2] * va[2]) / (rd * ra);
-      const double cc = fmin(fmax(cosv, -1.0), 1.0);
-      const double sin4 = 0.25 * (1 - cc) * (1 - cc);
-      const double eb = exp(-hb2 * bo_d);
-      const double Fb = hb1 * (1 - eb);
-      const double E2 = exp(-hb3 * (r0 / ra + ra / r0 - 2));
-      E += Fb * E2 * sin4;
-      atomicAdd(&BJV(BJ_BO, en.x), hb1 * hb2 * eb * E2 * sin4);
-      const double dE_dr = Fb * E2 * sin4 * (-hb3) * (-r0 / (ra * ra) + 1 / r0);
-      const double dE_dcos = (cosv > -1.0 && cosv < 1.0) ? Fb * E2 * (-0.5) * (1 - cc) : 0.0;
-      const double inv = 1.0 / (rd * ra);
-      double gd[3];
-      for (int c = 0; c < 3; ++c) {
-        gd[c] = dE_dcos * (va[c] * inv - cosv * vd[c] / (rd * rd));
-        const double gac = dE_dcos * (vd[c] * inv - cosv * va[c] / (ra * ra)) + dE_dr * va[c] / ra;
-        ga[c] += gac;
-        gh[c] -= gd[c] + gac;
-      }
-      atomic_add3(w.f, jd, gd[0], gd[1], gd[2]);
+      is_donor = (int)atom_prm(ff, w.type[jd], A_P_HBOND) == 2 && BFV(BF_BO, en.x) >= HBOND_THRESHOLD;
     }
-    if (ga[0] != 0.0 || ga[1] != 0.0 || ga[2] != 0.0) atomic_add3(w.f, ja, ga[0], ga[1], ga[2]);
+    unsigned msk = __ballot_sync(0xffffffffu, is_donor);
+    while (msk) {
+      const int nd = min(__popc(msk), kHbDonors);
+      // the first nd donors of the mask go into the shared list
+      const int rank = __popc(msk & ((1u << lane) - 1u));
+      const bool mine = is_donor && (msk >> lane & 1u) && rank < nd;
+      if (mine) {
+        HbDonor& d = don[wl][rank];
+        d.b = en.x;
+        d.jd = bond_other(w, en.x, en.y);
+        d.td = w.type[d.jd];
+        d.shift = bond_shift(w, en.x, en.y);
+        d.bo = BFV(BF_BO, en.x);
+        bond_vec(w, en.x, en.y, d.v);
+        d.r = w.b_r[en.x];
+        d.dbo = 0.0;
+        d.g[0] = d.g[1] = d.g[2] = 0.0;
+      }
+      // drop the loaded donors from the mask
+      for (int q = 0; q < nd; ++q) msk &= msk - 1u;
+      if (mine) is_donor = false;
+      __syncwarp();
+      for (int e = w.cnt[0 * L + h] + lane; e < w.cnt[0 * L + h + 1]; e += 32) {
+        const int2 ed = w.edge[e];
+        const uint32_t code = (uint32_t)ed.y;
+        if (!(code & XR_CODE_HB)) continue;
+        const int ja = ed.x, ta = w.type[ja];
+        if ((int)atom_prm(ff, ta, A_P_HBOND) != 2) continue;
+        const uint32_t sa = code & XR_SHIFT_MASK;
+        double va[3];
+        {
+          const double4_32a xa = w.x[ja];
+          const int sx = xr_sx(sa), sy = xr_sy(sa), sz = xr_sz(sa);
+          const double p0[3] = {xh.x, xh.y, xh.z}, p1[3] = {xa.x, xa.y, xa.z};
+          for (int c = 0; c < 3; ++c) {
+            const double off = __dadd_rn(__dadd_rn(__dmul_rn((double)sx, S.cell[c]), __dmul_rn((double)sy, S.cell[3 + c])),
+                                         __dmul_rn((double)sz, S.cell[6 + c]));
+            va[c] = __dadd_rn(__dsub_rn(p1[c], p0[c]), off);
+          }
+        }
+        const double ra = sqrt(va[0] * va[0] + va[1] * va[1] + va[2] * va[2]);
+        double ga[3] = {0, 0, 0};
+        for (int k = 0; k < nd; ++k) {
+          HbDonor& d = don[wl][k];
+          if (d.jd == ja && d.shift == sa) continue;  // same edge
+          const int row = __ldg(ff.hbond_index + (d.td * T + th) * T + ta);
+          if (row < 0) continue;
+          const double* prm = ff.hbond + 4 * row;
+          const double r0 = __ldg(prm + 0), hb1 = __ldg(prm + 1), hb2 = __ldg(prm + 2), hb3 = __ldg(prm + 3);
+          if (!(r0 > 0)) continue;
+          const double rd = d.r;
+          const double cosv = (d.v[0] * va[0] + d.v[1] * va[1] + d.v[2] * va[2]) / (rd * ra);
+          const double cc = fmin(fmax(cosv, -1.0), 1.0);
+          const double sin4 = 0.25 * (1 - cc) * (1 - cc);
+          const double eb = exp(-hb2 * d.bo);
+          const double Fb = hb1 * (1 - eb);
+          const double E2 = exp(-hb3 * (r0 / ra + ra / r0 - 2));
+          E += Fb * E2 * sin4;
+          atomicAdd(&d.dbo, hb1 * hb2 * eb * E2 * sin4);
+          const double dE_dr = Fb * E2 * sin4 * (-hb3) * (-r0 / (ra * ra) + 1 / r0);
+          const double dE_dcos = (cosv > -1.0 && cosv < 1.0) ? Fb * E2 * (-0.5) * (1 - cc) : 0.0;
+          const double inv = 1.0 / (rd * ra);
+          for (int c = 0; c < 3; ++c) {
+            const double gdc = dE_dcos * (va[c] * inv - cosv * d.v[c] / (rd * rd));
+            const double gac = dE_dcos * (d.v[c] * inv - cosv * va[c] / (ra * ra)) + dE_dr * va[c] / ra;
+            atomicAdd(&d.g[c], gdc);
+            ga[c] += gac;
+            gh[c] -= gdc + gac;
+          }
+        }
+        if (ga[0] != 0.0 || ga[1] != 0.0 || ga[2] != 0.0) atomic_add3(w.f, ja, ga[0], ga[1], ga[2]);
+      }
+      __syncwarp();
+      if (lane < nd) {
+        const HbDonor& d = don[wl][lane];
+        if (d.dbo != 0.0) atomicAdd(&BJV(BJ_BO, d.b), d.dbo);
+        if (d.g[0] != 0.0 || d.g[1] != 0.0 || d.g[2] != 0.0) atomic_add3(w.f, d.jd, d.g[0], d.g[1], d.g[2]);
+      }
+      __syncwarp();
+    }
   }
+#pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     E += __shfl_down_sync(0xffffffffu, E, o);
     gh[0] += __shfl_down_sync(0xffffffffu, gh[0], o);
@@ -841,8 +903,12 @@ void xr_launch_bonded(const XrWork& w, const XrFF& ff, cudaStream_t st) {
   k_atom2<<<gA, tb, 0, st>>>(w, ff);
   if (w.nB > 0) k_bond_energy<<<gB, tb, 0, st>>>(w, ff);
   k_angles<<<(w.A + 3) / 4, 128, 0, st>>>(w, ff);
-  if (w.nB > 0) k_torsions<<<gB, tb, 0, st>>>(w, ff);
-  k_hbonds<<<(w.A + 3) / 4, 128, 0, st>>>(w, ff);
+  if (w.nB > 0) {
+    cudaMemsetAsync(w.nmids, 0, sizeof(int), st);
+    k_torsion_middles<<<gB, tb, 0, st>>>(w);
+    k_torsions<<<152 * 8, 256, 0, st>>>(w, ff);
+  }
+  k_hbonds<<<(w.A + kHbWarps - 1) / kHbWarps, 32 * kHbWarps, 0, st>>>(w, ff);
   k_chain_atom<<<gA, tb, 0, st>>>(w, ff);
   if (w.nB > 0) {
     k_chain_bond<<<gB, tb, 0, st>>>(w, ff);

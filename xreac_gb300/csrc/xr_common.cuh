@@ -154,6 +154,8 @@ struct XrWork {
   int2* dbrow;                // [D] {bond id, +1 if the atom is the bond's source else -1}
   int2* arow;                 // [D] active bond-row entries (bo > 0.001) at the start of each atom's range
   int* nact;                  // [A] number of active entries per atom
+  int* mids;                  // [B] bonds with bo > 0.001 (torsion middles), compacted
+  int* nmids;                 // device count of mids
   // per-atom forward intermediates [AF_N][A] and adjoints [AJ_N][A] (structure of arrays)
   double* a_fwd;
   double* a_adj;

@@ -65,7 +65,7 @@ struct xr_ctx {
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   std::string err;
-  double cg_tol = 1e-13;
+  double cg_tol = 1e-11;
   int cg_max = 2000;
   int nsm = 0;
   int coop_per_sm = 0;
@@ -110,6 +110,8 @@ struct xr_ctx {
   size_t cesum = 0;
   int2* arow = nullptr;
   size_t carow = 0;
+  int* mids = nullptr;
+  int* nmids = nullptr;
   int* nact = nullptr;
   size_t cnact = 0;
   int4* chunks = nullptr;
@@ -335,7 +337,9 @@ bool ensure_lists(xr_ctx* c, long long E, long long P, long long B) {
     cudaFree(c->b_e);
     cudaFree(c->dbrow);
     cudaFree(c->arow);
+    cudaFree(c->mids);
     c->arow = nullptr;
+    c->mids = nullptr;
     c->bond_pair = c->bond_i = c->bond_j = nullptr;
     c->b_r = c->b_v = c->b_fwd = c->b_adj = c->b_e = nullptr;
     c->dbrow = nullptr;
@@ -348,7 +352,8 @@ bool ensure_lists(xr_ctx* c, long long E, long long P, long long B) {
               cudaMalloc((void**)&c->b_adj, (size_t)BJ_N * nb * sizeof(double)) == cudaSuccess &&
               cudaMalloc((void**)&c->b_e, 4 * nb * sizeof(double)) == cudaSuccess &&
               cudaMalloc((void**)&c->dbrow, 2 * nb * sizeof(int2)) == cudaSuccess &&
-              cudaMalloc((void**)&c->arow, 2 * nb * sizeof(int2)) == cudaSuccess;
+              cudaMalloc((void**)&c->arow, 2 * nb * sizeof(int2)) == cudaSuccess &&
+              cudaMalloc((void**)&c->mids, nb * sizeof(int)) == cudaSuccess;
     if (!ok) return false;
     c->capB = nb;
   }
@@ -416,6 +421,8 @@ void attach_lists(xr_ctx* c, XrWork& w) {
   w.b_e = c->b_e;
   w.dbrow = c->dbrow;
   w.arow = c->arow;
+  w.mids = c->mids;
+  w.nmids = c->nmids;
 }
 
 // Packs forces (-dE/dx), charges, total bond orders, lone pairs and bond counts per atom.
@@ -645,7 +652,7 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
   launches += 1;
   stage(c, 5, st);
   xr_launch_bonded(w, ff->d, st);
-  launches += 13;
+  launches += 14;
   stage(c, 6, st);
   xr_launch_forces(w, ff->d, st);
   launches += 1;
@@ -850,6 +857,7 @@ int xr_ctx_create(int device, void* stream, xr_ctx** out) {
             cudaMalloc((void**)&c->counts, 8 * sizeof(int)) == cudaSuccess &&
             cudaMalloc((void**)&c->barrier, 2 * sizeof(unsigned)) == cudaSuccess &&
             cudaMalloc((void**)&c->bx_count, sizeof(int)) == cudaSuccess &&
+            cudaMalloc((void**)&c->nmids, sizeof(int)) == cudaSuccess &&
             cudaMallocHost((void**)&c->h_small, 16 * sizeof(int)) == cudaSuccess;
   if (!ok) {
     xr_ctx_destroy(c);
@@ -868,7 +876,7 @@ void xr_ctx_destroy(xr_ctx* c) {
                   c->pair_bond, c->p_r, c->p_shield, c->p_dshield, c->p_g, c->p_evdw, c->p_ecoul, c->bond_pair,
                   c->bond_i, c->bond_j, c->b_r, c->b_v, c->b_fwd, c->b_adj, c->b_e, c->dbrow, c->sys, c->energy,
                   c->props, c->status, c->counts, c->barrier, c->red, c->bx_meta, c->bx_bo, c->bx_count,
-                  c->esum, c->arow, c->nact, c->chunks, c->sys_chunks, c->chunk_part};
+                  c->esum, c->arow, c->nact, c->chunks, c->sys_chunks, c->chunk_part, c->mids, c->nmids};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (c->h_x) cudaFreeHost(c->h_x);

@@ -91,17 +91,24 @@ __global__ void k_hval(XrWork w) {
 }
 
 // ---------------------------------------------------------------------------------- QEq
-// Solver vectors (QW slots).
-enum { Q_S = 0, Q_T, Q_RS, Q_RT, Q_PS, Q_PT, Q_APS, Q_APT, Q_MINV, Q_ZS, Q_ZT };
+// Minimise 1/2 q'Hq + chi'q on {sum q = Q} -- the KKT system of src/xreac/energy.py:95-102 -- by
+// projected preconditioned conjugate gradients (Gould, Hribar & Nocedal, SIAM J. Sci. Comput. 23,
+// 1376 (2001)) with the Jacobi preconditioner D = diag(H): one solve instead of the two of the
+// LAMMPS form, with the gradient re-projected every iteration (g <- g - lambda 1,
+// lambda = <D^-1, g> / <D^-1, 1>) so the multiplier direction never accumulates.
+// The product H z with z = D^-1 (g - lambda) is formed on the fly from a pre-scaled matrix
+// H'_ij = H_ij / D_jj and row sums c_i = sum_j H'_ij, so no vector other than g is gathered.
+// Per iteration: one matrix-vector product and two team-wide reductions (two barriers).
+enum { Q_X = 0, Q_G, Q_P, Q_HP, Q_DINV, Q_C };
 
-// Bounded grid barrier for a cooperative launch (all blocks co-resident). Returns false when the
-// wait ran out; the caller then leaves the solver and the host reports the status bit.
 __device__ inline unsigned ld_acquire(const unsigned* p) {
   unsigned v;
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
 
+// Bounded grid barrier for a cooperative launch (all blocks co-resident). Returns false when the
+// wait ran out; every block then leaves the solver and the host reports the status bit.
 __device__ bool grid_barrier(unsigned* bar, unsigned nblocks, int* status) {
   __syncthreads();
   __shared__ int ok;
@@ -131,30 +138,6 @@ __device__ bool grid_barrier(unsigned* bar, unsigned nblocks, int* status) {
   return ok;
 }
 
-// Row product for both right-hand sides: y = H x over atom a's full row.
-__device__ inline void row_matvec(const XrWork& w, const XrFF& ff, int a, int lane, const double* xs, const double* xt,
-                                  double* ys, double* yt) {
-  const int L = w.A + 1;
-  double ss = 0, st = 0;
-  for (int e = w.cnt[a] + lane; e < w.cnt[a + 1]; e += 32) {
-    const int j = w.edge[e].x;
-    const double h = w.hval[e];
-    ss += h * __ldcg(xs + j);
-    st += h * __ldcg(xt + j);
-  }
-  (void)L;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    ss += __shfl_down_sync(0xffffffffu, ss, o);
-    st += __shfl_down_sync(0xffffffffu, st, o);
-  }
-  if (lane == 0) {
-    const double eta = atom_prm(ff, w.type[a], A_ETA);
-    *ys = eta * __ldcg(xs + a) + ss;
-    *yt = eta * __ldcg(xt + a) + st;
-  }
-}
-
 // Block-wide sum of NV values; result broadcast to all threads.
 template <int NV>
 __device__ inline void block_sum(double* v, double* smem) {
@@ -175,15 +158,9 @@ __device__ inline void block_sum(double* v, double* smem) {
   __syncthreads();
 }
 
-// Team abstraction: either the whole cooperative grid working on one system, or one block.
+// Team: the whole cooperative grid on one system, or one block on one system of a batch.
 struct GridTeam {
-  unsigned nblocks;
-  __device__ int warp() const { return (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5); }
-  __device__ int nwarps() const { return (int)((gridDim.x * blockDim.x) >> 5); }
-  __device__ int thread() const { return (int)(blockIdx.x * blockDim.x + threadIdx.x); }
-  __device__ int nthreads() const { return (int)(gridDim.x * blockDim.x); }
-  __device__ bool sync(const XrWork& w) const { return grid_barrier(w.barrier, nblocks, w.status); }
-  // Sum NV values over the team: block sums written to w.red, then every block adds them in order.
+  __device__ bool sync(const XrWork& w) const { return grid_barrier(w.barrier, gridDim.x, w.status); }
   template <int NV>
   __device__ bool sum(const XrWork& w, double* v, double* smem, int slot) const {
     block_sum<NV>(v, smem);
@@ -208,10 +185,6 @@ struct GridTeam {
 };
 
 struct BlockTeam {
-  __device__ int warp() const { return (int)(threadIdx.x >> 5); }
-  __device__ int nwarps() const { return (int)(blockDim.x >> 5); }
-  __device__ int thread() const { return (int)threadIdx.x; }
-  __device__ int nthreads() const { return (int)blockDim.x; }
   __device__ bool sync(const XrWork&) const {
     __syncthreads();
     return true;
@@ -223,135 +196,171 @@ struct BlockTeam {
   }
 };
 
-// Preconditioned CG on both right-hand sides for the atoms [a0, a0 + n) of one system.
+// Rows [r0, r1) of the system starting at atom a0 belong to this block; warps take rows in turn.
+// When `cache` is non-null the block's matrix rows (column, H'_ij) are kept in shared memory.
 template <class Team>
-__device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int a0, int n, double Q, double* smem) {
-  const int lane = threadIdx.x & 31;
-  double* xs = &QW(Q_S, 0);
-  double* xt = &QW(Q_T, 0);
-  double* ps = &QW(Q_PS, 0);
-  double* pt = &QW(Q_PT, 0);
-  // Jacobi preconditioner: diag(H) = eta + self-image shields.
-  for (int r = team.warp(); r < n; r += team.nwarps()) {
+__device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int a0, int n, int r0, int r1,
+                          double Q, double* smem, int* cache_j, double* cache_h, int cache_cap) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  double* X = &QW(Q_X, 0);
+  double* G = &QW(Q_G, 0);
+  double* Pv = &QW(Q_P, 0);
+  double* HP = &QW(Q_HP, 0);
+  double* DI = &QW(Q_DINV, 0);
+  double* Cr = &QW(Q_C, 0);
+  // 1. Jacobi diagonal (eta + self-image shields) of the owned rows.
+  for (int r = r0 + wid; r < r1; r += nw) {
     const int a = a0 + r;
     double d = 0;
     for (int e = w.cnt[a] + lane; e < w.cnt[a + 1]; e += 32)
       if (w.edge[e].x == a) d += w.hval[e];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) d += __shfl_down_sync(0xffffffffu, d, o);
-    if (lane == 0) QW(Q_MINV, a) = 1.0 / (atom_prm(ff, w.type[a], A_ETA) + d);
+    for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+    if (lane == 0) DI[a] = 1.0 / (atom_prm(ff, w.type[a], A_ETA) + d);
   }
   if (!team.sync(w)) return;
-  double v[4] = {0, 0, 0, 0};
-  for (int r = team.thread(); r < n; r += team.nthreads()) {
+  // 2. Pre-scaled rows H'_ij = H_ij / D_jj (cached or in hval), row sums, and the start point
+  //    x0 = Q/n with gradient g0 = H x0 + chi = (Q/n) * rowsum(H) + chi.
+  const int ebeg = w.cnt[a0 + r0], eend = w.cnt[a0 + r1];
+  const bool cached = cache_j != nullptr && (eend - ebeg) <= cache_cap;
+  const double x0 = Q / n;
+  double acc[3] = {0, 0, 0};  // <D^-1, 1>, <D^-1, g>, <D^-1, g^2>
+  for (int r = r0 + wid; r < r1; r += nw) {
     const int a = a0 + r;
-    const double bs = -atom_prm(ff, w.type[a], A_CHI), bt = -1.0, m = QW(Q_MINV, a);
-    QW(Q_S, a) = 0.0;
-    QW(Q_T, a) = 0.0;
-    QW(Q_RS, a) = bs;
-    QW(Q_RT, a) = bt;
-    QW(Q_PS, a) = m * bs;
-    QW(Q_PT, a) = m * bt;
-    v[0] += bs * m * bs;
-    v[1] += bt * m * bt;
-    v[2] += bs * bs;
-    v[3] += bt * bt;
-  }
-  if (!team.template sum<4>(w, v, smem, 0)) return;
-  double rz_s = v[0], rz_t = v[1];
-  const double tol2 = w.cg_tol * w.cg_tol;
-  const double bb_s = v[2], bb_t = v[3];
-  bool done_s = v[2] <= tol2 * bb_s, done_t = v[3] <= tol2 * bb_t;
-  int it = 0;
-  int slot = 1;
-  while (!(done_s && done_t)) {
-    if (++it > w.cg_max_iter) {
-      if (team.thread() == 0) atomicOr(w.status, XR_S_CG);
-      break;
-    }
-    for (int r = team.warp(); r < n; r += team.nwarps()) {
-      const int a = a0 + r;
-      double ys, yt;
-      row_matvec(w, ff, a, lane, ps, pt, &ys, &yt);
-      if (lane == 0) {
-        QW(Q_APS, a) = ys;
-        QW(Q_APT, a) = yt;
+    const int t = w.type[a];
+    double rs = 0, cs = 0;
+    for (int e = w.cnt[a] + lane; e < w.cnt[a + 1]; e += 32) {
+      const int j = w.edge[e].x;
+      const double h = w.hval[e];
+      const double hp = h * __ldcg(DI + j);
+      rs += h;
+      cs += hp;
+      if (cached) {
+        cache_j[e - ebeg] = j;
+        cache_h[e - ebeg] = hp;
+      } else {
+        w.hval[e] = hp;  // scaled in place; hval is not read after the solve
       }
     }
-    if (!team.sync(w)) return;
-    double u[2] = {0, 0};
-    for (int r = team.thread(); r < n; r += team.nthreads()) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      rs += __shfl_xor_sync(0xffffffffu, rs, o);
+      cs += __shfl_xor_sync(0xffffffffu, cs, o);
+    }
+    if (lane == 0) {
+      const double eta = atom_prm(ff, t, A_ETA), di = DI[a];
+      const double g = x0 * (rs + eta) + atom_prm(ff, t, A_CHI);
+      Cr[a] = cs + eta * di;
+      X[a] = x0;
+      G[a] = g;
+      Pv[a] = 0.0;
+      HP[a] = 0.0;
+      acc[0] += di;
+      acc[1] += di * g;
+      acc[2] += di * g * g;
+    }
+  }
+  if (!team.template sum<3>(w, acc, smem, 0)) return;
+  const double s1 = acc[0];
+  double lam = acc[1] / s1;
+  double gz = acc[2] - lam * acc[1];
+  const double gz0 = gz;
+  const double tol2 = w.cg_tol * w.cg_tol;
+  double beta = 0.0;
+  int it = 0;
+  int slot = 1;
+  bool converged = !(gz0 > 0.0);
+  while (!converged) {
+    if (++it > w.cg_max_iter) {
+      if (threadIdx.x == 0) atomicOr(w.status, XR_S_CG);
+      break;
+    }
+    // p = -z + beta p,  Hp = -H z + beta Hp,  z = D^-1 (g - lambda)
+    double pHp[1] = {0.0};
+    for (int r = r0 + wid; r < r1; r += nw) {
       const int a = a0 + r;
-      u[0] += QW(Q_PS, a) * QW(Q_APS, a);
-      u[1] += QW(Q_PT, a) * QW(Q_APT, a);
+      double hz = 0;
+      const int eb = w.cnt[a], ee = w.cnt[a + 1];
+      if (cached) {
+        for (int e = eb + lane; e < ee; e += 32) hz += cache_h[e - ebeg] * __ldcg(G + cache_j[e - ebeg]);
+      } else {
+        for (int e = eb + lane; e < ee; e += 32) hz += w.hval[e] * __ldcg(G + w.edge[e].x);
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) hz += __shfl_xor_sync(0xffffffffu, hz, o);
+      if (lane == 0) {
+        const double ga = G[a];
+        const double di = DI[a];
+        const double eta = atom_prm(ff, w.type[a], A_ETA);
+        hz += eta * di * ga - lam * Cr[a];
+        const double z = di * (ga - lam);
+        const double p = -z + beta * Pv[a];
+        const double hp = -hz + beta * HP[a];
+        Pv[a] = p;
+        HP[a] = hp;
+        pHp[0] += p * hp;
+      }
+    }
+    if (!team.template sum<1>(w, pHp, smem, slot)) return;
+    slot = slot == 1 ? 2 : 1;
+    if (!(pHp[0] > 0.0)) {
+      if (threadIdx.x == 0) atomicOr(w.status, XR_S_NONSPD);
+      break;
+    }
+    const double alpha = gz / pHp[0];
+    double u[2] = {0, 0};
+    for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+      const int a = a0 + r;
+      const double g = G[a] + alpha * HP[a];
+      X[a] += alpha * Pv[a];
+      G[a] = g;
+      const double di = DI[a];
+      u[0] += di * g;
+      u[1] += di * g * g;
     }
     if (!team.template sum<2>(w, u, smem, slot)) return;
     slot = slot == 1 ? 2 : 1;
-    if ((!done_s && !(u[0] > 0)) || (!done_t && !(u[1] > 0))) {
-      if (team.thread() == 0) atomicOr(w.status, XR_S_NONSPD);
-      break;
-    }
-    const double as = done_s ? 0.0 : rz_s / u[0], at = done_t ? 0.0 : rz_t / u[1];
-    double z[4] = {0, 0, 0, 0};
-    for (int r = team.thread(); r < n; r += team.nthreads()) {
-      const int a = a0 + r;
-      const double m = QW(Q_MINV, a);
-      QW(Q_S, a) += as * QW(Q_PS, a);
-      QW(Q_T, a) += at * QW(Q_PT, a);
-      const double rs = QW(Q_RS, a) - as * QW(Q_APS, a);
-      const double rt = QW(Q_RT, a) - at * QW(Q_APT, a);
-      QW(Q_RS, a) = rs;
-      QW(Q_RT, a) = rt;
-      z[0] += rs * m * rs;
-      z[1] += rt * m * rt;
-      z[2] += rs * rs;
-      z[3] += rt * rt;
-    }
-    if (!team.template sum<4>(w, z, smem, slot)) return;
-    slot = slot == 1 ? 2 : 1;
-    const double bs = done_s ? 0.0 : z[0] / rz_s, bt = done_t ? 0.0 : z[1] / rz_t;
-    rz_s = z[0];
-    rz_t = z[1];
-    done_s = done_s || z[2] <= tol2 * bb_s;
-    done_t = done_t || z[3] <= tol2 * bb_t;
-    for (int r = team.thread(); r < n; r += team.nthreads()) {
-      const int a = a0 + r;
-      const double m = QW(Q_MINV, a);
-      QW(Q_PS, a) = m * QW(Q_RS, a) + bs * QW(Q_PS, a);
-      QW(Q_PT, a) = m * QW(Q_RT, a) + bt * QW(Q_PT, a);
-    }
-    if (!team.sync(w)) return;
+    lam = u[0] / s1;
+    const double gz_new = u[1] - lam * u[0];
+    converged = gz_new <= tol2 * gz0;
+    beta = gz_new / gz;
+    gz = gz_new;
   }
-  if (team.thread() == 0) atomicMax(w.counts + 4, it);
-  // q = s + mu t with mu = (Q - sum s) / sum t.
-  double sm[2] = {0, 0};
-  for (int r = team.thread(); r < n; r += team.nthreads()) {
-    sm[0] += xs[a0 + r];
-    sm[1] += xt[a0 + r];
-  }
-  if (!team.template sum<2>(w, sm, smem, 3)) return;
-  const double mu = (Q - sm[0]) / sm[1];
-  for (int r = team.thread(); r < n; r += team.nthreads()) {
+  if (threadIdx.x == 0) atomicMax(w.counts + 4, it);
+  // Final charges; the constraint is restored exactly against accumulated rounding.
+  double sx[1] = {0.0};
+  for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) sx[0] += X[a0 + r];
+  if (!team.template sum<1>(w, sx, smem, 3)) return;
+  const double shift = (Q - sx[0]) / n;
+  for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
     const int a = a0 + r;
-    const double q = xs[a] + mu * xt[a];
+    const double q = X[a] + shift;
     w.q[a] = q;
     const int t = w.type[a];
     AEV(6, a) = SELF_CONVERSION * (atom_prm(ff, t, A_CHI) * q + 0.5 * atom_prm(ff, t, A_ETA) * q * q);
   }
 }
 
+constexpr int kQeqCacheBytes = 200 * 1024;
+constexpr int kQeqCacheEdges = kQeqCacheBytes / 12;
+
 __global__ void __launch_bounds__(1024, 1) k_qeq_grid(XrWork w, XrFF ff) {
   __shared__ double smem[4 * 32];
+  extern __shared__ __align__(16) unsigned char dyn[];
   const XrSystem& S = w.sys[0];
-  GridTeam team{gridDim.x};
-  qeq_solve(w, ff, team, S.atom_off, S.natoms, S.total_charge, smem);
+  const int per = ((S.natoms + gridDim.x - 1) / gridDim.x + 31) / 32 * 32;
+  const int r0 = min(S.natoms, (int)blockIdx.x * per), r1 = min(S.natoms, r0 + per);
+  double* cache_h = reinterpret_cast<double*>(dyn);
+  int* cache_j = reinterpret_cast<int*>(dyn + sizeof(double) * kQeqCacheEdges);
+  GridTeam team;
+  qeq_solve(w, ff, team, S.atom_off, S.natoms, r0, r1, S.total_charge, smem, cache_j, cache_h, kQeqCacheEdges);
 }
 
-__global__ void k_qeq_block(XrWork w, XrFF ff) {
+__global__ void __launch_bounds__(1024, 1) k_qeq_block(XrWork w, XrFF ff) {
   __shared__ double smem[4 * 32];
   const XrSystem& S = w.sys[blockIdx.x];
   BlockTeam team;
-  qeq_solve(w, ff, team, S.atom_off, S.natoms, S.total_charge, smem);
+  qeq_solve(w, ff, team, S.atom_off, S.natoms, 0, S.natoms, S.total_charge, smem, nullptr, nullptr, 0);
 }
 
 // ------------------------------------------------------------------------------ Coulomb
@@ -515,9 +524,13 @@ void xr_launch_pairs(const XrWork& w, const XrFF& ff, cudaStream_t st) {
   if (w.nE > 0) k_hval<<<(w.nE + 255) / 256, 256, 0, st>>>(w);
 }
 
+// Dynamic shared memory of the grid solver: cached rows (8 B value + 4 B column each).
+constexpr size_t kQeqDynSmem = (size_t)kQeqCacheEdges * (sizeof(double) + sizeof(int));
+
 int xr_qeq_coop_blocks_per_sm() {
+  cudaFuncSetAttribute(k_qeq_grid, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kQeqDynSmem);
   int nb = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_qeq_grid, 1024, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_qeq_grid, 1024, kQeqDynSmem);
   return nb;
 }
 
@@ -528,10 +541,10 @@ int xr_launch_qeq(const XrWork& w, const XrFF& ff, cudaStream_t st, int coop_blo
     const int blocks = coop_blocks;
     cudaMemsetAsync(w.barrier, 0, 2 * sizeof(unsigned), st);
     void* args[] = {(void*)&w, (void*)&ff};
-    cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_qeq_grid, dim3(blocks), dim3(1024), args, 0, st);
+    cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_qeq_grid, dim3(blocks), dim3(1024), args, kQeqDynSmem, st);
     return (int)e;
   }
-  k_qeq_block<<<w.S, 256, 0, st>>>(w, ff);
+  k_qeq_block<<<w.S, 1024, 0, st>>>(w, ff);
   return (int)cudaGetLastError();
 }
 
