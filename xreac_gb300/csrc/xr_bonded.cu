@@ -658,10 +658,10 @@ __global__ void k_torsions(XrWork w, XrFF ff) {
 // lanes then take acceptor edges of its full row (heavy neighbour within min(7.5, cutoff)) and pair
 // each with every donor except the same edge. Donor sensitivities accumulate in shared memory.
 constexpr int kHbWarps = 4;
-constexpr int kHbDonors = 8;
+constexpr int kHbDonors = 4;
 struct HbDonor {
   double v[3];
-  double r, bo, dbo, g[3];
+  double r, bo;
   int b, jd, td;
   uint32_t shift;
 };
@@ -695,9 +695,8 @@ __global__ void k_hbonds(XrWork w, XrFF ff) {
     unsigned msk = __ballot_sync(0xffffffffu, is_donor);
     while (msk) {
       const int nd = min(__popc(msk), kHbDonors);
-      // the first nd donors of the mask go into the shared list
       const int rank = __popc(msk & ((1u << lane) - 1u));
-      const bool mine = is_donor && (msk >> lane & 1u) && rank < nd;
+      const bool mine = (msk >> lane & 1u) && rank < nd;
       if (mine) {
         HbDonor& d = don[wl][rank];
         d.b = en.x;
@@ -707,13 +706,13 @@ __global__ void k_hbonds(XrWork w, XrFF ff) {
         d.bo = BFV(BF_BO, en.x);
         bond_vec(w, en.x, en.y, d.v);
         d.r = w.b_r[en.x];
-        d.dbo = 0.0;
-        d.g[0] = d.g[1] = d.g[2] = 0.0;
       }
-      // drop the loaded donors from the mask
       for (int q = 0; q < nd; ++q) msk &= msk - 1u;
-      if (mine) is_donor = false;
       __syncwarp();
+      // per-lane donor accumulators (registers; fixed indices after unrolling)
+      double acc[kHbDonors][4];
+#pragma unroll
+      for (int k = 0; k < kHbDonors; ++k) acc[k][0] = acc[k][1] = acc[k][2] = acc[k][3] = 0.0;
       for (int e = w.cnt[0 * L + h] + lane; e < w.cnt[0 * L + h + 1]; e += 32) {
         const int2 ed = w.edge[e];
         const uint32_t code = (uint32_t)ed.y;
@@ -734,8 +733,10 @@ __global__ void k_hbonds(XrWork w, XrFF ff) {
         }
         const double ra = sqrt(va[0] * va[0] + va[1] * va[1] + va[2] * va[2]);
         double ga[3] = {0, 0, 0};
-        for (int k = 0; k < nd; ++k) {
-          HbDonor& d = don[wl][k];
+#pragma unroll
+        for (int k = 0; k < kHbDonors; ++k) {
+          if (k >= nd) break;
+          const HbDonor& d = don[wl][k];
           if (d.jd == ja && d.shift == sa) continue;  // same edge
           const int row = __ldg(ff.hbond_index + (d.td * T + th) * T + ta);
           if (row < 0) continue;
@@ -750,25 +751,35 @@ __global__ void k_hbonds(XrWork w, XrFF ff) {
           const double Fb = hb1 * (1 - eb);
           const double E2 = exp(-hb3 * (r0 / ra + ra / r0 - 2));
           E += Fb * E2 * sin4;
-          atomicAdd(&d.dbo, hb1 * hb2 * eb * E2 * sin4);
+          acc[k][3] += hb1 * hb2 * eb * E2 * sin4;
           const double dE_dr = Fb * E2 * sin4 * (-hb3) * (-r0 / (ra * ra) + 1 / r0);
           const double dE_dcos = (cosv > -1.0 && cosv < 1.0) ? Fb * E2 * (-0.5) * (1 - cc) : 0.0;
           const double inv = 1.0 / (rd * ra);
+#pragma unroll
           for (int c = 0; c < 3; ++c) {
             const double gdc = dE_dcos * (va[c] * inv - cosv * d.v[c] / (rd * rd));
             const double gac = dE_dcos * (d.v[c] * inv - cosv * va[c] / (ra * ra)) + dE_dr * va[c] / ra;
-            atomicAdd(&d.g[c], gdc);
+            acc[k][c] += gdc;
             ga[c] += gac;
             gh[c] -= gdc + gac;
           }
         }
         if (ga[0] != 0.0 || ga[1] != 0.0 || ga[2] != 0.0) atomic_add3(w.f, ja, ga[0], ga[1], ga[2]);
       }
-      __syncwarp();
-      if (lane < nd) {
-        const HbDonor& d = don[wl][lane];
-        if (d.dbo != 0.0) atomicAdd(&BJV(BJ_BO, d.b), d.dbo);
-        if (d.g[0] != 0.0 || d.g[1] != 0.0 || d.g[2] != 0.0) atomic_add3(w.f, d.jd, d.g[0], d.g[1], d.g[2]);
+      // donor sensitivities: warp sums, then one update per donor
+#pragma unroll
+      for (int k = 0; k < kHbDonors; ++k) {
+        if (k >= nd) break;
+#pragma unroll
+        for (int c = 0; c < 4; ++c)
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) acc[k][c] += __shfl_xor_sync(0xffffffffu, acc[k][c], o);
+        if (lane == 0) {
+          const HbDonor& d = don[wl][k];
+          if (acc[k][3] != 0.0) atomicAdd(&BJV(BJ_BO, d.b), acc[k][3]);
+          if (acc[k][0] != 0.0 || acc[k][1] != 0.0 || acc[k][2] != 0.0)
+            atomic_add3(w.f, d.jd, acc[k][0], acc[k][1], acc[k][2]);
+        }
       }
       __syncwarp();
     }

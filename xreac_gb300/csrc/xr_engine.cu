@@ -65,7 +65,7 @@ struct xr_ctx {
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   std::string err;
-  double cg_tol = 1e-11;
+  double cg_tol = 1e-13;
   int cg_max = 2000;
   int nsm = 0;
   int coop_per_sm = 0;

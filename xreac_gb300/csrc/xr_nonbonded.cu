@@ -98,8 +98,13 @@ __global__ void k_hval(XrWork w) {
 // lambda = <D^-1, g> / <D^-1, 1>) so the multiplier direction never accumulates.
 // The product H z with z = D^-1 (g - lambda) is formed on the fly from a pre-scaled matrix
 // H'_ij = H_ij / D_jj and row sums c_i = sum_j H'_ij, so no vector other than g is gathered.
+// The gradient lives in two buffers used in turn. The multiplier part that a step adds,
+// alpha <D^-1, Hp> / <D^-1, 1>, is reduced together with p'Hp, so the new gradient is written
+// already projected and the second reduction only sees rounding-level drift; the squared norm
+// g'D^-1 g is then free of cancellation against the multiplier direction (which grows towards
+// -mu 1 at convergence), and the solver reaches the FP64 floor on every system.
 // Per iteration: one matrix-vector product and two team-wide reductions (two barriers).
-enum { Q_X = 0, Q_G, Q_P, Q_HP, Q_DINV, Q_C };
+enum { Q_X = 0, Q_G, Q_P, Q_HP, Q_DINV, Q_C, Q_G2 };
 
 __device__ inline unsigned ld_acquire(const unsigned* p) {
   unsigned v;
@@ -107,64 +112,66 @@ __device__ inline unsigned ld_acquire(const unsigned* p) {
   return v;
 }
 
-// Bounded grid barrier for a cooperative launch (all blocks co-resident). Returns false when the
+// Bounded grid barrier for a cooperative launch (all blocks co-resident): every block adds one to a
+// monotonically increasing counter with release semantics and waits, with acquire loads, until it
+// reaches the episode's target (number of blocks times episodes so far). Returns false when the
 // wait ran out; every block then leaves the solver and the host reports the status bit.
-__device__ bool grid_barrier(unsigned* bar, unsigned nblocks, int* status) {
+__device__ bool grid_barrier(unsigned* bar, unsigned target, int* status) {
   __syncthreads();
   __shared__ int ok;
   if (threadIdx.x == 0) {
     ok = 1;
-    const unsigned g0 = ld_acquire(bar + 1);
-    __threadfence();
-    const unsigned arrived = atomicAdd(bar, 1u);
-    if (arrived == nblocks - 1) {
-      bar[0] = 0;
-      __threadfence();
-      atomicAdd(bar + 1, 1u);
-    } else {
-      long long it = 0;
-      while (ld_acquire(bar + 1) == g0) {
-        if (++it > (1ll << 24) || (*(volatile int*)status & XR_S_BARRIER)) {
-          atomicOr(status, XR_S_BARRIER);
-          ok = 0;
-          break;
-        }
-        if (it > 64) __nanosleep(32);
+    asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(bar) : "memory");
+    long long it = 0;
+    while (ld_acquire(bar) < target) {
+      if (++it > (1ll << 24) || (*(volatile int*)status & XR_S_BARRIER)) {
+        atomicOr(status, XR_S_BARRIER);
+        ok = 0;
+        break;
       }
+      if (it > 256) __nanosleep(32);
     }
-    __threadfence();
   }
   __syncthreads();
   return ok;
 }
 
-// Block-wide sum of NV values; result broadcast to all threads.
+// Block sum of NV values held by lane 0 of each warp (other lanes' values are ignored); warp 0 adds
+// the per-warp values and the result is broadcast to all threads. FP64 issues at 2 per cycle per SM
+// on this part, so the adds are kept to one warp.
 template <int NV>
 __device__ inline void block_sum(double* v, double* smem) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-#pragma unroll
-  for (int k = 0; k < NV; ++k)
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
-  __syncthreads();
   if (lane == 0)
     for (int k = 0; k < NV; ++k) smem[k * 32 + wid] = v[k];
   __syncthreads();
-  for (int k = 0; k < NV; ++k) {
-    double s = 0;
-    for (int q = 0; q < nw; ++q) s += smem[k * 32 + q];
-    v[k] = s;
+  if (wid == 0) {
+    for (int k = 0; k < NV; ++k) {
+      double s = lane < nw ? smem[k * 32 + lane] : 0.0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lane == 0) smem[128 + k] = s;
+    }
   }
+  __syncthreads();
+  for (int k = 0; k < NV; ++k) v[k] = smem[128 + k];
   __syncthreads();
 }
 
 // Team: the whole cooperative grid on one system, or one block on one system of a batch.
 struct GridTeam {
-  __device__ bool sync(const XrWork& w) const { return grid_barrier(w.barrier, gridDim.x, w.status); }
+  mutable unsigned target = 0;  // barrier episodes so far times the number of blocks
+  __device__ bool sync(const XrWork& w) const {
+    target += gridDim.x;
+    return grid_barrier(w.barrier, target, w.status);
+  }
   template <int NV>
   __device__ bool sum(const XrWork& w, double* v, double* smem, int slot) const {
     block_sum<NV>(v, smem);
-    double* red = w.red + (size_t)slot * NV * gridDim.x;
+    // Fixed-size slots (up to 4 values each); consecutive reductions never share a slot, so a block
+    // can write the next partials while a slower block still reads the previous ones.
+    static_assert(NV <= 4, "at most four values per reduction");
+    double* red = w.red + (size_t)slot * 4 * gridDim.x;
     if (threadIdx.x == 0)
       for (int k = 0; k < NV; ++k) red[k * gridDim.x + blockIdx.x] = v[k];
     if (!sync(w)) return false;
@@ -204,6 +211,7 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   double* X = &QW(Q_X, 0);
   double* G = &QW(Q_G, 0);
+  double* G2 = &QW(Q_G2, 0);
   double* Pv = &QW(Q_P, 0);
   double* HP = &QW(Q_HP, 0);
   double* DI = &QW(Q_DINV, 0);
@@ -269,14 +277,17 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
   double beta = 0.0;
   int it = 0;
   int slot = 1;
-  bool converged = !(gz0 > 0.0);
+  // Nothing to solve when the projected gradient is already at rounding level (one atom, or a
+  // start that is exact by symmetry).
+  const double gfloor = 1e-28 * acc[2];
+  bool converged = !(gz0 > gfloor) || n < 2;
   while (!converged) {
     if (++it > w.cg_max_iter) {
       if (threadIdx.x == 0) atomicOr(w.status, XR_S_CG);
       break;
     }
-    // p = -z + beta p,  Hp = -H z + beta Hp,  z = D^-1 (g - lambda)
-    double pHp[1] = {0.0};
+    // p = -z + beta p,  Hp = -H z + beta Hp,  z = D^-1 (g - lambda); the next buffer gets g - lambda
+    double pHp[2] = {0.0, 0.0};  // p'Hp and <D^-1, Hp>
     for (int r = r0 + wid; r < r1; r += nw) {
       const int a = a0 + r;
       double hz = 0;
@@ -298,25 +309,31 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
         const double hp = -hz + beta * HP[a];
         Pv[a] = p;
         HP[a] = hp;
+        G2[a] = ga - lam;
         pHp[0] += p * hp;
+        pHp[1] += di * hp;
       }
     }
-    if (!team.template sum<1>(w, pHp, smem, slot)) return;
+    if (!team.template sum<2>(w, pHp, smem, slot)) return;
     slot = slot == 1 ? 2 : 1;
     if (!(pHp[0] > 0.0)) {
-      if (threadIdx.x == 0) atomicOr(w.status, XR_S_NONSPD);
+      // a vanishing direction after convergence to rounding level is not a failure
+      if (!(gz <= 1e4 * gfloor) && threadIdx.x == 0) atomicOr(w.status, XR_S_NONSPD);
       break;
     }
     const double alpha = gz / pHp[0];
+    const double step_lam = alpha * pHp[1] / s1;
     double u[2] = {0, 0};
-    for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
-      const int a = a0 + r;
-      const double g = G[a] + alpha * HP[a];
-      X[a] += alpha * Pv[a];
-      G[a] = g;
-      const double di = DI[a];
-      u[0] += di * g;
-      u[1] += di * g * g;
+    if (lane == 0) {
+      for (int r = r0 + wid; r < r1; r += nw) {
+        const int a = a0 + r;
+        const double g = (G2[a] + alpha * HP[a]) - step_lam;
+        X[a] += alpha * Pv[a];
+        G2[a] = g;
+        const double di = DI[a];
+        u[0] += di * g;
+        u[1] += di * g * g;
+      }
     }
     if (!team.template sum<2>(w, u, smem, slot)) return;
     slot = slot == 1 ? 2 : 1;
@@ -325,11 +342,15 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
     converged = gz_new <= tol2 * gz0;
     beta = gz_new / gz;
     gz = gz_new;
+    double* tmp = G;  // the buffer just written becomes the one read next
+    G = G2;
+    G2 = tmp;
   }
   if (threadIdx.x == 0) atomicMax(w.counts + 4, it);
   // Final charges; the constraint is restored exactly against accumulated rounding.
   double sx[1] = {0.0};
-  for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) sx[0] += X[a0 + r];
+  if (lane == 0)
+    for (int r = r0 + wid; r < r1; r += nw) sx[0] += X[a0 + r];
   if (!team.template sum<1>(w, sx, smem, 3)) return;
   const double shift = (Q - sx[0]) / n;
   for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
@@ -345,7 +366,7 @@ constexpr int kQeqCacheBytes = 200 * 1024;
 constexpr int kQeqCacheEdges = kQeqCacheBytes / 12;
 
 __global__ void __launch_bounds__(1024, 1) k_qeq_grid(XrWork w, XrFF ff) {
-  __shared__ double smem[4 * 32];
+  __shared__ double smem[4 * 32 + 8];  // block_sum: per-warp inputs, then results at 128..
   extern __shared__ __align__(16) unsigned char dyn[];
   const XrSystem& S = w.sys[0];
   const int per = ((S.natoms + gridDim.x - 1) / gridDim.x + 31) / 32 * 32;
@@ -357,7 +378,7 @@ __global__ void __launch_bounds__(1024, 1) k_qeq_grid(XrWork w, XrFF ff) {
 }
 
 __global__ void __launch_bounds__(1024, 1) k_qeq_block(XrWork w, XrFF ff) {
-  __shared__ double smem[4 * 32];
+  __shared__ double smem[4 * 32 + 8];  // block_sum: per-warp inputs, then results at 128..
   const XrSystem& S = w.sys[blockIdx.x];
   BlockTeam team;
   qeq_solve(w, ff, team, S.atom_off, S.natoms, 0, S.natoms, S.total_charge, smem, nullptr, nullptr, 0);
