@@ -85,7 +85,7 @@ struct XrSystem {
   double rc, rc2, bond_cut, hb_cut;     // cutoff, cutoff^2, min(5, rc), min(7.5, rc)
   float cellf[9];
   float margin;          // bound on |FP32 squared distance - FP64 squared distance| (A^2)
-  int pad;
+  float rc2f, bc2f, hc2f;  // FP32 squared cutoff, bond cutoff and hydrogen-bond cutoff
 };
 
 // Force-field tables on the device (uploaded once per force field).

@@ -274,6 +274,9 @@ int build_system(xr_ctx* c, const xr_system& in, int atom_off, double rc, XrSyst
   S.rc2 = rc * rc;
   S.bond_cut = std::min(5.0, rc);
   S.hb_cut = std::min(7.5, rc);
+  S.rc2f = (float)S.rc2;
+  S.bc2f = (float)(S.bond_cut * S.bond_cut);
+  S.hc2f = (float)(S.hb_cut * S.hb_cut);
   return XR_OK;
 }
 

@@ -165,29 +165,63 @@ struct GridTeam {
     target += gridDim.x;
     return grid_barrier(w.barrier, target, w.status);
   }
+  // Sum NV values (held by lane 0 of each warp) over the grid, fused with the barrier: warp 0 adds
+  // the block's warps, lane 0 publishes the block partial and arrives (release), then warp 0 adds
+  // all blocks' partials in a fixed order (deterministic) and broadcasts them.
   template <int NV>
   __device__ bool sum(const XrWork& w, double* v, double* smem, int slot) const {
-    block_sum<NV>(v, smem);
-    // Fixed-size slots (up to 4 values each); consecutive reductions never share a slot, so a block
-    // can write the next partials while a slower block still reads the previous ones.
+    return sum<NV>(w, v, smem, slot, [](double*) {});
+  }
+  // As sum(), with post(values) run by thread 0 on the totals before they are shared, so scalar
+  // work derived from a reduction costs no extra block synchronisation.
+  template <int NV, class Post>
+  __device__ bool sum(const XrWork& w, double* v, double* smem, int slot, Post post) const {
     static_assert(NV <= 4, "at most four values per reduction");
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    __shared__ int ok;
+    if (lane == 0)
+      for (int k = 0; k < NV; ++k) smem[k * 32 + wid] = v[k];
+    __syncthreads();
+    target += gridDim.x;
+    // Fixed-size slots; consecutive reductions never share one, so a block may publish the next
+    // partials while a slower block still reads the previous ones.
     double* red = w.red + (size_t)slot * 4 * gridDim.x;
-    if (threadIdx.x == 0)
-      for (int k = 0; k < NV; ++k) red[k * gridDim.x + blockIdx.x] = v[k];
-    if (!sync(w)) return false;
-    if (threadIdx.x < 32) {
+    if (wid == 0) {
+      double s[NV];
       for (int k = 0; k < NV; ++k) {
-        double s = 0;
-        for (unsigned q = threadIdx.x; q < gridDim.x; q += 32) s += __ldcg(red + k * gridDim.x + q);
+        double t = lane < nw ? smem[k * 32 + lane] : 0.0;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if (threadIdx.x == 0) smem[k] = s;
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        s[k] = t;
       }
+      int good = 1;
+      if (lane == 0) {
+        for (int k = 0; k < NV; ++k) red[k * gridDim.x + blockIdx.x] = s[k];
+        asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(w.barrier) : "memory");
+        long long it = 0;
+        while (ld_acquire(w.barrier) < target) {
+          if (++it > (1ll << 24) || (*(volatile int*)w.status & XR_S_BARRIER)) {
+            atomicOr(w.status, XR_S_BARRIER);
+            good = 0;
+            break;
+          }
+          if (it > 256) __nanosleep(32);
+        }
+        ok = good;
+      }
+      __syncwarp();
+      for (int k = 0; k < NV; ++k) {
+        double t = 0;
+        for (unsigned q = lane; q < gridDim.x; q += 32) t += __ldcg(red + k * gridDim.x + q);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+        if (lane == 0) smem[128 + k] = t;
+      }
+      if (lane == 0) post(smem + 128);
     }
     __syncthreads();
-    for (int k = 0; k < NV; ++k) v[k] = smem[k];
-    __syncthreads();
-    return true;
+    for (int k = 0; k < NV; ++k) v[k] = smem[128 + k];
+    return ok;
   }
 };
 
@@ -201,13 +235,34 @@ struct BlockTeam {
     block_sum<NV>(v, smem);
     return true;
   }
+  template <int NV, class Post>
+  __device__ bool sum(const XrWork&, double* v, double* smem, int, Post post) const {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if (lane == 0)
+      for (int k = 0; k < NV; ++k) smem[k * 32 + wid] = v[k];
+    __syncthreads();
+    if (wid == 0) {
+      for (int k = 0; k < NV; ++k) {
+        double s = lane < nw ? smem[k * 32 + lane] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) smem[128 + k] = s;
+      }
+      if (lane == 0) post(smem + 128);
+    }
+    __syncthreads();
+    for (int k = 0; k < NV; ++k) v[k] = smem[128 + k];
+    __syncthreads();
+    return true;
+  }
 };
 
 // Rows [r0, r1) of the system starting at atom a0 belong to this block; warps take rows in turn.
 // When `cache` is non-null the block's matrix rows (column, H'_ij) are kept in shared memory.
 template <class Team>
 __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int a0, int n, int r0, int r1,
-                          double Q, double* smem, int* cache_j, double* cache_h, int cache_cap) {
+                          double Q, double* smem, unsigned short* cache_j, double* cache_h, int cache_cap,
+                          double* gstage) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   double* X = &QW(Q_X, 0);
   double* G = &QW(Q_G, 0);
@@ -244,7 +299,7 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
       rs += h;
       cs += hp;
       if (cached) {
-        cache_j[e - ebeg] = j;
+        cache_j[e - ebeg] = (unsigned short)(j - a0);
         cache_h[e - ebeg] = hp;
       } else {
         w.hval[e] = hp;  // scaled in place; hval is not read after the solve
@@ -269,83 +324,147 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
     }
   }
   if (!team.template sum<3>(w, acc, smem, 0)) return;
+  // Iteration scalars are computed by thread 0 alone and shared: FP64 divisions replicated over a
+  // thousand threads would cost more FP64 issue slots than the matrix-vector product.
+  __shared__ double sc_lam, sc_alpha, sc_step, sc_beta;
+  __shared__ int sc_state;  // 0 iterate, 1 converged, 2 stop
   const double s1 = acc[0];
-  double lam = acc[1] / s1;
-  double gz = acc[2] - lam * acc[1];
-  const double gz0 = gz;
+  double gz = 0.0, gz0 = 0.0;
   const double tol2 = w.cg_tol * w.cg_tol;
-  double beta = 0.0;
+  const double gfloor = 1e-28 * acc[2];
+  if (threadIdx.x == 0) {
+    sc_lam = acc[1] / s1;
+    gz = acc[2] - sc_lam * acc[1];
+    gz0 = gz;
+    sc_beta = 0.0;
+    // Nothing to solve when the projected gradient is already at rounding level (one atom, or a
+    // start that is exact by symmetry).
+    sc_state = (!(gz0 > gfloor) || n < 2) ? 1 : 0;
+  }
+  __syncthreads();
+  // One row per warp (the usual grid layout): the row's solver state lives in shared memory.
+  __shared__ double rs_x[32], rs_p[32], rs_hp[32], rs_di[32], rs_c[32], rs_eta[32], rs_g[32];
+  const bool row_smem = (r1 - r0) <= nw && nw <= 32;
+  if (row_smem && lane == 0 && r0 + wid < r1) {
+    const int a = a0 + r0 + wid;
+    rs_x[wid] = X[a];
+    rs_p[wid] = 0.0;
+    rs_hp[wid] = 0.0;
+    rs_di[wid] = DI[a];
+    rs_c[wid] = Cr[a];
+    rs_eta[wid] = atom_prm(ff, w.type[a], A_ETA);
+    rs_g[wid] = G[a];
+  }
+  __syncthreads();
   int it = 0;
   int slot = 1;
-  // Nothing to solve when the projected gradient is already at rounding level (one atom, or a
-  // start that is exact by symmetry).
-  const double gfloor = 1e-28 * acc[2];
-  bool converged = !(gz0 > gfloor) || n < 2;
-  while (!converged) {
+  while (sc_state == 0) {
     if (++it > w.cg_max_iter) {
       if (threadIdx.x == 0) atomicOr(w.status, XR_S_CG);
       break;
     }
+    const double lam = sc_lam, beta = sc_beta;
     // p = -z + beta p,  Hp = -H z + beta Hp,  z = D^-1 (g - lambda); the next buffer gets g - lambda
+    if (gstage) {  // the whole gradient of the system in shared memory: the gathers below stay on-chip
+      for (int q = threadIdx.x; q < n; q += blockDim.x) gstage[q] = __ldcg(G + a0 + q);
+      __syncthreads();
+    }
     double pHp[2] = {0.0, 0.0};  // p'Hp and <D^-1, Hp>
     for (int r = r0 + wid; r < r1; r += nw) {
       const int a = a0 + r;
       double hz = 0;
       const int eb = w.cnt[a], ee = w.cnt[a + 1];
-      if (cached) {
-        for (int e = eb + lane; e < ee; e += 32) hz += cache_h[e - ebeg] * __ldcg(G + cache_j[e - ebeg]);
+      if (cached && gstage) {
+        for (int e = eb + lane; e < ee; e += 32) hz += cache_h[e - ebeg] * gstage[cache_j[e - ebeg]];
+      } else if (cached) {
+        for (int e = eb + lane; e < ee; e += 32) hz += cache_h[e - ebeg] * __ldcg(G + a0 + cache_j[e - ebeg]);
       } else {
-        for (int e = eb + lane; e < ee; e += 32) hz += w.hval[e] * __ldcg(G + w.edge[e].x);
+        double h0 = 0, h1 = 0;
+        int e = eb + lane;
+        for (; e + 32 < ee; e += 64) {
+          const double g0 = __ldcg(G + w.edge[e].x), g1 = __ldcg(G + w.edge[e + 32].x);
+          h0 += w.hval[e] * g0;
+          h1 += w.hval[e + 32] * g1;
+        }
+        if (e < ee) h0 += w.hval[e] * __ldcg(G + w.edge[e].x);
+        hz = h0 + h1;
       }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) hz += __shfl_xor_sync(0xffffffffu, hz, o);
       if (lane == 0) {
-        const double ga = G[a];
-        const double di = DI[a];
-        const double eta = atom_prm(ff, w.type[a], A_ETA);
-        hz += eta * di * ga - lam * Cr[a];
+        const double ga = row_smem ? rs_g[wid] : (gstage ? gstage[r] : G[a]);
+        const double di = row_smem ? rs_di[wid] : DI[a];
+        const double eta = row_smem ? rs_eta[wid] : atom_prm(ff, w.type[a], A_ETA);
+        const double cr = row_smem ? rs_c[wid] : Cr[a];
+        const double p_old = row_smem ? rs_p[wid] : Pv[a];
+        const double hp_old = row_smem ? rs_hp[wid] : HP[a];
+        hz += eta * di * ga - lam * cr;
         const double z = di * (ga - lam);
-        const double p = -z + beta * Pv[a];
-        const double hp = -hz + beta * HP[a];
-        Pv[a] = p;
-        HP[a] = hp;
-        G2[a] = ga - lam;
+        const double p = -z + beta * p_old;
+        const double hp = -hz + beta * hp_old;
+        if (row_smem) {
+          rs_p[wid] = p;
+          rs_hp[wid] = hp;
+          rs_g[wid] = ga - lam;
+        } else {
+          Pv[a] = p;
+          HP[a] = hp;
+          G2[a] = ga - lam;
+        }
         pHp[0] += p * hp;
         pHp[1] += di * hp;
       }
     }
-    if (!team.template sum<2>(w, pHp, smem, slot)) return;
+    if (!team.template sum<2>(w, pHp, smem, slot, [&](double* t) {
+          if (!(t[0] > 0.0)) {
+            // a vanishing direction after convergence to rounding level is not a failure
+            if (!(gz <= 1e4 * gfloor)) atomicOr(w.status, XR_S_NONSPD);
+            sc_state = 2;
+          } else {
+            sc_alpha = gz / t[0];
+            sc_step = sc_alpha * t[1] / s1;
+          }
+        }))
+      return;
     slot = slot == 1 ? 2 : 1;
-    if (!(pHp[0] > 0.0)) {
-      // a vanishing direction after convergence to rounding level is not a failure
-      if (!(gz <= 1e4 * gfloor) && threadIdx.x == 0) atomicOr(w.status, XR_S_NONSPD);
-      break;
-    }
-    const double alpha = gz / pHp[0];
-    const double step_lam = alpha * pHp[1] / s1;
+    if (sc_state != 0) break;
+    const double alpha = sc_alpha, step_lam = sc_step;
     double u[2] = {0, 0};
     if (lane == 0) {
       for (int r = r0 + wid; r < r1; r += nw) {
         const int a = a0 + r;
-        const double g = (G2[a] + alpha * HP[a]) - step_lam;
-        X[a] += alpha * Pv[a];
-        G2[a] = g;
-        const double di = DI[a];
-        u[0] += di * g;
-        u[1] += di * g * g;
+        if (row_smem) {
+          const double g = (rs_g[wid] + alpha * rs_hp[wid]) - step_lam;
+          rs_x[wid] += alpha * rs_p[wid];
+          rs_g[wid] = g;
+          G2[a] = g;  // published for the other rows' products
+          u[0] += rs_di[wid] * g;
+          u[1] += rs_di[wid] * g * g;
+        } else {
+          const double g = (G2[a] + alpha * HP[a]) - step_lam;
+          X[a] += alpha * Pv[a];
+          G2[a] = g;
+          const double di = DI[a];
+          u[0] += di * g;
+          u[1] += di * g * g;
+        }
       }
     }
-    if (!team.template sum<2>(w, u, smem, slot)) return;
+    if (!team.template sum<2>(w, u, smem, slot, [&](double* t) {
+          sc_lam = t[0] / s1;
+          const double gz_new = t[1] - sc_lam * t[0];
+          if (gz_new <= tol2 * gz0) sc_state = 1;
+          sc_beta = gz_new / gz;
+          gz = gz_new;
+        }))
+      return;
     slot = slot == 1 ? 2 : 1;
-    lam = u[0] / s1;
-    const double gz_new = u[1] - lam * u[0];
-    converged = gz_new <= tol2 * gz0;
-    beta = gz_new / gz;
-    gz = gz_new;
     double* tmp = G;  // the buffer just written becomes the one read next
     G = G2;
     G2 = tmp;
   }
+  if (row_smem && lane == 0 && r0 + wid < r1) X[a0 + r0 + wid] = rs_x[wid];
+  __syncthreads();
   if (threadIdx.x == 0) atomicMax(w.counts + 4, it);
   // Final charges; the constraint is restored exactly against accumulated rounding.
   double sx[1] = {0.0};
@@ -362,26 +481,29 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
   }
 }
 
-constexpr int kQeqCacheBytes = 200 * 1024;
-constexpr int kQeqCacheEdges = kQeqCacheBytes / 12;
+// Dynamic shared memory of the grid solver: [gradient stage: n doubles][row cache values][row cache
+// columns (16-bit, local to the system)]. The host sizes the two parts per launch.
+constexpr int kQeqMaxDyn = 220 * 1024;
 
-__global__ void __launch_bounds__(1024, 1) k_qeq_grid(XrWork w, XrFF ff) {
-  __shared__ double smem[4 * 32 + 8];  // block_sum: per-warp inputs, then results at 128..
+__global__ void __launch_bounds__(1024, 1) k_qeq_grid(XrWork w, XrFF ff, int stage_n, int cache_cap) {
+  __shared__ double smem[4 * 32 + 8];  // reductions: per-warp inputs, then results at 128..
   extern __shared__ __align__(16) unsigned char dyn[];
   const XrSystem& S = w.sys[0];
   const int per = ((S.natoms + gridDim.x - 1) / gridDim.x + 31) / 32 * 32;
   const int r0 = min(S.natoms, (int)blockIdx.x * per), r1 = min(S.natoms, r0 + per);
-  double* cache_h = reinterpret_cast<double*>(dyn);
-  int* cache_j = reinterpret_cast<int*>(dyn + sizeof(double) * kQeqCacheEdges);
+  double* gstage = stage_n > 0 ? reinterpret_cast<double*>(dyn) : nullptr;
+  double* cache_h = reinterpret_cast<double*>(dyn + sizeof(double) * (size_t)stage_n);
+  unsigned short* cache_j = reinterpret_cast<unsigned short*>(dyn + sizeof(double) * ((size_t)stage_n + cache_cap));
   GridTeam team;
-  qeq_solve(w, ff, team, S.atom_off, S.natoms, r0, r1, S.total_charge, smem, cache_j, cache_h, kQeqCacheEdges);
+  qeq_solve(w, ff, team, S.atom_off, S.natoms, r0, r1, S.total_charge, smem, cache_cap > 0 ? cache_j : nullptr,
+            cache_h, cache_cap, gstage);
 }
 
 __global__ void __launch_bounds__(1024, 1) k_qeq_block(XrWork w, XrFF ff) {
-  __shared__ double smem[4 * 32 + 8];  // block_sum: per-warp inputs, then results at 128..
+  __shared__ double smem[4 * 32 + 8];  // reductions: per-warp inputs, then results at 128..
   const XrSystem& S = w.sys[blockIdx.x];
   BlockTeam team;
-  qeq_solve(w, ff, team, S.atom_off, S.natoms, 0, S.natoms, S.total_charge, smem, nullptr, nullptr, 0);
+  qeq_solve(w, ff, team, S.atom_off, S.natoms, 0, S.natoms, S.total_charge, smem, nullptr, nullptr, 0, nullptr);
 }
 
 // ------------------------------------------------------------------------------ Coulomb
@@ -545,13 +667,10 @@ void xr_launch_pairs(const XrWork& w, const XrFF& ff, cudaStream_t st) {
   if (w.nE > 0) k_hval<<<(w.nE + 255) / 256, 256, 0, st>>>(w);
 }
 
-// Dynamic shared memory of the grid solver: cached rows (8 B value + 4 B column each).
-constexpr size_t kQeqDynSmem = (size_t)kQeqCacheEdges * (sizeof(double) + sizeof(int));
-
 int xr_qeq_coop_blocks_per_sm() {
-  cudaFuncSetAttribute(k_qeq_grid, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kQeqDynSmem);
+  cudaFuncSetAttribute(k_qeq_grid, cudaFuncAttributeMaxDynamicSharedMemorySize, kQeqMaxDyn);
   int nb = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_qeq_grid, 1024, kQeqDynSmem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_qeq_grid, 1024, kQeqMaxDyn);
   return nb;
 }
 
@@ -560,9 +679,15 @@ int xr_launch_qeq(const XrWork& w, const XrFF& ff, cudaStream_t st, int coop_blo
   if (w.S == 1 && coop_blocks > 1) {
     // coop_blocks is already clamped by the host to the co-resident maximum and to the rows.
     const int blocks = coop_blocks;
+    const int n = w.A;
+    // Stage the gradient when it takes at most half the budget; columns of the row cache are
+    // 16-bit offsets, so the cache needs a system of at most 65536 atoms.
+    int stage_n = (n * 8 <= kQeqMaxDyn / 2) ? n : 0;
+    int cache_cap = n <= 65536 ? (int)((kQeqMaxDyn - (size_t)stage_n * 8) / (sizeof(double) + sizeof(unsigned short))) : 0;
+    const size_t dyn = (size_t)stage_n * 8 + (size_t)cache_cap * (sizeof(double) + sizeof(unsigned short));
     cudaMemsetAsync(w.barrier, 0, 2 * sizeof(unsigned), st);
-    void* args[] = {(void*)&w, (void*)&ff};
-    cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_qeq_grid, dim3(blocks), dim3(1024), args, kQeqDynSmem, st);
+    void* args[] = {(void*)&w, (void*)&ff, (void*)&stage_n, (void*)&cache_cap};
+    cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_qeq_grid, dim3(blocks), dim3(1024), args, dyn, st);
     return (int)e;
   }
   k_qeq_block<<<w.S, 1024, 0, st>>>(w, ff);

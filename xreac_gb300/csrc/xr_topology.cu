@@ -62,11 +62,11 @@ __device__ inline int classify(const XrWork& w, const XrSystem& S, int i, int j,
   const float vz = pj.z - pi.z + ((float)s0 * S.cellf[2] + (float)s1 * S.cellf[5] + (float)s2 * S.cellf[8]);
   const float r2 = vx * vx + vy * vy + vz * vz;
   const float mg = S.margin;
-  const float rc2f = (float)S.rc2;
+  const float rc2f = S.rc2f;
   if (r2 > rc2f + mg) return 0;
   const int sx = s0 - wj.x + wi.x, sy = s1 - wj.y + wi.y, sz = s2 - wj.z + wi.z;
   if (j == i && sx == 0 && sy == 0 && sz == 0) return 0;
-  const float bc2f = (float)(S.bond_cut * S.bond_cut), hc2f = (float)(S.hb_cut * S.hb_cut);
+  const float bc2f = S.bc2f, hc2f = S.hc2f;
   bool bond, hb;
   const bool exact = (r2 >= rc2f - mg) || (fabsf(r2 - bc2f) <= mg) || (fabsf(r2 - hc2f) <= mg) || (r2 < 1.0e-2f);
   if (exact) {
