@@ -124,6 +124,25 @@ int xr_last_transfer_bytes(const xr_ctx* ctx, long long* h2d, long long* d2h);
 int xr_ctx_set_profiling(xr_ctx* ctx, int enable);
 int xr_ctx_stage_times(const xr_ctx* ctx, double* ms, int n, long long* calls);
 
+/* Allocation-free neighbour counting (no counterpart in the reference, which always allocates
+ * through NumPy). For callers that cannot allocate device memory where they need the count: a
+ * process whose device memory belongs to a framework's pool allocator, a step loop that cannot
+ * take the device-wide synchronisation of cudaFree, or a caller sizing its own neighbour buffers.
+ * Writes counts[a] = number of directed neighbours (j, S) of atom a with |x_j - x_a + S @ cell|
+ * <= cutoff, zero-shift self pairs excluded -- the row lengths of xr_get_neighbors's list for the
+ * same cutoff -- and *total (may be NULL) = their sum. positions, cell and counts are HOST
+ * pointers; types is not read. Work is issued on `stream` (a cudaStream_t, NULL = default stream),
+ * which the call synchronises before returning.
+ * All device scratch is one static array of the library: no cudaMalloc, cudaFree or allocating
+ * library call. natoms above XR_STATIC_MAX_ATOMS is rejected with XR_ECAPACITY. Calls that overlap
+ * in time on one device (two threads, or unordered streams) race on the shared scratch. The first
+ * call on a device performs the set-up (a cudaGetSymbolAddress with that device current); make it
+ * before any stream capture begins. xr_static_last_error() gives the message of this thread's last
+ * failed call. */
+#define XR_STATIC_MAX_ATOMS 16384
+int xr_count_neighbors_static(const xr_system* sys, double cutoff, void* stream, int* counts, long long* total);
+const char* xr_static_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif

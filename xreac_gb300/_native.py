@@ -45,7 +45,11 @@ EXPORTED = (
     "xr_ctx_stage_times",
     "xr_last_transfer_bytes",
     "xr_last_qeq_iterations",
+    "xr_count_neighbors_static",
+    "xr_static_last_error",
 )
+
+XR_STATIC_MAX_ATOMS = 16384
 
 
 class System(ctypes.Structure):
@@ -120,6 +124,10 @@ def load():
     lib.xr_last_transfer_bytes.restype = c_int
     lib.xr_last_qeq_iterations.argtypes = [c_void_p]
     lib.xr_last_qeq_iterations.restype = c_int
+    lib.xr_count_neighbors_static.argtypes = [POINTER(System), c_double, c_void_p, POINTER(c_int), POINTER(c_longlong)]
+    lib.xr_count_neighbors_static.restype = c_int
+    lib.xr_static_last_error.argtypes = []
+    lib.xr_static_last_error.restype = c_char_p
     _LIB = lib
     return lib
 
