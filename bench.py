@@ -11,7 +11,7 @@ QEq charges, the 14 energy components and fixed-charge forces.
   the flush outside the events.
 - ``e2e``: the public ``Calculator.evaluate`` with host numpy arrays: host->device copy of the
   inputs, device->host copy of energy, forces, charges and bond properties every step.
-- ``roofline``: the dominant stage's algorithmic bytes / live CUDA-event time against the
+- ``roofline``: the dominant kernel's (QEq) algorithmic bytes / live CUDA-event time against the
   measured HBM copy bandwidth; ``cpu_baseline``: the CPU oracle on the host cores.
 
 ``--impl reference`` times the CPU oracle (the reference's algorithm restated for the CPU) on the
@@ -45,7 +45,88 @@ def peaks():
         return {}
 
 
-class ClockSampler:
+class NvmlClockSampler:
+    """SM clock and clock-event reasons polled through NVML (ctypes) every few ms during the timed
+    region; read-only queries. Falls back to ``nvidia-smi -lms 200`` when NVML cannot be loaded."""
+
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown",
+               0x80: "hw_power_brake_slowdown"}
+
+    def __init__(self, device=0, period_s=0.002):
+        self.device = device
+        self.period = period_s
+        self.sm, self.reasons, self.max_mhz = [], set(), None
+        self.lib = self.handle = None
+        self.stop = threading.Event()
+        self.thread = None
+        self.fallback = None
+
+    def _open(self):
+        import ctypes
+
+        lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if lib.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        handle = ctypes.c_void_p()
+        bus = None
+        try:
+            import torch
+
+            pr = torch.cuda.get_device_properties(self.device)
+            bus = f"{pr.pci_domain_id:08X}:{pr.pci_bus_id:02X}:{pr.pci_device_id:02X}.0"
+        except Exception:
+            bus = None
+        ok = bus is not None and lib.nvmlDeviceGetHandleByPciBusId_v2(bus.encode(), ctypes.byref(handle)) == 0
+        if not ok and lib.nvmlDeviceGetHandleByIndex_v2(self.device, ctypes.byref(handle)) != 0:
+            raise OSError("no NVML handle")
+        mx = ctypes.c_uint()
+        if lib.nvmlDeviceGetMaxClockInfo(handle, 1, ctypes.byref(mx)) == 0:
+            self.max_mhz = float(mx.value)
+        self.lib, self.handle = lib, handle
+
+    def _poll(self):
+        import ctypes
+
+        clk = ctypes.c_uint()
+        rs = ctypes.c_ulonglong()
+        get_reasons = getattr(self.lib, "nvmlDeviceGetCurrentClocksEventReasons", None)
+        while not self.stop.is_set():
+            if self.lib.nvmlDeviceGetClockInfo(self.handle, 1, ctypes.byref(clk)) == 0:
+                self.sm.append(float(clk.value))
+            if get_reasons is not None and get_reasons(self.handle, ctypes.byref(rs)) == 0:
+                for bit, name in self.REASONS.items():
+                    if rs.value & bit:
+                        self.reasons.add(name)
+            time.sleep(self.period)
+
+    def __enter__(self):
+        try:
+            self._open()
+        except Exception:
+            self.fallback = SmiClockSampler(self.device).__enter__()
+            return self
+        self.thread = threading.Thread(target=self._poll, daemon=True)
+        self.thread.start()
+        return self
+
+    def __exit__(self, *exc):
+        if self.fallback is not None:
+            return self.fallback.__exit__(*exc)
+        self.stop.set()
+        if self.thread is not None:
+            self.thread.join(timeout=2)
+
+    def summary(self):
+        if self.fallback is not None:
+            return self.fallback.summary()
+        if not self.sm:
+            return {"sm_mhz": None, "sm_max_mhz": self.max_mhz, "reasons": sorted(self.reasons), "samples": 0,
+                    "source": "nvml"}
+        return {"sm_mhz": statistics.median(self.sm), "sm_max_mhz": self.max_mhz or max(self.sm),
+                "reasons": sorted(self.reasons), "samples": len(self.sm), "source": "nvml"}
+
+
+class SmiClockSampler:
     """nvidia-smi clock and throttle-reason samples during the timed region."""
 
     def __init__(self, index=0):
@@ -97,8 +178,22 @@ class ClockSampler:
                 if v.strip().lower() == "active":
                     reasons.add(name)
         if not sm:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0, "source": "nvidia-smi"}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm),
+                "source": "nvidia-smi"}
+
+
+def profiled_traffic(kernel):
+    """DRAM bytes per launch of ``kernel`` recorded from an ``ncu`` capture in profiles/traffic.txt."""
+    path = ROOT / "profiles" / "traffic.txt"
+    try:
+        for line in path.read_text().splitlines():
+            parts = line.split()
+            if len(parts) >= 2 and parts[0] == kernel:
+                return float(parts[1])
+    except OSError:
+        pass
+    return None
 
 
 def dist_setup():
@@ -251,7 +346,7 @@ def main():
     if dist is not None:
         dist.barrier()
     torch.cuda.synchronize()
-    with ClockSampler(local) as clocks:
+    with NvmlClockSampler(local) as clocks:
         t_wall = time.perf_counter()
         for k in range(args.steps):
             flush.fill_(float(k))
@@ -292,32 +387,36 @@ def main():
     lib.xr_last_transfer_bytes(calc._ctx.handle, ctypes.byref(h2d), ctypes.byref(d2h))
     e2e_value = world * n * e2e_steps / e2e_s
 
-    # roofline of the dominant stage, from live CUDA-event times
+    # Roofline of the dominant kernel (the QEq solve, one k_qeq_grid launch per evaluation, timed
+    # alone between the stage events on the library stream). Algorithmic bytes per launch: a
+    # matrix-free mat-vec reads 8 B per unordered pair and 16 B per atom per CG iteration.
     pk = peaks()
     dominant = max(stages, key=stages.get)
     nb_count = ctypes.c_longlong()
     lib.xr_get_neighbors(ctx.handle, 0, None, None, None, 0, ctypes.byref(nb_count))
     m_half = nb_count.value // 2
-    # Algorithmic HBM bytes per evaluation of each stage (minimal traffic: inputs read once,
-    # outputs written once): pairs 8 B per half pair (index + image code) + 76 B per atom;
-    # QEq matrix-vector products 8 B per half pair + 16 B per atom per CG iteration is not
-    # counted here (the iteration count is not exported); the pair stage is reported.
-    alg_bytes = {"pairs_vdw_shield": 8 * m_half + 76 * n}
-    rstage = "pairs_vdw_shield"
-    achieved = alg_bytes[rstage] / (stages[rstage] / 1e3) / 1e9
     hbm_peak = float(pk.get("hbm_gbs", 6800.0))
+    peak_source = "MEASURED_PEAKS.json hbm_gbs (burst copy)" if "hbm_gbs" in pk else "fallback 6800 GB/s"
+    qeq_bytes = (8 * m_half + 16 * n) * max(qeq_iterations, 1)
+    qeq_achieved = qeq_bytes / (stages["qeq_cg"] / 1e3) / 1e9
     roofline = {
         "bound": "hbm",
-        "kernel": "k_pairs + k_hval (pair stage)",
-        "achieved": achieved,
+        "kernel": "k_qeq_grid",
+        "achieved": qeq_achieved,
         "peak": hbm_peak,
         "unit": "GB/s",
-        "frac": achieved / hbm_peak,
-        "traffic": None,
-        "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in pk else "fallback 6800 GB/s",
-        "note": "FP64-issue bound, not HBM bound: see fp64 below and DESIGN.md",
+        "frac": qeq_achieved / hbm_peak,
+        "traffic": profiled_traffic("k_qeq_grid"),
+        "algorithmic_bytes_per_launch": qeq_bytes,
+        "peak_source": peak_source,
         "dominant_stage": dominant,
+        "note": "latency/FP64-bound: CG iterations are separated by grid barriers; matrix rows stay on chip",
     }
+    pair_bytes = 8 * m_half + 76 * n
+    pair_achieved = pair_bytes / (stages["pairs_vdw_shield"] / 1e3) / 1e9
+    roofline_pairs = {"bound": "hbm", "kernel": "k_pairs + k_hval", "achieved": pair_achieved, "peak": hbm_peak,
+                      "unit": "GB/s", "frac": pair_achieved / hbm_peak, "traffic": profiled_traffic("k_pairs"),
+                      "algorithmic_bytes_per_launch": pair_bytes}
     clk = clocks.summary()
     line = {
         "metric": METRIC,
@@ -336,6 +435,7 @@ def main():
                    "parallelism": "replicas" if world > 1 else "single",
                    "l2": "flushed before every step (256 MiB write, outside the timed events)"},
         "roofline": roofline,
+        "roofline_pairs": roofline_pairs,
         "stages_ms": stages,
         "clocks": clk,
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d.value),

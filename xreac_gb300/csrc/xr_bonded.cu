@@ -653,26 +653,31 @@ __global__ void k_torsions(XrWork w, XrFF ff) {
   }
 }
 
-// Hydrogen bonds, one warp per hydrogen (src/xreac/energy.py:248-276). The hydrogen's donors
-// (active bonds to a heavy atom with bo >= 0.01) are gathered once into a per-warp shared list; the
-// lanes then take acceptor edges of its full row (heavy neighbour within min(7.5, cutoff)) and pair
-// each with every donor except the same edge. Donor sensitivities accumulate in shared memory.
 constexpr int kHbWarps = 4;
 constexpr int kHbDonors = 4;
+constexpr int kHbBuf = 64;  // per-warp acceptor candidates: at most 31 left over + 32 new
 struct HbDonor {
   double v[3];
-  double r, bo;
+  double ird, bo;  // 1 / |donor bond|, bond order
   int b, jd, td;
   uint32_t shift;
 };
 
+// Hydrogen bonds (src/xreac/energy.py:248-276), one warp per hydrogen (p_hbond = 1). Donors are the
+// H's active bonds to p_hbond = 2 atoms with bo >= 0.01 (held in shared memory); acceptors are its
+// edges within the H-bond cutoff to p_hbond = 2 atoms, other than the donor's own image. The warp
+// first compacts the acceptor candidates of its row into shared memory with ballots, then gives
+// each lane one candidate, so the FP64 work runs on full warps (an FP64 instruction costs the pipe
+// the same for one active lane as for 32). Reciprocals are formed once per acceptor, per donor and
+// per parameter row instead of once per (donor, acceptor) pair.
 __global__ void k_hbonds(XrWork w, XrFF ff) {
   __shared__ HbDonor don[kHbWarps][kHbDonors];
+  __shared__ int2 cand[kHbWarps][kHbBuf];
   const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
   const int h = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
   if (h >= w.A) return;
   const int th = w.type[h], T = ff.ntypes;
-  if ((int)atom_prm(ff, th, A_P_HBOND) != 1) {
+  if (__ldg(ff.hb_role + th) != 1) {
     if (lane == 0) AEV(5, h) = 0.0;
     return;
   }
@@ -680,6 +685,8 @@ __global__ void k_hbonds(XrWork w, XrFF ff) {
   const XrSystem& S = w.sys[w.sys_of[h]];
   const double4_32a xh = w.x[h];
   const int abeg = w.cnt[3 * L + h], na = w.nact[h];
+  const int ebeg = w.cnt[0 * L + h], eend = w.cnt[0 * L + h + 1];
+  const unsigned lt = (1u << lane) - 1u;
   double E = 0;
   double gh[3] = {0, 0, 0};
   // Donor batches of up to kHbDonors (normally one batch holds them all).
@@ -690,12 +697,12 @@ __global__ void k_hbonds(XrWork w, XrFF ff) {
     if (t < na) {
       en = w.arow[abeg + t];
       const int jd = bond_other(w, en.x, en.y);
-      is_donor = (int)atom_prm(ff, w.type[jd], A_P_HBOND) == 2 && BFV(BF_BO, en.x) >= HBOND_THRESHOLD;
+      is_donor = __ldg(ff.hb_role + w.type[jd]) == 2 && BFV(BF_BO, en.x) >= HBOND_THRESHOLD;
     }
     unsigned msk = __ballot_sync(0xffffffffu, is_donor);
     while (msk) {
       const int nd = min(__popc(msk), kHbDonors);
-      const int rank = __popc(msk & ((1u << lane) - 1u));
+      const int rank = __popc(msk & lt);
       const bool mine = (msk >> lane & 1u) && rank < nd;
       if (mine) {
         HbDonor& d = don[wl][rank];
@@ -705,21 +712,26 @@ __global__ void k_hbonds(XrWork w, XrFF ff) {
         d.shift = bond_shift(w, en.x, en.y);
         d.bo = BFV(BF_BO, en.x);
         bond_vec(w, en.x, en.y, d.v);
-        d.r = w.b_r[en.x];
+        d.ird = 1.0 / w.b_r[en.x];
       }
       for (int q = 0; q < nd; ++q) msk &= msk - 1u;
       __syncwarp();
-      // per-lane donor accumulators (registers; fixed indices after unrolling)
+      // per-lane donor accumulators (registers; fixed indices after unrolling) and per-lane caches
+      // of the last parameter row's constants and of exp(-hb2 bo) per donor
       double acc[kHbDonors][4];
+      double eb_k[kHbDonors];
+      int ebrow_k[kHbDonors];
 #pragma unroll
-      for (int k = 0; k < kHbDonors; ++k) acc[k][0] = acc[k][1] = acc[k][2] = acc[k][3] = 0.0;
-      for (int e = w.cnt[0 * L + h] + lane; e < w.cnt[0 * L + h + 1]; e += 32) {
-        const int2 ed = w.edge[e];
-        const uint32_t code = (uint32_t)ed.y;
-        if (!(code & XR_CODE_HB)) continue;
+      for (int k = 0; k < kHbDonors; ++k) {
+        acc[k][0] = acc[k][1] = acc[k][2] = acc[k][3] = 0.0;
+        eb_k[k] = 0.0;
+        ebrow_k[k] = -1;
+      }
+      int crow = -1;
+      double r0 = 0, ir0 = 0, hb1 = 0, hb2 = 0, hb3 = 0;
+      auto process = [&](int2 ed) {
         const int ja = ed.x, ta = w.type[ja];
-        if ((int)atom_prm(ff, ta, A_P_HBOND) != 2) continue;
-        const uint32_t sa = code & XR_SHIFT_MASK;
+        const uint32_t sa = (uint32_t)ed.y & XR_SHIFT_MASK;
         double va[3];
         {
           const double4_32a xa = w.x[ja];
@@ -732,6 +744,7 @@ __global__ void k_hbonds(XrWork w, XrFF ff) {
           }
         }
         const double ra = sqrt(va[0] * va[0] + va[1] * va[1] + va[2] * va[2]);
+        const double ira = 1.0 / ra, ira2 = ira * ira;
         double ga[3] = {0, 0, 0};
 #pragma unroll
         for (int k = 0; k < kHbDonors; ++k) {
@@ -740,32 +753,69 @@ __global__ void k_hbonds(XrWork w, XrFF ff) {
           if (d.jd == ja && d.shift == sa) continue;  // same edge
           const int row = __ldg(ff.hbond_index + (d.td * T + th) * T + ta);
           if (row < 0) continue;
-          const double* prm = ff.hbond + 4 * row;
-          const double r0 = __ldg(prm + 0), hb1 = __ldg(prm + 1), hb2 = __ldg(prm + 2), hb3 = __ldg(prm + 3);
+          if (row != crow) {
+            const double* prm = ff.hbond + 4 * row;
+            r0 = __ldg(prm + 0);
+            hb1 = __ldg(prm + 1);
+            hb2 = __ldg(prm + 2);
+            hb3 = __ldg(prm + 3);
+            ir0 = 1.0 / r0;
+            crow = row;
+          }
           if (!(r0 > 0)) continue;
-          const double rd = d.r;
-          const double cosv = (d.v[0] * va[0] + d.v[1] * va[1] + d.v[2] * va[2]) / (rd * ra);
+          if (ebrow_k[k] != row) {
+            eb_k[k] = exp(-hb2 * d.bo);
+            ebrow_k[k] = row;
+          }
+          const double eb = eb_k[k];
+          const double inv = d.ird * ira;
+          const double cosv = (d.v[0] * va[0] + d.v[1] * va[1] + d.v[2] * va[2]) * inv;
           const double cc = fmin(fmax(cosv, -1.0), 1.0);
-          const double sin4 = 0.25 * (1 - cc) * (1 - cc);
-          const double eb = exp(-hb2 * d.bo);
+          const double omc = 1 - cc;
+          const double sin4 = 0.25 * omc * omc;
           const double Fb = hb1 * (1 - eb);
-          const double E2 = exp(-hb3 * (r0 / ra + ra / r0 - 2));
-          E += Fb * E2 * sin4;
+          const double E2 = exp(-hb3 * (r0 * ira + ra * ir0 - 2));
+          const double FE = Fb * E2;
+          E += FE * sin4;
           acc[k][3] += hb1 * hb2 * eb * E2 * sin4;
-          const double dE_dr = Fb * E2 * sin4 * (-hb3) * (-r0 / (ra * ra) + 1 / r0);
-          const double dE_dcos = (cosv > -1.0 && cosv < 1.0) ? Fb * E2 * (-0.5) * (1 - cc) : 0.0;
-          const double inv = 1.0 / (rd * ra);
+          const double dE_dr_over_r = FE * sin4 * (-hb3) * (ir0 - r0 * ira2) * ira;
+          const double dE_dcos = (cosv > -1.0 && cosv < 1.0) ? -0.5 * FE * omc : 0.0;
+          const double ird2 = d.ird * d.ird;
 #pragma unroll
           for (int c = 0; c < 3; ++c) {
-            const double gdc = dE_dcos * (va[c] * inv - cosv * d.v[c] / (rd * rd));
-            const double gac = dE_dcos * (d.v[c] * inv - cosv * va[c] / (ra * ra)) + dE_dr * va[c] / ra;
+            const double gdc = dE_dcos * (va[c] * inv - cosv * d.v[c] * ird2);
+            const double gac = dE_dcos * (d.v[c] * inv - cosv * va[c] * ira2) + dE_dr_over_r * va[c];
             acc[k][c] += gdc;
             ga[c] += gac;
             gh[c] -= gdc + gac;
           }
         }
         if (ga[0] != 0.0 || ga[1] != 0.0 || ga[2] != 0.0) atomic_add3(w.f, ja, ga[0], ga[1], ga[2]);
+      };
+      // acceptor candidates: compacted in row order, processed 32 at a time
+      int ncand = 0;
+      for (int e0 = ebeg; e0 < eend; e0 += 32) {
+        const int e = e0 + lane;
+        bool ok = false;
+        int2 ed = make_int2(0, 0);
+        if (e < eend) {
+          ed = w.edge[e];
+          ok = ((uint32_t)ed.y & XR_CODE_HB) && __ldg(ff.hb_role + w.type[ed.x]) == 2;
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, ok);
+        if (ok) cand[wl][ncand + __popc(m & lt)] = ed;
+        ncand += __popc(m);
+        __syncwarp();
+        if (ncand >= 32) {
+          process(cand[wl][lane]);
+          ncand -= 32;
+          const int2 moved = lane < ncand ? cand[wl][32 + lane] : make_int2(0, 0);
+          __syncwarp();
+          if (lane < ncand) cand[wl][lane] = moved;
+          __syncwarp();
+        }
       }
+      if (lane < ncand) process(cand[wl][lane]);
       // donor sensitivities: warp sums, then one update per donor
 #pragma unroll
       for (int k = 0; k < kHbDonors; ++k) {

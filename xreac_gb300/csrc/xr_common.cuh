@@ -98,6 +98,7 @@ struct XrFF {
   const double* pair_gw;      // [T*T] (1/gamma_w)^g28 for shielded vdW
   const double* pair_logr;    // [T*T][3] log(r_s), log(r_p), log(r_pp) (0 where unused)
   const int* is_carbon;       // [T] label is "C" (case-insensitive): C2 correction applies
+  const int* hb_role;         // [T] 1 hydrogen-bond hydrogen, 2 donor/acceptor (p_hbond), 0 otherwise
   const int* angle_index;     // [T^3][2] first, count
   const double* angle;        // [R][7]
   const int* torsion_index;   // [T^4] row or -1 (rows with a nonzero V1, V2, V3 or V_conj)

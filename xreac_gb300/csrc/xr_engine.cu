@@ -814,6 +814,12 @@ int xr_ff_create(const double* general, int ntypes, const double* atom, const do
   d.pair_gw = (const double*)up(gw.data(), sizeof(double) * T * T);
   d.pair_logr = (const double*)up(logr.data(), sizeof(double) * 3 * T * T);
   d.is_carbon = (const int*)up(is_carbon, sizeof(int) * T);
+  std::vector<int> hb_role(T);
+  for (int t = 0; t < T; ++t) {
+    const double ph = atom[t * XR_NATOM_COLS + A_P_HBOND];
+    hb_role[t] = ph == 1.0 ? 1 : (ph == 2.0 ? 2 : 0);  // the reference compares p_hbond exactly
+  }
+  d.hb_role = (const int*)up(hb_role.data(), sizeof(int) * T);
   d.angle_index = (const int*)up(angle_index, sizeof(int) * 2 * T * T * T);
   d.angle = (const double*)up(angle, sizeof(double) * 7 * (size_t)nangle);
   d.torsion_index = (const int*)up(torsion_index, sizeof(int) * (size_t)T * T * T * T);

@@ -3,11 +3,11 @@
 // - Taper, shielded Coulomb kernel and tapered vdW (shielding and/or inner core) restate
 //   src/xreac/energy.py:89-92 and 213-219; each unordered image pair is evaluated once and counts
 //   for both of xreac's directed edges.
-// - QEq restates the KKT system of src/xreac/energy.py:95-102 as the two symmetric positive-definite
-//   systems H s = -chi and H t = -1 (H = 14.4 * sum of shields + diag(eta), self images on the
-//   diagonal), solved together by Jacobi-preconditioned conjugate gradients, with
-//   q = s + ((Q - sum s) / sum t) t. Matrix rows are gathered from the full directed neighbour
-//   rows, so a matrix-vector product needs no atomics and is deterministic.
+// - QEq restates the KKT system of src/xreac/energy.py:95-102 (H = 14.4 * sum of shields +
+//   diag(eta), self images on the diagonal, sum q = Q) and solves it by Jacobi-preconditioned
+//   conjugate gradients projected onto sum q = Q (one solve; Gould, Hribar and Nocedal's projected
+//   CG). Matrix rows are gathered from the full directed neighbour rows, so a matrix-vector product
+//   needs no atomics and is deterministic.
 // - A single large system runs the solver as one cooperative grid with a barrier whose every wait
 //   is bounded; batches of systems give each system one thread block.
 #include "xr_common.cuh"
@@ -136,67 +136,36 @@ __device__ bool grid_barrier(unsigned* bar, unsigned target, int* status) {
   return ok;
 }
 
-// Block sum of NV values held by lane 0 of each warp (other lanes' values are ignored); warp 0 adds
-// the per-warp values and the result is broadcast to all threads. FP64 issues at 2 per cycle per SM
-// on this part, so the adds are kept to one warp.
-template <int NV>
-__device__ inline void block_sum(double* v, double* smem) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  if (lane == 0)
-    for (int k = 0; k < NV; ++k) smem[k * 32 + wid] = v[k];
-  __syncthreads();
-  if (wid == 0) {
-    for (int k = 0; k < NV; ++k) {
-      double s = lane < nw ? smem[k * 32 + lane] : 0.0;
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-      if (lane == 0) smem[128 + k] = s;
-    }
-  }
-  __syncthreads();
-  for (int k = 0; k < NV; ++k) v[k] = smem[128 + k];
-  __syncthreads();
-}
-
 // Team: the whole cooperative grid on one system, or one block on one system of a batch.
+// Results of a reduction land in one of two result slots (by the parity of `slot`), so a reduction
+// may write its totals while a slow warp still reads the previous reduction's.
+__device__ inline double* result_slot(double* smem, int slot) { return smem + 128 + 4 * (slot & 1); }
+
 struct GridTeam {
   mutable unsigned target = 0;  // barrier episodes so far times the number of blocks
   __device__ bool sync(const XrWork& w) const {
     target += gridDim.x;
     return grid_barrier(w.barrier, target, w.status);
   }
-  // Sum NV values (held by lane 0 of each warp) over the grid, fused with the barrier: warp 0 adds
-  // the block's warps, lane 0 publishes the block partial and arrives (release), then warp 0 adds
-  // all blocks' partials in a fixed order (deterministic) and broadcasts them.
-  template <int NV>
-  __device__ bool sum(const XrWork& w, double* v, double* smem, int slot) const {
-    return sum<NV>(w, v, smem, slot, [](double*) {});
-  }
-  // As sum(), with post(values) run by thread 0 on the totals before they are shared, so scalar
-  // work derived from a reduction costs no extra block synchronisation.
+  // Grid-wide sum of NV block totals held by lane 0 of warp 0, fused with the barrier: lane 0
+  // publishes the block's values into a fixed slot and arrives (release); after the bounded wait
+  // warp 0 adds all blocks' values in block order (deterministic), thread 0 runs post() on the
+  // totals (scalar work that then costs no extra synchronisation), and every thread receives them.
   template <int NV, class Post>
-  __device__ bool sum(const XrWork& w, double* v, double* smem, int slot, Post post) const {
+  __device__ bool reduce(const XrWork& w, double* v, double* smem, int slot, Post post) const {
     static_assert(NV <= 4, "at most four values per reduction");
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
     __shared__ int ok;
-    if (lane == 0)
-      for (int k = 0; k < NV; ++k) smem[k * 32 + wid] = v[k];
-    __syncthreads();
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     target += gridDim.x;
+    double* res = result_slot(smem, slot);
     // Fixed-size slots; consecutive reductions never share one, so a block may publish the next
     // partials while a slower block still reads the previous ones.
     double* red = w.red + (size_t)slot * 4 * gridDim.x;
     if (wid == 0) {
-      double s[NV];
-      for (int k = 0; k < NV; ++k) {
-        double t = lane < nw ? smem[k * 32 + lane] : 0.0;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-        s[k] = t;
-      }
       int good = 1;
+      __syncwarp();  // orders warp 0's row writes before lane 0's release
       if (lane == 0) {
-        for (int k = 0; k < NV; ++k) red[k * gridDim.x + blockIdx.x] = s[k];
+        for (int k = 0; k < NV; ++k) red[k * gridDim.x + blockIdx.x] = v[k];
         asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(w.barrier) : "memory");
         long long it = 0;
         while (ld_acquire(w.barrier) < target) {
@@ -215,12 +184,12 @@ struct GridTeam {
         for (unsigned q = lane; q < gridDim.x; q += 32) t += __ldcg(red + k * gridDim.x + q);
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-        if (lane == 0) smem[128 + k] = t;
+        if (lane == 0) res[k] = t;
       }
-      if (lane == 0) post(smem + 128);
+      if (lane == 0) post(res);
     }
     __syncthreads();
-    for (int k = 0; k < NV; ++k) v[k] = smem[128 + k];
+    for (int k = 0; k < NV; ++k) v[k] = res[k];
     return ok;
   }
 };
@@ -230,35 +199,51 @@ struct BlockTeam {
     __syncthreads();
     return true;
   }
-  template <int NV>
-  __device__ bool sum(const XrWork&, double* v, double* smem, int) const {
-    block_sum<NV>(v, smem);
-    return true;
-  }
   template <int NV, class Post>
-  __device__ bool sum(const XrWork&, double* v, double* smem, int, Post post) const {
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    if (lane == 0)
-      for (int k = 0; k < NV; ++k) smem[k * 32 + wid] = v[k];
-    __syncthreads();
-    if (wid == 0) {
-      for (int k = 0; k < NV; ++k) {
-        double s = lane < nw ? smem[k * 32 + lane] : 0.0;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if (lane == 0) smem[128 + k] = s;
-      }
-      if (lane == 0) post(smem + 128);
+  __device__ bool reduce(const XrWork&, double* v, double* smem, int slot, Post post) const {
+    double* res = result_slot(smem, slot);
+    if (threadIdx.x == 0) {
+      for (int k = 0; k < NV; ++k) res[k] = v[k];
+      post(res);
     }
     __syncthreads();
-    for (int k = 0; k < NV; ++k) v[k] = smem[128 + k];
-    __syncthreads();
+    for (int k = 0; k < NV; ++k) v[k] = res[k];
     return true;
   }
 };
 
-// Rows [r0, r1) of the system starting at atom a0 belong to this block; warps take rows in turn.
-// When `cache` is non-null the block's matrix rows (column, H'_ij) are kept in shared memory.
+// Team sum of NV values held by lane 0 of every warp: warp 0 first adds the block's warps.
+template <int NV, class Team, class Post>
+__device__ bool team_sum(const Team& team, const XrWork& w, double* v, double* smem, int slot, Post post) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if (lane == 0)
+    for (int k = 0; k < NV; ++k) smem[k * 32 + wid] = v[k];
+  __syncthreads();
+  if (wid == 0)
+    for (int k = 0; k < NV; ++k) {
+      double t = lane < nw ? smem[k * 32 + lane] : 0.0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+      v[k] = t;
+    }
+  return team.template reduce<NV>(w, v, smem, slot, post);
+}
+
+// Warp-0 sum of a per-lane value (the block total ends in every lane of warp 0).
+__device__ inline double warp_total(double t) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  return t;
+}
+
+// Rows [r0, r1) of the system starting at atom a0 belong to this block. The matrix-vector product
+// runs on tiles of 32 rows, one row per warp; the lanes' partial row sums are transposed through
+// shared memory so that one warp owns the 32 rows of a tile, one row per lane, for the row
+// reductions and every per-row scalar update. On this part an FP64 instruction costs the FP64 pipe
+// the same whether one lane or 32 are active, so scalar row work done by lane 0 of 32 warps would
+// cost 32 times the issue slots of the same work spread over the lanes of one warp.
+// When `cache_j` is non-null the block's matrix rows (column, H'_ij) are kept in shared memory;
+// when `gstage` is non-null the whole gradient is staged in shared memory every iteration.
 template <class Team>
 __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int a0, int n, int r0, int r1,
                           double Q, double* smem, unsigned short* cache_j, double* cache_h, int cache_cap,
@@ -271,6 +256,7 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
   double* HP = &QW(Q_HP, 0);
   double* DI = &QW(Q_DINV, 0);
   double* Cr = &QW(Q_C, 0);
+  auto noop = [](double*) {};
   // 1. Jacobi diagonal (eta + self-image shields) of the owned rows.
   for (int r = r0 + wid; r < r1; r += nw) {
     const int a = a0 + r;
@@ -323,9 +309,8 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
       acc[2] += di * g * g;
     }
   }
-  if (!team.template sum<3>(w, acc, smem, 0)) return;
-  // Iteration scalars are computed by thread 0 alone and shared: FP64 divisions replicated over a
-  // thousand threads would cost more FP64 issue slots than the matrix-vector product.
+  if (!team_sum<3>(team, w, acc, smem, 0, noop)) return;
+  // Iteration scalars are computed by thread 0 alone (in the reductions' post hooks) and shared.
   __shared__ double sc_lam, sc_alpha, sc_step, sc_beta;
   __shared__ int sc_state;  // 0 iterate, 1 converged, 2 stop
   const double s1 = acc[0];
@@ -341,19 +326,21 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
     // start that is exact by symmetry).
     sc_state = (!(gz0 > gfloor) || n < 2) ? 1 : 0;
   }
-  __syncthreads();
-  // One row per warp (the usual grid layout): the row's solver state lives in shared memory.
+  // Tile transposition buffers and, for blocks of at most 32 rows (the grid layout), the rows'
+  // solver state, indexed by lane = row - r0.
+  __shared__ double part[32][33];
+  __shared__ double part4[4][32];
   __shared__ double rs_x[32], rs_p[32], rs_hp[32], rs_di[32], rs_c[32], rs_eta[32], rs_g[32];
-  const bool row_smem = (r1 - r0) <= nw && nw <= 32;
-  if (row_smem && lane == 0 && r0 + wid < r1) {
-    const int a = a0 + r0 + wid;
-    rs_x[wid] = X[a];
-    rs_p[wid] = 0.0;
-    rs_hp[wid] = 0.0;
-    rs_di[wid] = DI[a];
-    rs_c[wid] = Cr[a];
-    rs_eta[wid] = atom_prm(ff, w.type[a], A_ETA);
-    rs_g[wid] = G[a];
+  const bool row_smem = (r1 - r0) <= 32;
+  if (row_smem && wid == 0 && r0 + lane < r1) {
+    const int a = a0 + r0 + lane;
+    rs_x[lane] = X[a];
+    rs_p[lane] = 0.0;
+    rs_hp[lane] = 0.0;
+    rs_di[lane] = DI[a];
+    rs_c[lane] = Cr[a];
+    rs_eta[lane] = atom_prm(ff, w.type[a], A_ETA);
+    rs_g[lane] = G[a];
   }
   __syncthreads();
   int it = 0;
@@ -369,43 +356,55 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
       for (int q = threadIdx.x; q < n; q += blockDim.x) gstage[q] = __ldcg(G + a0 + q);
       __syncthreads();
     }
-    double pHp[2] = {0.0, 0.0};  // p'Hp and <D^-1, Hp>
-    for (int r = r0 + wid; r < r1; r += nw) {
-      const int a = a0 + r;
+    double pHp[2] = {0.0, 0.0};  // lane partials in warp 0: p'Hp and <D^-1, Hp>
+    for (int tb = r0; tb < r1; tb += 32) {
+      const int r = tb + wid;
       double hz = 0;
-      const int eb = w.cnt[a], ee = w.cnt[a + 1];
-      if (cached && gstage) {
-        for (int e = eb + lane; e < ee; e += 32) hz += cache_h[e - ebeg] * gstage[cache_j[e - ebeg]];
-      } else if (cached) {
-        for (int e = eb + lane; e < ee; e += 32) hz += cache_h[e - ebeg] * __ldcg(G + a0 + cache_j[e - ebeg]);
-      } else {
-        double h0 = 0, h1 = 0;
-        int e = eb + lane;
-        for (; e + 32 < ee; e += 64) {
-          const double g0 = __ldcg(G + w.edge[e].x), g1 = __ldcg(G + w.edge[e + 32].x);
-          h0 += w.hval[e] * g0;
-          h1 += w.hval[e + 32] * g1;
+      if (wid < 32 && r < r1) {
+        const int a = a0 + r;
+        const int eb = w.cnt[a], ee = w.cnt[a + 1];
+        if (cached && gstage) {
+          for (int e = eb + lane; e < ee; e += 32) hz += cache_h[e - ebeg] * gstage[cache_j[e - ebeg]];
+        } else if (cached) {
+          for (int e = eb + lane; e < ee; e += 32) hz += cache_h[e - ebeg] * __ldcg(G + a0 + cache_j[e - ebeg]);
+        } else {
+          double h0 = 0, h1 = 0;
+          int e = eb + lane;
+          for (; e + 32 < ee; e += 64) {
+            const double g0 = __ldcg(G + w.edge[e].x), g1 = __ldcg(G + w.edge[e + 32].x);
+            h0 += w.hval[e] * g0;
+            h1 += w.hval[e + 32] * g1;
+          }
+          if (e < ee) h0 += w.hval[e] * __ldcg(G + w.edge[e].x);
+          hz = h0 + h1;
         }
-        if (e < ee) h0 += w.hval[e] * __ldcg(G + w.edge[e].x);
-        hz = h0 + h1;
       }
+      if (wid < 32) part[wid][lane] = hz;
+      __syncthreads();
+      if (wid < 4) {  // lane = row of the tile; warp k adds lanes 8k .. 8k+7 of the row's partials
+        double s = part[lane][8 * wid];
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) hz += __shfl_xor_sync(0xffffffffu, hz, o);
-      if (lane == 0) {
-        const double ga = row_smem ? rs_g[wid] : (gstage ? gstage[r] : G[a]);
-        const double di = row_smem ? rs_di[wid] : DI[a];
-        const double eta = row_smem ? rs_eta[wid] : atom_prm(ff, w.type[a], A_ETA);
-        const double cr = row_smem ? rs_c[wid] : Cr[a];
-        const double p_old = row_smem ? rs_p[wid] : Pv[a];
-        const double hp_old = row_smem ? rs_hp[wid] : HP[a];
-        hz += eta * di * ga - lam * cr;
+        for (int k = 1; k < 8; ++k) s += part[lane][8 * wid + k];
+        part4[wid][lane] = s;
+      }
+      __syncthreads();
+      if (wid == 0 && tb + lane < r1) {
+        const int rr = tb + lane, a = a0 + rr;
+        double h = (part4[0][lane] + part4[1][lane]) + (part4[2][lane] + part4[3][lane]);
+        const double ga = row_smem ? rs_g[lane] : (gstage ? gstage[rr] : G[a]);
+        const double di = row_smem ? rs_di[lane] : DI[a];
+        const double eta = row_smem ? rs_eta[lane] : atom_prm(ff, w.type[a], A_ETA);
+        const double cr = row_smem ? rs_c[lane] : Cr[a];
+        const double p_old = row_smem ? rs_p[lane] : Pv[a];
+        const double hp_old = row_smem ? rs_hp[lane] : HP[a];
+        h += eta * di * ga - lam * cr;
         const double z = di * (ga - lam);
         const double p = -z + beta * p_old;
-        const double hp = -hz + beta * hp_old;
+        const double hp = -h + beta * hp_old;
         if (row_smem) {
-          rs_p[wid] = p;
-          rs_hp[wid] = hp;
-          rs_g[wid] = ga - lam;
+          rs_p[lane] = p;
+          rs_hp[lane] = hp;
+          rs_g[lane] = ga - lam;
         } else {
           Pv[a] = p;
           HP[a] = hp;
@@ -415,7 +414,11 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
         pHp[1] += di * hp;
       }
     }
-    if (!team.template sum<2>(w, pHp, smem, slot, [&](double* t) {
+    if (wid == 0) {
+      pHp[0] = warp_total(pHp[0]);
+      pHp[1] = warp_total(pHp[1]);
+    }
+    if (!team.template reduce<2>(w, pHp, smem, slot, [&](double* t) {
           if (!(t[0] > 0.0)) {
             // a vanishing direction after convergence to rounding level is not a failure
             if (!(gz <= 1e4 * gfloor)) atomicOr(w.status, XR_S_NONSPD);
@@ -428,18 +431,19 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
       return;
     slot = slot == 1 ? 2 : 1;
     if (sc_state != 0) break;
+    // Step: x += alpha p, g += alpha Hp - (multiplier change), one row per lane of warp 0.
     const double alpha = sc_alpha, step_lam = sc_step;
     double u[2] = {0, 0};
-    if (lane == 0) {
-      for (int r = r0 + wid; r < r1; r += nw) {
-        const int a = a0 + r;
+    if (wid == 0) {
+      for (int rr = r0 + lane; rr < r1; rr += 32) {
+        const int a = a0 + rr;
         if (row_smem) {
-          const double g = (rs_g[wid] + alpha * rs_hp[wid]) - step_lam;
-          rs_x[wid] += alpha * rs_p[wid];
-          rs_g[wid] = g;
+          const double g = (rs_g[lane] + alpha * rs_hp[lane]) - step_lam;
+          rs_x[lane] += alpha * rs_p[lane];
+          rs_g[lane] = g;
           G2[a] = g;  // published for the other rows' products
-          u[0] += rs_di[wid] * g;
-          u[1] += rs_di[wid] * g * g;
+          u[0] += rs_di[lane] * g;
+          u[1] += rs_di[lane] * g * g;
         } else {
           const double g = (G2[a] + alpha * HP[a]) - step_lam;
           X[a] += alpha * Pv[a];
@@ -449,8 +453,10 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
           u[1] += di * g * g;
         }
       }
+      u[0] = warp_total(u[0]);
+      u[1] = warp_total(u[1]);
     }
-    if (!team.template sum<2>(w, u, smem, slot, [&](double* t) {
+    if (!team.template reduce<2>(w, u, smem, slot, [&](double* t) {
           sc_lam = t[0] / s1;
           const double gz_new = t[1] - sc_lam * t[0];
           if (gz_new <= tol2 * gz0) sc_state = 1;
@@ -463,14 +469,14 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
     G = G2;
     G2 = tmp;
   }
-  if (row_smem && lane == 0 && r0 + wid < r1) X[a0 + r0 + wid] = rs_x[wid];
+  if (row_smem && wid == 0 && r0 + lane < r1) X[a0 + r0 + lane] = rs_x[lane];
   __syncthreads();
   if (threadIdx.x == 0) atomicMax(w.counts + 4, it);
   // Final charges; the constraint is restored exactly against accumulated rounding.
   double sx[1] = {0.0};
   if (lane == 0)
     for (int r = r0 + wid; r < r1; r += nw) sx[0] += X[a0 + r];
-  if (!team.template sum<1>(w, sx, smem, 3)) return;
+  if (!team_sum<1>(team, w, sx, smem, 3, noop)) return;
   const double shift = (Q - sx[0]) / n;
   for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
     const int a = a0 + r;
@@ -483,7 +489,7 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
 
 // Dynamic shared memory of the grid solver: [gradient stage: n doubles][row cache values][row cache
 // columns (16-bit, local to the system)]. The host sizes the two parts per launch.
-constexpr int kQeqMaxDyn = 220 * 1024;
+constexpr int kQeqMaxDyn = 208 * 1024;
 
 __global__ void __launch_bounds__(1024, 1) k_qeq_grid(XrWork w, XrFF ff, int stage_n, int cache_cap) {
   __shared__ double smem[4 * 32 + 8];  // reductions: per-warp inputs, then results at 128..
