@@ -189,7 +189,7 @@ def profiled_traffic(kernel):
     try:
         for line in path.read_text().splitlines():
             parts = line.split()
-            if len(parts) >= 2 and parts[0] == kernel:
+            if len(parts) >= 2 and parts[0] == kernel and not line.startswith("#"):
                 return float(parts[1])
     except OSError:
         pass
