@@ -17,6 +17,8 @@
 // Layout: bonds are half pairs (each unordered image pair once); dbrow lists, per atom, its
 // directed bond edges in canonical order as (bond id, +1 source / -1 target), so per-atom sums
 // are gathers in the reference's order and need no atomics.
+#include <algorithm>
+
 #include "xr_common.cuh"
 
 namespace {
@@ -341,56 +343,131 @@ __global__ void k_bond_energy(XrWork w, XrFF ff) {
   BEV(1, b) = e_c2;
 }
 
-// Valence angle, penalty and angle conjugation, one warp per centre atom; the lanes take the
-// pairs (left, right) of the centre's active bond-row entries, left before right in canonical
-// order (src/xreac/energy.py:278-318).
-__global__ void k_angles(XrWork w, XrFF ff) {
+// ---------------------------------------------------------------------------------------------
+// Many-body terms as compacted work items. A warp owns a chunk of kUnits units (valence centres or
+// torsion middles). It enumerates the units' (left, right) combinations, keeps those that pass the
+// cheap tests (bond-order product, parameter row), compacts them into shared memory with ballots
+// and evaluates them 32 at a time, one per lane. An FP64 instruction occupies this part's FP64 pipe
+// for the whole warp however few lanes are active, so a warp per centre (a handful of combinations)
+// would spend most of the pipe on idle lanes. Per-unit sums (energies, the unit's own adjoints and
+// force) are formed by a segmented warp reduction over the contiguous items of each unit, in lane
+// and pass order, so energies are deterministic; contributions to other atoms and bonds use atomics.
+constexpr int kUnits = 8;          // units per warp chunk
+constexpr int kItemBuf = 64;       // per-warp item buffer: at most 31 left over + 32 new
+constexpr int kBondedWarps = 4;    // warps per block of the item kernels
+
+__device__ inline uint32_t pack_item(int u, int a, int c) { return ((uint32_t)u << 28) | ((uint32_t)a << 14) | (uint32_t)c; }
+__device__ inline int item_unit(uint32_t it) { return (int)(it >> 28); }
+__device__ inline int item_a(uint32_t it) { return (int)((it >> 14) & 16383u); }
+__device__ inline int item_c(uint32_t it) { return (int)(it & 16383u); }
+
+// Segmented sum over lanes whose items belong to the same unit (items of a unit are contiguous in
+// lane order); the unit's first lane adds the sum into uacc[unit][*]. key < 0 marks an empty lane.
+template <int NV>
+__device__ inline void unit_sums(double (&v)[NV], int key, double* uacc) {
   const int lane = threadIdx.x & 31;
-  const int j = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
-  if (j >= w.A) return;
-  const int L = w.A + 1, T = ff.ntypes, tj = w.type[j];
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int ko = __shfl_down_sync(0xffffffffu, key, o);
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      const double t = __shfl_down_sync(0xffffffffu, v[k], o);
+      if (lane + o < 32 && ko == key) v[k] += t;
+    }
+  }
+  const int kp = __shfl_up_sync(0xffffffffu, key, 1);
+  if (key >= 0 && (lane == 0 || kp != key))
+#pragma unroll
+    for (int k = 0; k < NV; ++k) uacc[key * NV + k] += v[k];
+  __syncwarp();
+}
+
+// Appends the items flagged by `ok` to the warp's buffer and runs `process` on full batches of 32.
+template <class Proc>
+__device__ inline void push_items(uint32_t* buf, int& nbuf, bool ok, uint32_t item, Proc& process) {
+  const int lane = threadIdx.x & 31;
+  const unsigned m = __ballot_sync(0xffffffffu, ok);
+  if (ok) buf[nbuf + __popc(m & ((1u << lane) - 1u))] = item;
+  nbuf += __popc(m);
+  __syncwarp();
+  if (nbuf >= 32) {
+    process(buf[lane], true);
+    nbuf -= 32;
+    const uint32_t moved = lane < nbuf ? buf[32 + lane] : 0u;
+    __syncwarp();
+    if (lane < nbuf) buf[lane] = moved;
+    __syncwarp();
+  }
+}
+
+// Valence angle, penalty and coalition terms (src/xreac/energy.py:278-318 with the angle rule of
+// src/xreac/energy.py:49-55): units are centres j, items the pairs of j's active bonds.
+__global__ void __launch_bounds__(32 * kBondedWarps) k_angles(XrWork w, XrFF ff) {
+  constexpr int NC = 8, NV = 10;
+  __shared__ double ucon[kBondedWarps][kUnits][NC];
+  __shared__ double uacc[kBondedWarps][kUnits][NV];
+  __shared__ int ubeg[kBondedWarps][kUnits], ucnt[kBondedWarps][kUnits];
+  __shared__ uint32_t buf[kBondedWarps][kItemBuf];
+  const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+  const int chunk = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
+  const int j0 = chunk * kUnits;
+  if (j0 >= w.A) return;
+  const int nu = min(kUnits, w.A - j0);
+  const int L = w.A + 1, T = ff.ntypes;
   const double* g = ff.g;
-  const int beg = w.cnt[3 * L + j], m = w.nact[j];
-  const int npairs = m * (m - 1) / 2;
-  double E_ang = 0, E_pen = 0, E_coa = 0;
-  double A_sbo2 = 0, A_db = 0, A_d = 0, A_tj = 0;
-  double gj[3] = {0, 0, 0};
-  if (npairs > 0) {
+  const bool lammps = !w.full_derivative;
+  const double k180 = 3.14159265 / 180;
+  // unit constants, one centre per lane
+  if (lane < nu) {
+    const int j = j0 + lane, tj = w.type[j];
     const double total_j = AFV(AF_TOTAL, j);
     const double d_j = total_j - atom_prm(ff, tj, A_VALENCY);
-    const double db_j = total_j - atom_prm(ff, tj, A_VALENCY_BOC);
     const double sbo2 = AFV(AF_SBO2, j);
-    const double pv3 = atom_prm(ff, tj, A_P_VAL3), pv5 = atom_prm(ff, tj, A_P_VAL5);
-    const double valval = atom_prm(ff, tj, A_VALENCY_VAL);
-    const double k180 = 3.14159265 / 180;
-    const double e17 = exp(-g[17] * (2 - sbo2));
     const double ex3 = exp(-g[20] * d_j), ex4 = exp(g[21] * d_j);
     const double den34 = 1 + ex3 + ex4;
-    const double Fp = (2 + ex3) / den34;
-    const double dFp_dd = (-g[20] * ex3 * den34 - (2 + ex3) * (-g[20] * ex3 + g[21] * ex4)) / (den34 * den34);
-    const double e2 = exp(g[2] * (total_j - valval));
+    const double e2 = exp(g[2] * (total_j - atom_prm(ff, tj, A_VALENCY_VAL)));
     const double K1 = 1.0 / (1.0 + e2);
-    const double dK1_dt = -g[2] * e2 * K1 * K1;
-    const bool lammps = !w.full_derivative;
-    for (int t = lane; t < npairs; t += 32) {
-      int a = 0, rem = t;
-      while (rem >= m - 1 - a) {
-        rem -= m - 1 - a;
-        ++a;
-      }
-      const int2 ea = w.arow[beg + a], ec = w.arow[beg + a + 1 + rem];
+    double* cj = ucon[wl][lane];
+    cj[0] = exp(-g[17] * (2 - sbo2));
+    cj[1] = (2 + ex3) / den34;
+    cj[2] = (-g[20] * ex3 * den34 - (2 + ex3) * (-g[20] * ex3 + g[21] * ex4)) / (den34 * den34);
+    cj[3] = K1;
+    cj[4] = -g[2] * e2 * K1 * K1;
+    cj[5] = total_j - atom_prm(ff, tj, A_VALENCY_BOC);
+    cj[6] = atom_prm(ff, tj, A_P_VAL3);
+    cj[7] = atom_prm(ff, tj, A_P_VAL5);
+    ubeg[wl][lane] = w.cnt[3 * L + j];
+    ucnt[wl][lane] = w.nact[j];
+    if (w.nact[j] > 16383) atomicOr(w.status, XR_S_LIMIT);
+#pragma unroll
+    for (int k = 0; k < NV; ++k) uacc[wl][lane][k] = 0.0;
+  }
+  __syncwarp();
+  double* acc = &uacc[wl][0][0];
+  auto process = [&](uint32_t it, bool valid) {
+    double v[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) v[k] = 0.0;
+    int key = -1;
+    if (valid) {
+      const int u = item_unit(it), a = item_a(it), c = item_c(it);
+      key = u;
+      const int j = j0 + u, tj = w.type[j];
+      const double* cj = ucon[wl][u];
+      const double e17 = cj[0], Fp = cj[1], dFp_dd = cj[2], K1 = cj[3], dK1_dt = cj[4], db_j = cj[5];
+      const double pv3 = cj[6], pv5 = cj[7];
+      const int2 ea = w.arow[ubeg[wl][u] + a], ec = w.arow[ubeg[wl][u] + c];
       const double bo_l = BFV(BF_BO, ea.x), bo_r = BFV(BF_BO, ec.x);
-      if (bo_l * bo_r <= THB_PRODUCT_CUT) continue;
       const int i = bond_other(w, ea.x, ea.y), k = bond_other(w, ec.x, ec.y);
-      const int key = (w.type[i] * T + tj) * T + w.type[k];
-      const int first = __ldg(ff.angle_index + 2 * key), count = __ldg(ff.angle_index + 2 * key + 1);
-      if (count == 0) continue;
+      const int key3 = (w.type[i] * T + tj) * T + w.type[k];
+      const int first = __ldg(ff.angle_index + 2 * key3), count = __ldg(ff.angle_index + 2 * key3 + 1);
       double vl[3], vr[3];
       bond_vec(w, ea.x, ea.y, vl);
       bond_vec(w, ec.x, ec.y, vr);
-      const double rl = w.b_r[ea.x], rr = w.b_r[ec.x];
+      const double irl = 1.0 / w.b_r[ea.x], irr = 1.0 / w.b_r[ec.x];
       const double total_i = AFV(AF_TOTAL, i), total_k = AFV(AF_TOTAL, k);
-      const double cosv = (vl[0] * vr[0] + vl[1] * vr[1] + vl[2] * vr[2]) / (rl * rr);
+      const double inv = irl * irr;
+      const double cosv = (vl[0] * vr[0] + vl[1] * vr[1] + vl[2] * vr[2]) * inv;
       double theta, dth_dcos;
       if (lammps) {
         const double cc = fmin(fmax(cosv, -1.0), 1.0);
@@ -404,6 +481,9 @@ __global__ void k_angles(XrWork w, XrFF ff) {
       }
       const double bij = bo_l - THB_CUT, bjk = bo_r - THB_CUT;
       const double lbij = log(bij), lbjk = log(bjk);
+      const double ibij = 1.0 / bij, ibjk = 1.0 / bjk;
+      // terms that do not depend on the parameter record
+      const double ti_b = total_i - bij, tk_b = total_k - bjk;
       double dE_dcos = 0, dbij = 0, dbjk = 0, dtot_i = 0, dtot_k = 0;
       for (int q = 0; q < count; ++q) {
         const double* prm = ff.angle + 7 * (first + q);
@@ -415,8 +495,8 @@ __global__ void k_angles(XrWork w, XrFF ff) {
         const double pij = exp(v4 * lbij), pjk = exp(v4 * lbjk);
         const double A1 = exp(-pv3 * pij), A2 = exp(-pv3 * pjk);
         const double f7 = (1 - A1) * (1 - A2);
-        const double df7_dbij = pv3 * v4 * pij / bij * A1 * (1 - A2);
-        const double df7_dbjk = (1 - A1) * pv3 * v4 * pjk / bjk * A2;
+        const double df7_dbij = pv3 * v4 * pij * ibij * A1 * (1 - A2);
+        const double df7_dbjk = (1 - A1) * pv3 * v4 * pjk * ibjk * A2;
         const double ex6 = exp(g[14] * db_j), ex7 = exp(-v7 * db_j);
         const double den8 = 1 + ex6 + ex7;
         const double f8 = pv5 - (pv5 - 1) * (2 + ex6) / den8;
@@ -424,37 +504,35 @@ __global__ void k_angles(XrWork w, XrFF ff) {
         const double dt = theta0 - theta;
         const double exang = exp(-v2 * dt * dt);
         const double branch = v1 >= 0 ? 1 - exang : -exang;
-        E_ang += f7 * f8 * v1 * branch;
+        v[0] += f7 * f8 * v1 * branch;
         const double dE_ddt = f7 * f8 * v1 * 2 * v2 * dt * exang;
         dE_dcos += -dE_ddt * dth_dcos;
-        A_sbo2 += dE_ddt * dth0_dsbo2;
+        v[3] += dE_ddt * dth0_dsbo2;
         dbij += f8 * v1 * branch * df7_dbij;
         dbjk += f8 * v1 * branch * df7_dbjk;
-        A_db += f7 * v1 * branch * df8_ddb;
+        v[4] += f7 * v1 * branch * df8_ddb;
         const double Gp = exp(-g[19] * ((bij - 2) * (bij - 2) + (bjk - 2) * (bjk - 2)));
         const double ep = pen1 * Fp * Gp;
-        E_pen += ep;
-        A_d += pen1 * dFp_dd * Gp;
+        v[1] += ep;
+        v[5] += pen1 * dFp_dd * Gp;
         dbij += ep * (-2 * g[19] * (bij - 2));
         dbjk += ep * (-2 * g[19] * (bjk - 2));
-        const double ti_b = total_i - bij, tk_b = total_k - bjk;
         const double K2 = exp(-g[38] * (ti_b * ti_b + tk_b * tk_b));
         const double K3 = exp(-g[30] * ((bij - 1.5) * (bij - 1.5) + (bjk - 1.5) * (bjk - 1.5)));
         const double ec_ = coa1 * K1 * K2 * K3;
-        E_coa += ec_;
-        A_tj += coa1 * dK1_dt * K2 * K3;
+        v[2] += ec_;
+        v[6] += coa1 * dK1_dt * K2 * K3;
         dtot_i += ec_ * (-2 * g[38] * ti_b);
         dtot_k += ec_ * (-2 * g[38] * tk_b);
         dbij += ec_ * (2 * g[38] * ti_b) + ec_ * (-2 * g[30] * (bij - 1.5));
         dbjk += ec_ * (2 * g[38] * tk_b) + ec_ * (-2 * g[30] * (bjk - 1.5));
       }
       if (dE_dcos != 0.0) {
-        const double inv = 1.0 / (rl * rr);
         double gl[3], gr[3];
         for (int c3 = 0; c3 < 3; ++c3) {
-          gl[c3] = dE_dcos * (vr[c3] * inv - cosv * vl[c3] / (rl * rl));
-          gr[c3] = dE_dcos * (vl[c3] * inv - cosv * vr[c3] / (rr * rr));
-          gj[c3] -= gl[c3] + gr[c3];
+          gl[c3] = dE_dcos * (vr[c3] * inv - cosv * vl[c3] * irl * irl);
+          gr[c3] = dE_dcos * (vl[c3] * inv - cosv * vr[c3] * irr * irr);
+          v[7 + c3] = -(gl[c3] + gr[c3]);
         }
         atomic_add3(w.f, i, gl[0], gl[1], gl[2]);
         atomic_add3(w.f, k, gr[0], gr[1], gr[2]);
@@ -464,29 +542,47 @@ __global__ void k_angles(XrWork w, XrFF ff) {
       if (dtot_i != 0.0) atomicAdd(&AJV(AJ_TOTAL, i), dtot_i);
       if (dtot_k != 0.0) atomicAdd(&AJV(AJ_TOTAL, k), dtot_k);
     }
+    unit_sums<NV>(v, key, acc);
+  };
+  int nbuf = 0;
+  for (int u = 0; u < nu; ++u) {
+    const int m = ucnt[wl][u], beg = ubeg[wl][u];
+    const int tj = w.type[j0 + u];
+    const int npairs = m * (m - 1) / 2;
+    for (int t0 = 0; t0 < npairs; t0 += 32) {
+      const int t = t0 + lane;
+      bool ok = false;
+      uint32_t item = 0;
+      if (t < npairs) {
+        int a = 0, rem = t;
+        while (rem >= m - 1 - a) {
+          rem -= m - 1 - a;
+          ++a;
+        }
+        const int c = a + 1 + rem;
+        const int2 ea = w.arow[beg + a], ec = w.arow[beg + c];
+        if (BFV(BF_BO, ea.x) * BFV(BF_BO, ec.x) > THB_PRODUCT_CUT) {
+          const int i = bond_other(w, ea.x, ea.y), k = bond_other(w, ec.x, ec.y);
+          const int key3 = (w.type[i] * T + tj) * T + w.type[k];
+          ok = __ldg(ff.angle_index + 2 * key3 + 1) > 0;
+        }
+        item = pack_item(u, a, c);
+      }
+      push_items(buf[wl], nbuf, ok, item, process);
+    }
   }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    E_ang += __shfl_xor_sync(0xffffffffu, E_ang, o);
-    E_pen += __shfl_xor_sync(0xffffffffu, E_pen, o);
-    E_coa += __shfl_xor_sync(0xffffffffu, E_coa, o);
-    A_sbo2 += __shfl_xor_sync(0xffffffffu, A_sbo2, o);
-    A_db += __shfl_xor_sync(0xffffffffu, A_db, o);
-    A_d += __shfl_xor_sync(0xffffffffu, A_d, o);
-    A_tj += __shfl_xor_sync(0xffffffffu, A_tj, o);
-    gj[0] += __shfl_xor_sync(0xffffffffu, gj[0], o);
-    gj[1] += __shfl_xor_sync(0xffffffffu, gj[1], o);
-    gj[2] += __shfl_xor_sync(0xffffffffu, gj[2], o);
-  }
-  if (lane == 0) {
-    AEV(2, j) = E_ang;
-    AEV(3, j) = E_pen;
-    AEV(4, j) = E_coa;
-    if (A_sbo2 != 0.0) atomicAdd(&AJV(AJ_SBO2, j), A_sbo2);
-    if (A_db != 0.0) atomicAdd(&AJV(AJ_DB, j), A_db);
-    if (A_d != 0.0) atomicAdd(&AJV(AJ_D, j), A_d);
-    if (A_tj != 0.0) atomicAdd(&AJV(AJ_TOTAL, j), A_tj);
-    if (gj[0] != 0.0 || gj[1] != 0.0 || gj[2] != 0.0) atomic_add3(w.f, j, gj[0], gj[1], gj[2]);
+  if (nbuf > 0) process(buf[wl][lane], lane < nbuf);
+  if (lane < nu) {
+    const int j = j0 + lane;
+    const double* s = uacc[wl][lane];
+    AEV(2, j) = s[0];
+    AEV(3, j) = s[1];
+    AEV(4, j) = s[2];
+    if (s[3] != 0.0) atomicAdd(&AJV(AJ_SBO2, j), s[3]);
+    if (s[4] != 0.0) atomicAdd(&AJV(AJ_DB, j), s[4]);
+    if (s[5] != 0.0) atomicAdd(&AJV(AJ_D, j), s[5]);
+    if (s[6] != 0.0) atomicAdd(&AJV(AJ_TOTAL, j), s[6]);
+    if (s[7] != 0.0 || s[8] != 0.0 || s[9] != 0.0) atomic_add3(w.f, j, s[7], s[8], s[9]);
   }
 }
 
@@ -512,144 +608,200 @@ __global__ void k_torsion_middles(XrWork w) {
   if (keep) w.mids[base + __popc(msk & ((1u << lane) - 1u))] = b;
 }
 
-// Torsion and four-body conjugation, one warp per middle bond j -> k (the half direction); the lanes
-// take the (left, right) combinations of the two ends' active bond rows (src/xreac/energy.py:320-370).
-__global__ void k_torsions(XrWork w, XrFF ff) {
-  const int lane = threadIdx.x & 31;
+// Torsion and four-body conjugation (src/xreac/energy.py:320-370): units are middle bonds j -> k
+// (the half direction), items the (left, right) combinations of the two ends' active bond rows.
+__global__ void __launch_bounds__(32 * kBondedWarps) k_torsions(XrWork w, XrFF ff) {
+  constexpr int NC = 10, NV = 11;
+  struct UnitInt {
+    int m, j, k, tj, tk, jb, kb, jn, kn;
+    uint32_t sm;
+  };
+  __shared__ double ucon[kBondedWarps][kUnits][NC];
+  __shared__ double uacc[kBondedWarps][kUnits][NV];
+  __shared__ UnitInt uint_[kBondedWarps][kUnits];
+  __shared__ uint32_t buf[kBondedWarps][kItemBuf];
+  const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
   const int warp = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
   const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
-  const int L = w.A + 1, T = ff.ntypes;
+  const int T = ff.ntypes;
+  const int L = w.A + 1;
   const double* g = ff.g;
   const int nm = *w.nmids;
-  for (int q = warp; q < nm; q += nwarps) {
-    const int m = w.mids[q];
-    const double bo_m = BFV(BF_BO, m);
-    const int j = w.bond_i[m], k = w.bond_j[m];
-    const int tj = w.type[j], tk = w.type[k];
-    const uint32_t sm = (uint32_t)w.edge[w.pair_edge[w.bond_pair[m]]].y & XR_SHIFT_MASK;
-    double v[3];
-    bond_vec(w, m, 1, v);
-    const double rm = w.b_r[m];
-    const double pi_m = BFV(BF_PI, m);
-    const double db_j = AFV(AF_TOTAL, j) - atom_prm(ff, tj, A_VALENCY_BOC);
-    const double db_k = AFV(AF_TOTAL, k) - atom_prm(ff, tk, A_VALENCY_BOC);
-    const double ds = db_j + db_k;
-    const double ex3 = exp(-g[24] * ds), ex4 = exp(g[25] * ds);
-    const double den = 1 + ex3 + ex4;
-    const double f11 = (2 + ex3) / den;
-    const double df11_dds = (-g[24] * ex3 * den - (2 + ex3) * (-g[24] * ex3 + g[25] * ex4)) / (den * den);
-    const double b2 = bo_m - THB_CUT;
-    const double e2 = exp(-g[23] * b2);
-    const int jb = w.cnt[3 * L + j], kb = w.cnt[3 * L + k];
-    const int jn = w.nact[j], kn = w.nact[k];
-    double E_tor = 0, E_con = 0, A_bom = 0, A_pim = 0, A_ds = 0;
-    double g_j[3] = {0, 0, 0}, g_k[3] = {0, 0, 0};
-    for (int t = lane; t < jn * kn; t += 32) {
-      const int2 el = w.arow[jb + t / kn];
-      const int2 er = w.arow[kb + t % kn];
-      if (el.x == m && el.y > 0) continue;  // left == middle
-      if (er.x == m && er.y < 0) continue;  // right == reverse(middle)
-      const double bo_l = BFV(BF_BO, el.x), bo_r = BFV(BF_BO, er.x);
-      const int i = bond_other(w, el.x, el.y), l = bond_other(w, er.x, er.y);
-      const int row = __ldg(ff.torsion_index + ((w.type[i] * T + tj) * T + tk) * T + w.type[l]);
-      if (row < 0) continue;
-      if (bo_l * bo_m * bo_r <= THB_CUT) continue;
-      if (i == l) {
-        const uint32_t sl = bond_shift(w, el.x, el.y), sr = bond_shift(w, er.x, er.y);
-        if (xr_sx(sl) == xr_sx(sm) + xr_sx(sr) && xr_sy(sl) == xr_sy(sm) + xr_sy(sr) &&
-            xr_sz(sl) == xr_sz(sm) + xr_sz(sr))
-          continue;
-      }
-      double u[3], wv[3];
-      bond_vec(w, el.x, el.y, u);
-      bond_vec(w, er.x, er.y, wv);
-      const double rl = w.b_r[el.x], rr = w.b_r[er.x];
-      double n1[3], n2[3];
-      cross3(u, v, n1);
-      cross3(wv, v, n2);
-      const double A1 = n1[0] * n1[0] + n1[1] * n1[1] + n1[2] * n1[2];
-      const double A2 = n2[0] * n2[0] + n2[1] * n2[1] + n2[2] * n2[2];
-      const double s1 = A1 / ((rl * rm) * (rl * rm));
-      const double s2 = A2 / ((rm * rr) * (rm * rr));
-      if (s1 < 1e-20 || s2 < 1e-20) {
-        atomicOr(w.status, XR_S_COLLINEAR);
-        continue;
-      }
-      const double sinprod = sqrt(s1 * s2);
-      const double sq = sqrt(A1 * A2);
-      const double P = n1[0] * n2[0] + n1[1] * n2[1] + n1[2] * n2[2];
-      const double cw = P / sq;
-      const double* prm = ff.torsion + 5 * row;
-      const double V1 = __ldg(prm + 0), V2 = __ldg(prm + 1), V3 = __ldg(prm + 2), tor1 = __ldg(prm + 3),
-                   cot1 = __ldg(prm + 4);
-      const double b1 = bo_l - THB_CUT, b3 = bo_r - THB_CUT;
-      const double e1 = exp(-g[23] * b1), e3 = exp(-g[23] * b3);
-      const double y = 2 - pi_m - f11;
-      const double ex1 = exp(tor1 * y * y);
-      const double fn10 = (1 - e1) * (1 - e2) * (1 - e3);
-      const double cv = 0.5 * (V1 * (1 + cw) + V2 * ex1 * (2 - 2 * cw * cw) + V3 * (1 + 4 * cw * cw * cw - 3 * cw));
-      E_tor += fn10 * sinprod * cv;
-      const double q1 = b1 - 1.5, q2 = b2 - 1.5, q3 = b3 - 1.5;
-      const double fn12 = exp(-g[27] * (q1 * q1 + q2 * q2 + q3 * q3));
-      const double conj = 1 + (cw * cw - 1) * sinprod;
-      E_con += cot1 * fn12 * conj;
-      const double dcv_dcw = 0.5 * (V1 - 4 * V2 * ex1 * cw + V3 * (12 * cw * cw - 3));
-      const double dE_dcw = fn10 * sinprod * dcv_dcw + cot1 * fn12 * 2 * cw * sinprod;
-      const double dE_dsp = fn10 * cv + cot1 * fn12 * (cw * cw - 1);
-      const double dE_dex1 = fn10 * sinprod * 0.5 * V2 * (2 - 2 * cw * cw);
-      const double dex1_dy = 2 * tor1 * y * ex1;
-      A_pim += -dE_dex1 * dex1_dy;
-      A_ds += -dE_dex1 * dex1_dy * df11_dds;
-      const double sc = sinprod * cv, cc = cot1 * conj;
-      const double A_bol = sc * g[23] * e1 * (1 - e2) * (1 - e3) + cc * fn12 * (-2 * g[27] * q1);
-      A_bom += sc * g[23] * e2 * (1 - e1) * (1 - e3) + cc * fn12 * (-2 * g[27] * q2);
-      const double A_bor = sc * g[23] * e3 * (1 - e1) * (1 - e2) + cc * fn12 * (-2 * g[27] * q3);
-      atomicAdd(&BJV(BJ_BO, el.x), A_bol);
-      atomicAdd(&BJV(BJ_BO, er.x), A_bor);
-      double av[3], bv[3];
-      for (int c3 = 0; c3 < 3; ++c3) {
-        av[c3] = dE_dcw * (n2[c3] - (P / A1) * n1[c3]) / sq + dE_dsp * sinprod * n1[c3] / A1;
-        bv[c3] = dE_dcw * (n1[c3] - (P / A2) * n2[c3]) / sq + dE_dsp * sinprod * n2[c3] / A2;
-      }
-      double gu[3], gv[3], gw[3], t1[3], t2[3];
-      cross3(v, av, gu);
-      cross3(av, u, t1);
-      cross3(bv, wv, t2);
-      cross3(v, bv, gw);
-      for (int c3 = 0; c3 < 3; ++c3) {
-        gu[c3] += dE_dsp * (-sinprod) * u[c3] / (rl * rl);
-        gv[c3] = t1[c3] + t2[c3] + dE_dsp * (-2 * sinprod) * v[c3] / (rm * rm);
-        gw[c3] += dE_dsp * (-sinprod) * wv[c3] / (rr * rr);
-        g_j[c3] += -gu[c3] - gv[c3];
-        g_k[c3] += gv[c3] - gw[c3];
-      }
-      atomic_add3(w.f, i, gu[0], gu[1], gu[2]);
-      atomic_add3(w.f, l, gw[0], gw[1], gw[2]);
-    }
+  double* acc = &uacc[wl][0][0];
+  for (int q0 = warp * kUnits; q0 < nm; q0 += nwarps * kUnits) {
+    const int nu = min(kUnits, nm - q0);
+    if (lane < nu) {
+      UnitInt& ui = uint_[wl][lane];
+      const int m = w.mids[q0 + lane];
+      const int j = w.bond_i[m], k = w.bond_j[m];
+      const int tj = w.type[j], tk = w.type[k];
+      ui.m = m;
+      ui.j = j;
+      ui.k = k;
+      ui.tj = tj;
+      ui.tk = tk;
+      ui.jb = w.cnt[3 * L + j];
+      ui.kb = w.cnt[3 * L + k];
+      ui.jn = w.nact[j];
+      ui.kn = w.nact[k];
+      if (ui.jn > 16383 || ui.kn > 16383) atomicOr(w.status, XR_S_LIMIT);
+      ui.sm = (uint32_t)w.edge[w.pair_edge[w.bond_pair[m]]].y & XR_SHIFT_MASK;
+      double* cm = ucon[wl][lane];
+      double v[3];
+      bond_vec(w, m, 1, v);
+      const double db_j = AFV(AF_TOTAL, j) - atom_prm(ff, tj, A_VALENCY_BOC);
+      const double db_k = AFV(AF_TOTAL, k) - atom_prm(ff, tk, A_VALENCY_BOC);
+      const double ds = db_j + db_k;
+      const double ex3 = exp(-g[24] * ds), ex4 = exp(g[25] * ds);
+      const double den = 1 + ex3 + ex4;
+      const double b2 = BFV(BF_BO, m) - THB_CUT;
+      cm[0] = v[0];
+      cm[1] = v[1];
+      cm[2] = v[2];
+      cm[3] = w.b_r[m];
+      cm[4] = BFV(BF_PI, m);
+      cm[5] = (2 + ex3) / den;  // f11
+      cm[6] = (-g[24] * ex3 * den - (2 + ex3) * (-g[24] * ex3 + g[25] * ex4)) / (den * den);
+      cm[7] = b2;
+      cm[8] = exp(-g[23] * b2);
+      cm[9] = BFV(BF_BO, m);
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      E_tor += __shfl_xor_sync(0xffffffffu, E_tor, o);
-      E_con += __shfl_xor_sync(0xffffffffu, E_con, o);
-      A_bom += __shfl_xor_sync(0xffffffffu, A_bom, o);
-      A_pim += __shfl_xor_sync(0xffffffffu, A_pim, o);
-      A_ds += __shfl_xor_sync(0xffffffffu, A_ds, o);
-      for (int c3 = 0; c3 < 3; ++c3) {
-        g_j[c3] += __shfl_xor_sync(0xffffffffu, g_j[c3], o);
-        g_k[c3] += __shfl_xor_sync(0xffffffffu, g_k[c3], o);
+      for (int c = 0; c < NV; ++c) uacc[wl][lane][c] = 0.0;
+    }
+    __syncwarp();
+    auto process = [&](uint32_t it, bool valid) {
+      double acc_v[NV];
+#pragma unroll
+      for (int c = 0; c < NV; ++c) acc_v[c] = 0.0;
+      int key = -1;
+      if (valid) {
+        const int u = item_unit(it);
+        key = u;
+        const UnitInt& ui = uint_[wl][u];
+        const double* cm = ucon[wl][u];
+        const double v[3] = {cm[0], cm[1], cm[2]};
+        const double rm = cm[3], pi_m = cm[4], f11 = cm[5], df11_dds = cm[6], b2 = cm[7], e2 = cm[8];
+        const int2 el = w.arow[ui.jb + item_a(it)];
+        const int2 er = w.arow[ui.kb + item_c(it)];
+        const double bo_l = BFV(BF_BO, el.x), bo_r = BFV(BF_BO, er.x);
+        const int i = bond_other(w, el.x, el.y), l = bond_other(w, er.x, er.y);
+        const int row = __ldg(ff.torsion_index + ((w.type[i] * T + ui.tj) * T + ui.tk) * T + w.type[l]);
+        double u3[3], wv[3];
+        bond_vec(w, el.x, el.y, u3);
+        bond_vec(w, er.x, er.y, wv);
+        const double rl = w.b_r[el.x], rr = w.b_r[er.x];
+        double n1[3], n2[3];
+        cross3(u3, v, n1);
+        cross3(wv, v, n2);
+        const double A1 = n1[0] * n1[0] + n1[1] * n1[1] + n1[2] * n1[2];
+        const double A2 = n2[0] * n2[0] + n2[1] * n2[1] + n2[2] * n2[2];
+        const double s1 = A1 / ((rl * rm) * (rl * rm));
+        const double s2 = A2 / ((rm * rr) * (rm * rr));
+        if (s1 < 1e-20 || s2 < 1e-20) {
+          atomicOr(w.status, XR_S_COLLINEAR);
+        } else {
+          const double sinprod = sqrt(s1 * s2);
+          const double isq = 1.0 / sqrt(A1 * A2);
+          const double iA1 = 1.0 / A1, iA2 = 1.0 / A2;
+          const double P = n1[0] * n2[0] + n1[1] * n2[1] + n1[2] * n2[2];
+          const double cw = P * isq;
+          const double* prm = ff.torsion + 5 * row;
+          const double V1 = __ldg(prm + 0), V2 = __ldg(prm + 1), V3 = __ldg(prm + 2), tor1 = __ldg(prm + 3),
+                       cot1 = __ldg(prm + 4);
+          const double b1 = bo_l - THB_CUT, b3 = bo_r - THB_CUT;
+          const double e1 = exp(-g[23] * b1), e3 = exp(-g[23] * b3);
+          const double y = 2 - pi_m - f11;
+          const double ex1 = exp(tor1 * y * y);
+          const double fn10 = (1 - e1) * (1 - e2) * (1 - e3);
+          const double cv = 0.5 * (V1 * (1 + cw) + V2 * ex1 * (2 - 2 * cw * cw) + V3 * (1 + 4 * cw * cw * cw - 3 * cw));
+          acc_v[0] = fn10 * sinprod * cv;
+          const double q1 = b1 - 1.5, q2 = b2 - 1.5, q3 = b3 - 1.5;
+          const double fn12 = exp(-g[27] * (q1 * q1 + q2 * q2 + q3 * q3));
+          const double conj = 1 + (cw * cw - 1) * sinprod;
+          acc_v[1] = cot1 * fn12 * conj;
+          const double dcv_dcw = 0.5 * (V1 - 4 * V2 * ex1 * cw + V3 * (12 * cw * cw - 3));
+          const double dE_dcw = fn10 * sinprod * dcv_dcw + cot1 * fn12 * 2 * cw * sinprod;
+          const double dE_dsp = fn10 * cv + cot1 * fn12 * (cw * cw - 1);
+          const double dE_dex1 = fn10 * sinprod * 0.5 * V2 * (2 - 2 * cw * cw);
+          const double dex1_dy = 2 * tor1 * y * ex1;
+          acc_v[3] = -dE_dex1 * dex1_dy;             // pi of the middle
+          acc_v[4] = -dE_dex1 * dex1_dy * df11_dds;  // db of both ends
+          const double sc = sinprod * cv, cc = cot1 * conj;
+          const double A_bol = sc * g[23] * e1 * (1 - e2) * (1 - e3) + cc * fn12 * (-2 * g[27] * q1);
+          acc_v[2] = sc * g[23] * e2 * (1 - e1) * (1 - e3) + cc * fn12 * (-2 * g[27] * q2);
+          const double A_bor = sc * g[23] * e3 * (1 - e1) * (1 - e2) + cc * fn12 * (-2 * g[27] * q3);
+          atomicAdd(&BJV(BJ_BO, el.x), A_bol);
+          atomicAdd(&BJV(BJ_BO, er.x), A_bor);
+          double av[3], bv[3];
+          for (int c3 = 0; c3 < 3; ++c3) {
+            av[c3] = dE_dcw * (n2[c3] - (P * iA1) * n1[c3]) * isq + dE_dsp * sinprod * n1[c3] * iA1;
+            bv[c3] = dE_dcw * (n1[c3] - (P * iA2) * n2[c3]) * isq + dE_dsp * sinprod * n2[c3] * iA2;
+          }
+          double gu[3], gv[3], gw[3], t1[3], t2[3];
+          cross3(v, av, gu);
+          cross3(av, u3, t1);
+          cross3(bv, wv, t2);
+          cross3(v, bv, gw);
+          const double irl2 = 1.0 / (rl * rl), irm2 = 1.0 / (rm * rm), irr2 = 1.0 / (rr * rr);
+          for (int c3 = 0; c3 < 3; ++c3) {
+            gu[c3] += dE_dsp * (-sinprod) * u3[c3] * irl2;
+            gv[c3] = t1[c3] + t2[c3] + dE_dsp * (-2 * sinprod) * v[c3] * irm2;
+            gw[c3] += dE_dsp * (-sinprod) * wv[c3] * irr2;
+            acc_v[5 + c3] = -gu[c3] - gv[c3];
+            acc_v[8 + c3] = gv[c3] - gw[c3];
+          }
+          atomic_add3(w.f, i, gu[0], gu[1], gu[2]);
+          atomic_add3(w.f, l, gw[0], gw[1], gw[2]);
+        }
+      }
+      unit_sums<NV>(acc_v, key, acc);
+    };
+    int nbuf = 0;
+    for (int u = 0; u < nu; ++u) {
+      const UnitInt ui = uint_[wl][u];
+      const double bo_m = ucon[wl][u][9];
+      const int nit = ui.jn * ui.kn;
+      for (int t0 = 0; t0 < nit; t0 += 32) {
+        const int t = t0 + lane;
+        bool ok = false;
+        uint32_t item = 0;
+        if (t < nit) {
+          const int a = t / ui.kn, c = t % ui.kn;
+          const int2 el = w.arow[ui.jb + a];
+          const int2 er = w.arow[ui.kb + c];
+          ok = !(el.x == ui.m && el.y > 0) && !(er.x == ui.m && er.y < 0);  // left == middle, right == reverse
+          if (ok) {
+            const int i = bond_other(w, el.x, el.y), l = bond_other(w, er.x, er.y);
+            ok = __ldg(ff.torsion_index + ((w.type[i] * T + ui.tj) * T + ui.tk) * T + w.type[l]) >= 0 &&
+                 BFV(BF_BO, el.x) * bo_m * BFV(BF_BO, er.x) > THB_CUT;
+            if (ok && i == l) {
+              const uint32_t sl = bond_shift(w, el.x, el.y), sr = bond_shift(w, er.x, er.y);
+              if (xr_sx(sl) == xr_sx(ui.sm) + xr_sx(sr) && xr_sy(sl) == xr_sy(ui.sm) + xr_sy(sr) &&
+                  xr_sz(sl) == xr_sz(ui.sm) + xr_sz(sr))
+                ok = false;  // the same atom image at both ends
+            }
+          }
+          item = pack_item(u, a, c);
+        }
+        push_items(buf[wl], nbuf, ok, item, process);
       }
     }
-    if (lane == 0) {
-      BEV(2, m) = E_tor;
-      BEV(3, m) = E_con;
-      if (A_bom != 0.0) atomicAdd(&BJV(BJ_BO, m), A_bom);
-      if (A_pim != 0.0) atomicAdd(&BJV(BJ_PI, m), A_pim);
-      if (A_ds != 0.0) {
-        atomicAdd(&AJV(AJ_DB, j), A_ds);
-        atomicAdd(&AJV(AJ_DB, k), A_ds);
+    if (nbuf > 0) process(buf[wl][lane], lane < nbuf);
+    if (lane < nu) {
+      const UnitInt& ui = uint_[wl][lane];
+      const double* s = uacc[wl][lane];
+      BEV(2, ui.m) = s[0];
+      BEV(3, ui.m) = s[1];
+      if (s[2] != 0.0) atomicAdd(&BJV(BJ_BO, ui.m), s[2]);
+      if (s[3] != 0.0) atomicAdd(&BJV(BJ_PI, ui.m), s[3]);
+      if (s[4] != 0.0) {
+        atomicAdd(&AJV(AJ_DB, ui.j), s[4]);
+        atomicAdd(&AJV(AJ_DB, ui.k), s[4]);
       }
-      if (g_j[0] != 0.0 || g_j[1] != 0.0 || g_j[2] != 0.0) atomic_add3(w.f, j, g_j[0], g_j[1], g_j[2]);
-      if (g_k[0] != 0.0 || g_k[1] != 0.0 || g_k[2] != 0.0) atomic_add3(w.f, k, g_k[0], g_k[1], g_k[2]);
+      if (s[5] != 0.0 || s[6] != 0.0 || s[7] != 0.0) atomic_add3(w.f, ui.j, s[5], s[6], s[7]);
+      if (s[8] != 0.0 || s[9] != 0.0 || s[10] != 0.0) atomic_add3(w.f, ui.k, s[8], s[9], s[10]);
     }
+    __syncwarp();
   }
 }
 
@@ -963,11 +1115,16 @@ void xr_launch_bonded(const XrWork& w, const XrFF& ff, cudaStream_t st) {
   k_atom1<<<gA, tb, 0, st>>>(w, ff);
   k_atom2<<<gA, tb, 0, st>>>(w, ff);
   if (w.nB > 0) k_bond_energy<<<gB, tb, 0, st>>>(w, ff);
-  k_angles<<<(w.A + 3) / 4, 128, 0, st>>>(w, ff);
+  {
+    const int chunks = (w.A + kUnits - 1) / kUnits;
+    k_angles<<<(chunks + kBondedWarps - 1) / kBondedWarps, 32 * kBondedWarps, 0, st>>>(w, ff);
+  }
   if (w.nB > 0) {
     cudaMemsetAsync(w.nmids, 0, sizeof(int), st);
     k_torsion_middles<<<gB, tb, 0, st>>>(w);
-    k_torsions<<<152 * 8, 256, 0, st>>>(w, ff);
+    const int chunks = (w.nB + kUnits - 1) / kUnits;
+    const int blocks = std::min((chunks + kBondedWarps - 1) / kBondedWarps, 152 * 16);
+    k_torsions<<<blocks, 32 * kBondedWarps, 0, st>>>(w, ff);
   }
   k_hbonds<<<(w.A + kHbWarps - 1) / kHbWarps, 32 * kHbWarps, 0, st>>>(w, ff);
   k_chain_atom<<<gA, tb, 0, st>>>(w, ff);

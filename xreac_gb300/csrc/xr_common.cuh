@@ -51,6 +51,7 @@ enum XrStatusBits {
   XR_S_NONSPD = 1 << 7,       // QEq matrix not positive definite along a CG direction
   XR_S_BARRIER = 1 << 8,      // a grid barrier wait reached its iteration limit
   XR_S_REVERSE = 1 << 9,      // an edge without its reverse (internal consistency check)
+  XR_S_LIMIT = 1 << 10,       // an atom has more active bonds than the packed item indices hold
 };
 
 // Edge code: three 9-bit signed image shifts plus flags. Sx sits in the highest shift bits so the

@@ -493,6 +493,10 @@ int status_to_code(xr_ctx* c, int st) {
     c->err = "An image shift exceeds the supported range of +-255 cells; wrap the positions into the cell";
     return XR_ECAPACITY;
   }
+  if (st & XR_S_LIMIT) {
+    c->err = "An atom has more than 16383 active bonds; the many-body item lists cannot index them";
+    return XR_ECAPACITY;
+  }
   if (st & XR_S_REVERSE) {
     c->err = "neighbors must include both directions: (i, j, S) and (j, i, -S)";
     return XR_EINPUT;
