@@ -67,72 +67,112 @@ __device__ inline uint32_t bond_shift(const XrWork& w, int b, int dir) {
 // raw = sum; active when raw >= cut; bo0 = raw - cut (src/xreac/energy.py:130-149).
 __global__ void k_bo1(XrWork w, XrFF ff) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= w.nB) return;
-  const int i = w.bond_i[b], j = w.bond_j[b];
-  const uint32_t code = (uint32_t)w.edge[w.pair_edge[w.bond_pair[b]]].y;
-  const XrSystem& S = w.sys[w.sys_of[i]];
-  const int sx = xr_sx(code), sy = xr_sy(code), sz = xr_sz(code);
-  const double4_32a xi = w.x[i], xj = w.x[j];
-  const double xa[3] = {xi.x, xi.y, xi.z}, xb[3] = {xj.x, xj.y, xj.z};
-  double v[3];
-  for (int c = 0; c < 3; ++c) {
-    const double off = __dadd_rn(__dadd_rn(__dmul_rn((double)sx, S.cell[c]), __dmul_rn((double)sy, S.cell[3 + c])),
-                                 __dmul_rn((double)sz, S.cell[6 + c]));
-    v[c] = __dadd_rn(__dsub_rn(xb[c], xa[c]), off);
+  const int lane = threadIdx.x & 31;
+  bool mask = false;
+  if (b < w.nB) {
+    const int i = w.bond_i[b], j = w.bond_j[b];
+    const uint32_t code = (uint32_t)w.edge[w.pair_edge[w.bond_pair[b]]].y;
+    const XrSystem& S = w.sys[w.sys_of[i]];
+    const int sx = xr_sx(code), sy = xr_sy(code), sz = xr_sz(code);
+    const double4_32a xi = w.x[i], xj = w.x[j];
+    const double xa[3] = {xi.x, xi.y, xi.z}, xb[3] = {xj.x, xj.y, xj.z};
+    double v[3];
+    for (int c = 0; c < 3; ++c) {
+      const double off = __dadd_rn(__dadd_rn(__dmul_rn((double)sx, S.cell[c]), __dmul_rn((double)sy, S.cell[3 + c])),
+                                   __dmul_rn((double)sz, S.cell[6 + c]));
+      v[c] = __dadd_rn(__dsub_rn(xb[c], xa[c]), off);
+    }
+    const double r = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(v[0], v[0]), __dmul_rn(v[1], v[1])), __dmul_rn(v[2], v[2])));
+    w.b_r[b] = r;
+    w.b_v[0 * w.cap_B + b] = v[0];
+    w.b_v[1 * w.cap_B + b] = v[1];
+    w.b_v[2 * w.cap_B + b] = v[2];
+    const int ti = w.type[i], tj = w.type[j], T = ff.ntypes;
+    const int pt = ti * T + tj;
+    const double cut = 0.01 * ff.g[29];
+    double sig = 0, pi = 0, pp = 0, dsig = 0, dpi = 0, dpp = 0;
+    // Beyond the pair type's bound the uncorrected order is below a quarter of the cut: no term is
+    // evaluated, the bond is inactive with zero orders (as the full expression would give).
+    if (r <= __ldg(ff.pair_rmax + pt)) {
+      const double lr = log(r);
+      if (atom_prm(ff, ti, A_R_S) > 0 && atom_prm(ff, tj, A_R_S) > 0) {
+        const double p1 = pair_prm(ff, pt, P_BO1), p2 = pair_prm(ff, pt, P_BO2);
+        const double t = exp(p2 * (lr - __ldg(ff.pair_logr + 3 * pt + 0)));
+        sig = (1.0 + cut) * exp(p1 * t);
+        dsig = sig * p1 * p2 * t / r;
+      }
+      if (atom_prm(ff, ti, A_R_PI) > 0 && atom_prm(ff, tj, A_R_PI) > 0) {
+        const double p3 = pair_prm(ff, pt, P_BO3), p4 = pair_prm(ff, pt, P_BO4);
+        const double t = exp(p4 * (lr - __ldg(ff.pair_logr + 3 * pt + 1)));
+        pi = exp(p3 * t);
+        dpi = pi * p3 * p4 * t / r;
+      }
+      if (atom_prm(ff, ti, A_R_PI_PI) > 0 && atom_prm(ff, tj, A_R_PI_PI) > 0) {
+        const double p5 = pair_prm(ff, pt, P_BO5), p6 = pair_prm(ff, pt, P_BO6);
+        const double t = exp(p6 * (lr - __ldg(ff.pair_logr + 3 * pt + 2)));
+        pp = exp(p5 * t);
+        dpp = pp * p5 * p6 * t / r;
+      }
+    }
+    const double raw = sig + pi + pp;
+    mask = raw >= cut;
+    BFV(BF_BO0, b) = mask ? raw - cut : 0.0;
+    BFV(BF_PI0, b) = mask ? pi : 0.0;
+    BFV(BF_PP0, b) = mask ? pp : 0.0;
+    BFV(BF_DSIG, b) = dsig;
+    BFV(BF_DPI, b) = dpi;
+    BFV(BF_DPP, b) = dpp;
+    BFV(BF_MASK, b) = mask ? 1.0 : 0.0;
+    if (!mask) {  // the corrected orders of an inactive bond are zero; k_bo2 visits active bonds only
+      BFV(BF_BO, b) = 0.0;
+      BFV(BF_PI, b) = 0.0;
+      BFV(BF_PP, b) = 0.0;
+      BFV(BF_SIG, b) = 0.0;
+    }
   }
-  const double r = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(v[0], v[0]), __dmul_rn(v[1], v[1])), __dmul_rn(v[2], v[2])));
-  w.b_r[b] = r;
-  w.b_v[0 * w.cap_B + b] = v[0];
-  w.b_v[1 * w.cap_B + b] = v[1];
-  w.b_v[2 * w.cap_B + b] = v[2];
-  const int ti = w.type[i], tj = w.type[j], T = ff.ntypes;
-  const int pt = ti * T + tj;
-  const double cut = 0.01 * ff.g[29];
-  const double lr = log(r);
-  double sig = 0, pi = 0, pp = 0, dsig = 0, dpi = 0, dpp = 0;
-  if (atom_prm(ff, ti, A_R_S) > 0 && atom_prm(ff, tj, A_R_S) > 0) {
-    const double p1 = pair_prm(ff, pt, P_BO1), p2 = pair_prm(ff, pt, P_BO2);
-    const double t = exp(p2 * (lr - __ldg(ff.pair_logr + 3 * pt + 0)));
-    sig = (1.0 + cut) * exp(p1 * t);
-    dsig = sig * p1 * p2 * t / r;
-  }
-  if (atom_prm(ff, ti, A_R_PI) > 0 && atom_prm(ff, tj, A_R_PI) > 0) {
-    const double p3 = pair_prm(ff, pt, P_BO3), p4 = pair_prm(ff, pt, P_BO4);
-    const double t = exp(p4 * (lr - __ldg(ff.pair_logr + 3 * pt + 1)));
-    pi = exp(p3 * t);
-    dpi = pi * p3 * p4 * t / r;
-  }
-  if (atom_prm(ff, ti, A_R_PI_PI) > 0 && atom_prm(ff, tj, A_R_PI_PI) > 0) {
-    const double p5 = pair_prm(ff, pt, P_BO5), p6 = pair_prm(ff, pt, P_BO6);
-    const double t = exp(p6 * (lr - __ldg(ff.pair_logr + 3 * pt + 2)));
-    pp = exp(p5 * t);
-    dpp = pp * p5 * p6 * t / r;
-  }
-  const double raw = sig + pi + pp;
-  const bool mask = raw >= cut;
-  BFV(BF_BO0, b) = mask ? raw - cut : 0.0;
-  BFV(BF_PI0, b) = mask ? pi : 0.0;
-  BFV(BF_PP0, b) = mask ? pp : 0.0;
-  BFV(BF_DSIG, b) = dsig;
-  BFV(BF_DPI, b) = dpi;
-  BFV(BF_DPP, b) = dpp;
-  BFV(BF_MASK, b) = mask ? 1.0 : 0.0;
+  // active bonds join the list of bonds the per-bond kernels visit (order is irrelevant: each
+  // bond's results go to its own slots)
+  const unsigned m = __ballot_sync(0xffffffffu, mask);
+  int base = 0;
+  if (lane == 0 && m) base = atomicAdd(w.nmask, __popc(m));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (mask) w.mlist[base + __popc(m & ((1u << lane) - 1u))] = b;
 }
 
-// Delta'_a = sum of uncorrected bond orders over the atom's directed bond edges.
+// Delta'_a = sum of uncorrected bond orders over the atom's directed bond edges, one warp per atom.
+// The same pass compacts the entries whose uncorrected order passed the cut into nzrow (canonical
+// order kept): every other bond candidate within 5 A has zero bond orders and zero sensitivities,
+// so the later per-atom loops visit only these few entries instead of all candidates.
 __global__ void k_deltap(XrWork w) {
-  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int a = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
   if (a >= w.A) return;
-  const int L = w.A + 1;
+  const int L = w.A + 1, beg = w.cnt[3 * L + a], end = w.cnt[3 * L + a + 1];
   double s = 0;
-  for (int k = w.cnt[3 * L + a]; k < w.cnt[3 * L + a + 1]; ++k) s += BFV(BF_BO0, w.dbrow[k].x);
-  AFV(AF_DELTAP, a) = s;
+  int n = 0;
+  for (int k0 = beg; k0 < end; k0 += 32) {
+    const int k = k0 + lane;
+    bool keep = false;
+    int2 en = make_int2(0, 0);
+    if (k < end) {
+      en = w.dbrow[k];
+      keep = BFV(BF_MASK, en.x) != 0.0;
+      if (keep) s += BFV(BF_BO0, en.x);
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    if (keep) w.nzrow[beg + n + __popc(m & ((1u << lane) - 1u))] = en;
+    n += __popc(m);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) {
+    AFV(AF_DELTAP, a) = s;
+    w.nnz[a] = n;
+  }
 }
 
 // Corrected bond orders (src/xreac/energy.py:150-165).
-__global__ void k_bo2(XrWork w, XrFF ff) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= w.nB) return;
+__device__ inline void k_bo2_one(const XrWork& w, const XrFF& ff, int b) {
   const int i = w.bond_i[b], j = w.bond_j[b];
   const int ti = w.type[i], tj = w.type[j], T = ff.ntypes, pt = ti * T + tj;
   const double* g = ff.g;
@@ -179,6 +219,12 @@ __global__ void k_bo2(XrWork w, XrFF ff) {
   BFV(BF_DF1J, b) = df1j;
 }
 
+__global__ void k_bo2(XrWork w, XrFF ff) {
+  const int nm = *w.nmask;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nm; q += gridDim.x * blockDim.x)
+    k_bo2_one(w, ff, w.mlist[q]);
+}
+
 // Per-atom sums of corrected bond orders and the lone-pair quantities
 // (src/xreac/energy.py:185-199, 295-296).
 __global__ void k_atom1(XrWork w, XrFF ff) {
@@ -189,8 +235,8 @@ __global__ void k_atom1(XrWork w, XrFF ff) {
   double total = 0, sumpi = 0, prodsum = 0, ov1 = 0, n30 = 0;
   const int beg = w.cnt[3 * L + a];
   int nact = 0;
-  for (int k = beg; k < w.cnt[3 * L + a + 1]; ++k) {
-    const int2 en = w.dbrow[k];
+  for (int k = beg; k < beg + w.nnz[a]; ++k) {
+    const int2 en = w.nzrow[k];
     const int b = en.x;
     const double bo = BFV(BF_BO, b);
     if (bo > THB_CUT) w.arow[beg + nact++] = en;  // bonded rows of src/xreac/energy.py:220
@@ -249,8 +295,8 @@ __global__ void k_atom2(XrWork w, XrFF ff) {
   const double* g = ff.g;
   const double dfvl = atom_prm(ff, ta, A_MASS) <= 21 ? 1.0 : 0.0;
   double ov2 = 0;
-  for (int k = w.cnt[3 * L + a]; k < w.cnt[3 * L + a + 1]; ++k) {
-    const int2 en = w.dbrow[k];
+  for (int k = w.cnt[3 * L + a]; k < w.cnt[3 * L + a] + w.nnz[a]; ++k) {
+    const int2 en = w.nzrow[k];
     const int b = en.x, j = bond_other(w, b, en.y);
     const double dj = AFV(AF_TOTAL, j) - atom_prm(ff, w.type[j], A_VALENCY);
     ov2 += (dj - dfvl * AFV(AF_DLPT, j)) * (BFV(BF_PI, b) + BFV(BF_PP, b));
@@ -289,9 +335,7 @@ __global__ void k_atom2(XrWork w, XrFF ff) {
 
 // Bond energy, C2 correction and triple-bond stabilisation, per half bond
 // (src/xreac/energy.py:194-198, 231-246).
-__global__ void k_bond_energy(XrWork w, XrFF ff) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= w.nB) return;
+__device__ inline void k_bond_energy_one(const XrWork& w, const XrFF& ff, int b) {
   const int i = w.bond_i[b], j = w.bond_j[b];
   const int ti = w.type[i], tj = w.type[j], T = ff.ntypes, pt = ti * T + tj;
   const double* g = ff.g;
@@ -341,6 +385,12 @@ __global__ void k_bond_energy(XrWork w, XrFF ff) {
   if (dbo != 0.0) atomicAdd(&BJV(BJ_BO, b), dbo);
   BEV(0, b) = e_bond;
   BEV(1, b) = e_c2;
+}
+
+__global__ void k_bond_energy(XrWork w, XrFF ff) {
+  const int nm = *w.nmask;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nm; q += gridDim.x * blockDim.x)
+    k_bond_energy_one(w, ff, w.mlist[q]);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -1006,8 +1056,8 @@ __global__ void k_chain_atom(XrWork w, XrFF ff) {
   const int L = w.A + 1, ta = w.type[a];
   const double* g = ff.g;
   double A_d = AJV(AJ_D, a), A_dlpt = AJV(AJ_DLPT, a);
-  for (int k = w.cnt[3 * L + a]; k < w.cnt[3 * L + a + 1]; ++k) {
-    const int2 en = w.dbrow[k];
+  for (int k = w.cnt[3 * L + a]; k < w.cnt[3 * L + a] + w.nnz[a]; ++k) {
+    const int2 en = w.nzrow[k];
     const int j = bond_other(w, en.x, en.y);
     const double P = BFV(BF_PI, en.x) + BFV(BF_PP, en.x);
     if (P == 0.0) continue;
@@ -1033,9 +1083,7 @@ __global__ void k_chain_atom(XrWork w, XrFF ff) {
 }
 
 // Per-bond chain: from the thresholded outputs back through f1, f4, f5 to the uncorrected orders.
-__global__ void k_chain_bond(XrWork w, XrFF ff) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= w.nB) return;
+__device__ inline void k_chain_bond_one(const XrWork& w, const XrFF& ff, int b) {
   const int i = w.bond_i[b], j = w.bond_j[b];
   const int ti = w.type[i], tj = w.type[j], T = ff.ntypes, pt = ti * T + tj;
   const double bo = BFV(BF_BO, b), pi = BFV(BF_PI, b), pp = BFV(BF_PP, b), sig = BFV(BF_SIG, b);
@@ -1080,27 +1128,37 @@ __global__ void k_chain_bond(XrWork w, XrFF ff) {
   BJV(BJ_CJ, b) = d_f1 * BFV(BF_DF1J, b) + d_dbj;
 }
 
+__global__ void k_chain_bond(XrWork w, XrFF ff) {
+  const int nm = *w.nmask;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nm; q += gridDim.x * blockDim.x)
+    k_chain_bond_one(w, ff, w.mlist[q]);
+}
+
 __global__ void k_chain_deltap(XrWork w) {
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= w.A) return;
   const int L = w.A + 1;
   double s = 0;
-  for (int k = w.cnt[3 * L + a]; k < w.cnt[3 * L + a + 1]; ++k) {
-    const int2 en = w.dbrow[k];
+  for (int k = w.cnt[3 * L + a]; k < w.cnt[3 * L + a] + w.nnz[a]; ++k) {
+    const int2 en = w.nzrow[k];
     s += en.y > 0 ? BJV(BJ_CI, en.x) : BJV(BJ_CJ, en.x);
   }
   AJV(AJ_DELTAP, a) = s;
 }
 
 // dE/dr of each bond from the uncorrected bond orders; added to the pair's radial accumulator.
-__global__ void k_chain_radial(XrWork w) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= w.nB) return;
+__device__ inline void k_chain_radial_one(const XrWork& w, int b) {
   if (BFV(BF_MASK, b) == 0.0) return;
   const double d_bo0 = BJV(BJ_BO0, b) + AJV(AJ_DELTAP, w.bond_i[b]) + AJV(AJ_DELTAP, w.bond_j[b]);
   const double G = d_bo0 * BFV(BF_DSIG, b) + (d_bo0 + BJV(BJ_PI0, b)) * BFV(BF_DPI, b) +
                    (d_bo0 + BJV(BJ_PP0, b)) * BFV(BF_DPP, b);
   w.p_g[w.bond_pair[b]] += G;
+}
+
+__global__ void k_chain_radial(XrWork w) {
+  const int nm = *w.nmask;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nm; q += gridDim.x * blockDim.x)
+    k_chain_radial_one(w, w.mlist[q]);
 }
 
 }  // namespace
@@ -1109,18 +1167,21 @@ void xr_launch_bonded(const XrWork& w, const XrFF& ff, cudaStream_t st) {
   const int tb = 128;
   const int gA = (w.A + tb - 1) / tb;
   const int gB = (w.nB + tb - 1) / tb;
+  // per-bond kernels after k_bo1 run over the active-bond list (bonds whose uncorrected order
+  // passed the cut), grid-striding over its device-side length
+  const int gM = std::max(1, std::min(gB, 152 * 8));
+  cudaMemsetAsync(w.nmids, 0, 2 * sizeof(int), st);  // torsion middles, active bonds
   if (w.nB > 0) k_bo1<<<gB, tb, 0, st>>>(w, ff);
-  k_deltap<<<gA, tb, 0, st>>>(w);
-  if (w.nB > 0) k_bo2<<<gB, tb, 0, st>>>(w, ff);
+  k_deltap<<<(w.A + 3) / 4, 128, 0, st>>>(w);
+  if (w.nB > 0) k_bo2<<<gM, tb, 0, st>>>(w, ff);
   k_atom1<<<gA, tb, 0, st>>>(w, ff);
   k_atom2<<<gA, tb, 0, st>>>(w, ff);
-  if (w.nB > 0) k_bond_energy<<<gB, tb, 0, st>>>(w, ff);
+  if (w.nB > 0) k_bond_energy<<<gM, tb, 0, st>>>(w, ff);
   {
     const int chunks = (w.A + kUnits - 1) / kUnits;
     k_angles<<<(chunks + kBondedWarps - 1) / kBondedWarps, 32 * kBondedWarps, 0, st>>>(w, ff);
   }
   if (w.nB > 0) {
-    cudaMemsetAsync(w.nmids, 0, sizeof(int), st);
     k_torsion_middles<<<gB, tb, 0, st>>>(w);
     const int chunks = (w.nB + kUnits - 1) / kUnits;
     const int blocks = std::min((chunks + kBondedWarps - 1) / kBondedWarps, 152 * 16);
@@ -1129,8 +1190,8 @@ void xr_launch_bonded(const XrWork& w, const XrFF& ff, cudaStream_t st) {
   k_hbonds<<<(w.A + kHbWarps - 1) / kHbWarps, 32 * kHbWarps, 0, st>>>(w, ff);
   k_chain_atom<<<gA, tb, 0, st>>>(w, ff);
   if (w.nB > 0) {
-    k_chain_bond<<<gB, tb, 0, st>>>(w, ff);
+    k_chain_bond<<<gM, tb, 0, st>>>(w, ff);
     k_chain_deltap<<<gA, tb, 0, st>>>(w);
-    k_chain_radial<<<gB, tb, 0, st>>>(w);
+    k_chain_radial<<<gM, tb, 0, st>>>(w);
   }
 }

@@ -98,6 +98,7 @@ struct XrFF {
   const double* pair;         // [T*T][XR_NPAIR_COLS]
   const double* pair_gw;      // [T*T] (1/gamma_w)^g28 for shielded vdW
   const double* pair_logr;    // [T*T][3] log(r_s), log(r_p), log(r_pp) (0 where unused)
+  const double* pair_rmax;    // [T*T] distance beyond which the uncorrected bond order stays below cut/4
   const int* is_carbon;       // [T] label is "C" (case-insensitive): C2 correction applies
   const int* hb_role;         // [T] 1 hydrogen-bond hydrogen, 2 donor/acceptor (p_hbond), 0 otherwise
   const int* angle_index;     // [T^3][2] first, count
@@ -156,8 +157,12 @@ struct XrWork {
   int2* dbrow;                // [D] {bond id, +1 if the atom is the bond's source else -1}
   int2* arow;                 // [D] active bond-row entries (bo > 0.001) at the start of each atom's range
   int* nact;                  // [A] number of active entries per atom
+  int2* nzrow;                // [D] bond-row entries whose uncorrected bond order passed the cut (bo' > 0)
+  int* nnz;                   // [A] number of such entries per atom (every other entry has zero bond orders)
   int* mids;                  // [B] bonds with bo > 0.001 (torsion middles), compacted
   int* nmids;                 // device count of mids
+  int* mlist;                 // [B] active bonds (uncorrected order passed the cut), in any order
+  int* nmask;                 // length of mlist (device)
   // per-atom forward intermediates [AF_N][A] and adjoints [AJ_N][A] (structure of arrays)
   double* a_fwd;
   double* a_adj;

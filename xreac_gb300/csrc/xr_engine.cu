@@ -110,8 +110,12 @@ struct xr_ctx {
   size_t cesum = 0;
   int2* arow = nullptr;
   size_t carow = 0;
+  int2* nzrow = nullptr;
+  int* nnz = nullptr;
+  size_t cnnz = 0;
   int* mids = nullptr;
-  int* nmids = nullptr;
+  int* nmids = nullptr;  // [2] torsion middles, active bonds
+  int* mlist = nullptr;
   int* nact = nullptr;
   size_t cnact = 0;
   int4* chunks = nullptr;
@@ -302,6 +306,7 @@ bool ensure_atoms(xr_ctx* c, int A, int S) {
   GROW(outbuf, 8 * (size_t)A);
   GROW(esum, (size_t)XR_ESUM_N * A);
   GROW(nact, A);
+  GROW(nnz, A);
   GROW(sys_chunks, S);
   GROW(sys, S);
   GROW(energy, 16 * (size_t)S);
@@ -340,8 +345,12 @@ bool ensure_lists(xr_ctx* c, long long E, long long P, long long B) {
     cudaFree(c->b_e);
     cudaFree(c->dbrow);
     cudaFree(c->arow);
+    cudaFree(c->nzrow);
     cudaFree(c->mids);
+    cudaFree(c->mlist);
+    c->mlist = nullptr;
     c->arow = nullptr;
+    c->nzrow = nullptr;
     c->mids = nullptr;
     c->bond_pair = c->bond_i = c->bond_j = nullptr;
     c->b_r = c->b_v = c->b_fwd = c->b_adj = c->b_e = nullptr;
@@ -356,7 +365,9 @@ bool ensure_lists(xr_ctx* c, long long E, long long P, long long B) {
               cudaMalloc((void**)&c->b_e, 4 * nb * sizeof(double)) == cudaSuccess &&
               cudaMalloc((void**)&c->dbrow, 2 * nb * sizeof(int2)) == cudaSuccess &&
               cudaMalloc((void**)&c->arow, 2 * nb * sizeof(int2)) == cudaSuccess &&
-              cudaMalloc((void**)&c->mids, nb * sizeof(int)) == cudaSuccess;
+              cudaMalloc((void**)&c->nzrow, 2 * nb * sizeof(int2)) == cudaSuccess &&
+              cudaMalloc((void**)&c->mids, nb * sizeof(int)) == cudaSuccess &&
+              cudaMalloc((void**)&c->mlist, nb * sizeof(int)) == cudaSuccess;
     if (!ok) return false;
     c->capB = nb;
   }
@@ -392,6 +403,7 @@ void fill_work(xr_ctx* c, XrWork& w, int A, int S, unsigned flags) {
   w.props = c->props;
   w.esum = c->esum;
   w.nact = c->nact;
+  w.nnz = c->nnz;
   w.chunks = c->chunks;
   w.sys_chunks = c->sys_chunks;
   w.chunk_part = c->chunk_part;
@@ -424,8 +436,11 @@ void attach_lists(xr_ctx* c, XrWork& w) {
   w.b_e = c->b_e;
   w.dbrow = c->dbrow;
   w.arow = c->arow;
+  w.nzrow = c->nzrow;
   w.mids = c->mids;
   w.nmids = c->nmids;
+  w.nmask = c->nmids + 1;
+  w.mlist = c->mlist;
 }
 
 // Packs forces (-dE/dx), charges, total bond orders, lone pairs and bond counts per atom.
@@ -806,6 +821,49 @@ int xr_ff_create(const double* general, int ntypes, const double* atom, const do
     logr[3 * pt + 1] = p[P_RP] > 0 ? std::log(p[P_RP]) : 0.0;
     logr[3 * pt + 2] = p[P_RPP] > 0 ? std::log(p[P_RPP]) : 0.0;
   }
+  // Per pair type, the distance beyond which the uncorrected bond order sigma' + pi' + pi-pi' stays
+  // below a quarter of the cut. Each term exp(p_odd (r / r0)^p_even) decreases with r when
+  // p_odd < 0 < p_even; otherwise no bound is used (infinity) and every candidate is evaluated.
+  std::vector<double> rmax(T * T);
+  {
+    const double cut = 0.01 * general[29];
+    for (int pt = 0; pt < T * T; ++pt) {
+      const double* p = pair + pt * XR_NPAIR_COLS;
+      const double* ai = atom + (pt / T) * XR_NATOM_COLS;
+      const double* aj = atom + (pt % T) * XR_NATOM_COLS;
+      const bool use[3] = {ai[A_R_S] > 0 && aj[A_R_S] > 0, ai[A_R_PI] > 0 && aj[A_R_PI] > 0,
+                           ai[A_R_PI_PI] > 0 && aj[A_R_PI_PI] > 0};
+      const double pa[3] = {p[P_BO1], p[P_BO3], p[P_BO5]}, pb[3] = {p[P_BO2], p[P_BO4], p[P_BO6]};
+      const double r0[3] = {p[P_RS], p[P_RP], p[P_RPP]};
+      bool monotone = cut > 0;
+      for (int k = 0; k < 3; ++k)
+        if (use[k] && !(pa[k] < 0 && pb[k] > 0 && r0[k] > 0 && std::isfinite(pa[k]) && std::isfinite(pb[k])))
+          monotone = false;
+      auto raw = [&](double r) {
+        double v = 0;
+        for (int k = 0; k < 3; ++k)
+          if (use[k]) v += (k == 0 ? 1.0 + cut : 1.0) * std::exp(pa[k] * std::pow(r / r0[k], pb[k]));
+        return v;
+      };
+      double bound = INFINITY;
+      if (monotone) {
+        const double target = 0.25 * cut;
+        double lo = 1e-6, hi = 64.0;
+        if (raw(hi) < target) {
+          if (raw(lo) < target) {
+            bound = lo;
+          } else {
+            for (int it = 0; it < 200; ++it) {
+              const double mid = 0.5 * (lo + hi);
+              (raw(mid) < target ? hi : lo) = mid;
+            }
+            bound = hi;
+          }
+        }
+      }
+      rmax[pt] = bound;
+    }
+  }
   auto up = [&](const void* src, size_t bytes) -> void* {
     void* dst = nullptr;
     if (cudaMalloc(&dst, std::max<size_t>(bytes, 16)) != cudaSuccess) return nullptr;
@@ -817,6 +875,7 @@ int xr_ff_create(const double* general, int ntypes, const double* atom, const do
   d.pair = (const double*)up(pair, sizeof(double) * T * T * XR_NPAIR_COLS);
   d.pair_gw = (const double*)up(gw.data(), sizeof(double) * T * T);
   d.pair_logr = (const double*)up(logr.data(), sizeof(double) * 3 * T * T);
+  d.pair_rmax = (const double*)up(rmax.data(), sizeof(double) * T * T);
   d.is_carbon = (const int*)up(is_carbon, sizeof(int) * T);
   std::vector<int> hb_role(T);
   for (int t = 0; t < T; ++t) {
@@ -870,7 +929,7 @@ int xr_ctx_create(int device, void* stream, xr_ctx** out) {
             cudaMalloc((void**)&c->counts, 8 * sizeof(int)) == cudaSuccess &&
             cudaMalloc((void**)&c->barrier, 2 * sizeof(unsigned)) == cudaSuccess &&
             cudaMalloc((void**)&c->bx_count, sizeof(int)) == cudaSuccess &&
-            cudaMalloc((void**)&c->nmids, sizeof(int)) == cudaSuccess &&
+            cudaMalloc((void**)&c->nmids, 2 * sizeof(int)) == cudaSuccess &&
             cudaMallocHost((void**)&c->h_small, 16 * sizeof(int)) == cudaSuccess;
   if (!ok) {
     xr_ctx_destroy(c);
@@ -889,7 +948,7 @@ void xr_ctx_destroy(xr_ctx* c) {
                   c->pair_bond, c->p_r, c->p_shield, c->p_dshield, c->p_g, c->p_evdw, c->p_ecoul, c->bond_pair,
                   c->bond_i, c->bond_j, c->b_r, c->b_v, c->b_fwd, c->b_adj, c->b_e, c->dbrow, c->sys, c->energy,
                   c->props, c->status, c->counts, c->barrier, c->red, c->bx_meta, c->bx_bo, c->bx_count,
-                  c->esum, c->arow, c->nact, c->chunks, c->sys_chunks, c->chunk_part, c->mids, c->nmids};
+                  c->esum, c->arow, c->nact, c->nzrow, c->nnz, c->chunks, c->sys_chunks, c->chunk_part, c->mids, c->nmids, c->mlist};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (c->h_x) cudaFreeHost(c->h_x);
