@@ -44,7 +44,10 @@ typedef struct xr_ff xr_ff;
 typedef struct xr_ctx xr_ctx;
 
 /* One system. positions: natoms x 3. cell: 9 doubles (three row vectors) or NULL when no
- * direction is periodic. types: element numbers in parameter-file order. */
+ * direction is periodic. types: element numbers in parameter-file order. charges_guess: NULL, or
+ * natoms starting charges for the QEq solve (e.g. the previous step's charges of the same system;
+ * shifted to sum to total_charge). It changes only the iteration count: convergence is measured
+ * against the projected residual of the uniform start, so the result meets the same tolerance. */
 typedef struct {
   int natoms;
   const int* types;
@@ -52,6 +55,7 @@ typedef struct {
   const double* cell;
   int pbc[3];
   double total_charge;
+  const double* charges_guess;
 } xr_system;
 
 /* Results of one system. Any pointer may be NULL to skip that output.
@@ -85,6 +89,13 @@ void xr_ff_destroy(xr_ff* ff);
 int xr_ctx_create(int device, void* stream, xr_ctx** out);
 void xr_ctx_destroy(xr_ctx* ctx);
 const char* xr_last_error(const xr_ctx* ctx);
+
+/* Pre-size the context's device and pinned host buffers for batches of up to `atoms` atoms in
+ * `systems` systems with `edges` directed neighbour edges and `bonds` bond candidates (r <= 5 A),
+ * so later calls within these sizes never allocate (no reference counterpart; serving). Buffers
+ * otherwise grow on demand, and a growth frees and reallocates device memory, which synchronises
+ * the whole device. */
+int xr_ctx_reserve(xr_ctx* ctx, int atoms, int systems, long long edges, long long bonds);
 
 /* Solver settings: QEq conjugate-gradient relative residual and iteration limit. */
 int xr_ctx_set_qeq(xr_ctx* ctx, double tolerance, int max_iterations);

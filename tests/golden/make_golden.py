@@ -99,6 +99,9 @@ def workload_cases():
     picked = [r for r in stream if r.system.n <= 160][:8]
     for r in picked:
         add(f"stream_{r.index:02d}", r.system)
+    # A 342-atom C/H/O cluster of the serving stream whose QEq matrix has one negative eigenvalue:
+    # the reference's direct KKT solve accepts it, so an iterative solver must too.
+    add("stream_indefinite_qeq", w.request_stream(n_requests=120)[39].system)
     return out
 
 

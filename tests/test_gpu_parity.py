@@ -233,3 +233,19 @@ def test_small_cell_memory_limit():
     with pytest.raises(ValueError, match="max_expanded_atoms"):
         Calculator(ForceField.bundled("ffield.reax.HO.2015"), max_expanded_atoms=80).evaluate(
             g["symbols"], g["positions"], cell=[4.0] * 3)
+
+
+def test_identical_atoms_need_no_qeq_iterations():
+    """Three O2 molecules: by symmetry of the element the QEq solution is q = 0 exactly, and the
+    start point already solves it (the projected start gradient is pure rounding noise)."""
+    import oracle
+    from xreac_gb300 import ForceField
+
+    x = np.array([[3.50123, 2.24014, 1.17288], [4.30737, 1.30776, 1.52977], [0.98644, 0.98603, 4.08601],
+                  [2.17758, 1.10723, 3.7871], [2.28101, 3.78692, 3.64103], [3.19255, 3.38801, 3.9615]])
+    c = calc("ffield.reax.CHO.2008")
+    r = c.evaluate(["O"] * 6, x)
+    np.testing.assert_allclose(r.charges, 0.0, atol=1e-12)
+    ref = oracle.evaluate(ForceField.bundled("ffield.reax.CHO.2008"), ["O"] * 6, x)
+    assert abs(r.energy - ref["energy"]) <= 1e-9 * 6
+    np.testing.assert_allclose(r.forces, ref["forces"], atol=2e-8, rtol=0)

@@ -36,6 +36,7 @@ EXPORTED = (
     "xr_ctx_destroy",
     "xr_last_error",
     "xr_ctx_set_qeq",
+    "xr_ctx_reserve",
     "xr_eval",
     "xr_eval_batch",
     "xr_get_neighbors",
@@ -60,6 +61,7 @@ class System(ctypes.Structure):
         ("cell", POINTER(c_double)),
         ("pbc", c_int * 3),
         ("total_charge", c_double),
+        ("charges_guess", POINTER(c_double)),
     ]
 
 
@@ -104,6 +106,8 @@ def load():
     lib.xr_last_error.restype = c_char_p
     lib.xr_ctx_set_qeq.argtypes = [c_void_p, c_double, c_int]
     lib.xr_ctx_set_qeq.restype = c_int
+    lib.xr_ctx_reserve.argtypes = [c_void_p, c_int, c_int, c_longlong, c_longlong]
+    lib.xr_ctx_reserve.restype = c_int
     lib.xr_eval.argtypes = [c_void_p, c_void_p, POINTER(System), c_uint, POINTER(Result)]
     lib.xr_eval.restype = c_int
     lib.xr_eval_batch.argtypes = [c_void_p, c_void_p, c_int, POINTER(System), c_uint, POINTER(Result)]

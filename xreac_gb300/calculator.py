@@ -78,6 +78,15 @@ class Evaluation:
         return dense
 
 
+def _guess(initial_charges, n):
+    if initial_charges is None:
+        return None
+    g = np.ascontiguousarray(initial_charges, dtype=np.float64)
+    if g.shape != (n,) or not np.isfinite(g).all():
+        raise ValueError("initial_charges must be a finite array with one charge per atom")
+    return g
+
+
 def _is_carbon(ff):
     return np.array([s.upper() == "C" for s in ff.elements], dtype=np.int32)
 
@@ -97,12 +106,26 @@ class Calculator:
     def set_qeq(self, tolerance=1e-13, max_iterations=2000):
         """QEq solver tolerance and iteration limit.
 
-        ``tolerance`` bounds the preconditioned projected residual relative to its starting value.
-        The default 1e-13 keeps charges within about 1e-12 e of the exact KKT solution, which holds
-        fixed-charge forces of ionic systems (Ti/O) within 2e-8 kcal/mol/A of the reference.
+        ``tolerance`` bounds the preconditioned projected residual relative to its value at the
+        uniform start q = Q/n (also for warm starts from ``initial_charges``). The default 1e-13
+        keeps charges within about 1e-12 e of the exact KKT solution, which holds fixed-charge
+        forces of ionic systems (Ti/O) within 2e-8 kcal/mol/A of the reference.
         """
         if self._lib.xr_ctx_set_qeq(self._ctx.handle, float(tolerance), int(max_iterations)) != nat.XR_OK:
             raise ValueError("QEq tolerance must be positive and the iteration limit at least 1")
+
+    def reserve(self, atoms, systems=1, edges_per_atom=450, bonds_per_atom=30):
+        """Pre-size the device buffers for batches of up to ``atoms`` atoms in ``systems`` systems.
+
+        Buffers otherwise grow on demand, and a growth reallocates device memory, which
+        synchronises the whole device (a stall for every other stream, e.g. other server workers).
+        ``edges_per_atom`` bounds the directed neighbours within the cutoff per atom (about 420 at
+        liquid water density with a 10 A cutoff); ``bonds_per_atom`` the bond candidates within 5 A.
+        """
+        code = self._lib.xr_ctx_reserve(self._ctx.handle, int(atoms), int(systems), int(atoms * edges_per_atom),
+                                        int(atoms * bonds_per_atom))
+        if code != nat.XR_OK:
+            raise RuntimeError(self._ctx.last_error())
 
     def _prepare(self, symbols, positions, total_charge, cell, pbc, full_derivative):
         if not isinstance(full_derivative, bool):
@@ -124,8 +147,13 @@ class Calculator:
         raise ValueError(msg)
 
     def evaluate(self, symbols, positions, *, total_charge=0, cell=None, pbc=None, full_derivative=False,
-                 neighbors=None):
-        """Energy, QEq charges and fixed-charge forces of one system (src/xreac/calculator.py:76-165)."""
+                 neighbors=None, initial_charges=None):
+        """Energy, QEq charges and fixed-charge forces of one system (src/xreac/calculator.py:76-165).
+
+        ``initial_charges`` (an extension; xreac has no such argument) starts the QEq solve from
+        given charges, e.g. those of the previous step of a relaxation or MD run. The result meets
+        the same tolerance; only the iteration count changes.
+        """
         symbols, x, types, flags, cellm, reps = self._prepare(symbols, positions, total_charge, cell, pbc,
                                                               full_derivative)
         backend = "replicated"
@@ -134,71 +162,80 @@ class Calculator:
 
             check_supplied(neighbors, len(symbols), flags)
             reps, backend = (1, 1, 1), "provided"
-        return self._run([(types, x, flags, cellm, float(total_charge))], full_derivative, [reps], backend)[0]
+        guess = _guess(initial_charges, len(symbols))
+        return self._run([(types, x, flags, cellm, float(total_charge), guess)], full_derivative, [reps], backend)[0]
 
     def evaluate_many(self, systems, *, full_derivative=False):
         """Evaluate independent systems in one ragged device batch.
 
         ``systems`` is a sequence of dicts with the keyword arguments of :meth:`evaluate`
-        (``symbols``, ``positions`` and optionally ``total_charge``, ``cell``, ``pbc``).
-        Returns a list of :class:`Evaluation` in the same order.
+        (``symbols``, ``positions`` and optionally ``total_charge``, ``cell``, ``pbc``,
+        ``initial_charges``). Returns a list of :class:`Evaluation` in the same order.
         """
         batch, reps = [], []
         for s in systems:
             sym, x, types, flags, cellm, rp = self._prepare(s["symbols"], s["positions"], s.get("total_charge", 0),
                                                             s.get("cell"), s.get("pbc"), full_derivative)
-            batch.append((types, x, flags, cellm, float(s.get("total_charge", 0))))
+            guess = _guess(s.get("initial_charges"), len(sym))
+            batch.append((types, x, flags, cellm, float(s.get("total_charge", 0)), guess))
             reps.append(rp)
         return self._run(batch, full_derivative, reps, "replicated")
 
     def _run(self, batch, full_derivative, reps, backend):
         lib = self._lib
         n_sys = len(batch)
+        sizes = [len(b[0]) for b in batch]
+        total = sum(sizes)
+        # one allocation per kind for the whole batch; each Evaluation gets views
+        energy = np.zeros((n_sys, 15))
+        dipole = np.zeros((n_sys, 3))
+        forces = np.zeros((total, 3))
+        per_atom = np.zeros((3, total))  # charges, total bond orders, lone pairs
+        counts = np.zeros(total, dtype=np.int32)
         sys_arr = (nat.System * n_sys)()
         res_arr = (nat.Result * n_sys)()
-        outs = []
+        offsets = np.concatenate(([0], np.cumsum(sizes))).astype(int)
         keep = []
-        for k, (types, x, flags, cellm, q) in enumerate(batch):
-            n = len(types)
-            o = dict(
-                energy=np.zeros(15), forces=np.zeros((n, 3)), charges=np.zeros(n), tbo=np.zeros(n), nlp=np.zeros(n),
-                counts=np.zeros(n, dtype=np.int32), dipole=np.zeros(3),
-            )
-            outs.append(o)
-            keep.append((types, x, cellm))
+        for k, (types, x, flags, cellm, q, guess) in enumerate(batch):
+            a0 = offsets[k]
+            keep.append((types, x, cellm, guess))
             s = sys_arr[k]
-            s.natoms = n
+            s.natoms = sizes[k]
             s.types = nat.ptr(types, nat.c_int)
             s.positions = nat.ptr(x, nat.c_double)
             s.cell = nat.ptr(cellm, nat.c_double) if cellm is not None else None
             for d in range(3):
                 s.pbc[d] = int(flags[d])
             s.total_charge = q
+            s.charges_guess = nat.ptr(guess, nat.c_double)
             r = res_arr[k]
-            r.energy = nat.ptr(o["energy"], nat.c_double)
-            r.forces = nat.ptr(o["forces"], nat.c_double)
-            r.charges = nat.ptr(o["charges"], nat.c_double)
-            r.total_bond_orders = nat.ptr(o["tbo"], nat.c_double)
-            r.lone_pairs = nat.ptr(o["nlp"], nat.c_double)
-            r.bond_counts = nat.ptr(o["counts"], nat.c_int)
-            r.dipole = nat.ptr(o["dipole"], nat.c_double)
+            r.energy = nat.ptr(energy[k], nat.c_double)
+            r.forces = nat.ptr(forces[a0:], nat.c_double)
+            r.charges = nat.ptr(per_atom[0, a0:], nat.c_double)
+            r.total_bond_orders = nat.ptr(per_atom[1, a0:], nat.c_double)
+            r.lone_pairs = nat.ptr(per_atom[2, a0:], nat.c_double)
+            r.bond_counts = nat.ptr(counts[a0:], nat.c_int)
+            r.dipole = nat.ptr(dipole[k], nat.c_double)
         flags_ = nat.XR_FLAG_FULL_DERIVATIVE if full_derivative else 0
         code = lib.xr_eval_batch(self._ctx.handle, self._ff.handle, n_sys, sys_arr, flags_, res_arr)
         if code != nat.XR_OK:
             self._raise(code)
+        counts64 = counts.astype(int)
         results = []
-        for k, o in enumerate(outs):
+        for k in range(n_sys):
+            a0, a1 = offsets[k], offsets[k + 1]
+            e = energy[k]
             results.append(
                 Evaluation(
-                    energy=float(o["energy"][14]),
-                    forces=o["forces"],
-                    charges=o["charges"],
-                    components=dict(zip(COMPONENTS, map(float, o["energy"][:14]))),
+                    energy=float(e[14]),
+                    forces=forces[a0:a1],
+                    charges=per_atom[0, a0:a1],
+                    components=dict(zip(COMPONENTS, e[:14].tolist())),
                     full_derivative=full_derivative,
-                    total_bond_orders=o["tbo"],
-                    lone_pairs=o["nlp"],
-                    bond_counts=o["counts"].astype(int),
-                    dipole=o["dipole"],
+                    total_bond_orders=per_atom[1, a0:a1],
+                    lone_pairs=per_atom[2, a0:a1],
+                    bond_counts=counts64[a0:a1],
+                    dipole=dipole[k],
                     cell_repetitions=reps[k],
                     neighbor_backend=backend,
                     bonds=self._bonds(k),

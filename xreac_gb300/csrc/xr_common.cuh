@@ -83,6 +83,7 @@ struct XrSystem {
   double inv[9];         // inverse of cell (row-vector convention: frac = x @ inv)
   double origin[3];      // reference point subtracted before FP32 rounding
   double total_charge;
+  int has_guess;         // QEq starts from w.qguess (charges of an earlier step) instead of Q/n
   double rc, rc2, bond_cut, hb_cut;     // cutoff, cutoff^2, min(5, rc), min(7.5, rc)
   float cellf[9];
   float margin;          // bound on |FP32 squared distance - FP64 squared distance| (A^2)
@@ -169,10 +170,11 @@ struct XrWork {
   double* a_e;                // [8][A] per-atom energies: lp, atom, angle, penalty, coa, hb, qeq, spare
   // charges and forces
   double* q;
+  const double* qguess;       // [A] initial QEq charges of systems with has_guess (sum = total charge)
   double* f;                  // [A][3] gradient dE/dx accumulator (forces = -f)
   double* qwork;              // [XR_QW_N][A] QEq solver vectors
   double* red;                // reduction scratch for solvers
-  unsigned* barrier;          // [2] grid-barrier counter and generation
+  unsigned* barrier;          // [2048] arrival counters of the QEq teams (indexed by a team's first block)
   // outputs
   double* energy;             // [S][16]: 14 components, total, pad
   double* props;              // [S][4]: dipole xyz, pad
@@ -209,7 +211,8 @@ void xr_launch_topology(const XrWork& w, cudaStream_t st);
 void xr_launch_scan(const XrWork& w, cudaStream_t st);
 void xr_launch_topology_fill(const XrWork& w, cudaStream_t st);
 void xr_launch_pairs(const XrWork& w, const XrFF& ff, cudaStream_t st);
-int xr_launch_qeq(const XrWork& w, const XrFF& ff, cudaStream_t st, int coop_blocks);
+int xr_launch_qeq(const XrWork& w, const XrFF& ff, cudaStream_t st, int nblocks, const int4* map, int nteam,
+                  const int* small, int nsmall);
 int xr_qeq_coop_blocks_per_sm();
 void xr_launch_coulomb(const XrWork& w, const XrFF& ff, cudaStream_t st);
 void xr_launch_bonded(const XrWork& w, const XrFF& ff, cudaStream_t st);

@@ -100,6 +100,8 @@ struct xr_ctx {
   size_t ca_e = 0;
   double* q = nullptr;
   size_t cq = 0;
+  double* qguess = nullptr;
+  size_t cqguess = 0;
   double* f = nullptr;
   size_t cf = 0;
   double* qwork = nullptr;
@@ -154,6 +156,11 @@ struct xr_ctx {
   int* status = nullptr;
   int* counts = nullptr;
   unsigned* barrier = nullptr;
+  int4* qmap = nullptr;  // [2048] QEq team blocks of the current batch
+  int* qsmall = nullptr;
+  size_t cqsmall = 0;
+  std::vector<int4> h_qmap;
+  std::vector<int> h_qsmall;
   double* red = nullptr;
   size_t cred = 0;
   // per-stage timing (CUDA events on the context stream), enabled by xr_ctx_set_profiling
@@ -175,6 +182,8 @@ struct xr_ctx {
   size_t ch_x = 0;
   double* h_out = nullptr;
   size_t ch_out = 0;
+  double* h_guess = nullptr;
+  size_t ch_guess = 0;
   int* h_small = nullptr;  // status + counts
 };
 
@@ -301,6 +310,7 @@ bool ensure_atoms(xr_ctx* c, int A, int S) {
   GROW(a_adj, (size_t)AJ_N * A);
   GROW(a_e, 8 * (size_t)A);
   GROW(q, A);
+  GROW(qguess, A);
   GROW(f, 3 * (size_t)A);
   GROW(qwork, (size_t)XR_QW_N * A);
   GROW(outbuf, 8 * (size_t)A);
@@ -308,11 +318,12 @@ bool ensure_atoms(xr_ctx* c, int A, int S) {
   GROW(nact, A);
   GROW(nnz, A);
   GROW(sys_chunks, S);
+  GROW(qsmall, S);
   GROW(sys, S);
   GROW(energy, 16 * (size_t)S);
   GROW(props, 4 * (size_t)S);
   const size_t scan_ints = 4 * ((size_t)(A + 1) / 4096 + 2);
-  const size_t red = std::max<size_t>(scan_ints / 2 + 8, (size_t)4 * 4 * 2048);
+  const size_t red = std::max<size_t>(scan_ints / 2 + 8, (size_t)4 * 8 * 2048);
   GROW(red, red);
   return true;
 }
@@ -440,6 +451,7 @@ void attach_lists(xr_ctx* c, XrWork& w) {
   w.mids = c->mids;
   w.nmids = c->nmids;
   w.nmask = c->nmids + 1;
+  w.qguess = c->qguess;
   w.mlist = c->mlist;
 }
 
@@ -535,6 +547,51 @@ int status_to_code(xr_ctx* c, int st) {
   return XR_OK;
 }
 
+// QEq work plan of a batch for the cooperative solver (at most kQeqBlocks co-resident blocks):
+// systems above kQeqSmall atoms get a team of ceil(n / 32) blocks (32 rows per 1024-thread block),
+// scaled down when the teams do not fit; the other systems are shared, largest first and round
+// robin, by the remaining blocks, each solving its systems alone. A one-block team is no team:
+// such a system joins the small ones.
+constexpr int kQeqSmall = 160;
+constexpr int kQeqBlocks = 2048;
+
+void plan_qeq(xr_ctx* c, const xr_system* sys, int nsys, int* nblocks, int* nteam, int* nsmall) {
+  const int budget = std::min(c->nsm * c->coop_per_sm, kQeqBlocks);
+  std::vector<int> large, small;
+  for (int s = 0; s < nsys; ++s) (sys[s].natoms > kQeqSmall ? large : small).push_back(s);
+  std::sort(large.begin(), large.end(), [&](int a, int b) { return sys[a].natoms > sys[b].natoms; });
+  std::vector<int> team(large.size());
+  for (;;) {
+    const int small_blocks = small.empty() ? 0 : (large.empty() ? std::min<int>((int)small.size(), budget)
+                                                                 : std::min<int>((int)small.size(), std::max(1, budget / 4)));
+    const int avail = budget - small_blocks;
+    long long want = 0;
+    for (size_t k = 0; k < large.size(); ++k) want += (sys[large[k]].natoms + 31) / 32;
+    long long have = 0;
+    for (size_t k = 0; k < large.size(); ++k) {
+      const long long d = (sys[large[k]].natoms + 31) / 32;
+      team[k] = (int)std::max<long long>(2, want > avail ? d * avail / std::max<long long>(want, 1) : d);
+      have += team[k];
+    }
+    if (have <= avail || large.empty()) {
+      *nsmall = (int)small.size();
+      std::sort(small.begin(), small.end(), [&](int a, int b) { return sys[a].natoms > sys[b].natoms; });
+      c->h_qsmall.assign(small.begin(), small.end());
+      c->h_qmap.clear();
+      for (size_t k = 0; k < large.size(); ++k) {
+        const int first = (int)c->h_qmap.size();
+        for (int r = 0; r < team[k]; ++r) c->h_qmap.push_back(make_int4(large[k], r, team[k], first));
+      }
+      *nteam = (int)c->h_qmap.size();
+      *nblocks = *nteam + small_blocks;
+      return;
+    }
+    small.push_back(large.back());  // the smallest large system is solved by one block
+    large.pop_back();
+    team.pop_back();
+  }
+}
+
 int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsigned flags, xr_result* out) {
   if (!c || !ff || nsys < 1 || !sys) {
     if (c) c->err = "invalid arguments";
@@ -569,6 +626,7 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
     return cuda_fail(c, cudaErrorMemoryAllocation, "allocation");
   c->host_sys.resize(nsys);
   std::vector<int> types(A), sys_of(A);
+  bool any_guess = false;
   int off = 0;
   for (int s = 0; s < nsys; ++s) {
     const xr_system& in = sys[s];
@@ -592,6 +650,28 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
       }
       types[off + a] = t;
       sys_of[off + a] = s;
+    }
+    if (in.charges_guess) {
+      // starting charges of the QEq solve (a warm start), shifted onto sum q = total_charge
+      if (!host_grow(&c->h_guess, &c->ch_guess, (size_t)A)) return cuda_fail(c, cudaErrorMemoryAllocation, "allocation");
+      double* hg = c->h_guess + off;
+      if (dev_io) {
+        cudaMemcpy(hg, in.charges_guess, sizeof(double) * in.natoms, cudaMemcpyDeviceToHost);
+      } else {
+        std::memcpy(hg, in.charges_guess, sizeof(double) * in.natoms);
+      }
+      double sum = 0;
+      for (int a = 0; a < in.natoms; ++a) {
+        if (!std::isfinite(hg[a])) {
+          c->err = "initial charges must be finite";
+          return XR_EINPUT;
+        }
+        sum += hg[a];
+      }
+      const double shift = (in.total_charge - sum) / in.natoms;
+      for (int a = 0; a < in.natoms; ++a) hg[a] += shift;
+      c->host_sys[s].has_guess = 1;
+      any_guess = true;
     }
     off += in.natoms;
   }
@@ -617,6 +697,10 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
   } else {
     cudaMemcpyAsync(c->x, c->h_x, sizeof(double4_32a) * A, cudaMemcpyHostToDevice, st);
     h2d += sizeof(double4_32a) * (long long)A;
+  }
+  if (any_guess) {
+    cudaMemcpyAsync(c->qguess, c->h_guess, sizeof(double) * A, cudaMemcpyHostToDevice, st);
+    h2d += sizeof(double) * (long long)A;
   }
   cudaMemcpyAsync(c->type, types.data(), sizeof(int) * A, cudaMemcpyHostToDevice, st);
   cudaMemcpyAsync(c->sys_of, sys_of.data(), sizeof(int) * A, cudaMemcpyHostToDevice, st);
@@ -660,14 +744,15 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
   xr_launch_pairs(w, ff->d, st);
   launches += 2;
   stage(c, 3, st);
-  int coop = 0;
-  if (nsys == 1) {
-    const int rows_blocks = (A + 31) / 32;  // 32 warps (rows) per 1024-thread block
-    coop = std::min(c->nsm * std::max(c->coop_per_sm, 1), rows_blocks);
-    coop = std::min(coop, 2048);
-    if (coop < 2) coop = 0;
+  int qblocks = 0, qteam = 0, qsmall = 0;
+  if (c->coop_per_sm > 0) {
+    plan_qeq(c, sys, nsys, &qblocks, &qteam, &qsmall);
+    if (qteam > 0) cudaMemcpyAsync(c->qmap, c->h_qmap.data(), sizeof(int4) * qteam, cudaMemcpyHostToDevice, st);
+    if (qsmall > 0) cudaMemcpyAsync(c->qsmall, c->h_qsmall.data(), sizeof(int) * qsmall, cudaMemcpyHostToDevice, st);
+    h2d += sizeof(int4) * (long long)qteam + sizeof(int) * (long long)qsmall;
   }
-  if (int le = xr_launch_qeq(w, ff->d, st, coop)) return cuda_fail(c, (cudaError_t)le, "QEq launch");
+  if (int le = xr_launch_qeq(w, ff->d, st, qblocks, c->qmap, qteam, c->qsmall, qsmall))
+    return cuda_fail(c, (cudaError_t)le, "QEq launch");
   launches += 1;
   stage(c, 4, st);
   xr_launch_coulomb(w, ff->d, st);
@@ -927,7 +1012,8 @@ int xr_ctx_create(int device, void* stream, xr_ctx** out) {
   if (!coop_ok) c->coop_per_sm = 0;
   bool ok = cudaMalloc((void**)&c->status, sizeof(int)) == cudaSuccess &&
             cudaMalloc((void**)&c->counts, 8 * sizeof(int)) == cudaSuccess &&
-            cudaMalloc((void**)&c->barrier, 2 * sizeof(unsigned)) == cudaSuccess &&
+            cudaMalloc((void**)&c->barrier, kQeqBlocks * sizeof(unsigned)) == cudaSuccess &&
+            cudaMalloc((void**)&c->qmap, kQeqBlocks * sizeof(int4)) == cudaSuccess &&
             cudaMalloc((void**)&c->bx_count, sizeof(int)) == cudaSuccess &&
             cudaMalloc((void**)&c->nmids, 2 * sizeof(int)) == cudaSuccess &&
             cudaMallocHost((void**)&c->h_small, 16 * sizeof(int)) == cudaSuccess;
@@ -947,12 +1033,13 @@ void xr_ctx_destroy(xr_ctx* c) {
                   c->qwork, c->outbuf, c->edge, c->edge_pair, c->edge_dbslot, c->hval, c->pair_edge, c->pair_i,
                   c->pair_bond, c->p_r, c->p_shield, c->p_dshield, c->p_g, c->p_evdw, c->p_ecoul, c->bond_pair,
                   c->bond_i, c->bond_j, c->b_r, c->b_v, c->b_fwd, c->b_adj, c->b_e, c->dbrow, c->sys, c->energy,
-                  c->props, c->status, c->counts, c->barrier, c->red, c->bx_meta, c->bx_bo, c->bx_count,
+                  c->props, c->status, c->counts, c->barrier, c->qmap, c->qsmall, c->red, c->qguess, c->bx_meta, c->bx_bo, c->bx_count,
                   c->esum, c->arow, c->nact, c->nzrow, c->nnz, c->chunks, c->sys_chunks, c->chunk_part, c->mids, c->nmids, c->mlist};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (c->h_x) cudaFreeHost(c->h_x);
   if (c->h_out) cudaFreeHost(c->h_out);
+  if (c->h_guess) cudaFreeHost(c->h_guess);
   if (c->h_small) cudaFreeHost(c->h_small);
   for (int k = 0; k <= xr_ctx::kStages; ++k)
     if (c->ev[k]) cudaEventDestroy(c->ev[k]);
@@ -1035,6 +1122,21 @@ int xr_get_bonds(xr_ctx* c, int index, int* i, int* j, int* S, double* bo, long 
     S[3 * k + 2] = xr_sz(code);
     bo[k] = c->h_bx_bo[it - m.begin()];
   }
+  return XR_OK;
+}
+
+int xr_ctx_reserve(xr_ctx* c, int atoms, int systems, long long edges, long long bonds) {
+  if (!c || atoms < 1 || systems < 1 || edges < 0 || bonds < 0) return XR_EINPUT;
+  cudaSetDevice(c->device);
+  const long long chunks = (long long)systems + atoms / XR_CHUNK_ATOMS + 1;
+  if (!ensure_atoms(c, atoms, systems) || !host_grow(&c->h_x, &c->ch_x, (size_t)atoms) ||
+      !host_grow(&c->h_out, &c->ch_out, 8 * (size_t)atoms + 32 * (size_t)systems + 8) ||
+      !host_grow(&c->h_guess, &c->ch_guess, (size_t)atoms) || !ensure_lists(c, edges, edges / 2, bonds) ||
+      !grow(&c->chunks, &c->cchunks, (size_t)chunks) ||
+      !grow(&c->chunk_part, &c->cchunk_part, (size_t)chunks * XR_PART_N) ||
+      !grow(&c->bx_meta, &c->cbx_meta, (size_t)std::max<long long>(bonds, 1)) ||
+      !grow(&c->bx_bo, &c->cbx_bo, (size_t)std::max<long long>(bonds, 1)))
+    return cuda_fail(c, cudaErrorMemoryAllocation, "reservation");
   return XR_OK;
 }
 

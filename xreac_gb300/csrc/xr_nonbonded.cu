@@ -139,36 +139,41 @@ __device__ bool grid_barrier(unsigned* bar, unsigned target, int* status) {
 // Team: the whole cooperative grid on one system, or one block on one system of a batch.
 // Results of a reduction land in one of two result slots (by the parity of `slot`), so a reduction
 // may write its totals while a slow warp still reads the previous reduction's.
-__device__ inline double* result_slot(double* smem, int slot) { return smem + 128 + 4 * (slot & 1); }
+// smem layout of the reductions: per-warp inputs at [k * 32 + warp] (k < 8), results from 256 on.
+constexpr int kRedSmem = 8 * 32 + 16;
+__device__ inline double* result_slot(double* smem, int slot) { return smem + 256 + 8 * (slot & 1); }
 
 struct GridTeam {
-  mutable unsigned target = 0;  // barrier episodes so far times the number of blocks
+  unsigned* bar;                // arrival counter of this team (zeroed before the launch)
+  double* red;                  // the team's reduction slots: [slot][value][rank]
+  int nb, rank;                 // blocks in the team and this block's rank
+  mutable unsigned target = 0;  // barrier episodes so far times nb
   __device__ bool sync(const XrWork& w) const {
-    target += gridDim.x;
-    return grid_barrier(w.barrier, target, w.status);
+    target += nb;
+    return grid_barrier(bar, target, w.status);
   }
-  // Grid-wide sum of NV block totals held by lane 0 of warp 0, fused with the barrier: lane 0
+  // Team-wide sum of NV block totals held by lane 0 of warp 0, fused with the barrier: lane 0
   // publishes the block's values into a fixed slot and arrives (release); after the bounded wait
-  // warp 0 adds all blocks' values in block order (deterministic), thread 0 runs post() on the
+  // warp 0 adds all blocks' values in rank order (deterministic), thread 0 runs post() on the
   // totals (scalar work that then costs no extra synchronisation), and every thread receives them.
   template <int NV, class Post>
   __device__ bool reduce(const XrWork& w, double* v, double* smem, int slot, Post post) const {
-    static_assert(NV <= 4, "at most four values per reduction");
+    static_assert(NV <= 8, "at most eight values per reduction");
     __shared__ int ok;
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    target += gridDim.x;
+    target += nb;
     double* res = result_slot(smem, slot);
     // Fixed-size slots; consecutive reductions never share one, so a block may publish the next
     // partials while a slower block still reads the previous ones.
-    double* red = w.red + (size_t)slot * 4 * gridDim.x;
+    double* rs = red + (size_t)slot * 8 * nb;
     if (wid == 0) {
       int good = 1;
       __syncwarp();  // orders warp 0's row writes before lane 0's release
       if (lane == 0) {
-        for (int k = 0; k < NV; ++k) red[k * gridDim.x + blockIdx.x] = v[k];
-        asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(w.barrier) : "memory");
+        for (int k = 0; k < NV; ++k) rs[k * nb + rank] = v[k];
+        asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(bar) : "memory");
         long long it = 0;
-        while (ld_acquire(w.barrier) < target) {
+        while (ld_acquire(bar) < target) {
           if (++it > (1ll << 24) || (*(volatile int*)w.status & XR_S_BARRIER)) {
             atomicOr(w.status, XR_S_BARRIER);
             good = 0;
@@ -181,7 +186,7 @@ struct GridTeam {
       __syncwarp();
       for (int k = 0; k < NV; ++k) {
         double t = 0;
-        for (unsigned q = lane; q < gridDim.x; q += 32) t += __ldcg(red + k * gridDim.x + q);
+        for (int q = lane; q < nb; q += 32) t += __ldcg(rs + k * nb + q);
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
         if (lane == 0) res[k] = t;
@@ -236,6 +241,18 @@ __device__ inline double warp_total(double t) {
   return t;
 }
 
+// Block-shared state of one solve: the reductions' buffer, the iteration scalars (written by thread 0
+// in the reductions' post hooks), the tile transposition buffers and, for blocks of at most 32 rows,
+// the rows' solver state indexed by row - r0. One instance per kernel serves both team kinds.
+struct QeqShared {
+  double red[kRedSmem];
+  double sc_lam, sc_alpha, sc_step, sc_beta;
+  int sc_state;  // 0 iterate, 1 converged, 2 stop
+  double part[32][33];
+  double part4[4][32];
+  double rs_x[32], rs_p[32], rs_hp[32], rs_di[32], rs_c[32], rs_eta[32], rs_g[32];
+};
+
 // Rows [r0, r1) of the system starting at atom a0 belong to this block. The matrix-vector product
 // runs on tiles of 32 rows, one row per warp; the lanes' partial row sums are transposed through
 // shared memory so that one warp owns the 32 rows of a tile, one row per lane, for the row
@@ -246,8 +263,15 @@ __device__ inline double warp_total(double t) {
 // when `gstage` is non-null the whole gradient is staged in shared memory every iteration.
 template <class Team>
 __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int a0, int n, int r0, int r1,
-                          double Q, double* smem, unsigned short* cache_j, double* cache_h, int cache_cap,
-                          double* gstage) {
+                          double Q, bool warm, QeqShared& sh, unsigned short* cache_j, double* cache_h,
+                          int cache_cap, double* gstage) {
+  double* smem = sh.red;
+  double &sc_lam = sh.sc_lam, &sc_alpha = sh.sc_alpha, &sc_step = sh.sc_step, &sc_beta = sh.sc_beta;
+  int& sc_state = sh.sc_state;
+  auto& part = sh.part;
+  auto& part4 = sh.part4;
+  double *rs_x = sh.rs_x, *rs_p = sh.rs_p, *rs_hp = sh.rs_hp, *rs_di = sh.rs_di, *rs_c = sh.rs_c, *rs_eta = sh.rs_eta,
+         *rs_g = sh.rs_g;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   double* X = &QW(Q_X, 0);
   double* G = &QW(Q_G, 0);
@@ -257,7 +281,9 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
   double* DI = &QW(Q_DINV, 0);
   double* Cr = &QW(Q_C, 0);
   auto noop = [](double*) {};
-  // 1. Jacobi diagonal (eta + self-image shields) of the owned rows.
+  const double x0 = Q / n;
+  // 1. Jacobi diagonal (eta + self-image shields) of the owned rows, and the start point: the
+  //    uniform x0 = Q/n, or the caller's charges of an earlier step (already summing to Q).
   for (int r = r0 + wid; r < r1; r += nw) {
     const int a = a0 + r;
     double d = 0;
@@ -265,25 +291,30 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
       if (w.edge[e].x == a) d += w.hval[e];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
-    if (lane == 0) DI[a] = 1.0 / (atom_prm(ff, w.type[a], A_ETA) + d);
+    if (lane == 0) {
+      DI[a] = 1.0 / (atom_prm(ff, w.type[a], A_ETA) + d);
+      X[a] = warm ? w.qguess[a] : x0;
+    }
   }
   if (!team.sync(w)) return;
   // 2. Pre-scaled rows H'_ij = H_ij / D_jj (cached or in hval), row sums, and the start point
   //    x0 = Q/n with gradient g0 = H x0 + chi = (Q/n) * rowsum(H) + chi.
   const int ebeg = w.cnt[a0 + r0], eend = w.cnt[a0 + r1];
   const bool cached = cache_j != nullptr && (eend - ebeg) <= cache_cap;
-  const double x0 = Q / n;
-  double acc[3] = {0, 0, 0};  // <D^-1, 1>, <D^-1, g>, <D^-1, g^2>
+  // <D^-1, 1>, <D^-1, g>, <D^-1, g^2> at the start point, and <D^-1, g_u>, <D^-1, g_u^2> at the
+  // uniform start x0, whose projected norm sets the convergence scale for cold and warm starts alike
+  double acc[5] = {0, 0, 0, 0, 0};
   for (int r = r0 + wid; r < r1; r += nw) {
     const int a = a0 + r;
     const int t = w.type[a];
-    double rs = 0, cs = 0;
+    double rs = 0, cs = 0, hx = 0;
     for (int e = w.cnt[a] + lane; e < w.cnt[a + 1]; e += 32) {
       const int j = w.edge[e].x;
       const double h = w.hval[e];
       const double hp = h * __ldcg(DI + j);
       rs += h;
       cs += hp;
+      if (warm) hx += h * __ldcg(X + j);
       if (cached) {
         cache_j[e - ebeg] = (unsigned short)(j - a0);
         cache_h[e - ebeg] = hp;
@@ -295,42 +326,59 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
     for (int o = 16; o > 0; o >>= 1) {
       rs += __shfl_xor_sync(0xffffffffu, rs, o);
       cs += __shfl_xor_sync(0xffffffffu, cs, o);
+      if (warm) hx += __shfl_xor_sync(0xffffffffu, hx, o);
     }
     if (lane == 0) {
-      const double eta = atom_prm(ff, t, A_ETA), di = DI[a];
-      const double g = x0 * (rs + eta) + atom_prm(ff, t, A_CHI);
+      const double eta = atom_prm(ff, t, A_ETA), di = DI[a], chi = atom_prm(ff, t, A_CHI);
+      const double gu = x0 * (rs + eta) + chi;
+      const double g = warm ? hx + eta * X[a] + chi : gu;
       Cr[a] = cs + eta * di;
-      X[a] = x0;
       G[a] = g;
       Pv[a] = 0.0;
-      HP[a] = 0.0;
+      HP[a] = gu;  // kept for the projection step below, then cleared
       acc[0] += di;
       acc[1] += di * g;
       acc[2] += di * g * g;
+      acc[3] += di * gu;
+      acc[4] += di * gu * gu;
     }
   }
-  if (!team_sum<3>(team, w, acc, smem, 0, noop)) return;
+  if (!team_sum<5>(team, w, acc, smem, 0, noop)) return;
   // Iteration scalars are computed by thread 0 alone (in the reductions' post hooks) and shared.
-  __shared__ double sc_lam, sc_alpha, sc_step, sc_beta;
-  __shared__ int sc_state;  // 0 iterate, 1 converged, 2 stop
   const double s1 = acc[0];
-  double gz = 0.0, gz0 = 0.0;
-  const double tol2 = w.cg_tol * w.cg_tol;
-  const double gfloor = 1e-28 * acc[2];
-  if (threadIdx.x == 0) {
-    sc_lam = acc[1] / s1;
-    gz = acc[2] - sc_lam * acc[1];
-    gz0 = gz;
-    sc_beta = 0.0;
-    // Nothing to solve when the projected gradient is already at rounding level (one atom, or a
-    // start that is exact by symmetry).
-    sc_state = (!(gz0 > gfloor) || n < 2) ? 1 : 0;
+  // 3. Project the start gradient explicitly (g - lambda with lambda = <D^-1, g> / <D^-1, 1>) and take
+  //    its norm from the projected values: sum D^-1 g^2 - lambda sum D^-1 g cancels to rounding noise
+  //    of the unprojected gradient when the start is (nearly) the solution, e.g. q = 0 for identical
+  //    atoms. The uniform start's projected norm sets the convergence scale.
+  const double lam0 = acc[1] / s1, lamu = acc[3] / s1;
+  double acc2[3] = {0, 0, 0};  // <D^-1, g~^2>, <D^-1, g~_u^2>, <D^-1, g~>
+  for (int r = r0 + wid; r < r1; r += nw) {
+    const int a = a0 + r;
+    if (lane == 0) {
+      const double di = DI[a];
+      const double gt = G[a] - lam0;
+      const double gut = HP[a] - lamu;  // the uniform start's gradient, parked in HP by step 2
+      G[a] = gt;
+      HP[a] = 0.0;
+      acc2[0] += di * gt * gt;
+      acc2[1] += di * gut * gut;
+      acc2[2] += di * gt;
+    }
   }
-  // Tile transposition buffers and, for blocks of at most 32 rows (the grid layout), the rows'
-  // solver state, indexed by lane = row - r0.
-  __shared__ double part[32][33];
-  __shared__ double part4[4][32];
-  __shared__ double rs_x[32], rs_p[32], rs_hp[32], rs_di[32], rs_c[32], rs_eta[32], rs_g[32];
+  const double tol2 = w.cg_tol * w.cg_tol;
+  const double gfloor = 1e-28 * fmax(acc[2], acc[4]);
+  double gz = 0.0, gz0 = 0.0;
+  if (!team_sum<3>(team, w, acc2, smem, 1, noop)) return;
+  if (threadIdx.x == 0) {
+    gz = acc2[0];
+    gz0 = acc2[1];  // the uniform start's projected norm (= gz when cold)
+    sc_lam = acc2[2] / s1;  // rounding-level drift of the projection, removed in the first step
+    sc_beta = 0.0;
+    // Nothing to solve when the projected gradient is already at rounding level (one atom, a start
+    // that is exact by symmetry) or a warm start already meets the tolerance.
+    sc_state = (!(gz > gfloor) || n < 2 || gz <= tol2 * gz0) ? 1 : 0;
+  }
+  // For blocks of at most 32 rows (the grid layout) the rows' solver state lives in shared memory.
   const bool row_smem = (r1 - r0) <= 32;
   if (row_smem && wid == 0 && r0 + lane < r1) {
     const int a = a0 + r0 + lane;
@@ -344,7 +392,7 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
   }
   __syncthreads();
   int it = 0;
-  int slot = 1;
+  int slot = 2;
   while (sc_state == 0) {
     if (++it > w.cg_max_iter) {
       if (threadIdx.x == 0) atomicOr(w.status, XR_S_CG);
@@ -419,9 +467,13 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
       pHp[1] = warp_total(pHp[1]);
     }
     if (!team.template reduce<2>(w, pHp, smem, slot, [&](double* t) {
-          if (!(t[0] > 0.0)) {
-            // a vanishing direction after convergence to rounding level is not a failure
-            if (!(gz <= 1e4 * gfloor)) atomicOr(w.status, XR_S_NONSPD);
+          // The QEq matrix of a close-packed geometry can have a negative eigenvalue (the reference's
+          // direct KKT solve accepts it); CG then takes steps of negative curvature (alpha < 0) and
+          // still converges. Only an exactly vanishing or non-finite p'Hp is a breakdown, and a
+          // non-positive one at rounding level means the solve has converged.
+          const bool rounding = gz <= 1e4 * gfloor;
+          if (!(fabs(t[0]) > 0.0) || !isfinite(t[0]) || (t[0] < 0.0 && rounding)) {
+            if (!rounding) atomicOr(w.status, XR_S_NONSPD);
             sc_state = 2;
           } else {
             sc_alpha = gz / t[0];
@@ -487,29 +539,62 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
   }
 }
 
-// Dynamic shared memory of the grid solver: [gradient stage: n doubles][row cache values][row cache
-// columns (16-bit, local to the system)]. The host sizes the two parts per launch.
+// Dynamic shared memory of the solver kernel: [gradient stage: n doubles][row cache values][row
+// cache columns (16-bit, local to the system)]. Each system's solve splits it the same way.
 constexpr int kQeqMaxDyn = 208 * 1024;
 
-__global__ void __launch_bounds__(1024, 1) k_qeq_grid(XrWork w, XrFF ff, int stage_n, int cache_cap) {
-  __shared__ double smem[4 * 32 + 8];  // reductions: per-warp inputs, then results at 128..
-  extern __shared__ __align__(16) unsigned char dyn[];
-  const XrSystem& S = w.sys[0];
-  const int per = ((S.natoms + gridDim.x - 1) / gridDim.x + 31) / 32 * 32;
-  const int r0 = min(S.natoms, (int)blockIdx.x * per), r1 = min(S.natoms, r0 + per);
-  double* gstage = stage_n > 0 ? reinterpret_cast<double*>(dyn) : nullptr;
-  double* cache_h = reinterpret_cast<double*>(dyn + sizeof(double) * (size_t)stage_n);
-  unsigned short* cache_j = reinterpret_cast<unsigned short*>(dyn + sizeof(double) * ((size_t)stage_n + cache_cap));
-  GridTeam team;
-  qeq_solve(w, ff, team, S.atom_off, S.natoms, r0, r1, S.total_charge, smem, cache_cap > 0 ? cache_j : nullptr,
-            cache_h, cache_cap, gstage);
+__device__ inline void qeq_smem_plan(unsigned char* dyn, int n, double** gstage, double** cache_h,
+                                     unsigned short** cache_j, int* cache_cap) {
+  // stage the gradient when it takes at most half the space; 16-bit cache columns need n <= 65536
+  const int stage_n = (n * 8 <= kQeqMaxDyn / 2) ? n : 0;
+  const int cap = n <= 65536 ? (int)((kQeqMaxDyn - (size_t)stage_n * 8) / (sizeof(double) + sizeof(unsigned short))) : 0;
+  *gstage = stage_n > 0 ? reinterpret_cast<double*>(dyn) : nullptr;
+  *cache_h = reinterpret_cast<double*>(dyn + sizeof(double) * (size_t)stage_n);
+  *cache_j = cap > 0 ? reinterpret_cast<unsigned short*>(dyn + sizeof(double) * ((size_t)stage_n + cap)) : nullptr;
+  *cache_cap = cap;
 }
 
+// Cooperative solver launch for a batch: the first nteam blocks form teams, one per large system
+// (map[b] = {system, rank, team size, first block of the team}); each team splits its system's rows
+// and synchronises through its own bounded counter. The remaining blocks each solve a share of the
+// small systems (small[k], k = b - nteam, b - nteam + (gridDim.x - nteam), ...) alone, with block
+// barriers only. All blocks are co-resident (cooperative launch, one block per SM).
+__global__ void __launch_bounds__(1024, 1) k_qeq_grid(XrWork w, XrFF ff, const int4* map, int nteam, const int* small,
+                                                      int nsmall) {
+  __shared__ QeqShared sh;
+  extern __shared__ __align__(16) unsigned char dyn[];
+  double *gstage, *cache_h;
+  unsigned short* cache_j;
+  int cache_cap;
+  if ((int)blockIdx.x < nteam) {
+    const int4 m = map[blockIdx.x];
+    const XrSystem& S = w.sys[m.x];
+    const int per = ((S.natoms + m.z - 1) / m.z + 31) / 32 * 32;
+    const int r0 = min(S.natoms, m.y * per), r1 = min(S.natoms, r0 + per);
+    qeq_smem_plan(dyn, S.natoms, &gstage, &cache_h, &cache_j, &cache_cap);
+    GridTeam team{w.barrier + m.w, w.red + (size_t)32 * m.w, m.z, m.y};
+    qeq_solve(w, ff, team, S.atom_off, S.natoms, r0, r1, S.total_charge, S.has_guess != 0, sh, cache_j, cache_h,
+              cache_cap, gstage);
+    return;
+  }
+  const int nsb = (int)gridDim.x - nteam;
+  for (int k = (int)blockIdx.x - nteam; k < nsmall; k += nsb) {
+    const XrSystem& S = w.sys[small[k]];
+    qeq_smem_plan(dyn, S.natoms, &gstage, &cache_h, &cache_j, &cache_cap);
+    BlockTeam team;
+    qeq_solve(w, ff, team, S.atom_off, S.natoms, 0, S.natoms, S.total_charge, S.has_guess != 0, sh, cache_j, cache_h,
+              cache_cap, gstage);
+    __syncthreads();
+  }
+}
+
+// Fallback without cooperative launch: one block per system, no shared-memory row cache.
 __global__ void __launch_bounds__(1024, 1) k_qeq_block(XrWork w, XrFF ff) {
-  __shared__ double smem[4 * 32 + 8];  // reductions: per-warp inputs, then results at 128..
+  __shared__ QeqShared sh;
   const XrSystem& S = w.sys[blockIdx.x];
   BlockTeam team;
-  qeq_solve(w, ff, team, S.atom_off, S.natoms, 0, S.natoms, S.total_charge, smem, nullptr, nullptr, 0, nullptr);
+  qeq_solve(w, ff, team, S.atom_off, S.natoms, 0, S.natoms, S.total_charge, S.has_guess != 0, sh, nullptr, nullptr,
+            0, nullptr);
 }
 
 // ------------------------------------------------------------------------------ Coulomb
@@ -680,20 +765,15 @@ int xr_qeq_coop_blocks_per_sm() {
   return nb;
 }
 
-// Returns 0 on success or a CUDA error code from the launch.
-int xr_launch_qeq(const XrWork& w, const XrFF& ff, cudaStream_t st, int coop_blocks) {
-  if (w.S == 1 && coop_blocks > 1) {
-    // coop_blocks is already clamped by the host to the co-resident maximum and to the rows.
-    const int blocks = coop_blocks;
-    const int n = w.A;
-    // Stage the gradient when it takes at most half the budget; columns of the row cache are
-    // 16-bit offsets, so the cache needs a system of at most 65536 atoms.
-    int stage_n = (n * 8 <= kQeqMaxDyn / 2) ? n : 0;
-    int cache_cap = n <= 65536 ? (int)((kQeqMaxDyn - (size_t)stage_n * 8) / (sizeof(double) + sizeof(unsigned short))) : 0;
-    const size_t dyn = (size_t)stage_n * 8 + (size_t)cache_cap * (sizeof(double) + sizeof(unsigned short));
-    cudaMemsetAsync(w.barrier, 0, 2 * sizeof(unsigned), st);
-    void* args[] = {(void*)&w, (void*)&ff, (void*)&stage_n, (void*)&cache_cap};
-    cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_qeq_grid, dim3(blocks), dim3(1024), args, dyn, st);
+// Returns 0 on success or a CUDA error code from the launch. With nblocks > 0 the cooperative
+// solver runs nblocks blocks (nteam team blocks described by map, the rest over the small list);
+// nblocks = 0 selects the one-block-per-system fallback.
+int xr_launch_qeq(const XrWork& w, const XrFF& ff, cudaStream_t st, int nblocks, const int4* map, int nteam,
+                  const int* small, int nsmall) {
+  if (nblocks > 0) {
+    if (nteam > 0) cudaMemsetAsync(w.barrier, 0, sizeof(unsigned) * (size_t)nteam, st);
+    void* args[] = {(void*)&w, (void*)&ff, (void*)&map, (void*)&nteam, (void*)&small, (void*)&nsmall};
+    cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_qeq_grid, dim3(nblocks), dim3(1024), args, kQeqMaxDyn, st);
     return (int)e;
   }
   k_qeq_block<<<w.S, 1024, 0, st>>>(w, ff);

@@ -320,14 +320,23 @@ class ForceField:
 
     def validate_model(self, elements=None):
         """Reject models outside the implemented equations (src/xreac/forcefield.py:317-341)."""
+        if elements is not None:
+            key = frozenset(elements)
+            validated = self.__dict__.setdefault("_validated_elements", set())
+            if key in validated:
+                return
+            self.validate_model(None)
+            self._validate_elements(key)
+            validated.add(key)
+            return
         self.vdw_type
         g = self.general
         if g[11] != 0 or g[12] <= 0:
             raise ValueError("Only zero lower taper radius and a positive upper cutoff are supported")
         if g[1] <= 0 or g[28] <= 0 or g[29] <= 0:
             raise ValueError("Invalid bond-order correction, vdW exponent, or bond-order cutoff")
-        if elements is None:
-            return
+
+    def _validate_elements(self, elements):
         missing = set(elements) - self.atoms.keys()
         if missing:
             raise ValueError(f"Atom types absent from the force field: {', '.join(sorted(missing))}")
@@ -398,5 +407,7 @@ class ForceField:
 
     def type_indices(self, symbols):
         """Element numbers (file order) of a sequence of labels, as int32."""
-        pos = {s: k for k, s in enumerate(self.elements)}
-        return np.array([pos[s] for s in symbols], dtype=np.int32)
+        pos = self.__dict__.get("_type_pos")
+        if pos is None:
+            pos = self.__dict__["_type_pos"] = {s: k for k, s in enumerate(self.elements)}
+        return np.fromiter((pos[s] for s in symbols), dtype=np.int32, count=len(symbols))

@@ -30,7 +30,7 @@ def boundary(cell, pbc):
     if pbc is None:
         pbc = cell is not None
     flags = np.asarray(pbc)
-    if flags.shape not in ((), (3,)) or flags.dtype.kind not in "biu" or not np.isin(flags, [0, 1]).all():
+    if flags.shape not in ((), (3,)) or flags.dtype.kind not in "biu" or not ((flags == 0) | (flags == 1)).all():
         raise ValueError("pbc must be a boolean or three boolean flags")
     flags = np.broadcast_to(flags.astype(bool), (3,)).copy()
     if not flags.any():

@@ -1,0 +1,227 @@
+"""Continuous-batching evaluation server on one GPU.
+
+Requests (one system each: symbols, positions, optional cell/pbc/total charge, a force-field name
+and an optional session key) are admitted into per-force-field queues. Each worker owns a device
+context (its own CUDA stream and buffers) and repeatedly takes every request waiting for one force
+field, up to an atom budget, and evaluates them as one ragged batch (``Calculator.evaluate_many``,
+C entry point ``xr_eval_batch``). With two or more workers a new batch is formed and launched while
+the previous one is still on the GPU, so requests that arrive during a batch join the next one and
+the batches' work overlaps on the device. The C library releases the Python GIL for the duration
+of a batch.
+
+Sessions: requests that carry the same ``session`` key are successive steps of one system (a
+relaxation or MD trajectory). The server keeps the last QEq charges of each session and starts the
+next step's solve from them (a warm start); results meet the same tolerance either way.
+
+xreac itself has no serving layer; every request's result is the ``Evaluation`` that
+``Calculator.evaluate`` (src/xreac/calculator.py:76-165) would return for it alone.
+"""
+
+from __future__ import annotations
+
+import collections
+import threading
+import time
+from concurrent.futures import Future
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .calculator import Calculator
+
+
+@dataclass
+class Request:
+    """One evaluation request."""
+
+    symbols: list
+    positions: np.ndarray
+    force_field: str
+    cell: np.ndarray | None = None
+    pbc: object = None
+    total_charge: float = 0.0
+    session: object = None
+    arrival: float = field(default=0.0)  # time.perf_counter() at admission (set by submit)
+
+    @property
+    def natoms(self):
+        return len(self.symbols)
+
+
+@dataclass
+class Served:
+    """Result of one request: the evaluation plus its timing."""
+
+    evaluation: object
+    arrival: float
+    done: float
+    batch_size: int
+    start: float = 0.0  # when its batch was formed
+
+    @property
+    def queued(self):
+        return self.start - self.arrival
+
+    @property
+    def latency(self):
+        return self.done - self.arrival
+
+
+class Server:
+    """Continuous-batching server.
+
+    ``force_fields`` maps names to ``ForceField`` objects. ``workers`` device contexts run batches
+    concurrently; ``max_batch_atoms`` and ``max_batch_requests`` bound one batch, and every context
+    is sized for that bound at start-up (``reserve``), so admission never waits on a device
+    allocation. ``warm_start`` enables the per-session QEq warm start.
+    """
+
+    def __init__(self, force_fields, *, workers=2, max_batch_atoms=16384, max_batch_requests=512, device=0,
+                 warm_start=True, max_expanded_atoms=512, reserve=True):
+        if workers < 1:
+            raise ValueError("workers must be at least 1")
+        self.force_fields = dict(force_fields)
+        self.max_batch_atoms = int(max_batch_atoms)
+        self.max_batch_requests = int(max_batch_requests)
+        self.warm_start = warm_start
+        self._queues = {name: collections.deque() for name in self.force_fields}
+        self._cv = threading.Condition()
+        self._closed = False
+        self._charges = {}  # session -> last charges
+        self._charges_lock = threading.Lock()
+        self.batches = []  # (force field, requests, atoms, seconds) per batch, for reporting
+        self._calcs = [
+            {name: Calculator(ff, device=device, max_expanded_atoms=max_expanded_atoms)
+             for name, ff in self.force_fields.items()}
+            for _ in range(workers)
+        ]
+        if reserve:
+            # size every context for the largest admissible batch up front: a buffer growth during
+            # serving would reallocate device memory and stall the other workers' batches
+            for calcs in self._calcs:
+                for calc in calcs.values():
+                    calc.reserve(self.max_batch_atoms, self.max_batch_requests)
+        self._threads = [threading.Thread(target=self._worker, args=(k,), daemon=True) for k in range(workers)]
+        for t in self._threads:
+            t.start()
+
+    # ------------------------------------------------------------------ client side
+    def submit(self, request, arrival=None):
+        """Admit a request; returns a Future that resolves to a :class:`Served`."""
+        if request.force_field not in self._queues:
+            raise ValueError(f"Unknown force field {request.force_field!r}")
+        fut = Future()
+        request.arrival = time.perf_counter() if arrival is None else arrival
+        with self._cv:
+            if self._closed:
+                raise RuntimeError("server is closed")
+            self._queues[request.force_field].append((request, fut))
+            self._cv.notify()
+        return fut
+
+    def close(self):
+        """Stop accepting requests, finish the queued ones and join the workers."""
+        with self._cv:
+            self._closed = True
+            self._cv.notify_all()
+        for t in self._threads:
+            t.join()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # ------------------------------------------------------------------ worker side
+    def _take_batch(self):
+        """Oldest-first: the force field whose head request waited longest, then FIFO up to the budget."""
+        best = None
+        for name, q in self._queues.items():
+            if q and (best is None or q[0][0].arrival < self._queues[best][0][0].arrival):
+                best = name
+        if best is None:
+            return None, []
+        q = self._queues[best]
+        batch, atoms = [], 0
+        while q and len(batch) < self.max_batch_requests:
+            n = q[0][0].natoms
+            if batch and atoms + n > self.max_batch_atoms:
+                break
+            batch.append(q.popleft())
+            atoms += n
+        return best, batch
+
+    def _worker(self, k):
+        calcs = self._calcs[k]
+        while True:
+            with self._cv:
+                while not self._closed and not any(self._queues.values()):
+                    self._cv.wait()
+                name, batch = self._take_batch()
+                if not batch:
+                    if self._closed:
+                        return
+                    continue
+            self._run(calcs[name], name, batch)
+
+    def _guess(self, req):
+        if not self.warm_start or req.session is None:
+            return None
+        with self._charges_lock:
+            g = self._charges.get(req.session)
+        return g if g is not None and len(g) == req.natoms else None
+
+    def _run(self, calc, name, batch):
+        systems = []
+        for req, _ in batch:
+            s = dict(symbols=req.symbols, positions=req.positions, cell=req.cell, pbc=req.pbc,
+                     total_charge=req.total_charge)
+            g = self._guess(req)
+            if g is not None:
+                s["initial_charges"] = g
+            systems.append(s)
+        t0 = time.perf_counter()
+        try:
+            results = calc.evaluate_many(systems)
+        except Exception:
+            # isolate the failing request(s): evaluate one by one
+            results = []
+            for s in systems:
+                try:
+                    results.append(calc.evaluate_many([s])[0])
+                except Exception as err:  # noqa: BLE001 - reported through the future
+                    results.append(err)
+        done = time.perf_counter()
+        self.batches.append((name, len(batch), sum(r.natoms for r, _ in batch), done - t0))
+        for (req, fut), res in zip(batch, results):
+            if isinstance(res, Exception):
+                fut.set_exception(res)
+                continue
+            if req.session is not None:
+                with self._charges_lock:
+                    self._charges[req.session] = res.charges
+            fut.set_result(Served(res, req.arrival, done, len(batch), t0))
+
+
+def replay(server, requests, arrivals=None, speedup=1.0):
+    """Submit ``requests`` at their ``arrivals`` (seconds from the start; None = all at once) and
+    wait for all results. Returns (list of Served or exceptions in request order, wall seconds)."""
+    futures = []
+    t_start = time.perf_counter()
+    for k, req in enumerate(requests):
+        if arrivals is not None:
+            target = t_start + arrivals[k] / speedup
+            delay = target - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            futures.append(server.submit(req, arrival=max(target, t_start)))
+        else:
+            futures.append(server.submit(req, arrival=t_start))
+    out = []
+    for f in futures:
+        try:
+            out.append(f.result())
+        except Exception as err:  # noqa: BLE001
+            out.append(err)
+    return out, time.perf_counter() - t_start
