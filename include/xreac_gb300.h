@@ -113,7 +113,8 @@ int xr_get_neighbors(xr_ctx* ctx, int index, int* i, int* j, int* S, long long c
 
 /* Nonzero corrected bond orders of the last evaluation of system `index`, one entry per unordered
  * image pair (i, j, S) in pair order; the directed pair (j, i, -S) carries the same value.
- * Host pointers; *count as for xr_get_neighbors. */
+ * index -1 returns those of every system of the batch at once, with atom indices counted over the
+ * systems concatenated in call order. Host pointers; *count as for xr_get_neighbors. */
 int xr_get_bonds(xr_ctx* ctx, int index, int* i, int* j, int* S, double* bo, long long capacity, long long* count);
 
 /* Number of CUDA kernels the last xr_eval / xr_eval_batch call launched. */
@@ -122,6 +123,11 @@ long long xr_last_launches(const xr_ctx* ctx);
 /* QEq conjugate-gradient iterations of the last call (largest over its systems; no reference
  * counterpart: the reference solves the KKT system directly). */
 int xr_last_qeq_iterations(const xr_ctx* ctx);
+
+/* QEq work of the last call (no reference counterpart; instrumentation): the conjugate-gradient
+ * iterations summed over its systems, and the algorithmic bytes of a matrix-free product summed
+ * over every iteration of every system: iterations x (8 B per unordered pair + 16 B per atom). */
+int xr_last_qeq_work(const xr_ctx* ctx, long long* iterations, double* matvec_bytes);
 
 /* Host-to-device and device-to-host bytes the last call moved (no reference counterpart). */
 int xr_last_transfer_bytes(const xr_ctx* ctx, long long* h2d, long long* d2h);

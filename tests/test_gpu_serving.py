@@ -41,7 +41,7 @@ def test_each_request_alone_equals_in_the_mix():
         served, _ = replay(srv, reqs)
         batches = list(srv.batches)
     assert len(batches) < len(reqs)  # requests really were batched
-    assert max(b[1] for b in batches) > 1
+    assert max(b.requests for b in batches) > 1
     for req, out in zip(reqs, served):
         assert not isinstance(out, Exception), out
         ref = alone[req.force_field].evaluate(req.symbols, req.positions, cell=req.cell, pbc=req.pbc,

@@ -19,8 +19,8 @@ def _system_struct(nat, x, cell, pbc):
     s = nat.System()
     s.natoms = len(x)
     s.types = None
-    s.positions = nat.ptr(x, nat.c_double)
-    s.cell = nat.ptr(cell, nat.c_double) if cell is not None else None
+    s.positions = nat.addr(x)
+    s.cell = nat.addr(cell)
     for d in range(3):
         s.pbc[d] = int(pbc)
     s.total_charge = 0.0

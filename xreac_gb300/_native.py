@@ -46,6 +46,7 @@ EXPORTED = (
     "xr_ctx_stage_times",
     "xr_last_transfer_bytes",
     "xr_last_qeq_iterations",
+    "xr_last_qeq_work",
     "xr_count_neighbors_static",
     "xr_static_last_error",
 )
@@ -53,27 +54,28 @@ EXPORTED = (
 XR_STATIC_MAX_ATOMS = 16384
 
 
+# Pointer members are declared as void* (the C layout is the same); assign addresses with addr().
 class System(ctypes.Structure):
     _fields_ = [
         ("natoms", c_int),
-        ("types", POINTER(c_int)),
-        ("positions", POINTER(c_double)),
-        ("cell", POINTER(c_double)),
+        ("types", c_void_p),          # const int*
+        ("positions", c_void_p),      # const double*, natoms x 3
+        ("cell", c_void_p),           # const double*, 9 or NULL
         ("pbc", c_int * 3),
         ("total_charge", c_double),
-        ("charges_guess", POINTER(c_double)),
+        ("charges_guess", c_void_p),  # const double* or NULL
     ]
 
 
 class Result(ctypes.Structure):
     _fields_ = [
-        ("energy", POINTER(c_double)),
-        ("forces", POINTER(c_double)),
-        ("charges", POINTER(c_double)),
-        ("total_bond_orders", POINTER(c_double)),
-        ("lone_pairs", POINTER(c_double)),
-        ("bond_counts", POINTER(c_int)),
-        ("dipole", POINTER(c_double)),
+        ("energy", c_void_p),             # double[15]
+        ("forces", c_void_p),             # double[natoms * 3]
+        ("charges", c_void_p),            # double[natoms]
+        ("total_bond_orders", c_void_p),  # double[natoms]
+        ("lone_pairs", c_void_p),         # double[natoms]
+        ("bond_counts", c_void_p),        # int[natoms]
+        ("dipole", c_void_p),             # double[3]
     ]
 
 
@@ -128,12 +130,21 @@ def load():
     lib.xr_last_transfer_bytes.restype = c_int
     lib.xr_last_qeq_iterations.argtypes = [c_void_p]
     lib.xr_last_qeq_iterations.restype = c_int
+    lib.xr_last_qeq_work.argtypes = [c_void_p, POINTER(c_longlong), POINTER(c_double)]
+    lib.xr_last_qeq_work.restype = c_int
     lib.xr_count_neighbors_static.argtypes = [POINTER(System), c_double, c_void_p, POINTER(c_int), POINTER(c_longlong)]
     lib.xr_count_neighbors_static.restype = c_int
     lib.xr_static_last_error.argtypes = []
     lib.xr_static_last_error.restype = c_char_p
     _LIB = lib
     return lib
+
+
+def addr(a):
+    """Address of a C-contiguous numpy array's data (None for None), for the void* struct members."""
+    if a is None:
+        return None
+    return a.__array_interface__["data"][0]
 
 
 def ptr(a, ctype):

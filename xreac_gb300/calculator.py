@@ -15,7 +15,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import _native as nat
-from .geometry import cell_repetitions, validate_expansion_limit, validate_input
+from .geometry import boundary, cell_repetitions, validate_expansion_limit, validate_input, validate_total_charge
 
 COMPONENTS = (
     "bond",
@@ -102,6 +102,7 @@ class Calculator:
         self._ff = nat.ForceFieldHandle(force_field.tables(), _is_carbon(force_field), force_field.vdw_type)
         self._ctx = nat.Context(device)
         self._lib = nat.load()
+        self._type_pos = {s: k for k, s in enumerate(force_field.elements) if isinstance(s, str) and s}
 
     def set_qeq(self, tolerance=1e-13, max_iterations=2000):
         """QEq solver tolerance and iteration limit.
@@ -130,13 +131,28 @@ class Calculator:
     def _prepare(self, symbols, positions, total_charge, cell, pbc, full_derivative):
         if not isinstance(full_derivative, bool):
             raise ValueError("full_derivative must be a boolean")
-        symbols, x, flags, m = validate_input(symbols, positions, total_charge, cell, pbc)
         ff = self.force_field
-        ff.validate_model(symbols)
+        symbols = tuple(symbols)
+        # Fast path: every label maps to an element of the force field (str keys only, so a
+        # non-string or empty label falls through to the full validation and its message).
+        try:
+            types = np.fromiter(map(self._type_pos.__getitem__, symbols), dtype=np.int32, count=len(symbols))
+        except (KeyError, TypeError):
+            types = None
+        if types is None or not symbols:
+            symbols, x, flags, m = validate_input(symbols, positions, total_charge, cell, pbc)
+            ff.validate_model(symbols)
+            types = ff.type_indices(symbols)
+        else:
+            validate_total_charge(total_charge)
+            x = np.array(positions, dtype=np.float64, copy=True)
+            if x.shape != (len(symbols), 3) or not np.isfinite(x).all():
+                raise ValueError("positions must be a finite (N, 3) array in Angstrom")
+            flags, m = boundary(cell, pbc)
+            ff.validate_model(symbols)
         reps = cell_repetitions(float(ff.general[12]), flags, m, len(symbols), self.max_expanded_atoms)
-        types = np.ascontiguousarray(ff.type_indices(symbols))
         cellm = None if m is None else np.ascontiguousarray(m, dtype=np.float64)
-        return symbols, np.ascontiguousarray(x), types, flags, cellm, reps
+        return symbols, x, types, flags, cellm, reps
 
     def _raise(self, code):
         if code in _ERRORS:
@@ -194,33 +210,38 @@ class Calculator:
         counts = np.zeros(total, dtype=np.int32)
         sys_arr = (nat.System * n_sys)()
         res_arr = (nat.Result * n_sys)()
-        offsets = np.concatenate(([0], np.cumsum(sizes))).astype(int)
+        offsets = np.concatenate(([0], np.cumsum(sizes))).astype(int).tolist()
+        addr = nat.addr
+        e_base, f_base, q_base = addr(energy), addr(forces), addr(per_atom)
+        c_base, d_base = addr(counts), addr(dipole)
         keep = []
         for k, (types, x, flags, cellm, q, guess) in enumerate(batch):
             a0 = offsets[k]
             keep.append((types, x, cellm, guess))
             s = sys_arr[k]
             s.natoms = sizes[k]
-            s.types = nat.ptr(types, nat.c_int)
-            s.positions = nat.ptr(x, nat.c_double)
-            s.cell = nat.ptr(cellm, nat.c_double) if cellm is not None else None
+            s.types = addr(types)
+            s.positions = addr(x)
+            s.cell = addr(cellm)
             for d in range(3):
                 s.pbc[d] = int(flags[d])
             s.total_charge = q
-            s.charges_guess = nat.ptr(guess, nat.c_double)
+            s.charges_guess = addr(guess)
             r = res_arr[k]
-            r.energy = nat.ptr(energy[k], nat.c_double)
-            r.forces = nat.ptr(forces[a0:], nat.c_double)
-            r.charges = nat.ptr(per_atom[0, a0:], nat.c_double)
-            r.total_bond_orders = nat.ptr(per_atom[1, a0:], nat.c_double)
-            r.lone_pairs = nat.ptr(per_atom[2, a0:], nat.c_double)
-            r.bond_counts = nat.ptr(counts[a0:], nat.c_int)
-            r.dipole = nat.ptr(dipole[k], nat.c_double)
+            r.energy = e_base + 120 * k
+            r.forces = f_base + 24 * a0
+            r.charges = q_base + 8 * a0
+            r.total_bond_orders = q_base + 8 * (total + a0)
+            r.lone_pairs = q_base + 8 * (2 * total + a0)
+            r.bond_counts = c_base + 4 * a0
+            r.dipole = d_base + 24 * k
         flags_ = nat.XR_FLAG_FULL_DERIVATIVE if full_derivative else 0
         code = lib.xr_eval_batch(self._ctx.handle, self._ff.handle, n_sys, sys_arr, flags_, res_arr)
         if code != nat.XR_OK:
             self._raise(code)
         counts64 = counts.astype(int)
+        bi, bj, bS, bbo = self._bonds(-1)
+        cut = np.searchsorted(bi, offsets).tolist()  # bonds are grouped by system, in pair order
         results = []
         for k in range(n_sys):
             a0, a1 = offsets[k], offsets[k + 1]
@@ -238,7 +259,8 @@ class Calculator:
                     dipole=dipole[k],
                     cell_repetitions=reps[k],
                     neighbor_backend=backend,
-                    bonds=self._bonds(k),
+                    bonds=(bi[cut[k]:cut[k + 1]] - a0, bj[cut[k]:cut[k + 1]] - a0, bS[cut[k]:cut[k + 1]],
+                           bbo[cut[k]:cut[k + 1]]),
                 )
             )
         return results
@@ -271,4 +293,30 @@ class Calculator:
 
     @property
     def last_launches(self):
+        """Kernels launched by the last evaluation call."""
         return int(self._lib.xr_last_launches(self._ctx.handle))
+
+    def qeq_work(self):
+        """(CG iterations summed over the last call's systems, their matrix-free algorithmic bytes)."""
+        its = nat.c_longlong()
+        b = nat.c_double()
+        self._lib.xr_last_qeq_work(self._ctx.handle, nat.byref(its), nat.byref(b))
+        return int(its.value), float(b.value)
+
+    def transfer_bytes(self):
+        """(host-to-device, device-to-host) bytes moved by the last evaluation call."""
+        h2d = nat.c_longlong()
+        d2h = nat.c_longlong()
+        self._lib.xr_last_transfer_bytes(self._ctx.handle, nat.byref(h2d), nat.byref(d2h))
+        return int(h2d.value), int(d2h.value)
+
+    def set_profiling(self, enable=True):
+        """Per-stage CUDA-event timing of later calls (resets the accumulators)."""
+        self._lib.xr_ctx_set_profiling(self._ctx.handle, 1 if enable else 0)
+
+    def stage_times(self):
+        """(summed milliseconds of the 7 stages, number of calls) since profiling was enabled."""
+        ms = (nat.c_double * 8)()
+        calls = nat.c_longlong()
+        self._lib.xr_ctx_stage_times(self._ctx.handle, ms, 7, nat.byref(calls))
+        return np.array(ms[:7]), int(calls.value)

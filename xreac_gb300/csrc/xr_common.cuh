@@ -171,6 +171,7 @@ struct XrWork {
   // charges and forces
   double* q;
   const double* qguess;       // [A] initial QEq charges of systems with has_guess (sum = total charge)
+  int* qiters;                // [S] QEq conjugate-gradient iterations of each system
   double* f;                  // [A][3] gradient dE/dx accumulator (forces = -f)
   double* qwork;              // [XR_QW_N][A] QEq solver vectors
   double* red;                // reduction scratch for solvers

@@ -72,6 +72,9 @@ struct xr_ctx {
   long long launches = 0;
   long long h2d_bytes = 0, d2h_bytes = 0;  // host<->device bytes moved by the last evaluation
   int qeq_iterations = 0;                   // CG iterations of the last evaluation (largest system)
+  int* qiters = nullptr;                    // [S] per-system iterations (device)
+  size_t cqiters = 0;
+  std::vector<int> h_qiters;
   // last batch layout (host copies for export)
   std::vector<XrSystem> host_sys;
   std::vector<int> host_cnt;  // [4][A+1] scans of the last evaluation
@@ -319,6 +322,7 @@ bool ensure_atoms(xr_ctx* c, int A, int S) {
   GROW(nnz, A);
   GROW(sys_chunks, S);
   GROW(qsmall, S);
+  GROW(qiters, S);
   GROW(sys, S);
   GROW(energy, 16 * (size_t)S);
   GROW(props, 4 * (size_t)S);
@@ -452,6 +456,7 @@ void attach_lists(xr_ctx* c, XrWork& w) {
   w.nmids = c->nmids;
   w.nmask = c->nmids + 1;
   w.qguess = c->qguess;
+  w.qiters = c->qiters;
   w.mlist = c->mlist;
 }
 
@@ -711,6 +716,7 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
          (long long)(sizeof(int4) * chunk_tab.size() + sizeof(int2) * nsys);
   cudaMemsetAsync(c->status, 0, sizeof(int), st);
   cudaMemsetAsync(c->counts, 0, 8 * sizeof(int), st);
+  cudaMemsetAsync(c->qiters, 0, sizeof(int) * nsys, st);
   cudaMemsetAsync(c->cnt, 0, sizeof(int) * 4 * (size_t)(A + 1), st);
   XrWork w;
   fill_work(c, w, A, nsys, flags);
@@ -774,6 +780,9 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
   }
   cudaMemcpyAsync(c->h_small + 5, c->bx_count, sizeof(int), cudaMemcpyDeviceToHost, st);
   cudaMemcpyAsync(c->h_small + 6, c->counts + 4, sizeof(int), cudaMemcpyDeviceToHost, st);
+  c->h_qiters.resize(nsys);
+  cudaMemcpyAsync(c->h_qiters.data(), c->qiters, sizeof(int) * nsys, cudaMemcpyDeviceToHost, st);
+  d2h += sizeof(int) * (long long)nsys;
   d2h += 3 * sizeof(int);
   if (dev_io) {
     const xr_result& r = out[0];
@@ -809,6 +818,7 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
     if (nx > 0) {
       cudaMemcpy(c->h_bx_meta.data(), c->bx_meta, sizeof(int4) * nx, cudaMemcpyDeviceToHost);
       cudaMemcpy(c->h_bx_bo.data(), c->bx_bo, sizeof(double) * nx, cudaMemcpyDeviceToHost);
+      d2h += (long long)(sizeof(int4) + sizeof(double)) * nx;
       std::vector<int> order(nx);
       for (int k = 0; k < nx; ++k) order[k] = k;
       std::sort(order.begin(), order.end(), [&](int a, int b) { return c->h_bx_meta[a].x < c->h_bx_meta[b].x; });
@@ -825,12 +835,13 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
   if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(c, e, "kernel launch");
   c->launches = launches;
   c->qeq_iterations = c->h_small[6];
-  c->h2d_bytes = h2d;
-  c->d2h_bytes = d2h;
   c->last_A = A;
   // keep the scans for export
   c->host_cnt.resize(4 * (size_t)(A + 1));
   cudaMemcpy(c->host_cnt.data(), c->cnt, sizeof(int) * 4 * (size_t)(A + 1), cudaMemcpyDeviceToHost);
+  d2h += sizeof(int) * 4 * (long long)(A + 1);
+  c->h2d_bytes = h2d;
+  c->d2h_bytes = d2h;
   if (int code = status_to_code(c, c->h_small[4])) return code;
   if (dev_io) {
     const xr_result& r = out[0];
@@ -1033,7 +1044,7 @@ void xr_ctx_destroy(xr_ctx* c) {
                   c->qwork, c->outbuf, c->edge, c->edge_pair, c->edge_dbslot, c->hval, c->pair_edge, c->pair_i,
                   c->pair_bond, c->p_r, c->p_shield, c->p_dshield, c->p_g, c->p_evdw, c->p_ecoul, c->bond_pair,
                   c->bond_i, c->bond_j, c->b_r, c->b_v, c->b_fwd, c->b_adj, c->b_e, c->dbrow, c->sys, c->energy,
-                  c->props, c->status, c->counts, c->barrier, c->qmap, c->qsmall, c->red, c->qguess, c->bx_meta, c->bx_bo, c->bx_count,
+                  c->props, c->status, c->counts, c->barrier, c->qmap, c->qsmall, c->qiters, c->red, c->qguess, c->bx_meta, c->bx_bo, c->bx_count,
                   c->esum, c->arow, c->nact, c->nzrow, c->nnz, c->chunks, c->sys_chunks, c->chunk_part, c->mids, c->nmids, c->mlist};
   for (void* p : bufs)
     if (p) cudaFree(p);
@@ -1068,6 +1079,22 @@ long long xr_last_launches(const xr_ctx* c) { return c ? c->launches : 0; }
 
 int xr_last_qeq_iterations(const xr_ctx* c) { return c ? c->qeq_iterations : 0; }
 
+int xr_last_qeq_work(const xr_ctx* c, long long* iterations, double* matvec_bytes) {
+  if (!c || !iterations || !matvec_bytes) return XR_EINPUT;
+  const int L = c->last_A + 1;
+  long long its = 0;
+  double bytes = 0;
+  for (size_t s = 0; s < c->h_qiters.size() && s < c->host_sys.size(); ++s) {
+    const XrSystem& sy = c->host_sys[s];
+    const long long pairs = c->host_cnt[1 * L + sy.atom_off + sy.natoms] - c->host_cnt[1 * L + sy.atom_off];
+    its += c->h_qiters[s];
+    bytes += (double)c->h_qiters[s] * (8.0 * (double)pairs + 16.0 * sy.natoms);
+  }
+  *iterations = its;
+  *matvec_bytes = bytes;
+  return XR_OK;
+}
+
 int xr_last_transfer_bytes(const xr_ctx* c, long long* h2d, long long* d2h) {
   if (!c) return XR_EINPUT;
   if (h2d) *h2d = c->h2d_bytes;
@@ -1100,10 +1127,11 @@ int xr_get_neighbors(xr_ctx* c, int index, int* i, int* j, int* S, long long cap
 }
 
 int xr_get_bonds(xr_ctx* c, int index, int* i, int* j, int* S, double* bo, long long capacity, long long* count) {
-  if (!c || index < 0 || index >= (int)c->host_sys.size() || !count) return XR_EINPUT;
+  if (!c || index < -1 || index >= (int)c->host_sys.size() || !count) return XR_EINPUT;
   const int L = c->last_A + 1;
-  const XrSystem& sy = c->host_sys[index];
-  const int a0 = sy.atom_off, a1 = sy.atom_off + sy.natoms;
+  // index -1: every system of the batch, atom indices counted over the concatenated systems
+  const int a0 = index < 0 ? 0 : c->host_sys[index].atom_off;
+  const int a1 = index < 0 ? c->last_A : a0 + c->host_sys[index].natoms;
   const int b0 = c->host_cnt[2 * L + a0], b1 = c->host_cnt[2 * L + a1];
   // exported entries are sorted by bond id: the system's are one contiguous run
   const auto& m = c->h_bx_meta;

@@ -241,17 +241,316 @@ __device__ inline double warp_total(double t) {
   return t;
 }
 
+// Per-row solver state of a block with at most 32 rows (the grid layout), indexed by row - r0.
+template <class T>
+struct QeqRows {
+  T x[32], p[32], hp[32], di[32], c[32], eta_di[32], g[32];
+};
+
 // Block-shared state of one solve: the reductions' buffer, the iteration scalars (written by thread 0
-// in the reductions' post hooks), the tile transposition buffers and, for blocks of at most 32 rows,
-// the rows' solver state indexed by row - r0. One instance per kernel serves both team kinds.
+// in the reductions' post hooks, in FP64 and as FP32 copies for the FP32 solve), the tile
+// transposition buffers and the per-row state. One instance per kernel serves both team kinds.
 struct QeqShared {
   double red[kRedSmem];
   double sc_lam, sc_alpha, sc_step, sc_beta;
+  float sf_lam, sf_alpha, sf_step, sf_beta;
   int sc_state;  // 0 iterate, 1 converged, 2 stop
-  double part[32][33];
-  double part4[4][32];
-  double rs_x[32], rs_p[32], rs_hp[32], rs_di[32], rs_c[32], rs_eta[32], rs_g[32];
+  union {
+    double d[32][33];
+    float f[32][33];
+  } part;
+  union {
+    double d[4][32];
+    float f[4][32];
+  } part4;
+  QeqRows<double> rd;
+  QeqRows<float> rf;
 };
+
+template <class T>
+__device__ inline QeqRows<T>& qeq_rows(QeqShared& sh);
+template <>
+__device__ inline QeqRows<double>& qeq_rows<double>(QeqShared& sh) { return sh.rd; }
+template <>
+__device__ inline QeqRows<float>& qeq_rows<float>(QeqShared& sh) { return sh.rf; }
+template <class T>
+__device__ inline T (&qeq_part(QeqShared& sh))[32][33];
+template <>
+__device__ inline double (&qeq_part<double>(QeqShared& sh))[32][33] { return sh.part.d; }
+template <>
+__device__ inline float (&qeq_part<float>(QeqShared& sh))[32][33] { return sh.part.f; }
+template <class T>
+__device__ inline T (&qeq_part4(QeqShared& sh))[4][32];
+template <>
+__device__ inline double (&qeq_part4<double>(QeqShared& sh))[4][32] { return sh.part4.d; }
+template <>
+__device__ inline float (&qeq_part4<float>(QeqShared& sh))[4][32] { return sh.part4.f; }
+
+template <class T>
+__device__ inline T pick(double d, float f) {
+  if constexpr (sizeof(T) == 8)
+    return d;
+  else
+    return f;
+}
+
+template <class T>
+__device__ inline T warp_total_t(T t) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  return t;
+}
+
+// Vectors of one conjugate-gradient solve (global, indexed by atom): the projected gradient in two
+// buffers used in turn, the search direction, its product with H, and the accumulated step.
+template <class T>
+struct QeqVecs {
+  T* g;
+  T* g2;
+  T* p;
+  T* hp;
+  T* y;
+  // optional row constants in precision T (D^-1, eta D^-1, row sums), else formed from the FP64 ones
+  const T* di = nullptr;
+  const T* etadi = nullptr;
+  const T* c = nullptr;
+};
+
+// Matrix rows of the owning block for the product: shared-memory cache of H'_ij = H_ij / D_jj with
+// 16-bit columns (cached), else the global neighbour rows (hval holds H'_ij when `scaled`, else H_ij).
+template <class T>
+struct QeqMatrix {
+  const T* cache_h;
+  const unsigned short* cache_j;
+  bool cached;
+  bool scaled;
+  int ebeg;
+  T* gstage;  // the whole gradient of the system staged per iteration (or null)
+};
+
+// Projected, Jacobi-preconditioned conjugate gradients in precision T on
+//   minimise 1/2 y'Hy + g0'y  subject to  sum y = 0,
+// starting from y = v.y (its current content, normally 0 or the start point) with the projected
+// gradient in v.g. Gould, Hribar and Nocedal's projected CG with z = D^-1 (g - lambda): the products
+// use the pre-scaled rows (H z = H'(g - lambda) with row sums c), and the multiplier change of a
+// step, alpha <D^-1, Hp> / <D^-1, 1>, is reduced together with p'Hp, so the gradient is written
+// already projected and its norm g'D^-1 g is free of cancellation. Stops when that norm is at most
+// `stop`, at `max_it` iterations (flagging XR_S_CG when `flag_limit`), or on breakdown.
+// Per iteration: one product and two team-wide reductions. Returns the iterations taken, or -1
+// when a team barrier gave up.
+template <class Team, class T>
+__device__ int qeq_cg(const XrWork& w, const XrFF& ff, const Team& team, QeqShared& sh, int a0, int n, int r0,
+                      int r1, QeqVecs<T> v, const QeqMatrix<T>& M, double s1, double gz_start, double stop,
+                      double gfloor, int max_it, bool flag_limit, int& slot) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const double* DI = &QW(Q_DINV, 0);
+  const double* Cr = &QW(Q_C, 0);
+  QeqRows<T>& R = qeq_rows<T>(sh);
+  auto& part = qeq_part<T>(sh);
+  auto& part4 = qeq_part4<T>(sh);
+  const bool row_smem = (r1 - r0) <= 32;
+  double gz = gz_start;  // meaningful in thread 0
+  if (threadIdx.x == 0) {
+    sh.sc_beta = 0.0;
+    sh.sf_beta = 0.0f;
+    sh.sc_lam = 0.0;
+    sh.sf_lam = 0.0f;
+    sh.sc_state = (!(gz_start > gfloor) || n < 2 || gz_start <= stop) ? 1 : 0;
+  }
+  if (row_smem && wid == 0 && r0 + lane < r1) {
+    const int a = a0 + r0 + lane;
+    const double di = DI[a];
+    R.x[lane] = v.y[a];
+    R.p[lane] = T(0);
+    R.hp[lane] = T(0);
+    R.di[lane] = T(di);
+    R.c[lane] = T(Cr[a]);
+    R.eta_di[lane] = T(atom_prm(ff, w.type[a], A_ETA) * di);
+    R.g[lane] = v.g[a];
+  }
+  __syncthreads();
+  T* G = v.g;
+  T* G2 = v.g2;
+  int it = 0;
+  while (sh.sc_state == 0) {
+    if (++it > max_it) {
+      if (flag_limit && threadIdx.x == 0) atomicOr(w.status, XR_S_CG);
+      --it;
+      break;
+    }
+    const T lam = pick<T>(sh.sc_lam, sh.sf_lam);
+    const T beta = pick<T>(sh.sc_beta, sh.sf_beta);
+    // p = -z + beta p,  Hp = -H z + beta Hp,  z = D^-1 (g - lambda); the next buffer gets g - lambda
+    if (M.gstage) {  // the whole gradient of the system in shared memory: the gathers stay on-chip
+      for (int q = threadIdx.x; q < n; q += blockDim.x) M.gstage[q] = __ldcg(G + a0 + q);
+      __syncthreads();
+    }
+    T php0 = T(0), php1 = T(0);  // lane partials in warp 0: p'Hp and <D^-1, Hp>
+    for (int tb = r0; tb < r1; tb += 32) {
+      const int r = tb + wid;
+      T hz = T(0);
+      if (wid < 32 && r < r1) {
+        const int a = a0 + r;
+        const int eb = w.cnt[a], ee = w.cnt[a + 1];
+        if (M.cached && M.gstage) {
+          for (int e = eb + lane; e < ee; e += 32) hz += M.cache_h[e - M.ebeg] * M.gstage[M.cache_j[e - M.ebeg]];
+        } else if (M.cached) {
+          for (int e = eb + lane; e < ee; e += 32) hz += M.cache_h[e - M.ebeg] * __ldcg(G + a0 + M.cache_j[e - M.ebeg]);
+        } else {
+          for (int e = eb + lane; e < ee; e += 32) {
+            const int j = w.edge[e].x;
+            const double h = M.scaled ? w.hval[e] : w.hval[e] * __ldcg(DI + j);
+            hz += T(h) * __ldcg(G + j);
+          }
+        }
+      }
+      if (wid < 32) part[wid][lane] = hz;
+      __syncthreads();
+      if (wid < 4) {  // lane = row of the tile; warp k adds lanes 8k .. 8k+7 of the row's partials
+        T s = part[lane][8 * wid];
+#pragma unroll
+        for (int k = 1; k < 8; ++k) s += part[lane][8 * wid + k];
+        part4[wid][lane] = s;
+      }
+      __syncthreads();
+      if (wid == 0 && tb + lane < r1) {
+        const int rr = tb + lane, a = a0 + rr;
+        T h = (part4[0][lane] + part4[1][lane]) + (part4[2][lane] + part4[3][lane]);
+        const T ga = row_smem ? R.g[lane] : (M.gstage ? M.gstage[rr] : G[a]);
+        const T di = row_smem ? R.di[lane] : (v.di ? v.di[a] : T(DI[a]));
+        const T etadi = row_smem ? R.eta_di[lane] : (v.etadi ? v.etadi[a] : T(atom_prm(ff, w.type[a], A_ETA) * DI[a]));
+        const T cr = row_smem ? R.c[lane] : (v.c ? v.c[a] : T(Cr[a]));
+        const T p_old = row_smem ? R.p[lane] : v.p[a];
+        const T hp_old = row_smem ? R.hp[lane] : v.hp[a];
+        h += etadi * ga - lam * cr;
+        const T z = di * (ga - lam);
+        const T p = -z + beta * p_old;
+        const T hp = -h + beta * hp_old;
+        if (row_smem) {
+          R.p[lane] = p;
+          R.hp[lane] = hp;
+          R.g[lane] = ga - lam;
+        } else {
+          v.p[a] = p;
+          v.hp[a] = hp;
+          G2[a] = ga - lam;
+        }
+        php0 += p * hp;
+        php1 += di * hp;
+      }
+    }
+    double pHp[2] = {0.0, 0.0};
+    if (wid == 0) {
+      pHp[0] = double(warp_total_t<T>(php0));
+      pHp[1] = double(warp_total_t<T>(php1));
+    }
+    if (!team.template reduce<2>(w, pHp, sh.red, slot, [&](double* t) {
+          // The QEq matrix of a close-packed geometry can have a negative eigenvalue (the reference's
+          // direct KKT solve accepts it); CG then takes steps of negative curvature (alpha < 0) and
+          // still converges. Only an exactly vanishing or non-finite p'Hp is a breakdown, and a
+          // non-positive one at rounding level means the solve has converged.
+          const bool rounding = gz <= 1e4 * gfloor;
+          if (!(fabs(t[0]) > 0.0) || !isfinite(t[0]) || (t[0] < 0.0 && rounding)) {
+            if (!rounding && flag_limit) atomicOr(w.status, XR_S_NONSPD);
+            sh.sc_state = 2;
+          } else {
+            sh.sc_alpha = gz / t[0];
+            sh.sc_step = sh.sc_alpha * t[1] / s1;
+            sh.sf_alpha = float(sh.sc_alpha);
+            sh.sf_step = float(sh.sc_step);
+          }
+        }))
+      return -1;
+    slot = slot == 1 ? 2 : 1;
+    if (sh.sc_state != 0) break;
+    // Step: y += alpha p, g += alpha Hp - (multiplier change), one row per lane of warp 0.
+    const T alpha = pick<T>(sh.sc_alpha, sh.sf_alpha);
+    const T step_lam = pick<T>(sh.sc_step, sh.sf_step);
+    double u[2] = {0, 0};
+    if (wid == 0) {
+      T u0 = T(0), u1 = T(0);
+      for (int rr = r0 + lane; rr < r1; rr += 32) {
+        const int a = a0 + rr;
+        if (row_smem) {
+          const T g = (R.g[lane] + alpha * R.hp[lane]) - step_lam;
+          R.x[lane] += alpha * R.p[lane];
+          R.g[lane] = g;
+          G2[a] = g;  // published for the other rows' products
+          u0 += R.di[lane] * g;
+          u1 += R.di[lane] * g * g;
+        } else {
+          const T g = (G2[a] + alpha * v.hp[a]) - step_lam;
+          v.y[a] += alpha * v.p[a];
+          G2[a] = g;
+          const T di = v.di ? v.di[a] : T(DI[a]);
+          u0 += di * g;
+          u1 += di * g * g;
+        }
+      }
+      u[0] = double(warp_total_t<T>(u0));
+      u[1] = double(warp_total_t<T>(u1));
+    }
+    if (!team.template reduce<2>(w, u, sh.red, slot, [&](double* t) {
+          sh.sc_lam = t[0] / s1;
+          sh.sf_lam = float(sh.sc_lam);
+          const double gz_new = t[1] - sh.sc_lam * t[0];
+          if (gz_new <= stop) sh.sc_state = 1;
+          sh.sc_beta = gz_new / gz;
+          sh.sf_beta = float(sh.sc_beta);
+          gz = gz_new;
+        }))
+      return -1;
+    slot = slot == 1 ? 2 : 1;
+    T* tmp = G;  // the buffer just written becomes the one read next
+    G = G2;
+    G2 = tmp;
+  }
+  if (row_smem && wid == 0 && r0 + lane < r1) v.y[a0 + r0 + lane] = R.x[lane];
+  __syncthreads();
+  return it;
+}
+
+// FP64 gradient of the QEq energy at the current charges X for the owned rows, projected onto
+// sum q = Q: g = H x + chi, lambda = <D^-1, g> / <D^-1, 1>, G = g - lambda, and its norm
+// <D^-1, G^2> (from the projected values, so free of cancellation). Two team reductions.
+template <class Team>
+__device__ bool qeq_residual(const XrWork& w, const XrFF& ff, const Team& team, QeqShared& sh, int a0, int r0, int r1,
+                             double s1, double* gz_out, int& slot) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  double* X = &QW(Q_X, 0);
+  double* G = &QW(Q_G, 0);
+  const double* DI = &QW(Q_DINV, 0);
+  auto noop = [](double*) {};
+  double acc[1] = {0.0};
+  for (int r = r0 + wid; r < r1; r += nw) {
+    const int a = a0 + r;
+    double hx = 0;
+    for (int e = w.cnt[a] + lane; e < w.cnt[a + 1]; e += 32) hx += w.hval[e] * __ldcg(X + w.edge[e].x);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) hx += __shfl_xor_sync(0xffffffffu, hx, o);
+    if (lane == 0) {
+      const int t = w.type[a];
+      const double g = hx + atom_prm(ff, t, A_ETA) * X[a] + atom_prm(ff, t, A_CHI);
+      G[a] = g;
+      acc[0] += DI[a] * g;
+    }
+  }
+  if (!team_sum<1>(team, w, acc, sh.red, slot, noop)) return false;
+  slot = slot == 1 ? 2 : 1;
+  const double lam = acc[0] / s1;
+  double acc2[1] = {0.0};
+  for (int r = r0 + wid; r < r1; r += nw)
+    if (lane == 0) {
+      const int a = a0 + r;
+      const double g = G[a] - lam;
+      G[a] = g;
+      acc2[0] += DI[a] * g * g;
+    }
+  if (!team_sum<1>(team, w, acc2, sh.red, slot, noop)) return false;
+  slot = slot == 1 ? 2 : 1;
+  *gz_out = acc2[0];
+  return true;
+}
 
 // Rows [r0, r1) of the system starting at atom a0 belong to this block. The matrix-vector product
 // runs on tiles of 32 rows, one row per warp; the lanes' partial row sums are transposed through
@@ -259,29 +558,46 @@ struct QeqShared {
 // reductions and every per-row scalar update. On this part an FP64 instruction costs the FP64 pipe
 // the same whether one lane or 32 are active, so scalar row work done by lane 0 of 32 warps would
 // cost 32 times the issue slots of the same work spread over the lanes of one warp.
-// When `cache_j` is non-null the block's matrix rows (column, H'_ij) are kept in shared memory;
-// when `gstage` is non-null the whole gradient is staged in shared memory every iteration.
+//
+// Mixed precision (when the block's rows fit the shared-memory cache as FP32): iterative refinement
+// around FP32 solves. Each sweep solves the correction problem (the current projected FP64
+// gradient as g0) with the FP32 projected CG to a relative norm of 1e-5, adds the correction to
+// the FP64 charges and recomputes the projected gradient in FP64 from the unscaled matrix. FP32
+// issues at 64 times the FP64 rate here, so a sweep costs a fraction of the FP64 iterations it
+// replaces, and the FP64 residual decides convergence against the same tolerance as the FP64
+// solve. If a sweep fails to cut the residual by 1e3 the FP64 solve takes over from the current
+// charges.
+//
+// When `cache_j` is non-null the block's matrix rows are kept in shared memory (FP32 in the mixed
+// mode, else FP64); when `gstage` is non-null the whole gradient is staged in shared memory.
 template <class Team>
 __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int a0, int n, int r0, int r1,
-                          double Q, bool warm, QeqShared& sh, unsigned short* cache_j, double* cache_h,
-                          int cache_cap, double* gstage) {
+                          double Q, bool warm, QeqShared& sh, unsigned char* dyn, int dyn_bytes) {
   double* smem = sh.red;
-  double &sc_lam = sh.sc_lam, &sc_alpha = sh.sc_alpha, &sc_step = sh.sc_step, &sc_beta = sh.sc_beta;
-  int& sc_state = sh.sc_state;
-  auto& part = sh.part;
-  auto& part4 = sh.part4;
-  double *rs_x = sh.rs_x, *rs_p = sh.rs_p, *rs_hp = sh.rs_hp, *rs_di = sh.rs_di, *rs_c = sh.rs_c, *rs_eta = sh.rs_eta,
-         *rs_g = sh.rs_g;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   double* X = &QW(Q_X, 0);
   double* G = &QW(Q_G, 0);
-  double* G2 = &QW(Q_G2, 0);
-  double* Pv = &QW(Q_P, 0);
-  double* HP = &QW(Q_HP, 0);
   double* DI = &QW(Q_DINV, 0);
   double* Cr = &QW(Q_C, 0);
+  float* F = reinterpret_cast<float*>(&QW(7, 0));  // FP32 vectors and row constants: 8 x A floats in slots 7..10
   auto noop = [](double*) {};
   const double x0 = Q / n;
+  const int ebeg = w.cnt[a0 + r0], eend = w.cnt[a0 + r1];
+  const int nent = eend - ebeg;
+  // Shared-memory plan: [gradient stage: n doubles when it takes at most half the space][row cache].
+  // The cache holds FP32 values + 16-bit columns (6 B per entry, mixed precision) when the block's
+  // rows fit, else FP64 values + columns (10 B), else nothing (rows read from global memory).
+  const int stage_n = (dyn != nullptr && n * 8 <= dyn_bytes / 2) ? n : 0;
+  void* gstage = stage_n > 0 ? dyn : nullptr;
+  unsigned char* region = dyn != nullptr ? dyn + 8 * (size_t)stage_n : nullptr;
+  const long long region_bytes = dyn != nullptr ? dyn_bytes - 8ll * stage_n : 0;
+  const bool cols16 = n <= 65536;
+  const bool mixed = region != nullptr && cols16 && nent <= region_bytes / 6;
+  const bool cached64 = !mixed && region != nullptr && cols16 && nent <= region_bytes / 10;
+  void* cache_h = region;
+  unsigned short* cache_j = nullptr;
+  if (mixed) cache_j = reinterpret_cast<unsigned short*>(region + 4 * (size_t)(region_bytes / 6));
+  if (cached64) cache_j = reinterpret_cast<unsigned short*>(region + 8 * (size_t)(region_bytes / 10));
   // 1. Jacobi diagonal (eta + self-image shields) of the owned rows, and the start point: the
   //    uniform x0 = Q/n, or the caller's charges of an earlier step (already summing to Q).
   for (int r = r0 + wid; r < r1; r += nw) {
@@ -297,12 +613,8 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
     }
   }
   if (!team.sync(w)) return;
-  // 2. Pre-scaled rows H'_ij = H_ij / D_jj (cached or in hval), row sums, and the start point
-  //    x0 = Q/n with gradient g0 = H x0 + chi = (Q/n) * rowsum(H) + chi.
-  const int ebeg = w.cnt[a0 + r0], eend = w.cnt[a0 + r1];
-  const bool cached = cache_j != nullptr && (eend - ebeg) <= cache_cap;
-  // <D^-1, 1>, <D^-1, g>, <D^-1, g^2> at the start point, and <D^-1, g_u>, <D^-1, g_u^2> at the
-  // uniform start x0, whose projected norm sets the convergence scale for cold and warm starts alike
+  // 2. Pre-scaled rows H'_ij = H_ij / D_jj (cached in FP32 or FP64, or in hval in place), row sums
+  //    c_i = sum_j H'_ij + eta_i D_ii^-1, and the start gradient g = H x + chi.
   double acc[5] = {0, 0, 0, 0, 0};
   for (int r = r0 + wid; r < r1; r += nw) {
     const int a = a0 + r;
@@ -315,9 +627,12 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
       rs += h;
       cs += hp;
       if (warm) hx += h * __ldcg(X + j);
-      if (cached) {
+      if (mixed) {
         cache_j[e - ebeg] = (unsigned short)(j - a0);
-        cache_h[e - ebeg] = hp;
+        reinterpret_cast<float*>(cache_h)[e - ebeg] = float(hp);
+      } else if (cached64) {
+        cache_j[e - ebeg] = (unsigned short)(j - a0);
+        reinterpret_cast<double*>(cache_h)[e - ebeg] = hp;
       } else {
         w.hval[e] = hp;  // scaled in place; hval is not read after the solve
       }
@@ -334,8 +649,7 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
       const double g = warm ? hx + eta * X[a] + chi : gu;
       Cr[a] = cs + eta * di;
       G[a] = g;
-      Pv[a] = 0.0;
-      HP[a] = gu;  // kept for the projection step below, then cleared
+      QW(Q_HP, a) = gu;  // parked for the projection step below
       acc[0] += di;
       acc[1] += di * g;
       acc[2] += di * g * g;
@@ -344,7 +658,6 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
     }
   }
   if (!team_sum<5>(team, w, acc, smem, 0, noop)) return;
-  // Iteration scalars are computed by thread 0 alone (in the reductions' post hooks) and shared.
   const double s1 = acc[0];
   // 3. Project the start gradient explicitly (g - lambda with lambda = <D^-1, g> / <D^-1, 1>) and take
   //    its norm from the projected values: sum D^-1 g^2 - lambda sum D^-1 g cancels to rounding noise
@@ -352,179 +665,100 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
   //    atoms. The uniform start's projected norm sets the convergence scale.
   const double lam0 = acc[1] / s1, lamu = acc[3] / s1;
   double acc2[3] = {0, 0, 0};  // <D^-1, g~^2>, <D^-1, g~_u^2>, <D^-1, g~>
-  for (int r = r0 + wid; r < r1; r += nw) {
-    const int a = a0 + r;
+  for (int r = r0 + wid; r < r1; r += nw)
     if (lane == 0) {
+      const int a = a0 + r;
       const double di = DI[a];
       const double gt = G[a] - lam0;
-      const double gut = HP[a] - lamu;  // the uniform start's gradient, parked in HP by step 2
+      const double gut = QW(Q_HP, a) - lamu;
       G[a] = gt;
-      HP[a] = 0.0;
       acc2[0] += di * gt * gt;
       acc2[1] += di * gut * gut;
       acc2[2] += di * gt;
     }
-  }
+  if (!team_sum<3>(team, w, acc2, smem, 1, noop)) return;
   const double tol2 = w.cg_tol * w.cg_tol;
   const double gfloor = 1e-28 * fmax(acc[2], acc[4]);
-  double gz = 0.0, gz0 = 0.0;
-  if (!team_sum<3>(team, w, acc2, smem, 1, noop)) return;
-  if (threadIdx.x == 0) {
-    gz = acc2[0];
-    gz0 = acc2[1];  // the uniform start's projected norm (= gz when cold)
-    sc_lam = acc2[2] / s1;  // rounding-level drift of the projection, removed in the first step
-    sc_beta = 0.0;
-    // Nothing to solve when the projected gradient is already at rounding level (one atom, a start
-    // that is exact by symmetry) or a warm start already meets the tolerance.
-    sc_state = (!(gz > gfloor) || n < 2 || gz <= tol2 * gz0) ? 1 : 0;
-  }
-  // For blocks of at most 32 rows (the grid layout) the rows' solver state lives in shared memory.
-  const bool row_smem = (r1 - r0) <= 32;
-  if (row_smem && wid == 0 && r0 + lane < r1) {
-    const int a = a0 + r0 + lane;
-    rs_x[lane] = X[a];
-    rs_p[lane] = 0.0;
-    rs_hp[lane] = 0.0;
-    rs_di[lane] = DI[a];
-    rs_c[lane] = Cr[a];
-    rs_eta[lane] = atom_prm(ff, w.type[a], A_ETA);
-    rs_g[lane] = G[a];
-  }
-  __syncthreads();
-  int it = 0;
+  const double gz0 = acc2[1];  // the uniform start's projected norm (= the start's when cold)
+  const double target = tol2 * gz0;
+  double gz = acc2[0];
   int slot = 2;
-  while (sc_state == 0) {
-    if (++it > w.cg_max_iter) {
-      if (threadIdx.x == 0) atomicOr(w.status, XR_S_CG);
-      break;
+  int iters = 0;
+  bool fp64 = !mixed;
+  if (mixed) {
+    // 4a. Iterative refinement around FP32 solves of the correction problem.
+    const size_t A = w.A;
+    QeqVecs<float> v32{F, F + A, F + 2 * A, F + 3 * A, F + 4 * A, F + 5 * A, F + 6 * A, F + 7 * A};
+    for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+      const int a = a0 + r;
+      F[5 * A + a] = float(DI[a]);
+      F[6 * A + a] = float(atom_prm(ff, w.type[a], A_ETA) * DI[a]);
+      F[7 * A + a] = float(Cr[a]);
     }
-    const double lam = sc_lam, beta = sc_beta;
-    // p = -z + beta p,  Hp = -H z + beta Hp,  z = D^-1 (g - lambda); the next buffer gets g - lambda
-    if (gstage) {  // the whole gradient of the system in shared memory: the gathers below stay on-chip
-      for (int q = threadIdx.x; q < n; q += blockDim.x) gstage[q] = __ldcg(G + a0 + q);
-      __syncthreads();
-    }
-    double pHp[2] = {0.0, 0.0};  // lane partials in warp 0: p'Hp and <D^-1, Hp>
-    for (int tb = r0; tb < r1; tb += 32) {
-      const int r = tb + wid;
-      double hz = 0;
-      if (wid < 32 && r < r1) {
+    QeqMatrix<float> M32{reinterpret_cast<const float*>(cache_h), cache_j, true, true, ebeg,
+                         reinterpret_cast<float*>(gstage)};
+    for (int sweep = 0; sweep < 8; ++sweep) {
+      if (!(gz > target) || !(gz > gfloor) || n < 2) break;
+      for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
         const int a = a0 + r;
-        const int eb = w.cnt[a], ee = w.cnt[a + 1];
-        if (cached && gstage) {
-          for (int e = eb + lane; e < ee; e += 32) hz += cache_h[e - ebeg] * gstage[cache_j[e - ebeg]];
-        } else if (cached) {
-          for (int e = eb + lane; e < ee; e += 32) hz += cache_h[e - ebeg] * __ldcg(G + a0 + cache_j[e - ebeg]);
-        } else {
-          double h0 = 0, h1 = 0;
-          int e = eb + lane;
-          for (; e + 32 < ee; e += 64) {
-            const double g0 = __ldcg(G + w.edge[e].x), g1 = __ldcg(G + w.edge[e + 32].x);
-            h0 += w.hval[e] * g0;
-            h1 += w.hval[e + 32] * g1;
-          }
-          if (e < ee) h0 += w.hval[e] * __ldcg(G + w.edge[e].x);
-          hz = h0 + h1;
-        }
+        v32.g[a] = float(G[a]);
+        v32.p[a] = 0.0f;
+        v32.hp[a] = 0.0f;
+        v32.y[a] = 0.0f;
       }
-      if (wid < 32) part[wid][lane] = hz;
-      __syncthreads();
-      if (wid < 4) {  // lane = row of the tile; warp k adds lanes 8k .. 8k+7 of the row's partials
-        double s = part[lane][8 * wid];
-#pragma unroll
-        for (int k = 1; k < 8; ++k) s += part[lane][8 * wid + k];
-        part4[wid][lane] = s;
-      }
-      __syncthreads();
-      if (wid == 0 && tb + lane < r1) {
-        const int rr = tb + lane, a = a0 + rr;
-        double h = (part4[0][lane] + part4[1][lane]) + (part4[2][lane] + part4[3][lane]);
-        const double ga = row_smem ? rs_g[lane] : (gstage ? gstage[rr] : G[a]);
-        const double di = row_smem ? rs_di[lane] : DI[a];
-        const double eta = row_smem ? rs_eta[lane] : atom_prm(ff, w.type[a], A_ETA);
-        const double cr = row_smem ? rs_c[lane] : Cr[a];
-        const double p_old = row_smem ? rs_p[lane] : Pv[a];
-        const double hp_old = row_smem ? rs_hp[lane] : HP[a];
-        h += eta * di * ga - lam * cr;
-        const double z = di * (ga - lam);
-        const double p = -z + beta * p_old;
-        const double hp = -h + beta * hp_old;
-        if (row_smem) {
-          rs_p[lane] = p;
-          rs_hp[lane] = hp;
-          rs_g[lane] = ga - lam;
-        } else {
-          Pv[a] = p;
-          HP[a] = hp;
-          G2[a] = ga - lam;
+      if (!team.sync(w)) return;
+      // the correction's own projected norm starts at gz; 1e-10 of it (1e-5 in norm) per sweep,
+      // and no further than a hundredth of the final target
+      const double stop = fmax(1e-10 * gz, 0.01 * target);
+      const int it = qeq_cg<Team, float>(w, ff, team, sh, a0, n, r0, r1, v32, M32, s1, gz, stop, 0.0, 400, false, slot);
+      if (it < 0) return;
+      iters += it;
+      // x += y, then restore sum x = Q exactly: the FP32 step keeps sum y = 0 only to FP32 rounding,
+      // and the residual must be taken at a point on the constraint (a uniform shift added after
+      // convergence would change the projected gradient)
+      double sx[1] = {0.0};
+      for (int r = r0 + wid; r < r1; r += nw)
+        if (lane == 0) {
+          const int a = a0 + r;
+          X[a] += double(v32.y[a]);
+          sx[0] += X[a];
         }
-        pHp[0] += p * hp;
-        pHp[1] += di * hp;
+      if (!team_sum<1>(team, w, sx, smem, slot, noop)) return;
+      slot = slot == 1 ? 2 : 1;
+      const double shift = (Q - sx[0]) / n;
+      for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) X[a0 + r] += shift;
+      if (!team.sync(w)) return;
+      double gz_new = 0.0;
+      if (!qeq_residual(w, ff, team, sh, a0, r0, r1, s1, &gz_new, slot)) return;
+      const bool stalled = gz_new > 1e-3 * gz;
+      gz = gz_new;
+      if (stalled && gz > target) {
+        fp64 = true;  // FP32 solves no longer reduce the residual: finish in FP64
+        break;
       }
     }
-    if (wid == 0) {
-      pHp[0] = warp_total(pHp[0]);
-      pHp[1] = warp_total(pHp[1]);
-    }
-    if (!team.template reduce<2>(w, pHp, smem, slot, [&](double* t) {
-          // The QEq matrix of a close-packed geometry can have a negative eigenvalue (the reference's
-          // direct KKT solve accepts it); CG then takes steps of negative curvature (alpha < 0) and
-          // still converges. Only an exactly vanishing or non-finite p'Hp is a breakdown, and a
-          // non-positive one at rounding level means the solve has converged.
-          const bool rounding = gz <= 1e4 * gfloor;
-          if (!(fabs(t[0]) > 0.0) || !isfinite(t[0]) || (t[0] < 0.0 && rounding)) {
-            if (!rounding) atomicOr(w.status, XR_S_NONSPD);
-            sc_state = 2;
-          } else {
-            sc_alpha = gz / t[0];
-            sc_step = sc_alpha * t[1] / s1;
-          }
-        }))
-      return;
-    slot = slot == 1 ? 2 : 1;
-    if (sc_state != 0) break;
-    // Step: x += alpha p, g += alpha Hp - (multiplier change), one row per lane of warp 0.
-    const double alpha = sc_alpha, step_lam = sc_step;
-    double u[2] = {0, 0};
-    if (wid == 0) {
-      for (int rr = r0 + lane; rr < r1; rr += 32) {
-        const int a = a0 + rr;
-        if (row_smem) {
-          const double g = (rs_g[lane] + alpha * rs_hp[lane]) - step_lam;
-          rs_x[lane] += alpha * rs_p[lane];
-          rs_g[lane] = g;
-          G2[a] = g;  // published for the other rows' products
-          u[0] += rs_di[lane] * g;
-          u[1] += rs_di[lane] * g * g;
-        } else {
-          const double g = (G2[a] + alpha * HP[a]) - step_lam;
-          X[a] += alpha * Pv[a];
-          G2[a] = g;
-          const double di = DI[a];
-          u[0] += di * g;
-          u[1] += di * g * g;
-        }
-      }
-      u[0] = warp_total(u[0]);
-      u[1] = warp_total(u[1]);
-    }
-    if (!team.template reduce<2>(w, u, smem, slot, [&](double* t) {
-          sc_lam = t[0] / s1;
-          const double gz_new = t[1] - sc_lam * t[0];
-          if (gz_new <= tol2 * gz0) sc_state = 1;
-          sc_beta = gz_new / gz;
-          gz = gz_new;
-        }))
-      return;
-    slot = slot == 1 ? 2 : 1;
-    double* tmp = G;  // the buffer just written becomes the one read next
-    G = G2;
-    G2 = tmp;
+    if (!fp64 && gz > target && gz > gfloor && n >= 2) fp64 = true;  // sweep limit
   }
-  if (row_smem && wid == 0 && r0 + lane < r1) X[a0 + r0 + lane] = rs_x[lane];
-  __syncthreads();
-  if (threadIdx.x == 0) atomicMax(w.counts + 4, it);
-  // Final charges; the constraint is restored exactly against accumulated rounding.
+  if (fp64) {
+    // 4b. FP64 projected CG from the current charges (cold: the start point) to the tolerance.
+    QeqVecs<double> v64{G, &QW(Q_G2, 0), &QW(Q_P, 0), &QW(Q_HP, 0), X};
+    QeqMatrix<double> M64{reinterpret_cast<const double*>(cache_h), cache_j, cached64, !mixed, ebeg,
+                          reinterpret_cast<double*>(gstage)};
+    for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+      QW(Q_P, a0 + r) = 0.0;
+      QW(Q_HP, a0 + r) = 0.0;
+    }
+    __syncthreads();
+    const int it = qeq_cg<Team, double>(w, ff, team, sh, a0, n, r0, r1, v64, M64, s1, gz, target, gfloor,
+                                        w.cg_max_iter, true, slot);
+    if (it < 0) return;
+    iters += it;
+  }
+  if (threadIdx.x == 0) {
+    atomicMax(w.counts + 4, iters);
+    atomicMax(w.qiters + w.sys_of[a0], iters);
+  }
+  // 5. Final charges; the constraint is restored exactly against accumulated rounding.
   double sx[1] = {0.0};
   if (lane == 0)
     for (int r = r0 + wid; r < r1; r += nw) sx[0] += X[a0 + r];
@@ -543,17 +777,6 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
 // cache columns (16-bit, local to the system)]. Each system's solve splits it the same way.
 constexpr int kQeqMaxDyn = 208 * 1024;
 
-__device__ inline void qeq_smem_plan(unsigned char* dyn, int n, double** gstage, double** cache_h,
-                                     unsigned short** cache_j, int* cache_cap) {
-  // stage the gradient when it takes at most half the space; 16-bit cache columns need n <= 65536
-  const int stage_n = (n * 8 <= kQeqMaxDyn / 2) ? n : 0;
-  const int cap = n <= 65536 ? (int)((kQeqMaxDyn - (size_t)stage_n * 8) / (sizeof(double) + sizeof(unsigned short))) : 0;
-  *gstage = stage_n > 0 ? reinterpret_cast<double*>(dyn) : nullptr;
-  *cache_h = reinterpret_cast<double*>(dyn + sizeof(double) * (size_t)stage_n);
-  *cache_j = cap > 0 ? reinterpret_cast<unsigned short*>(dyn + sizeof(double) * ((size_t)stage_n + cap)) : nullptr;
-  *cache_cap = cap;
-}
-
 // Cooperative solver launch for a batch: the first nteam blocks form teams, one per large system
 // (map[b] = {system, rank, team size, first block of the team}); each team splits its system's rows
 // and synchronises through its own bounded counter. The remaining blocks each solve a share of the
@@ -563,27 +786,20 @@ __global__ void __launch_bounds__(1024, 1) k_qeq_grid(XrWork w, XrFF ff, const i
                                                       int nsmall) {
   __shared__ QeqShared sh;
   extern __shared__ __align__(16) unsigned char dyn[];
-  double *gstage, *cache_h;
-  unsigned short* cache_j;
-  int cache_cap;
   if ((int)blockIdx.x < nteam) {
     const int4 m = map[blockIdx.x];
     const XrSystem& S = w.sys[m.x];
     const int per = ((S.natoms + m.z - 1) / m.z + 31) / 32 * 32;
     const int r0 = min(S.natoms, m.y * per), r1 = min(S.natoms, r0 + per);
-    qeq_smem_plan(dyn, S.natoms, &gstage, &cache_h, &cache_j, &cache_cap);
     GridTeam team{w.barrier + m.w, w.red + (size_t)32 * m.w, m.z, m.y};
-    qeq_solve(w, ff, team, S.atom_off, S.natoms, r0, r1, S.total_charge, S.has_guess != 0, sh, cache_j, cache_h,
-              cache_cap, gstage);
+    qeq_solve(w, ff, team, S.atom_off, S.natoms, r0, r1, S.total_charge, S.has_guess != 0, sh, dyn, kQeqMaxDyn);
     return;
   }
   const int nsb = (int)gridDim.x - nteam;
   for (int k = (int)blockIdx.x - nteam; k < nsmall; k += nsb) {
     const XrSystem& S = w.sys[small[k]];
-    qeq_smem_plan(dyn, S.natoms, &gstage, &cache_h, &cache_j, &cache_cap);
     BlockTeam team;
-    qeq_solve(w, ff, team, S.atom_off, S.natoms, 0, S.natoms, S.total_charge, S.has_guess != 0, sh, cache_j, cache_h,
-              cache_cap, gstage);
+    qeq_solve(w, ff, team, S.atom_off, S.natoms, 0, S.natoms, S.total_charge, S.has_guess != 0, sh, dyn, kQeqMaxDyn);
     __syncthreads();
   }
 }
@@ -593,8 +809,7 @@ __global__ void __launch_bounds__(1024, 1) k_qeq_block(XrWork w, XrFF ff) {
   __shared__ QeqShared sh;
   const XrSystem& S = w.sys[blockIdx.x];
   BlockTeam team;
-  qeq_solve(w, ff, team, S.atom_off, S.natoms, 0, S.natoms, S.total_charge, S.has_guess != 0, sh, nullptr, nullptr,
-            0, nullptr);
+  qeq_solve(w, ff, team, S.atom_off, S.natoms, 0, S.natoms, S.total_charge, S.has_guess != 0, sh, nullptr, 0);
 }
 
 // ------------------------------------------------------------------------------ Coulomb

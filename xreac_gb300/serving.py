@@ -67,6 +67,21 @@ class Served:
         return self.done - self.arrival
 
 
+@dataclass
+class Batch:
+    """Record of one evaluated batch."""
+
+    force_field: str
+    requests: int
+    atoms: int
+    seconds: float       # wall time of the batch call (host preparation, device work, results)
+    launches: int        # kernels launched
+    qeq_iterations: int  # conjugate-gradient iterations summed over its systems
+    qeq_bytes: float     # algorithmic matrix-free bytes of those iterations
+    h2d_bytes: int = 0   # host-to-device bytes of the batch call
+    d2h_bytes: int = 0   # device-to-host bytes of the batch call
+
+
 class Server:
     """Continuous-batching server.
 
@@ -133,6 +148,23 @@ class Server:
     def __exit__(self, *exc):
         self.close()
 
+    # ------------------------------------------------------------------ instrumentation
+    def set_profiling(self, enable=True):
+        """Per-stage CUDA-event timing on every worker context (resets the accumulators)."""
+        for calcs in self._calcs:
+            for calc in calcs.values():
+                calc.set_profiling(enable)
+
+    def stage_times(self):
+        """Summed per-stage device milliseconds over every context, and the number of batches."""
+        total, calls = np.zeros(7), 0
+        for calcs in self._calcs:
+            for calc in calcs.values():
+                ms, n = calc.stage_times()
+                total += ms
+                calls += n
+        return total, calls
+
     # ------------------------------------------------------------------ worker side
     def _take_batch(self):
         """Oldest-first: the force field whose head request waited longest, then FIFO up to the budget."""
@@ -193,7 +225,10 @@ class Server:
                 except Exception as err:  # noqa: BLE001 - reported through the future
                     results.append(err)
         done = time.perf_counter()
-        self.batches.append((name, len(batch), sum(r.natoms for r, _ in batch), done - t0))
+        its, qbytes = calc.qeq_work()
+        h2d, d2h = calc.transfer_bytes()
+        self.batches.append(Batch(name, len(batch), sum(r.natoms for r, _ in batch), done - t0, calc.last_launches,
+                                  its, qbytes, h2d, d2h))
         for (req, fut), res in zip(batch, results):
             if isinstance(res, Exception):
                 fut.set_exception(res)
