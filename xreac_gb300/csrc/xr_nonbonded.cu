@@ -163,14 +163,14 @@ struct GridTeam {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     target += nb;
     double* res = result_slot(smem, slot);
-    // Fixed-size slots; consecutive reductions never share one, so a block may publish the next
-    // partials while a slower block still reads the previous ones.
+    // Fixed-size slots ([rank][8] doubles); consecutive reductions never share one, so a block may
+    // publish the next partials while a slower block still reads the previous ones.
     double* rs = red + (size_t)slot * 8 * nb;
     if (wid == 0) {
       int good = 1;
       __syncwarp();  // orders warp 0's row writes before lane 0's release
       if (lane == 0) {
-        for (int k = 0; k < NV; ++k) rs[k * nb + rank] = v[k];
+        for (int k = 0; k < NV; ++k) rs[rank * 8 + k] = v[k];
         asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(bar) : "memory");
         long long it = 0;
         while (ld_acquire(bar) < target) {
@@ -184,12 +184,30 @@ struct GridTeam {
         ok = good;
       }
       __syncwarp();
-      for (int k = 0; k < NV; ++k) {
-        double t = 0;
-        for (int q = lane; q < nb; q += 32) t += __ldcg(rs + k * nb + q);
+      // every lane issues all of its loads before adding (one memory round trip, not one per block);
+      // lane sums in rank order, then a fixed shuffle tree: deterministic
+      double t[NV];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-        if (lane == 0) res[k] = t;
+      for (int k = 0; k < NV; ++k) t[k] = 0.0;
+      for (int base = 0; base < nb; base += 5 * 32) {
+        double x[5][NV];
+#pragma unroll
+        for (int u = 0; u < 5; ++u) {
+          const int q = base + lane + 32 * u;
+#pragma unroll
+          for (int k = 0; k < NV; ++k) x[u][k] = q < nb ? __ldcg(rs + q * 8 + k) : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < 5; ++u)
+#pragma unroll
+          for (int k = 0; k < NV; ++k) t[k] += x[u][k];
+      }
+#pragma unroll
+      for (int k = 0; k < NV; ++k) {
+        double s = t[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) res[k] = s;
       }
       if (lane == 0) post(res);
     }
