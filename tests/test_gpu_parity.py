@@ -93,6 +93,36 @@ def water_4608():
     return workloads.water_box()
 
 
+@pytest.mark.parametrize("name", [n for n in golden_names() if n.endswith("_full")])
+def test_reference_fixture_charge_response(name):
+    """full_derivative=True: forces through the QEq solve (adjoint solve on the device)."""
+    g = load_golden(name)
+    c = calc(g["ff"])
+    r = c.evaluate(g["symbols"], g["positions"], cell=g["cell"], pbc=g["pbc"], total_charge=g["total_charge"],
+                   full_derivative=True)
+    assert r.full_derivative and r.force_convention == "charge_response"
+    check_strict(r, g, len(g["symbols"]))
+
+
+def test_fixed_and_charge_response_forces_differ():
+    """tests/test_calculator.py:14-28 and 109-119 of the reference: the two conventions differ by more
+    than 0.03 kcal/mol/A on a distorted water dimer, and the charge-response forces match central
+    finite differences of the energy."""
+    g = load_golden("water_distorted_dimer")
+    c = calc(g["ff"])
+    fixed = c.evaluate(g["symbols"], g["positions"])
+    full = c.evaluate(g["symbols"], g["positions"], full_derivative=True)
+    assert np.abs(fixed.forces - full.forces).max() > 0.03
+    h = 1e-5
+    x = np.array(g["positions"], dtype=float)
+    for a, d in ((0, 0), (1, 2), (3, 1)):
+        xp, xm = x.copy(), x.copy()
+        xp[a, d] += h
+        xm[a, d] -= h
+        fd = -(c.evaluate(g["symbols"], xp).energy - c.evaluate(g["symbols"], xm).energy) / (2 * h)
+        assert abs(full.forces[a, d] - fd) < 1e-5
+
+
 def test_full_size_water_box_against_oracle(water_4608):
     """The 1,536-H2O (4,608-atom) periodic water box against the CPU oracle."""
     from oracle import evaluate as oracle_evaluate

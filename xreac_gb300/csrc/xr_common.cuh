@@ -172,6 +172,8 @@ struct XrWork {
   double* q;
   const double* qguess;       // [A] initial QEq charges of systems with has_guess (sum = total charge)
   int* qiters;                // [S] QEq conjugate-gradient iterations of each system
+  double* qrhs;               // [A] adjoint QEq right-hand side (-dE/dq), full-derivative forces
+  double* qadj;               // [A] adjoint QEq solution lambda (sum lambda = 0 per system)
   double* f;                  // [A][3] gradient dE/dx accumulator (forces = -f)
   double* qwork;              // [XR_QW_N][A] QEq solver vectors
   double* red;                // reduction scratch for solvers
@@ -213,7 +215,8 @@ void xr_launch_scan(const XrWork& w, cudaStream_t st);
 void xr_launch_topology_fill(const XrWork& w, cudaStream_t st);
 void xr_launch_pairs(const XrWork& w, const XrFF& ff, cudaStream_t st);
 int xr_launch_qeq(const XrWork& w, const XrFF& ff, cudaStream_t st, int nblocks, const int4* map, int nteam,
-                  const int* small, int nsmall);
+                  const int* small, int nsmall, bool adjoint = false);
+void xr_launch_charge_response(const XrWork& w, const XrFF& ff, cudaStream_t st, int stage);
 int xr_qeq_coop_blocks_per_sm();
 void xr_launch_coulomb(const XrWork& w, const XrFF& ff, cudaStream_t st);
 void xr_launch_bonded(const XrWork& w, const XrFF& ff, cudaStream_t st);

@@ -105,6 +105,10 @@ struct xr_ctx {
   size_t cq = 0;
   double* qguess = nullptr;
   size_t cqguess = 0;
+  double* qrhs = nullptr;
+  size_t cqrhs = 0;
+  double* qadj = nullptr;
+  size_t cqadj = 0;
   double* f = nullptr;
   size_t cf = 0;
   double* qwork = nullptr;
@@ -314,6 +318,8 @@ bool ensure_atoms(xr_ctx* c, int A, int S) {
   GROW(a_e, 8 * (size_t)A);
   GROW(q, A);
   GROW(qguess, A);
+  GROW(qrhs, A);
+  GROW(qadj, A);
   GROW(f, 3 * (size_t)A);
   GROW(qwork, (size_t)XR_QW_N * A);
   GROW(outbuf, 8 * (size_t)A);
@@ -456,6 +462,8 @@ void attach_lists(xr_ctx* c, XrWork& w) {
   w.nmids = c->nmids;
   w.nmask = c->nmids + 1;
   w.qguess = c->qguess;
+  w.qrhs = c->qrhs;
+  w.qadj = c->qadj;
   w.qiters = c->qiters;
   w.mlist = c->mlist;
 }
@@ -601,10 +609,6 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
   if (!c || !ff || nsys < 1 || !sys) {
     if (c) c->err = "invalid arguments";
     return XR_EINPUT;
-  }
-  if (flags & XR_FLAG_FULL_DERIVATIVE) {
-    c->err = "full_derivative forces are not available in this build";
-    return XR_EUNSUPPORTED;
   }
   const bool dev_io = (flags & XR_FLAG_DEVICE_IO) != 0;
   if (dev_io && nsys != 1) {
@@ -763,6 +767,14 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
   stage(c, 4, st);
   xr_launch_coulomb(w, ff->d, st);
   launches += 1;
+  if (w.full_derivative) {
+    // charge-response forces: adjoint QEq solve with the same plan, then its radial pair terms
+    xr_launch_charge_response(w, ff->d, st, 0);
+    if (int le = xr_launch_qeq(w, ff->d, st, qblocks, c->qmap, qteam, c->qsmall, qsmall, true))
+      return cuda_fail(c, (cudaError_t)le, "adjoint QEq launch");
+    xr_launch_charge_response(w, ff->d, st, 1);
+    launches += 4;
+  }
   stage(c, 5, st);
   xr_launch_bonded(w, ff->d, st);
   launches += 14;
@@ -1044,7 +1056,7 @@ void xr_ctx_destroy(xr_ctx* c) {
                   c->qwork, c->outbuf, c->edge, c->edge_pair, c->edge_dbslot, c->hval, c->pair_edge, c->pair_i,
                   c->pair_bond, c->p_r, c->p_shield, c->p_dshield, c->p_g, c->p_evdw, c->p_ecoul, c->bond_pair,
                   c->bond_i, c->bond_j, c->b_r, c->b_v, c->b_fwd, c->b_adj, c->b_e, c->dbrow, c->sys, c->energy,
-                  c->props, c->status, c->counts, c->barrier, c->qmap, c->qsmall, c->qiters, c->red, c->qguess, c->bx_meta, c->bx_bo, c->bx_count,
+                  c->props, c->status, c->counts, c->barrier, c->qmap, c->qsmall, c->qiters, c->red, c->qguess, c->qrhs, c->qadj, c->bx_meta, c->bx_bo, c->bx_count,
                   c->esum, c->arow, c->nact, c->nzrow, c->nnz, c->chunks, c->sys_chunks, c->chunk_part, c->mids, c->nmids, c->mlist};
   for (void* p : bufs)
     if (p) cudaFree(p);

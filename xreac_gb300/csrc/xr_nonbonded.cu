@@ -533,7 +533,7 @@ __device__ int qeq_cg(const XrWork& w, const XrFF& ff, const Team& team, QeqShar
 // <D^-1, G^2> (from the projected values, so free of cancellation). Two team reductions.
 template <class Team>
 __device__ bool qeq_residual(const XrWork& w, const XrFF& ff, const Team& team, QeqShared& sh, int a0, int r0, int r1,
-                             double s1, double* gz_out, int& slot) {
+                             double s1, double* gz_out, int& slot, bool adjoint) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   double* X = &QW(Q_X, 0);
   double* G = &QW(Q_G, 0);
@@ -548,7 +548,7 @@ __device__ bool qeq_residual(const XrWork& w, const XrFF& ff, const Team& team, 
     for (int o = 16; o > 0; o >>= 1) hx += __shfl_xor_sync(0xffffffffu, hx, o);
     if (lane == 0) {
       const int t = w.type[a];
-      const double g = hx + atom_prm(ff, t, A_ETA) * X[a] + atom_prm(ff, t, A_CHI);
+      const double g = hx + atom_prm(ff, t, A_ETA) * X[a] + (adjoint ? w.qrhs[a] : atom_prm(ff, t, A_CHI));
       G[a] = g;
       acc[0] += DI[a] * g;
     }
@@ -590,7 +590,7 @@ __device__ bool qeq_residual(const XrWork& w, const XrFF& ff, const Team& team, 
 // mode, else FP64); when `gstage` is non-null the whole gradient is staged in shared memory.
 template <class Team>
 __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int a0, int n, int r0, int r1,
-                          double Q, bool warm, QeqShared& sh, unsigned char* dyn, int dyn_bytes) {
+                          double Q, bool warm, QeqShared& sh, unsigned char* dyn, int dyn_bytes, bool adjoint) {
   double* smem = sh.red;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   double* X = &QW(Q_X, 0);
@@ -662,7 +662,7 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
       if (warm) hx += __shfl_xor_sync(0xffffffffu, hx, o);
     }
     if (lane == 0) {
-      const double eta = atom_prm(ff, t, A_ETA), di = DI[a], chi = atom_prm(ff, t, A_CHI);
+      const double eta = atom_prm(ff, t, A_ETA), di = DI[a], chi = adjoint ? w.qrhs[a] : atom_prm(ff, t, A_CHI);
       const double gu = x0 * (rs + eta) + chi;
       const double g = warm ? hx + eta * X[a] + chi : gu;
       Cr[a] = cs + eta * di;
@@ -747,7 +747,7 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
       for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) X[a0 + r] += shift;
       if (!team.sync(w)) return;
       double gz_new = 0.0;
-      if (!qeq_residual(w, ff, team, sh, a0, r0, r1, s1, &gz_new, slot)) return;
+      if (!qeq_residual(w, ff, team, sh, a0, r0, r1, s1, &gz_new, slot, adjoint)) return;
       const bool stalled = gz_new > 1e-3 * gz;
       gz = gz_new;
       if (stalled && gz > target) {
@@ -785,6 +785,10 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
   for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
     const int a = a0 + r;
     const double q = X[a] + shift;
+    if (adjoint) {
+      w.qadj[a] = q;
+      continue;
+    }
     w.q[a] = q;
     const int t = w.type[a];
     AEV(6, a) = SELF_CONVERSION * (atom_prm(ff, t, A_CHI) * q + 0.5 * atom_prm(ff, t, A_ETA) * q * q);
@@ -801,7 +805,7 @@ constexpr int kQeqMaxDyn = 208 * 1024;
 // small systems (small[k], k = b - nteam, b - nteam + (gridDim.x - nteam), ...) alone, with block
 // barriers only. All blocks are co-resident (cooperative launch, one block per SM).
 __global__ void __launch_bounds__(1024, 1) k_qeq_grid(XrWork w, XrFF ff, const int4* map, int nteam, const int* small,
-                                                      int nsmall) {
+                                                      int nsmall, int adjoint) {
   __shared__ QeqShared sh;
   extern __shared__ __align__(16) unsigned char dyn[];
   if ((int)blockIdx.x < nteam) {
@@ -810,24 +814,27 @@ __global__ void __launch_bounds__(1024, 1) k_qeq_grid(XrWork w, XrFF ff, const i
     const int per = ((S.natoms + m.z - 1) / m.z + 31) / 32 * 32;
     const int r0 = min(S.natoms, m.y * per), r1 = min(S.natoms, r0 + per);
     GridTeam team{w.barrier + m.w, w.red + (size_t)32 * m.w, m.z, m.y};
-    qeq_solve(w, ff, team, S.atom_off, S.natoms, r0, r1, S.total_charge, S.has_guess != 0, sh, dyn, kQeqMaxDyn);
+    qeq_solve(w, ff, team, S.atom_off, S.natoms, r0, r1, adjoint ? 0.0 : S.total_charge, !adjoint && S.has_guess != 0,
+              sh, dyn, kQeqMaxDyn, adjoint != 0);
     return;
   }
   const int nsb = (int)gridDim.x - nteam;
   for (int k = (int)blockIdx.x - nteam; k < nsmall; k += nsb) {
     const XrSystem& S = w.sys[small[k]];
     BlockTeam team;
-    qeq_solve(w, ff, team, S.atom_off, S.natoms, 0, S.natoms, S.total_charge, S.has_guess != 0, sh, dyn, kQeqMaxDyn);
+    qeq_solve(w, ff, team, S.atom_off, S.natoms, 0, S.natoms, adjoint ? 0.0 : S.total_charge,
+              !adjoint && S.has_guess != 0, sh, dyn, kQeqMaxDyn, adjoint != 0);
     __syncthreads();
   }
 }
 
 // Fallback without cooperative launch: one block per system, no shared-memory row cache.
-__global__ void __launch_bounds__(1024, 1) k_qeq_block(XrWork w, XrFF ff) {
+__global__ void __launch_bounds__(1024, 1) k_qeq_block(XrWork w, XrFF ff, int adjoint) {
   __shared__ QeqShared sh;
   const XrSystem& S = w.sys[blockIdx.x];
   BlockTeam team;
-  qeq_solve(w, ff, team, S.atom_off, S.natoms, 0, S.natoms, S.total_charge, S.has_guess != 0, sh, nullptr, 0);
+  qeq_solve(w, ff, team, S.atom_off, S.natoms, 0, S.natoms, adjoint ? 0.0 : S.total_charge,
+            !adjoint && S.has_guess != 0, sh, nullptr, 0, adjoint != 0);
 }
 
 // ------------------------------------------------------------------------------ Coulomb
@@ -984,7 +991,39 @@ __global__ void k_reduce_final(XrWork w) {
   }
 }
 
+// -dE/dq per atom (warp per atom over its directed edges).
+__global__ void k_qeq_rhs(XrWork w, XrFF ff) {
+  const int lane = threadIdx.x & 31;
+  const int a = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
+  if (a >= w.A) return;
+  double s = 0;
+  for (int e = w.cnt[a] + lane; e < w.cnt[a + 1]; e += 32) s += w.q[w.edge[e].x] * w.p_shield[w.edge_pair[e]];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) {
+    const int t = w.type[a];
+    const double dEdq = C_ELE * s + SELF_CONVERSION * (atom_prm(ff, t, A_CHI) + atom_prm(ff, t, A_ETA) * w.q[a]);
+    w.qrhs[a] = -dEdq;
+  }
+}
+
+__global__ void k_charge_response_radial(XrWork w) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= w.nP) return;
+  const int i = w.pair_i[p], j = w.edge[w.pair_edge[p]].x;
+  w.p_g[p] += -QEQ_COULOMB * (w.qadj[i] * w.q[j] + w.qadj[j] * w.q[i]) * w.p_dshield[p];
+}
+
 }  // namespace
+
+void xr_launch_charge_response(const XrWork& w, const XrFF& ff, cudaStream_t st, int stage) {
+  if (stage == 0) {
+    k_qeq_rhs<<<(w.A + 3) / 4, 128, 0, st>>>(w, ff);
+    if (w.nE > 0) k_hval<<<(w.nE + 255) / 256, 256, 0, st>>>(w);  // the solve may have scaled them in place
+  } else if (w.nP > 0) {
+    k_charge_response_radial<<<(w.nP + 255) / 256, 256, 0, st>>>(w);
+  }
+}
 
 void xr_launch_pairs(const XrWork& w, const XrFF& ff, cudaStream_t st) {
   if (w.nP > 0) k_pairs<<<(w.nP + 127) / 128, 128, 0, st>>>(w, ff);
@@ -1002,16 +1041,26 @@ int xr_qeq_coop_blocks_per_sm() {
 // solver runs nblocks blocks (nteam team blocks described by map, the rest over the small list);
 // nblocks = 0 selects the one-block-per-system fallback.
 int xr_launch_qeq(const XrWork& w, const XrFF& ff, cudaStream_t st, int nblocks, const int4* map, int nteam,
-                  const int* small, int nsmall) {
+                  const int* small, int nsmall, bool adjoint) {
+  int adj = adjoint ? 1 : 0;
   if (nblocks > 0) {
     if (nteam > 0) cudaMemsetAsync(w.barrier, 0, sizeof(unsigned) * (size_t)nteam, st);
-    void* args[] = {(void*)&w, (void*)&ff, (void*)&map, (void*)&nteam, (void*)&small, (void*)&nsmall};
+    void* args[] = {(void*)&w, (void*)&ff, (void*)&map, (void*)&nteam, (void*)&small, (void*)&nsmall, (void*)&adj};
     cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_qeq_grid, dim3(nblocks), dim3(1024), args, kQeqMaxDyn, st);
     return (int)e;
   }
-  k_qeq_block<<<w.S, 1024, 0, st>>>(w, ff);
+  k_qeq_block<<<w.S, 1024, 0, st>>>(w, ff, adj);
   return (int)cudaGetLastError();
 }
+
+// Charge-response (full-derivative) forces, xreac's full_derivative=True (src/xreac/calculator.py:
+// 134-148 differentiates through the KKT solve of src/xreac/energy.py:95-102). With E(q(x), x) and
+// H q + chi = mu 1, sum q = Q, the adjoint lambda solves H lambda = dE/dq - nu 1, sum lambda = 0, and
+// dE/dx = dE/dx|_q - lambda' (dH/dx) q. dE/dq_k = 332.06371 sum_(k->j) q_j shield + 23.02 (chi_k +
+// eta_k q_k) (the Coulomb and self energies; the QEq matrix uses 14.4, so E is not stationary in q).
+// stage 0: the adjoint right-hand side -dE/dq (the solver's "chi") and the unscaled matrix entries;
+// stage 1: each pair's radial term -14.4 (lambda_i q_j + lambda_j q_i) dshield/dr.
+
 
 void xr_launch_coulomb(const XrWork& w, const XrFF& ff, cudaStream_t st) {
   (void)ff;
