@@ -39,6 +39,7 @@ enum xr_status {
 /* Evaluation flags. */
 #define XR_FLAG_FULL_DERIVATIVE 1u /* charge-response forces (xreac full_derivative=True) */
 #define XR_FLAG_DEVICE_IO 2u       /* positions and result arrays are device pointers */
+#define XR_FLAG_PARAM_GRADIENT 4u  /* also dE/dtheta for bond, angle and vdW parameters (xr_get_param_gradient) */
 
 typedef struct xr_ff xr_ff;
 typedef struct xr_ctx xr_ctx;
@@ -116,6 +117,17 @@ int xr_get_neighbors(xr_ctx* ctx, int index, int* i, int* j, int* S, long long c
  * index -1 returns those of every system of the batch at once, with atom indices counted over the
  * systems concatenated in call order. Host pointers; *count as for xr_get_neighbors. */
 int xr_get_bonds(xr_ctx* ctx, int index, int* i, int* j, int* S, double* bo, long long capacity, long long* count);
+
+/* Gradient of the total energy, summed over the systems of the last call made with
+ * XR_FLAG_PARAM_GRADIENT, with respect to force-field parameters (no reference counterpart; the
+ * reference has no parameter derivatives): pair_grad[(s*ntypes + t)*28 + column] over the pair-table
+ * columns of xr_ff_create (filled: De_s, De_p, De_pp, p_be1, p_be2, p_ovun1, p_bo1..p_bo6, r_s, r_p, r_pp, D,
+ * alpha, gamma_w, r_vdW, rcore, ecore, acore; others 0), and angle_grad[row*7 + k] over the angle
+ * records (theta00, p_val1, p_val2, p_coa1, p_val7, p_pen1, p_val4). A parameter stored once for
+ * both orders of a pair (or for both ends of an angle) gets the sum of its rows. Charges do not
+ * depend on these parameters, so this is the total derivative. npair = ntypes^2 * 28 and
+ * nangle = 7 * (angle records) must match. */
+int xr_get_param_gradient(const xr_ctx* ctx, double* pair_grad, long long npair, double* angle_grad, long long nangle);
 
 /* Number of CUDA kernels the last xr_eval / xr_eval_batch call launched. */
 long long xr_last_launches(const xr_ctx* ctx);

@@ -28,6 +28,7 @@ XR_EUNSUPPORTED = 10
 
 XR_FLAG_FULL_DERIVATIVE = 1
 XR_FLAG_DEVICE_IO = 2
+XR_FLAG_PARAM_GRADIENT = 4
 
 EXPORTED = (
     "xr_ff_create",
@@ -47,6 +48,7 @@ EXPORTED = (
     "xr_last_transfer_bytes",
     "xr_last_qeq_iterations",
     "xr_last_qeq_work",
+    "xr_get_param_gradient",
     "xr_count_neighbors_static",
     "xr_static_last_error",
 )
@@ -132,6 +134,8 @@ def load():
     lib.xr_last_qeq_iterations.restype = c_int
     lib.xr_last_qeq_work.argtypes = [c_void_p, POINTER(c_longlong), POINTER(c_double)]
     lib.xr_last_qeq_work.restype = c_int
+    lib.xr_get_param_gradient.argtypes = [c_void_p, POINTER(c_double), c_longlong, POINTER(c_double), c_longlong]
+    lib.xr_get_param_gradient.restype = c_int
     lib.xr_count_neighbors_static.argtypes = [POINTER(System), c_double, c_void_p, POINTER(c_int), POINTER(c_longlong)]
     lib.xr_count_neighbors_static.restype = c_int
     lib.xr_static_last_error.argtypes = []

@@ -78,6 +78,60 @@ class Evaluation:
         return dense
 
 
+# Pair-table columns (xreac_gb300.forcefield.PAIR_COLUMNS order) with a parameter gradient, and the
+# angle record entries (src/xreac/forcefield.py angle block order).
+GRADIENT_PAIR_COLUMNS = ("De_s", "De_p", "De_pp", "p_be1", "p_be2", "p_ovun1", "p_bo1", "p_bo2", "p_bo3", "p_bo4",
+                         "p_bo5", "p_bo6", "r_s", "r_p", "r_pp", "D", "alpha", "gamma_w", "r_vdW", "rcore", "ecore",
+                         "acore")
+ANGLE_PARAMETERS = ("theta_00", "p_val1", "p_val2", "p_coa1", "p_val7", "p_pen1", "p_val4")
+
+
+@dataclass(frozen=True)
+class ParameterGradient:
+    """dE/dtheta keyed like ``ForceField.pairs`` and ``ForceField.angles``.
+
+    ``pairs[(s, t)][name]`` and ``angles[(a, b, c)][record][k]`` (k in ``ANGLE_PARAMETERS`` order).
+    A parameter the force field stores once for several keys (a pair's two orders, an angle's two
+    ends) appears under each of them with the summed gradient of all its table rows, i.e. the
+    derivative with respect to that single stored value.
+    """
+
+    pairs: dict
+    angles: dict
+
+    @classmethod
+    def from_rows(cls, ff, pair_rows, angle_rows, angle_keys):
+        from .forcefield import PAIR_COLUMNS
+
+        names = ff.elements
+        T = len(names)
+        cols = [PAIR_COLUMNS.index(c) for c in GRADIENT_PAIR_COLUMNS]
+        by_obj = {}
+        for si, s in enumerate(names):
+            for ti, t in enumerate(names):
+                key = (s, t)
+                if key not in ff.pairs:
+                    continue
+                by_obj.setdefault(id(ff.pairs[key]), [np.zeros(len(cols)), []])
+                acc = by_obj[id(ff.pairs[key])]
+                acc[0] += pair_rows[si * T + ti, cols]
+                acc[1].append(key)
+        pairs = {}
+        for vec, keys in by_obj.values():
+            d = dict(zip(GRADIENT_PAIR_COLUMNS, map(float, vec)))
+            for key in keys:
+                pairs[key] = d
+        rec = {}
+        for row, (key, q) in enumerate(angle_keys):
+            obj = id(ff.angles[key][q])
+            rec.setdefault(obj, np.zeros(7))
+            rec[obj] += angle_rows[row]
+        angles = {}
+        for key, records in ff.angles.items():
+            angles[key] = [rec.get(id(r), np.zeros(7)).copy() for r in records]
+        return cls(pairs, angles)
+
+
 def _guess(initial_charges, n):
     if initial_charges is None:
         return None
@@ -103,6 +157,7 @@ class Calculator:
         self._ctx = nat.Context(device)
         self._lib = nat.load()
         self._type_pos = {s: k for k, s in enumerate(force_field.elements) if isinstance(s, str) and s}
+        self._angle_rows = force_field.angle_row_keys()
 
     def set_qeq(self, tolerance=1e-13, max_iterations=2000):
         """QEq solver tolerance and iteration limit.
@@ -181,6 +236,39 @@ class Calculator:
         guess = _guess(initial_charges, len(symbols))
         return self._run([(types, x, flags, cellm, float(total_charge), guess)], full_derivative, [reps], backend)[0]
 
+    def parameter_gradient(self, symbols, positions, *, total_charge=0, cell=None, pbc=None, initial_charges=None):
+        """Energy, forces and dE/dtheta for the bond, angle and vdW parameters (an extension; xreac
+        has no parameter derivatives). Returns ``(Evaluation, ParameterGradient)``.
+
+        The gradient comes from the same hand-written adjoint as the forces: each energy kernel adds
+        its parameter sensitivities, the bond-order parameters get theirs through the bond-order
+        chain's adjoints. Charges do not depend on these parameters, so it is the total derivative.
+        """
+        return self.parameter_gradient_many([dict(symbols=symbols, positions=positions, total_charge=total_charge,
+                                                  cell=cell, pbc=pbc, initial_charges=initial_charges)])
+
+    def parameter_gradient_many(self, systems):
+        """As :meth:`parameter_gradient` for a batch: a list of evaluations and the gradient of their
+        summed energy."""
+        batch, reps = [], []
+        for s in systems:
+            sym, x, types, flags, cellm, rp = self._prepare(s["symbols"], s["positions"], s.get("total_charge", 0),
+                                                            s.get("cell"), s.get("pbc"), False)
+            guess = _guess(s.get("initial_charges"), len(sym))
+            batch.append((types, x, flags, cellm, float(s.get("total_charge", 0)), guess))
+            reps.append(rp)
+        results = self._run(batch, False, reps, "replicated", nat.XR_FLAG_PARAM_GRADIENT)
+        T = len(self.force_field.elements)
+        pair = np.zeros(T * T * 28)
+        angle = np.zeros(7 * len(self._angle_rows))
+        code = self._lib.xr_get_param_gradient(self._ctx.handle, nat.ptr(pair, nat.c_double), len(pair),
+                                               nat.ptr(angle, nat.c_double) if len(angle) else None, len(angle))
+        if code != nat.XR_OK:
+            raise RuntimeError("parameter gradient unavailable")
+        grad = ParameterGradient.from_rows(self.force_field, pair.reshape(T * T, 28), angle.reshape(-1, 7),
+                                           self._angle_rows)
+        return (results[0] if len(systems) == 1 else results), grad
+
     def evaluate_many(self, systems, *, full_derivative=False):
         """Evaluate independent systems in one ragged device batch.
 
@@ -197,7 +285,7 @@ class Calculator:
             reps.append(rp)
         return self._run(batch, full_derivative, reps, "replicated")
 
-    def _run(self, batch, full_derivative, reps, backend):
+    def _run(self, batch, full_derivative, reps, backend, extra_flags=0):
         lib = self._lib
         n_sys = len(batch)
         sizes = [len(b[0]) for b in batch]
@@ -235,7 +323,7 @@ class Calculator:
             r.lone_pairs = q_base + 8 * (2 * total + a0)
             r.bond_counts = c_base + 4 * a0
             r.dipole = d_base + 24 * k
-        flags_ = nat.XR_FLAG_FULL_DERIVATIVE if full_derivative else 0
+        flags_ = (nat.XR_FLAG_FULL_DERIVATIVE if full_derivative else 0) | extra_flags
         code = lib.xr_eval_batch(self._ctx.handle, self._ff.handle, n_sys, sys_arr, flags_, res_arr)
         if code != nat.XR_OK:
             self._raise(code)

@@ -346,6 +346,16 @@ __device__ inline void k_bond_energy_one(const XrWork& w, const XrFF& ff, int b)
   const double ex = exp(be1 * (1.0 - powv));
   double e_bond = -(Des * sig * ex + Dep * pi + Depp * pp);
   BJV(BJ_SIG, b) = -Des * ex * (1.0 - be1 * be2 * powv);
+  if (w.pgrad) {  // dE/d(De_s, De_p, De_pp, p_be1, p_be2)
+    double* gp = w.pgrad + (size_t)pt * XR_NPAIR_COLS;
+    atomicAdd(gp + P_DE_S, -sig * ex);
+    if (pi != 0.0) atomicAdd(gp + P_DE_P, -pi);
+    if (pp != 0.0) atomicAdd(gp + P_DE_PP, -pp);
+    if (sig > 0) {
+      atomicAdd(gp + P_BE1, -Des * sig * ex * (1.0 - powv));
+      atomicAdd(gp + P_BE2, Des * sig * ex * be1 * powv * log(sig));
+    }
+  }
   BJV(BJ_PI, b) += -Dep;
   BJV(BJ_PP, b) += -Depp;
   double e_c2 = 0.0, dbo = 0.0;
@@ -563,6 +573,19 @@ __global__ void __launch_bounds__(32 * kBondedWarps) k_angles(XrWork w, XrFF ff)
         v[4] += f7 * v1 * branch * df8_ddb;
         const double Gp = exp(-g[19] * ((bij - 2) * (bij - 2) + (bjk - 2) * (bjk - 2)));
         const double ep = pen1 * Fp * Gp;
+        if (w.pgrad) {
+          // dE/d(theta00, v1, v2, coa1, v7, pen1, v4) of this record
+          double* ga = w.pgrad + w.pgrad_angle_off + 7 * (size_t)(first + q);
+          const double sgn_dt2 = dt * dt * exang;  // d branch / d v2 (either sign of v1)
+          const double df7_dv4 = pv3 * pij * lbij * A1 * (1 - A2) + (1 - A1) * pv3 * pjk * lbjk * A2;
+          const double df8_dv7 = (pv5 - 1) * (2 + ex6) / (den8 * den8) * (-db_j * ex7);
+          atomicAdd(ga + 0, dE_ddt * (-(1 - e17) * k180));
+          atomicAdd(ga + 1, f7 * f8 * branch);
+          atomicAdd(ga + 2, f7 * f8 * v1 * sgn_dt2);
+          atomicAdd(ga + 4, f7 * v1 * branch * df8_dv7);
+          atomicAdd(ga + 5, Fp * Gp);
+          atomicAdd(ga + 6, f8 * v1 * branch * df7_dv4);
+        }
         v[1] += ep;
         v[5] += pen1 * dFp_dd * Gp;
         dbij += ep * (-2 * g[19] * (bij - 2));
@@ -570,6 +593,7 @@ __global__ void __launch_bounds__(32 * kBondedWarps) k_angles(XrWork w, XrFF ff)
         const double K2 = exp(-g[38] * (ti_b * ti_b + tk_b * tk_b));
         const double K3 = exp(-g[30] * ((bij - 1.5) * (bij - 1.5) + (bjk - 1.5) * (bjk - 1.5)));
         const double ec_ = coa1 * K1 * K2 * K3;
+        if (w.pgrad) atomicAdd(w.pgrad + w.pgrad_angle_off + 7 * (size_t)(first + q) + 3, K1 * K2 * K3);
         v[2] += ec_;
         v[6] += coa1 * dK1_dt * K2 * K3;
         dtot_i += ec_ * (-2 * g[38] * ti_b);
@@ -1091,6 +1115,13 @@ __device__ inline void k_chain_bond_one(const XrWork& w, const XrFF& ff, int b) 
   double A_bo = BJV(BJ_BO, b) + AJV(AJ_TOTAL_ALL, i) + AJV(AJ_TOTAL_ALL, j) +
                 (AJV(AJ_OV1, i) + AJV(AJ_OV1, j)) * pair_prm(ff, pt, P_OVUN1) * pair_prm(ff, pt, P_DE_S) +
                 (AJV(AJ_PRODSUM, i) + AJV(AJ_PRODSUM, j)) * 8.0 * b7;
+  if (w.pgrad && bo != 0.0) {
+    // De_s and p_ovun1 also weight the over-coordination sum ov1 = sum p_ovun1 De_s bo of both ends
+    double* gp = w.pgrad + (size_t)pt * XR_NPAIR_COLS;
+    const double a_ov = (AJV(AJ_OV1, i) + AJV(AJ_OV1, j)) * bo;
+    atomicAdd(gp + P_DE_S, a_ov * pair_prm(ff, pt, P_OVUN1));
+    atomicAdd(gp + P_OVUN1, a_ov * pair_prm(ff, pt, P_DE_S));
+  }
   const double di = AFV(AF_TOTAL, i) - atom_prm(ff, ti, A_VALENCY), dj = AFV(AF_TOTAL, j) - atom_prm(ff, tj, A_VALENCY);
   const double dfi = atom_prm(ff, ti, A_MASS) <= 21 ? 1.0 : 0.0, dfj = atom_prm(ff, tj, A_MASS) <= 21 ? 1.0 : 0.0;
   const double A_P = AJV(AJ_OV2, i) * (dj - dfi * AFV(AF_DLPT, j)) + AJV(AJ_OV2, j) * (di - dfj * AFV(AF_DLPT, i)) +
@@ -1147,18 +1178,38 @@ __global__ void k_chain_deltap(XrWork w) {
 }
 
 // dE/dr of each bond from the uncorrected bond orders; added to the pair's radial accumulator.
-__device__ inline void k_chain_radial_one(const XrWork& w, int b) {
+__device__ inline void k_chain_radial_one(const XrWork& w, const XrFF& ff, int b) {
   if (BFV(BF_MASK, b) == 0.0) return;
   const double d_bo0 = BJV(BJ_BO0, b) + AJV(AJ_DELTAP, w.bond_i[b]) + AJV(AJ_DELTAP, w.bond_j[b]);
   const double G = d_bo0 * BFV(BF_DSIG, b) + (d_bo0 + BJV(BJ_PI0, b)) * BFV(BF_DPI, b) +
                    (d_bo0 + BJV(BJ_PP0, b)) * BFV(BF_DPP, b);
   w.p_g[w.bond_pair[b]] += G;
+  if (w.pgrad) {
+    // dE/d(p_bo1..6, r_s, r_p, r_pp): the uncorrected orders' parameters, through the same chain
+    // adjoints (dE/dsigma' = dE/dBO0, dE/dpi' = dE/dBO0 + dE/dPI0, dE/dpipi' = dE/dBO0 + dE/dPP0)
+    const int ti = w.type[w.bond_i[b]], tj = w.type[w.bond_j[b]], T = ff.ntypes, pt = ti * T + tj;
+    double* gp = w.pgrad + (size_t)pt * XR_NPAIR_COLS;
+    const double r = w.b_r[b], lr = log(r), cut = 0.01 * ff.g[29];
+    const double adj[3] = {d_bo0, d_bo0 + BJV(BJ_PI0, b), d_bo0 + BJV(BJ_PP0, b)};
+    const int cr[3] = {A_R_S, A_R_PI, A_R_PI_PI};
+    const int ca[3] = {P_BO1, P_BO3, P_BO5}, cb[3] = {P_BO2, P_BO4, P_BO6}, cr0[3] = {P_RS, P_RP, P_RPP};
+    for (int k = 0; k < 3; ++k) {
+      if (!(atom_prm(ff, ti, cr[k]) > 0 && atom_prm(ff, tj, cr[k]) > 0) || adj[k] == 0.0) continue;
+      const double pa = pair_prm(ff, pt, ca[k]), pb = pair_prm(ff, pt, cb[k]), r0 = pair_prm(ff, pt, cr0[k]);
+      const double lt = lr - __ldg(ff.pair_logr + 3 * pt + k);
+      const double t = exp(pb * lt);
+      const double bo = (k == 0 ? 1.0 + cut : 1.0) * exp(pa * t);
+      atomicAdd(gp + ca[k], adj[k] * bo * t);
+      atomicAdd(gp + cb[k], adj[k] * bo * pa * t * lt);
+      atomicAdd(gp + cr0[k], adj[k] * bo * pa * t * (-pb / r0));
+    }
+  }
 }
 
-__global__ void k_chain_radial(XrWork w) {
+__global__ void k_chain_radial(XrWork w, XrFF ff) {
   const int nm = *w.nmask;
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nm; q += gridDim.x * blockDim.x)
-    k_chain_radial_one(w, w.mlist[q]);
+    k_chain_radial_one(w, ff, w.mlist[q]);
 }
 
 }  // namespace
@@ -1192,6 +1243,6 @@ void xr_launch_bonded(const XrWork& w, const XrFF& ff, cudaStream_t st) {
   if (w.nB > 0) {
     k_chain_bond<<<gM, tb, 0, st>>>(w, ff);
     k_chain_deltap<<<gA, tb, 0, st>>>(w);
-    k_chain_radial<<<gM, tb, 0, st>>>(w);
+    k_chain_radial<<<gM, tb, 0, st>>>(w, ff);
   }
 }

@@ -174,6 +174,10 @@ struct XrWork {
   int* qiters;                // [S] QEq conjugate-gradient iterations of each system
   double* qrhs;               // [A] adjoint QEq right-hand side (-dE/dq), full-derivative forces
   double* qadj;               // [A] adjoint QEq solution lambda (sum lambda = 0 per system)
+  // Force-field parameter gradient dE/dtheta (null unless requested), summed over the batch:
+  // [T*T][XR_NPAIR_COLS] pair-table columns, then [R][7] angle records.
+  double* pgrad;
+  int pgrad_angle_off;
   double* f;                  // [A][3] gradient dE/dx accumulator (forces = -f)
   double* qwork;              // [XR_QW_N][A] QEq solver vectors
   double* red;                // reduction scratch for solvers

@@ -58,6 +58,7 @@ struct xr_ff {
   XrFF d{};
   std::vector<void*> allocs;
   int device = 0;
+  int nangle = 0;
 };
 
 struct xr_ctx {
@@ -107,6 +108,10 @@ struct xr_ctx {
   size_t cqguess = 0;
   double* qrhs = nullptr;
   size_t cqrhs = 0;
+  double* pgrad = nullptr;  // force-field parameter gradient of the last call (when requested)
+  size_t cpgrad = 0;
+  std::vector<double> h_pgrad;
+  long long pgrad_pairs = 0, pgrad_angles = 0;
   double* qadj = nullptr;
   size_t cqadj = 0;
   double* f = nullptr;
@@ -725,6 +730,16 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
   XrWork w;
   fill_work(c, w, A, nsys, flags);
   w.nchunks = (int)chunk_tab.size();
+  c->pgrad_pairs = c->pgrad_angles = 0;
+  if (flags & XR_FLAG_PARAM_GRADIENT) {
+    const long long np = (long long)ff->d.ntypes * ff->d.ntypes * XR_NPAIR_COLS, na = 7ll * ff->nangle;
+    if (!grow(&c->pgrad, &c->cpgrad, (size_t)(np + na + 1))) return cuda_fail(c, cudaErrorMemoryAllocation, "allocation");
+    cudaMemsetAsync(c->pgrad, 0, sizeof(double) * (size_t)(np + na), st);
+    w.pgrad = c->pgrad;
+    w.pgrad_angle_off = (int)np;
+    c->pgrad_pairs = np;
+    c->pgrad_angles = na;
+  }
   attach_lists(c, w);
   stage(c, 0, st);
   xr_launch_topology(w, st);
@@ -847,6 +862,11 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
   if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(c, e, "kernel launch");
   c->launches = launches;
   c->qeq_iterations = c->h_small[6];
+  if (c->pgrad_pairs > 0) {
+    c->h_pgrad.resize((size_t)(c->pgrad_pairs + c->pgrad_angles));
+    cudaMemcpy(c->h_pgrad.data(), c->pgrad, sizeof(double) * c->h_pgrad.size(), cudaMemcpyDeviceToHost);
+    d2h += sizeof(double) * (long long)c->h_pgrad.size();
+  }
   c->last_A = A;
   // keep the scans for export
   c->host_cnt.resize(4 * (size_t)(A + 1));
@@ -915,6 +935,7 @@ int xr_ff_create(const double* general, int ntypes, const double* atom, const do
   if (vdw_type < 1 || vdw_type > 3) return XR_EINPUT;
   xr_ff* f = new xr_ff();
   cudaGetDevice(&f->device);
+  f->nangle = nangle;
   const int T = ntypes;
   XrFF& d = f->d;
   d.ntypes = T;
@@ -1056,7 +1077,7 @@ void xr_ctx_destroy(xr_ctx* c) {
                   c->qwork, c->outbuf, c->edge, c->edge_pair, c->edge_dbslot, c->hval, c->pair_edge, c->pair_i,
                   c->pair_bond, c->p_r, c->p_shield, c->p_dshield, c->p_g, c->p_evdw, c->p_ecoul, c->bond_pair,
                   c->bond_i, c->bond_j, c->b_r, c->b_v, c->b_fwd, c->b_adj, c->b_e, c->dbrow, c->sys, c->energy,
-                  c->props, c->status, c->counts, c->barrier, c->qmap, c->qsmall, c->qiters, c->red, c->qguess, c->qrhs, c->qadj, c->bx_meta, c->bx_bo, c->bx_count,
+                  c->props, c->status, c->counts, c->barrier, c->qmap, c->qsmall, c->qiters, c->red, c->qguess, c->qrhs, c->qadj, c->pgrad, c->bx_meta, c->bx_bo, c->bx_count,
                   c->esum, c->arow, c->nact, c->nzrow, c->nnz, c->chunks, c->sys_chunks, c->chunk_part, c->mids, c->nmids, c->mlist};
   for (void* p : bufs)
     if (p) cudaFree(p);
@@ -1090,6 +1111,14 @@ int xr_eval_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, un
 long long xr_last_launches(const xr_ctx* c) { return c ? c->launches : 0; }
 
 int xr_last_qeq_iterations(const xr_ctx* c) { return c ? c->qeq_iterations : 0; }
+
+int xr_get_param_gradient(const xr_ctx* c, double* pair_grad, long long npair, double* angle_grad, long long nangle) {
+  if (!c || c->pgrad_pairs == 0) return XR_EINPUT;
+  if (npair != c->pgrad_pairs || nangle != c->pgrad_angles || !pair_grad || (nangle > 0 && !angle_grad)) return XR_EINPUT;
+  std::memcpy(pair_grad, c->h_pgrad.data(), sizeof(double) * (size_t)npair);
+  if (nangle > 0) std::memcpy(angle_grad, c->h_pgrad.data() + npair, sizeof(double) * (size_t)nangle);
+  return XR_OK;
+}
 
 int xr_last_qeq_work(const xr_ctx* c, long long* iterations, double* matvec_bytes) {
   if (!c || !iterations || !matvec_bytes) return XR_EINPUT;

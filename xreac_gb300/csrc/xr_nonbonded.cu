@@ -82,6 +82,28 @@ __global__ void k_pairs(XrWork w, XrFF ff) {
   w.p_dshield[p] = dshield;
   w.p_evdw[p] = E;
   w.p_g[p] = G;
+  if (w.pgrad && taper != 0.0) {
+    // dE/d(D, alpha, r_vdW, gamma_w) of this pair's tapered vdW term (and the inner core's)
+    double* gp = w.pgrad + (size_t)pt * XR_NPAIR_COLS;
+    const double m = taper * D * (2 * ev - 2) * ev;  // dE/d(log ev) per unit of the exponent's argument
+    atomicAdd(gp + P_D, taper * (ev * ev - 2 * ev));
+    atomicAdd(gp + P_ALPHA, m * 0.5 * (1 - f13 / rvdw));
+    atomicAdd(gp + P_RVDW, m * 0.5 * alpha * f13 / (rvdw * rvdw));
+    if (ff.vdw_type == 1 || ff.vdw_type == 3) {
+      // f13 = (r^p + gw)^(1/p) with gw = gamma_w^-p: d f13 / d gamma_w = -f13 gw / (sum gamma_w)
+      const double pw = ff.g[28], gw = __ldg(ff.pair_gw + pt);
+      const double sum = exp(pw * log(r)) + gw;
+      const double gamw = pair_prm(ff, pt, P_GAMMA_W);
+      atomicAdd(gp + P_GAMMA_W, m * (-0.5 * alpha / rvdw) * (-f13 * gw / (sum * gamw)));
+    }
+    if (ff.vdw_type == 2 || ff.vdw_type == 3) {
+      const double ecore = pair_prm(ff, pt, P_ECORE), acore = pair_prm(ff, pt, P_ACORE), rcore = pair_prm(ff, pt, P_RCORE);
+      const double ex = exp(acore * (1 - r / rcore));
+      atomicAdd(gp + P_ECORE, taper * ex);
+      atomicAdd(gp + P_ACORE, taper * ecore * ex * (1 - r / rcore));
+      atomicAdd(gp + P_RCORE, taper * ecore * ex * acore * r / (rcore * rcore));
+    }
+  }
 }
 
 __global__ void k_hval(XrWork w) {

@@ -405,6 +405,10 @@ class ForceField:
             ntypes=T,
         )
 
+    def angle_row_keys(self):
+        """``(key, record index)`` of every row of ``tables()["angle"]``, in row order."""
+        return [(key, q) for key, records in self.angles.items() for q in range(len(records))]
+
     def type_indices(self, symbols):
         """Element numbers (file order) of a sequence of labels, as int32."""
         pos = self.__dict__.get("_type_pos")
