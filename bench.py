@@ -21,6 +21,8 @@ One step = one pass of the whole stream through the continuous-batching server
 - ``water_box``: the 4,608-atom periodic water box (1,536 H2O, 35.8 A) evaluated alone with
   device-resident positions, L2 flushed before every step: per-stage times and the roofline of its
   dominant kernel (k_qeq_grid).
+- ``differentiation``: 256 perturbed copies of the TiO2/water slab: reference E+F, then the E+F
+  squared-error loss and its force-field parameter gradient (device adjoint) per copy.
 - ``cpu_baseline``: the CPU oracle (the reference's algorithm restated) on a sample of the stream.
 
 ``--impl reference`` times the CPU oracle on samples of the same stream with every host thread and
@@ -387,6 +389,40 @@ def water_box_numbers(lib, nat, local, steps, warmup):
     }
 
 
+def differentiation_numbers(local, copies=256):
+    """The differentiation workload: per perturbed copy, the unperturbed reference (E, F), then the
+    E+F squared-error loss and its parameter gradient (three adjoint evaluations)."""
+    import torch
+    from xreac_gb300 import Calculator, ForceField, workloads
+    from xreac_gb300.differentiation import energy_force_loss
+
+    ref_calc = Calculator(ForceField.bundled("ffield.reax.TiOH.Kim2013"), device=local)
+    gen = workloads.perturbed_copies(n_copies=copies)
+    first = next(gen)
+    ref = ref_calc.evaluate(first[0].symbols, first[0].positions, cell=first[0].cell, pbc=first[0].pbc)
+    energy_force_loss(Calculator(first[1], device=local), first[0].symbols, first[0].positions, ref.energy,
+                      ref.forces, cell=first[0].cell, pbc=first[0].pbc)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    n = 0
+    losses = []
+    for system, ff in workloads.perturbed_copies(n_copies=copies):
+        ref = ref_calc.evaluate(system.symbols, system.positions, cell=system.cell, pbc=system.pbc)
+        loss, grad, _ = energy_force_loss(Calculator(ff, device=local), system.symbols, system.positions, ref.energy,
+                                          ref.forces, cell=system.cell, pbc=system.pbc)
+        losses.append(loss)
+        n += 1
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    return {"workload": f"{copies} perturbed copies of the anatase TiO2 4x4x1 slab + 32 H2O (288 atoms), "
+                        "ffield.reax.TiOH.Kim2013, +-2% bond/angle/vdW parameters, 0.05 A displacements",
+            "copies": n, "seconds": wall, "ms_per_copy": 1e3 * wall / n,
+            "evaluations_per_copy": 4, "atoms_evals_per_s": 4 * 288 * n / wall,
+            "mean_loss": float(np.mean(losses)),
+            "note": "per copy: force-field upload, reference E+F, loss gradient by the device adjoint plus a "
+                    "positional central difference of it (force term)"}
+
+
 STAGE_NAMES = ["neighbour_count_scan", "neighbour_fill_reverse", "pairs_vdw_shield", "qeq_cg", "coulomb",
                "bonded_and_adjoint", "forces_reduce_pack"]
 
@@ -516,6 +552,7 @@ def main():
         "gpu_launches": int(sum(b.launches for b in batches)),
     }
     line["water_box"] = water_box_numbers(lib, nat, local, max(3, min(args.steps * 4, 20)), args.warmup)
+    line["differentiation"] = differentiation_numbers(local)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cores = os.cpu_count() or 1
         torch.set_num_threads(cores)

@@ -259,6 +259,47 @@ def anatase_slab_water(nx=4, ny=4, a=3.785, c=9.514, u=0.2081, gap=15.0, n_water
     return System(symbols, x, np.diag([lx, ly, lz]), True, 0.0, "ffield.reax.TiOH.Kim2013")
 
 
+# The parameter groups the differentiation workload perturbs and differentiates: bond (bond energy,
+# bond order, over-coordination weight), vdW, and valence-angle records.
+BOND_PARAMETERS = ("De_s", "De_p", "De_pp", "p_be1", "p_be2", "p_ovun1", "p_bo1", "p_bo2", "p_bo3", "p_bo4", "p_bo5",
+                   "p_bo6")
+VDW_PARAMETERS = ("D", "alpha", "gamma_w", "r_vdW")
+
+
+def perturbed_copies(n_copies=256, seed=5, displacement=0.05, relative=0.02):
+    """The differentiation workload: ``n_copies`` copies of the anatase slab with water, each with
+    seeded Gaussian displacements of ``displacement`` A and its own uniform +-``relative``
+    perturbation of every bond, vdW and angle parameter of ffield.reax.TiOH.Kim2013.
+
+    Yields ``(System, perturbed ForceField)``; the unperturbed force field is the reference.
+    """
+    import copy
+
+    from .forcefield import ForceField
+
+    base = anatase_slab_water()
+    ff0 = ForceField.bundled(base.force_field)
+    rng = np.random.default_rng(seed)
+    for _ in range(n_copies):
+        x = base.positions + rng.normal(0.0, displacement, base.positions.shape)
+        ff = copy.deepcopy(ff0)
+        seen = set()
+        for key, prm in ff.pairs.items():
+            if id(prm) in seen:
+                continue
+            seen.add(id(prm))
+            for name in BOND_PARAMETERS + VDW_PARAMETERS:
+                if name in prm and prm[name] != 0:
+                    prm[name] *= 1.0 + rng.uniform(-relative, relative)
+        for records in ff.angles.values():
+            for rec in records:
+                if id(rec) in seen:
+                    continue
+                seen.add(id(rec))
+                rec *= 1.0 + rng.uniform(-relative, relative, rec.shape)
+        yield System(list(base.symbols), x, base.cell.copy(), True, 0.0, base.force_field), ff
+
+
 def hydrogen_peroxide():
     """H2O2 (O-O 1.475 A, O-H 0.95 A, O-O-H 94.8 deg, H-O-O-H dihedral 111.5 deg)."""
     th, ph = np.deg2rad(94.8), np.deg2rad(111.5)
