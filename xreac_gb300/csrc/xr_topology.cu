@@ -54,19 +54,38 @@ __device__ inline double exact_d2(const double v[3]) {
   return __dadd_rn(__dadd_rn(__dmul_rn(v[0], v[0]), __dmul_rn(v[1], v[1])), __dmul_rn(v[2], v[2]));
 }
 
+// The FP32 screening constants of a system, held in registers for the candidate loop (the loop's
+// status atomics would otherwise force the compiler to re-read them from global memory).
+struct ScreenConsts {
+  float cellf[9];
+  float margin, rc2f, bc2f, hc2f;
+};
+
+__device__ inline ScreenConsts screen_consts(const XrSystem& S) {
+  ScreenConsts c;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) c.cellf[k] = S.cellf[k];
+  c.margin = S.margin;
+  c.rc2f = S.rc2f;
+  c.bc2f = S.bc2f;
+  c.hc2f = S.hc2f;
+  return c;
+}
+
 // Classify one candidate image. Returns 0 (no edge) or kHitBit | code.
-__device__ inline int classify(const XrWork& w, const XrSystem& S, int i, int j, const float4& pi, const float4& pj,
-                               const int4& wi, const int4& wj, int s0, int s1, int s2, const double4_32a& xi) {
-  const float vx = pj.x - pi.x + ((float)s0 * S.cellf[0] + (float)s1 * S.cellf[3] + (float)s2 * S.cellf[6]);
-  const float vy = pj.y - pi.y + ((float)s0 * S.cellf[1] + (float)s1 * S.cellf[4] + (float)s2 * S.cellf[7]);
-  const float vz = pj.z - pi.z + ((float)s0 * S.cellf[2] + (float)s1 * S.cellf[5] + (float)s2 * S.cellf[8]);
+__device__ inline int classify(const XrWork& w, const XrSystem& S, const ScreenConsts& K, int i, int j, const float4& pi,
+                               const float4& pj, const int4& wi, const int4& wj, int s0, int s1, int s2,
+                               const double4_32a& xi) {
+  const float vx = pj.x - pi.x + ((float)s0 * K.cellf[0] + (float)s1 * K.cellf[3] + (float)s2 * K.cellf[6]);
+  const float vy = pj.y - pi.y + ((float)s0 * K.cellf[1] + (float)s1 * K.cellf[4] + (float)s2 * K.cellf[7]);
+  const float vz = pj.z - pi.z + ((float)s0 * K.cellf[2] + (float)s1 * K.cellf[5] + (float)s2 * K.cellf[8]);
   const float r2 = vx * vx + vy * vy + vz * vz;
-  const float mg = S.margin;
-  const float rc2f = S.rc2f;
+  const float mg = K.margin;
+  const float rc2f = K.rc2f;
   if (r2 > rc2f + mg) return 0;
   const int sx = s0 - wj.x + wi.x, sy = s1 - wj.y + wi.y, sz = s2 - wj.z + wi.z;
   if (j == i && sx == 0 && sy == 0 && sz == 0) return 0;
-  const float bc2f = S.bc2f, hc2f = S.hc2f;
+  const float bc2f = K.bc2f, hc2f = K.hc2f;
   bool bond, hb;
   const bool exact = (r2 >= rc2f - mg) || (fabsf(r2 - bc2f) <= mg) || (fabsf(r2 - hc2f) <= mg) || (r2 < 1.0e-2f);
   if (exact) {
@@ -124,21 +143,24 @@ __global__ void k_neighbors(XrWork w) {
     bd = w.cnt[3 * L + i];
   }
   const int r0 = S.reach[0], r1 = S.reach[1], r2 = S.reach[2];
-  for (int jb = 0; jb < S.natoms; jb += 32) {
+  const ScreenConsts K = screen_consts(S);
+  const int natoms = S.natoms, atom_off = S.atom_off;
+  const bool per0 = S.periodic[0] != 0, per1 = S.periodic[1] != 0, per2 = S.periodic[2] != 0;
+  for (int jb = 0; jb < natoms; jb += 32) {
     const int jl = jb + lane;
-    const bool valid = jl < S.natoms;
-    const int j = S.atom_off + (valid ? jl : 0);
+    const bool valid = jl < natoms;
+    const int j = atom_off + (valid ? jl : 0);
     const float4 pj = w.xw[j], fj = w.fw[j];
     const int4 wj = w.wrap[j];
-    const int b0 = S.periodic[0] ? -__float2int_rn(fj.x - fi.x) : 0;
-    const int b1 = S.periodic[1] ? -__float2int_rn(fj.y - fi.y) : 0;
-    const int b2 = S.periodic[2] ? -__float2int_rn(fj.z - fi.z) : 0;
+    const int b0 = per0 ? -__float2int_rn(fj.x - fi.x) : 0;
+    const int b1 = per1 ? -__float2int_rn(fj.y - fi.y) : 0;
+    const int b2 = per2 ? -__float2int_rn(fj.z - fi.z) : 0;
     int c_e = 0, c_h = 0, c_bh = 0, c_ba = 0;
     if (valid) {
       for (int o0 = -r0; o0 <= r0; ++o0)
         for (int o1 = -r1; o1 <= r1; ++o1)
           for (int o2 = -r2; o2 <= r2; ++o2) {
-            const int code = classify(w, S, i, j, pi, pj, wi, wj, b0 + o0, b1 + o1, b2 + o2, xi);
+            const int code = classify(w, S, K, i, j, pi, pj, wi, wj, b0 + o0, b1 + o1, b2 + o2, xi);
             if (code) {
               ++c_e;
               const bool half = code & XR_CODE_HALF, bond = code & XR_CODE_BOND;
@@ -158,7 +180,7 @@ __global__ void k_neighbors(XrWork w) {
       for (int o0 = -r0; o0 <= r0; ++o0)
         for (int o1 = -r1; o1 <= r1; ++o1)
           for (int o2 = -r2; o2 <= r2; ++o2) {
-            const int code = classify(w, S, i, j, pi, pj, wi, wj, b0 + o0, b1 + o1, b2 + o2, xi);
+            const int code = classify(w, S, K, i, j, pi, pj, wi, wj, b0 + o0, b1 + o1, b2 + o2, xi);
             if (!code) continue;
             const uint32_t c = (uint32_t)code & ~(uint32_t)kHitBit;
             const bool half = c & XR_CODE_HALF, bond = c & XR_CODE_BOND;
