@@ -189,9 +189,33 @@ struct xr_ctx {
   int* bx_count = nullptr;
   std::vector<int4> h_bx_meta;
   std::vector<double> h_bx_bo;
-  // pinned host staging
+  // pinned host staging (every host<->device copy of a call is asynchronous from/to these)
   double4_32a* h_x = nullptr;
   size_t ch_x = 0;
+  int* h_types = nullptr;
+  size_t ch_types = 0;
+  int* h_sysof = nullptr;
+  size_t ch_sysof = 0;
+  XrSystem* h_sysd = nullptr;
+  size_t ch_sysd = 0;
+  int4* h_chunks = nullptr;
+  size_t ch_chunks = 0;
+  int2* h_syschunks = nullptr;
+  size_t ch_syschunks = 0;
+  int4* h_qmap_p = nullptr;
+  size_t ch_qmap_p = 0;
+  int* h_qsmall_p = nullptr;
+  size_t ch_qsmall_p = 0;
+  int* h_cnt = nullptr;  // [4][A+1] scans of the last evaluation
+  size_t ch_cnt = 0;
+  int4* h_bxm = nullptr;
+  size_t ch_bxm = 0;
+  double* h_bxb = nullptr;
+  size_t ch_bxb = 0;
+  int* h_qit = nullptr;
+  size_t ch_qit = 0;
+  double* h_pg = nullptr;
+  size_t ch_pg = 0;
   double* h_out = nullptr;
   size_t ch_out = 0;
   double* h_guess = nullptr;
@@ -639,7 +663,12 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
       !host_grow(&c->h_out, &c->ch_out, 8 * (size_t)A + 32 * (size_t)nsys + 8))
     return cuda_fail(c, cudaErrorMemoryAllocation, "allocation");
   c->host_sys.resize(nsys);
-  std::vector<int> types(A), sys_of(A);
+  if (!host_grow(&c->h_types, &c->ch_types, (size_t)A) || !host_grow(&c->h_sysof, &c->ch_sysof, (size_t)A) ||
+      !host_grow(&c->h_sysd, &c->ch_sysd, (size_t)nsys) || !host_grow(&c->h_qit, &c->ch_qit, (size_t)nsys) ||
+      !host_grow(&c->h_cnt, &c->ch_cnt, 4 * (size_t)(A + 1)))
+    return cuda_fail(c, cudaErrorMemoryAllocation, "allocation");
+  int* types = c->h_types;
+  int* sys_of = c->h_sysof;
   bool any_guess = false;
   int off = 0;
   for (int s = 0; s < nsys; ++s) {
@@ -689,18 +718,24 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
     }
     off += in.natoms;
   }
-  std::vector<int4> chunk_tab;
-  std::vector<int2> sys_chunk_tab(nsys);
-  for (int s = 0, a = 0; s < nsys; ++s) {
-    sys_chunk_tab[s].x = (int)chunk_tab.size();
-    for (int b = 0; b < sys[s].natoms; b += XR_CHUNK_ATOMS)
-      chunk_tab.push_back(make_int4(s, a + b, a + std::min(sys[s].natoms, b + XR_CHUNK_ATOMS), 0));
-    sys_chunk_tab[s].y = (int)chunk_tab.size();
-    a += sys[s].natoms;
-  }
-  if (!grow(&c->chunks, &c->cchunks, chunk_tab.size()) ||
-      !grow(&c->chunk_part, &c->cchunk_part, chunk_tab.size() * (size_t)XR_PART_N))
+  size_t nchunk = 0;
+  for (int s = 0; s < nsys; ++s) nchunk += (size_t)(sys[s].natoms + XR_CHUNK_ATOMS - 1) / XR_CHUNK_ATOMS;
+  if (!host_grow(&c->h_chunks, &c->ch_chunks, nchunk) || !host_grow(&c->h_syschunks, &c->ch_syschunks, (size_t)nsys) ||
+      !grow(&c->chunks, &c->cchunks, nchunk) || !grow(&c->chunk_part, &c->cchunk_part, nchunk * (size_t)XR_PART_N))
     return cuda_fail(c, cudaErrorMemoryAllocation, "allocation");
+  int4* chunk_tab = c->h_chunks;
+  int2* sys_chunk_tab = c->h_syschunks;
+  {
+    int k = 0;
+    for (int s = 0, a = 0; s < nsys; ++s) {
+      sys_chunk_tab[s].x = k;
+      for (int b = 0; b < sys[s].natoms; b += XR_CHUNK_ATOMS)
+        chunk_tab[k++] = make_int4(s, a + b, a + std::min(sys[s].natoms, b + XR_CHUNK_ATOMS), 0);
+      sys_chunk_tab[s].y = k;
+      a += sys[s].natoms;
+    }
+  }
+  std::memcpy(c->h_sysd, c->host_sys.data(), sizeof(XrSystem) * nsys);
   cudaStream_t st = c->stream;
   long long launches = 0;
   long long h2d = 0, d2h = 0;
@@ -716,20 +751,20 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
     cudaMemcpyAsync(c->qguess, c->h_guess, sizeof(double) * A, cudaMemcpyHostToDevice, st);
     h2d += sizeof(double) * (long long)A;
   }
-  cudaMemcpyAsync(c->type, types.data(), sizeof(int) * A, cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(c->sys_of, sys_of.data(), sizeof(int) * A, cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(c->sys, c->host_sys.data(), sizeof(XrSystem) * nsys, cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(c->chunks, chunk_tab.data(), sizeof(int4) * chunk_tab.size(), cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(c->sys_chunks, sys_chunk_tab.data(), sizeof(int2) * nsys, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(c->type, types, sizeof(int) * A, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(c->sys_of, sys_of, sizeof(int) * A, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(c->sys, c->h_sysd, sizeof(XrSystem) * nsys, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(c->chunks, chunk_tab, sizeof(int4) * nchunk, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(c->sys_chunks, sys_chunk_tab, sizeof(int2) * nsys, cudaMemcpyHostToDevice, st);
   h2d += 2 * sizeof(int) * (long long)A + sizeof(XrSystem) * (long long)nsys +
-         (long long)(sizeof(int4) * chunk_tab.size() + sizeof(int2) * nsys);
+         (long long)(sizeof(int4) * nchunk + sizeof(int2) * nsys);
   cudaMemsetAsync(c->status, 0, sizeof(int), st);
   cudaMemsetAsync(c->counts, 0, 8 * sizeof(int), st);
   cudaMemsetAsync(c->qiters, 0, sizeof(int) * nsys, st);
   cudaMemsetAsync(c->cnt, 0, sizeof(int) * 4 * (size_t)(A + 1), st);
   XrWork w;
   fill_work(c, w, A, nsys, flags);
-  w.nchunks = (int)chunk_tab.size();
+  w.nchunks = (int)nchunk;
   c->pgrad_pairs = c->pgrad_angles = 0;
   if (flags & XR_FLAG_PARAM_GRADIENT) {
     const long long np = (long long)ff->d.ntypes * ff->d.ntypes * XR_NPAIR_COLS, na = 7ll * ff->nangle;
@@ -772,8 +807,17 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
   int qblocks = 0, qteam = 0, qsmall = 0;
   if (c->coop_per_sm > 0) {
     plan_qeq(c, sys, nsys, &qblocks, &qteam, &qsmall);
-    if (qteam > 0) cudaMemcpyAsync(c->qmap, c->h_qmap.data(), sizeof(int4) * qteam, cudaMemcpyHostToDevice, st);
-    if (qsmall > 0) cudaMemcpyAsync(c->qsmall, c->h_qsmall.data(), sizeof(int) * qsmall, cudaMemcpyHostToDevice, st);
+    if (!host_grow(&c->h_qmap_p, &c->ch_qmap_p, (size_t)std::max(qteam, 1)) ||
+        !host_grow(&c->h_qsmall_p, &c->ch_qsmall_p, (size_t)std::max(qsmall, 1)))
+      return cuda_fail(c, cudaErrorMemoryAllocation, "allocation");
+    if (qteam > 0) {
+      std::memcpy(c->h_qmap_p, c->h_qmap.data(), sizeof(int4) * qteam);
+      cudaMemcpyAsync(c->qmap, c->h_qmap_p, sizeof(int4) * qteam, cudaMemcpyHostToDevice, st);
+    }
+    if (qsmall > 0) {
+      std::memcpy(c->h_qsmall_p, c->h_qsmall.data(), sizeof(int) * qsmall);
+      cudaMemcpyAsync(c->qsmall, c->h_qsmall_p, sizeof(int) * qsmall, cudaMemcpyHostToDevice, st);
+    }
     h2d += sizeof(int4) * (long long)qteam + sizeof(int) * (long long)qsmall;
   }
   if (int le = xr_launch_qeq(w, ff->d, st, qblocks, c->qmap, qteam, c->qsmall, qsmall))
@@ -807,9 +851,25 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
   }
   cudaMemcpyAsync(c->h_small + 5, c->bx_count, sizeof(int), cudaMemcpyDeviceToHost, st);
   cudaMemcpyAsync(c->h_small + 6, c->counts + 4, sizeof(int), cudaMemcpyDeviceToHost, st);
-  c->h_qiters.resize(nsys);
-  cudaMemcpyAsync(c->h_qiters.data(), c->qiters, sizeof(int) * nsys, cudaMemcpyDeviceToHost, st);
+  cudaMemcpyAsync(c->h_qit, c->qiters, sizeof(int) * nsys, cudaMemcpyDeviceToHost, st);
   d2h += sizeof(int) * (long long)nsys;
+  // bond export (the nonzero bonds are a prefix of at most nB entries), the scans and the parameter
+  // gradient come back in the same stream, so the call synchronises once more only at its end
+  if (!host_grow(&c->h_bxm, &c->ch_bxm, (size_t)std::max(nB, 1)) || !host_grow(&c->h_bxb, &c->ch_bxb, (size_t)std::max(nB, 1)))
+    return cuda_fail(c, cudaErrorMemoryAllocation, "allocation");
+  if (nB > 0) {
+    cudaMemcpyAsync(c->h_bxm, c->bx_meta, sizeof(int4) * nB, cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(c->h_bxb, c->bx_bo, sizeof(double) * nB, cudaMemcpyDeviceToHost, st);
+  }
+  cudaMemcpyAsync(c->h_cnt, c->cnt, sizeof(int) * 4 * (size_t)(A + 1), cudaMemcpyDeviceToHost, st);
+  d2h += sizeof(int) * 4 * (long long)(A + 1);
+  if (c->pgrad_pairs > 0) {
+    if (!host_grow(&c->h_pg, &c->ch_pg, (size_t)(c->pgrad_pairs + c->pgrad_angles)))
+      return cuda_fail(c, cudaErrorMemoryAllocation, "allocation");
+    cudaMemcpyAsync(c->h_pg, c->pgrad, sizeof(double) * (size_t)(c->pgrad_pairs + c->pgrad_angles),
+                    cudaMemcpyDeviceToHost, st);
+    d2h += sizeof(double) * (c->pgrad_pairs + c->pgrad_angles);
+  }
   d2h += 3 * sizeof(int);
   if (dev_io) {
     const xr_result& r = out[0];
@@ -839,39 +899,26 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
   }
   {
     const int nx = c->h_small[5];
+    d2h += (sizeof(int4) + sizeof(double)) * (long long)nB;
+    // exported in arrival order; sorted by bond id (system, then pair order) for the exporters
+    std::vector<int> order(nx);
+    for (int k = 0; k < nx; ++k) order[k] = k;
+    std::sort(order.begin(), order.end(), [&](int a, int b) { return c->h_bxm[a].x < c->h_bxm[b].x; });
     c->h_bx_meta.resize(nx);
     c->h_bx_bo.resize(nx);
-    d2h += (sizeof(int4) + sizeof(double)) * (long long)nx;
-    if (nx > 0) {
-      cudaMemcpy(c->h_bx_meta.data(), c->bx_meta, sizeof(int4) * nx, cudaMemcpyDeviceToHost);
-      cudaMemcpy(c->h_bx_bo.data(), c->bx_bo, sizeof(double) * nx, cudaMemcpyDeviceToHost);
-      d2h += (long long)(sizeof(int4) + sizeof(double)) * nx;
-      std::vector<int> order(nx);
-      for (int k = 0; k < nx; ++k) order[k] = k;
-      std::sort(order.begin(), order.end(), [&](int a, int b) { return c->h_bx_meta[a].x < c->h_bx_meta[b].x; });
-      std::vector<int4> m2(nx);
-      std::vector<double> b2(nx);
-      for (int k = 0; k < nx; ++k) {
-        m2[k] = c->h_bx_meta[order[k]];
-        b2[k] = c->h_bx_bo[order[k]];
-      }
-      c->h_bx_meta.swap(m2);
-      c->h_bx_bo.swap(b2);
+    for (int k = 0; k < nx; ++k) {
+      c->h_bx_meta[k] = c->h_bxm[order[k]];
+      c->h_bx_bo[k] = c->h_bxb[order[k]];
     }
   }
+  c->h_qiters.assign(c->h_qit, c->h_qit + nsys);
   if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(c, e, "kernel launch");
   c->launches = launches;
   c->qeq_iterations = c->h_small[6];
-  if (c->pgrad_pairs > 0) {
-    c->h_pgrad.resize((size_t)(c->pgrad_pairs + c->pgrad_angles));
-    cudaMemcpy(c->h_pgrad.data(), c->pgrad, sizeof(double) * c->h_pgrad.size(), cudaMemcpyDeviceToHost);
-    d2h += sizeof(double) * (long long)c->h_pgrad.size();
-  }
+  if (c->pgrad_pairs > 0) c->h_pgrad.assign(c->h_pg, c->h_pg + (c->pgrad_pairs + c->pgrad_angles));
   c->last_A = A;
   // keep the scans for export
-  c->host_cnt.resize(4 * (size_t)(A + 1));
-  cudaMemcpy(c->host_cnt.data(), c->cnt, sizeof(int) * 4 * (size_t)(A + 1), cudaMemcpyDeviceToHost);
-  d2h += sizeof(int) * 4 * (long long)(A + 1);
+  c->host_cnt.assign(c->h_cnt, c->h_cnt + 4 * (size_t)(A + 1));
   c->h2d_bytes = h2d;
   c->d2h_bytes = d2h;
   if (int code = status_to_code(c, c->h_small[4])) return code;
@@ -1084,6 +1131,10 @@ void xr_ctx_destroy(xr_ctx* c) {
   if (c->h_x) cudaFreeHost(c->h_x);
   if (c->h_out) cudaFreeHost(c->h_out);
   if (c->h_guess) cudaFreeHost(c->h_guess);
+  for (void* hp : {(void*)c->h_types, (void*)c->h_sysof, (void*)c->h_sysd, (void*)c->h_chunks, (void*)c->h_syschunks,
+                   (void*)c->h_qmap_p, (void*)c->h_qsmall_p, (void*)c->h_cnt, (void*)c->h_bxm, (void*)c->h_bxb,
+                   (void*)c->h_qit, (void*)c->h_pg})
+    if (hp) cudaFreeHost(hp);
   if (c->h_small) cudaFreeHost(c->h_small);
   for (int k = 0; k <= xr_ctx::kStages; ++k)
     if (c->ev[k]) cudaEventDestroy(c->ev[k]);

@@ -10,6 +10,8 @@
 //   needs no atomics and is deterministic.
 // - A single large system runs the solver as one cooperative grid with a barrier whose every wait
 //   is bounded; batches of systems give each system one thread block.
+#include <type_traits>
+
 #include "xr_common.cuh"
 
 namespace {
@@ -293,7 +295,7 @@ struct QeqRows {
 struct QeqShared {
   double red[kRedSmem];
   double sc_lam, sc_alpha, sc_step, sc_beta;
-  float sf_lam, sf_alpha, sf_step, sf_beta;
+  float sf_lam, sf_alpha, sf_step, sf_beta, sf_gz;
   int sc_state;  // 0 iterate, 1 converged, 2 stop
   union {
     double d[32][33];
@@ -550,6 +552,121 @@ __device__ int qeq_cg(const XrWork& w, const XrFF& ff, const Team& team, QeqShar
   return it;
 }
 
+// Sum of two floats over the block (every thread passes its values; the block total reaches thread 0,
+// which runs post() on it; everyone waits for post()).
+template <class Post>
+__device__ inline void block_sum2(float a, float b, float* smem, Post post) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  a = warp_total_t<float>(a);
+  b = warp_total_t<float>(b);
+  if (lane == 0) {
+    smem[wid] = a;
+    smem[32 + wid] = b;
+  }
+  __syncthreads();
+  if (wid == 0) {
+    float x = lane < nw ? smem[lane] : 0.0f, y = lane < nw ? smem[32 + lane] : 0.0f;
+    x = warp_total_t<float>(x);
+    y = warp_total_t<float>(y);
+    if (lane == 0) post(x, y);
+  }
+  __syncthreads();
+}
+
+// The FP32 solve of a refinement sweep for a system of at most 1024 atoms solved by one block: every
+// row's state (g, p, Hp, y, D^-1, eta D^-1, c, H'g) in shared memory, a warp per row for the product
+// (FP32 shuffles cost little), one thread per row for the updates and FP32 iteration scalars. Same
+// projected PCG as qeq_cg; about three block barriers per iteration instead of three per 32-row tile.
+// The correction y is written to y_out (global, indexed by atom).
+__device__ int qeq_cg_block32(const XrWork& w, const XrFF& ff, QeqShared& sh, int a0, int n, float* rows,
+                              const QeqMatrix<float>& M, float* y_out, double s1d, double gz_start, double stop,
+                              int max_it) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5, tid = threadIdx.x;
+  float *g = rows, *p = rows + n, *hp = rows + 2 * n, *y = rows + 3 * n, *di = rows + 4 * n, *etadi = rows + 5 * n,
+        *cr = rows + 6 * n, *hz = rows + 7 * n;
+  const double* DI = &QW(Q_DINV, 0);
+  const double* Cr = &QW(Q_C, 0);
+  const double* G = &QW(Q_G, 0);
+  float* red = reinterpret_cast<float*>(sh.red);
+  for (int i = tid; i < n; i += blockDim.x) {
+    const int a = a0 + i;
+    g[i] = float(G[a]);
+    p[i] = 0.0f;
+    hp[i] = 0.0f;
+    y[i] = 0.0f;
+    di[i] = float(DI[a]);
+    etadi[i] = float(atom_prm(ff, w.type[a], A_ETA) * DI[a]);
+    cr[i] = float(Cr[a]);
+  }
+  const float s1 = float(s1d);
+  if (tid == 0) {
+    sh.sf_lam = 0.0f;
+    sh.sf_beta = 0.0f;
+    sh.sf_gz = float(gz_start);
+    sh.sc_state = (!(gz_start > 0.0) || n < 2 || gz_start <= stop) ? 1 : 0;
+  }
+  __syncthreads();
+  const float fstop = float(stop);
+  int it = 0;
+  while (sh.sc_state == 0) {
+    if (++it > max_it) {
+      --it;
+      break;
+    }
+    const float lam = sh.sf_lam, beta = sh.sf_beta;
+    for (int i = wid; i < n; i += nw) {  // H'g over the cached rows, a warp per row
+      float s = 0.0f;
+      for (int e = w.cnt[a0 + i] + lane; e < w.cnt[a0 + i + 1]; e += 32) s += M.cache_h[e - M.ebeg] * g[M.cache_j[e - M.ebeg]];
+      s = warp_total_t<float>(s);
+      if (lane == 0) hz[i] = s;
+    }
+    __syncthreads();
+    float php0 = 0.0f, php1 = 0.0f;
+    for (int i = tid; i < n; i += blockDim.x) {
+      const float ga = g[i];
+      const float h = hz[i] + etadi[i] * ga - lam * cr[i];
+      const float z = di[i] * (ga - lam);
+      const float pv = -z + beta * p[i];
+      const float hpv = -h + beta * hp[i];
+      p[i] = pv;
+      hp[i] = hpv;
+      g[i] = ga - lam;
+      php0 += pv * hpv;
+      php1 += di[i] * hpv;
+    }
+    block_sum2(php0, php1, red, [&](float t0, float t1) {
+      const float gz = sh.sf_gz;
+      if (!(fabsf(t0) > 0.0f) || !isfinite(t0)) {
+        sh.sc_state = 2;  // breakdown: the FP64 residual of the sweep decides what follows
+      } else {
+        sh.sf_alpha = gz / t0;
+        sh.sf_step = sh.sf_alpha * t1 / s1;
+      }
+    });
+    if (sh.sc_state != 0) break;
+    const float alpha = sh.sf_alpha, step = sh.sf_step;
+    float u0 = 0.0f, u1 = 0.0f;
+    for (int i = tid; i < n; i += blockDim.x) {
+      const float gn = (g[i] + alpha * hp[i]) - step;
+      y[i] += alpha * p[i];
+      g[i] = gn;
+      u0 += di[i] * gn;
+      u1 += di[i] * gn * gn;
+    }
+    block_sum2(u0, u1, red, [&](float t0, float t1) {
+      const float lamn = t0 / s1;
+      const float gzn = t1 - lamn * t0;
+      sh.sf_lam = lamn;
+      sh.sf_beta = gzn / sh.sf_gz;
+      sh.sf_gz = gzn;
+      if (gzn <= fstop) sh.sc_state = 1;
+    });
+  }
+  for (int i = tid; i < n; i += blockDim.x) y_out[a0 + i] = y[i];
+  __syncthreads();
+  return it;
+}
+
 // FP64 gradient of the QEq energy at the current charges X for the owned rows, projected onto
 // sum q = Q: g = H x + chi, lambda = <D^-1, g> / <D^-1, 1>, G = g - lambda, and its norm
 // <D^-1, G^2> (from the projected values, so free of cancellation). Two team reductions.
@@ -627,10 +744,15 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
   // Shared-memory plan: [gradient stage: n doubles when it takes at most half the space][row cache].
   // The cache holds FP32 values + 16-bit columns (6 B per entry, mixed precision) when the block's
   // rows fit, else FP64 values + columns (10 B), else nothing (rows read from global memory).
-  const int stage_n = (dyn != nullptr && n * 8 <= dyn_bytes / 2) ? n : 0;
+  // A block that solves a system of at most 1024 atoms alone keeps every row's FP32 state in shared
+  // memory instead (8 vectors, 32 B per atom; the space doubles as the FP64 stage of a fallback).
+  constexpr bool kBlock = std::is_same<Team, BlockTeam>::value;
+  const bool small_rows = kBlock && dyn != nullptr && n <= 1024;
+  const int stage_n = (dyn != nullptr && (small_rows || n * 8 <= dyn_bytes / 2)) ? n : 0;
+  const size_t stage_bytes = small_rows ? 32 * (size_t)n : 8 * (size_t)stage_n;
   void* gstage = stage_n > 0 ? dyn : nullptr;
-  unsigned char* region = dyn != nullptr ? dyn + 8 * (size_t)stage_n : nullptr;
-  const long long region_bytes = dyn != nullptr ? dyn_bytes - 8ll * stage_n : 0;
+  unsigned char* region = dyn != nullptr ? dyn + stage_bytes : nullptr;
+  const long long region_bytes = dyn != nullptr ? dyn_bytes - (long long)stage_bytes : 0;
   const bool cols16 = n <= 65536;
   const bool mixed = region != nullptr && cols16 && nent <= region_bytes / 6;
   const bool cached64 = !mixed && region != nullptr && cols16 && nent <= region_bytes / 10;
@@ -750,7 +872,9 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
       // the correction's own projected norm starts at gz; 1e-10 of it (1e-5 in norm) per sweep,
       // and no further than a hundredth of the final target
       const double stop = fmax(1e-10 * gz, 0.01 * target);
-      const int it = qeq_cg<Team, float>(w, ff, team, sh, a0, n, r0, r1, v32, M32, s1, gz, stop, 0.0, 400, false, slot);
+      const int it = small_rows
+                         ? qeq_cg_block32(w, ff, sh, a0, n, reinterpret_cast<float*>(dyn), M32, v32.y, s1, gz, stop, 400)
+                         : qeq_cg<Team, float>(w, ff, team, sh, a0, n, r0, r1, v32, M32, s1, gz, stop, 0.0, 400, false, slot);
       if (it < 0) return;
       iters += it;
       // x += y, then restore sum x = Q exactly: the FP32 step keeps sum y = 0 only to FP32 rounding,
