@@ -10,6 +10,7 @@ CUDA library (include/xreac_gb300.h); there is no CPU path.
 
 from __future__ import annotations
 
+import math
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -33,6 +34,13 @@ COMPONENTS = (
     "electric_field",
     "qeq",
 )
+
+_NO_PBC = np.zeros(3, dtype=bool)
+_NO_PBC.flags.writeable = False
+_SYSTEM_DTYPE = np.dtype(nat.System)
+_RESULT_DTYPE = np.dtype(nat.Result)
+_SYSTEM_P = nat.POINTER(nat.System)
+_RESULT_P = nat.POINTER(nat.Result)
 
 _ERRORS = {
     nat.XR_ECOINCIDENT: "Coincident atoms are not supported",
@@ -158,6 +166,13 @@ class Calculator:
         self._lib = nat.load()
         self._type_pos = {s: k for k, s in enumerate(force_field.elements) if isinstance(s, str) and s}
         self._angle_rows = force_field.angle_row_keys()
+        # When every labelled element passes the model checks together, so does every subset of them
+        # (the checks are per element and per pair), and requests need no per-call check.
+        try:
+            force_field.validate_model(tuple(self._type_pos))
+            self._all_valid = True
+        except (ValueError, KeyError):
+            self._all_valid = False
 
     def set_qeq(self, tolerance=1e-13, max_iterations=2000):
         """QEq solver tolerance and iteration limit.
@@ -184,7 +199,12 @@ class Calculator:
             raise RuntimeError(self._ctx.last_error())
 
     def _prepare(self, symbols, positions, total_charge, cell, pbc, full_derivative):
-        if not isinstance(full_derivative, bool):
+        """Validated ``(symbols, positions, types, pbc flags, cell or None, repetitions)``.
+
+        The positions are float64 and C-contiguous, but not copied when they already are, and not
+        yet checked for finite values: ``_run`` checks the whole batch at once.
+        """
+        if full_derivative is not True and full_derivative is not False:
             raise ValueError("full_derivative must be a boolean")
         ff = self.force_field
         symbols = tuple(symbols)
@@ -199,15 +219,21 @@ class Calculator:
             ff.validate_model(symbols)
             types = ff.type_indices(symbols)
         else:
-            validate_total_charge(total_charge)
-            x = np.array(positions, dtype=np.float64, copy=True)
-            if x.shape != (len(symbols), 3) or not np.isfinite(x).all():
+            if type(total_charge) not in (int, float) or not math.isfinite(total_charge):
+                validate_total_charge(total_charge)
+            x = np.ascontiguousarray(positions, dtype=np.float64)
+            if x.shape != (len(symbols), 3):
                 raise ValueError("positions must be a finite (N, 3) array in Angstrom")
-            flags, m = boundary(cell, pbc)
-            ff.validate_model(symbols)
+            if (pbc is None and cell is None) or pbc is False:
+                flags, m = _NO_PBC, None
+            else:
+                flags, m = boundary(cell, pbc)
+            if not self._all_valid:
+                ff.validate_model(symbols)
+        if m is None:
+            return symbols, x, types, flags, None, (1, 1, 1)
         reps = cell_repetitions(float(ff.general[12]), flags, m, len(symbols), self.max_expanded_atoms)
-        cellm = None if m is None else np.ascontiguousarray(m, dtype=np.float64)
-        return symbols, x, types, flags, cellm, reps
+        return symbols, x, types, flags, np.ascontiguousarray(m, dtype=np.float64), reps
 
     def _raise(self, code):
         if code in _ERRORS:
@@ -250,14 +276,9 @@ class Calculator:
     def parameter_gradient_many(self, systems):
         """As :meth:`parameter_gradient` for a batch: a list of evaluations and the gradient of their
         summed energy."""
-        batch, reps = [], []
-        for s in systems:
-            sym, x, types, flags, cellm, rp = self._prepare(s["symbols"], s["positions"], s.get("total_charge", 0),
-                                                            s.get("cell"), s.get("pbc"), False)
-            guess = _guess(s.get("initial_charges"), len(sym))
-            batch.append((types, x, flags, cellm, float(s.get("total_charge", 0)), guess))
-            reps.append(rp)
-        results = self._run(batch, False, reps, "replicated", nat.XR_FLAG_PARAM_GRADIENT)
+        results = self._evaluate_items([(s["symbols"], s["positions"], s.get("total_charge", 0), s.get("cell"),
+                                         s.get("pbc"), s.get("initial_charges")) for s in systems], False,
+                                       nat.XR_FLAG_PARAM_GRADIENT)
         T = len(self.force_field.elements)
         pair = np.zeros(T * T * 28)
         angle = np.zeros(7 * len(self._angle_rows))
@@ -276,81 +297,101 @@ class Calculator:
         (``symbols``, ``positions`` and optionally ``total_charge``, ``cell``, ``pbc``,
         ``initial_charges``). Returns a list of :class:`Evaluation` in the same order.
         """
+        return self._evaluate_items([(s["symbols"], s["positions"], s.get("total_charge", 0), s.get("cell"),
+                                      s.get("pbc"), s.get("initial_charges")) for s in systems], full_derivative)
+
+    def _evaluate_items(self, items, full_derivative=False, extra_flags=0):
+        """``evaluate_many`` on tuples (symbols, positions, total_charge, cell, pbc, initial_charges)."""
         batch, reps = [], []
-        for s in systems:
-            sym, x, types, flags, cellm, rp = self._prepare(s["symbols"], s["positions"], s.get("total_charge", 0),
-                                                            s.get("cell"), s.get("pbc"), full_derivative)
-            guess = _guess(s.get("initial_charges"), len(sym))
-            batch.append((types, x, flags, cellm, float(s.get("total_charge", 0)), guess))
+        prepare = self._prepare
+        for symbols, positions, total_charge, cell, pbc, initial in items:
+            sym, x, types, flags, cellm, rp = prepare(symbols, positions, total_charge, cell, pbc, full_derivative)
+            guess = None if initial is None else _guess(initial, len(sym))
+            batch.append((types, x, flags, cellm, float(total_charge), guess))
             reps.append(rp)
-        return self._run(batch, full_derivative, reps, "replicated")
+        return self._run(batch, full_derivative, reps, "replicated", extra_flags)
 
     def _run(self, batch, full_derivative, reps, backend, extra_flags=0):
+        """One ``xr_eval_batch`` call over ``batch`` = [(types, positions, pbc flags, cell, total
+        charge, initial charges)]. The inputs are packed into one array per kind and the
+        per-system descriptors are filled column-wise, so the host cost per system is a handful of
+        numpy operations; each ``Evaluation`` gets views of the batch's result arrays."""
         lib = self._lib
         n_sys = len(batch)
-        sizes = [len(b[0]) for b in batch]
-        total = sum(sizes)
+        types_l, xs, flags_l, cells, charges, guesses = zip(*batch)
+        sizes = np.fromiter(map(len, types_l), dtype=np.int64, count=n_sys)
+        offsets = np.zeros(n_sys + 1, dtype=np.int64)
+        np.cumsum(sizes, out=offsets[1:])
+        total = int(offsets[-1])
+        types = np.concatenate(types_l) if n_sys > 1 else types_l[0]
+        x = np.concatenate(xs) if n_sys > 1 else xs[0]
+        if not np.isfinite(x).all():
+            raise ValueError("positions must be a finite (N, 3) array in Angstrom")
+        sys_arr = np.zeros(n_sys, dtype=_SYSTEM_DTYPE)
+        sys_arr["natoms"] = sizes
+        sys_arr["types"] = nat.addr(types) + 4 * offsets[:-1]
+        sys_arr["positions"] = nat.addr(x) + 24 * offsets[:-1]
+        sys_arr["pbc"] = flags_l
+        sys_arr["total_charge"] = charges
+        if any(c is not None for c in cells):
+            sys_arr["cell"] = [0 if c is None else nat.addr(c) for c in cells]
+        if any(g is not None for g in guesses):
+            sys_arr["charges_guess"] = [0 if g is None else nat.addr(g) for g in guesses]
         # one allocation per kind for the whole batch; each Evaluation gets views
         energy = np.zeros((n_sys, 15))
         dipole = np.zeros((n_sys, 3))
         forces = np.zeros((total, 3))
         per_atom = np.zeros((3, total))  # charges, total bond orders, lone pairs
         counts = np.zeros(total, dtype=np.int32)
-        sys_arr = (nat.System * n_sys)()
-        res_arr = (nat.Result * n_sys)()
-        offsets = np.concatenate(([0], np.cumsum(sizes))).astype(int).tolist()
-        addr = nat.addr
-        e_base, f_base, q_base = addr(energy), addr(forces), addr(per_atom)
-        c_base, d_base = addr(counts), addr(dipole)
-        keep = []
-        for k, (types, x, flags, cellm, q, guess) in enumerate(batch):
-            a0 = offsets[k]
-            keep.append((types, x, cellm, guess))
-            s = sys_arr[k]
-            s.natoms = sizes[k]
-            s.types = addr(types)
-            s.positions = addr(x)
-            s.cell = addr(cellm)
-            for d in range(3):
-                s.pbc[d] = int(flags[d])
-            s.total_charge = q
-            s.charges_guess = addr(guess)
-            r = res_arr[k]
-            r.energy = e_base + 120 * k
-            r.forces = f_base + 24 * a0
-            r.charges = q_base + 8 * a0
-            r.total_bond_orders = q_base + 8 * (total + a0)
-            r.lone_pairs = q_base + 8 * (2 * total + a0)
-            r.bond_counts = c_base + 4 * a0
-            r.dipole = d_base + 24 * k
+        res_arr = np.empty(n_sys, dtype=_RESULT_DTYPE)
+        ks = np.arange(n_sys, dtype=np.int64)
+        a0s = offsets[:-1]
+        q_base = nat.addr(per_atom)
+        res_arr["energy"] = nat.addr(energy) + 120 * ks
+        res_arr["forces"] = nat.addr(forces) + 24 * a0s
+        res_arr["charges"] = q_base + 8 * a0s
+        res_arr["total_bond_orders"] = q_base + 8 * (total + a0s)
+        res_arr["lone_pairs"] = q_base + 8 * (2 * total + a0s)
+        res_arr["bond_counts"] = nat.addr(counts) + 4 * a0s
+        res_arr["dipole"] = nat.addr(dipole) + 24 * ks
         flags_ = (nat.XR_FLAG_FULL_DERIVATIVE if full_derivative else 0) | extra_flags
-        code = lib.xr_eval_batch(self._ctx.handle, self._ff.handle, n_sys, sys_arr, flags_, res_arr)
+        code = lib.xr_eval_batch(self._ctx.handle, self._ff.handle, n_sys, sys_arr.ctypes.data_as(_SYSTEM_P), flags_,
+                                 res_arr.ctypes.data_as(_RESULT_P))
         if code != nat.XR_OK:
             self._raise(code)
-        counts64 = counts.astype(int)
+        counts64 = counts.astype(np.int64)
         bi, bj, bS, bbo = self._bonds(-1)
-        cut = np.searchsorted(bi, offsets).tolist()  # bonds are grouped by system, in pair order
+        cut = np.searchsorted(bi, offsets)  # bonds are grouped by system, in pair order
+        if len(bi):
+            shift = np.repeat(a0s.astype(np.int32), np.diff(cut))
+            bi -= shift
+            bj -= shift
+        cut = cut.tolist()
+        offs = offsets.tolist()
+        etot = energy[:, 14].tolist()
+        comps = energy[:, :14].tolist()
+        charges_v, tbo_v, lp_v = per_atom
         results = []
+        new = object.__new__
         for k in range(n_sys):
-            a0, a1 = offsets[k], offsets[k + 1]
-            e = energy[k]
-            results.append(
-                Evaluation(
-                    energy=float(e[14]),
-                    forces=forces[a0:a1],
-                    charges=per_atom[0, a0:a1],
-                    components=dict(zip(COMPONENTS, e[:14].tolist())),
-                    full_derivative=full_derivative,
-                    total_bond_orders=per_atom[1, a0:a1],
-                    lone_pairs=per_atom[2, a0:a1],
-                    bond_counts=counts64[a0:a1],
-                    dipole=dipole[k],
-                    cell_repetitions=reps[k],
-                    neighbor_backend=backend,
-                    bonds=(bi[cut[k]:cut[k + 1]] - a0, bj[cut[k]:cut[k + 1]] - a0, bS[cut[k]:cut[k + 1]],
-                           bbo[cut[k]:cut[k + 1]]),
-                )
+            a0, a1 = offs[k], offs[k + 1]
+            c0, c1 = cut[k], cut[k + 1]
+            ev = new(Evaluation)  # a frozen dataclass: fields set without the per-field setattr checks
+            ev.__dict__.update(
+                energy=etot[k],
+                forces=forces[a0:a1],
+                charges=charges_v[a0:a1],
+                components=dict(zip(COMPONENTS, comps[k])),
+                full_derivative=full_derivative,
+                total_bond_orders=tbo_v[a0:a1],
+                lone_pairs=lp_v[a0:a1],
+                bond_counts=counts64[a0:a1],
+                dipole=dipole[k],
+                cell_repetitions=reps[k],
+                neighbor_backend=backend,
+                bonds=(bi[c0:c1], bj[c0:c1], bS[c0:c1], bbo[c0:c1]),
             )
+            results.append(ev)
         return results
 
     def _bonds(self, index):

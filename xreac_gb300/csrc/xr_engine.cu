@@ -147,6 +147,10 @@ struct xr_ctx {
   size_t cedge_dbslot = 0;
   double* hval = nullptr;
   size_t chval = 0;
+  float* qch = nullptr;  // FP32 pre-scaled QEq rows of systems whose rows exceed shared memory
+  size_t cqch = 0;
+  unsigned short* qcj = nullptr;
+  size_t cqcj = 0;
   int *pair_edge = nullptr, *pair_i = nullptr, *pair_bond = nullptr;
   size_t cpair_edge = 0, cpair_i = 0, cpair_bond = 0;
   double *p_r = nullptr, *p_shield = nullptr, *p_dshield = nullptr, *p_g = nullptr, *p_evdw = nullptr, *p_ecoul = nullptr;
@@ -372,6 +376,8 @@ bool ensure_lists(xr_ctx* c, long long E, long long P, long long B) {
   GROW(edge_pair, E);
   GROW(edge_dbslot, E);
   GROW(hval, E);
+  GROW(qch, E);
+  GROW(qcj, E);
   GROW(pair_edge, P);
   GROW(pair_i, P);
   GROW(pair_bond, P);
@@ -467,6 +473,8 @@ void attach_lists(xr_ctx* c, XrWork& w) {
   w.edge_pair = c->edge_pair;
   w.edge_dbslot = c->edge_dbslot;
   w.hval = c->hval;
+  w.qch = c->qch;
+  w.qcj = c->qcj;
   w.pair_edge = c->pair_edge;
   w.pair_i = c->pair_i;
   w.pair_bond = c->pair_bond;
@@ -589,18 +597,22 @@ int status_to_code(xr_ctx* c, int st) {
   return XR_OK;
 }
 
-// QEq work plan of a batch for the cooperative solver (at most kQeqBlocks co-resident blocks):
-// systems above kQeqSmall atoms get a team of ceil(n / 32) blocks (32 rows per 1024-thread block),
-// scaled down when the teams do not fit; the other systems are shared, largest first and round
-// robin, by the remaining blocks, each solving its systems alone. A one-block team is no team:
-// such a system joins the small ones.
+// QEq work plan of a batch for the solver kernel (at most kQeqBlocks co-resident blocks). A team
+// of ceil(n / 32) blocks (32 rows per 1024-thread block) solves a large system with grid-level
+// reductions, which shortens one solve; a single block solves a system with block barriers only,
+// which costs the fewest SM-cycles. So a single-system call gives a team to a system above
+// kQeqSmall atoms, and a batch (throughput) only to systems above kQeqBatchBlock atoms. Teams are
+// scaled down when they do not fit; the other systems are taken, largest first, by whichever block
+// is free. A one-block team is no team: such a system joins the small ones.
 constexpr int kQeqSmall = 160;
+constexpr int kQeqBatchBlock = 1024;
 constexpr int kQeqBlocks = 2048;
 
 void plan_qeq(xr_ctx* c, const xr_system* sys, int nsys, int* nblocks, int* nteam, int* nsmall) {
   const int budget = std::min(c->nsm * c->coop_per_sm, kQeqBlocks);
+  const int team_above = nsys > 1 ? kQeqBatchBlock : kQeqSmall;
   std::vector<int> large, small;
-  for (int s = 0; s < nsys; ++s) (sys[s].natoms > kQeqSmall ? large : small).push_back(s);
+  for (int s = 0; s < nsys; ++s) (sys[s].natoms > team_above ? large : small).push_back(s);
   std::sort(large.begin(), large.end(), [&](int a, int b) { return sys[a].natoms > sys[b].natoms; });
   std::vector<int> team(large.size());
   for (;;) {
@@ -1103,7 +1115,7 @@ int xr_ctx_create(int device, void* stream, xr_ctx** out) {
   if (!coop_ok) c->coop_per_sm = 0;
   bool ok = cudaMalloc((void**)&c->status, sizeof(int)) == cudaSuccess &&
             cudaMalloc((void**)&c->counts, 8 * sizeof(int)) == cudaSuccess &&
-            cudaMalloc((void**)&c->barrier, kQeqBlocks * sizeof(unsigned)) == cudaSuccess &&
+            cudaMalloc((void**)&c->barrier, (kQeqBlocks + 1) * sizeof(unsigned)) == cudaSuccess &&
             cudaMalloc((void**)&c->qmap, kQeqBlocks * sizeof(int4)) == cudaSuccess &&
             cudaMalloc((void**)&c->bx_count, sizeof(int)) == cudaSuccess &&
             cudaMalloc((void**)&c->nmids, 2 * sizeof(int)) == cudaSuccess &&
@@ -1121,7 +1133,7 @@ void xr_ctx_destroy(xr_ctx* c) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   void* bufs[] = {c->x, c->type, c->sys_of, c->wrap, c->xw, c->fw, c->cnt, c->a_fwd, c->a_adj, c->a_e, c->q, c->f,
-                  c->qwork, c->outbuf, c->edge, c->edge_pair, c->edge_dbslot, c->hval, c->pair_edge, c->pair_i,
+                  c->qwork, c->outbuf, c->edge, c->edge_pair, c->edge_dbslot, c->hval, c->qch, c->qcj, c->pair_edge, c->pair_i,
                   c->pair_bond, c->p_r, c->p_shield, c->p_dshield, c->p_g, c->p_evdw, c->p_ecoul, c->bond_pair,
                   c->bond_i, c->bond_j, c->b_r, c->b_v, c->b_fwd, c->b_adj, c->b_e, c->dbrow, c->sys, c->energy,
                   c->props, c->status, c->counts, c->barrier, c->qmap, c->qsmall, c->qiters, c->red, c->qguess, c->qrhs, c->qadj, c->pgrad, c->bx_meta, c->bx_bo, c->bx_count,

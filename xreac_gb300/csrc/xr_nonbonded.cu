@@ -296,6 +296,7 @@ struct QeqShared {
   double red[kRedSmem];
   double sc_lam, sc_alpha, sc_step, sc_beta;
   float sf_lam, sf_alpha, sf_step, sf_beta, sf_gz;
+  int sc_next;  // the next small system of the block (work sharing)
   int sc_state;  // 0 iterate, 1 converged, 2 stop
   union {
     double d[32][33];
@@ -574,16 +575,17 @@ __device__ inline void block_sum2(float a, float b, float* smem, Post post) {
 }
 
 // The FP32 solve of a refinement sweep for a system of at most 1024 atoms solved by one block: every
-// row's state (g, p, Hp, y, D^-1, eta D^-1, c, H'g) in shared memory, a warp per row for the product
-// (FP32 shuffles cost little), one thread per row for the updates and FP32 iteration scalars. Same
-// projected PCG as qeq_cg; about three block barriers per iteration instead of three per 32-row tile.
-// The correction y is written to y_out (global, indexed by atom).
+// row's state (g, p, Hp, y, D^-1, eta D^-1, c, H'g, row starts) in shared memory, a warp per row for
+// the product (FP32 shuffles cost little), one thread per row for the updates and FP32 iteration
+// scalars. Same projected PCG as qeq_cg; about five block barriers per iteration instead of three
+// per 32-row tile. The correction y is written to y_out (global, indexed by atom).
 __device__ int qeq_cg_block32(const XrWork& w, const XrFF& ff, QeqShared& sh, int a0, int n, float* rows,
                               const QeqMatrix<float>& M, float* y_out, double s1d, double gz_start, double stop,
                               int max_it) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5, tid = threadIdx.x;
   float *g = rows, *p = rows + n, *hp = rows + 2 * n, *y = rows + 3 * n, *di = rows + 4 * n, *etadi = rows + 5 * n,
         *cr = rows + 6 * n, *hz = rows + 7 * n;
+  int* rp = reinterpret_cast<int*>(rows + 8 * n);  // row starts relative to the cache
   const double* DI = &QW(Q_DINV, 0);
   const double* Cr = &QW(Q_C, 0);
   const double* G = &QW(Q_G, 0);
@@ -597,7 +599,9 @@ __device__ int qeq_cg_block32(const XrWork& w, const XrFF& ff, QeqShared& sh, in
     di[i] = float(DI[a]);
     etadi[i] = float(atom_prm(ff, w.type[a], A_ETA) * DI[a]);
     cr[i] = float(Cr[a]);
+    rp[i] = w.cnt[a] - M.ebeg;
   }
+  if (tid == 0) rp[n] = w.cnt[a0 + n] - M.ebeg;
   const float s1 = float(s1d);
   if (tid == 0) {
     sh.sf_lam = 0.0f;
@@ -616,7 +620,18 @@ __device__ int qeq_cg_block32(const XrWork& w, const XrFF& ff, QeqShared& sh, in
     const float lam = sh.sf_lam, beta = sh.sf_beta;
     for (int i = wid; i < n; i += nw) {  // H'g over the cached rows, a warp per row
       float s = 0.0f;
-      for (int e = w.cnt[a0 + i] + lane; e < w.cnt[a0 + i + 1]; e += 32) s += M.cache_h[e - M.ebeg] * g[M.cache_j[e - M.ebeg]];
+      const int ee = rp[i + 1];
+      int e = rp[i] + lane;
+      // four entries per lane in flight: the rows may stream from L2 rather than shared memory
+      for (; e + 96 < ee; e += 128) {
+        const float h0 = M.cache_h[e], h1 = M.cache_h[e + 32], h2 = M.cache_h[e + 64], h3 = M.cache_h[e + 96];
+        const int j0 = M.cache_j[e], j1 = M.cache_j[e + 32], j2 = M.cache_j[e + 64], j3 = M.cache_j[e + 96];
+        s += h0 * g[j0];
+        s += h1 * g[j1];
+        s += h2 * g[j2];
+        s += h3 * g[j3];
+      }
+      for (; e < ee; e += 32) s += M.cache_h[e] * g[M.cache_j[e]];
       s = warp_total_t<float>(s);
       if (lane == 0) hz[i] = s;
     }
@@ -745,20 +760,29 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
   // The cache holds FP32 values + 16-bit columns (6 B per entry, mixed precision) when the block's
   // rows fit, else FP64 values + columns (10 B), else nothing (rows read from global memory).
   // A block that solves a system of at most 1024 atoms alone keeps every row's FP32 state in shared
-  // memory instead (8 vectors, 32 B per atom; the space doubles as the FP64 stage of a fallback).
+  // memory instead (8 vectors and the row starts, 36 B per atom; the space doubles as the FP64 stage of
+// a fallback).
   constexpr bool kBlock = std::is_same<Team, BlockTeam>::value;
   const bool small_rows = kBlock && dyn != nullptr && n <= 1024;
   const int stage_n = (dyn != nullptr && (small_rows || n * 8 <= dyn_bytes / 2)) ? n : 0;
-  const size_t stage_bytes = small_rows ? 32 * (size_t)n : 8 * (size_t)stage_n;
+  const size_t stage_bytes = small_rows ? (36 * (size_t)n + 4 + 15) / 16 * 16 : 8 * (size_t)stage_n;
   void* gstage = stage_n > 0 ? dyn : nullptr;
   unsigned char* region = dyn != nullptr ? dyn + stage_bytes : nullptr;
   const long long region_bytes = dyn != nullptr ? dyn_bytes - (long long)stage_bytes : 0;
+  // Rows that do not fit are kept in FP32 in global memory (L2-resident for a batch) instead, so the
+  // solve stays mixed-precision; FP64 rows from hval are the path without that buffer.
   const bool cols16 = n <= 65536;
-  const bool mixed = region != nullptr && cols16 && nent <= region_bytes / 6;
+  const bool fits32 = region != nullptr && cols16 && nent <= region_bytes / 6;
+  const bool glob32 = !fits32 && cols16 && w.qch != nullptr;
+  const bool mixed = fits32 || glob32;
   const bool cached64 = !mixed && region != nullptr && cols16 && nent <= region_bytes / 10;
   void* cache_h = region;
   unsigned short* cache_j = nullptr;
-  if (mixed) cache_j = reinterpret_cast<unsigned short*>(region + 4 * (size_t)(region_bytes / 6));
+  if (fits32) cache_j = reinterpret_cast<unsigned short*>(region + 4 * (size_t)(region_bytes / 6));
+  if (glob32) {
+    cache_h = w.qch + ebeg;
+    cache_j = w.qcj + ebeg;
+  }
   if (cached64) cache_j = reinterpret_cast<unsigned short*>(region + 8 * (size_t)(region_bytes / 10));
   // 1. Jacobi diagonal (eta + self-image shields) of the owned rows, and the start point: the
   //    uniform x0 = Q/n, or the caller's charges of an earlier step (already summing to Q).
@@ -945,6 +969,24 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
 // cache columns (16-bit, local to the system)]. Each system's solve splits it the same way.
 constexpr int kQeqMaxDyn = 208 * 1024;
 
+// The systems solved by one block each, largest first, taken one at a time from a shared counter
+// by whichever block is free (a block of a team joins once its team's system is solved).
+__device__ void qeq_small_systems(const XrWork& w, const XrFF& ff, const int* small, int nsmall, unsigned* next,
+                                  int adjoint, QeqShared& sh, unsigned char* dyn) {
+  for (;;) {
+    if (threadIdx.x == 0) sh.sc_next = (int)atomicAdd(next, 1u);
+    __syncthreads();
+    const int k = sh.sc_next;
+    __syncthreads();
+    if (k >= nsmall) return;
+    const XrSystem& S = w.sys[small[k]];
+    BlockTeam team;
+    qeq_solve(w, ff, team, S.atom_off, S.natoms, 0, S.natoms, adjoint ? 0.0 : S.total_charge,
+              !adjoint && S.has_guess != 0, sh, dyn, kQeqMaxDyn, adjoint != 0);
+    __syncthreads();
+  }
+}
+
 // Cooperative solver launch for a batch: the first nteam blocks form teams, one per large system
 // (map[b] = {system, rank, team size, first block of the team}); each team splits its system's rows
 // and synchronises through its own bounded counter. The remaining blocks each solve a share of the
@@ -962,16 +1004,9 @@ __global__ void __launch_bounds__(1024, 1) k_qeq_grid(XrWork w, XrFF ff, const i
     GridTeam team{w.barrier + m.w, w.red + (size_t)32 * m.w, m.z, m.y};
     qeq_solve(w, ff, team, S.atom_off, S.natoms, r0, r1, adjoint ? 0.0 : S.total_charge, !adjoint && S.has_guess != 0,
               sh, dyn, kQeqMaxDyn, adjoint != 0);
-    return;
-  }
-  const int nsb = (int)gridDim.x - nteam;
-  for (int k = (int)blockIdx.x - nteam; k < nsmall; k += nsb) {
-    const XrSystem& S = w.sys[small[k]];
-    BlockTeam team;
-    qeq_solve(w, ff, team, S.atom_off, S.natoms, 0, S.natoms, adjoint ? 0.0 : S.total_charge,
-              !adjoint && S.has_guess != 0, sh, dyn, kQeqMaxDyn, adjoint != 0);
     __syncthreads();
   }
+  qeq_small_systems(w, ff, small, nsmall, w.barrier + nteam, adjoint, sh, dyn);
 }
 
 // Fallback without cooperative launch: one block per system, no shared-memory row cache.
@@ -1190,7 +1225,12 @@ int xr_launch_qeq(const XrWork& w, const XrFF& ff, cudaStream_t st, int nblocks,
                   const int* small, int nsmall, bool adjoint) {
   int adj = adjoint ? 1 : 0;
   if (nblocks > 0) {
-    if (nteam > 0) cudaMemsetAsync(w.barrier, 0, sizeof(unsigned) * (size_t)nteam, st);
+    // team barrier counters, then the small-system counter
+    cudaMemsetAsync(w.barrier, 0, sizeof(unsigned) * (size_t)(nteam + 1), st);
+    if (nteam == 0) {  // no block waits on another: an ordinary launch, which may overlap other streams' work
+      k_qeq_grid<<<nblocks, 1024, kQeqMaxDyn, st>>>(w, ff, map, nteam, small, nsmall, adj);
+      return (int)cudaGetLastError();
+    }
     void* args[] = {(void*)&w, (void*)&ff, (void*)&map, (void*)&nteam, (void*)&small, (void*)&nsmall, (void*)&adj};
     cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_qeq_grid, dim3(nblocks), dim3(1024), args, kQeqMaxDyn, st);
     return (int)e;

@@ -197,46 +197,42 @@ class Server:
                     continue
             self._run(calcs[name], name, batch)
 
-    def _guess(self, req):
-        if not self.warm_start or req.session is None:
-            return None
-        with self._charges_lock:
-            g = self._charges.get(req.session)
-        return g if g is not None and len(g) == req.natoms else None
-
     def _run(self, calc, name, batch):
-        systems = []
-        for req, _ in batch:
-            s = dict(symbols=req.symbols, positions=req.positions, cell=req.cell, pbc=req.pbc,
-                     total_charge=req.total_charge)
-            g = self._guess(req)
-            if g is not None:
-                s["initial_charges"] = g
-            systems.append(s)
+        charges = self._charges
+        warm = self.warm_start
+        items = []
+        with self._charges_lock:
+            for req, _ in batch:
+                g = charges.get(req.session) if warm and req.session is not None else None
+                if g is not None and len(g) != len(req.symbols):
+                    g = None
+                items.append((req.symbols, req.positions, req.total_charge, req.cell, req.pbc, g))
         t0 = time.perf_counter()
         try:
-            results = calc.evaluate_many(systems)
+            results = calc._evaluate_items(items)
         except Exception:
             # isolate the failing request(s): evaluate one by one
             results = []
-            for s in systems:
+            for it in items:
                 try:
-                    results.append(calc.evaluate_many([s])[0])
+                    results.append(calc._evaluate_items([it])[0])
                 except Exception as err:  # noqa: BLE001 - reported through the future
                     results.append(err)
         done = time.perf_counter()
         its, qbytes = calc.qeq_work()
         h2d, d2h = calc.transfer_bytes()
-        self.batches.append(Batch(name, len(batch), sum(r.natoms for r, _ in batch), done - t0, calc.last_launches,
+        self.batches.append(Batch(name, len(batch), sum(len(it[0]) for it in items), done - t0, calc.last_launches,
                                   its, qbytes, h2d, d2h))
+        with self._charges_lock:
+            for (req, _), res in zip(batch, results):
+                if req.session is not None and not isinstance(res, Exception):
+                    charges[req.session] = res.charges
+        nb = len(batch)
         for (req, fut), res in zip(batch, results):
             if isinstance(res, Exception):
                 fut.set_exception(res)
-                continue
-            if req.session is not None:
-                with self._charges_lock:
-                    self._charges[req.session] = res.charges
-            fut.set_result(Served(res, req.arrival, done, len(batch), t0))
+            else:
+                fut.set_result(Served(res, req.arrival, done, nb, t0))
 
 
 def replay(server, requests, arrivals=None, speedup=1.0):
