@@ -224,6 +224,13 @@ int xr_launch_qeq(const XrWork& w, const XrFF& ff, cudaStream_t st, int nblocks,
                   const int* small, int nsmall, bool adjoint = false);
 void xr_launch_charge_response(const XrWork& w, const XrFF& ff, cudaStream_t st, int stage);
 int xr_qeq_coop_blocks_per_sm();
+// Thread-block-cluster QEq solver for batches: blocks per cluster, how many such clusters can be
+// resident at once (0: unavailable), and its launch over `list` = nbig cluster systems followed by
+// nsmall single-block systems (nblocks a multiple of kQeqCluster).
+constexpr int kQeqCluster = 8;
+int xr_qeq_max_clusters();
+int xr_launch_qeq_cluster(const XrWork& w, const XrFF& ff, cudaStream_t st, int nblocks, const int* list, int nbig,
+                          int nsmall, bool adjoint = false);
 void xr_launch_coulomb(const XrWork& w, const XrFF& ff, cudaStream_t st);
 void xr_launch_bonded(const XrWork& w, const XrFF& ff, cudaStream_t st);
 void xr_launch_forces(const XrWork& w, const XrFF& ff, cudaStream_t st);

@@ -70,6 +70,7 @@ struct xr_ctx {
   int cg_max = 2000;
   int nsm = 0;
   int coop_per_sm = 0;
+  int max_clusters = 0;  // resident thread-block clusters of the cluster QEq solver (0: unavailable)
   long long launches = 0;
   long long h2d_bytes = 0, d2h_bytes = 0;  // host<->device bytes moved by the last evaluation
   int qeq_iterations = 0;                   // CG iterations of the last evaluation (largest system)
@@ -646,6 +647,35 @@ void plan_qeq(xr_ctx* c, const xr_system* sys, int nsys, int* nblocks, int* ntea
   }
 }
 
+// Cluster plan: every system above kQeqSmall atoms is solved by one thread-block cluster
+// (kQeqCluster blocks, rows split over them, reductions in distributed shared memory), the others
+// by single blocks. Taken when no system is too large for a cluster to be the better choice: above
+// kQeqClusterMax atoms a single-system call spreads the rows over a grid-wide team instead, and
+// above kQeqBatchBlock atoms a batch does. h_qsmall receives the cluster systems, then the others,
+// each largest first.
+constexpr int kQeqClusterMax = 640;
+
+bool plan_qeq_cluster(xr_ctx* c, const xr_system* sys, int nsys, int* nblocks, int* nbig, int* nsmall) {
+  if (c->max_clusters < 1) return false;
+  const int limit = nsys > 1 ? kQeqBatchBlock : kQeqClusterMax;
+  std::vector<int> big, small;
+  for (int s = 0; s < nsys; ++s) {
+    if (sys[s].natoms > limit) return false;
+    (sys[s].natoms > kQeqSmall ? big : small).push_back(s);
+  }
+  auto larger = [&](int a, int b) { return sys[a].natoms > sys[b].natoms; };
+  std::sort(big.begin(), big.end(), larger);
+  std::sort(small.begin(), small.end(), larger);
+  const int clusters = std::max(1, std::min(c->nsm / kQeqCluster,
+                                            (int)big.size() + ((int)small.size() + kQeqCluster - 1) / kQeqCluster));
+  *nblocks = clusters * kQeqCluster;
+  *nbig = (int)big.size();
+  *nsmall = (int)small.size();
+  c->h_qsmall.assign(big.begin(), big.end());
+  c->h_qsmall.insert(c->h_qsmall.end(), small.begin(), small.end());
+  return true;
+}
+
 int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsigned flags, xr_result* out) {
   if (!c || !ff || nsys < 1 || !sys) {
     if (c) c->err = "invalid arguments";
@@ -816,23 +846,30 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
   xr_launch_pairs(w, ff->d, st);
   launches += 2;
   stage(c, 3, st);
-  int qblocks = 0, qteam = 0, qsmall = 0;
+  int qblocks = 0, qteam = 0, qsmall = 0, qbig = 0;
+  bool qcluster = false;
   if (c->coop_per_sm > 0) {
-    plan_qeq(c, sys, nsys, &qblocks, &qteam, &qsmall);
+    qcluster = plan_qeq_cluster(c, sys, nsys, &qblocks, &qbig, &qsmall);
+    if (!qcluster) plan_qeq(c, sys, nsys, &qblocks, &qteam, &qsmall);
+    const int nlist = qbig + qsmall;
     if (!host_grow(&c->h_qmap_p, &c->ch_qmap_p, (size_t)std::max(qteam, 1)) ||
-        !host_grow(&c->h_qsmall_p, &c->ch_qsmall_p, (size_t)std::max(qsmall, 1)))
+        !host_grow(&c->h_qsmall_p, &c->ch_qsmall_p, (size_t)std::max(nlist, 1)))
       return cuda_fail(c, cudaErrorMemoryAllocation, "allocation");
     if (qteam > 0) {
       std::memcpy(c->h_qmap_p, c->h_qmap.data(), sizeof(int4) * qteam);
       cudaMemcpyAsync(c->qmap, c->h_qmap_p, sizeof(int4) * qteam, cudaMemcpyHostToDevice, st);
     }
-    if (qsmall > 0) {
-      std::memcpy(c->h_qsmall_p, c->h_qsmall.data(), sizeof(int) * qsmall);
-      cudaMemcpyAsync(c->qsmall, c->h_qsmall_p, sizeof(int) * qsmall, cudaMemcpyHostToDevice, st);
+    if (nlist > 0) {
+      std::memcpy(c->h_qsmall_p, c->h_qsmall.data(), sizeof(int) * nlist);
+      cudaMemcpyAsync(c->qsmall, c->h_qsmall_p, sizeof(int) * nlist, cudaMemcpyHostToDevice, st);
     }
-    h2d += sizeof(int4) * (long long)qteam + sizeof(int) * (long long)qsmall;
+    h2d += sizeof(int4) * (long long)qteam + sizeof(int) * (long long)nlist;
   }
-  if (int le = xr_launch_qeq(w, ff->d, st, qblocks, c->qmap, qteam, c->qsmall, qsmall))
+  auto launch_qeq = [&](bool adjoint) {
+    return qcluster ? xr_launch_qeq_cluster(w, ff->d, st, qblocks, c->qsmall, qbig, qsmall, adjoint)
+                    : xr_launch_qeq(w, ff->d, st, qblocks, c->qmap, qteam, c->qsmall, qsmall, adjoint);
+  };
+  if (int le = launch_qeq(false))
     return cuda_fail(c, (cudaError_t)le, "QEq launch");
   launches += 1;
   stage(c, 4, st);
@@ -841,7 +878,7 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
   if (w.full_derivative) {
     // charge-response forces: adjoint QEq solve with the same plan, then its radial pair terms
     xr_launch_charge_response(w, ff->d, st, 0);
-    if (int le = xr_launch_qeq(w, ff->d, st, qblocks, c->qmap, qteam, c->qsmall, qsmall, true))
+    if (int le = launch_qeq(true))
       return cuda_fail(c, (cudaError_t)le, "adjoint QEq launch");
     xr_launch_charge_response(w, ff->d, st, 1);
     launches += 4;
@@ -1110,6 +1147,7 @@ int xr_ctx_create(int device, void* stream, xr_ctx** out) {
   }
   cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device);
   c->coop_per_sm = xr_qeq_coop_blocks_per_sm();
+  c->max_clusters = xr_qeq_max_clusters();
   int coop_ok = 0;
   cudaDeviceGetAttribute(&coop_ok, cudaDevAttrCooperativeLaunch, device);
   if (!coop_ok) c->coop_per_sm = 0;

@@ -148,7 +148,7 @@ __device__ bool grid_barrier(unsigned* bar, unsigned target, int* status) {
     asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(bar) : "memory");
     long long it = 0;
     while (ld_acquire(bar) < target) {
-      if (++it > (1ll << 24) || (*(volatile int*)status & XR_S_BARRIER)) {
+      if (++it > (1ll << 24) || ((it & 255) == 0 && (*(volatile int*)status & XR_S_BARRIER))) {
         atomicOr(status, XR_S_BARRIER);
         ok = 0;
         break;
@@ -198,7 +198,7 @@ struct GridTeam {
         asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(bar) : "memory");
         long long it = 0;
         while (ld_acquire(bar) < target) {
-          if (++it > (1ll << 24) || (*(volatile int*)w.status & XR_S_BARRIER)) {
+          if (++it > (1ll << 24) || ((it & 255) == 0 && (*(volatile int*)w.status & XR_S_BARRIER))) {
             atomicOr(w.status, XR_S_BARRIER);
             good = 0;
             break;
@@ -260,6 +260,131 @@ struct BlockTeam {
 };
 
 // Team sum of NV values held by lane 0 of every warp: warp 0 first adds the block's warps.
+// Distributed shared memory of a thread-block cluster (sm_90+): 32-bit shared-window addresses, the
+// same variable in another block of the cluster, and mbarrier operations on it.
+__device__ inline unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ inline unsigned cluster_map(unsigned addr, unsigned rank) {
+  unsigned r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
+  return r;
+}
+__device__ inline unsigned cluster_rank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ inline unsigned cluster_size() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+  return r;
+}
+// Hardware barrier of all threads of the cluster; only where every block is known to arrive (kernel
+// entry and exit), never inside the solver.
+__device__ inline void cluster_barrier_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// Team of the blocks of one thread-block cluster (at most 8), exchanging through distributed shared
+// memory. A reduction or barrier is one exchange, numbered m = 1, 2, ...: lane r of warp 0 of every
+// block writes that block's partials into block r's slot array and then the exchange number into
+// the entry's sequence word (a release store, cluster scope); lane r of each block waits (bounded,
+// acquire loads) until entry r of its own slot array carries m. The partials are then added in rank
+// order, so every block holds bit-identical totals and takes the same path. Two slot arrays
+// alternate by the parity of m: block X writes exchange m + 2 into block Y only after seeing Y's
+// entry of exchange m + 1, which Y wrote after reading exchange m.
+struct ClusterTeam {
+  double* slots;    // this block's partials, [parity][rank][value], 2 x 8 x 8
+  unsigned* seqs;   // the exchange number of each entry, [parity][rank], 2 x 8 (zeroed at entry)
+  int nb, rank;
+  mutable unsigned count = 0;  // exchanges so far
+  // Warp 0: push v[0..nv) (valid in lanes < nb) into every block's entry `rank` of slot array
+  // `par`, then wait until this block's entries 0..nb-1 carry exchange number `count`. Lane r
+  // (< nb) returns entry r's values in t. Bounded: false after about 2^22 polls or once another
+  // wait has given up (the status bit).
+  template <int NV>
+  __device__ bool exchange(const XrWork& w, const double* v, unsigned par, double* t) const {
+    const int lane = threadIdx.x & 31;
+    const unsigned m = count;
+    __syncwarp();
+    if (lane < nb) {
+      const unsigned dst = cluster_map(smem_u32(slots + (par * 8 + rank) * 8), lane);
+#pragma unroll
+      for (int k = 0; k < NV; ++k) asm volatile("st.shared::cluster.f64 [%0], %1;" ::"r"(dst + 8 * k), "d"(v[k]) : "memory");
+      asm volatile("st.release.cluster.shared::cluster.u32 [%0], %1;" ::"r"(cluster_map(smem_u32(seqs + par * 8 + rank), lane)),
+                   "r"(m)
+                   : "memory");
+    }
+    bool mine = lane >= nb;
+    const unsigned mine_addr = smem_u32(seqs + par * 8 + (lane & 7));
+    long long it = 0;
+    int good = 1;
+    for (;;) {
+      if (!mine) {
+        unsigned sq;
+        asm volatile("ld.acquire.cluster.shared::cta.u32 %0, [%1];" : "=r"(sq) : "r"(mine_addr) : "memory");
+        mine = sq == m;
+      }
+      if (__all_sync(0xffffffffu, mine)) break;
+      bool stop = ++it > (1ll << 22);
+      if (lane == 0 && (it & 1023) == 0) stop = stop || (*(volatile int*)w.status & XR_S_BARRIER);
+      if (__any_sync(0xffffffffu, stop)) {
+        if (lane == 0) atomicOr(w.status, XR_S_BARRIER);
+        good = 0;
+        break;
+      }
+    }
+    if (lane < nb) {
+      const double* src = slots + (par * 8 + lane) * 8;
+#pragma unroll
+      for (int k = 0; k < NV; ++k) t[k] = src[k];
+    } else {
+#pragma unroll
+      for (int k = 0; k < NV; ++k) t[k] = 0.0;
+    }
+    return good;
+  }
+  // Totals of the entries over lanes 0..7 of warp 0, a fixed tree (the same in every block).
+  __device__ static double rank_total(double t) {
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    return t;
+  }
+  __device__ bool sync(const XrWork& w) const {
+    __shared__ int ok;
+    __syncthreads();
+    const unsigned par = ++count & 1;
+    if (threadIdx.x < 32) {
+      if (threadIdx.x == 0) asm volatile("fence.acq_rel.cluster;" ::: "memory");
+      double t[1];
+      const bool g = exchange<0>(w, nullptr, par, t);
+      if (threadIdx.x == 0) ok = g;
+    }
+    __syncthreads();
+    return ok;
+  }
+  template <int NV, class Post>
+  __device__ bool reduce(const XrWork& w, double* v, double* smem, int slot, Post post) const {
+    static_assert(NV <= 8, "at most eight values per reduction");
+    __shared__ int ok;
+    double* res = result_slot(smem, slot);
+    const unsigned par = ++count & 1;
+    if (threadIdx.x < 32) {
+      double t[NV > 0 ? NV : 1];
+      const bool g = exchange<NV>(w, v, par, t);
+#pragma unroll
+      for (int k = 0; k < NV; ++k) t[k] = rank_total(t[k]);
+      if (threadIdx.x == 0) {
+        ok = g;
+        for (int k = 0; k < NV; ++k) res[k] = t[k];
+        post(res);
+      }
+    }
+    __syncthreads();
+    for (int k = 0; k < NV; ++k) v[k] = res[k];
+    return ok;
+  }
+};
+
 template <int NV, class Team, class Post>
 __device__ bool team_sum(const Team& team, const XrWork& w, double* v, double* smem, int slot, Post post) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -276,13 +401,6 @@ __device__ bool team_sum(const Team& team, const XrWork& w, double* v, double* s
   return team.template reduce<NV>(w, v, smem, slot, post);
 }
 
-// Warp-0 sum of a per-lane value (the block total ends in every lane of warp 0).
-__device__ inline double warp_total(double t) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
-  return t;
-}
-
 // Per-row solver state of a block with at most 32 rows (the grid layout), indexed by row - r0.
 template <class T>
 struct QeqRows {
@@ -297,6 +415,8 @@ struct QeqShared {
   double sc_lam, sc_alpha, sc_step, sc_beta;
   float sf_lam, sf_alpha, sf_step, sf_beta, sf_gz;
   int sc_next;  // the next small system of the block (work sharing)
+  double cred[2][8][8];  // cluster team: partials pushed by the blocks of the cluster
+  unsigned cseq[2][8];   // cluster team: exchange number of each pushed entry
   int sc_state;  // 0 iterate, 1 converged, 2 stop
   union {
     double d[32][33];
@@ -553,10 +673,29 @@ __device__ int qeq_cg(const XrWork& w, const XrFF& ff, const Team& team, QeqShar
   return it;
 }
 
-// Sum of two floats over the block (every thread passes its values; the block total reaches thread 0,
-// which runs post() on it; everyone waits for post()).
-template <class Post>
-__device__ inline void block_sum2(float a, float b, float* smem, Post post) {
+// Every lane of the warp gets the warp's totals of v[0..NV) (fixed shuffle tree: deterministic).
+template <int NV>
+__device__ inline void warp_sum_all(double* v) {
+#pragma unroll
+  for (int k = 0; k < NV; ++k) v[k] = warp_total_t<double>(v[k]);
+}
+
+// Lanes per matrix row in the per-row loops over a block's m rows: as many as keep the rows within
+// two passes of the block's warps (at least 4), so short rows of small systems do not leave most
+// lanes idle; each lane keeps four entries' loads in flight.
+__device__ inline int row_group(int m) {
+  int g = 32;
+  while (g > 4 && m * g > 2048) g >>= 1;
+  return g;
+}
+
+// Sum of two floats over the team: every thread passes its values; the block totals are formed in
+// warp 0 and, for a cluster team, exchanged and added in rank order; thread 0 of each block runs
+// post() on the totals (bit-identical in every block) and the block waits for it. Returns false
+// when a cluster exchange gave up.
+template <class Team, class Post>
+__device__ inline bool team_sum2f(const Team& team, const XrWork& w, float a, float b, float* smem, Post post) {
+  constexpr bool kCluster = std::is_same<Team, ClusterTeam>::value;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   a = warp_total_t<float>(a);
   b = warp_total_t<float>(b);
@@ -565,43 +704,81 @@ __device__ inline void block_sum2(float a, float b, float* smem, Post post) {
     smem[32 + wid] = b;
   }
   __syncthreads();
+  bool good = true;
   if (wid == 0) {
     float x = lane < nw ? smem[lane] : 0.0f, y = lane < nw ? smem[32 + lane] : 0.0f;
     x = warp_total_t<float>(x);
     y = warp_total_t<float>(y);
-    if (lane == 0) post(x, y);
+    if constexpr (kCluster) {
+      const unsigned par = ++team.count & 1;
+      const double v[2] = {double(x), double(y)};
+      double t[2];
+      good = team.template exchange<2>(w, v, par, t);
+      x = float(ClusterTeam::rank_total(t[0]));
+      y = float(ClusterTeam::rank_total(t[1]));
+    }
+    if (lane == 0) {
+      post(x, y);
+      if (!good) smem[64] = -1.0f;
+    }
+  }
+  if constexpr (kCluster) {
+    if (threadIdx.x == 0 && good) smem[64] = 0.0f;
   }
   __syncthreads();
+  if constexpr (kCluster) return smem[64] == 0.0f;
+  return true;
 }
 
-// The FP32 solve of a refinement sweep for a system of at most 1024 atoms solved by one block: every
-// row's state (g, p, Hp, y, D^-1, eta D^-1, c, H'g, row starts) in shared memory, a warp per row for
-// the product (FP32 shuffles cost little), one thread per row for the updates and FP32 iteration
-// scalars. Same projected PCG as qeq_cg; about five block barriers per iteration instead of three
-// per 32-row tile. The correction y is written to y_out (global, indexed by atom).
-__device__ int qeq_cg_block32(const XrWork& w, const XrFF& ff, QeqShared& sh, int a0, int n, float* rows,
-                              const QeqMatrix<float>& M, float* y_out, double s1d, double gz_start, double stop,
-                              int max_it) {
+// The FP32 solve of a refinement sweep with every vector in shared memory, for a system of at most
+// 1024 atoms solved by one block (rows [0, n)) or by a thread-block cluster (this block's rows
+// [r0, r1), at most 128). The block holds the whole gradient g (n values, indexed by row of the
+// system) and the state of its own rows: p, Hp, y, D^-1, eta D^-1, c, the shifted gradient and the
+// row starts. A group of lanes per row forms the product and its first lane the row's first
+// update, a thread per row the second; the scalars are FP32. In a cluster, each
+// block writes its rows' new gradient into every other block's copy (distributed shared memory)
+// before the second reduction, whose exchange publishes it. Same projected PCG as qeq_cg. The
+// correction y of the own rows is written to y_out (global, indexed by atom).
+// The vectors start at the beginning of the kernel's dynamic shared memory; naming it here (rather
+// than taking a pointer) lets the compiler use shared-memory loads and stores, and the function is
+// kept out of line so that its loops do not share registers with the rest of the solve.
+template <class Team>
+__device__ __noinline__ int qeq_cg_rows32(const XrWork& w, const XrFF& ff, const Team& team, QeqShared& sh, int a0,
+                                          int n, int r0, int r1, const QeqMatrix<float>& M, float* y_out, double s1d,
+                                          double gz_start, double stop, int max_it) {
+  extern __shared__ __align__(16) unsigned char qeq_dyn[];
+  constexpr bool kCluster = std::is_same<Team, ClusterTeam>::value;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5, tid = threadIdx.x;
-  float *g = rows, *p = rows + n, *hp = rows + 2 * n, *y = rows + 3 * n, *di = rows + 4 * n, *etadi = rows + 5 * n,
-        *cr = rows + 6 * n, *hz = rows + 7 * n;
-  int* rp = reinterpret_cast<int*>(rows + 8 * n);  // row starts relative to the cache
+  const int m = r1 - r0;
+  float* const rows = reinterpret_cast<float*>(qeq_dyn);
+  float *g = rows, *p = rows + n, *hp = p + m, *y = hp + m, *di = y + m, *etadi = di + m, *cr = etadi + m,
+        *gown = cr + m;  // gown: the own rows' gradient minus the multiplier, between the two updates
+  int* rp = reinterpret_cast<int*>(gown + m);  // row starts relative to the cache
+  // the row cache: in this block's shared memory, or FP32 rows in global memory
+  const bool cache_shared = __isShared(M.cache_h);
+  const float* const ch_g = M.cache_h;
+  const unsigned short* const cj_g = M.cache_j;
+  const float* const ch_s =
+      reinterpret_cast<const float*>(qeq_dyn + (cache_shared ? (reinterpret_cast<const unsigned char*>(M.cache_h) - qeq_dyn) : 0));
+  const unsigned short* const cj_s = reinterpret_cast<const unsigned short*>(
+      qeq_dyn + (cache_shared ? (reinterpret_cast<const unsigned char*>(M.cache_j) - qeq_dyn) : 0));
+  const int ebeg = M.ebeg;
   const double* DI = &QW(Q_DINV, 0);
   const double* Cr = &QW(Q_C, 0);
   const double* G = &QW(Q_G, 0);
   float* red = reinterpret_cast<float*>(sh.red);
-  for (int i = tid; i < n; i += blockDim.x) {
-    const int a = a0 + i;
-    g[i] = float(G[a]);
+  for (int q = tid; q < n; q += blockDim.x) g[q] = float(__ldcg(G + a0 + q));
+  for (int i = tid; i < m; i += blockDim.x) {
+    const int a = a0 + r0 + i;
     p[i] = 0.0f;
     hp[i] = 0.0f;
     y[i] = 0.0f;
     di[i] = float(DI[a]);
     etadi[i] = float(atom_prm(ff, w.type[a], A_ETA) * DI[a]);
     cr[i] = float(Cr[a]);
-    rp[i] = w.cnt[a] - M.ebeg;
+    rp[i] = w.cnt[a] - ebeg;
   }
-  if (tid == 0) rp[n] = w.cnt[a0 + n] - M.ebeg;
+  if (tid == 0) rp[m] = w.cnt[a0 + r1] - ebeg;
   const float s1 = float(s1d);
   if (tid == 0) {
     sh.sf_lam = 0.0f;
@@ -610,7 +787,11 @@ __device__ int qeq_cg_block32(const XrWork& w, const XrFF& ff, QeqShared& sh, in
     sh.sc_state = (!(gz_start > 0.0) || n < 2 || gz_start <= stop) ? 1 : 0;
   }
   __syncthreads();
+  // remote addresses of this block's rows in the other blocks' gradient copies
+  unsigned gremote = 0;
+  if constexpr (kCluster) gremote = smem_u32(g + r0);
   const float fstop = float(stop);
+  const int gs = row_group(m), sub = lane & (gs - 1), gpw = 32 / gs;
   int it = 0;
   while (sh.sc_state == 0) {
     if (++it > max_it) {
@@ -618,66 +799,77 @@ __device__ int qeq_cg_block32(const XrWork& w, const XrFF& ff, QeqShared& sh, in
       break;
     }
     const float lam = sh.sf_lam, beta = sh.sf_beta;
-    for (int i = wid; i < n; i += nw) {  // H'g over the cached rows, a warp per row
+    // H'g over the cached rows, gs lanes per row; the group's first lane then updates the row:
+    // p = -z + beta p, Hp = -H z + beta Hp with z = D^-1 (g - lambda), H z = H'g - lambda c.
+    float php0 = 0.0f, php1 = 0.0f;
+    // four entries per lane in flight: the rows may stream from L2 rather than shared memory
+    auto row_dot = [&](const float* ch, const unsigned short* cj, int e, int ee) {
       float s = 0.0f;
-      const int ee = rp[i + 1];
-      int e = rp[i] + lane;
-      // four entries per lane in flight: the rows may stream from L2 rather than shared memory
-      for (; e + 96 < ee; e += 128) {
-        const float h0 = M.cache_h[e], h1 = M.cache_h[e + 32], h2 = M.cache_h[e + 64], h3 = M.cache_h[e + 96];
-        const int j0 = M.cache_j[e], j1 = M.cache_j[e + 32], j2 = M.cache_j[e + 64], j3 = M.cache_j[e + 96];
+      for (; e + 3 * gs < ee; e += 4 * gs) {
+        const float h0 = ch[e], h1 = ch[e + gs], h2 = ch[e + 2 * gs], h3 = ch[e + 3 * gs];
+        const int j0 = cj[e], j1 = cj[e + gs], j2 = cj[e + 2 * gs], j3 = cj[e + 3 * gs];
         s += h0 * g[j0];
         s += h1 * g[j1];
         s += h2 * g[j2];
         s += h3 * g[j3];
       }
-      for (; e < ee; e += 32) s += M.cache_h[e] * g[M.cache_j[e]];
-      s = warp_total_t<float>(s);
-      if (lane == 0) hz[i] = s;
-    }
-    __syncthreads();
-    float php0 = 0.0f, php1 = 0.0f;
-    for (int i = tid; i < n; i += blockDim.x) {
-      const float ga = g[i];
-      const float h = hz[i] + etadi[i] * ga - lam * cr[i];
-      const float z = di[i] * (ga - lam);
-      const float pv = -z + beta * p[i];
-      const float hpv = -h + beta * hp[i];
-      p[i] = pv;
-      hp[i] = hpv;
-      g[i] = ga - lam;
-      php0 += pv * hpv;
-      php1 += di[i] * hpv;
-    }
-    block_sum2(php0, php1, red, [&](float t0, float t1) {
-      const float gz = sh.sf_gz;
-      if (!(fabsf(t0) > 0.0f) || !isfinite(t0)) {
-        sh.sc_state = 2;  // breakdown: the FP64 residual of the sweep decides what follows
-      } else {
-        sh.sf_alpha = gz / t0;
-        sh.sf_step = sh.sf_alpha * t1 / s1;
+      for (; e < ee; e += gs) s += ch[e] * g[cj[e]];
+      return s;
+    };
+    for (int ib = wid * gpw; ib < m; ib += nw * gpw) {
+      const int i = ib + lane / gs;
+      float s = 0.0f;
+      if (i < m) s = cache_shared ? row_dot(ch_s, cj_s, rp[i] + sub, rp[i + 1]) : row_dot(ch_g, cj_g, rp[i] + sub, rp[i + 1]);
+      for (int o = gs / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (sub == 0 && i < m) {
+        const float ga = g[r0 + i];
+        const float h = s + etadi[i] * ga - lam * cr[i];
+        const float z = di[i] * (ga - lam);
+        const float pv = -z + beta * p[i];
+        const float hpv = -h + beta * hp[i];
+        p[i] = pv;
+        hp[i] = hpv;
+        gown[i] = ga - lam;  // g itself stays as is until every row's product is done
+        php0 += pv * hpv;
+        php1 += di[i] * hpv;
       }
-    });
+    }
+    if (!team_sum2f(team, w, php0, php1, red, [&](float t0, float t1) {
+          const float gz = sh.sf_gz;
+          if (!(fabsf(t0) > 0.0f) || !isfinite(t0)) {
+            sh.sc_state = 2;  // breakdown: the FP64 residual of the sweep decides what follows
+          } else {
+            sh.sf_alpha = gz / t0;
+            sh.sf_step = sh.sf_alpha * t1 / s1;
+          }
+        }))
+      return -1;
     if (sh.sc_state != 0) break;
     const float alpha = sh.sf_alpha, step = sh.sf_step;
     float u0 = 0.0f, u1 = 0.0f;
-    for (int i = tid; i < n; i += blockDim.x) {
-      const float gn = (g[i] + alpha * hp[i]) - step;
+    for (int i = tid; i < m; i += blockDim.x) {
+      const float gn = (gown[i] + alpha * hp[i]) - step;
       y[i] += alpha * p[i];
-      g[i] = gn;
+      g[r0 + i] = gn;
+      if constexpr (kCluster) {
+        for (int r = 0; r < team.nb; ++r)
+          if (r != team.rank)
+            asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(cluster_map(gremote + 4 * i, r)), "f"(gn) : "memory");
+      }
       u0 += di[i] * gn;
       u1 += di[i] * gn * gn;
     }
-    block_sum2(u0, u1, red, [&](float t0, float t1) {
-      const float lamn = t0 / s1;
-      const float gzn = t1 - lamn * t0;
-      sh.sf_lam = lamn;
-      sh.sf_beta = gzn / sh.sf_gz;
-      sh.sf_gz = gzn;
-      if (gzn <= fstop) sh.sc_state = 1;
-    });
+    if (!team_sum2f(team, w, u0, u1, red, [&](float t0, float t1) {
+          const float lamn = t0 / s1;
+          const float gzn = t1 - lamn * t0;
+          sh.sf_lam = lamn;
+          sh.sf_beta = gzn / sh.sf_gz;
+          sh.sf_gz = gzn;
+          if (gzn <= fstop) sh.sc_state = 1;
+        }))
+      return -1;
   }
-  for (int i = tid; i < n; i += blockDim.x) y_out[a0 + i] = y[i];
+  for (int i = tid; i < m; i += blockDim.x) y_out[a0 + r0 + i] = y[i];
   __syncthreads();
   return it;
 }
@@ -693,31 +885,49 @@ __device__ bool qeq_residual(const XrWork& w, const XrFF& ff, const Team& team, 
   double* G = &QW(Q_G, 0);
   const double* DI = &QW(Q_DINV, 0);
   auto noop = [](double*) {};
+  const int gs = row_group(r1 - r0), sub = lane & (gs - 1), gpw = 32 / gs;
   double acc[1] = {0.0};
-  for (int r = r0 + wid; r < r1; r += nw) {
-    const int a = a0 + r;
+  for (int rb = r0 + wid * gpw; rb < r1; rb += nw * gpw) {
+    const int r = rb + lane / gs, a = a0 + r;
     double hx = 0;
-    for (int e = w.cnt[a] + lane; e < w.cnt[a + 1]; e += 32) hx += w.hval[e] * __ldcg(X + w.edge[e].x);
+    if (r < r1) {
+      const int ee = w.cnt[a + 1];
+      int e = w.cnt[a] + sub;
+      for (; e + 3 * gs < ee; e += 4 * gs) {
+        int j[4];
+        double h[4], x[4];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) hx += __shfl_xor_sync(0xffffffffu, hx, o);
-    if (lane == 0) {
+        for (int u = 0; u < 4; ++u) {
+          j[u] = w.edge[e + u * gs].x;
+          h[u] = w.hval[e + u * gs];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) x[u] = __ldcg(X + j[u]);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) hx += h[u] * x[u];
+      }
+      for (; e < ee; e += gs) hx += w.hval[e] * __ldcg(X + w.edge[e].x);
+    }
+    for (int o = gs / 2; o > 0; o >>= 1) hx += __shfl_xor_sync(0xffffffffu, hx, o);
+    if (sub == 0 && r < r1) {
       const int t = w.type[a];
       const double g = hx + atom_prm(ff, t, A_ETA) * X[a] + (adjoint ? w.qrhs[a] : atom_prm(ff, t, A_CHI));
       G[a] = g;
       acc[0] += DI[a] * g;
     }
   }
+  warp_sum_all<1>(acc);
   if (!team_sum<1>(team, w, acc, sh.red, slot, noop)) return false;
   slot = slot == 1 ? 2 : 1;
   const double lam = acc[0] / s1;
   double acc2[1] = {0.0};
-  for (int r = r0 + wid; r < r1; r += nw)
-    if (lane == 0) {
-      const int a = a0 + r;
-      const double g = G[a] - lam;
-      G[a] = g;
-      acc2[0] += DI[a] * g * g;
-    }
+  for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+    const int a = a0 + r;
+    const double g = G[a] - lam;
+    G[a] = g;
+    acc2[0] += DI[a] * g * g;
+  }
+  warp_sum_all<1>(acc2);
   if (!team_sum<1>(team, w, acc2, sh.red, slot, noop)) return false;
   slot = slot == 1 ? 2 : 1;
   *gz_out = acc2[0];
@@ -760,12 +970,16 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
   // The cache holds FP32 values + 16-bit columns (6 B per entry, mixed precision) when the block's
   // rows fit, else FP64 values + columns (10 B), else nothing (rows read from global memory).
   // A block that solves a system of at most 1024 atoms alone keeps every row's FP32 state in shared
-  // memory instead (8 vectors and the row starts, 36 B per atom; the space doubles as the FP64 stage of
-// a fallback).
+  // memory instead, and so does each block of a cluster team for its rows (at most 128) plus the
+  // whole gradient: 4 B per atom of the system and 32 B per own row, and at least the n doubles of
+  // the FP64 stage of a fallback.
   constexpr bool kBlock = std::is_same<Team, BlockTeam>::value;
-  const bool small_rows = kBlock && dyn != nullptr && n <= 1024;
+  constexpr bool kCluster = std::is_same<Team, ClusterTeam>::value;
+  const bool small_rows = (kBlock || kCluster) && dyn != nullptr && n <= 1024 && r1 - r0 <= (kBlock ? 1024 : 128);
   const int stage_n = (dyn != nullptr && (small_rows || n * 8 <= dyn_bytes / 2)) ? n : 0;
-  const size_t stage_bytes = small_rows ? (36 * (size_t)n + 4 + 15) / 16 * 16 : 8 * (size_t)stage_n;
+  const size_t stage_bytes =
+      small_rows ? std::max<size_t>((4 * (size_t)n + 32 * (size_t)(r1 - r0) + 4 + 15) / 16 * 16, 8 * (size_t)n)
+                 : 8 * (size_t)stage_n;
   void* gstage = stage_n > 0 ? dyn : nullptr;
   unsigned char* region = dyn != nullptr ? dyn + stage_bytes : nullptr;
   const long long region_bytes = dyn != nullptr ? dyn_bytes - (long long)stage_bytes : 0;
@@ -786,14 +1000,26 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
   if (cached64) cache_j = reinterpret_cast<unsigned short*>(region + 8 * (size_t)(region_bytes / 10));
   // 1. Jacobi diagonal (eta + self-image shields) of the owned rows, and the start point: the
   //    uniform x0 = Q/n, or the caller's charges of an earlier step (already summing to Q).
-  for (int r = r0 + wid; r < r1; r += nw) {
-    const int a = a0 + r;
+  const int gs = row_group(r1 - r0), sub = lane & (gs - 1), gpw = 32 / gs;
+  for (int rb = r0 + wid * gpw; rb < r1; rb += nw * gpw) {
+    const int r = rb + lane / gs, a = a0 + r;
     double d = 0;
-    for (int e = w.cnt[a] + lane; e < w.cnt[a + 1]; e += 32)
-      if (w.edge[e].x == a) d += w.hval[e];
+    if (r < r1) {
+      const int ee = w.cnt[a + 1];
+      int e = w.cnt[a] + sub;
+      for (; e + 3 * gs < ee; e += 4 * gs) {
+        int j[4];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
-    if (lane == 0) {
+        for (int u = 0; u < 4; ++u) j[u] = w.edge[e + u * gs].x;
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          if (j[u] == a) d += w.hval[e + u * gs];
+      }
+      for (; e < ee; e += gs)
+        if (w.edge[e].x == a) d += w.hval[e];
+    }
+    for (int o = gs / 2; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+    if (sub == 0 && r < r1) {
       DI[a] = 1.0 / (atom_prm(ff, w.type[a], A_ETA) + d);
       X[a] = warm ? w.qguess[a] : x0;
     }
@@ -802,17 +1028,14 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
   // 2. Pre-scaled rows H'_ij = H_ij / D_jj (cached in FP32 or FP64, or in hval in place), row sums
   //    c_i = sum_j H'_ij + eta_i D_ii^-1, and the start gradient g = H x + chi.
   double acc[5] = {0, 0, 0, 0, 0};
-  for (int r = r0 + wid; r < r1; r += nw) {
-    const int a = a0 + r;
-    const int t = w.type[a];
+  for (int rb = r0 + wid * gpw; rb < r1; rb += nw * gpw) {
+    const int r = rb + lane / gs, a = a0 + r;
     double rs = 0, cs = 0, hx = 0;
-    for (int e = w.cnt[a] + lane; e < w.cnt[a + 1]; e += 32) {
-      const int j = w.edge[e].x;
-      const double h = w.hval[e];
-      const double hp = h * __ldcg(DI + j);
+    auto put = [&](int e, int j, double h, double dj, double xj) {
+      const double hp = h * dj;
       rs += h;
       cs += hp;
-      if (warm) hx += h * __ldcg(X + j);
+      if (warm) hx += h * xj;
       if (mixed) {
         cache_j[e - ebeg] = (unsigned short)(j - a0);
         reinterpret_cast<float*>(cache_h)[e - ebeg] = float(hp);
@@ -822,14 +1045,38 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
       } else {
         w.hval[e] = hp;  // scaled in place; hval is not read after the solve
       }
-    }
+    };
+    if (r < r1) {
+      const int ee = w.cnt[a + 1];
+      int e = w.cnt[a] + sub;
+      for (; e + 3 * gs < ee; e += 4 * gs) {
+        int j[4];
+        double h[4], dj[4], xj[4] = {0, 0, 0, 0};
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
+        for (int u = 0; u < 4; ++u) {
+          j[u] = w.edge[e + u * gs].x;
+          h[u] = w.hval[e + u * gs];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          dj[u] = __ldcg(DI + j[u]);
+          if (warm) xj[u] = __ldcg(X + j[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) put(e + u * gs, j[u], h[u], dj[u], xj[u]);
+      }
+      for (; e < ee; e += gs) {
+        const int j = w.edge[e].x;
+        put(e, j, w.hval[e], __ldcg(DI + j), warm ? __ldcg(X + j) : 0.0);
+      }
+    }
+    for (int o = gs / 2; o > 0; o >>= 1) {
       rs += __shfl_xor_sync(0xffffffffu, rs, o);
       cs += __shfl_xor_sync(0xffffffffu, cs, o);
       if (warm) hx += __shfl_xor_sync(0xffffffffu, hx, o);
     }
-    if (lane == 0) {
+    if (sub == 0 && r < r1) {
+      const int t = w.type[a];
       const double eta = atom_prm(ff, t, A_ETA), di = DI[a], chi = adjoint ? w.qrhs[a] : atom_prm(ff, t, A_CHI);
       const double gu = x0 * (rs + eta) + chi;
       const double g = warm ? hx + eta * X[a] + chi : gu;
@@ -843,6 +1090,7 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
       acc[4] += di * gu * gu;
     }
   }
+  warp_sum_all<5>(acc);
   if (!team_sum<5>(team, w, acc, smem, 0, noop)) return;
   const double s1 = acc[0];
   // 3. Project the start gradient explicitly (g - lambda with lambda = <D^-1, g> / <D^-1, 1>) and take
@@ -851,8 +1099,8 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
   //    atoms. The uniform start's projected norm sets the convergence scale.
   const double lam0 = acc[1] / s1, lamu = acc[3] / s1;
   double acc2[3] = {0, 0, 0};  // <D^-1, g~^2>, <D^-1, g~_u^2>, <D^-1, g~>
-  for (int r = r0 + wid; r < r1; r += nw)
-    if (lane == 0) {
+  for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+    {
       const int a = a0 + r;
       const double di = DI[a];
       const double gt = G[a] - lam0;
@@ -862,6 +1110,8 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
       acc2[1] += di * gut * gut;
       acc2[2] += di * gt;
     }
+  }
+  warp_sum_all<3>(acc2);
   if (!team_sum<3>(team, w, acc2, smem, 1, noop)) return;
   const double tol2 = w.cg_tol * w.cg_tol;
   const double gfloor = 1e-28 * fmax(acc[2], acc[4]);
@@ -875,7 +1125,7 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
     // 4a. Iterative refinement around FP32 solves of the correction problem.
     const size_t A = w.A;
     QeqVecs<float> v32{F, F + A, F + 2 * A, F + 3 * A, F + 4 * A, F + 5 * A, F + 6 * A, F + 7 * A};
-    for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+    for (int r = r0 + threadIdx.x; r < r1 && !small_rows; r += blockDim.x) {
       const int a = a0 + r;
       F[5 * A + a] = float(DI[a]);
       F[6 * A + a] = float(atom_prm(ff, w.type[a], A_ETA) * DI[a]);
@@ -885,32 +1135,39 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
                          reinterpret_cast<float*>(gstage)};
     for (int sweep = 0; sweep < 8; ++sweep) {
       if (!(gz > target) || !(gz > gfloor) || n < 2) break;
-      for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
-        const int a = a0 + r;
-        v32.g[a] = float(G[a]);
-        v32.p[a] = 0.0f;
-        v32.hp[a] = 0.0f;
-        v32.y[a] = 0.0f;
+      if (!small_rows) {  // the shared-memory solver reads the FP64 gradient itself (published by the
+                          // reduction that ended the residual)
+        for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+          const int a = a0 + r;
+          v32.g[a] = float(G[a]);
+          v32.p[a] = 0.0f;
+          v32.hp[a] = 0.0f;
+          v32.y[a] = 0.0f;
+        }
+        if (!team.sync(w)) return;
       }
-      if (!team.sync(w)) return;
       // the correction's own projected norm starts at gz; 1e-10 of it (1e-5 in norm) per sweep,
       // and no further than a hundredth of the final target
       const double stop = fmax(1e-10 * gz, 0.01 * target);
-      const int it = small_rows
-                         ? qeq_cg_block32(w, ff, sh, a0, n, reinterpret_cast<float*>(dyn), M32, v32.y, s1, gz, stop, 400)
-                         : qeq_cg<Team, float>(w, ff, team, sh, a0, n, r0, r1, v32, M32, s1, gz, stop, 0.0, 400, false, slot);
+      int it;
+      if constexpr (kBlock || kCluster) {
+        it = small_rows ? qeq_cg_rows32(w, ff, team, sh, a0, n, r0, r1, M32, v32.y, s1, gz, stop, 400)
+                        : qeq_cg<Team, float>(w, ff, team, sh, a0, n, r0, r1, v32, M32, s1, gz, stop, 0.0, 400, false, slot);
+      } else {
+        it = qeq_cg<Team, float>(w, ff, team, sh, a0, n, r0, r1, v32, M32, s1, gz, stop, 0.0, 400, false, slot);
+      }
       if (it < 0) return;
       iters += it;
       // x += y, then restore sum x = Q exactly: the FP32 step keeps sum y = 0 only to FP32 rounding,
       // and the residual must be taken at a point on the constraint (a uniform shift added after
       // convergence would change the projected gradient)
       double sx[1] = {0.0};
-      for (int r = r0 + wid; r < r1; r += nw)
-        if (lane == 0) {
-          const int a = a0 + r;
-          X[a] += double(v32.y[a]);
-          sx[0] += X[a];
-        }
+      for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+        const int a = a0 + r;
+        X[a] += double(v32.y[a]);
+        sx[0] += X[a];
+      }
+      warp_sum_all<1>(sx);
       if (!team_sum<1>(team, w, sx, smem, slot, noop)) return;
       slot = slot == 1 ? 2 : 1;
       const double shift = (Q - sx[0]) / n;
@@ -948,8 +1205,8 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
   }
   // 5. Final charges; the constraint is restored exactly against accumulated rounding.
   double sx[1] = {0.0};
-  if (lane == 0)
-    for (int r = r0 + wid; r < r1; r += nw) sx[0] += X[a0 + r];
+  for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) sx[0] += X[a0 + r];
+  warp_sum_all<1>(sx);
   if (!team_sum<1>(team, w, sx, smem, 3, noop)) return;
   const double shift = (Q - sx[0]) / n;
   for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
@@ -1007,6 +1264,54 @@ __global__ void __launch_bounds__(1024, 1) k_qeq_grid(XrWork w, XrFF ff, const i
     __syncthreads();
   }
   qeq_small_systems(w, ff, small, nsmall, w.barrier + nteam, adjoint, sh, dyn);
+}
+
+// Batch solver on thread-block clusters of kQeqCluster blocks, one block per SM: the systems of
+// `big` (largest first) are each solved by a whole cluster, rows split over its blocks, with
+// reductions through distributed shared memory; then every block takes systems of `small` alone.
+// A cluster's leader draws the next big system from a counter and the draw reaches the other
+// blocks through an exchange. Ordinary launch: no block waits on a block of another cluster.
+__global__ void __launch_bounds__(1024, 1) k_qeq_cluster(XrWork w, XrFF ff, const int* big, int nbig, const int* small,
+                                                         int nsmall, int adjoint) {
+  __shared__ QeqShared sh;
+  extern __shared__ __align__(16) unsigned char dyn[];
+  const unsigned rank = cluster_rank(), nb = cluster_size();
+  if (threadIdx.x < 16) (&sh.cseq[0][0])[threadIdx.x] = 0u;
+  cluster_barrier_all();  // every block's sequence words are zero before the first remote write
+  ClusterTeam team{&sh.cred[0][0][0], &sh.cseq[0][0], (int)nb, (int)rank};
+  auto noop = [](double*) {};
+  for (;;) {
+    double v[1] = {0.0};
+    if (threadIdx.x < 32) {
+      double d = 0.0;
+      if (rank == 0 && threadIdx.x == 0) d = (double)atomicAdd(w.barrier, 1u);
+      v[0] = __shfl_sync(0xffffffffu, d, 0);
+    }
+    if (!team.template reduce<1>(w, v, sh.red, 0, noop)) break;
+    const int k = (int)v[0];
+    if (k >= nbig) break;
+    const XrSystem& S = w.sys[big[k]];
+    // rows split so that every block holds about the same number of matrix entries
+    const int* cnt = w.cnt + S.atom_off;
+    const long long E = cnt[S.natoms] - cnt[0];
+    auto split = [&](int q) {
+      const long long target = cnt[0] + E * q / (int)nb;
+      int lo = 0, hi = S.natoms;
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (cnt[mid] < target) lo = mid + 1;
+        else hi = mid;
+      }
+      return q == (int)nb ? S.natoms : lo;
+    };
+    const int r0 = split((int)rank), r1 = split((int)rank + 1);
+    qeq_solve(w, ff, team, S.atom_off, S.natoms, r0, r1, adjoint ? 0.0 : S.total_charge, !adjoint && S.has_guess != 0,
+              sh, dyn, kQeqMaxDyn, adjoint != 0);
+    __syncthreads();
+    if (*(volatile int*)w.status & XR_S_BARRIER) break;
+  }
+  qeq_small_systems(w, ff, small, nsmall, w.barrier + 1, adjoint, sh, dyn);
+  cluster_barrier_all();  // no block leaves while a peer may still write into its shared memory
 }
 
 // Fallback without cooperative launch: one block per system, no shared-memory row cache.
@@ -1216,6 +1521,48 @@ int xr_qeq_coop_blocks_per_sm() {
   int nb = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_qeq_grid, 1024, kQeqMaxDyn);
   return nb;
+}
+
+namespace {
+cudaLaunchConfig_t cluster_config(int nblocks, cudaStream_t st, cudaLaunchAttribute* attr) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(nblocks);
+  cfg.blockDim = dim3(1024);
+  cfg.dynamicSmemBytes = kQeqMaxDyn;
+  cfg.stream = st;
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = kQeqCluster;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cfg;
+}
+}  // namespace
+
+int xr_qeq_max_clusters() {
+  if (cudaFuncSetAttribute(k_qeq_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, kQeqMaxDyn) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  cudaLaunchAttribute attr[1];
+  cudaLaunchConfig_t cfg = cluster_config(kQeqCluster, nullptr, attr);
+  int n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, (void*)k_qeq_cluster, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
+int xr_launch_qeq_cluster(const XrWork& w, const XrFF& ff, cudaStream_t st, int nblocks, const int* list, int nbig,
+                          int nsmall, bool adjoint) {
+  cudaMemsetAsync(w.barrier, 0, 2 * sizeof(unsigned), st);  // big-system and small-system counters
+  cudaLaunchAttribute attr[1];
+  cudaLaunchConfig_t cfg = cluster_config(nblocks, st, attr);
+  const int* small = list + nbig;
+  int adj = adjoint ? 1 : 0;
+  return (int)cudaLaunchKernelEx(&cfg, k_qeq_cluster, w, ff, list, nbig, small, nsmall, adj);
 }
 
 // Returns 0 on success or a CUDA error code from the launch. With nblocks > 0 the cooperative
