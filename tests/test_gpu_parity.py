@@ -203,6 +203,29 @@ def test_batch_matches_single_evaluations():
         np.testing.assert_allclose(rb.charges, r1.charges, atol=1e-11, rtol=0)
 
 
+def test_batch_solver_layouts_agree():
+    """The same systems through every QEq layout: alone, a 1,000-atom periodic box is solved by a
+    grid-wide team and a 300-atom cluster by one thread-block cluster; in a batch the box goes to a
+    cluster whose blocks' FP32 rows exceed shared memory (rows from global memory), and a small
+    system to a single block. Charges agree to the solver tolerance, energies and forces to rounding."""
+    from xreac_gb300 import workloads
+
+    box = workloads.water_box(n_mol=334, box=21.6, seed=21)
+    clus = workloads.water_cluster(n_mol=100, box=14.0, seed=5)
+    small = workloads.water_cluster(n_mol=8, box=6.0, seed=5)
+    c = calc("ffield.reax.HO.2015")
+    systems = [dict(symbols=s.symbols, positions=s.positions, cell=s.cell, pbc=s.pbc) for s in (box, clus, small)]
+    assert len(box.symbols) == 1002 and len(clus.symbols) == 300
+    batch = c.evaluate_many(systems)
+    for s, rb in zip(systems, batch):
+        r1 = c.evaluate(**s)
+        n = len(s["symbols"])
+        assert rb.energy == pytest.approx(r1.energy, abs=1e-9 * n)
+        np.testing.assert_allclose(rb.charges, r1.charges, atol=1e-10, rtol=0)
+        np.testing.assert_allclose(rb.forces, r1.forces, atol=1e-8, rtol=0)
+        assert abs(rb.charges.sum()) < 1e-10
+
+
 def test_symmetries_cluster():
     """Rotation, translation and permutation (tests/test_calculator.py:77-90 of the reference)."""
     g = load_golden("zno_cluster20")

@@ -76,6 +76,16 @@ class Evaluation:
         """Name of the derivative used for ``forces``."""
         return "charge_response" if self.full_derivative else "fixed_charge"
 
+    def __getattr__(self, name):
+        # Only reached for a field that is not set yet: an evaluation of a batch makes its array
+        # fields (views of the batch's result arrays) on first access.
+        batch = self.__dict__.get("_batch")
+        if batch is None or name not in _BATCH_FIELDS:
+            raise AttributeError(name)
+        value = batch.field(name, self.__dict__["_index"])
+        object.__setattr__(self, name, value)
+        return value
+
     @property
     def bond_orders(self):
         n = len(self.charges)
@@ -84,6 +94,37 @@ class Evaluation:
         np.add.at(dense, (i, j), bo)
         np.add.at(dense, (j, i), bo)
         return dense
+
+
+# fields without a class default (a class attribute would shadow __getattr__)
+_BATCH_FIELDS = frozenset(("forces", "charges", "components", "total_bond_orders", "lone_pairs", "bond_counts",
+                           "dipole"))
+
+
+class _BatchResults:
+    """The result arrays of one ``xr_eval_batch`` call; the fields of its k-th system are views."""
+
+    __slots__ = ("energy", "forces", "per_atom", "counts", "dipole", "offsets")
+
+    def __init__(self, energy, forces, per_atom, counts, dipole, offsets):
+        self.energy, self.forces, self.per_atom, self.counts = energy, forces, per_atom, counts
+        self.dipole, self.offsets = dipole, offsets
+
+    def field(self, name, k):
+        a0, a1 = self.offsets[k], self.offsets[k + 1]
+        if name == "forces":
+            return self.forces[a0:a1]
+        if name == "charges":
+            return self.per_atom[0, a0:a1]
+        if name == "total_bond_orders":
+            return self.per_atom[1, a0:a1]
+        if name == "lone_pairs":
+            return self.per_atom[2, a0:a1]
+        if name == "bond_counts":
+            return self.counts[a0:a1].astype(np.int64)
+        if name == "dipole":
+            return self.dipole[k]
+        return dict(zip(COMPONENTS, self.energy[k, :14].tolist()))  # components
 
 
 # Pair-table columns (xreac_gb300.forcefield.PAIR_COLUMNS order) with a parameter gradient, and the
@@ -359,38 +400,24 @@ class Calculator:
                                  res_arr.ctypes.data_as(_RESULT_P))
         if code != nat.XR_OK:
             self._raise(code)
-        counts64 = counts.astype(np.int64)
         bi, bj, bS, bbo = self._bonds(-1)
         cut = np.searchsorted(bi, offsets)  # bonds are grouped by system, in pair order
         if len(bi):
             shift = np.repeat(a0s.astype(np.int32), np.diff(cut))
             bi -= shift
             bj -= shift
+        held = _BatchResults(energy, forces, per_atom, counts, dipole, offsets.tolist())
         cut = cut.tolist()
-        offs = offsets.tolist()
         etot = energy[:, 14].tolist()
-        comps = energy[:, :14].tolist()
-        charges_v, tbo_v, lp_v = per_atom
         results = []
         new = object.__new__
         for k in range(n_sys):
-            a0, a1 = offs[k], offs[k + 1]
+            # a frozen dataclass: set without the per-field checks; the array fields follow on access
             c0, c1 = cut[k], cut[k + 1]
-            ev = new(Evaluation)  # a frozen dataclass: fields set without the per-field setattr checks
-            ev.__dict__.update(
-                energy=etot[k],
-                forces=forces[a0:a1],
-                charges=charges_v[a0:a1],
-                components=dict(zip(COMPONENTS, comps[k])),
-                full_derivative=full_derivative,
-                total_bond_orders=tbo_v[a0:a1],
-                lone_pairs=lp_v[a0:a1],
-                bond_counts=counts64[a0:a1],
-                dipole=dipole[k],
-                cell_repetitions=reps[k],
-                neighbor_backend=backend,
-                bonds=(bi[c0:c1], bj[c0:c1], bS[c0:c1], bbo[c0:c1]),
-            )
+            ev = new(Evaluation)
+            ev.__dict__.update(energy=etot[k], full_derivative=full_derivative, cell_repetitions=reps[k],
+                               neighbor_backend=backend, bonds=(bi[c0:c1], bj[c0:c1], bS[c0:c1], bbo[c0:c1]),
+                               _batch=held, _index=k)
             results.append(ev)
         return results
 

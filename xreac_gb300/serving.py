@@ -22,7 +22,6 @@ from __future__ import annotations
 import collections
 import threading
 import time
-from concurrent.futures import Future
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -48,7 +47,44 @@ class Request:
         return len(self.symbols)
 
 
-@dataclass
+class Pending:
+    """Handle of a submitted request. ``result()`` waits for its batch and returns the
+    :class:`Served` (or raises the request's error); ``done()`` tells whether it has finished.
+
+    One condition variable of the server wakes all waiters once per finished batch, rather than
+    one synchronisation object per request."""
+
+    __slots__ = ("_cv", "_value", "_error", "_done")
+
+    def __init__(self, cv):
+        self._cv = cv
+        self._value = None
+        self._error = None
+        self._done = False
+
+    def done(self):
+        return self._done
+
+    def result(self, timeout=None):
+        if not self._done:
+            with self._cv:
+                if not self._cv.wait_for(self.done, timeout):
+                    raise TimeoutError("request not finished")
+        if self._error is not None:
+            raise self._error
+        return self._value
+
+    def exception(self, timeout=None):
+        try:
+            self.result(timeout)
+        except TimeoutError:
+            raise
+        except Exception as err:  # noqa: BLE001 - the request's own error
+            return err
+        return None
+
+
+@dataclass(slots=True)
 class Served:
     """Result of one request: the evaluation plus its timing."""
 
@@ -101,6 +137,7 @@ class Server:
         self.warm_start = warm_start
         self._queues = {name: collections.deque() for name in self.force_fields}
         self._cv = threading.Condition()
+        self._done_cv = threading.Condition()  # signalled once per finished batch
         self._closed = False
         self._charges = {}  # session -> last charges
         self._charges_lock = threading.Lock()
@@ -122,10 +159,10 @@ class Server:
 
     # ------------------------------------------------------------------ client side
     def submit(self, request, arrival=None):
-        """Admit a request; returns a Future that resolves to a :class:`Served`."""
+        """Admit a request; returns a :class:`Pending` that resolves to a :class:`Served`."""
         if request.force_field not in self._queues:
             raise ValueError(f"Unknown force field {request.force_field!r}")
-        fut = Future()
+        fut = Pending(self._done_cv)
         request.arrival = time.perf_counter() if arrival is None else arrival
         with self._cv:
             if self._closed:
@@ -230,9 +267,12 @@ class Server:
         nb = len(batch)
         for (req, fut), res in zip(batch, results):
             if isinstance(res, Exception):
-                fut.set_exception(res)
+                fut._error = res
             else:
-                fut.set_result(Served(res, req.arrival, done, nb, t0))
+                fut._value = Served(res, req.arrival, done, nb, t0)
+            fut._done = True
+        with self._done_cv:
+            self._done_cv.notify_all()
 
 
 def replay(server, requests, arrivals=None, speedup=1.0):
