@@ -12,6 +12,7 @@ from __future__ import annotations
 
 import math
 from dataclasses import dataclass, field
+from numbers import Real
 
 import numpy as np
 
@@ -133,6 +134,18 @@ GRADIENT_PAIR_COLUMNS = ("De_s", "De_p", "De_pp", "p_be1", "p_be2", "p_ovun1", "
                          "p_bo5", "p_bo6", "r_s", "r_p", "r_pp", "D", "alpha", "gamma_w", "r_vdW", "rcore", "ecore",
                          "acore")
 ANGLE_PARAMETERS = ("theta_00", "p_val1", "p_val2", "p_coa1", "p_val7", "p_pen1", "p_val4")
+
+
+@dataclass
+class Relaxation:
+    """Result of :meth:`Calculator.relax` (src/xreac/calculator.py:37-42): final positions, the
+    evaluation at them, whether the force tolerance was reached, iterations taken, a message."""
+
+    positions: np.ndarray
+    evaluation: Evaluation
+    converged: bool
+    iterations: int
+    message: str
 
 
 @dataclass(frozen=True)
@@ -433,6 +446,77 @@ class Calculator:
         lib.xr_get_bonds(h, index, nat.ptr(i, nat.c_int), nat.ptr(j, nat.c_int), nat.ptr(S, nat.c_int),
                          nat.ptr(bo, nat.c_double), m, nat.byref(count))
         return i, j, S, bo
+
+    def relax(self, symbols, positions, *, force_tolerance=1e-4, max_iterations=500, total_charge=0, cell=None,
+              pbc=None, backend="ase"):
+        """Relax with fixed-charge forces by FIRE (src/xreac/calculator.py:167-246); the cell stays fixed.
+
+        Convergence requires the largest absolute Cartesian force component to be at most
+        ``force_tolerance`` (kcal/mol/A). ``backend="native"`` runs xreac's own FIRE: unit masses,
+        dt = 0.02 growing by 1.1 up to 0.2 after more than five steps with positive power, halved
+        (and the velocity reset) otherwise, mixing alpha = 0.1 decaying by 0.99, and the largest
+        atomic step capped at 0.1 A (Bitzek et al., Phys. Rev. Lett. 97, 170201, 2006). Every step
+        is one device evaluation whose QEq starts from the previous step's charges; the returned
+        evaluation is a plain one at the final positions, identical to :meth:`evaluate` there.
+        ``backend="ase"`` runs ASE's FIRE through :class:`xreac_gb300.ase.ReaxFFCalculator`,
+        which needs ASE installed, as xreac's does.
+        """
+        symbols, x, _, _ = validate_input(symbols, positions, total_charge, cell, pbc)
+        if isinstance(force_tolerance, bool) or not isinstance(force_tolerance, Real) \
+                or not np.isfinite(force_tolerance) or force_tolerance <= 0:
+            raise ValueError("force_tolerance must be positive and finite")
+        if isinstance(max_iterations, bool) or not isinstance(max_iterations, (int, np.integer)) or max_iterations < 1:
+            raise ValueError("max_iterations must be a positive integer")
+        if backend not in ("ase", "native"):
+            raise ValueError("backend must be 'ase' or 'native'")
+        kw = dict(total_charge=total_charge, cell=cell, pbc=pbc)
+        if backend == "ase":
+            from .ase import relax_with_ase
+
+            flags, _ = boundary(cell, pbc)
+            x, result, converged, iterations = relax_with_ase(self, symbols, x, force_tolerance, max_iterations,
+                                                              cell=cell, pbc=flags, total_charge=total_charge)
+            message = "Fixed-charge force tolerance reached" if converged else "Maximum relaxation iterations reached"
+            return Relaxation(x, result, converged, iterations, message)
+        velocity = np.zeros_like(x)
+        dt, dt_max, alpha = 0.02, 0.2, 0.1
+        positive_steps = 0
+        result = self.evaluate(symbols, x, **kw)
+        warm = result
+        iteration = 0
+        while True:
+            force = warm.forces
+            if np.max(np.abs(force)) <= force_tolerance:
+                if warm is not result:  # confirm on the plain evaluation that is returned
+                    result = self.evaluate(symbols, x, **kw)
+                    warm = result
+                    continue
+                return Relaxation(x, result, True, iteration, "Fixed-charge force tolerance reached")
+            if iteration == max_iterations:
+                if warm is not result:
+                    result = self.evaluate(symbols, x, **kw)
+                return Relaxation(x, result, False, max_iterations, "Maximum relaxation iterations reached")
+            power = float(np.sum(velocity * force))
+            if power > 0:
+                velocity = (1 - alpha) * velocity + alpha * np.linalg.norm(velocity) / np.linalg.norm(force) * force
+                positive_steps += 1
+                if positive_steps > 5:
+                    dt = min(dt * 1.1, dt_max)
+                    alpha *= 0.99
+            else:
+                velocity.fill(0.0)
+                positive_steps = 0
+                alpha = 0.1
+                if iteration > 0:
+                    dt *= 0.5
+            velocity += dt * force
+            step = dt * velocity
+            largest = float(np.max(np.linalg.norm(step, axis=1)))
+            if largest > 0.1:
+                step *= 0.1 / largest
+            x = x + step
+            iteration += 1
+            warm = self.evaluate(symbols, x, initial_charges=warm.charges, **kw)
 
     def neighbor_list(self, index=0):
         """Canonical directed neighbour list ``(i, j, S)`` of the last evaluation (system ``index``)."""
