@@ -413,7 +413,8 @@ struct QeqRows {
 struct QeqShared {
   double red[kRedSmem];
   double sc_lam, sc_alpha, sc_step, sc_beta;
-  float sf_lam, sf_alpha, sf_step, sf_beta, sf_gz;
+  float sf_lam, sf_alpha, sf_step, sf_beta, sf_gz, sf_stop;
+  double sd_s1w;  // <1, M^-1 1> of the FP32 row solver's block-Jacobi preconditioner
   int sc_next;  // the next small system of the block (work sharing)
   double cred[2][8][8];  // cluster team: partials pushed by the blocks of the cluster
   unsigned cseq[2][8];   // cluster team: exchange number of each pushed entry
@@ -730,30 +731,261 @@ __device__ inline bool team_sum2f(const Team& team, const XrWork& w, float a, fl
   return true;
 }
 
-// The FP32 solve of a refinement sweep with every vector in shared memory, for a system of at most
-// 1024 atoms solved by one block (rows [0, n)) or by a thread-block cluster (this block's rows
-// [r0, r1), at most 128). The block holds the whole gradient g (n values, indexed by row of the
-// system) and the state of its own rows: p, Hp, y, D^-1, eta D^-1, c, the shifted gradient and the
-// row starts. A group of lanes per row forms the product and its first lane the row's first
-// update, a thread per row the second; the scalars are FP32. In a cluster, each
-// block writes its rows' new gradient into every other block's copy (distributed shared memory)
-// before the second reduction, whose exchange publishes it. Same projected PCG as qeq_cg. The
-// correction y of the own rows is written to y_out (global, indexed by atom).
-// The vectors start at the beginning of the kernel's dynamic shared memory; naming it here (rather
-// than taking a pointer) lets the compiler use shared-memory loads and stores, and the function is
-// kept out of line so that its loops do not share registers with the rest of the solve.
+// Shared-memory layout of the FP32 row solver, at the start of the kernel's dynamic shared memory,
+// for a system of n atoms of which this block owns m rows (r0 .. r1):
+//   yt[n4]  D y for every row of the system (y = M^-1 g), the vector the product gathers; n4 = n
+//           rounded up to a multiple of 4
+//   own rows, m floats each: p, Hp, x (the correction), D_ii, eta D^-1, c = H w, w = M^-1 1, g, y
+//   binv[8m] row r of its group's inverse block (columns: the group's rows in order)
+//   rp[m + 1] row starts relative to the cache; first[m], size[m] the group of each row (16-bit)
+// M is block-Jacobi: groups of at most 8 consecutive own rows whose atoms are joined by distances
+// below 1.3 A (molecules), each block H restricted to the group. One-row groups are Jacobi.
+constexpr int kGroupMax = 8;
+constexpr double kGroupBond = 1.3;
+
+struct Rows32 {
+  float *yt, *p, *hp, *x, *dd, *etadi, *cw, *wv, *gl, *yl, *binv;
+  int* rp;
+  unsigned short *first, *size;
+  __device__ Rows32(unsigned char* base, int n, int m) {
+    float* f = reinterpret_cast<float*>(base);
+    yt = f;
+    p = f + (n + 3) / 4 * 4;
+    hp = p + m;
+    x = hp + m;
+    dd = x + m;
+    etadi = dd + m;
+    cw = etadi + m;
+    wv = cw + m;
+    gl = wv + m;
+    yl = gl + m;
+    binv = yl + m;
+    rp = reinterpret_cast<int*>(binv + kGroupMax * m);
+    first = reinterpret_cast<unsigned short*>(rp + m + 1);
+    size = first + m;
+  }
+  // FP64 scratch of the setup (8 per row), over p .. binv (68 B per row, 16-byte aligned start)
+  __device__ double* scratch() const { return reinterpret_cast<double*>(p); }
+};
+
+__host__ __device__ constexpr size_t rows32_bytes(int n, int m) {
+  return (4 * (size_t)((n + 3) / 4 * 4) + 4 * (size_t)(9 + kGroupMax) * m + 4 * (size_t)(m + 1) + 4 * (size_t)m + 15) /
+         16 * 16;
+}
+
+// LU factorisation with partial pivoting of the k x k block a (in place; row r of the factors
+// holds original row piv[r]); false when a pivot vanishes against the block's scale.
+__device__ inline bool small_lu(double (&a)[kGroupMax][kGroupMax], int (&piv)[kGroupMax], int k) {
+  double scale = 0.0;
+  for (int r = 0; r < k; ++r) {
+    piv[r] = r;
+    for (int c = 0; c < k; ++c) scale = fmax(scale, fabs(a[r][c]));
+  }
+  for (int c = 0; c < k; ++c) {
+    int best = c;
+    for (int r = c + 1; r < k; ++r)
+      if (fabs(a[r][c]) > fabs(a[best][c])) best = r;
+    if (!(fabs(a[best][c]) > 1e-12 * scale)) return false;
+    if (best != c) {
+      for (int q = 0; q < k; ++q) {
+        const double t = a[c][q];
+        a[c][q] = a[best][q];
+        a[best][q] = t;
+      }
+      const int t = piv[c];
+      piv[c] = piv[best];
+      piv[best] = t;
+    }
+    for (int r = c + 1; r < k; ++r) {
+      const double f = a[r][c] / a[c][c];
+      a[r][c] = f;
+      for (int q = c + 1; q < k; ++q) a[r][q] -= f * a[c][q];
+    }
+  }
+  return true;
+}
+
+// Column c of the inverse from the factors of small_lu, into x.
+__device__ inline void small_lu_column(const double (&a)[kGroupMax][kGroupMax], const int (&piv)[kGroupMax], int k,
+                                       int c, double (&x)[kGroupMax]) {
+  for (int r = 0; r < k; ++r) {  // L y = P e_c
+    double t = piv[r] == c ? 1.0 : 0.0;
+    for (int q = 0; q < r; ++q) t -= a[r][q] * x[q];
+    x[r] = t;
+  }
+  for (int r = k - 1; r >= 0; --r) {  // U x = y
+    double t = x[r];
+    for (int q = r + 1; q < k; ++q) t -= a[r][q] * x[q];
+    x[r] = t / a[r][r];
+  }
+}
+
+// Setup of the row solver's preconditioner and constants, once per solve (after the Jacobi diagonal
+// and the row cache are in place): the groups, their inverse blocks, w = M^-1 1, D, eta D^-1, the
+// row starts, s1 = <1, w> (team total, into sh.sd_s1w) and c = H w. Returns false when a team
+// exchange gave up.
 template <class Team>
-__device__ __noinline__ int qeq_cg_rows32(const XrWork& w, const XrFF& ff, const Team& team, QeqShared& sh, int a0,
-                                          int n, int r0, int r1, const QeqMatrix<float>& M, float* y_out, double s1d,
-                                          double gz_start, double stop, int max_it) {
+__device__ __noinline__ bool qeq_rows32_setup(const XrWork& w, const XrFF& ff, const Team& team, QeqShared& sh, int a0,
+                                              int n, int r0, int r1, const QeqMatrix<float>& M) {
   extern __shared__ __align__(16) unsigned char qeq_dyn[];
   constexpr bool kCluster = std::is_same<Team, ClusterTeam>::value;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5, tid = threadIdx.x;
   const int m = r1 - r0;
-  float* const rows = reinterpret_cast<float*>(qeq_dyn);
-  float *g = rows, *p = rows + n, *hp = p + m, *y = hp + m, *di = y + m, *etadi = di + m, *cr = etadi + m,
-        *gown = cr + m;  // gown: the own rows' gradient minus the multiplier, between the two updates
-  int* rp = reinterpret_cast<int*>(gown + m);  // row starts relative to the cache
+  Rows32 R(qeq_dyn, n, m);
+  const double* DI = &QW(Q_DINV, 0);
+  const int gs = row_group(m), sub = lane & (gs - 1), gpw = 32 / gs;
+  // 1. for every own row, the latest earlier own row bonded to it (distance below kGroupBond)
+  int* prev = reinterpret_cast<int*>(R.binv);  // scratch until the inverses are written
+  for (int ib = wid * gpw; ib < m; ib += nw * gpw) {
+    const int i = ib + lane / gs;
+    int best = -1;
+    if (i < m) {
+      const int a = a0 + r0 + i;
+      for (int e = w.cnt[a] + sub; e < w.cnt[a + 1]; e += gs) {
+        const int c = w.edge[e].x - a0 - r0;
+        if (c >= 0 && c < i && c > best && __ldg(w.p_r + w.edge_pair[e]) < kGroupBond) best = c;
+      }
+    }
+    for (int o = gs / 2; o > 0; o >>= 1) best = max(best, __shfl_xor_sync(0xffffffffu, best, o));
+    if (sub == 0 && i < m) prev[i] = best;
+  }
+  __syncthreads();
+  // 2. groups: runs of consecutive rows, each bonded to an earlier row of its run, at most kGroupMax
+  if (tid == 0) {
+    int start = 0;
+    for (int i = 0; i < m; ++i) {
+      if (!(i > start && prev[i] >= start && i - start < kGroupMax)) start = i;
+      R.first[i] = (unsigned short)start;
+    }
+    int end = m;
+    for (int i = m - 1; i >= 0; --i) {
+      R.size[i] = (unsigned short)(end - R.first[i]);
+      if (R.first[i] == i) end = i;
+    }
+  }
+  __syncthreads();
+  // 3. each row of a group of two or more: its row of the group's block (FP64), into the scratch
+  double* B = R.scratch();
+  for (int ib = wid * gpw; ib < m; ib += nw * gpw) {
+    const int i = ib + lane / gs;
+    const int k = i < m ? R.size[i] : 1;
+    if (__all_sync(0xffffffffu, k < 2)) continue;
+    double acc[kGroupMax];
+#pragma unroll
+    for (int b = 0; b < kGroupMax; ++b) acc[b] = 0.0;
+    if (i < m && k > 1) {
+      const int f = R.first[i], a = a0 + r0 + i;
+      for (int e = w.cnt[a] + sub; e < w.cnt[a + 1]; e += gs) {
+        const int b = w.edge[e].x - a0 - r0 - f;
+        if (b >= 0 && b < k && b != i - f) {
+          const double h = w.hval[e];
+#pragma unroll
+          for (int q = 0; q < kGroupMax; ++q)
+            if (q == b) acc[q] += h;
+        }
+      }
+    }
+#pragma unroll
+    for (int b = 0; b < kGroupMax; ++b)
+      for (int o = gs / 2; o > 0; o >>= 1) acc[b] += __shfl_xor_sync(0xffffffffu, acc[b], o);
+    if (sub == 0 && i < m && k > 1) {
+      const int f = R.first[i];
+#pragma unroll
+      for (int b = 0; b < kGroupMax; ++b) B[kGroupMax * i + b] = b == i - f ? 1.0 / DI[a0 + r0 + i] : acc[b];
+    }
+  }
+  __syncthreads();
+  // 4. inverse blocks: the first row of each group reads its block, then (after everyone has read)
+  //    factorises it and writes the inverse rows and w = M^-1 1 of its rows; a singular block falls
+  //    back to Jacobi
+  double blk[kGroupMax][kGroupMax];
+  int lead_k = 0, lead_f = -1;
+  for (int i = tid; i < m; i += blockDim.x)
+    if (R.first[i] == i && R.size[i] > 1) {
+      lead_f = i;
+      lead_k = R.size[i];
+      for (int r = 0; r < lead_k; ++r)
+        for (int c = 0; c < lead_k; ++c) blk[r][c] = B[kGroupMax * (i + r) + c];
+      break;  // at most one group per thread: blockDim >= m and group starts are distinct rows
+    }
+  __syncthreads();
+  if (lead_f >= 0) {
+    int piv[kGroupMax];
+    const bool ok = small_lu(blk, piv, lead_k);
+    double wsum[kGroupMax], col[kGroupMax];
+    for (int r = 0; r < kGroupMax; ++r) wsum[r] = 0.0;
+    for (int c = 0; c < kGroupMax; ++c) {
+      if (c < lead_k && ok) small_lu_column(blk, piv, lead_k, c, col);
+      for (int r = 0; r < lead_k; ++r) {
+        const double v = c >= lead_k ? 0.0 : ok ? col[r] : (c == r ? DI[a0 + r0 + lead_f + r] : 0.0);
+        R.binv[kGroupMax * (lead_f + r) + c] = float(v);
+        wsum[r] += v;
+      }
+    }
+    for (int r = 0; r < lead_k; ++r) R.wv[lead_f + r] = float(wsum[r]);
+  }
+  double s1[1] = {0.0};
+  for (int i = tid; i < m; i += blockDim.x) {
+    const int a = a0 + r0 + i;
+    const double di = DI[a];
+    if (R.size[i] < 2) {
+      R.binv[kGroupMax * i] = float(di);
+      for (int c = 1; c < kGroupMax; ++c) R.binv[kGroupMax * i + c] = 0.0f;
+      R.wv[i] = float(di);
+    }
+    R.dd[i] = float(1.0 / di);
+    R.etadi[i] = float(atom_prm(ff, w.type[a], A_ETA) * di);
+    R.rp[i] = w.cnt[a] - M.ebeg;
+  }
+  if (tid == 0) R.rp[m] = w.cnt[a0 + r1] - M.ebeg;
+  __syncthreads();
+  for (int i = tid; i < m; i += blockDim.x) s1[0] += double(R.wv[i]);
+  warp_sum_all<1>(s1);
+  auto keep = [&](double* t) { sh.sd_s1w = t[0]; };
+  if (!team_sum<1>(team, w, s1, sh.red, 0, keep)) return false;
+  // 5. c = H w: D w of the own rows into every block's yt, then the product over the cached rows
+  unsigned remote = 0;
+  if constexpr (kCluster) remote = smem_u32(R.yt + r0);
+  for (int i = tid; i < m; i += blockDim.x) {
+    const float v = R.wv[i] * R.dd[i];
+    R.yt[r0 + i] = v;
+    if constexpr (kCluster) {
+      for (int r = 0; r < team.nb; ++r)
+        if (r != team.rank) asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(cluster_map(remote + 4 * i, r)), "f"(v) : "memory");
+    }
+  }
+  if (!team.sync(w)) return false;
+  for (int ib = wid * gpw; ib < m; ib += nw * gpw) {
+    const int i = ib + lane / gs;
+    float t = 0.0f;
+    if (i < m)
+      for (int e = R.rp[i] + sub; e < R.rp[i + 1]; e += gs) t += M.cache_h[e] * R.yt[M.cache_j[e]];
+    for (int o = gs / 2; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    if (sub == 0 && i < m) R.cw[i] = t + R.etadi[i] * R.yt[r0 + i];
+  }
+  __syncthreads();
+  return true;
+}
+
+// The FP32 solve of a refinement sweep with every vector in shared memory (layout Rows32), for a
+// system of at most 1024 atoms solved by one block (rows [0, n)) or by a thread-block cluster (this
+// block's rows [r0, r1), at most 128). Projected PCG with the block-Jacobi M of the setup:
+// z = M^-1 (g - lambda 1) with lambda = <w, g> / <w, 1>; the product gathers yt = D M^-1 g over the
+// pre-scaled rows (H'_ij = H_ij / D_jj), so H z = H'yt - lambda c. g is kept projected (shifted
+// by the multiplier each step), so <g, z> is free of cancellation. A group of lanes per row forms
+// the product and its first lane the first update; a thread per row the second update and the
+// group products M^-1 g. In a cluster each block writes its rows' D M^-1 g into every other
+// block's yt before the second reduction, whose exchange publishes it. The iteration stops when
+// <g, z> falls to `ratio` times its start value. The correction x of the own rows is written to
+// y_out (global, indexed by atom).
+template <class Team>
+__device__ __noinline__ int qeq_cg_rows32(const XrWork& w, const Team& team, QeqShared& sh, int a0, int n, int r0,
+                                          int r1, const QeqMatrix<float>& M, float* y_out, double ratio, int max_it) {
+  extern __shared__ __align__(16) unsigned char qeq_dyn[];
+  constexpr bool kCluster = std::is_same<Team, ClusterTeam>::value;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5, tid = threadIdx.x;
+  const int m = r1 - r0;
+  Rows32 R(qeq_dyn, n, m);
   // the row cache: in this block's shared memory, or FP32 rows in global memory
   const bool cache_shared = __isShared(M.cache_h);
   const float* const ch_g = M.cache_h;
@@ -762,35 +994,52 @@ __device__ __noinline__ int qeq_cg_rows32(const XrWork& w, const XrFF& ff, const
       reinterpret_cast<const float*>(qeq_dyn + (cache_shared ? (reinterpret_cast<const unsigned char*>(M.cache_h) - qeq_dyn) : 0));
   const unsigned short* const cj_s = reinterpret_cast<const unsigned short*>(
       qeq_dyn + (cache_shared ? (reinterpret_cast<const unsigned char*>(M.cache_j) - qeq_dyn) : 0));
-  const int ebeg = M.ebeg;
-  const double* DI = &QW(Q_DINV, 0);
-  const double* Cr = &QW(Q_C, 0);
   const double* G = &QW(Q_G, 0);
   float* red = reinterpret_cast<float*>(sh.red);
-  for (int q = tid; q < n; q += blockDim.x) g[q] = float(__ldcg(G + a0 + q));
+  const float s1 = float(sh.sd_s1w);
+  unsigned remote = 0;
+  if constexpr (kCluster) remote = smem_u32(R.yt + r0);
+  auto publish = [&](int i, float v) {  // D M^-1 g of own row i, here and in the other blocks
+    R.yt[r0 + i] = v;
+    if constexpr (kCluster) {
+      for (int r = 0; r < team.nb; ++r)
+        if (r != team.rank) asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(cluster_map(remote + 4 * i, r)), "f"(v) : "memory");
+    }
+  };
+  auto group_apply = [&](int i) {  // (M^-1 g)_i over the group of row i
+    const int f = R.first[i], k = R.size[i];
+    const float* bi = R.binv + kGroupMax * i;
+    float t = 0.0f;
+    for (int b = 0; b < k; ++b) t += bi[b] * R.gl[f + b];
+    return t;
+  };
   for (int i = tid; i < m; i += blockDim.x) {
-    const int a = a0 + r0 + i;
-    p[i] = 0.0f;
-    hp[i] = 0.0f;
-    y[i] = 0.0f;
-    di[i] = float(DI[a]);
-    etadi[i] = float(atom_prm(ff, w.type[a], A_ETA) * DI[a]);
-    cr[i] = float(Cr[a]);
-    rp[i] = w.cnt[a] - ebeg;
-  }
-  if (tid == 0) rp[m] = w.cnt[a0 + r1] - ebeg;
-  const float s1 = float(s1d);
-  if (tid == 0) {
-    sh.sf_lam = 0.0f;
-    sh.sf_beta = 0.0f;
-    sh.sf_gz = float(gz_start);
-    sh.sc_state = (!(gz_start > 0.0) || n < 2 || gz_start <= stop) ? 1 : 0;
+    R.gl[i] = float(__ldcg(G + a0 + r0 + i));
+    R.p[i] = 0.0f;
+    R.hp[i] = 0.0f;
+    R.x[i] = 0.0f;
   }
   __syncthreads();
-  // remote addresses of this block's rows in the other blocks' gradient copies
-  unsigned gremote = 0;
-  if constexpr (kCluster) gremote = smem_u32(g + r0);
-  const float fstop = float(stop);
+  float u0 = 0.0f, u1 = 0.0f;
+  for (int i = tid; i < m; i += blockDim.x) {
+    const float y = group_apply(i);
+    R.yl[i] = y;
+    publish(i, y * R.dd[i]);
+    u0 += R.wv[i] * R.gl[i];
+    u1 += R.gl[i] * y;
+  }
+  // start: lambda = <w, g> / <w, 1>, and <g - lambda, M^-1 (g - lambda)> = <g, M^-1 g> - lambda <w, g>
+  if (!team_sum2f(team, w, u0, u1, red, [&](float t0, float t1) {
+        const float lam = t0 / s1;
+        const float gz = t1 - lam * t0;
+        sh.sf_lam = lam;
+        sh.sf_beta = 0.0f;
+        sh.sf_gz = gz;
+        sh.sf_stop = float(ratio) * gz;
+        sh.sc_state = (!(gz > 0.0f) || n < 2) ? 1 : 0;
+      }))
+    return -1;
+  const float fstop = sh.sf_stop;
   const int gs = row_group(m), sub = lane & (gs - 1), gpw = 32 / gs;
   int it = 0;
   while (sh.sc_state == 0) {
@@ -799,8 +1048,8 @@ __device__ __noinline__ int qeq_cg_rows32(const XrWork& w, const XrFF& ff, const
       break;
     }
     const float lam = sh.sf_lam, beta = sh.sf_beta;
-    // H'g over the cached rows, gs lanes per row; the group's first lane then updates the row:
-    // p = -z + beta p, Hp = -H z + beta Hp with z = D^-1 (g - lambda), H z = H'g - lambda c.
+    // H y over the cached rows (gs lanes per row); the group's first lane then updates the row:
+    // z = y - lambda w, Hz = Hy - lambda c, p = -z + beta p, Hp = -Hz + beta Hp, g -= lambda
     float php0 = 0.0f, php1 = 0.0f;
     // four entries per lane in flight: the rows may stream from L2 rather than shared memory
     auto row_dot = [&](const float* ch, const unsigned short* cj, int e, int ee) {
@@ -808,30 +1057,30 @@ __device__ __noinline__ int qeq_cg_rows32(const XrWork& w, const XrFF& ff, const
       for (; e + 3 * gs < ee; e += 4 * gs) {
         const float h0 = ch[e], h1 = ch[e + gs], h2 = ch[e + 2 * gs], h3 = ch[e + 3 * gs];
         const int j0 = cj[e], j1 = cj[e + gs], j2 = cj[e + 2 * gs], j3 = cj[e + 3 * gs];
-        s += h0 * g[j0];
-        s += h1 * g[j1];
-        s += h2 * g[j2];
-        s += h3 * g[j3];
+        s += h0 * R.yt[j0];
+        s += h1 * R.yt[j1];
+        s += h2 * R.yt[j2];
+        s += h3 * R.yt[j3];
       }
-      for (; e < ee; e += gs) s += ch[e] * g[cj[e]];
+      for (; e < ee; e += gs) s += ch[e] * R.yt[cj[e]];
       return s;
     };
     for (int ib = wid * gpw; ib < m; ib += nw * gpw) {
       const int i = ib + lane / gs;
       float s = 0.0f;
-      if (i < m) s = cache_shared ? row_dot(ch_s, cj_s, rp[i] + sub, rp[i + 1]) : row_dot(ch_g, cj_g, rp[i] + sub, rp[i + 1]);
+      if (i < m)
+        s = cache_shared ? row_dot(ch_s, cj_s, R.rp[i] + sub, R.rp[i + 1]) : row_dot(ch_g, cj_g, R.rp[i] + sub, R.rp[i + 1]);
       for (int o = gs / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
       if (sub == 0 && i < m) {
-        const float ga = g[r0 + i];
-        const float h = s + etadi[i] * ga - lam * cr[i];
-        const float z = di[i] * (ga - lam);
-        const float pv = -z + beta * p[i];
-        const float hpv = -h + beta * hp[i];
-        p[i] = pv;
-        hp[i] = hpv;
-        gown[i] = ga - lam;  // g itself stays as is until every row's product is done
+        const float hz = s + R.etadi[i] * R.yt[r0 + i] - lam * R.cw[i];
+        const float z = R.yl[i] - lam * R.wv[i];
+        const float pv = -z + beta * R.p[i];
+        const float hpv = -hz + beta * R.hp[i];
+        R.p[i] = pv;
+        R.hp[i] = hpv;
+        R.gl[i] -= lam;
         php0 += pv * hpv;
-        php1 += di[i] * hpv;
+        php1 += R.wv[i] * hpv;
       }
     }
     if (!team_sum2f(team, w, php0, php1, red, [&](float t0, float t1) {
@@ -846,18 +1095,19 @@ __device__ __noinline__ int qeq_cg_rows32(const XrWork& w, const XrFF& ff, const
       return -1;
     if (sh.sc_state != 0) break;
     const float alpha = sh.sf_alpha, step = sh.sf_step;
-    float u0 = 0.0f, u1 = 0.0f;
     for (int i = tid; i < m; i += blockDim.x) {
-      const float gn = (gown[i] + alpha * hp[i]) - step;
-      y[i] += alpha * p[i];
-      g[r0 + i] = gn;
-      if constexpr (kCluster) {
-        for (int r = 0; r < team.nb; ++r)
-          if (r != team.rank)
-            asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(cluster_map(gremote + 4 * i, r)), "f"(gn) : "memory");
-      }
-      u0 += di[i] * gn;
-      u1 += di[i] * gn * gn;
+      R.gl[i] = (R.gl[i] + alpha * R.hp[i]) - step;
+      R.x[i] += alpha * R.p[i];
+    }
+    __syncthreads();  // the group products read the other rows of the group
+    u0 = 0.0f;
+    u1 = 0.0f;
+    for (int i = tid; i < m; i += blockDim.x) {
+      const float y = group_apply(i);
+      R.yl[i] = y;
+      publish(i, y * R.dd[i]);
+      u0 += R.wv[i] * R.gl[i];
+      u1 += R.gl[i] * y;
     }
     if (!team_sum2f(team, w, u0, u1, red, [&](float t0, float t1) {
           const float lamn = t0 / s1;
@@ -869,7 +1119,7 @@ __device__ __noinline__ int qeq_cg_rows32(const XrWork& w, const XrFF& ff, const
         }))
       return -1;
   }
-  for (int i = tid; i < m; i += blockDim.x) y_out[a0 + r0 + i] = y[i];
+  for (int i = tid; i < m; i += blockDim.x) y_out[a0 + r0 + i] = R.x[i];
   __syncthreads();
   return it;
 }
@@ -970,16 +1220,15 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
   // The cache holds FP32 values + 16-bit columns (6 B per entry, mixed precision) when the block's
   // rows fit, else FP64 values + columns (10 B), else nothing (rows read from global memory).
   // A block that solves a system of at most 1024 atoms alone keeps every row's FP32 state in shared
-  // memory instead, and so does each block of a cluster team for its rows (at most 128) plus the
-  // whole gradient: 4 B per atom of the system and 32 B per own row, and at least the n doubles of
-  // the FP64 stage of a fallback.
+  // memory instead, and so does each block of a cluster team for its rows plus the whole vector the
+  // product gathers (layout Rows32: 4 B per atom of the system and 72 B per own row), and at least
+  // the n doubles of the FP64 stage of a fallback.
   constexpr bool kBlock = std::is_same<Team, BlockTeam>::value;
   constexpr bool kCluster = std::is_same<Team, ClusterTeam>::value;
-  const bool small_rows = (kBlock || kCluster) && dyn != nullptr && n <= 1024 && r1 - r0 <= (kBlock ? 1024 : 128);
+  // (the same for every block of a team: it depends on the system only)
+  const bool small_rows = (kBlock || kCluster) && dyn != nullptr && n <= 1024;
   const int stage_n = (dyn != nullptr && (small_rows || n * 8 <= dyn_bytes / 2)) ? n : 0;
-  const size_t stage_bytes =
-      small_rows ? std::max<size_t>((4 * (size_t)n + 32 * (size_t)(r1 - r0) + 4 + 15) / 16 * 16, 8 * (size_t)n)
-                 : 8 * (size_t)stage_n;
+  const size_t stage_bytes = small_rows ? std::max<size_t>(rows32_bytes(n, r1 - r0), 8 * (size_t)n) : 8 * (size_t)stage_n;
   void* gstage = stage_n > 0 ? dyn : nullptr;
   unsigned char* region = dyn != nullptr ? dyn + stage_bytes : nullptr;
   const long long region_bytes = dyn != nullptr ? dyn_bytes - (long long)stage_bytes : 0;
@@ -1133,6 +1382,10 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
     }
     QeqMatrix<float> M32{reinterpret_cast<const float*>(cache_h), cache_j, true, true, ebeg,
                          reinterpret_cast<float*>(gstage)};
+    if constexpr (kBlock || kCluster) {
+      if (small_rows && gz > target && gz > gfloor && n >= 2 && !qeq_rows32_setup(w, ff, team, sh, a0, n, r0, r1, M32))
+        return;
+    }
     for (int sweep = 0; sweep < 8; ++sweep) {
       if (!(gz > target) || !(gz > gfloor) || n < 2) break;
       if (!small_rows) {  // the shared-memory solver reads the FP64 gradient itself (published by the
@@ -1151,7 +1404,7 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
       const double stop = fmax(1e-10 * gz, 0.01 * target);
       int it;
       if constexpr (kBlock || kCluster) {
-        it = small_rows ? qeq_cg_rows32(w, ff, team, sh, a0, n, r0, r1, M32, v32.y, s1, gz, stop, 400)
+        it = small_rows ? qeq_cg_rows32(w, team, sh, a0, n, r0, r1, M32, v32.y, stop / gz, 400)
                         : qeq_cg<Team, float>(w, ff, team, sh, a0, n, r0, r1, v32, M32, s1, gz, stop, 0.0, 400, false, slot);
       } else {
         it = qeq_cg<Team, float>(w, ff, team, sh, a0, n, r0, r1, v32, M32, s1, gz, stop, 0.0, 400, false, slot);
