@@ -1,0 +1,103 @@
+"""Server host logic on CPU: batching, error isolation, worker failures, warm-start hand-off.
+
+The device calculator is replaced by a recorder (no GPU): each result's energy is the request's atom
+count, so every request can be matched to its own result.
+"""
+
+import threading
+
+import numpy as np
+import pytest
+
+import xreac_gb300.serving as serving
+
+
+class _Eval:
+    def __init__(self, n, charges):
+        self.energy = float(n)
+        self.charges = charges
+
+
+class _Calc:
+    fail_next_batch = threading.Event()
+
+    def __init__(self, force_field, device=0, max_expanded_atoms=512):
+        self.batches = []
+        self.last_launches = 1
+
+    def reserve(self, atoms, systems):
+        pass
+
+    def _evaluate_items(self, items):
+        self.batches.append(len(items))
+        out = []
+        for symbols, positions, q, cell, pbc, initial in items:
+            if symbols[0] == "Bad":
+                raise ValueError("unknown element")
+            n = len(symbols)
+            out.append(_Eval(n, np.full(n, 0.5) if initial is None else initial + 1.0))
+        return out
+
+    def qeq_work(self):
+        if _Calc.fail_next_batch.is_set():
+            _Calc.fail_next_batch.clear()
+            raise RuntimeError("device fault report")
+        return 0, 0.0
+
+    def transfer_bytes(self):
+        return 0, 0
+
+
+@pytest.fixture()
+def server(monkeypatch):
+    monkeypatch.setattr(serving, "Calculator", _Calc)
+    srv = serving.Server({"ff": object()}, workers=2)
+    yield srv
+    srv.close()
+
+
+def _req(n, session=None, bad=False):
+    symbols = ["Bad"] * n if bad else ["H"] * n
+    return serving.Request(symbols, np.zeros((n, 3)), "ff", session=session)
+
+
+def test_every_request_gets_its_own_result(server):
+    reqs = [_req(1 + k % 7) for k in range(200)]
+    out, _ = serving.replay(server, reqs)
+    assert [o.evaluation.energy for o in out] == [float(r.natoms) for r in reqs]
+    assert len(server.batches) < len(reqs)
+    assert all(o.batch_size >= 1 and o.latency >= 0 for o in out)
+
+
+def test_a_bad_request_fails_alone(server):
+    reqs = [_req(3), _req(2, bad=True), _req(4)]
+    out, _ = serving.replay(server, reqs)
+    assert isinstance(out[1], ValueError)
+    assert out[0].evaluation.energy == 3.0 and out[2].evaluation.energy == 4.0
+
+
+def test_worker_failure_fails_the_batch_and_serving_continues(server):
+    _Calc.fail_next_batch.set()
+    first = server.submit(_req(2))
+    with pytest.raises(RuntimeError):
+        first.result(timeout=10)
+    assert first.done() and isinstance(first.exception(), RuntimeError)
+    later = server.submit(_req(5))
+    assert later.result(timeout=10).evaluation.energy == 5.0
+
+
+def test_sessions_hand_charges_to_the_next_step(server):
+    a = server.submit(_req(3, session="traj")).result(timeout=10)
+    b = server.submit(_req(3, session="traj")).result(timeout=10)
+    np.testing.assert_array_equal(a.evaluation.charges, 0.5)
+    np.testing.assert_array_equal(b.evaluation.charges, 1.5)  # started from a's charges
+    c = server.submit(_req(4, session="traj")).result(timeout=10)  # another size: no warm start
+    np.testing.assert_array_equal(c.evaluation.charges, 0.5)
+
+
+def test_unknown_force_field_and_closed_server(server):
+    with pytest.raises(ValueError):
+        server.submit(serving.Request(["H"], np.zeros((1, 3)), "other"))
+    server.close()
+    with pytest.raises(RuntimeError):
+        server.submit(_req(1))

@@ -232,7 +232,15 @@ class Server:
                     if self._closed:
                         return
                     continue
-            self._run(calcs[name], name, batch)
+            try:
+                self._run(calcs[name], name, batch)
+            except BaseException as err:  # noqa: BLE001 - an unexpected failure fails the batch, not the worker
+                for _, fut in batch:
+                    if not fut._done:
+                        fut._error = err if isinstance(err, Exception) else RuntimeError(repr(err))
+                        fut._done = True
+                with self._done_cv:
+                    self._done_cv.notify_all()
 
     def _run(self, calc, name, batch):
         charges = self._charges
