@@ -76,7 +76,33 @@ def build(force=False, verbose=False, extra_flags=()):
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    build_host(force, verbose)
     return LIB
+
+
+def build_host(force=False, verbose=False):
+    """The host-side batch packing module ``_lib/_xr_host.so`` (CPython C API, g++). Skipped, with the
+    pure-Python packing path used instead, when the compiler or the Python headers are missing."""
+    import sysconfig
+
+    src = CSRC / "xr_host.cpp"
+    out = LIBDIR / "_xr_host.so"
+    include = sysconfig.get_paths().get("include")
+    if not include or not (Path(include) / "Python.h").exists():
+        return None
+    if not force and not _stale(out, [src]):
+        return out
+    cxx = os.environ.get("CXX", "g++")
+    cmd = [cxx, "-O2", "-std=c++17", "-shared", "-fPIC", "-I", include, str(src), "-o", str(out)]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    try:
+        r = subprocess.run(cmd, capture_output=True, text=True)
+    except OSError:
+        return None
+    if r.returncode != 0:
+        raise RuntimeError(f"host module build failed:\n{r.stdout}\n{r.stderr}")
+    return out
 
 
 if __name__ == "__main__":

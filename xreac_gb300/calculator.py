@@ -36,6 +36,11 @@ COMPONENTS = (
     "qeq",
 )
 
+try:  # the host-side batch packing module (built with the CUDA library; optional)
+    from ._lib import _xr_host as _host
+except ImportError:
+    _host = None
+
 _NO_PBC = np.zeros(3, dtype=bool)
 _NO_PBC.flags.writeable = False
 _SYSTEM_DTYPE = np.dtype(nat.System)
@@ -356,6 +361,10 @@ class Calculator:
 
     def _evaluate_items(self, items, full_derivative=False, extra_flags=0):
         """``evaluate_many`` on tuples (symbols, positions, total_charge, cell, pbc, initial_charges)."""
+        if _host is not None and self._all_valid and type(items) is list and items:
+            packed = self._pack(items, full_derivative)
+            if packed is not None:
+                return self._run_packed(*packed, full_derivative, "replicated", extra_flags)
         batch, reps = [], []
         prepare = self._prepare
         for symbols, positions, total_charge, cell, pbc, initial in items:
@@ -365,20 +374,76 @@ class Calculator:
             reps.append(rp)
         return self._run(batch, full_derivative, reps, "replicated", extra_flags)
 
+    def _pack(self, items, full_derivative):
+        """The batch's types and positions packed by the host module (one C pass over the requests);
+        requests it leaves (any input the fast path does not take as is) go through ``_prepare``,
+        and cells, periodicity and initial charges through the Python checks. None when the batch
+        needs the general path."""
+        if full_derivative is not True and full_derivative is not False:
+            raise ValueError("full_derivative must be a boolean")
+        try:
+            sizes = [len(it[0]) for it in items]
+        except TypeError:
+            return None
+        total = sum(sizes)
+        types = np.empty(total, dtype=np.int32)
+        x = np.empty((total, 3))
+        slow = _host.fill(items, self._type_pos, types, x)
+        n_sys = len(items)
+        flags_l = [_NO_PBC] * n_sys
+        cells = [None] * n_sys
+        reps = [(1, 1, 1)] * n_sys
+        guesses = [None] * n_sys
+        offsets = np.zeros(n_sys + 1, dtype=np.int64)
+        np.cumsum(sizes, out=offsets[1:])
+        for k in slow:
+            sym, xk, tk, fk, ck, rk = self._prepare(*items[k][:5], full_derivative)
+            a0, a1 = int(offsets[k]), int(offsets[k + 1])
+            if len(tk) != a1 - a0:
+                return None
+            types[a0:a1] = tk
+            x[a0:a1] = xk
+            flags_l[k], cells[k], reps[k] = fk, ck, rk
+        cutoff = None
+        slow_set = set(slow)
+        for k, it in enumerate(items):
+            cell, pbc, initial = it[3], it[4], it[5]
+            if k not in slow_set and not ((pbc is None and cell is None) or pbc is False):
+                flags, m = boundary(cell, pbc)
+                if m is not None:
+                    if cutoff is None:
+                        cutoff = float(self.force_field.general[12])
+                    reps[k] = cell_repetitions(cutoff, flags, m, sizes[k], self.max_expanded_atoms)
+                    cells[k] = np.ascontiguousarray(m, dtype=np.float64)
+                flags_l[k] = flags
+            if initial is not None:
+                guesses[k] = _guess(initial, sizes[k])
+        charges = [float(it[2]) for it in items]
+        return types, x, offsets, flags_l, cells, charges, guesses, reps
+
     def _run(self, batch, full_derivative, reps, backend, extra_flags=0):
         """One ``xr_eval_batch`` call over ``batch`` = [(types, positions, pbc flags, cell, total
-        charge, initial charges)]. The inputs are packed into one array per kind and the
-        per-system descriptors are filled column-wise, so the host cost per system is a handful of
-        numpy operations; each ``Evaluation`` gets views of the batch's result arrays."""
-        lib = self._lib
+        charge, initial charges)]: the inputs are packed into one array per kind, then as
+        ``_run_packed``."""
         n_sys = len(batch)
         types_l, xs, flags_l, cells, charges, guesses = zip(*batch)
         sizes = np.fromiter(map(len, types_l), dtype=np.int64, count=n_sys)
         offsets = np.zeros(n_sys + 1, dtype=np.int64)
         np.cumsum(sizes, out=offsets[1:])
-        total = int(offsets[-1])
         types = np.concatenate(types_l) if n_sys > 1 else types_l[0]
         x = np.concatenate(xs) if n_sys > 1 else xs[0]
+        return self._run_packed(types, x, offsets, flags_l, cells, charges, guesses, reps, full_derivative, backend,
+                                extra_flags)
+
+    def _run_packed(self, types, x, offsets, flags_l, cells, charges, guesses, reps, full_derivative, backend,
+                    extra_flags=0):
+        """One ``xr_eval_batch`` call: the per-system descriptors are filled column-wise over the
+        packed types and positions, so the host cost per system is a handful of numpy operations;
+        each ``Evaluation`` gets views of the batch's result arrays."""
+        lib = self._lib
+        n_sys = len(offsets) - 1
+        sizes = np.diff(offsets)
+        total = int(offsets[-1])
         if not np.isfinite(x).all():
             raise ValueError("positions must be a finite (N, 3) array in Angstrom")
         sys_arr = np.zeros(n_sys, dtype=_SYSTEM_DTYPE)
