@@ -233,6 +233,44 @@ def stream_requests():
     return reqs, arrivals - arrivals[0]
 
 
+def serialised_device(reqs, ffs, local, steps, warmup):
+    """The stream's batches (the server's grouping: per force field in arrival order, up to
+    SERVER_BATCH_ATOMS atoms each) evaluated one after another on one context per force field, with
+    CUDA-event stage times: the device time of a pass when no two batches overlap. Returns the
+    stage milliseconds per pass, the QEq algorithmic bytes per pass, kernel launches per pass and
+    the number of batches per pass."""
+    from xreac_gb300 import Calculator
+
+    calcs = {name: Calculator(ff, device=local) for name, ff in ffs.items()}
+    for c in calcs.values():
+        c.reserve(SERVER_BATCH_ATOMS, 512)
+    batches, cur, held = [], {n: [] for n in ffs}, {n: 0 for n in ffs}
+    for r in reqs:
+        n = r.force_field
+        if cur[n] and held[n] + r.natoms > SERVER_BATCH_ATOMS:
+            batches.append((n, cur[n]))
+            cur[n], held[n] = [], 0
+        cur[n].append((r.symbols, r.positions, r.total_charge, r.cell, r.pbc, None))
+        held[n] += r.natoms
+    batches += [(n, items) for n, items in cur.items() if items]
+    for _ in range(max(warmup, 1)):
+        for n, items in batches[:4]:
+            calcs[n]._evaluate_items(items)
+    for c in calcs.values():
+        c.set_profiling(True)
+    qbytes, launches = 0.0, 0
+    for _ in range(steps):
+        for n, items in batches:
+            calcs[n]._evaluate_items(items)
+            qbytes += calcs[n].qeq_work()[1]
+            launches += calcs[n].last_launches
+    total = np.zeros(7)
+    for c in calcs.values():
+        total += c.stage_times()[0]
+        c.set_profiling(False)
+    return total / steps, qbytes / steps, launches / steps, len(batches)
+
+
 def stream_pass(reqs, tag, part=None):
     """A fresh copy of the stream (or of its first ``part`` requests) for one pass: session keys are
     tagged with the pass, so the only warm starts are the stream's own repeat evaluations (25 %,
@@ -434,6 +472,12 @@ def differentiation_numbers(local, copies=256):
                     "positional central difference of it (force term)"}
 
 
+# Server shape: six worker contexts keep enough batches in flight to fill the GPU (measured on one GB300:
+# 3.5 M atoms*evals/s with two workers, 4.7 M with four, 5.0 M with six and 8,192-atom batches, after which
+# the host's Python work per request bounds it).
+SERVER_WORKERS = 6
+SERVER_BATCH_ATOMS = 8192
+
 STAGE_NAMES = ["neighbour_count_scan", "neighbour_fill_reverse", "pairs_vdw_shield", "qeq_cg", "coulomb",
                "bonded_and_adjoint", "forces_reduce_pack"]
 
@@ -477,7 +521,7 @@ def main():
         print(json.dumps({"profile": "water", "ms_per_step": d["ms_per_step"], "stages_ms": d["stages_ms"]}), flush=True)
         return 0
     if args.profile == "serving":
-        with Server(ffs, workers=2, device=local) as srv:
+        with Server(ffs, workers=SERVER_WORKERS, max_batch_atoms=SERVER_BATCH_ATOMS, device=local) as srv:
             for k in range(args.warmup):
                 replay(srv, stream_pass(reqs, ("warmup", k), 512))
             for k in range(args.steps):
@@ -503,7 +547,7 @@ def main():
     warm_passes = [stream_pass(reqs, ("warmup", k), 512) for k in range(max(args.warmup, 3))]
     timed_passes = [stream_pass(reqs, ("timed", k)) for k in range(args.steps)]
     latency_pass = stream_pass(reqs, "latency")
-    with Server(ffs, workers=2, device=local) as srv:
+    with Server(ffs, workers=SERVER_WORKERS, max_batch_atoms=SERVER_BATCH_ATOMS, device=local) as srv:
         for wp in warm_passes:
             replay(srv, wp)
         # The long-lived objects made so far (the stream's copies, force fields, contexts) go to the
@@ -511,7 +555,6 @@ def main():
         # full collection during the timed passes walks them again.
         gc.collect()
         gc.freeze()
-        srv.set_profiling(True)
         srv.batches.clear()
         if dist is not None:
             dist.barrier()
@@ -527,9 +570,7 @@ def main():
             dist.barrier()
         errors = sum(isinstance(o, Exception) for o in out)
         timed_passes.clear()
-        stage_ms, calls = srv.stage_times()
         batches = list(srv.batches)
-        srv.set_profiling(False)
         # latency: the stream replayed at its arrival times, with the throughput passes' results
         # released first
         del out
@@ -540,17 +581,19 @@ def main():
         lat = np.array([o.latency for o in timed if not isinstance(o, Exception)]) * 1e3
         qwait = np.array([o.queued for o in timed if not isinstance(o, Exception)]) * 1e3
         replay_batches = len(srv.batches)
+    # device time of a pass with the batches run one after another (no overlap between batches)
+    stage_ms, qeq_bytes, serial_launches, serial_batches = serialised_device(reqs, ffs, local, args.steps,
+                                                                             args.warmup)
     device_ms = float(stage_ms.sum())
     wall_s = float(sum(wall))
     if dist is not None:
         t = torch.tensor([device_ms, wall_s], device="cuda", dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         device_ms, wall_s = float(t[0]), float(t[1])
-    value = world * atoms * args.steps / (device_ms / 1e3)
+    value = world * atoms / (device_ms / 1e3)
     e2e_value = world * atoms * args.steps / wall_s
     stages = {nm: float(stage_ms[k]) for k, nm in enumerate(STAGE_NAMES)}
     dominant = max(stages, key=stages.get)
-    qeq_bytes = sum(b.qeq_bytes for b in batches)
     qeq_achieved = qeq_bytes / (stages["qeq_cg"] / 1e3) / 1e9
     pk = peaks()
     hbm_peak = float(pk.get("hbm_gbs", 6800.0))
@@ -564,14 +607,14 @@ def main():
         "n_gpus": world,
         "steps": args.steps,
         "warmup": max(args.warmup, 3),
-        "ms_per_step": device_ms / args.steps,
+        "ms_per_step": device_ms,
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic (seeded request stream; molecules placed at random)",
-        "config": {"workload": WORKLOAD, "requests": len(reqs), "atoms_per_pass": atoms, "server_workers": 2,
-                   "max_batch_atoms": 16384, "parallelism": "replicas" if world > 1 else "single",
+        "config": {"workload": WORKLOAD, "requests": len(reqs), "atoms_per_pass": atoms, "server_workers": SERVER_WORKERS,
+                   "max_batch_atoms": SERVER_BATCH_ATOMS, "parallelism": "replicas" if world > 1 else "single",
                    "l2": "not flushed: every pass streams 4,096 distinct systems (inputs about 13 MB)"},
         "plain": {"value": plain_value, "unit": UNIT, "ms_per_request": 1e3 * plain_s / len(reqs),
                   "api": "one xreac_gb300.Calculator.evaluate per request"},
@@ -583,13 +626,16 @@ def main():
         "roofline": {"bound": "hbm", "kernel": "k_qeq_cluster (QEq solve of the served batches)",
                      "achieved": qeq_achieved, "peak": hbm_peak, "unit": "GB/s", "frac": qeq_achieved / hbm_peak,
                      "traffic": profiled_traffic("k_qeq_cluster"),
-                     "algorithmic_bytes_per_launch": qeq_bytes / max(len(batches), 1), "dominant_stage": dominant,
+                     "algorithmic_bytes_per_launch": qeq_bytes / max(serial_batches, 1), "dominant_stage": dominant,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in pk else "fallback 6800 GB/s",
                      "note": "achieved = matrix-free algorithmic bytes / QEq event time, averaged over the launches "
                              "(one per batch); traffic = DRAM bytes of one served batch's launch from an ncu "
                              "capture. The solve keeps its matrix rows on chip and is bound by the cluster "
                              "exchanges and shared-memory gathers, not HBM"},
-        "stages_ms_per_pass": {k: v / args.steps for k, v in stages.items()},
+        "stages_ms_per_pass": stages,
+        "device_time": "value, ms_per_step and stages: the stream's batches (8,192 atoms at most, per force field) "
+                       "evaluated one after another on one context, CUDA events per stage, no overlap between batches; "
+                       "e2e: the server's workers run batches concurrently",
         "batches_per_pass": len(batches) / args.steps,
         "errors": errors,
         "clocks": clocks.summary(),

@@ -127,7 +127,7 @@ class Server:
     allocation. ``warm_start`` enables the per-session QEq warm start.
     """
 
-    def __init__(self, force_fields, *, workers=2, max_batch_atoms=16384, max_batch_requests=512, device=0,
+    def __init__(self, force_fields, *, workers=4, max_batch_atoms=16384, max_batch_requests=512, device=0,
                  warm_start=True, max_expanded_atoms=512, reserve=True):
         if workers < 1:
             raise ValueError("workers must be at least 1")
