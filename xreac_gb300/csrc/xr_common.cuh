@@ -224,13 +224,15 @@ int xr_launch_qeq(const XrWork& w, const XrFF& ff, cudaStream_t st, int nblocks,
                   const int* small, int nsmall, bool adjoint = false);
 void xr_launch_charge_response(const XrWork& w, const XrFF& ff, cudaStream_t st, int stage);
 int xr_qeq_coop_blocks_per_sm();
-// Thread-block-cluster QEq solver for batches: blocks per cluster, how many such clusters can be
-// resident at once (0: unavailable), and its launch over `list` = nbig cluster systems followed by
-// nsmall single-block systems (nblocks a multiple of kQeqCluster).
-constexpr int kQeqCluster = 8;
-int xr_qeq_max_clusters();
-int xr_launch_qeq_cluster(const XrWork& w, const XrFF& ff, cudaStream_t st, int nblocks, const int* list, int nbig,
-                          int nsmall, bool adjoint = false);
+// Thread-block-cluster QEq solver: `csize` blocks per cluster (kQeqClusterBatch for batches, whose
+// many systems share the SMs; kQeqClusterSingle for a single system, whose solve time is the call's
+// latency); how many such clusters can be resident at once (0: unavailable); and its launch over
+// `list` = nbig cluster systems followed by nsmall single-block systems (nblocks a multiple of csize).
+constexpr int kQeqClusterBatch = 4;
+constexpr int kQeqClusterSingle = 8;
+int xr_qeq_max_clusters(int csize);
+int xr_launch_qeq_cluster(const XrWork& w, const XrFF& ff, cudaStream_t st, int csize, int nblocks, const int* list,
+                          int nbig, int nsmall, bool adjoint = false);
 void xr_launch_coulomb(const XrWork& w, const XrFF& ff, cudaStream_t st);
 void xr_launch_bonded(const XrWork& w, const XrFF& ff, cudaStream_t st);
 void xr_launch_forces(const XrWork& w, const XrFF& ff, cudaStream_t st);

@@ -70,7 +70,8 @@ struct xr_ctx {
   int cg_max = 2000;
   int nsm = 0;
   int coop_per_sm = 0;
-  int max_clusters = 0;  // resident thread-block clusters of the cluster QEq solver (0: unavailable)
+  int max_clusters = 0;  // resident thread-block clusters of the cluster QEq solver (0: unavailable),
+  int max_clusters_batch = 0;  // for the single-system and the batch cluster size
   long long launches = 0;
   long long h2d_bytes = 0, d2h_bytes = 0;  // host<->device bytes moved by the last evaluation
   int qeq_iterations = 0;                   // CG iterations of the last evaluation (largest system)
@@ -648,15 +649,18 @@ void plan_qeq(xr_ctx* c, const xr_system* sys, int nsys, int* nblocks, int* ntea
 }
 
 // Cluster plan: every system above kQeqSmall atoms is solved by one thread-block cluster
-// (kQeqCluster blocks, rows split over them, reductions in distributed shared memory), the others
+// (4 blocks in a batch, 8 for a single system; rows split over them, reductions in distributed
+// shared memory), the others
 // by single blocks. Taken when no system is too large for a cluster to be the better choice: above
 // kQeqClusterMax atoms a single-system call spreads the rows over a grid-wide team instead, and
 // above kQeqBatchBlock atoms a batch does. h_qsmall receives the cluster systems, then the others,
 // each largest first.
 constexpr int kQeqClusterMax = 640;
 
-bool plan_qeq_cluster(xr_ctx* c, const xr_system* sys, int nsys, int* nblocks, int* nbig, int* nsmall) {
-  if (c->max_clusters < 1) return false;
+bool plan_qeq_cluster(xr_ctx* c, const xr_system* sys, int nsys, int* csize, int* nblocks, int* nbig, int* nsmall) {
+  *csize = nsys > 1 ? kQeqClusterBatch : kQeqClusterSingle;
+  if ((nsys > 1 ? c->max_clusters_batch : c->max_clusters) < 1) return false;
+  const int cs = *csize;
   const int limit = nsys > 1 ? kQeqBatchBlock : kQeqClusterMax;
   std::vector<int> big, small;
   for (int s = 0; s < nsys; ++s) {
@@ -666,9 +670,8 @@ bool plan_qeq_cluster(xr_ctx* c, const xr_system* sys, int nsys, int* nblocks, i
   auto larger = [&](int a, int b) { return sys[a].natoms > sys[b].natoms; };
   std::sort(big.begin(), big.end(), larger);
   std::sort(small.begin(), small.end(), larger);
-  const int clusters = std::max(1, std::min(c->nsm / kQeqCluster,
-                                            (int)big.size() + ((int)small.size() + kQeqCluster - 1) / kQeqCluster));
-  *nblocks = clusters * kQeqCluster;
+  const int clusters = std::max(1, std::min(c->nsm / cs, (int)big.size() + ((int)small.size() + cs - 1) / cs));
+  *nblocks = clusters * cs;
   *nbig = (int)big.size();
   *nsmall = (int)small.size();
   c->h_qsmall.assign(big.begin(), big.end());
@@ -846,10 +849,10 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
   xr_launch_pairs(w, ff->d, st);
   launches += 2;
   stage(c, 3, st);
-  int qblocks = 0, qteam = 0, qsmall = 0, qbig = 0;
+  int qblocks = 0, qteam = 0, qsmall = 0, qbig = 0, qcsize = 0;
   bool qcluster = false;
   if (c->coop_per_sm > 0) {
-    qcluster = plan_qeq_cluster(c, sys, nsys, &qblocks, &qbig, &qsmall);
+    qcluster = plan_qeq_cluster(c, sys, nsys, &qcsize, &qblocks, &qbig, &qsmall);
     if (!qcluster) plan_qeq(c, sys, nsys, &qblocks, &qteam, &qsmall);
     const int nlist = qbig + qsmall;
     if (!host_grow(&c->h_qmap_p, &c->ch_qmap_p, (size_t)std::max(qteam, 1)) ||
@@ -866,7 +869,7 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
     h2d += sizeof(int4) * (long long)qteam + sizeof(int) * (long long)nlist;
   }
   auto launch_qeq = [&](bool adjoint) {
-    return qcluster ? xr_launch_qeq_cluster(w, ff->d, st, qblocks, c->qsmall, qbig, qsmall, adjoint)
+    return qcluster ? xr_launch_qeq_cluster(w, ff->d, st, qcsize, qblocks, c->qsmall, qbig, qsmall, adjoint)
                     : xr_launch_qeq(w, ff->d, st, qblocks, c->qmap, qteam, c->qsmall, qsmall, adjoint);
   };
   if (int le = launch_qeq(false))
@@ -1147,7 +1150,8 @@ int xr_ctx_create(int device, void* stream, xr_ctx** out) {
   }
   cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device);
   c->coop_per_sm = xr_qeq_coop_blocks_per_sm();
-  c->max_clusters = xr_qeq_max_clusters();
+  c->max_clusters = xr_qeq_max_clusters(kQeqClusterSingle);
+  c->max_clusters_batch = xr_qeq_max_clusters(kQeqClusterBatch);
   int coop_ok = 0;
   cudaDeviceGetAttribute(&coop_ok, cudaDevAttrCooperativeLaunch, device);
   if (!coop_ok) c->coop_per_sm = 0;

@@ -1519,7 +1519,7 @@ __global__ void __launch_bounds__(1024, 1) k_qeq_grid(XrWork w, XrFF ff, const i
   qeq_small_systems(w, ff, small, nsmall, w.barrier + nteam, adjoint, sh, dyn);
 }
 
-// Batch solver on thread-block clusters of kQeqCluster blocks, one block per SM: the systems of
+// Solver on thread-block clusters (4 or 8 blocks, set at launch), one block per SM: the systems of
 // `big` (largest first) are each solved by a whole cluster, rows split over its blocks, with
 // reductions through distributed shared memory; then every block takes systems of `small` alone.
 // A cluster's leader draws the next big system from a counter and the draw reaches the other
@@ -1777,14 +1777,14 @@ int xr_qeq_coop_blocks_per_sm() {
 }
 
 namespace {
-cudaLaunchConfig_t cluster_config(int nblocks, cudaStream_t st, cudaLaunchAttribute* attr) {
+cudaLaunchConfig_t cluster_config(int csize, int nblocks, cudaStream_t st, cudaLaunchAttribute* attr) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(nblocks);
   cfg.blockDim = dim3(1024);
   cfg.dynamicSmemBytes = kQeqMaxDyn;
   cfg.stream = st;
   attr[0].id = cudaLaunchAttributeClusterDimension;
-  attr[0].val.clusterDim.x = kQeqCluster;
+  attr[0].val.clusterDim.x = csize;
   attr[0].val.clusterDim.y = 1;
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
@@ -1793,13 +1793,13 @@ cudaLaunchConfig_t cluster_config(int nblocks, cudaStream_t st, cudaLaunchAttrib
 }
 }  // namespace
 
-int xr_qeq_max_clusters() {
+int xr_qeq_max_clusters(int csize) {
   if (cudaFuncSetAttribute(k_qeq_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, kQeqMaxDyn) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
   cudaLaunchAttribute attr[1];
-  cudaLaunchConfig_t cfg = cluster_config(kQeqCluster, nullptr, attr);
+  cudaLaunchConfig_t cfg = cluster_config(csize, csize, nullptr, attr);
   int n = 0;
   if (cudaOccupancyMaxActiveClusters(&n, (void*)k_qeq_cluster, &cfg) != cudaSuccess) {
     cudaGetLastError();
@@ -1808,11 +1808,11 @@ int xr_qeq_max_clusters() {
   return n;
 }
 
-int xr_launch_qeq_cluster(const XrWork& w, const XrFF& ff, cudaStream_t st, int nblocks, const int* list, int nbig,
-                          int nsmall, bool adjoint) {
+int xr_launch_qeq_cluster(const XrWork& w, const XrFF& ff, cudaStream_t st, int csize, int nblocks, const int* list,
+                          int nbig, int nsmall, bool adjoint) {
   cudaMemsetAsync(w.barrier, 0, 2 * sizeof(unsigned), st);  // big-system and small-system counters
   cudaLaunchAttribute attr[1];
-  cudaLaunchConfig_t cfg = cluster_config(nblocks, st, attr);
+  cudaLaunchConfig_t cfg = cluster_config(csize, nblocks, st, attr);
   const int* small = list + nbig;
   int adj = adjoint ? 1 : 0;
   return (int)cudaLaunchKernelEx(&cfg, k_qeq_cluster, w, ff, list, nbig, small, nsmall, adj);
