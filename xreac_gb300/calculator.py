@@ -17,7 +17,8 @@ from numbers import Real
 import numpy as np
 
 from . import _native as nat
-from .geometry import boundary, cell_repetitions, validate_expansion_limit, validate_input, validate_total_charge
+from .geometry import (boundary, cell_repetitions, periodic_cell, validate_expansion_limit, validate_input,
+                       validate_total_charge)
 
 COMPONENTS = (
     "bond",
@@ -286,6 +287,11 @@ class Calculator:
             if (pbc is None and cell is None) or pbc is False:
                 flags, m = _NO_PBC, None
             else:
+                fast = periodic_cell(cell, pbc, float(ff.general[12]), len(symbols), self.max_expanded_atoms)
+                if fast is not None:
+                    if not self._all_valid:
+                        ff.validate_model(symbols)
+                    return symbols, x, types, fast[0], fast[1], fast[2]
                 flags, m = boundary(cell, pbc)
             if not self._all_valid:
                 ff.validate_model(symbols)
@@ -409,13 +415,17 @@ class Calculator:
         for k, it in enumerate(items):
             cell, pbc, initial = it[3], it[4], it[5]
             if k not in slow_set and not ((pbc is None and cell is None) or pbc is False):
-                flags, m = boundary(cell, pbc)
-                if m is not None:
-                    if cutoff is None:
-                        cutoff = float(self.force_field.general[12])
-                    reps[k] = cell_repetitions(cutoff, flags, m, sizes[k], self.max_expanded_atoms)
-                    cells[k] = np.ascontiguousarray(m, dtype=np.float64)
-                flags_l[k] = flags
+                if cutoff is None:
+                    cutoff = float(self.force_field.general[12])
+                fast = periodic_cell(cell, pbc, cutoff, sizes[k], self.max_expanded_atoms)
+                if fast is not None:
+                    flags_l[k], cells[k], reps[k] = fast
+                else:
+                    flags, m = boundary(cell, pbc)
+                    if m is not None:
+                        reps[k] = cell_repetitions(cutoff, flags, m, sizes[k], self.max_expanded_atoms)
+                        cells[k] = np.ascontiguousarray(m, dtype=np.float64)
+                    flags_l[k] = flags
             if initial is not None:
                 guesses[k] = _guess(initial, sizes[k])
         charges = [float(it[2]) for it in items]

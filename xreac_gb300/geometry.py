@@ -10,6 +10,7 @@ compatibility only. The coincident-atom check runs on the device as part of the 
 
 from __future__ import annotations
 
+import math
 from numbers import Real
 
 import numpy as np
@@ -66,6 +67,51 @@ def cell_repetitions(cutoff, flags, m, atoms, max_expanded_atoms=512):
         )
     reps[flags] = required.astype(int)
     return tuple(int(v) for v in reps)
+
+
+_ALL_PBC = np.ones(3, dtype=bool)
+_ALL_PBC.flags.writeable = False
+
+
+def periodic_cell(cell, pbc, cutoff, atoms, max_expanded_atoms):
+    """``(pbc flags, cell matrix, repetitions)`` of a fully periodic cell given as three lengths or a (3, 3)
+    matrix with ``pbc`` True (or None), computed with scalar arithmetic, which for a 3 x 3 cell is
+    several times cheaper than the general path; None for any other input or any input the general
+    path would reject, which then gives the same result or error through ``boundary`` and
+    ``cell_repetitions``. Face heights are volume / area of the opposite face, the same quantity as
+    the inverse of the reciprocal vectors' norms."""
+    if not (pbc is True or (pbc is None and cell is not None)):
+        return None
+    try:
+        m = np.array(cell, dtype=np.float64)
+    except (TypeError, ValueError):
+        return None
+    if m.shape == (3,):
+        if not (m > 0).all():
+            return None
+        m = np.diag(m)
+    if m.shape != (3, 3):
+        return None
+    a, b, c = m.tolist()
+    if not all(math.isfinite(v) for v in a + b + c):
+        return None
+    bc = (b[1] * c[2] - b[2] * c[1], b[2] * c[0] - b[0] * c[2], b[0] * c[1] - b[1] * c[0])
+    ca = (c[1] * a[2] - c[2] * a[1], c[2] * a[0] - c[0] * a[2], c[0] * a[1] - c[1] * a[0])
+    ab = (a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0])
+    det = a[0] * bc[0] + a[1] * bc[1] + a[2] * bc[2]
+    norms = [math.sqrt(sum(v * v for v in r)) for r in (a, b, c)]
+    if not det > 1e-12 * norms[0] * norms[1] * norms[2]:
+        return None
+    reps = []
+    for face in (bc, ca, ab):
+        ratio = cutoff * (1 + 1e-12) * math.sqrt(face[0] ** 2 + face[1] ** 2 + face[2] ** 2) / det
+        if abs(ratio - round(ratio)) < 1e-9:
+            return None  # on a boundary the general path's rounding decides
+        reps.append(int(math.floor(ratio)) + 1)
+    copies = reps[0] * reps[1] * reps[2]
+    if copies > 1 and copies * atoms > max_expanded_atoms:
+        return None
+    return _ALL_PBC, m, tuple(reps)
 
 
 def validate_input(symbols, positions, total_charge=0, cell=None, pbc=None):
