@@ -695,8 +695,10 @@ __device__ inline int row_group(int m) {
 // post() on the totals (bit-identical in every block) and the block waits for it. Returns false
 // when a cluster exchange gave up.
 template <class Team, class Post>
-__device__ inline bool team_sum2f(const Team& team, const XrWork& w, float a, float b, float* smem, Post post) {
+__device__ inline bool team_sum2f(const Team& team, const XrWork& w, float a, float b, float* smem, Post post,
+                                  int* slot = nullptr) {
   constexpr bool kCluster = std::is_same<Team, ClusterTeam>::value;
+  constexpr bool kGrid = std::is_same<Team, GridTeam>::value;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   a = warp_total_t<float>(a);
   b = warp_total_t<float>(b);
@@ -705,6 +707,17 @@ __device__ inline bool team_sum2f(const Team& team, const XrWork& w, float a, fl
     smem[32 + wid] = b;
   }
   __syncthreads();
+  if constexpr (kGrid) {  // a grid-wide reduction of the block totals (FP64 slots, alternating)
+    double v[2] = {0.0, 0.0};
+    if (wid == 0) {
+      v[0] = double(warp_total_t<float>(lane < nw ? smem[lane] : 0.0f));
+      v[1] = double(warp_total_t<float>(lane < nw ? smem[32 + lane] : 0.0f));
+    }
+    const bool ok = team.template reduce<2>(w, v, reinterpret_cast<double*>(smem), *slot,
+                                            [&](double* t) { post(float(t[0]), float(t[1])); });
+    *slot = *slot == 1 ? 2 : 1;
+    return ok;
+  }
   bool good = true;
   if (wid == 0) {
     float x = lane < nw ? smem[lane] : 0.0f, y = lane < nw ? smem[32 + lane] : 0.0f;
@@ -826,9 +839,10 @@ __device__ inline void small_lu_column(const double (&a)[kGroupMax][kGroupMax], 
 // exchange gave up.
 template <class Team>
 __device__ __noinline__ bool qeq_rows32_setup(const XrWork& w, const XrFF& ff, const Team& team, QeqShared& sh, int a0,
-                                              int n, int r0, int r1, const QeqMatrix<float>& M) {
+                                              int n, int r0, int r1, const QeqMatrix<float>& M, float* gyt) {
   extern __shared__ __align__(16) unsigned char qeq_dyn[];
   constexpr bool kCluster = std::is_same<Team, ClusterTeam>::value;
+  constexpr bool kGrid = std::is_same<Team, GridTeam>::value;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5, tid = threadIdx.x;
   const int m = r1 - r0;
   Rows32 R(qeq_dyn, n, m);
@@ -953,8 +967,13 @@ __device__ __noinline__ bool qeq_rows32_setup(const XrWork& w, const XrFF& ff, c
       for (int r = 0; r < team.nb; ++r)
         if (r != team.rank) asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(cluster_map(remote + 4 * i, r)), "f"(v) : "memory");
     }
+    if constexpr (kGrid) gyt[a0 + r0 + i] = v;
   }
   if (!team.sync(w)) return false;
+  if constexpr (kGrid) {
+    for (int q = tid; q < n; q += blockDim.x) R.yt[q] = __ldcg(gyt + a0 + q);
+    __syncthreads();
+  }
   for (int ib = wid * gpw; ib < m; ib += nw * gpw) {
     const int i = ib + lane / gs;
     float t = 0.0f;
@@ -980,9 +999,11 @@ __device__ __noinline__ bool qeq_rows32_setup(const XrWork& w, const XrFF& ff, c
 // y_out (global, indexed by atom).
 template <class Team>
 __device__ __noinline__ int qeq_cg_rows32(const XrWork& w, const Team& team, QeqShared& sh, int a0, int n, int r0,
-                                          int r1, const QeqMatrix<float>& M, float* y_out, double ratio, int max_it) {
+                                          int r1, const QeqMatrix<float>& M, float* y_out, double ratio, int max_it,
+                                          float* gyt, int* slot) {
   extern __shared__ __align__(16) unsigned char qeq_dyn[];
   constexpr bool kCluster = std::is_same<Team, ClusterTeam>::value;
+  constexpr bool kGrid = std::is_same<Team, GridTeam>::value;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5, tid = threadIdx.x;
   const int m = r1 - r0;
   Rows32 R(qeq_dyn, n, m);
@@ -1004,6 +1025,13 @@ __device__ __noinline__ int qeq_cg_rows32(const XrWork& w, const Team& team, Qeq
     if constexpr (kCluster) {
       for (int r = 0; r < team.nb; ++r)
         if (r != team.rank) asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(cluster_map(remote + 4 * i, r)), "f"(v) : "memory");
+    }
+    if constexpr (kGrid) gyt[a0 + r0 + i] = v;  // global: the other blocks stage it after the reduction
+  };
+  auto stage = [&]() {  // a grid team's whole yt from global memory, after the reduction that published it
+    if constexpr (kGrid) {
+      for (int q = tid; q < n; q += blockDim.x) R.yt[q] = __ldcg(gyt + a0 + q);
+      __syncthreads();
     }
   };
   auto group_apply = [&](int i) {  // (M^-1 g)_i over the group of row i
@@ -1037,8 +1065,9 @@ __device__ __noinline__ int qeq_cg_rows32(const XrWork& w, const Team& team, Qeq
         sh.sf_gz = gz;
         sh.sf_stop = float(ratio) * gz;
         sh.sc_state = (!(gz > 0.0f) || n < 2) ? 1 : 0;
-      }))
+      }, slot))
     return -1;
+  stage();
   const float fstop = sh.sf_stop;
   const int gs = row_group(m), sub = lane & (gs - 1), gpw = 32 / gs;
   int it = 0;
@@ -1091,7 +1120,7 @@ __device__ __noinline__ int qeq_cg_rows32(const XrWork& w, const Team& team, Qeq
             sh.sf_alpha = gz / t0;
             sh.sf_step = sh.sf_alpha * t1 / s1;
           }
-        }))
+        }, slot))
       return -1;
     if (sh.sc_state != 0) break;
     const float alpha = sh.sf_alpha, step = sh.sf_step;
@@ -1116,8 +1145,9 @@ __device__ __noinline__ int qeq_cg_rows32(const XrWork& w, const Team& team, Qeq
           sh.sf_beta = gzn / sh.sf_gz;
           sh.sf_gz = gzn;
           if (gzn <= fstop) sh.sc_state = 1;
-        }))
+        }, slot))
       return -1;
+    stage();
   }
   for (int i = tid; i < m; i += blockDim.x) y_out[a0 + r0 + i] = R.x[i];
   __syncthreads();
@@ -1226,7 +1256,11 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
   constexpr bool kBlock = std::is_same<Team, BlockTeam>::value;
   constexpr bool kCluster = std::is_same<Team, ClusterTeam>::value;
   // (the same for every block of a team: it depends on the system only)
-  const bool small_rows = (kBlock || kCluster) && dyn != nullptr && n <= 1024;
+  constexpr bool kGridTeam = std::is_same<Team, GridTeam>::value;
+  int team_rows = n;  // the most rows any block of the team owns (the same value in every block)
+  if constexpr (kGridTeam) team_rows = min(n, ((n + team.nb - 1) / team.nb + 31) / 32 * 32);
+  const bool small_rows =
+      dyn != nullptr && ((kBlock || kCluster) ? n <= 1024 : rows32_bytes(n, team_rows) <= (size_t)dyn_bytes / 2);
   const int stage_n = (dyn != nullptr && (small_rows || n * 8 <= dyn_bytes / 2)) ? n : 0;
   const size_t stage_bytes = small_rows ? std::max<size_t>(rows32_bytes(n, r1 - r0), 8 * (size_t)n) : 8 * (size_t)stage_n;
   void* gstage = stage_n > 0 ? dyn : nullptr;
@@ -1382,10 +1416,8 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
     }
     QeqMatrix<float> M32{reinterpret_cast<const float*>(cache_h), cache_j, true, true, ebeg,
                          reinterpret_cast<float*>(gstage)};
-    if constexpr (kBlock || kCluster) {
-      if (small_rows && gz > target && gz > gfloor && n >= 2 && !qeq_rows32_setup(w, ff, team, sh, a0, n, r0, r1, M32))
-        return;
-    }
+    if (small_rows && gz > target && gz > gfloor && n >= 2 && !qeq_rows32_setup(w, ff, team, sh, a0, n, r0, r1, M32, v32.g))
+      return;
     for (int sweep = 0; sweep < 8; ++sweep) {
       if (!(gz > target) || !(gz > gfloor) || n < 2) break;
       if (!small_rows) {  // the shared-memory solver reads the FP64 gradient itself (published by the
@@ -1402,13 +1434,9 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
       // the correction's own projected norm starts at gz; 1e-10 of it (1e-5 in norm) per sweep,
       // and no further than a hundredth of the final target
       const double stop = fmax(1e-10 * gz, 0.01 * target);
-      int it;
-      if constexpr (kBlock || kCluster) {
-        it = small_rows ? qeq_cg_rows32(w, team, sh, a0, n, r0, r1, M32, v32.y, stop / gz, 400)
-                        : qeq_cg<Team, float>(w, ff, team, sh, a0, n, r0, r1, v32, M32, s1, gz, stop, 0.0, 400, false, slot);
-      } else {
-        it = qeq_cg<Team, float>(w, ff, team, sh, a0, n, r0, r1, v32, M32, s1, gz, stop, 0.0, 400, false, slot);
-      }
+      const int it = small_rows ? qeq_cg_rows32(w, team, sh, a0, n, r0, r1, M32, v32.y, stop / gz, 400, v32.g, &slot)
+                                : qeq_cg<Team, float>(w, ff, team, sh, a0, n, r0, r1, v32, M32, s1, gz, stop, 0.0, 400,
+                                                      false, slot);
       if (it < 0) return;
       iters += it;
       // x += y, then restore sum x = Q exactly: the FP32 step keeps sum y = 0 only to FP32 rounding,
