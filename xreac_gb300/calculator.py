@@ -460,18 +460,23 @@ class Calculator:
         sys_arr["natoms"] = sizes
         sys_arr["types"] = nat.addr(types) + 4 * offsets[:-1]
         sys_arr["positions"] = nat.addr(x) + 24 * offsets[:-1]
-        sys_arr["pbc"] = flags_l
+        periodic = [k for k, f in enumerate(flags_l) if f is not _NO_PBC]
+        if periodic:
+            pbc = sys_arr["pbc"]
+            for k in periodic:
+                pbc[k] = flags_l[k]
         sys_arr["total_charge"] = charges
         if any(c is not None for c in cells):
             sys_arr["cell"] = [0 if c is None else nat.addr(c) for c in cells]
         if any(g is not None for g in guesses):
             sys_arr["charges_guess"] = [0 if g is None else nat.addr(g) for g in guesses]
-        # one allocation per kind for the whole batch; each Evaluation gets views
-        energy = np.zeros((n_sys, 15))
-        dipole = np.zeros((n_sys, 3))
-        forces = np.zeros((total, 3))
-        per_atom = np.zeros((3, total))  # charges, total bond orders, lone pairs
-        counts = np.zeros(total, dtype=np.int32)
+        # one allocation per kind for the whole batch, every element written by the call; each
+        # Evaluation gets views
+        energy = np.empty((n_sys, 15))
+        dipole = np.empty((n_sys, 3))
+        forces = np.empty((total, 3))
+        per_atom = np.empty((3, total))  # charges, total bond orders, lone pairs
+        counts = np.empty(total, dtype=np.int32)
         res_arr = np.empty(n_sys, dtype=_RESULT_DTYPE)
         ks = np.arange(n_sys, dtype=np.int64)
         a0s = offsets[:-1]

@@ -29,13 +29,30 @@ int fill_one(PyObject* item, PyObject* type_map, int* types, double* x, Py_ssize
   if (!PyList_CheckExact(symbols) && !PyTuple_CheckExact(symbols)) return 1;
   PyObject** sym = PySequence_Fast_ITEMS(symbols);
   if (PySequence_Fast_GET_SIZE(symbols) != natoms || natoms == 0) return 1;
+  // Labels repeat, usually as the same string objects: a few recently seen objects are matched by
+  // identity before the dictionary is asked.
+  constexpr int kSeen = 8;
+  PyObject* seen[kSeen] = {};
+  int seen_type[kSeen] = {};
+  int nseen = 0;
   for (Py_ssize_t a = 0; a < natoms; ++a) {
-    if (!PyUnicode_CheckExact(sym[a])) return 1;
-    PyObject* t = PyDict_GetItemWithError(type_map, sym[a]);  // borrowed
+    PyObject* label = sym[a];
+    int k = 0;
+    while (k < nseen && seen[k] != label) ++k;
+    if (k < nseen) {
+      types[a] = seen_type[k];
+      continue;
+    }
+    if (!PyUnicode_CheckExact(label)) return 1;
+    PyObject* t = PyDict_GetItemWithError(type_map, label);  // borrowed
     if (!t) return PyErr_Occurred() ? -1 : 1;
     const long v = PyLong_AsLong(t);
     if (v == -1 && PyErr_Occurred()) return -1;
     types[a] = (int)v;
+    if (nseen < kSeen) {
+      seen[nseen] = label;
+      seen_type[nseen++] = (int)v;
+    }
   }
   Py_buffer view;
   if (PyObject_GetBuffer(positions, &view, PyBUF_C_CONTIGUOUS | PyBUF_FORMAT | PyBUF_ND) != 0) {
