@@ -89,3 +89,40 @@ def test_warm_start_reaches_the_same_charges_in_fewer_iterations():
     np.testing.assert_allclose(off.charges, cold.charges, atol=1e-10, rtol=0)
     with pytest.raises(ValueError):
         calc.evaluate(s.symbols, x2, cell=s.cell, pbc=s.pbc, initial_charges=first.charges[:-1])
+
+
+def test_many_workers_and_small_batches_give_the_same_results():
+    """Six workers with 2,048-atom batches: many batches in flight on the device at once (their QEq
+    clusters, grid teams and single blocks interleaved), each request still matching its result alone."""
+    from xreac_gb300 import Calculator, ForceField
+    from xreac_gb300.serving import Server, replay
+
+    stream, reqs = _requests(n=96, seed=11)
+    ffs = {n: ForceField.bundled(n) for n in FFS}
+    alone = {n: Calculator(f) for n, f in ffs.items()}
+    with Server(ffs, workers=6, max_batch_atoms=2048) as srv:
+        served, _ = replay(srv, reqs)
+        assert len(srv.batches) > 6
+    for req, out in zip(reqs, served):
+        assert not isinstance(out, Exception), out
+        ref = alone[req.force_field].evaluate(req.symbols, req.positions, cell=req.cell, pbc=req.pbc,
+                                              total_charge=req.total_charge)
+        _close(out.evaluation, ref)
+
+
+def test_batches_are_deterministic():
+    """The same batch twice gives bit-identical results (fixed-order reductions everywhere, including
+    the thread-block-cluster exchanges of the QEq solve)."""
+    from xreac_gb300 import Calculator, ForceField
+
+    stream, _ = _requests(n=64, seed=13)
+    ff = "ffield.reax.CHO.2008"
+    systems = [dict(symbols=r.system.symbols, positions=r.system.positions, cell=r.system.cell, pbc=r.system.pbc,
+                    total_charge=r.system.total_charge) for r in stream if r.system.force_field == ff]
+    calc = Calculator(ForceField.bundled(ff))
+    a = calc.evaluate_many(systems)
+    b = calc.evaluate_many(systems)
+    for x, y in zip(a, b):
+        assert x.energy == y.energy
+        np.testing.assert_array_equal(x.forces, y.forces)
+        np.testing.assert_array_equal(x.charges, y.charges)
