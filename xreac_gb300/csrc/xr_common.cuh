@@ -85,6 +85,7 @@ struct XrSystem {
   double total_charge;
   int has_guess;         // QEq starts from w.qguess (charges of an earlier step) instead of Q/n
   double rc, rc2, bond_cut, hb_cut;     // cutoff, cutoff^2, min(5, rc), min(7.5, rc)
+  double inv_rc;                        // 1 / rc
   float cellf[9];
   float margin;          // bound on |FP32 squared distance - FP64 squared distance| (A^2)
   float rc2f, bc2f, hc2f;  // FP32 squared cutoff, bond cutoff and hydrogen-bond cutoff
@@ -100,6 +101,8 @@ struct XrFF {
   const double* pair_gw;      // [T*T] (1/gamma_w)^g28 for shielded vdW
   const double* pair_logr;    // [T*T][3] log(r_s), log(r_p), log(r_pp) (0 where unused)
   const double* pair_rmax;    // [T*T] distance beyond which the uncorrected bond order stays below cut/4
+  const double* pair_inv;     // [T*T][2] 1 / r_vdW, 1 / rcore (IEEE: infinite for a zero rcore)
+  double inv_g28;             // 1 / g[28], the vdW shielding exponent
   const int* is_carbon;       // [T] label is "C" (case-insensitive): C2 correction applies
   const int* hb_role;         // [T] 1 hydrogen-bond hydrogen, 2 donor/acceptor (p_hbond), 0 otherwise
   const int* angle_index;     // [T^3][2] first, count

@@ -326,6 +326,7 @@ int build_system(xr_ctx* c, const xr_system& in, int atom_off, double rc, XrSyst
   for (int q = 0; q < 3; ++q) S.origin[q] = origin[q];
   S.total_charge = in.total_charge;
   S.rc = rc;
+  S.inv_rc = 1.0 / rc;
   S.rc2 = rc * rc;
   S.bond_cut = std::min(5.0, rc);
   S.hb_cut = std::min(7.5, rc);
@@ -1104,6 +1105,13 @@ int xr_ff_create(const double* general, int ntypes, const double* atom, const do
   d.pair_gw = (const double*)up(gw.data(), sizeof(double) * T * T);
   d.pair_logr = (const double*)up(logr.data(), sizeof(double) * 3 * T * T);
   d.pair_rmax = (const double*)up(rmax.data(), sizeof(double) * T * T);
+  std::vector<double> pinv(2 * (size_t)T * T);
+  for (int pt = 0; pt < T * T; ++pt) {
+    pinv[2 * pt] = 1.0 / pair[pt * XR_NPAIR_COLS + P_RVDW];
+    pinv[2 * pt + 1] = 1.0 / pair[pt * XR_NPAIR_COLS + P_RCORE];
+  }
+  d.pair_inv = (const double*)up(pinv.data(), sizeof(double) * 2 * T * T);
+  d.inv_g28 = 1.0 / d.g[28];
   d.is_carbon = (const int*)up(is_carbon, sizeof(int) * T);
   std::vector<int> hb_role(T);
   for (int t = 0; t < T; ++t) {

@@ -36,6 +36,16 @@ __device__ inline void edge_vector(const XrSystem& S, const double4_32a& xi, con
   }
 }
 
+// t^(-1/3) for t in the float range: an FP32 seed, then two Newton-Raphson steps on f(z) = z^-3 - t,
+// z <- z (4 - t z^3) / 3, each of which squares the relative error (about 1e-7, 1e-14, then FP64
+// rounding). Multiplies only: it replaces a double cube root and the divisions by it.
+__device__ inline double inv_cbrt(double t) {
+  double z = (double)rcbrtf((float)t);
+  z = z * (4.0 - t * z * z * z) * (1.0 / 3.0);
+  z = z * (4.0 - t * z * z * z) * (1.0 / 3.0);
+  return z;
+}
+
 // ------------------------------------------------------------------------------ pair kernel
 __global__ void k_pairs(XrWork w, XrFF ff) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -51,33 +61,36 @@ __global__ void k_pairs(XrWork w, XrFF ff) {
   const int T = ff.ntypes, pt = w.type[i] * T + w.type[j];
   double taper = 0.0, dtaper = 0.0;
   if (r < rc) {
-    const double u = r / rc;
+    const double u = r * S.inv_rc;
     taper = 1 + u * u * u * u * (-35 + u * (84 + u * (-70 + 20 * u)));
     const double um = u - 1;
-    dtaper = 140.0 / rc * u * u * u * um * um * um;
+    dtaper = 140.0 * S.inv_rc * u * u * u * um * um * um;
   }
   const double gam = pair_prm(ff, pt, P_GAMMA);
-  const double c = cbrt(r * r * r + gam);
-  const double shield = taper / c;
-  const double dshield = dtaper / c - taper * r * r / (c * c * c * c);
+  const double z = inv_cbrt(r * r * r + gam);  // (r^3 + gamma)^(-1/3)
+  const double z2 = z * z;
+  const double shield = taper * z;
+  const double dshield = dtaper * z - taper * r * r * (z2 * z2);
   double f13 = r, df13 = 1.0;
   if (ff.vdw_type == 1 || ff.vdw_type == 3) {
     const double pw = ff.g[28];
     const double rp = exp(pw * log(r));
     const double sum = rp + __ldg(ff.pair_gw + pt);
-    f13 = exp(log(sum) / pw);
+    f13 = exp(log(sum) * ff.inv_g28);
     df13 = f13 * rp / (sum * r);
   }
-  const double D = pair_prm(ff, pt, P_D), alpha = pair_prm(ff, pt, P_ALPHA), rvdw = pair_prm(ff, pt, P_RVDW);
-  const double ev = exp(0.5 * alpha * (1 - f13 / rvdw));
-  const double dev = ev * (-0.5 * alpha / rvdw) * df13;
+  // reciprocals of the pair's radii from the table: multiplies instead of FP64 divisions
+  const double D = pair_prm(ff, pt, P_D), alpha = pair_prm(ff, pt, P_ALPHA);
+  const double2 inv = __ldg(reinterpret_cast<const double2*>(ff.pair_inv) + pt);  // 1/r_vdW, 1/rcore
+  const double ev = exp(0.5 * alpha * (1 - f13 * inv.x));
+  const double dev = ev * (-0.5 * alpha * inv.x) * df13;
   double E = taper * D * (ev * ev - 2 * ev);
   double G = dtaper * D * (ev * ev - 2 * ev) + taper * D * (2 * ev - 2) * dev;
   if (ff.vdw_type == 2 || ff.vdw_type == 3) {
-    const double ecore = pair_prm(ff, pt, P_ECORE), acore = pair_prm(ff, pt, P_ACORE), rcore = pair_prm(ff, pt, P_RCORE);
-    const double ec = ecore * exp(acore * (1 - r / rcore));
+    const double ecore = pair_prm(ff, pt, P_ECORE), acore = pair_prm(ff, pt, P_ACORE);
+    const double ec = ecore * exp(acore * (1 - r * inv.y));
     E += taper * ec;
-    G += dtaper * ec + taper * ec * (-acore / rcore);
+    G += dtaper * ec + taper * ec * (-acore * inv.y);
   }
   w.p_r[p] = r;
   w.p_shield[p] = shield;
@@ -86,6 +99,7 @@ __global__ void k_pairs(XrWork w, XrFF ff) {
   w.p_g[p] = G;
   if (w.pgrad && taper != 0.0) {
     // dE/d(D, alpha, r_vdW, gamma_w) of this pair's tapered vdW term (and the inner core's)
+    const double rvdw = pair_prm(ff, pt, P_RVDW);
     double* gp = w.pgrad + (size_t)pt * XR_NPAIR_COLS;
     const double m = taper * D * (2 * ev - 2) * ev;  // dE/d(log ev) per unit of the exponent's argument
     atomicAdd(gp + P_D, taper * (ev * ev - 2 * ev));
