@@ -101,3 +101,11 @@ def test_unknown_force_field_and_closed_server(server):
     server.close()
     with pytest.raises(RuntimeError):
         server.submit(_req(1))
+
+
+def test_submit_many_matches_single_submits(server):
+    reqs = [_req(1 + k % 5) for k in range(50)]
+    futs = server.submit_many(reqs)
+    assert [f.result(timeout=10).evaluation.energy for f in futs] == [float(r.natoms) for r in reqs]
+    with pytest.raises(ValueError):
+        server.submit_many([_req(1), serving.Request(["H"], np.zeros((1, 3)), "other")])

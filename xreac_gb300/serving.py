@@ -171,6 +171,25 @@ class Server:
             self._cv.notify()
         return fut
 
+    def submit_many(self, requests, arrival=None):
+        """Admit several requests at once (one lock acquisition and one wake-up for all of them);
+        returns their :class:`Pending` handles in order."""
+        for request in requests:
+            if request.force_field not in self._queues:
+                raise ValueError(f"Unknown force field {request.force_field!r}")
+        now = time.perf_counter() if arrival is None else arrival
+        cv = self._done_cv
+        futs = [Pending(cv) for _ in requests]
+        queues = self._queues
+        with self._cv:
+            if self._closed:
+                raise RuntimeError("server is closed")
+            for request, fut in zip(requests, futs):
+                request.arrival = now
+                queues[request.force_field].append((request, fut))
+            self._cv.notify_all()
+        return futs
+
     def close(self):
         """Stop accepting requests, finish the queued ones and join the workers."""
         with self._cv:
@@ -286,17 +305,17 @@ class Server:
 def replay(server, requests, arrivals=None, speedup=1.0):
     """Submit ``requests`` at their ``arrivals`` (seconds from the start; None = all at once) and
     wait for all results. Returns (list of Served or exceptions in request order, wall seconds)."""
-    futures = []
     t_start = time.perf_counter()
-    for k, req in enumerate(requests):
-        if arrivals is not None:
+    if arrivals is None:
+        futures = server.submit_many(requests, arrival=t_start)
+    else:
+        futures = []
+        for k, req in enumerate(requests):
             target = t_start + arrivals[k] / speedup
             delay = target - time.perf_counter()
             if delay > 0:
                 time.sleep(delay)
             futures.append(server.submit(req, arrival=max(target, t_start)))
-        else:
-            futures.append(server.submit(req, arrival=t_start))
     out = []
     for f in futures:
         try:
