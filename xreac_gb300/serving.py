@@ -139,7 +139,7 @@ class Server:
         self._cv = threading.Condition()
         self._done_cv = threading.Condition()  # signalled once per finished batch
         self._closed = False
-        self._charges = {}  # session -> last charges
+        self._charges = {}  # session -> its last evaluation (the next step starts from its charges)
         self._charges_lock = threading.Lock()
         self.batches = []  # (force field, requests, atoms, seconds) per batch, for reporting
         self._calcs = [
@@ -267,7 +267,8 @@ class Server:
         items = []
         with self._charges_lock:
             for req, _ in batch:
-                g = charges.get(req.session) if warm and req.session is not None else None
+                prev = charges.get(req.session) if warm and req.session is not None else None
+                g = None if prev is None else prev.charges  # the session's last evaluation
                 if g is not None and len(g) != len(req.symbols):
                     g = None
                 items.append((req.symbols, req.positions, req.total_charge, req.cell, req.pbc, g))
@@ -290,7 +291,7 @@ class Server:
         with self._charges_lock:
             for (req, _), res in zip(batch, results):
                 if req.session is not None and not isinstance(res, Exception):
-                    charges[req.session] = res.charges
+                    charges[req.session] = res  # its charges are read when the session's next step comes
         nb = len(batch)
         for (req, fut), res in zip(batch, results):
             if isinstance(res, Exception):
