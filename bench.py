@@ -640,7 +640,8 @@ def main():
         "errors": errors,
         "clocks": clocks.summary(),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "api": "xreac_gb300.serving.Server.submit with host numpy arrays (results as Evaluation objects)"},
+                "api": "xreac_gb300.serving.Server.submit_many (the whole pass at once) with host numpy arrays, "
+                       "results as Evaluation objects"},
         "gpu_launches": int(sum(b.launches for b in batches)),
     }
     line["water_box"] = water_box_numbers(lib, nat, local, max(3, min(args.steps * 4, 20)), args.warmup)
