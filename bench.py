@@ -214,6 +214,20 @@ def profiled_traffic(kernel):
     return None
 
 
+def profiled_fp64(kernel):
+    """FP64-pipe utilisation (% of peak, elapsed) of ``kernel`` from an ``ncu`` capture, recorded in
+    profiles/fp64_pipe.txt."""
+    path = ROOT / "profiles" / "fp64_pipe.txt"
+    try:
+        for line in path.read_text().splitlines():
+            parts = line.split()
+            if len(parts) >= 2 and parts[0] == kernel and not line.startswith("#"):
+                return float(parts[1])
+    except OSError:
+        pass
+    return None
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -421,6 +435,7 @@ def water_box_numbers(lib, nat, local, steps, warmup):
     pk = peaks()
     hbm_peak = float(pk.get("hbm_gbs", 6800.0))
     achieved = qbytes.value / (stages["qeq_cg"] / 1e3) / 1e9
+    pair_bytes = 8.0 * (nb_count.value // 2) + 76.0 * n
     return {
         "workload": BOX_WORKLOAD,
         "value": steps * n / (total_ms / 1e3),
@@ -435,6 +450,14 @@ def water_box_numbers(lib, nat, local, steps, warmup):
                      "frac": achieved / hbm_peak, "traffic": profiled_traffic("k_qeq_grid"),
                      "algorithmic_bytes_per_launch": qbytes.value,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs" if "hbm_gbs" in pk else "fallback 6800 GB/s"},
+        # the pair kernel against both roofs: its algorithmic bytes (8 B per half pair + 76 B per atom)
+        # over the pair stage's event time against HBM, and the FP64 pipe's busy share from ncu
+        "pair_kernel": {"kernel": "k_pairs (stage: k_pairs + k_hval)", "bound": "fp64 pipe",
+                        "algorithmic_bytes": pair_bytes,
+                        "achieved_gbs": pair_bytes / (stages["pairs_vdw_shield"] / 1e3) / 1e9,
+                        "hbm_frac": pair_bytes / (stages["pairs_vdw_shield"] / 1e3) / 1e9 / hbm_peak,
+                        "fp64_pipe_busy_pct": profiled_fp64("k_pairs"),
+                        "traffic": profiled_traffic("k_pairs")},
     }
 
 

@@ -143,6 +143,8 @@ __global__ void k_neighbors(XrWork w) {
     bd = w.cnt[3 * L + i];
   }
   const int r0 = S.reach[0], r1 = S.reach[1], r2 = S.reach[2];
+  // a lane's counts are at most its images, so 32 lanes' sums fit 16 bits when images < 2048
+  const bool packed = (2 * r0 + 1) * (2 * r1 + 1) * (2 * r2 + 1) < 2048;
   const ScreenConsts K = screen_consts(S);
   const int natoms = S.natoms, atom_off = S.atom_off;
   const bool per0 = S.periodic[0] != 0, per1 = S.periodic[1] != 0, per2 = S.periodic[2] != 0;
@@ -171,10 +173,30 @@ __global__ void k_neighbors(XrWork w) {
           }
     }
     int t_e, t_h, t_bh, t_ba;
-    const int o_e = warp_excl_scan(c_e, lane, &t_e);
-    const int o_h = warp_excl_scan(c_h, lane, &t_h);
-    const int o_bh = warp_excl_scan(c_bh, lane, &t_bh);
-    const int o_ba = warp_excl_scan(c_ba, lane, &t_ba);
+    int o_e = 0, o_h = 0, o_bh = 0, o_ba = 0;
+    if (!FILL) {  // the count pass needs the warp's totals only
+      t_e = __reduce_add_sync(0xffffffffu, c_e);
+      t_h = __reduce_add_sync(0xffffffffu, c_h);
+      t_bh = __reduce_add_sync(0xffffffffu, c_bh);
+      t_ba = __reduce_add_sync(0xffffffffu, c_ba);
+    } else if (packed) {  // two counters per 32-bit scan: every prefix fits in 16 bits
+      int t0, t1;
+      const int s0 = warp_excl_scan(c_e | (c_h << 16), lane, &t0);
+      const int s1 = warp_excl_scan(c_bh | (c_ba << 16), lane, &t1);
+      o_e = s0 & 0xffff;
+      o_h = s0 >> 16;
+      o_bh = s1 & 0xffff;
+      o_ba = s1 >> 16;
+      t_e = t0 & 0xffff;
+      t_h = t0 >> 16;
+      t_bh = t1 & 0xffff;
+      t_ba = t1 >> 16;
+    } else {
+      o_e = warp_excl_scan(c_e, lane, &t_e);
+      o_h = warp_excl_scan(c_h, lane, &t_h);
+      o_bh = warp_excl_scan(c_bh, lane, &t_bh);
+      o_ba = warp_excl_scan(c_ba, lane, &t_ba);
+    }
     if (FILL && c_e) {
       int k_e = 0, k_h = 0, k_bh = 0, k_ba = 0;
       for (int o0 = -r0; o0 <= r0; ++o0)
