@@ -1000,15 +1000,18 @@ __device__ __noinline__ bool qeq_rows32_setup(const XrWork& w, const XrFF& ff, c
   return true;
 }
 
-// The FP32 solve of a refinement sweep with every vector in shared memory (layout Rows32), for a
-// system of at most 1024 atoms solved by one block (rows [0, n)) or by a thread-block cluster (this
-// block's rows [r0, r1), at most 128). Projected PCG with the block-Jacobi M of the setup:
+// The FP32 solve of a refinement sweep with every vector in shared memory (layout Rows32): a system
+// of at most 1024 atoms solved by one block (rows [0, n)) or by a thread-block cluster, or a larger
+// system by a grid-wide team (this block's rows [r0, r1)). Projected PCG with the block-Jacobi M of
+// the setup:
 // z = M^-1 (g - lambda 1) with lambda = <w, g> / <w, 1>; the product gathers yt = D M^-1 g over the
 // pre-scaled rows (H'_ij = H_ij / D_jj), so H z = H'yt - lambda c. g is kept projected (shifted
 // by the multiplier each step), so <g, z> is free of cancellation. A group of lanes per row forms
 // the product and its first lane the first update; a thread per row the second update and the
 // group products M^-1 g. In a cluster each block writes its rows' D M^-1 g into every other
-// block's yt before the second reduction, whose exchange publishes it. The iteration stops when
+// block's yt before the second reduction, whose exchange publishes it; a grid team writes it to
+// global memory (gyt) and every block stages the whole vector after the reduction. The iteration
+// stops when
 // <g, z> falls to `ratio` times its start value. The correction x of the own rows is written to
 // y_out (global, indexed by atom).
 template <class Team>
