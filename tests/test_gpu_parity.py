@@ -302,3 +302,21 @@ def test_identical_atoms_need_no_qeq_iterations():
     ref = oracle.evaluate(ForceField.bundled("ffield.reax.CHO.2008"), ["O"] * 6, x)
     assert abs(r.energy - ref["energy"]) <= 1e-9 * 6
     np.testing.assert_allclose(r.forces, ref["forces"], atol=2e-8, rtol=0)
+
+
+def test_batch_charge_response_forces_match_single():
+    """full_derivative=True in a batch (the adjoint QEq solve on 4-block clusters and single blocks)
+    against the same systems alone (8-block clusters, single blocks)."""
+    from xreac_gb300 import workloads
+
+    systems = [workloads.water_cluster(n_mol=100, box=14.0, seed=5), workloads.water_cluster(n_mol=8, box=6.0, seed=5),
+               workloads.water_cluster(n_mol=60, box=12.0, seed=6)]
+    c = calc("ffield.reax.HO.2015")
+    items = [dict(symbols=s.symbols, positions=s.positions) for s in systems]
+    batch = c.evaluate_many(items, full_derivative=True)
+    for d, rb in zip(items, batch):
+        r1 = c.evaluate(d["symbols"], d["positions"], full_derivative=True)
+        assert rb.full_derivative and rb.force_convention == "charge_response"
+        assert rb.energy == pytest.approx(r1.energy, abs=1e-9 * len(d["symbols"]))
+        np.testing.assert_allclose(rb.forces, r1.forces, atol=1e-8, rtol=0)
+        np.testing.assert_allclose(rb.charges, r1.charges, atol=1e-10, rtol=0)
