@@ -103,19 +103,22 @@ class Evaluation:
         return dense
 
 
-# fields without a class default (a class attribute would shadow __getattr__)
+# A batch's evaluations make these fields on first access. ``bonds`` has a default in the dataclass;
+# its class attribute is removed below (the default stays in ``__init__``) so that the lookup of a
+# missing value reaches ``__getattr__``.
 _BATCH_FIELDS = frozenset(("forces", "charges", "components", "total_bond_orders", "lone_pairs", "bond_counts",
-                           "dipole"))
+                           "dipole", "bonds"))
+del Evaluation.bonds
 
 
 class _BatchResults:
     """The result arrays of one ``xr_eval_batch`` call; the fields of its k-th system are views."""
 
-    __slots__ = ("energy", "forces", "per_atom", "counts", "dipole", "offsets")
+    __slots__ = ("energy", "forces", "per_atom", "counts", "dipole", "offsets", "bonds", "cut")
 
-    def __init__(self, energy, forces, per_atom, counts, dipole, offsets):
+    def __init__(self, energy, forces, per_atom, counts, dipole, offsets, bonds, cut):
         self.energy, self.forces, self.per_atom, self.counts = energy, forces, per_atom, counts
-        self.dipole, self.offsets = dipole, offsets
+        self.dipole, self.offsets, self.bonds, self.cut = dipole, offsets, bonds, cut
 
     def field(self, name, k):
         a0, a1 = self.offsets[k], self.offsets[k + 1]
@@ -131,6 +134,9 @@ class _BatchResults:
             return self.counts[a0:a1].astype(np.int64)
         if name == "dipole":
             return self.dipole[k]
+        if name == "bonds":
+            c0, c1 = self.cut[k], self.cut[k + 1]
+            return tuple(a[c0:c1] for a in self.bonds)
         return dict(zip(COMPONENTS, self.energy[k, :14].tolist()))  # components
 
 
@@ -499,18 +505,16 @@ class Calculator:
             shift = np.repeat(a0s.astype(np.int32), np.diff(cut))
             bi -= shift
             bj -= shift
-        held = _BatchResults(energy, forces, per_atom, counts, dipole, offsets.tolist())
-        cut = cut.tolist()
+        held = _BatchResults(energy, forces, per_atom, counts, dipole, offsets.tolist(), (bi, bj, bS, bbo),
+                             cut.tolist())
         etot = energy[:, 14].tolist()
         results = []
         new = object.__new__
         for k in range(n_sys):
             # a frozen dataclass: set without the per-field checks; the array fields follow on access
-            c0, c1 = cut[k], cut[k + 1]
             ev = new(Evaluation)
             ev.__dict__.update(energy=etot[k], full_derivative=full_derivative, cell_repetitions=reps[k],
-                               neighbor_backend=backend, bonds=(bi[c0:c1], bj[c0:c1], bS[c0:c1], bbo[c0:c1]),
-                               _batch=held, _index=k)
+                               neighbor_backend=backend, _batch=held, _index=k)
             results.append(ev)
         return results
 
