@@ -139,8 +139,8 @@ struct XrWork {
   int* edge_pair;             // pair id of every edge (its own or its reverse's)
   int* edge_dbslot;           // bond-row slot of bond edges, -1 otherwise
   double* hval;               // per edge: 14.4 * shield of its pair (QEq matrix row entries)
-  float* qch;                 // per edge: FP32 pre-scaled row entry H_ij / D_jj of a system whose
-  unsigned short* qcj;        //   rows exceed shared memory, and its column within the system
+  float* qch;                 // per edge: FP32 hval, then (a system whose rows exceed shared memory)
+  unsigned short* qcj;        //   the pre-scaled row entry H_ij / D_jj and its column within the system
   // pairs
   int* pair_edge;             // half edge of each pair
   int* pair_i;                // source atom of each pair

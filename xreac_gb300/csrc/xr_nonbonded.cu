@@ -125,7 +125,9 @@ __global__ void k_pairs(XrWork w, XrFF ff) {
 __global__ void k_hval(XrWork w) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= w.nE) return;
-  w.hval[e] = QEQ_COULOMB * w.p_shield[w.edge_pair[e]];
+  const double h = QEQ_COULOMB * w.p_shield[w.edge_pair[e]];
+  w.hval[e] = h;
+  w.qch[e] = float(h);  // FP32 copy for the solver's row cache (which may overwrite it, scaled)
 }
 
 // ---------------------------------------------------------------------------------- QEq
@@ -430,6 +432,7 @@ struct QeqShared {
   float sf_lam, sf_alpha, sf_step, sf_beta, sf_gz, sf_stop;
   double sd_s1w;  // <1, M^-1 1> of the FP32 row solver's block-Jacobi preconditioner
   int sc_next;  // the next small system of the block (work sharing)
+  int sc_groups;  // preconditioner groups of two or more rows (row solver setup)
   double cred[2][8][8];  // cluster team: partials pushed by the blocks of the cluster
   unsigned cseq[2][8];   // cluster team: exchange number of each pushed entry
   int sc_state;  // 0 iterate, 1 converged, 2 stop
@@ -695,6 +698,14 @@ __device__ inline void warp_sum_all(double* v) {
   for (int k = 0; k < NV; ++k) v[k] = warp_total_t<double>(v[k]);
 }
 
+// warp_sum_all after a loop of one row per thread over this block's m rows: the warps past the rows
+// hold zeros and skip the shuffle tree, which costs the FP64 pipe as much for idle warps as for busy
+// ones.
+template <int NV>
+__device__ inline void rows_sum_all(double* v, int m) {
+  if ((int)(threadIdx.x & ~31u) < m) warp_sum_all<NV>(v);
+}
+
 // Lanes per matrix row in the per-row loops over a block's m rows: as many as keep the rows within
 // two passes of the block's warps (at least 4), so short rows of small systems do not leave most
 // lanes idle; each lane keeps four entries' loads in flight.
@@ -791,60 +802,13 @@ struct Rows32 {
     first = reinterpret_cast<unsigned short*>(rp + m + 1);
     size = first + m;
   }
-  // FP64 scratch of the setup (8 per row), over p .. binv (68 B per row, 16-byte aligned start)
-  __device__ double* scratch() const { return reinterpret_cast<double*>(p); }
+  // FP32 scratch of the setup, 8 per row over p .. gl
+  __device__ float* scratch32() const { return p; }
 };
 
 __host__ __device__ constexpr size_t rows32_bytes(int n, int m) {
   return (4 * (size_t)((n + 3) / 4 * 4) + 4 * (size_t)(9 + kGroupMax) * m + 4 * (size_t)(m + 1) + 4 * (size_t)m + 15) /
          16 * 16;
-}
-
-// LU factorisation with partial pivoting of the k x k block a (in place; row r of the factors
-// holds original row piv[r]); false when a pivot vanishes against the block's scale.
-__device__ inline bool small_lu(double (&a)[kGroupMax][kGroupMax], int (&piv)[kGroupMax], int k) {
-  double scale = 0.0;
-  for (int r = 0; r < k; ++r) {
-    piv[r] = r;
-    for (int c = 0; c < k; ++c) scale = fmax(scale, fabs(a[r][c]));
-  }
-  for (int c = 0; c < k; ++c) {
-    int best = c;
-    for (int r = c + 1; r < k; ++r)
-      if (fabs(a[r][c]) > fabs(a[best][c])) best = r;
-    if (!(fabs(a[best][c]) > 1e-12 * scale)) return false;
-    if (best != c) {
-      for (int q = 0; q < k; ++q) {
-        const double t = a[c][q];
-        a[c][q] = a[best][q];
-        a[best][q] = t;
-      }
-      const int t = piv[c];
-      piv[c] = piv[best];
-      piv[best] = t;
-    }
-    for (int r = c + 1; r < k; ++r) {
-      const double f = a[r][c] / a[c][c];
-      a[r][c] = f;
-      for (int q = c + 1; q < k; ++q) a[r][q] -= f * a[c][q];
-    }
-  }
-  return true;
-}
-
-// Column c of the inverse from the factors of small_lu, into x.
-__device__ inline void small_lu_column(const double (&a)[kGroupMax][kGroupMax], const int (&piv)[kGroupMax], int k,
-                                       int c, double (&x)[kGroupMax]) {
-  for (int r = 0; r < k; ++r) {  // L y = P e_c
-    double t = piv[r] == c ? 1.0 : 0.0;
-    for (int q = 0; q < r; ++q) t -= a[r][q] * x[q];
-    x[r] = t;
-  }
-  for (int r = k - 1; r >= 0; --r) {  // U x = y
-    double t = x[r];
-    for (int q = r + 1; q < k; ++q) t -= a[r][q] * x[q];
-    x[r] = t / a[r][r];
-  }
 }
 
 // Setup of the row solver's preconditioner and constants, once per solve (after the Jacobi diagonal
@@ -862,16 +826,18 @@ __device__ __noinline__ bool qeq_rows32_setup(const XrWork& w, const XrFF& ff, c
   Rows32 R(qeq_dyn, n, m);
   const double* DI = &QW(Q_DINV, 0);
   const int gs = row_group(m), sub = lane & (gs - 1), gpw = 32 / gs;
-  // 1. for every own row, the latest earlier own row bonded to it (distance below kGroupBond)
+  // 1. for every own row, the latest of the kGroupMax - 1 own rows before it that is bonded to it
+  //    (distance below kGroupBond); rows further back cannot share its group. Columns come from the
+  //    row cache, and a distance is read only for a candidate column.
   int* prev = reinterpret_cast<int*>(R.binv);  // scratch until the inverses are written
   for (int ib = wid * gpw; ib < m; ib += nw * gpw) {
     const int i = ib + lane / gs;
     int best = -1;
     if (i < m) {
-      const int a = a0 + r0 + i;
+      const int a = a0 + r0 + i, lo = max(0, i - (kGroupMax - 1));
       for (int e = w.cnt[a] + sub; e < w.cnt[a + 1]; e += gs) {
-        const int c = w.edge[e].x - a0 - r0;
-        if (c >= 0 && c < i && c > best && __ldg(w.p_r + w.edge_pair[e]) < kGroupBond) best = c;
+        const int c = int(M.cache_j[e - M.ebeg]) - r0;
+        if (c >= lo && c < i && c > best && __ldg(w.p_r + w.edge_pair[e]) < kGroupBond) best = c;
       }
     }
     for (int o = gs / 2; o > 0; o >>= 1) best = max(best, __shfl_xor_sync(0xffffffffu, best, o));
@@ -892,21 +858,23 @@ __device__ __noinline__ bool qeq_rows32_setup(const XrWork& w, const XrFF& ff, c
     }
   }
   __syncthreads();
-  // 3. each row of a group of two or more: its row of the group's block (FP64), into the scratch
-  double* B = R.scratch();
+  // 3. each row of a group of two or more: its row of the group's block (FP32: the inverse is
+  //    stored in FP32), into the scratch. The off-diagonal entries are read from hval, and only
+  //    those in the group.
+  float* B = R.scratch32();
   for (int ib = wid * gpw; ib < m; ib += nw * gpw) {
     const int i = ib + lane / gs;
     const int k = i < m ? R.size[i] : 1;
     if (__all_sync(0xffffffffu, k < 2)) continue;
-    double acc[kGroupMax];
+    float acc[kGroupMax];
 #pragma unroll
-    for (int b = 0; b < kGroupMax; ++b) acc[b] = 0.0;
+    for (int b = 0; b < kGroupMax; ++b) acc[b] = 0.0f;
     if (i < m && k > 1) {
       const int f = R.first[i], a = a0 + r0 + i;
       for (int e = w.cnt[a] + sub; e < w.cnt[a + 1]; e += gs) {
-        const int b = w.edge[e].x - a0 - r0 - f;
+        const int b = int(M.cache_j[e - M.ebeg]) - r0 - f;
         if (b >= 0 && b < k && b != i - f) {
-          const double h = w.hval[e];
+          const float h = float(w.hval[e]);
 #pragma unroll
           for (int q = 0; q < kGroupMax; ++q)
             if (q == b) acc[q] += h;
@@ -918,57 +886,74 @@ __device__ __noinline__ bool qeq_rows32_setup(const XrWork& w, const XrFF& ff, c
       for (int o = gs / 2; o > 0; o >>= 1) acc[b] += __shfl_xor_sync(0xffffffffu, acc[b], o);
     if (sub == 0 && i < m && k > 1) {
       const int f = R.first[i];
+      const float d = 1.0f / float(DI[a0 + r0 + i]);
 #pragma unroll
-      for (int b = 0; b < kGroupMax; ++b) B[kGroupMax * i + b] = b == i - f ? 1.0 / DI[a0 + r0 + i] : acc[b];
+      for (int b = 0; b < kGroupMax; ++b) B[kGroupMax * i + b] = b == i - f ? d : acc[b];
     }
   }
+  // 4. inverse blocks by Gauss-Jordan elimination without pivoting: the blocks of H are symmetric
+  //    positive definite, so every pivot is positive, and a block whose pivot is not falls back to
+  //    Jacobi. Eight lanes per group, lane r holding row r of the block (rows past the group's
+  //    size padded with the identity); the groups' first rows are listed in rp (written in step 5).
+  int* list = R.rp;
+  if (tid == 0) sh.sc_groups = 0;
   __syncthreads();
-  // 4. inverse blocks: the first row of each group reads its block, then (after everyone has read)
-  //    factorises it and writes the inverse rows and w = M^-1 1 of its rows; a singular block falls
-  //    back to Jacobi
-  double blk[kGroupMax][kGroupMax];
-  int lead_k = 0, lead_f = -1;
   for (int i = tid; i < m; i += blockDim.x)
-    if (R.first[i] == i && R.size[i] > 1) {
-      lead_f = i;
-      lead_k = R.size[i];
-      for (int r = 0; r < lead_k; ++r)
-        for (int c = 0; c < lead_k; ++c) blk[r][c] = B[kGroupMax * (i + r) + c];
-      break;  // at most one group per thread: blockDim >= m and group starts are distinct rows
-    }
+    if (R.first[i] == i && R.size[i] > 1) list[atomicAdd(&sh.sc_groups, 1)] = i;
   __syncthreads();
-  if (lead_f >= 0) {
-    int piv[kGroupMax];
-    const bool ok = small_lu(blk, piv, lead_k);
-    double wsum[kGroupMax], col[kGroupMax];
-    for (int r = 0; r < kGroupMax; ++r) wsum[r] = 0.0;
+  const int ngroups = sh.sc_groups;
+  for (int g0 = wid * 4; g0 < ngroups; g0 += nw * 4) {
+    const int g = g0 + (lane >> 3), r = lane & 7;
+    const bool active = g < ngroups;
+    const int f = active ? list[g] : 0;
+    const int k = active ? (int)R.size[f] : 0;
+    float a[kGroupMax];
+#pragma unroll
+    for (int q = 0; q < kGroupMax; ++q) a[q] = (r < k && q < k) ? B[kGroupMax * (f + r) + q] : (q == r ? 1.0f : 0.0f);
+    bool ok = true;
+#pragma unroll
     for (int c = 0; c < kGroupMax; ++c) {
-      if (c < lead_k && ok) small_lu_column(blk, piv, lead_k, c, col);
-      for (int r = 0; r < lead_k; ++r) {
-        const double v = c >= lead_k ? 0.0 : ok ? col[r] : (c == r ? DI[a0 + r0 + lead_f + r] : 0.0);
-        R.binv[kGroupMax * (lead_f + r) + c] = float(v);
-        wsum[r] += v;
+      float pr[kGroupMax];  // pivot row c, from lane c of the eight
+#pragma unroll
+      for (int q = 0; q < kGroupMax; ++q) pr[q] = __shfl_sync(0xffffffffu, a[q], c, 8);
+      const float piv = pr[c];
+      ok = ok && piv > 0.0f && isfinite(piv);
+      const float inv = 1.0f / piv, fr = a[c];
+#pragma unroll
+      for (int q = 0; q < kGroupMax; ++q) {
+        if (q == c) a[q] = r == c ? inv : -fr * inv;
+        else a[q] = r == c ? pr[q] * inv : a[q] - fr * (pr[q] * inv);
       }
     }
-    for (int r = 0; r < lead_k; ++r) R.wv[lead_f + r] = float(wsum[r]);
+    if (active && r < k) {
+      const float di = float(DI[a0 + r0 + f + r]);
+#pragma unroll
+      for (int q = 0; q < kGroupMax; ++q) R.binv[kGroupMax * (f + r) + q] = q >= k ? 0.0f : ok ? a[q] : (q == r ? di : 0.0f);
+    }
   }
+  __syncthreads();  // the scratch (p .. gl) is free again
+  // 5. Jacobi rows, w = M^-1 1 (the stored inverse rows' sums), D, eta D^-1, the row starts
   double s1[1] = {0.0};
   for (int i = tid; i < m; i += blockDim.x) {
     const int a = a0 + r0 + i;
     const double di = DI[a];
+    float wsum = float(di);
     if (R.size[i] < 2) {
       R.binv[kGroupMax * i] = float(di);
       for (int c = 1; c < kGroupMax; ++c) R.binv[kGroupMax * i + c] = 0.0f;
-      R.wv[i] = float(di);
+    } else {
+      wsum = 0.0f;
+      for (int c = 0; c < kGroupMax; ++c) wsum += R.binv[kGroupMax * i + c];
     }
+    R.wv[i] = wsum;
     R.dd[i] = float(1.0 / di);
     R.etadi[i] = float(atom_prm(ff, w.type[a], A_ETA) * di);
     R.rp[i] = w.cnt[a] - M.ebeg;
+    s1[0] += double(wsum);
   }
   if (tid == 0) R.rp[m] = w.cnt[a0 + r1] - M.ebeg;
   __syncthreads();
-  for (int i = tid; i < m; i += blockDim.x) s1[0] += double(R.wv[i]);
-  warp_sum_all<1>(s1);
+  rows_sum_all<1>(s1, m);
   auto keep = [&](double* t) { sh.sd_s1w = t[0]; };
   if (!team_sum<1>(team, w, s1, sh.red, 0, keep)) return false;
   // 5. c = H w: D w of the own rows into every block's yt, then the product over the cached rows
@@ -1206,14 +1191,16 @@ __device__ bool qeq_residual(const XrWork& w, const XrFF& ff, const Team& team, 
       for (; e < ee; e += gs) hx += w.hval[e] * __ldcg(X + w.edge[e].x);
     }
     for (int o = gs / 2; o > 0; o >>= 1) hx += __shfl_xor_sync(0xffffffffu, hx, o);
-    if (sub == 0 && r < r1) {
-      const int t = w.type[a];
-      const double g = hx + atom_prm(ff, t, A_ETA) * X[a] + (adjoint ? w.qrhs[a] : atom_prm(ff, t, A_CHI));
-      G[a] = g;
-      acc[0] += DI[a] * g;
-    }
+    if (sub == 0 && r < r1) G[a] = hx;  // finished one row per thread below
   }
-  warp_sum_all<1>(acc);
+  __syncthreads();
+  for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+    const int a = a0 + r, t = w.type[a];
+    const double g = G[a] + atom_prm(ff, t, A_ETA) * X[a] + (adjoint ? w.qrhs[a] : atom_prm(ff, t, A_CHI));
+    G[a] = g;
+    acc[0] += DI[a] * g;
+  }
+  rows_sum_all<1>(acc, r1 - r0);
   if (!team_sum<1>(team, w, acc, sh.red, slot, noop)) return false;
   slot = slot == 1 ? 2 : 1;
   const double lam = acc[0] / s1;
@@ -1224,7 +1211,7 @@ __device__ bool qeq_residual(const XrWork& w, const XrFF& ff, const Team& team, 
     G[a] = g;
     acc2[0] += DI[a] * g * g;
   }
-  warp_sum_all<1>(acc2);
+  rows_sum_all<1>(acc2, r1 - r0);
   if (!team_sum<1>(team, w, acc2, sh.red, slot, noop)) return false;
   slot = slot == 1 ? 2 : 1;
   *gz_out = acc2[0];
@@ -1318,17 +1305,60 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
       for (; e < ee; e += gs)
         if (w.edge[e].x == a) d += w.hval[e];
     }
-    for (int o = gs / 2; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
-    if (sub == 0 && r < r1) {
-      DI[a] = 1.0 / (atom_prm(ff, w.type[a], A_ETA) + d);
-      X[a] = warm ? w.qguess[a] : x0;
-    }
+    if (__any_sync(0xffffffffu, d != 0.0))  // self images: small periodic cells only
+      for (int o = gs / 2; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+    if (sub == 0 && r < r1) DI[a] = d;  // the shield sum; the diagonal follows one row per thread
+  }
+  __syncthreads();
+  for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+    const int a = a0 + r;
+    const double di = 1.0 / (atom_prm(ff, w.type[a], A_ETA) + DI[a]);
+    DI[a] = di;
+    F[5 * w.A + a] = float(di);
+    X[a] = warm ? w.qguess[a] : x0;
   }
   if (!team.sync(w)) return;
   // 2. Pre-scaled rows H'_ij = H_ij / D_jj (cached in FP32 or FP64, or in hval in place), row sums
-  //    c_i = sum_j H'_ij + eta_i D_ii^-1, and the start gradient g = H x + chi.
-  double acc[5] = {0, 0, 0, 0, 0};
-  for (int rb = r0 + wid * gpw; rb < r1; rb += nw * gpw) {
+  //    c_i = sum_j H'_ij + eta_i D_ii^-1, and the start gradient g = H x + chi. The FP64 sums are
+  //    formed only where they are read: the row sums r_i = sum_j H_ij for a uniform start x0 != 0,
+  //    H x for a warm start, and c for the solves other than the shared-memory row solver (whose
+  //    FP64 fallback forms c itself). A cold neutral start with FP32 rows needs no FP64 per entry:
+  //    its cache entries are hval's FP32 copy times the FP32 diagonal.
+  const bool need_rs = x0 != 0.0;
+  const bool need_cs = !(small_rows && mixed);
+  const bool fast = mixed && !need_rs && !need_cs && !warm;
+  const float* const DI32 = F + 5 * w.A;
+  for (int rb = r0 + wid * gpw; rb < r1 && fast; rb += nw * gpw) {
+    const int r = rb + lane / gs, a = a0 + r;
+    if (r < r1) {
+      float* const ch = reinterpret_cast<float*>(cache_h);
+      const int ee = w.cnt[a + 1];
+      int e = w.cnt[a] + sub;
+      for (; e + 3 * gs < ee; e += 4 * gs) {
+        int j[4];
+        float h[4], dj[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          j[u] = w.edge[e + u * gs].x;
+          h[u] = w.qch[e + u * gs];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) dj[u] = __ldcg(DI32 + j[u]);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          cache_j[e + u * gs - ebeg] = (unsigned short)(j[u] - a0);
+          ch[e + u * gs - ebeg] = h[u] * dj[u];
+        }
+      }
+      for (; e < ee; e += gs) {
+        const int j = w.edge[e].x;
+        const float h = w.qch[e];
+        cache_j[e - ebeg] = (unsigned short)(j - a0);
+        ch[e - ebeg] = h * __ldcg(DI32 + j);
+      }
+    }
+  }
+  for (int rb = r0 + wid * gpw; rb < r1 && !fast; rb += nw * gpw) {
     const int r = rb + lane / gs, a = a0 + r;
     double rs = 0, cs = 0, hx = 0;
     auto put = [&](int e, int j, double h, double dj, double xj) {
@@ -1371,26 +1401,33 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
       }
     }
     for (int o = gs / 2; o > 0; o >>= 1) {
-      rs += __shfl_xor_sync(0xffffffffu, rs, o);
-      cs += __shfl_xor_sync(0xffffffffu, cs, o);
+      if (need_rs) rs += __shfl_xor_sync(0xffffffffu, rs, o);
+      if (need_cs) cs += __shfl_xor_sync(0xffffffffu, cs, o);
       if (warm) hx += __shfl_xor_sync(0xffffffffu, hx, o);
     }
-    if (sub == 0 && r < r1) {
-      const int t = w.type[a];
-      const double eta = atom_prm(ff, t, A_ETA), di = DI[a], chi = adjoint ? w.qrhs[a] : atom_prm(ff, t, A_CHI);
-      const double gu = x0 * (rs + eta) + chi;
-      const double g = warm ? hx + eta * X[a] + chi : gu;
-      Cr[a] = cs + eta * di;
-      G[a] = g;
-      QW(Q_HP, a) = gu;  // parked for the projection step below
-      acc[0] += di;
-      acc[1] += di * g;
-      acc[2] += di * g * g;
-      acc[3] += di * gu;
-      acc[4] += di * gu * gu;
+    if (sub == 0 && r < r1) {  // the row's sums, finished one row per thread below
+      Cr[a] = cs;
+      QW(Q_HP, a) = rs;
+      G[a] = hx;
     }
   }
-  warp_sum_all<5>(acc);
+  __syncthreads();
+  double acc[5] = {0, 0, 0, 0, 0};
+  for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+    const int a = a0 + r, t = w.type[a];
+    const double eta = atom_prm(ff, t, A_ETA), di = DI[a], chi = adjoint ? w.qrhs[a] : atom_prm(ff, t, A_CHI);
+    const double gu = need_rs ? x0 * (QW(Q_HP, a) + eta) + chi : chi;
+    const double g = warm ? G[a] + eta * X[a] + chi : gu;
+    if (need_cs) Cr[a] = Cr[a] + eta * di;
+    G[a] = g;
+    QW(Q_HP, a) = gu;  // parked for the projection step below
+    acc[0] += di;
+    acc[1] += di * g;
+    acc[2] += di * g * g;
+    acc[3] += di * gu;
+    acc[4] += di * gu * gu;
+  }
+  rows_sum_all<5>(acc, r1 - r0);
   if (!team_sum<5>(team, w, acc, smem, 0, noop)) return;
   const double s1 = acc[0];
   // 3. Project the start gradient explicitly (g - lambda with lambda = <D^-1, g> / <D^-1, 1>) and take
@@ -1411,7 +1448,7 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
       acc2[2] += di * gt;
     }
   }
-  warp_sum_all<3>(acc2);
+  rows_sum_all<3>(acc2, r1 - r0);
   if (!team_sum<3>(team, w, acc2, smem, 1, noop)) return;
   const double tol2 = w.cg_tol * w.cg_tol;
   const double gfloor = 1e-28 * fmax(acc[2], acc[4]);
@@ -1465,7 +1502,7 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
         X[a] += double(v32.y[a]);
         sx[0] += X[a];
       }
-      warp_sum_all<1>(sx);
+      rows_sum_all<1>(sx, r1 - r0);
       if (!team_sum<1>(team, w, sx, smem, slot, noop)) return;
       slot = slot == 1 ? 2 : 1;
       const double shift = (Q - sx[0]) / n;
@@ -1484,6 +1521,17 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
   }
   if (fp64) {
     // 4b. FP64 projected CG from the current charges (cold: the start point) to the tolerance.
+    if (!need_cs) {  // its row sums c, which the row solver's setup did not need
+      for (int rb = r0 + wid * gpw; rb < r1; rb += nw * gpw) {
+        const int r = rb + lane / gs, a = a0 + r;
+        double cs = 0;
+        if (r < r1)
+          for (int e = w.cnt[a] + sub; e < w.cnt[a + 1]; e += gs) cs += w.hval[e] * __ldcg(DI + w.edge[e].x);
+        for (int o = gs / 2; o > 0; o >>= 1) cs += __shfl_xor_sync(0xffffffffu, cs, o);
+        if (sub == 0 && r < r1) Cr[a] = cs + atom_prm(ff, w.type[a], A_ETA) * DI[a];
+      }
+      __syncthreads();
+    }
     QeqVecs<double> v64{G, &QW(Q_G2, 0), &QW(Q_P, 0), &QW(Q_HP, 0), X};
     QeqMatrix<double> M64{reinterpret_cast<const double*>(cache_h), cache_j, cached64, !mixed, ebeg,
                           reinterpret_cast<double*>(gstage)};
@@ -1504,7 +1552,7 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
   // 5. Final charges; the constraint is restored exactly against accumulated rounding.
   double sx[1] = {0.0};
   for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) sx[0] += X[a0 + r];
-  warp_sum_all<1>(sx);
+  rows_sum_all<1>(sx, r1 - r0);
   if (!team_sum<1>(team, w, sx, smem, 3, noop)) return;
   const double shift = (Q - sx[0]) / n;
   for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
