@@ -431,6 +431,10 @@ struct QeqShared {
   double sc_lam, sc_alpha, sc_step, sc_beta;
   float sf_lam, sf_alpha, sf_step, sf_beta, sf_gz, sf_stop;
   double sd_s1w;  // <1, M^-1 1> of the FP32 row solver's block-Jacobi preconditioner
+  // Scalars of the solve formed once, by the thread that runs a reduction's post hook (a division
+  // done by every warp would cost the FP64 pipe once per warp): the start multipliers, the target,
+  // the floor and the next sweep's stop ratio.
+  double sd_l0, sd_lu, sd_target, sd_gfloor, sd_ratio;
   int sc_next;  // the next small system of the block (work sharing)
   int sc_groups;  // preconditioner groups of two or more rows (row solver setup)
   double cred[2][8][8];  // cluster team: partials pushed by the blocks of the cluster
@@ -1161,12 +1165,11 @@ __device__ __noinline__ int qeq_cg_rows32(const XrWork& w, const Team& team, Qeq
 // <D^-1, G^2> (from the projected values, so free of cancellation). Two team reductions.
 template <class Team>
 __device__ bool qeq_residual(const XrWork& w, const XrFF& ff, const Team& team, QeqShared& sh, int a0, int r0, int r1,
-                             double s1, double* gz_out, int& slot, bool adjoint) {
+                             double s1, double target, double* gz_out, int& slot, bool adjoint) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   double* X = &QW(Q_X, 0);
   double* G = &QW(Q_G, 0);
   const double* DI = &QW(Q_DINV, 0);
-  auto noop = [](double*) {};
   const int gs = row_group(r1 - r0), sub = lane & (gs - 1), gpw = 32 / gs;
   double acc[1] = {0.0};
   for (int rb = r0 + wid * gpw; rb < r1; rb += nw * gpw) {
@@ -1201,9 +1204,9 @@ __device__ bool qeq_residual(const XrWork& w, const XrFF& ff, const Team& team, 
     acc[0] += DI[a] * g;
   }
   rows_sum_all<1>(acc, r1 - r0);
-  if (!team_sum<1>(team, w, acc, sh.red, slot, noop)) return false;
+  if (!team_sum<1>(team, w, acc, sh.red, slot, [&](double* t) { t[0] = t[0] / s1; })) return false;
   slot = slot == 1 ? 2 : 1;
-  const double lam = acc[0] / s1;
+  const double lam = acc[0];
   double acc2[1] = {0.0};
   for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
     const int a = a0 + r;
@@ -1212,7 +1215,9 @@ __device__ bool qeq_residual(const XrWork& w, const XrFF& ff, const Team& team, 
     acc2[0] += DI[a] * g * g;
   }
   rows_sum_all<1>(acc2, r1 - r0);
-  if (!team_sum<1>(team, w, acc2, sh.red, slot, noop)) return false;
+  // (and the stop ratio of a sweep from here: 1e-10 of the norm, no further than 1e-2 of the target)
+  auto ratio = [&](double* t) { sh.sd_ratio = t[0] > 0.0 ? fmax(1e-10 * t[0], 0.01 * target) / t[0] : 1.0; };
+  if (!team_sum<1>(team, w, acc2, sh.red, slot, ratio)) return false;
   slot = slot == 1 ? 2 : 1;
   *gz_out = acc2[0];
   return true;
@@ -1247,7 +1252,7 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
   double* Cr = &QW(Q_C, 0);
   float* F = reinterpret_cast<float*>(&QW(7, 0));  // FP32 vectors and row constants: 8 x A floats in slots 7..10
   auto noop = [](double*) {};
-  const double x0 = Q / n;
+  const double x0 = Q == 0.0 ? 0.0 : Q / n;
   const int ebeg = w.cnt[a0 + r0], eend = w.cnt[a0 + r1];
   const int nent = eend - ebeg;
   // Shared-memory plan: [gradient stage: n doubles when it takes at most half the space][row cache].
@@ -1428,13 +1433,17 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
     acc[4] += di * gu * gu;
   }
   rows_sum_all<5>(acc, r1 - r0);
-  if (!team_sum<5>(team, w, acc, smem, 0, noop)) return;
+  if (!team_sum<5>(team, w, acc, smem, 0, [&](double* t) {
+        sh.sd_l0 = t[1] / t[0];
+        sh.sd_lu = t[3] / t[0];
+      }))
+    return;
   const double s1 = acc[0];
   // 3. Project the start gradient explicitly (g - lambda with lambda = <D^-1, g> / <D^-1, 1>) and take
   //    its norm from the projected values: sum D^-1 g^2 - lambda sum D^-1 g cancels to rounding noise
   //    of the unprojected gradient when the start is (nearly) the solution, e.g. q = 0 for identical
   //    atoms. The uniform start's projected norm sets the convergence scale.
-  const double lam0 = acc[1] / s1, lamu = acc[3] / s1;
+  const double lam0 = sh.sd_l0, lamu = sh.sd_lu;
   double acc2[3] = {0, 0, 0};  // <D^-1, g~^2>, <D^-1, g~_u^2>, <D^-1, g~>
   for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
     {
@@ -1449,11 +1458,14 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
     }
   }
   rows_sum_all<3>(acc2, r1 - r0);
-  if (!team_sum<3>(team, w, acc2, smem, 1, noop)) return;
-  const double tol2 = w.cg_tol * w.cg_tol;
-  const double gfloor = 1e-28 * fmax(acc[2], acc[4]);
-  const double gz0 = acc2[1];  // the uniform start's projected norm (= the start's when cold)
-  const double target = tol2 * gz0;
+  // the target: tol^2 of the uniform start's projected norm (= the start's when cold)
+  if (!team_sum<3>(team, w, acc2, smem, 1, [&](double* t) {
+        sh.sd_target = w.cg_tol * w.cg_tol * t[1];
+        sh.sd_gfloor = 1e-28 * fmax(acc[2], acc[4]);
+        sh.sd_ratio = t[0] > 0.0 ? fmax(1e-10 * t[0], 0.01 * sh.sd_target) / t[0] : 1.0;
+      }))
+    return;
+  const double target = sh.sd_target, gfloor = sh.sd_gfloor;
   double gz = acc2[0];
   int slot = 2;
   int iters = 0;
@@ -1486,11 +1498,10 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
         if (!team.sync(w)) return;
       }
       // the correction's own projected norm starts at gz; 1e-10 of it (1e-5 in norm) per sweep,
-      // and no further than a hundredth of the final target
-      const double stop = fmax(1e-10 * gz, 0.01 * target);
-      const int it = small_rows ? qeq_cg_rows32(w, team, sh, a0, n, r0, r1, M32, v32.y, stop / gz, 400, v32.g, &slot)
-                                : qeq_cg<Team, float>(w, ff, team, sh, a0, n, r0, r1, v32, M32, s1, gz, stop, 0.0, 400,
-                                                      false, slot);
+      // and no further than a hundredth of the final target (sd_ratio: that stop over gz)
+      const int it = small_rows ? qeq_cg_rows32(w, team, sh, a0, n, r0, r1, M32, v32.y, sh.sd_ratio, 400, v32.g, &slot)
+                                : qeq_cg<Team, float>(w, ff, team, sh, a0, n, r0, r1, v32, M32, s1, gz,
+                                                      fmax(1e-10 * gz, 0.01 * target), 0.0, 400, false, slot);
       if (it < 0) return;
       iters += it;
       // x += y, then restore sum x = Q exactly: the FP32 step keeps sum y = 0 only to FP32 rounding,
@@ -1503,13 +1514,13 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
         sx[0] += X[a];
       }
       rows_sum_all<1>(sx, r1 - r0);
-      if (!team_sum<1>(team, w, sx, smem, slot, noop)) return;
+      if (!team_sum<1>(team, w, sx, smem, slot, [&](double* t) { t[0] = (Q - t[0]) / n; })) return;
       slot = slot == 1 ? 2 : 1;
-      const double shift = (Q - sx[0]) / n;
+      const double shift = sx[0];
       for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) X[a0 + r] += shift;
       if (!team.sync(w)) return;
       double gz_new = 0.0;
-      if (!qeq_residual(w, ff, team, sh, a0, r0, r1, s1, &gz_new, slot, adjoint)) return;
+      if (!qeq_residual(w, ff, team, sh, a0, r0, r1, s1, target, &gz_new, slot, adjoint)) return;
       const bool stalled = gz_new > 1e-3 * gz;
       gz = gz_new;
       if (stalled && gz > target) {
@@ -1553,8 +1564,8 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
   double sx[1] = {0.0};
   for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) sx[0] += X[a0 + r];
   rows_sum_all<1>(sx, r1 - r0);
-  if (!team_sum<1>(team, w, sx, smem, 3, noop)) return;
-  const double shift = (Q - sx[0]) / n;
+  if (!team_sum<1>(team, w, sx, smem, 3, [&](double* t) { t[0] = (Q - t[0]) / n; })) return;
+  const double shift = sx[0];
   for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
     const int a = a0 + r;
     const double q = X[a] + shift;
