@@ -157,7 +157,8 @@ def test_full_size_properties(water_4608):
     b = c.evaluate(s.symbols, s.positions, cell=s.cell, pbc=s.pbc)
     assert a.energy == b.energy  # deterministic reductions
     np.testing.assert_array_equal(a.charges, b.charges)
-    np.testing.assert_allclose(a.forces, b.forces, atol=1e-12, rtol=0)
+    # forces repeat to the last bits only (the many-body kernels add with atomics): a few ulps
+    np.testing.assert_allclose(a.forces, b.forces, atol=1e-12, rtol=1e-13)
     assert abs(a.charges.sum()) < 1e-10
     np.testing.assert_allclose(a.forces.sum(axis=0), 0.0, atol=1e-8)
     # periodic wrapping and translation leave the physics unchanged

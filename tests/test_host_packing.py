@@ -94,3 +94,31 @@ def test_fill_checks_its_arguments(host):
         host.fill([item, item], TYPES, types, x)  # more atoms than the outputs hold
     with pytest.raises(ValueError):
         host.fill([["C", "H"]], TYPES, types, x)  # a request is a tuple
+
+
+def test_guesses_takes_float64_charges_in_place(host):
+    sym = ["C", "H", "O"]
+    q = np.array([0.1, -0.2, 0.1])
+    wide = np.array([[0.1, -0.2, 0.1], [0.0, 0.0, 0.0]])
+    items = [
+        request(sym, np.zeros((3, 3))),                                  # 0 none: address 0
+        request(sym, np.zeros((3, 3)), initial=q),                       # 1 taken in place
+        request(sym, np.zeros((3, 3)), initial=q.astype(np.float32)),    # 2 not float64
+        request(sym, np.zeros((3, 3)), initial=q[:2]),                   # 3 not one per atom
+        request(sym, np.zeros((3, 3)), initial=np.array([0.1, np.inf, 0.0])),  # 4 non-finite
+        request(sym, np.zeros((3, 3)), initial=q.tolist()),              # 5 no buffer
+        request(sym, np.zeros((3, 3)), initial=wide[:, 0:3:1][0:1]),     # 6 two-dimensional
+        request(sym, np.zeros((3, 3)), initial=np.arange(6.0)[::2]),     # 7 strided
+        request(sym, np.zeros((3, 3)), initial=wide[1]),                 # 8 a C-contiguous row view: taken
+        (sym, np.zeros((3, 3)), 0, None, None),                          # 9 not the six fields
+    ]
+    addr = np.full(len(items), 99, dtype=np.uint64)
+    slow = host.guesses(items, addr)
+    assert slow == [2, 3, 4, 5, 6, 7, 9]
+    assert addr[0] == 0
+    assert addr[1] == q.__array_interface__["data"][0]
+    assert addr[8] == wide.__array_interface__["data"][0] + 24
+    with pytest.raises(ValueError):
+        host.guesses(items, np.zeros(len(items) - 1, dtype=np.uint64))
+    with pytest.raises(TypeError):
+        host.guesses(tuple(items), addr)

@@ -13,6 +13,7 @@ from __future__ import annotations
 import math
 from dataclasses import dataclass, field
 from numbers import Real
+from typing import NamedTuple
 
 import numpy as np
 
@@ -204,6 +205,14 @@ class ParameterGradient:
         for key, records in ff.angles.items():
             angles[key] = [rec.get(id(r), np.zeros(7)).copy() for r in records]
         return cls(pairs, angles)
+
+
+class _GuessAddresses(NamedTuple):
+    """Initial charges of a packed batch: one address per system (0: none) and the converted arrays
+    that some of them point into (held until the call returns)."""
+
+    addr: np.ndarray
+    keep: list
 
 
 def _guess(initial_charges, n):
@@ -405,7 +414,15 @@ class Calculator:
         flags_l = [_NO_PBC] * n_sys
         cells = [None] * n_sys
         reps = [(1, 1, 1)] * n_sys
-        guesses = [None] * n_sys
+        # initial charges: the host module takes float64 arrays of finite charges as they are; the
+        # rest get the Python checks (and a converted copy, held with the addresses)
+        guess_addr = np.zeros(n_sys, dtype=np.uint64)
+        keep = []
+        for k in _host.guesses(items, guess_addr):
+            g = _guess(items[k][5], sizes[k])
+            if g is not None:
+                keep.append(g)
+                guess_addr[k] = nat.addr(g)
         offsets = np.zeros(n_sys + 1, dtype=np.int64)
         np.cumsum(sizes, out=offsets[1:])
         for k in slow:
@@ -419,7 +436,7 @@ class Calculator:
         cutoff = None
         slow_set = set(slow)
         for k, it in enumerate(items):
-            cell, pbc, initial = it[3], it[4], it[5]
+            cell, pbc = it[3], it[4]
             if k not in slow_set and not ((pbc is None and cell is None) or pbc is False):
                 if cutoff is None:
                     cutoff = float(self.force_field.general[12])
@@ -432,10 +449,8 @@ class Calculator:
                         reps[k] = cell_repetitions(cutoff, flags, m, sizes[k], self.max_expanded_atoms)
                         cells[k] = np.ascontiguousarray(m, dtype=np.float64)
                     flags_l[k] = flags
-            if initial is not None:
-                guesses[k] = _guess(initial, sizes[k])
         charges = [float(it[2]) for it in items]
-        return types, x, offsets, flags_l, cells, charges, guesses, reps
+        return types, x, offsets, flags_l, cells, charges, _GuessAddresses(guess_addr, keep), reps
 
     def _run(self, batch, full_derivative, reps, backend, extra_flags=0):
         """One ``xr_eval_batch`` call over ``batch`` = [(types, positions, pbc flags, cell, total
@@ -474,7 +489,10 @@ class Calculator:
         sys_arr["total_charge"] = charges
         if any(c is not None for c in cells):
             sys_arr["cell"] = [0 if c is None else nat.addr(c) for c in cells]
-        if any(g is not None for g in guesses):
+        if isinstance(guesses, _GuessAddresses):
+            if guesses.addr.any():
+                sys_arr["charges_guess"] = guesses.addr
+        elif any(g is not None for g in guesses):
             sys_arr["charges_guess"] = [0 if g is None else nat.addr(g) for g in guesses]
         # one allocation per kind for the whole batch, every element written by the call; each
         # Evaluation gets views

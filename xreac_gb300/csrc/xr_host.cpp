@@ -7,7 +7,11 @@
 // after a finiteness check. A request this cannot take as is (another container or dtype, a label
 // missing from the map, a non-finite coordinate, a total charge that is not a finite int or float)
 // is left for the Python path, which applies xreac's validation and messages; fill returns the
-// indices of those requests. Cells, periodicity and initial charges are always handled in Python.
+// indices of those requests. Cells and periodicity are always handled in Python.
+//
+// guesses(items, addr_out) takes the requests' initial charges: None gives address 0, a C-contiguous
+// float64 buffer of one finite charge per atom gives its data address (valid while the caller holds
+// the request), and anything else is left for the Python checks; it returns the indices of those.
 #include <Python.h>
 
 #include <cmath>
@@ -127,8 +131,66 @@ PyObject* fill(PyObject*, PyObject* args) {
   return slow;
 }
 
+// 0: taken (address in *addr, 0 for None); 1: left for Python
+int guess_one(PyObject* item, unsigned long long* addr) {
+  *addr = 0;
+  if (!PyTuple_Check(item) || PyTuple_GET_SIZE(item) != 6) return 1;
+  PyObject* initial = PyTuple_GET_ITEM(item, 5);
+  if (initial == Py_None) return 0;
+  const Py_ssize_t n = PyObject_Length(PyTuple_GET_ITEM(item, 0));
+  if (n < 0) {
+    PyErr_Clear();
+    return 1;
+  }
+  Py_buffer view;
+  if (PyObject_GetBuffer(initial, &view, PyBUF_C_CONTIGUOUS | PyBUF_FORMAT | PyBUF_ND) != 0) {
+    PyErr_Clear();
+    return 1;
+  }
+  int rc = 1;
+  if (view.ndim == 1 && view.shape[0] == n && view.itemsize == 8 && view.format && std::strcmp(view.format, "d") == 0) {
+    const double* q = static_cast<const double*>(view.buf);
+    bool ok = true;
+    for (Py_ssize_t k = 0; k < n; ++k) ok = ok && std::isfinite(q[k]);
+    if (ok) {
+      *addr = reinterpret_cast<unsigned long long>(view.buf);
+      rc = 0;
+    }
+  }
+  PyBuffer_Release(&view);
+  return rc;
+}
+
+PyObject* guesses(PyObject*, PyObject* args) {
+  PyObject *items, *addr_obj;
+  if (!PyArg_ParseTuple(args, "O!O", &PyList_Type, &items, &addr_obj)) return nullptr;
+  Py_buffer av;
+  if (PyObject_GetBuffer(addr_obj, &av, PyBUF_C_CONTIGUOUS | PyBUF_WRITABLE | PyBUF_FORMAT) != 0) return nullptr;
+  const Py_ssize_t nitems = PyList_GET_SIZE(items);
+  PyObject* slow = nullptr;
+  if (av.itemsize != 8 || av.len != 8 * nitems) {
+    PyErr_SetString(PyExc_ValueError, "guesses needs one uint64 address per request");
+  } else if ((slow = PyList_New(0)) != nullptr) {
+    unsigned long long* addr = static_cast<unsigned long long*>(av.buf);
+    for (Py_ssize_t k = 0; k < nitems; ++k) {
+      if (guess_one(PyList_GET_ITEM(items, k), addr + k) == 0) continue;
+      PyObject* idx = PyLong_FromSsize_t(k);
+      if (!idx || PyList_Append(slow, idx) != 0) {
+        Py_XDECREF(idx);
+        Py_CLEAR(slow);
+        break;
+      }
+      Py_DECREF(idx);
+    }
+  }
+  PyBuffer_Release(&av);
+  return slow;
+}
+
 PyMethodDef methods[] = {
     {"fill", fill, METH_VARARGS, "Pack a batch's symbols and positions; returns the requests left for Python."},
+    {"guesses", guesses, METH_VARARGS,
+     "Addresses of the requests' initial charges (0 for None); returns the requests left for Python."},
     {nullptr, nullptr, 0, nullptr},
 };
 

@@ -288,17 +288,16 @@ class Server:
         h2d, d2h = calc.transfer_bytes()
         self.batches.append(Batch(name, len(batch), sum(len(it[0]) for it in items), done - t0, calc.last_launches,
                                   its, qbytes, h2d, d2h))
-        with self._charges_lock:
-            for (req, _), res in zip(batch, results):
-                if req.session is not None and not isinstance(res, Exception):
-                    charges[req.session] = res  # its charges are read when the session's next step comes
         nb = len(batch)
-        for (req, fut), res in zip(batch, results):
-            if isinstance(res, Exception):
-                fut._error = res
-            else:
-                fut._value = Served(res, req.arrival, done, nb, t0)
-            fut._done = True
+        with self._charges_lock:
+            for (req, fut), res in zip(batch, results):
+                if isinstance(res, Exception):
+                    fut._error = res
+                else:
+                    if req.session is not None:
+                        charges[req.session] = res  # its charges are read when the session's next step comes
+                    fut._value = Served(res, req.arrival, done, nb, t0)
+                fut._done = True
         with self._done_cv:
             self._done_cv.notify_all()
 
