@@ -111,10 +111,11 @@ def test_guesses_takes_float64_charges_in_place(host):
         request(sym, np.zeros((3, 3)), initial=np.arange(6.0)[::2]),     # 7 strided
         request(sym, np.zeros((3, 3)), initial=wide[1]),                 # 8 a C-contiguous row view: taken
         (sym, np.zeros((3, 3)), 0, None, None),                          # 9 not the six fields
+        request(sym, np.zeros((3, 3)), initial=memoryview(q)),           # 10 a buffer, not an array
     ]
     addr = np.full(len(items), 99, dtype=np.uint64)
     slow = host.guesses(items, addr)
-    assert slow == [2, 3, 4, 5, 6, 7, 9]
+    assert slow == [2, 3, 4, 5, 6, 7, 9, 10]
     assert addr[0] == 0
     assert addr[1] == q.__array_interface__["data"][0]
     assert addr[8] == wide.__array_interface__["data"][0] + 24

@@ -10,8 +10,9 @@
 // indices of those requests. Cells and periodicity are always handled in Python.
 //
 // guesses(items, addr_out) takes the requests' initial charges: None gives address 0, a C-contiguous
-// float64 buffer of one finite charge per atom gives its data address (valid while the caller holds
-// the request), and anything else is left for the Python checks; it returns the indices of those.
+// float64 numpy array of one finite charge per atom gives its data address (valid while the caller
+// holds the request; other buffer exporters may not keep their memory after the export ends), and
+// anything else is left for the Python checks; it returns the indices of those.
 #include <Python.h>
 
 #include <cmath>
@@ -137,6 +138,7 @@ int guess_one(PyObject* item, unsigned long long* addr) {
   if (!PyTuple_Check(item) || PyTuple_GET_SIZE(item) != 6) return 1;
   PyObject* initial = PyTuple_GET_ITEM(item, 5);
   if (initial == Py_None) return 0;
+  if (std::strcmp(Py_TYPE(initial)->tp_name, "numpy.ndarray") != 0) return 1;
   const Py_ssize_t n = PyObject_Length(PyTuple_GET_ITEM(item, 0));
   if (n < 0) {
     PyErr_Clear();
