@@ -95,6 +95,15 @@ def test_sessions_hand_charges_to_the_next_step(server):
     np.testing.assert_array_equal(c.evaluation.charges, 0.5)
 
 
+def test_a_failed_step_keeps_the_session_charges(server):
+    server.submit(_req(3, session="traj")).result(timeout=10)  # charges 0.5
+    bad = server.submit(_req(3, session="traj", bad=True))
+    with pytest.raises(ValueError):
+        bad.result(timeout=10)
+    c = server.submit(_req(3, session="traj")).result(timeout=10)
+    np.testing.assert_array_equal(c.evaluation.charges, 1.5)  # from the last good step
+
+
 def test_unknown_force_field_and_closed_server(server):
     with pytest.raises(ValueError):
         server.submit(serving.Request(["H"], np.zeros((1, 3)), "other"))
