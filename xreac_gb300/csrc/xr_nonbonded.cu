@@ -897,8 +897,9 @@ __device__ __noinline__ bool qeq_rows32_setup(const XrWork& w, const XrFF& ff, c
   }
   // 4. inverse blocks by Gauss-Jordan elimination without pivoting: a group's block is symmetric
   //    and, for a molecule, positive definite, so its pivots are positive; a block with a pivot
-  //    that is not (H can be indefinite for close-packed atoms) falls back to Jacobi. Eight lanes per group, lane r holding row r of the block (rows past the group's
-  //    size padded with the identity); the groups' first rows are listed in rp (written in step 5).
+  //    that is not (H can be indefinite for close-packed atoms) falls back to Jacobi. Eight lanes
+  //    per group, lane r holding row r of the block (rows past the group's size padded with the
+  //    identity); the groups' first rows are listed in rp (written in step 5).
   int* list = R.rp;
   if (tid == 0) sh.sc_groups = 0;
   __syncthreads();
