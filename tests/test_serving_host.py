@@ -118,3 +118,17 @@ def test_submit_many_matches_single_submits(server):
     assert [f.result(timeout=10).evaluation.energy for f in futs] == [float(r.natoms) for r in reqs]
     with pytest.raises(ValueError):
         server.submit_many([_req(1), serving.Request(["H"], np.zeros((1, 3)), "other")])
+
+
+def test_batches_respect_the_atom_and_request_budgets(monkeypatch):
+    monkeypatch.setattr(serving, "Calculator", _Calc)
+    sizes = (3, 3, 3, 3, 12, 2, 2, 2, 2, 1)
+    with serving.Server({"ff": object()}, workers=1, max_batch_atoms=10, max_batch_requests=3) as srv:
+        reqs = [_req(n) for n in sizes]
+        out, _ = serving.replay(srv, reqs)
+        batches = [(b.requests, b.atoms) for b in srv.batches]
+    assert [o.evaluation.energy for o in out] == [float(n) for n in sizes]
+    assert sum(r for r, _ in batches) == len(sizes)
+    assert all(r <= 3 for r, _ in batches)
+    assert all(a <= 10 or r == 1 for r, a in batches)  # a request above the budget is a batch alone
+    assert (1, 12) in batches
