@@ -33,7 +33,10 @@ enum xr_status {
   XR_ECAPACITY = 7,     /* a device list outgrew its limit (image shifts beyond +-255 cells) */
   XR_EBADPARAM = 8,     /* "Invalid p_boc* mixing for an active bond-order correction" */
   XR_ECUDA = 9,         /* CUDA runtime failure */
-  XR_EUNSUPPORTED = 10  /* requested option not available */
+  XR_EUNSUPPORTED = 10, /* requested option not available */
+  XR_ECG_NOCONV = 11,   /* the QEq conjugate gradient reached its iteration limit (xr_ctx_set_qeq) */
+  XR_EWAIT = 12         /* a device-side wait of the QEq solver gave up: a scheduling failure, not an
+                           input error; the context stays usable and the call may be repeated */
 };
 
 /* Evaluation flags. */
@@ -101,6 +104,14 @@ int xr_ctx_reserve(xr_ctx* ctx, int atoms, int systems, long long edges, long lo
 /* Solver settings: QEq conjugate-gradient relative residual and iteration limit. */
 int xr_ctx_set_qeq(xr_ctx* ctx, double tolerance, int max_iterations);
 
+/* Tests of the failure path of the QEq solver's team waits (no reference counterpart). Every wait
+ * of a thread-block cluster or grid team is bounded; polls > 0 replaces the default limits (2^22
+ * polls for a cluster exchange, 2^24 for a grid barrier; 0 restores them). fail_at > 0 makes team
+ * wait number fail_at of each solve wait for an arrival that never comes, so it runs out, the call
+ * returns XR_EWAIT and the context stays usable; 0 turns this off. Systems of at most 160 atoms
+ * (a single block, no team waits) are not affected. */
+int xr_ctx_set_wait_test(xr_ctx* ctx, long long polls, int fail_at);
+
 /* Evaluate one system (energy, fixed-charge forces, QEq charges, per-atom bond properties). */
 int xr_eval(xr_ctx* ctx, const xr_ff* ff, const xr_system* sys, unsigned flags, xr_result* out);
 
@@ -160,13 +171,16 @@ int xr_ctx_stage_times(const xr_ctx* ctx, double* ms, int n, long long* calls);
  * Writes counts[a] = number of directed neighbours (j, S) of atom a with |x_j - x_a + S @ cell|
  * <= cutoff, zero-shift self pairs excluded -- the row lengths of xr_get_neighbors's list for the
  * same cutoff -- and *total (may be NULL) = their sum. positions, cell and counts are HOST
- * pointers; types is not read. Work is issued on `stream` (a cudaStream_t, NULL = default stream),
- * which the call synchronises before returning.
+ * pointers; types is not read. Work is issued on `stream` (a cudaStream_t of the current device,
+ * NULL = default stream; a stream of another device is rejected with XR_EINPUT), which the call
+ * synchronises before returning.
  * All device scratch is one static array of the library: no cudaMalloc, cudaFree or allocating
  * library call. natoms above XR_STATIC_MAX_ATOMS is rejected with XR_ECAPACITY. Calls that overlap
  * in time on one device (two threads, or unordered streams) race on the shared scratch. The first
  * call on a device performs the set-up (a cudaGetSymbolAddress with that device current); make it
- * before any stream capture begins. xr_static_last_error() gives the message of this thread's last
+ * before any stream capture begins. The address found then is kept for the life of the process, so
+ * do not call this again on a device after cudaDeviceReset. Cells follow xr_eval's rules (finite,
+ * nonsingular, right-handed). xr_static_last_error() gives the message of this thread's last
  * failed call. */
 #define XR_STATIC_MAX_ATOMS 16384
 int xr_count_neighbors_static(const xr_system* sys, double cutoff, void* stream, int* counts, long long* total);

@@ -2,7 +2,7 @@
 
 Usage (needs the reference checkout; not run by the test suite):
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <path of the xreac v0.10.0 checkout> [case ...]
 
 The reference depends on HIPS ``autograd``, which is not installed here, so the
 torch-backed stand-in in ``tests/golden/shim`` goes first on ``sys.path``. With
@@ -199,4 +199,6 @@ def main(reference, only=None):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference", set(sys.argv[2:]) or None)
+    if len(sys.argv) < 2:
+        sys.exit("usage: python tests/golden/make_golden.py <reference checkout> [case ...]")
+    main(sys.argv[1], set(sys.argv[2:]) or None)

@@ -100,3 +100,16 @@ def test_static_counts_of_a_small_cell_match_the_image_list():
     got, total = _static_counts(nat, nat.load(), x, cell, True, float(ff.general[12]))
     np.testing.assert_array_equal(got, want)
     assert total == len(i)
+
+
+def test_static_counts_reject_a_left_handed_cell():
+    from xreac_gb300 import _native as nat
+
+    lib = nat.load()
+    x = np.array([[0.0, 0.0, 0.0], [1.0, 0.0, 0.0]])
+    cell = np.diag([-20.0, 20.0, 20.0])  # det < 0: xr_eval rejects it with the same message
+    s = _system_struct(nat, x, cell, True)
+    counts = np.zeros(2, dtype=np.int32)
+    code = lib.xr_count_neighbors_static(ctypes.byref(s), 10.0, None, nat.ptr(counts, nat.c_int), None)
+    assert code == nat.XR_EINPUT
+    assert lib.xr_static_last_error().decode() == "Periodic cells must be nonsingular and right-handed"

@@ -25,6 +25,8 @@ XR_ECAPACITY = 7
 XR_EBADPARAM = 8
 XR_ECUDA = 9
 XR_EUNSUPPORTED = 10
+XR_ECG_NOCONV = 11
+XR_EWAIT = 12
 
 XR_FLAG_FULL_DERIVATIVE = 1
 XR_FLAG_DEVICE_IO = 2
@@ -38,6 +40,7 @@ EXPORTED = (
     "xr_last_error",
     "xr_ctx_set_qeq",
     "xr_ctx_reserve",
+    "xr_ctx_set_wait_test",
     "xr_eval",
     "xr_eval_batch",
     "xr_get_neighbors",
@@ -112,6 +115,8 @@ def load():
     lib.xr_ctx_set_qeq.restype = c_int
     lib.xr_ctx_reserve.argtypes = [c_void_p, c_int, c_int, c_longlong, c_longlong]
     lib.xr_ctx_reserve.restype = c_int
+    lib.xr_ctx_set_wait_test.argtypes = [c_void_p, c_longlong, c_int]
+    lib.xr_ctx_set_wait_test.restype = c_int
     lib.xr_eval.argtypes = [c_void_p, c_void_p, POINTER(System), c_uint, POINTER(Result)]
     lib.xr_eval.restype = c_int
     lib.xr_eval_batch.argtypes = [c_void_p, c_void_p, c_int, POINTER(System), c_uint, POINTER(Result)]

@@ -33,7 +33,7 @@ def _nvcc():
 
 
 def _headers():
-    return list(CSRC.glob("*.cuh")) + [ROOT / "include" / "xreac_gb300.h"]
+    return list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) + [ROOT / "include" / "xreac_gb300.h"]
 
 
 def _stale(target, deps):

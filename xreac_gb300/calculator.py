@@ -260,6 +260,14 @@ class Calculator:
         if self._lib.xr_ctx_set_qeq(self._ctx.handle, float(tolerance), int(max_iterations)) != nat.XR_OK:
             raise ValueError("QEq tolerance must be positive and the iteration limit at least 1")
 
+    def set_wait_test(self, polls=0, fail_at=0):
+        """For tests of the QEq solver's failure path (``xr_ctx_set_wait_test``): ``polls`` > 0
+        replaces the poll limits of the bounded team waits, and ``fail_at`` > 0 makes team wait number
+        ``fail_at`` of every solve wait for an arrival that never comes, so the call raises
+        ``RuntimeError`` while the context stays usable. ``set_wait_test()`` restores the defaults."""
+        if self._lib.xr_ctx_set_wait_test(self._ctx.handle, int(polls), int(fail_at)) != nat.XR_OK:
+            raise ValueError("polls and fail_at must be non-negative")
+
     def reserve(self, atoms, systems=1, edges_per_atom=450, bonds_per_atom=30):
         """Pre-size the device buffers for batches of up to ``atoms`` atoms in ``systems`` systems.
 
@@ -319,7 +327,7 @@ class Calculator:
         if code in _ERRORS:
             raise ValueError(_ERRORS[code])
         msg = self._ctx.last_error()
-        if code in (nat.XR_ECUDA,):
+        if code in (nat.XR_ECUDA, nat.XR_EWAIT):
             raise RuntimeError(msg)
         raise ValueError(msg)
 

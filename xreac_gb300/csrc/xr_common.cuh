@@ -122,6 +122,11 @@ struct XrWork {
   int full_derivative;
   int cg_max_iter;
   double cg_tol;
+  // Team waits of the QEq solver: polls before a wait gives up (0: the defaults, 2^22 for a cluster
+  // exchange and 2^24 for a grid barrier), and, for tests of the give-up path, the number of the
+  // team wait (1, 2, ...; 0: none) that waits for an arrival that never comes.
+  long long wait_polls;
+  int wait_fail_at;
   const XrSystem* sys;
   int* status;                // one int of XR_S_* bits
   int* counts;                // [4]: E, P, B, D totals (last entries of the scans)

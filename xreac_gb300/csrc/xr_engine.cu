@@ -12,13 +12,10 @@
 #include <vector>
 
 #include "xr_common.cuh"
+#include "xr_describe.h"
 #include "xreac_gb300.h"
 
 namespace {
-
-struct DevArena {
-  std::vector<std::pair<void**, size_t>> dummy;
-};
 
 template <class T>
 bool grow(T** p, size_t* cap, size_t need) {
@@ -34,22 +31,6 @@ bool grow(T** p, size_t* cap, size_t need) {
   }
   *cap = n;
   return true;
-}
-
-void inverse3(const double m[9], double inv[9], double* det_out) {
-  const double a = m[0], b = m[1], c = m[2], d = m[3], e = m[4], f = m[5], g = m[6], h = m[7], i = m[8];
-  const double A = e * i - f * h, B = -(d * i - f * g), C = d * h - e * g;
-  const double det = a * A + b * B + c * C;
-  *det_out = det;
-  inv[0] = A / det;
-  inv[3] = B / det;
-  inv[6] = C / det;
-  inv[1] = -(b * i - c * h) / det;
-  inv[4] = (a * i - c * g) / det;
-  inv[7] = -(a * h - b * g) / det;
-  inv[2] = (b * f - c * e) / det;
-  inv[5] = -(a * f - c * d) / det;
-  inv[8] = (a * e - b * d) / det;
 }
 
 }  // namespace
@@ -68,6 +49,8 @@ struct xr_ctx {
   std::string err;
   double cg_tol = 1e-13;
   int cg_max = 2000;
+  long long wait_polls = 0;  // QEq team waits: poll limit (0: defaults) and the wait a test makes run out
+  int wait_fail_at = 0;
   int nsm = 0;
   int coop_per_sm = 0;
   int max_clusters = 0;  // resident thread-block clusters of the cluster QEq solver (0: unavailable),
@@ -257,82 +240,15 @@ bool host_grow(T** p, size_t* cap, size_t need) {
   return true;
 }
 
-// Per-system descriptor: cell inverse, image scan reach and the FP32 error band.
+// Per-system descriptor (xr_describe.h) plus the system's total charge.
 int build_system(xr_ctx* c, const xr_system& in, int atom_off, double rc, XrSystem& S, double4_32a* xpack) {
-  std::memset(&S, 0, sizeof(S));
-  S.atom_off = atom_off;
-  S.natoms = in.natoms;
-  bool any = false;
-  for (int k = 0; k < 3; ++k) {
-    S.periodic[k] = in.pbc[k] ? 1 : 0;
-    any = any || S.periodic[k];
+  const char* msg = "";
+  const int code = xr_host::describe_system(in, atom_off, rc, S, xpack, &msg);
+  if (code != XR_OK) {
+    c->err = msg;
+    return code;
   }
-  double cell[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
-  if (any) {
-    if (!in.cell) {
-      c->err = "A cell is required when pbc is enabled";
-      return XR_EINPUT;
-    }
-    for (int k = 0; k < 9; ++k) cell[k] = in.cell[k];
-  }
-  double inv[9], det;
-  inverse3(cell, inv, &det);
-  if (!(std::fabs(det) > 0) || !std::isfinite(det)) {
-    c->err = "Periodic cells must be nonsingular and right-handed";
-    return XR_EINPUT;
-  }
-  for (int k = 0; k < 9; ++k) {
-    S.cell[k] = cell[k];
-    S.inv[k] = inv[k];
-    S.cellf[k] = (float)cell[k];
-  }
-  double heights[3], lens[3];
-  for (int k = 0; k < 3; ++k) {
-    heights[k] = 1.0 / std::sqrt(inv[k] * inv[k] + inv[3 + k] * inv[3 + k] + inv[6 + k] * inv[6 + k]);
-    lens[k] = std::sqrt(cell[3 * k] * cell[3 * k] + cell[3 * k + 1] * cell[3 * k + 1] + cell[3 * k + 2] * cell[3 * k + 2]);
-    S.reach[k] = 0;
-    if (S.periodic[k] && !(heights[k] > 2.0 * rc * (1.0 + 1e-9))) S.reach[k] = (int)std::floor(rc / heights[k] + 0.5) + 1;
-  }
-  // Wrapped positions (as the device computes them) bound the FP32 coordinate magnitudes.
-  double origin[3] = {0, 0, 0};
-  double ext = 0.0;
-  for (int a = 0; a < in.natoms; ++a) {
-    const double* p = in.positions + 3 * a;
-    for (int k = 0; k < 3; ++k)
-      if (!std::isfinite(p[k])) {
-        c->err = "positions must be a finite (N, 3) array in Angstrom";
-        return XR_EINPUT;
-      }
-    double wr[3];
-    for (int k = 0; k < 3; ++k) {
-      const double fk = p[0] * inv[k] + p[1] * inv[3 + k] + p[2] * inv[6 + k];
-      wr[k] = S.periodic[k] ? std::floor(fk) : 0.0;
-    }
-    double xw[3];
-    for (int q = 0; q < 3; ++q) xw[q] = p[q] - (wr[0] * cell[q] + wr[1] * cell[3 + q] + wr[2] * cell[6 + q]);
-    if (a == 0)
-      for (int q = 0; q < 3; ++q) origin[q] = xw[q];
-    for (int q = 0; q < 3; ++q) ext = std::max(ext, std::fabs(xw[q] - origin[q]));
-    xpack[a] = make_double4_32a(p[0], p[1], p[2], 0.0);
-  }
-  double img = 0.0;
-  for (int k = 0; k < 3; ++k)
-    if (S.periodic[k]) img += (S.reach[k] + 2) * lens[k];
-  const double C = 2.0 * ext + img + 1.0;
-  const double u = 1.0 / 16777216.0;  // 2^-24
-  const double delta = 8.0 * u * C;    // per-component bound on |FP32 v - FP64 v|
-  const double margin = 2.0 * std::sqrt(3.0) * (rc + 2.0 * delta) * delta + 3.0 * delta * delta + 8.0 * u * rc * rc;
-  S.margin = (float)(4.0 * margin + 1e-6);
-  for (int q = 0; q < 3; ++q) S.origin[q] = origin[q];
   S.total_charge = in.total_charge;
-  S.rc = rc;
-  S.inv_rc = 1.0 / rc;
-  S.rc2 = rc * rc;
-  S.bond_cut = std::min(5.0, rc);
-  S.hb_cut = std::min(7.5, rc);
-  S.rc2f = (float)S.rc2;
-  S.bc2f = (float)(S.bond_cut * S.bond_cut);
-  S.hc2f = (float)(S.hb_cut * S.hb_cut);
   return XR_OK;
 }
 
@@ -440,6 +356,8 @@ void fill_work(xr_ctx* c, XrWork& w, int A, int S, unsigned flags) {
   w.full_derivative = (flags & XR_FLAG_FULL_DERIVATIVE) ? 1 : 0;
   w.cg_max_iter = c->cg_max;
   w.cg_tol = c->cg_tol;
+  w.wait_polls = c->wait_polls;
+  w.wait_fail_at = c->wait_fail_at;
   w.sys = c->sys;
   w.status = c->status;
   w.counts = c->counts;
@@ -589,9 +507,19 @@ int status_to_code(xr_ctx* c, int st) {
     c->err = "Collinear atoms in an active torsion: the dihedral derivative is undefined; perturb the geometry";
     return XR_ECOLLINEAR;
   }
-  if (st & (XR_S_CG | XR_S_NONSPD | XR_S_BARRIER)) {
+  if (st & XR_S_BARRIER) {
+    c->err = "A device-side wait of the QEq solver gave up (a scheduling failure, not an input error); "
+             "the evaluation may be repeated";
+    return XR_EWAIT;
+  }
+  if (st & XR_S_NONSPD) {
     c->err = "Singular QEq system; check the geometry and parameters";
     return XR_ESINGULAR;
+  }
+  if (st & XR_S_CG) {
+    c->err = "QEq did not converge within the iteration limit; raise it (set_qeq) or check the geometry and "
+             "parameters";
+    return XR_ECG_NOCONV;
   }
   if (st & XR_S_NONFINITE) {
     c->err = "Non-finite energy, charges, or forces; check the geometry";
@@ -1210,6 +1138,13 @@ int xr_ctx_set_qeq(xr_ctx* c, double tolerance, int max_iterations) {
   if (!c || !(tolerance > 0) || max_iterations < 1) return XR_EINPUT;
   c->cg_tol = tolerance;
   c->cg_max = max_iterations;
+  return XR_OK;
+}
+
+int xr_ctx_set_wait_test(xr_ctx* c, long long polls, int fail_at) {
+  if (!c || polls < 0 || fail_at < 0) return XR_EINPUT;
+  c->wait_polls = polls;
+  c->wait_fail_at = fail_at;
   return XR_OK;
 }
 

@@ -152,20 +152,28 @@ __device__ inline unsigned ld_acquire(const unsigned* p) {
   return v;
 }
 
+// Polls before a team wait gives up, and whether wait number `episode` of a team is the one a test
+// made unsatisfiable (XrWork::wait_fail_at).
+__device__ inline long long wait_cap(const XrWork& w, long long dflt) { return w.wait_polls > 0 ? w.wait_polls : dflt; }
+__device__ inline bool wait_poisoned(const XrWork& w, unsigned episode) {
+  return w.wait_fail_at > 0 && episode == (unsigned)w.wait_fail_at;
+}
+
 // Bounded grid barrier for a cooperative launch (all blocks co-resident): every block adds one to a
 // monotonically increasing counter with release semantics and waits, with acquire loads, until it
 // reaches the episode's target (number of blocks times episodes so far). Returns false when the
 // wait ran out; every block then leaves the solver and the host reports the status bit.
-__device__ bool grid_barrier(unsigned* bar, unsigned target, int* status) {
+__device__ bool grid_barrier(unsigned* bar, unsigned target, const XrWork& w, bool poisoned) {
   __syncthreads();
   __shared__ int ok;
   if (threadIdx.x == 0) {
     ok = 1;
     asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(bar) : "memory");
+    const long long cap = wait_cap(w, 1ll << 24);
     long long it = 0;
-    while (ld_acquire(bar) < target) {
-      if (++it > (1ll << 24) || ((it & 255) == 0 && (*(volatile int*)status & XR_S_BARRIER))) {
-        atomicOr(status, XR_S_BARRIER);
+    while (poisoned || ld_acquire(bar) < target) {
+      if (++it > cap || ((it & 255) == 0 && (*(volatile int*)w.status & XR_S_BARRIER))) {
+        atomicOr(w.status, XR_S_BARRIER);
         ok = 0;
         break;
       }
@@ -190,7 +198,7 @@ struct GridTeam {
   mutable unsigned target = 0;  // barrier episodes so far times nb
   __device__ bool sync(const XrWork& w) const {
     target += nb;
-    return grid_barrier(bar, target, w.status);
+    return grid_barrier(bar, target, w, wait_poisoned(w, target / nb));
   }
   // Team-wide sum of NV block totals held by lane 0 of warp 0, fused with the barrier: lane 0
   // publishes the block's values into a fixed slot and arrives (release); after the bounded wait
@@ -212,9 +220,11 @@ struct GridTeam {
       if (lane == 0) {
         for (int k = 0; k < NV; ++k) rs[rank * 8 + k] = v[k];
         asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(bar) : "memory");
+        const long long cap = wait_cap(w, 1ll << 24);
+        const bool poisoned = wait_poisoned(w, target / nb);
         long long it = 0;
-        while (ld_acquire(bar) < target) {
-          if (++it > (1ll << 24) || ((it & 255) == 0 && (*(volatile int*)w.status & XR_S_BARRIER))) {
+        while (poisoned || ld_acquire(bar) < target) {
+          if (++it > cap || ((it & 255) == 0 && (*(volatile int*)w.status & XR_S_BARRIER))) {
             atomicOr(w.status, XR_S_BARRIER);
             good = 0;
             break;
@@ -332,16 +342,18 @@ struct ClusterTeam {
     }
     bool mine = lane >= nb;
     const unsigned mine_addr = smem_u32(seqs + par * 8 + (lane & 7));
+    const long long cap = wait_cap(w, 1ll << 22);
+    const bool poisoned = wait_poisoned(w, m);
     long long it = 0;
     int good = 1;
     for (;;) {
       if (!mine) {
         unsigned sq;
         asm volatile("ld.acquire.cluster.shared::cta.u32 %0, [%1];" : "=r"(sq) : "r"(mine_addr) : "memory");
-        mine = sq == m;
+        mine = sq == m && !poisoned;
       }
       if (__all_sync(0xffffffffu, mine)) break;
-      bool stop = ++it > (1ll << 22);
+      bool stop = ++it > cap;
       if (lane == 0 && (it & 1023) == 0) stop = stop || (*(volatile int*)w.status & XR_S_BARRIER);
       if (__any_sync(0xffffffffu, stop)) {
         if (lane == 0) atomicOr(w.status, XR_S_BARRIER);
@@ -1487,6 +1499,9 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
       return;
     for (int sweep = 0; sweep < 8; ++sweep) {
       if (!(gz > target) || !(gz > gfloor) || n < 2) break;
+      // the iteration limit bounds the FP32 and FP64 iterations together
+      const int budget = min(400, w.cg_max_iter - iters);
+      if (budget <= 0) break;
       if (!small_rows) {  // the shared-memory solver reads the FP64 gradient itself (published by the
                           // reduction that ended the residual)
         for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
@@ -1500,9 +1515,9 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
       }
       // the correction's own projected norm starts at gz; 1e-10 of it (1e-5 in norm) per sweep,
       // and no further than a hundredth of the final target (sd_ratio: that stop over gz)
-      const int it = small_rows ? qeq_cg_rows32(w, team, sh, a0, n, r0, r1, M32, v32.y, sh.sd_ratio, 400, v32.g, &slot)
+      const int it = small_rows ? qeq_cg_rows32(w, team, sh, a0, n, r0, r1, M32, v32.y, sh.sd_ratio, budget, v32.g, &slot)
                                 : qeq_cg<Team, float>(w, ff, team, sh, a0, n, r0, r1, v32, M32, s1, gz,
-                                                      fmax(1e-10 * gz, 0.01 * target), 0.0, 400, false, slot);
+                                                      fmax(1e-10 * gz, 0.01 * target), 0.0, budget, false, slot);
       if (it < 0) return;
       iters += it;
       // x += y, then restore sum x = Q exactly: the FP32 step keeps sum y = 0 only to FP32 rounding,
@@ -1552,8 +1567,9 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
       QW(Q_HP, a0 + r) = 0.0;
     }
     __syncthreads();
+    // what the FP32 sweeps left of the iteration limit (none: the limit is flagged unless converged)
     const int it = qeq_cg<Team, double>(w, ff, team, sh, a0, n, r0, r1, v64, M64, s1, gz, target, gfloor,
-                                        w.cg_max_iter, true, slot);
+                                        max(0, w.cg_max_iter - iters), true, slot);
     if (it < 0) return;
     iters += it;
   }

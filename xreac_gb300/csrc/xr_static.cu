@@ -17,12 +17,16 @@
 // the process on that device, so calls that overlap in time (two host threads, or two streams
 // without ordering between them) race on it. The first call on a device does the set-up
 // (cudaGetSymbolAddress with that device current, which also loads this module's device code);
-// make that first call before any stream capture begins.
+// make that first call before any stream capture begins. The looked-up address is kept for the
+// life of the process: after cudaDeviceReset (or anything else that destroys the device's primary
+// context) the array may move, so this entry point must not be used on that device again. A
+// caller-supplied stream must belong to the current device.
 #include <cmath>
 #include <cstring>
 #include <mutex>
 
 #include "xr_common.cuh"
+#include "xr_describe.h"
 #include "xreac_gb300.h"
 
 namespace {
@@ -72,87 +76,6 @@ int scratch_for_current_device(unsigned char** out) {
   return XR_OK;
 }
 
-void inverse3(const double m[9], double inv[9], double* det_out) {
-  const double a = m[0], b = m[1], c = m[2], d = m[3], e = m[4], f = m[5], g = m[6], h = m[7], i = m[8];
-  const double A = e * i - f * h, B = -(d * i - f * g), C = d * h - e * g;
-  const double det = a * A + b * B + c * C;
-  *det_out = det;
-  inv[0] = A / det;
-  inv[3] = B / det;
-  inv[6] = C / det;
-  inv[1] = -(b * i - c * h) / det;
-  inv[4] = (a * i - c * g) / det;
-  inv[7] = -(a * h - b * g) / det;
-  inv[2] = (b * f - c * e) / det;
-  inv[5] = -(a * f - c * d) / det;
-  inv[8] = (a * e - b * d) / det;
-}
-
-// System descriptor with the same fields, image reach and FP32 error band as xr_eval's.
-int describe(const xr_system& in, double rc, XrSystem& S) {
-  std::memset(&S, 0, sizeof(S));
-  S.natoms = in.natoms;
-  bool any = false;
-  for (int k = 0; k < 3; ++k) {
-    S.periodic[k] = in.pbc[k] ? 1 : 0;
-    any = any || S.periodic[k];
-  }
-  double cell[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
-  if (any) {
-    if (!in.cell) return fail(XR_EINPUT, "A cell is required when pbc is enabled");
-    for (int k = 0; k < 9; ++k) cell[k] = in.cell[k];
-  }
-  double inv[9], det;
-  inverse3(cell, inv, &det);
-  if (!(std::fabs(det) > 0) || !std::isfinite(det))
-    return fail(XR_EINPUT, "Periodic cells must be nonsingular and right-handed");
-  double heights[3], lens[3];
-  for (int k = 0; k < 3; ++k) {
-    S.cell[k] = cell[k];
-    S.cell[3 + k] = cell[3 + k];
-    S.cell[6 + k] = cell[6 + k];
-    heights[k] = 1.0 / std::sqrt(inv[k] * inv[k] + inv[3 + k] * inv[3 + k] + inv[6 + k] * inv[6 + k]);
-    lens[k] = std::sqrt(cell[3 * k] * cell[3 * k] + cell[3 * k + 1] * cell[3 * k + 1] + cell[3 * k + 2] * cell[3 * k + 2]);
-    if (S.periodic[k] && !(heights[k] > 2.0 * rc * (1.0 + 1e-9))) S.reach[k] = (int)std::floor(rc / heights[k] + 0.5) + 1;
-  }
-  for (int k = 0; k < 9; ++k) {
-    S.inv[k] = inv[k];
-    S.cellf[k] = (float)cell[k];
-  }
-  double origin[3] = {0, 0, 0}, ext = 0.0;
-  for (int a = 0; a < in.natoms; ++a) {
-    const double* p = in.positions + 3 * a;
-    if (!std::isfinite(p[0]) || !std::isfinite(p[1]) || !std::isfinite(p[2]))
-      return fail(XR_EINPUT, "positions must be a finite (N, 3) array in Angstrom");
-    double wr[3], xw[3];
-    for (int k = 0; k < 3; ++k) {
-      const double fk = p[0] * inv[k] + p[1] * inv[3 + k] + p[2] * inv[6 + k];
-      wr[k] = S.periodic[k] ? std::floor(fk) : 0.0;
-    }
-    for (int q = 0; q < 3; ++q) xw[q] = p[q] - (wr[0] * cell[q] + wr[1] * cell[3 + q] + wr[2] * cell[6 + q]);
-    if (a == 0)
-      for (int q = 0; q < 3; ++q) origin[q] = xw[q];
-    for (int q = 0; q < 3; ++q) ext = std::fmax(ext, std::fabs(xw[q] - origin[q]));
-  }
-  double img = 0.0;
-  for (int k = 0; k < 3; ++k)
-    if (S.periodic[k]) img += (S.reach[k] + 2) * lens[k];
-  const double C = 2.0 * ext + img + 1.0;
-  const double u = 1.0 / 16777216.0;  // 2^-24
-  const double delta = 8.0 * u * C;    // per-component bound on |FP32 v - FP64 v|
-  const double margin = 2.0 * std::sqrt(3.0) * (rc + 2.0 * delta) * delta + 3.0 * delta * delta + 8.0 * u * rc * rc;
-  S.margin = (float)(4.0 * margin + 1e-6);
-  for (int q = 0; q < 3; ++q) S.origin[q] = origin[q];
-  S.rc = rc;
-  S.rc2 = rc * rc;
-  S.bond_cut = std::fmin(5.0, rc);
-  S.hb_cut = std::fmin(7.5, rc);
-  S.rc2f = (float)S.rc2;
-  S.bc2f = (float)(S.bond_cut * S.bond_cut);
-  S.hc2f = (float)(S.hb_cut * S.hb_cut);
-  return XR_OK;
-}
-
 // Writes the descriptor, packs the uploaded positions, and clears the status word (the only
 // scratch the count pass accumulates into; the per-atom counts are stored, not added).
 __global__ void k_static_setup(XrSystem S, XrSystem* sys, const double* xyz, double4_32a* x, int* sys_of,
@@ -184,13 +107,22 @@ extern "C" int xr_count_neighbors_static(const xr_system* sys, double cutoff, vo
   const int n = sys->natoms;
   if (n == 0) return XR_OK;
   XrSystem S;
-  int code = describe(*sys, cutoff, S);
-  if (code != XR_OK) return code;
+  const char* msg = "";
+  int code = xr_host::describe_system(*sys, 0, cutoff, S, nullptr, &msg);
+  if (code != XR_OK) return fail(code, msg);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (st) {
+    // the scratch address belongs to the current device; work on another device's stream would
+    // touch memory that is not this device's array
+    int cur = -1, sdev = -1;
+    if (cudaGetDevice(&cur) != cudaSuccess || cudaStreamGetDevice(st, &sdev) != cudaSuccess)
+      return fail(XR_EINPUT, "the stream's device could not be determined");
+    if (sdev != cur) return fail(XR_EINPUT, "stream belongs to another device than the current one");
+  }
   unsigned char* base = nullptr;
   code = scratch_for_current_device(&base);
   if (code != XR_OK) return code;
 
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
   XrWork w;
   std::memset(&w, 0, sizeof(w));
   w.A = n;
