@@ -23,10 +23,15 @@ One step = one pass of the whole stream through the continuous-batching server
   dominant kernel (k_qeq_grid).
 - ``differentiation``: 256 perturbed copies of the TiO2/water slab: reference E+F, then the E+F
   squared-error loss and its force-field parameter gradient (device adjoint) per copy.
-- ``cpu_baseline``: the CPU oracle (the reference's algorithm restated) on a sample of the stream.
+- ``cpu_baseline``: the unmodified reference (xreac v0.10.0 installed in ``baseline/_ref``, run through
+  the torch-backed autograd stand-in of ``tests/golden/shim``) on a sample of the stream; the CPU
+  oracle (the reference's algorithm restated) only where that install is absent.
 
-``--impl reference`` times the CPU oracle on samples of the same stream with every host thread and
-prints the same JSON line with ``"impl": "reference"``.
+``--impl reference`` times the same reference, one ``xreac.Calculator.evaluate`` per request of the
+same seeded stream (consecutive requests, each step a bounded sample), with every host thread, and
+prints the same JSON line with ``"impl": "reference"`` and the same ``config``. That arm imports
+nothing of the product package: the stream comes from ``xreac_gb300/workloads.py`` loaded from its
+file (pure numpy), and force fields are parsed by the reference itself.
 """
 
 from __future__ import annotations
@@ -235,12 +240,55 @@ def dist_setup():
     return world, rank, local
 
 
+REFERENCE_DIR = ROOT / "baseline" / "_ref"
+SHIM_DIR = ROOT / "tests" / "golden" / "shim"
+
+
+def workloads_module():
+    """The seeded input generator, ``xreac_gb300/workloads.py`` (numpy only), loaded from its file under
+    its own name: the reference arm gets the same requests without importing the product package."""
+    import importlib.util
+
+    name = "xr_bench_workloads"
+    if name not in sys.modules:
+        spec = importlib.util.spec_from_file_location(name, ROOT / "xreac_gb300" / "workloads.py")
+        mod = importlib.util.module_from_spec(spec)
+        sys.modules[name] = mod
+        spec.loader.exec_module(mod)
+    return sys.modules[name]
+
+
+def reference_package():
+    """``(xreac module, None)`` for the unmodified reference installed in baseline/_ref, or ``(None,
+    reason)``. Every installed file must still match the SHA-256 recorded at install time, which in
+    turn matched the reference checkout (baseline/install_reference.py). HIPS autograd is absent, so
+    its torch-backed stand-in goes first on sys.path."""
+    import hashlib
+
+    record = REFERENCE_DIR / "XREAC_INSTALL.json"
+    if not record.is_file():
+        return None, "baseline/_ref is not installed (python baseline/install_reference.py <checkout>)"
+    rec = json.loads(record.read_text())
+    for rel, v in rec["files"].items():
+        path = REFERENCE_DIR / "xreac" / rel
+        if not path.is_file() or hashlib.sha256(path.read_bytes()).hexdigest() != v["sha256"] \
+                or v["sha256"] != v["source_sha256"]:
+            return None, f"baseline/_ref/xreac/{rel} differs from the reference checkout"
+    for p in (str(REFERENCE_DIR), str(SHIM_DIR)):
+        if p not in sys.path:
+            sys.path.insert(0, p)
+    import xreac
+
+    if Path(xreac.__file__).resolve().parent != (REFERENCE_DIR / "xreac").resolve():
+        return None, f"another xreac shadows baseline/_ref ({xreac.__file__})"
+    return xreac, None
+
+
 def stream_requests():
     """The serving stream as server requests (sessions mark repeat evaluations)."""
-    from xreac_gb300 import workloads
     from xreac_gb300.serving import Request
 
-    stream = workloads.request_stream()
+    stream = workloads_module().request_stream()
     reqs = [Request(r.system.symbols, r.system.positions, r.system.force_field, r.system.cell, r.system.pbc,
                     r.system.total_charge, session=r.index if r.repeat_of is None else r.repeat_of) for r in stream]
     arrivals = np.array([r.arrival for r in stream])
@@ -294,22 +342,57 @@ def stream_pass(reqs, tag, part=None):
             for r in (reqs if part is None else reqs[:part])]
 
 
-def oracle_sample(reqs, start, budget_s, min_requests=1):
-    """CPU-oracle evaluations of consecutive requests from ``start`` until ``budget_s`` is spent.
-    Returns (atoms evaluated, seconds, requests evaluated)."""
-    import oracle
-    from xreac_gb300.forcefield import ForceField
+class CpuArm:
+    """The CPU implementation timed as the reference: the unmodified xreac from baseline/_ref
+    (``kind`` "reference"), or, where it is absent, the CPU oracle ("port")."""
 
-    ffs = {}
-    atoms, k, t0 = 0, start, time.perf_counter()
-    while k < start + len(reqs) and (k - start < min_requests or time.perf_counter() - t0 < budget_s):
-        r = reqs[k % len(reqs)]
-        ff = ffs.setdefault(r.force_field, ForceField.bundled(r.force_field))
-        oracle.evaluate(ff, r.symbols, r.positions, total_charge=r.total_charge, cell=r.cell, pbc=r.pbc,
-                        dense_bond_orders=False)
-        atoms += r.natoms
-        k += 1
-    return atoms, time.perf_counter() - t0, k - start
+    def __init__(self):
+        self.xreac, why = reference_package()
+        self.kind = "reference" if self.xreac is not None else "port"
+        self.why = why
+        self.calcs = {}
+        if self.xreac is None:
+            import oracle
+
+            self.oracle = oracle
+
+    def describe(self):
+        if self.kind == "reference":
+            return ("unmodified xreac v0.10.0 (baseline/_ref), Calculator.evaluate per request; HIPS autograd "
+                    "replaced by the torch-backed stand-in tests/golden/shim")
+        return f"CPU oracle (the reference's algorithm restated; {self.why})"
+
+    def evaluate(self, system):
+        s = system
+        if self.kind == "reference":
+            calc = self.calcs.get(s.force_field)
+            if calc is None:
+                calc = self.calcs[s.force_field] = self.xreac.Calculator(self.xreac.ForceField.bundled(s.force_field))
+            return calc.evaluate(s.symbols, s.positions, total_charge=s.total_charge, cell=s.cell, pbc=s.pbc)
+        from xreac_gb300.forcefield import ForceField
+
+        ff = self.calcs.get(s.force_field)
+        if ff is None:
+            ff = self.calcs[s.force_field] = ForceField.bundled(s.force_field)
+        return self.oracle.evaluate(ff, s.symbols, s.positions, total_charge=s.total_charge, cell=s.cell, pbc=s.pbc,
+                                    dense_bond_orders=False)
+
+    def sample(self, stream, start, budget_s, min_requests=1):
+        """Consecutive requests of the stream from ``start`` (wrapping) until ``budget_s`` is spent.
+        Returns (atoms evaluated, seconds, requests evaluated)."""
+        atoms, k, t0 = 0, start, time.perf_counter()
+        while k - start < min_requests or time.perf_counter() - t0 < budget_s:
+            r = stream[k % len(stream)]
+            self.evaluate(r.system)
+            atoms += r.system.n
+            k += 1
+        return atoms, time.perf_counter() - t0, k - start
+
+
+def bench_config(atoms):
+    """``config`` of both arms' lines: the workload, whatever implementation runs it."""
+    return {"workload": WORKLOAD, "requests": 4096, "atoms_per_pass": atoms,
+            "l2": "not flushed: every pass streams 4,096 distinct systems (inputs about 13 MB)"}
 
 
 def run_reference(args, world, rank):
@@ -319,17 +402,21 @@ def run_reference(args, world, rank):
 
     cores = os.cpu_count() or 1
     torch.set_num_threads(cores)
-    reqs, _ = stream_requests()
+    stream = workloads_module().request_stream()
+    atoms_per_pass = sum(r.system.n for r in stream)
+    arm = CpuArm()
     step_budget = float(os.environ.get("XR_REFERENCE_STEP_S", "5"))
     pos = 0
     for _ in range(max(args.warmup, 1)):
-        _, _, n = oracle_sample(reqs, pos, 0.0)
+        _, _, n = arm.sample(stream, pos, 0.0)
         pos += n
-    atoms, secs, nreq = 0, 0.0, 0
+    atoms, secs, nreq, first = 0, 0.0, 0, pos
     for _ in range(args.steps):
-        a, t, n = oracle_sample(reqs, pos, step_budget)
+        a, t, n = arm.sample(stream, pos, step_budget)
         atoms, secs, nreq, pos = atoms + a, secs + t, nreq + n, pos + n
     value = atoms / secs
+    sample = (f"requests {first}..{pos - 1} of the stream ({nreq} requests, {atoms} atoms) in arrival order, one "
+              f"evaluation each; {args.steps} steps of about {step_budget:.0f} s, {cores} threads")
     line = {
         "impl": "reference",
         "metric": METRIC,
@@ -343,16 +430,10 @@ def run_reference(args, world, rank):
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f64",
-        "data": "synthetic (seeded request stream)",
-        "config": {"workload": WORKLOAD, "requests": len(reqs), "parallelism": "cpu"},
-        "cpu_baseline": {
-            "value": value,
-            "unit": UNIT,
-            "cores": cores,
-            "kind": "port",
-            "sample": f"{nreq} consecutive requests of the stream ({atoms} atoms) evaluated one by one by the CPU "
-                      f"oracle (torch/numpy FP64, {cores} threads); each step about {step_budget:.0f} s of requests",
-        },
+        "data": "synthetic (seeded request stream; molecules placed at random)",
+        "config": bench_config(atoms_per_pass),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": arm.kind,
+                         "sample": sample, "implementation": arm.describe()},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -636,9 +717,9 @@ def main():
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic (seeded request stream; molecules placed at random)",
-        "config": {"workload": WORKLOAD, "requests": len(reqs), "atoms_per_pass": atoms, "server_workers": SERVER_WORKERS,
-                   "max_batch_atoms": SERVER_BATCH_ATOMS, "parallelism": "replicas" if world > 1 else "single",
-                   "l2": "not flushed: every pass streams 4,096 distinct systems (inputs about 13 MB)"},
+        "config": bench_config(atoms),
+        "server": {"workers": SERVER_WORKERS, "max_batch_atoms": SERVER_BATCH_ATOMS,
+                   "parallelism": "replicas" if world > 1 else "single"},
         "plain": {"value": plain_value, "unit": UNIT, "ms_per_request": 1e3 * plain_s / len(reqs),
                   "api": "one xreac_gb300.Calculator.evaluate per request"},
         "served_over_plain": e2e_value / plain_value,
@@ -672,14 +753,17 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cores = os.cpu_count() or 1
         torch.set_num_threads(cores)
-        a, secs, n = oracle_sample(reqs, 0, 10.0)
+        arm = CpuArm()
+        stream = workloads_module().request_stream()
+        arm.sample(stream, 0, 0.0)  # imports and first-call costs
+        a, secs, n = arm.sample(stream, 1, 10.0)
         line["cpu_baseline"] = {
             "value": a / secs,
             "unit": UNIT,
             "cores": cores,
-            "kind": "port",
-            "sample": f"the first {n} requests of the stream ({a} atoms) evaluated one by one by the CPU oracle "
-                      f"(torch/numpy FP64, {cores} threads)",
+            "kind": arm.kind,
+            "sample": f"requests 1..{n} of the stream ({a} atoms) evaluated one by one, {cores} threads",
+            "implementation": arm.describe(),
         }
     if dist is not None:
         dist.destroy_process_group()
