@@ -326,7 +326,7 @@ def serialised_device(reqs, ffs, local, steps, warmup):
             calcs[n]._evaluate_items(items)
             qbytes += calcs[n].qeq_work()[1]
             launches += calcs[n].last_launches
-    total = np.zeros(7)
+    total = np.zeros(len(STAGE_NAMES))
     for c in calcs.values():
         total += c.stage_times()[0]
         c.set_profiling(False)
@@ -506,7 +506,9 @@ def water_box_numbers(lib, nat, local, steps, warmup):
     total_ms = sum(s_.elapsed_time(e_) for s_, e_ in zip(starts, ends))
     stage_ms = (ctypes.c_double * 8)()
     calls = ctypes.c_longlong()
-    lib.xr_ctx_stage_times(ctx.handle, stage_ms, 7, ctypes.byref(calls))
+    lib.xr_ctx_stage_times(ctx.handle, stage_ms, len(STAGE_NAMES), ctypes.byref(calls))
+    sizes = (ctypes.c_longlong * 6)()
+    lib.xr_last_list_sizes(ctx.handle, sizes, 6)
     stages = {nm: stage_ms[k] / max(calls.value, 1) for k, nm in enumerate(STAGE_NAMES)}
     its = ctypes.c_longlong()
     qbytes = ctypes.c_double()
@@ -517,6 +519,9 @@ def water_box_numbers(lib, nat, local, steps, warmup):
     hbm_peak = float(pk.get("hbm_gbs", 6800.0))
     achieved = qbytes.value / (stages["qeq_cg"] / 1e3) / 1e9
     pair_bytes = 8.0 * (nb_count.value // 2) + 76.0 * n
+    # bond orders: 8 B per candidate half-edge (r <= 5 A), 28 B per atom, 32 B per active bond
+    bo_bytes = 8.0 * sizes[2] + 28.0 * n + 32.0 * sizes[4]
+    bo_ms = stages["bond_orders"]
     return {
         "workload": BOX_WORKLOAD,
         "value": steps * n / (total_ms / 1e3),
@@ -539,6 +544,13 @@ def water_box_numbers(lib, nat, local, steps, warmup):
                         "hbm_frac": pair_bytes / (stages["pairs_vdw_shield"] / 1e3) / 1e9 / hbm_peak,
                         "fp64_pipe_busy_pct": profiled_fp64("k_pairs"),
                         "traffic": profiled_traffic("k_pairs")},
+        "bond_order_kernel": {"kernel": "k_bo1 + k_deltap + k_bo2 (stage: bond_orders)", "bound": "fp64 pipe",
+                              "bond_candidates": int(sizes[2]), "active_bonds": int(sizes[4]),
+                              "algorithmic_bytes": bo_bytes, "ms": bo_ms,
+                              "achieved_gbs": bo_bytes / (bo_ms / 1e3) / 1e9,
+                              "hbm_frac": bo_bytes / (bo_ms / 1e3) / 1e9 / hbm_peak,
+                              "fp64_pipe_busy_pct": {"k_bo1": profiled_fp64("k_bo1"), "k_bo2": profiled_fp64("k_bo2")},
+                              "traffic": {"k_bo1": profiled_traffic("k_bo1"), "k_bo2": profiled_traffic("k_bo2")}},
     }
 
 
@@ -583,7 +595,7 @@ SERVER_WORKERS = 6
 SERVER_BATCH_ATOMS = 8192
 
 STAGE_NAMES = ["neighbour_count_scan", "neighbour_fill_reverse", "pairs_vdw_shield", "qeq_cg", "coulomb",
-               "bonded_and_adjoint", "forces_reduce_pack"]
+               "bond_orders", "bonded_terms_and_adjoint", "forces_reduce_pack"]
 
 
 def main():

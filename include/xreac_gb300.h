@@ -143,6 +143,12 @@ int xr_get_param_gradient(const xr_ctx* ctx, double* pair_grad, long long npair,
 /* Number of CUDA kernels the last xr_eval / xr_eval_batch call launched. */
 long long xr_last_launches(const xr_ctx* ctx);
 
+/* List sizes of the last call, summed over its systems (no reference counterpart; instrumentation):
+ * sizes[0] directed edges within the cutoff, [1] unordered pairs, [2] bond candidates (pairs with
+ * r <= 5 A), [3] directed bond-row entries, [4] active bonds (uncorrected order at or above the cut),
+ * [5] torsion middle bonds (bo > 0.001). The first n (at most 6) are written. */
+int xr_last_list_sizes(const xr_ctx* ctx, long long* sizes, int n);
+
 /* QEq conjugate-gradient iterations of the last call (largest over its systems; no reference
  * counterpart: the reference solves the KKT system directly). */
 int xr_last_qeq_iterations(const xr_ctx* ctx);
@@ -158,9 +164,9 @@ int xr_last_transfer_bytes(const xr_ctx* ctx, long long* h2d, long long* d2h);
 /* Per-stage device timing with CUDA events on the context stream (no reference counterpart;
  * instrumentation). enable=1 resets the accumulators. Stages: 0 neighbour count + scan (including
  * the host read of the list sizes), 1 row fill + reverse map, 2 pair kernel (vdW, shield) and QEq
- * matrix rows, 3 QEq solve, 4 Coulomb, 5 bond orders + bonded terms + adjoint chain, 6 force
- * assembly + reductions + result packing. ms receives the summed
- * milliseconds of the first n stages over *calls evaluations. */
+ * matrix rows, 3 QEq solve, 4 Coulomb, 5 bond orders (uncorrected, Delta', corrected), 6 bonded
+ * terms + adjoint chain, 7 force assembly + reductions + result packing. ms receives the summed
+ * milliseconds of the first n (at most 8) stages over *calls evaluations. */
 int xr_ctx_set_profiling(xr_ctx* ctx, int enable);
 int xr_ctx_stage_times(const xr_ctx* ctx, double* ms, int n, long long* calls);
 

@@ -46,6 +46,7 @@ EXPORTED = (
     "xr_get_neighbors",
     "xr_get_bonds",
     "xr_last_launches",
+    "xr_last_list_sizes",
     "xr_ctx_set_profiling",
     "xr_ctx_stage_times",
     "xr_last_transfer_bytes",
@@ -129,6 +130,8 @@ def load():
     lib.xr_get_bonds.restype = c_int
     lib.xr_last_launches.argtypes = [c_void_p]
     lib.xr_last_launches.restype = c_longlong
+    lib.xr_last_list_sizes.argtypes = [c_void_p, POINTER(c_longlong), c_int]
+    lib.xr_last_list_sizes.restype = c_int
     lib.xr_ctx_set_profiling.argtypes = [c_void_p, c_int]
     lib.xr_ctx_set_profiling.restype = c_int
     lib.xr_ctx_stage_times.argtypes = [c_void_p, POINTER(c_double), c_int, POINTER(c_longlong)]

@@ -665,8 +665,15 @@ class Calculator:
         self._lib.xr_ctx_set_profiling(self._ctx.handle, 1 if enable else 0)
 
     def stage_times(self):
-        """(summed milliseconds of the 7 stages, number of calls) since profiling was enabled."""
+        """(summed milliseconds of the 8 stages, number of calls) since profiling was enabled."""
         ms = (nat.c_double * 8)()
         calls = nat.c_longlong()
-        self._lib.xr_ctx_stage_times(self._ctx.handle, ms, 7, nat.byref(calls))
-        return np.array(ms[:7]), int(calls.value)
+        self._lib.xr_ctx_stage_times(self._ctx.handle, ms, 8, nat.byref(calls))
+        return np.array(ms[:8]), int(calls.value)
+
+    def list_sizes(self):
+        """Sizes of the last call's lists: directed edges, pairs, bond candidates, bond-row entries,
+        active bonds, torsion middles (summed over its systems)."""
+        out = (nat.c_longlong * 6)()
+        self._lib.xr_last_list_sizes(self._ctx.handle, out, 6)
+        return tuple(int(v) for v in out)

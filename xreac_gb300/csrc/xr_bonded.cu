@@ -1214,17 +1214,24 @@ __global__ void k_chain_radial(XrWork w, XrFF ff) {
 
 }  // namespace
 
+// Per-bond kernels after k_bo1 run over the active-bond list (bonds whose uncorrected order passed
+// the cut), grid-striding over its device-side length.
+static int active_grid(const XrWork& w, int tb) { return std::max(1, std::min((w.nB + tb - 1) / tb, 152 * 8)); }
+
+void xr_launch_bond_orders(const XrWork& w, const XrFF& ff, cudaStream_t st) {
+  const int tb = 128;
+  const int gB = (w.nB + tb - 1) / tb;
+  cudaMemsetAsync(w.nmids, 0, 2 * sizeof(int), st);  // torsion middles, active bonds
+  if (w.nB > 0) k_bo1<<<gB, tb, 0, st>>>(w, ff);
+  k_deltap<<<(w.A + 3) / 4, 128, 0, st>>>(w);
+  if (w.nB > 0) k_bo2<<<active_grid(w, tb), tb, 0, st>>>(w, ff);
+}
+
 void xr_launch_bonded(const XrWork& w, const XrFF& ff, cudaStream_t st) {
   const int tb = 128;
   const int gA = (w.A + tb - 1) / tb;
   const int gB = (w.nB + tb - 1) / tb;
-  // per-bond kernels after k_bo1 run over the active-bond list (bonds whose uncorrected order
-  // passed the cut), grid-striding over its device-side length
-  const int gM = std::max(1, std::min(gB, 152 * 8));
-  cudaMemsetAsync(w.nmids, 0, 2 * sizeof(int), st);  // torsion middles, active bonds
-  if (w.nB > 0) k_bo1<<<gB, tb, 0, st>>>(w, ff);
-  k_deltap<<<(w.A + 3) / 4, 128, 0, st>>>(w);
-  if (w.nB > 0) k_bo2<<<gM, tb, 0, st>>>(w, ff);
+  const int gM = active_grid(w, tb);
   k_atom1<<<gA, tb, 0, st>>>(w, ff);
   k_atom2<<<gA, tb, 0, st>>>(w, ff);
   if (w.nB > 0) k_bond_energy<<<gM, tb, 0, st>>>(w, ff);

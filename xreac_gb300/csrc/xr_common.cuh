@@ -242,6 +242,7 @@ int xr_qeq_max_clusters(int csize);
 int xr_launch_qeq_cluster(const XrWork& w, const XrFF& ff, cudaStream_t st, int csize, int nblocks, const int* list,
                           int nbig, int nsmall, bool adjoint = false);
 void xr_launch_coulomb(const XrWork& w, const XrFF& ff, cudaStream_t st);
-void xr_launch_bonded(const XrWork& w, const XrFF& ff, cudaStream_t st);
+void xr_launch_bond_orders(const XrWork& w, const XrFF& ff, cudaStream_t st);  // k_bo1, k_deltap, k_bo2
+void xr_launch_bonded(const XrWork& w, const XrFF& ff, cudaStream_t st);       // energy terms and adjoint chain
 void xr_launch_forces(const XrWork& w, const XrFF& ff, cudaStream_t st);
 void xr_launch_reduce(const XrWork& w, const XrFF& ff, cudaStream_t st);

@@ -58,6 +58,7 @@ struct xr_ctx {
   long long launches = 0;
   long long h2d_bytes = 0, d2h_bytes = 0;  // host<->device bytes moved by the last evaluation
   int qeq_iterations = 0;                   // CG iterations of the last evaluation (largest system)
+  long long list_sizes[6] = {};             // edges, pairs, bond candidates, bond rows, active bonds, middles
   int* qiters = nullptr;                    // [S] per-system iterations (device)
   size_t cqiters = 0;
   std::vector<int> h_qiters;
@@ -166,7 +167,7 @@ struct xr_ctx {
   size_t cred = 0;
   // per-stage timing (CUDA events on the context stream), enabled by xr_ctx_set_profiling
   bool profile = false;
-  static constexpr int kStages = 8;
+  static constexpr int kStages = 9;
   cudaEvent_t ev[kStages + 1] = {};
   double stage_ms[kStages] = {};
   long long stage_calls = 0;
@@ -816,9 +817,12 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
     launches += 4;
   }
   stage(c, 5, st);
-  xr_launch_bonded(w, ff->d, st);
-  launches += 14;
+  xr_launch_bond_orders(w, ff->d, st);
+  launches += 3;
   stage(c, 6, st);
+  xr_launch_bonded(w, ff->d, st);
+  launches += 11;
+  stage(c, 7, st);
   xr_launch_forces(w, ff->d, st);
   launches += 1;
   xr_launch_reduce(w, ff->d, st);
@@ -869,10 +873,11 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
     d2h += sizeof(double) * (8 * (long long)A + 20 * (long long)nsys);
   }
   cudaMemcpyAsync(c->h_small + 4, c->status, sizeof(int), cudaMemcpyDeviceToHost, st);
-  stage(c, 7, st);
+  cudaMemcpyAsync(c->h_small + 7, c->nmids, 2 * sizeof(int), cudaMemcpyDeviceToHost, st);
+  stage(c, 8, st);
   if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(c, e, "evaluation");
   if (c->profile) {
-    for (int k = 0; k < 7; ++k) {
+    for (int k = 0; k < 8; ++k) {
       float ms = 0.f;
       if (cudaEventElapsedTime(&ms, c->ev[k], c->ev[k + 1]) == cudaSuccess) c->stage_ms[k] += ms;
     }
@@ -896,6 +901,12 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
   if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(c, e, "kernel launch");
   c->launches = launches;
   c->qeq_iterations = c->h_small[6];
+  c->list_sizes[0] = nE;
+  c->list_sizes[1] = nP;
+  c->list_sizes[2] = nB;
+  c->list_sizes[3] = nD;
+  c->list_sizes[4] = c->h_small[8];  // active bonds (uncorrected order passed the cut)
+  c->list_sizes[5] = c->h_small[7];  // torsion middles (bo > 0.001)
   if (c->pgrad_pairs > 0) c->h_pgrad.assign(c->h_pg, c->h_pg + (c->pgrad_pairs + c->pgrad_angles));
   c->last_A = A;
   // keep the scans for export
@@ -1157,6 +1168,12 @@ int xr_eval_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, un
 }
 
 long long xr_last_launches(const xr_ctx* c) { return c ? c->launches : 0; }
+
+int xr_last_list_sizes(const xr_ctx* c, long long* sizes, int n) {
+  if (!c || !sizes || n < 0) return XR_EINPUT;
+  for (int k = 0; k < n && k < 6; ++k) sizes[k] = c->list_sizes[k];
+  return XR_OK;
+}
 
 int xr_last_qeq_iterations(const xr_ctx* c) { return c ? c->qeq_iterations : 0; }
 

@@ -213,7 +213,7 @@ class Server:
 
     def stage_times(self):
         """Summed per-stage device milliseconds over every context, and the number of batches."""
-        total, calls = np.zeros(7), 0
+        total, calls = np.zeros(8), 0
         for calcs in self._calcs:
             for calc in calcs.values():
                 ms, n = calc.stage_times()
