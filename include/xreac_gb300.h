@@ -62,6 +62,17 @@ typedef struct {
   const double* charges_guess;
 } xr_system;
 
+/* A caller-supplied directed neighbour list of one system, xreac's neighbors=(i, j, S)
+ * (src/xreac/calculator.py:113-120, src/xreac/neighbors.py:101-131): edge e points from atom i[e] to
+ * the image of atom j[e] at x[j] + S[e] @ cell. Both directions of every pair, any order, no
+ * zero-shift self edge; edges beyond the cutoff (a skin) are allowed. Host pointers. */
+typedef struct {
+  long long count;  /* number of directed edges */
+  const int* i;     /* count source atoms */
+  const int* j;     /* count target atoms */
+  const int* S;     /* count x 3 integer lattice shifts */
+} xr_neighbors;
+
 /* Results of one system. Any pointer may be NULL to skip that output.
  * energy: 15 doubles = the 14 components in xreac's order (bond, atom, lone_pair, molecule, angle,
  * penalty, angle_conjugation, hydrogen_bond, torsion, conjugation, vdw, coulomb, electric_field,
@@ -114,6 +125,33 @@ int xr_ctx_set_wait_test(xr_ctx* ctx, long long polls, int fail_at);
 
 /* Evaluate one system (energy, fixed-charge forces, QEq charges, per-atom bond properties). */
 int xr_eval(xr_ctx* ctx, const xr_ff* ff, const xr_system* sys, unsigned flags, xr_result* out);
+
+/* Evaluate one system on exactly the edges of a caller-supplied list: Calculator.evaluate with
+ * neighbors=(i, j, S) (src/xreac/calculator.py:113-120). The list is validated with xreac's rules and
+ * messages (XR_EINPUT: indices out of range, nonzero shifts in non-periodic directions, zero-shift self
+ * edges, duplicates, a missing reverse direction), put in canonical order, and reduced on the device
+ * to its edges within the cutoff, which are the only ones that contribute; pairs missing from the list
+ * contribute nothing, as in xreac. Shifts beyond +-255 cells give XR_ECAPACITY. */
+int xr_eval_neighbors(xr_ctx* ctx, const xr_ff* ff, const xr_system* sys, const xr_neighbors* nb, unsigned flags,
+                      xr_result* out);
+
+/* The validation of xr_eval_neighbors alone, on the host (no device work): XR_OK, or the status and,
+ * in msg (msg_len bytes, NUL-terminated), the message xreac's ValueError carries. pbc: 3 flags. */
+int xr_neighbors_check(int natoms, const int* pbc, const xr_neighbors* nb, char* msg, int msg_len);
+
+/* Neighbour-list reuse across calls, as ASE's skin list does (src/xreac/ase.py:107-131): with
+ * skin > 0 each xr_eval / xr_eval_batch call keeps on the device a list of every image within
+ * cutoff + 2 skin, and a later call on the same systems (atom counts, types, pbc, cells, cutoff)
+ * reuses it while no atom has moved more than `skin` from its position at the build; the edges
+ * within the cutoff are then re-selected from that list by exact distance tests, so results equal
+ * those of a fresh list. skin = 0 (the default) scans every call. Setting the skin, even to its
+ * current value, drops the kept list. */
+int xr_ctx_set_skin(xr_ctx* ctx, double skin);
+
+/* How the last call got its neighbour rows (mode: 0 image scan, 1 skin list built, 2 skin list
+ * reused, 3 supplied list) and how many skin lists the context has built (no reference counterpart;
+ * instrumentation). */
+int xr_last_list_info(const xr_ctx* ctx, int* mode, long long* builds);
 
 /* Evaluate nsys independent systems in one ragged batch with per-system offsets. */
 int xr_eval_batch(xr_ctx* ctx, const xr_ff* ff, int nsys, const xr_system* sys, unsigned flags, xr_result* out);

@@ -19,7 +19,9 @@ can be checked without the reference present.
 Cases: the reference's own test geometries (imported from its ``examples/`` and
 ``tests/``), small versions of the benchmark workloads generated with
 ``xreac_gb300.workloads`` (the 192-atom water cluster is the full-size cluster
-workload), and a few request-stream samples.
+workload), a few request-stream samples, and caller-supplied neighbour lists
+(``supplied_*``: skin lists and thinned lists in shuffled order, whose lists are
+stored as ``sup_i``, ``sup_j``, ``sup_S``).
 """
 
 from __future__ import annotations
@@ -105,6 +107,54 @@ def workload_cases():
     return out
 
 
+def supplied_cases(cases):
+    """Caller-supplied neighbour lists, built with the reference's own replicated_neighbors at a larger
+    cutoff (a skin list: the result must equal the replicated one) or thinned (a partial list: the
+    result must follow the list, not the geometry), and handed over in a shuffled order."""
+    from xreac.neighbors import replicated_neighbors
+
+    rng = np.random.default_rng(8)
+    out = {}
+
+    def shuffled(i, j, S):
+        order = rng.permutation(len(i))
+        return i[order], j[order], S[order]
+
+    def half_mask(i, j, S):
+        neg = (S[:, 0] < 0) | ((S[:, 0] == 0) & ((S[:, 1] < 0) | ((S[:, 1] == 0) & (S[:, 2] < 0))))
+        return (i < j) | ((i == j) & neg)
+
+    def thinned(i, j, S, keep_half):
+        """Keep the half edges where keep_half, and with each its reverse."""
+        half = half_mask(i, j, S)
+        kept = {(int(a), int(b), *map(int, s)) for a, b, s, h, k in zip(i, j, S, half, keep_half) if h and k}
+        keep = np.array([((int(a), int(b), *map(int, s)) in kept) if h else
+                         ((int(b), int(a), *(-int(v) for v in s)) in kept) for a, b, s, h in zip(i, j, S, half)])
+        return i[keep], j[keep], S[keep]
+
+    def distances(x, i, j, S, cell):
+        lat = np.eye(3) if cell is None else np.asarray(cell, dtype=float)
+        v = x[j] - x[i] + S @ lat
+        return np.sqrt(np.sum(v * v, axis=1))
+
+    for base in ("small_water_4A", "periodic_carbon_chain", "cluster_water_192"):
+        ff_name, s, x, cell, pbc, charge = cases[base]
+        x = np.asarray(x, dtype=float)
+        from xreac import ForceField
+
+        rc = float(ForceField.bundled(ff_name).general[12])
+        (i, j, S), _ = replicated_neighbors(x, rc + 1.0, cell, pbc, max_expanded_atoms=100000)
+        out[f"supplied_skin_{base}"] = (ff_name, s, x, cell, pbc, charge, shuffled(i, j, S))
+        r = distances(x, i, j, S, cell)
+        if base == "cluster_water_192":
+            # drop about half of the pairs beyond 2.5 A (H-bond acceptors, vdW and Coulomb partners)
+            keep = (r <= 2.5) | (rng.random(len(i)) < 0.5)
+        else:
+            keep = r <= 6.0  # only the pairs within 6 A
+        out[f"supplied_partial_{base}"] = (ff_name, s, x, cell, pbc, charge, shuffled(*thinned(i, j, S, keep)))
+    return out
+
+
 def _ff_to_json(ff):
     def num(v):
         return [float(t) for t in np.asarray(v).ravel()]
@@ -123,7 +173,7 @@ def _ff_to_json(ff):
     )
 
 
-def run_case(name, ff_name, symbols, x, cell, pbc, charge, full_derivative=False):
+def run_case(name, ff_name, symbols, x, cell, pbc, charge, full_derivative=False, neighbors=None):
     import xreac
     from xreac.energy import EnergyModel
     from xreac.neighbors import replicated_neighbors
@@ -131,10 +181,14 @@ def run_case(name, ff_name, symbols, x, cell, pbc, charge, full_derivative=False
     ff = xreac.ForceField.bundled(ff_name)
     calc = xreac.Calculator(ff)
     t0 = time.time()
-    res = calc.evaluate(symbols, x, cell=cell, pbc=pbc, total_charge=charge, full_derivative=full_derivative)
+    res = calc.evaluate(symbols, x, cell=cell, pbc=pbc, total_charge=charge, full_derivative=full_derivative,
+                        neighbors=neighbors)
     elapsed = time.time() - t0
     # Per-edge quantities from the pure-numpy forward pass of the same model.
-    (nb, _) = replicated_neighbors(np.asarray(x, float), ff.general[12], cell, pbc)
+    if neighbors is None:
+        (nb, _) = replicated_neighbors(np.asarray(x, float), ff.general[12], cell, pbc)
+    else:
+        nb = neighbors
     model = EnergyModel(ff, symbols, nb, cell, pbc, total_charge=charge)
     _, r = model.edges.geometry(np.asarray(x, float))
     q = model.electrostatics(r)[0]
@@ -164,7 +218,11 @@ def run_case(name, ff_name, symbols, x, cell, pbc, charge, full_derivative=False
         edge_sha256=np.array(hashlib.sha256(np.ascontiguousarray(canon).tobytes()).hexdigest()),
         bo_value=bo[nz],
         seconds=np.array(elapsed),
+        neighbor_backend=np.array(res.neighbor_backend),
     )
+    if neighbors is not None:  # the list as handed over (not canonical; edges beyond the cutoff included)
+        data.update(sup_i=np.asarray(neighbors[0], dtype=np.int32), sup_j=np.asarray(neighbors[1], dtype=np.int32),
+                    sup_S=np.asarray(neighbors[2], dtype=np.int32))
     if len(canon) <= 100_000:  # small lists are stored in full; large ones by count and hash
         data.update(edge_i=canon[:, 0], edge_j=canon[:, 1], edge_S=canon[:, 2:].astype(np.int8), bo_index=nz.astype(np.int32))
     else:
@@ -190,6 +248,11 @@ def main(reference, only=None):
             continue
         dt, m = run_case(name, ff_name, list(s), x, cell, pbc, charge)
         print(f"{name:28s} n={len(s):4d} edges={m:7d} {dt:6.2f} s", flush=True)
+    for name, (ff_name, s, x, cell, pbc, charge, nb) in supplied_cases(cases).items():
+        if only and name not in only:
+            continue
+        dt, m = run_case(name, ff_name, list(s), x, cell, pbc, charge, neighbors=nb)
+        print(f"{name:28s} n={len(s):4d} edges={m:7d} {dt:6.2f} s (supplied list)", flush=True)
     for name in ("water_distorted_dimer", "zno_cluster20", "small_water_4A", "carbon_methane"):
         if only and name + "_full" not in only:
             continue

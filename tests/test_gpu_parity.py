@@ -57,7 +57,7 @@ def canonical_bonds(r):
     return ii[order], jj[order], SS[order], bb[order]
 
 
-@pytest.mark.parametrize("name", [n for n in golden_names() if not n.endswith("_full")])
+@pytest.mark.parametrize("name", [n for n in golden_names() if not n.endswith("_full") and not n.startswith("supplied_")])
 def test_reference_fixture(name):
     g = load_golden(name)
     c = calc(g["ff"])

@@ -31,9 +31,10 @@ def check_neighbors(g, i, j, s):
 
 def run_oracle(g):
     ff = ForceField.bundled(g["ff"])
+    supplied = (g["sup_i"], g["sup_j"], g["sup_S"]) if "sup_i" in g else None
     return evaluate(
         ff, g["symbols"], g["positions"], cell=g["cell"], pbc=g["pbc"], total_charge=g["total_charge"],
-        full_derivative=g["full_derivative"], dense_bond_orders="bond_orders" in g,
+        full_derivative=g["full_derivative"], dense_bond_orders="bond_orders" in g, neighbors=supplied,
     )
 
 

@@ -43,6 +43,10 @@ EXPORTED = (
     "xr_ctx_set_wait_test",
     "xr_eval",
     "xr_eval_batch",
+    "xr_eval_neighbors",
+    "xr_neighbors_check",
+    "xr_ctx_set_skin",
+    "xr_last_list_info",
     "xr_get_neighbors",
     "xr_get_bonds",
     "xr_last_launches",
@@ -70,6 +74,15 @@ class System(ctypes.Structure):
         ("pbc", c_int * 3),
         ("total_charge", c_double),
         ("charges_guess", c_void_p),  # const double* or NULL
+    ]
+
+
+class Neighbors(ctypes.Structure):
+    _fields_ = [
+        ("count", c_longlong),
+        ("i", c_void_p),  # const int*, count
+        ("j", c_void_p),  # const int*, count
+        ("S", c_void_p),  # const int*, count x 3
     ]
 
 
@@ -122,6 +135,14 @@ def load():
     lib.xr_eval.restype = c_int
     lib.xr_eval_batch.argtypes = [c_void_p, c_void_p, c_int, POINTER(System), c_uint, POINTER(Result)]
     lib.xr_eval_batch.restype = c_int
+    lib.xr_eval_neighbors.argtypes = [c_void_p, c_void_p, POINTER(System), POINTER(Neighbors), c_uint, POINTER(Result)]
+    lib.xr_eval_neighbors.restype = c_int
+    lib.xr_neighbors_check.argtypes = [c_int, POINTER(c_int), POINTER(Neighbors), c_char_p, c_int]
+    lib.xr_neighbors_check.restype = c_int
+    lib.xr_ctx_set_skin.argtypes = [c_void_p, c_double]
+    lib.xr_ctx_set_skin.restype = c_int
+    lib.xr_last_list_info.argtypes = [c_void_p, POINTER(c_int), POINTER(c_longlong)]
+    lib.xr_last_list_info.restype = c_int
     lib.xr_get_neighbors.argtypes = [c_void_p, c_int, POINTER(c_int), POINTER(c_int), POINTER(c_int), c_longlong,
                                      POINTER(c_longlong)]
     lib.xr_get_neighbors.restype = c_int

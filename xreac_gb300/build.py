@@ -20,7 +20,7 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIBDIR = PKG / "_lib"
 LIB = LIBDIR / "libxreac_gb300.so"
-SOURCES = ("xr_topology.cu", "xr_bonded.cu", "xr_nonbonded.cu", "xr_engine.cu", "xr_static.cu")
+SOURCES = ("xr_topology.cu", "xr_bonded.cu", "xr_nonbonded.cu", "xr_engine.cu", "xr_static.cu", "xr_lists.cu")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 

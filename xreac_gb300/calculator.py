@@ -107,6 +107,9 @@ class Evaluation:
 # A batch's evaluations make these fields on first access. ``bonds`` has a default in the dataclass;
 # its class attribute is removed below (the default stays in ``__init__``) so that the lookup of a
 # missing value reaches ``__getattr__``.
+# Skin of the device neighbour list during a native relaxation (A), ASE's default.
+RELAX_SKIN = 0.3
+
 _BATCH_FIELDS = frozenset(("forces", "charges", "components", "total_bond_orders", "lone_pairs", "bond_counts",
                            "dipole", "bonds"))
 del Evaluation.bonds
@@ -260,6 +263,33 @@ class Calculator:
         if self._lib.xr_ctx_set_qeq(self._ctx.handle, float(tolerance), int(max_iterations)) != nat.XR_OK:
             raise ValueError("QEq tolerance must be positive and the iteration limit at least 1")
 
+    def set_neighbor_skin(self, skin):
+        """Reuse the device neighbour list across calls (``xr_ctx_set_skin``), ASE's skin rule.
+
+        With ``skin`` > 0 (A) each call keeps a list of every image within cutoff + 2 skin on the
+        device, and a later call on the same systems (atom counts, labels, cell, pbc) reuses it while
+        no atom has moved more than ``skin`` from where it was at the build. The edges within the
+        cutoff are re-selected from it by exact distance tests each call, so results equal those of
+        a fresh list. 0 (the default) scans every call.
+        """
+        if isinstance(skin, bool) or not isinstance(skin, Real) or not math.isfinite(skin) or skin < 0:
+            raise ValueError("neighbor_skin must be a finite nonnegative number")
+        if self._lib.xr_ctx_set_skin(self._ctx.handle, float(skin)) != nat.XR_OK:
+            raise ValueError("neighbor_skin must be a finite nonnegative number")
+        self._skin = float(skin)
+
+    @property
+    def neighbor_skin(self):
+        return getattr(self, "_skin", 0.0)
+
+    def list_info(self):
+        """(how the last call got its neighbour rows: "scan", "built", "reused" or "supplied", skin
+        lists built so far)."""
+        mode = nat.c_int()
+        builds = nat.c_longlong()
+        self._lib.xr_last_list_info(self._ctx.handle, nat.byref(mode), nat.byref(builds))
+        return ("scan", "built", "reused", "supplied")[mode.value], int(builds.value)
+
     def set_wait_test(self, polls=0, fail_at=0):
         """For tests of the QEq solver's failure path (``xr_ctx_set_wait_test``): ``polls`` > 0
         replaces the poll limits of the bounded team waits, and ``fail_at`` > 0 makes team wait number
@@ -281,11 +311,14 @@ class Calculator:
         if code != nat.XR_OK:
             raise RuntimeError(self._ctx.last_error())
 
-    def _prepare(self, symbols, positions, total_charge, cell, pbc, full_derivative):
+    def _prepare(self, symbols, positions, total_charge, cell, pbc, full_derivative, replicate=True):
         """Validated ``(symbols, positions, types, pbc flags, cell or None, repetitions)``.
 
         The positions are float64 and C-contiguous, but not copied when they already are, and not
-        yet checked for finite values: ``_run`` checks the whole batch at once.
+        yet checked for finite values: ``_run`` checks the whole batch at once. ``replicate=False``
+        (a caller-supplied list) skips xreac's small-cell replication count and its
+        ``max_expanded_atoms`` limit, as xreac does when it is given neighbours, and reports
+        (1, 1, 1).
         """
         if full_derivative is not True and full_derivative is not False:
             raise ValueError("full_derivative must be a boolean")
@@ -310,17 +343,19 @@ class Calculator:
             if (pbc is None and cell is None) or pbc is False:
                 flags, m = _NO_PBC, None
             else:
-                fast = periodic_cell(cell, pbc, float(ff.general[12]), len(symbols), self.max_expanded_atoms)
+                limit = self.max_expanded_atoms if replicate else 1 << 62
+                fast = periodic_cell(cell, pbc, float(ff.general[12]), len(symbols), limit)
                 if fast is not None:
                     if not self._all_valid:
                         ff.validate_model(symbols)
-                    return symbols, x, types, fast[0], fast[1], fast[2]
+                    return symbols, x, types, fast[0], fast[1], fast[2] if replicate else (1, 1, 1)
                 flags, m = boundary(cell, pbc)
             if not self._all_valid:
                 ff.validate_model(symbols)
         if m is None:
             return symbols, x, types, flags, None, (1, 1, 1)
-        reps = cell_repetitions(float(ff.general[12]), flags, m, len(symbols), self.max_expanded_atoms)
+        reps = (cell_repetitions(float(ff.general[12]), flags, m, len(symbols), self.max_expanded_atoms) if replicate
+                else (1, 1, 1))
         return symbols, x, types, flags, np.ascontiguousarray(m, dtype=np.float64), reps
 
     def _raise(self, code):
@@ -340,15 +375,31 @@ class Calculator:
         the same tolerance; only the iteration count changes.
         """
         symbols, x, types, flags, cellm, reps = self._prepare(symbols, positions, total_charge, cell, pbc,
-                                                              full_derivative)
-        backend = "replicated"
-        if neighbors is not None:
-            from .neighbors import check_supplied
-
-            check_supplied(neighbors, len(symbols), flags)
-            reps, backend = (1, 1, 1), "provided"
+                                                              full_derivative, replicate=neighbors is None)
         guess = _guess(initial_charges, len(symbols))
-        return self._run([(types, x, flags, cellm, float(total_charge), guess)], full_derivative, [reps], backend)[0]
+        if neighbors is not None:
+            from .neighbors import supplied_arrays
+
+            # exactly the caller's edges (their validation, canonical order and reduction to the
+            # cutoff run in the library: xr_eval_neighbors)
+            i, j, shifts = supplied_arrays(neighbors, len(symbols))
+            nb = nat.Neighbors(len(i), nat.addr(i), nat.addr(j), nat.addr(shifts))
+            return self._run([(types, x, flags, cellm, float(total_charge), guess)], full_derivative, [(1, 1, 1)],
+                             "provided", supplied=nb)[0]
+        return self._run([(types, x, flags, cellm, float(total_charge), guess)], full_derivative, [reps],
+                         "replicated")[0]
+
+    def _evaluate_backend(self, symbols, positions, *, total_charge=0, cell=None, pbc=None, full_derivative=False,
+                          backend="replicated"):
+        """``evaluate`` for the ASE adapter. ``backend="ase"`` evaluates as xreac does with ASE's image
+        lists: no small-cell replication count or ``max_expanded_atoms`` limit, ``cell_repetitions``
+        (1, 1, 1) and the result labelled "ase"; the device list (and its skin reuse) is the same."""
+        if backend != "ase":
+            return self.evaluate(symbols, positions, total_charge=total_charge, cell=cell, pbc=pbc,
+                                 full_derivative=full_derivative)
+        symbols, x, types, flags, cellm, _ = self._prepare(symbols, positions, total_charge, cell, pbc,
+                                                           full_derivative, replicate=False)
+        return self._run([(types, x, flags, cellm, float(total_charge), None)], full_derivative, [(1, 1, 1)], "ase")[0]
 
     def parameter_gradient(self, symbols, positions, *, total_charge=0, cell=None, pbc=None, initial_charges=None):
         """Energy, forces and dE/dtheta for the bond, angle and vdW parameters (an extension; xreac
@@ -460,10 +511,10 @@ class Calculator:
         charges = [float(it[2]) for it in items]
         return types, x, offsets, flags_l, cells, charges, _GuessAddresses(guess_addr, keep), reps
 
-    def _run(self, batch, full_derivative, reps, backend, extra_flags=0):
+    def _run(self, batch, full_derivative, reps, backend, extra_flags=0, supplied=None):
         """One ``xr_eval_batch`` call over ``batch`` = [(types, positions, pbc flags, cell, total
         charge, initial charges)]: the inputs are packed into one array per kind, then as
-        ``_run_packed``."""
+        ``_run_packed`` (``xr_eval_neighbors`` with a supplied list for a single system)."""
         n_sys = len(batch)
         types_l, xs, flags_l, cells, charges, guesses = zip(*batch)
         sizes = np.fromiter(map(len, types_l), dtype=np.int64, count=n_sys)
@@ -472,10 +523,10 @@ class Calculator:
         types = np.concatenate(types_l) if n_sys > 1 else types_l[0]
         x = np.concatenate(xs) if n_sys > 1 else xs[0]
         return self._run_packed(types, x, offsets, flags_l, cells, charges, guesses, reps, full_derivative, backend,
-                                extra_flags)
+                                extra_flags, supplied)
 
     def _run_packed(self, types, x, offsets, flags_l, cells, charges, guesses, reps, full_derivative, backend,
-                    extra_flags=0):
+                    extra_flags=0, supplied=None):
         """One ``xr_eval_batch`` call: the per-system descriptors are filled column-wise over the
         packed types and positions, so the host cost per system is a handful of numpy operations;
         each ``Evaluation`` gets views of the batch's result arrays."""
@@ -521,8 +572,12 @@ class Calculator:
         res_arr["bond_counts"] = nat.addr(counts) + 4 * a0s
         res_arr["dipole"] = nat.addr(dipole) + 24 * ks
         flags_ = (nat.XR_FLAG_FULL_DERIVATIVE if full_derivative else 0) | extra_flags
-        code = lib.xr_eval_batch(self._ctx.handle, self._ff.handle, n_sys, sys_arr.ctypes.data_as(_SYSTEM_P), flags_,
-                                 res_arr.ctypes.data_as(_RESULT_P))
+        if supplied is not None:
+            code = lib.xr_eval_neighbors(self._ctx.handle, self._ff.handle, sys_arr.ctypes.data_as(_SYSTEM_P),
+                                         nat.byref(supplied), flags_, res_arr.ctypes.data_as(_RESULT_P))
+        else:
+            code = lib.xr_eval_batch(self._ctx.handle, self._ff.handle, n_sys, sys_arr.ctypes.data_as(_SYSTEM_P),
+                                     flags_, res_arr.ctypes.data_as(_RESULT_P))
         if code != nat.XR_OK:
             self._raise(code)
         bi, bj, bS, bbo = self._bonds(-1)
@@ -566,10 +621,11 @@ class Calculator:
         dt = 0.02 growing by 1.1 up to 0.2 after more than five steps with positive power, halved
         (and the velocity reset) otherwise, mixing alpha = 0.1 decaying by 0.99, and the largest
         atomic step capped at 0.1 A (Bitzek et al., Phys. Rev. Lett. 97, 170201, 2006). Every step
-        is one device evaluation whose QEq starts from the previous step's charges; the returned
-        evaluation is a plain one at the final positions, identical to :meth:`evaluate` there.
-        ``backend="ase"`` runs ASE's FIRE through :class:`xreac_gb300.ase.ReaxFFCalculator`,
-        which needs ASE installed, as xreac's does.
+        is one device evaluation whose QEq starts from the previous step's charges and whose
+        neighbour list is the device's skin list (0.3 A, rebuilt only when an atom has moved that
+        far); the returned evaluation is a plain one at the final positions, identical to
+        :meth:`evaluate` there. ``backend="ase"`` runs ASE's FIRE through
+        :class:`xreac_gb300.ase.ReaxFFCalculator`, which needs ASE installed, as xreac's does.
         """
         symbols, x, _, _ = validate_input(symbols, positions, total_charge, cell, pbc)
         if isinstance(force_tolerance, bool) or not isinstance(force_tolerance, Real) \
@@ -588,6 +644,15 @@ class Calculator:
                                                               cell=cell, pbc=flags, total_charge=total_charge)
             message = "Fixed-charge force tolerance reached" if converged else "Maximum relaxation iterations reached"
             return Relaxation(x, result, converged, iterations, message)
+        skin = self.neighbor_skin
+        self.set_neighbor_skin(RELAX_SKIN)
+        try:
+            return self._fire(symbols, x, force_tolerance, max_iterations, kw)
+        finally:
+            self.set_neighbor_skin(skin)
+
+    def _fire(self, symbols, x, force_tolerance, max_iterations, kw):
+        """xreac's native FIRE recurrence (src/xreac/calculator.py:213-246) on device evaluations."""
         velocity = np.zeros_like(x)
         dt, dt_max, alpha = 0.02, 0.2, 0.1
         positive_steps = 0

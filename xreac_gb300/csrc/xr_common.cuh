@@ -129,7 +129,7 @@ struct XrWork {
   int wait_fail_at;
   const XrSystem* sys;
   int* status;                // one int of XR_S_* bits
-  int* counts;                // [4]: E, P, B, D totals (last entries of the scans)
+  int* counts;                // [8]: E, P, B, D totals (last entries of the scans), [4] QEq iterations, [5] candidates
   // atoms
   const double4_32a* x;           // positions (w unused)
   const int* type;
@@ -139,6 +139,10 @@ struct XrWork {
   float4* fw;                 // wrapped fractional coordinates, FP32
   int* cnt;                   // [4][A+1] counts, then exclusive scans in place:
                               //   0: edges, 1: half edges (pairs), 2: half bonds, 3: bond rows
+  // candidate list: per atom, a superset of its edges as {j, shift bits} in canonical order (a skin
+  // list kept from an earlier call, or a caller-supplied list); CSR by cand_cnt [A+1]
+  int* cand_cnt;
+  int2* cand_edge;
   // edges
   int2* edge;                 // {j, code}
   int* edge_pair;             // pair id of every edge (its own or its reverse's)
@@ -224,9 +228,19 @@ enum BJ { BJ_BO = 0, BJ_PI, BJ_PP, BJ_SIG, BJ_BO0, BJ_PI0, BJ_PP0, BJ_CI, BJ_CJ,
 #define XR_CHUNK_ATOMS 1024
 
 // Kernel launchers (defined in the .cu files, called by the engine).
-void xr_launch_topology(const XrWork& w, cudaStream_t st);
+void xr_launch_topology(const XrWork& w, cudaStream_t st);  // xr_launch_prep, then xr_launch_count
+void xr_launch_prep(const XrWork& w, cudaStream_t st);      // wrapped FP32 coordinates (k_prep)
+void xr_launch_count(const XrWork& w, cudaStream_t st);     // all-pairs image scan, counts (k_neighbors<false>)
+void xr_launch_rows(const XrWork& w, cudaStream_t st);      // all-pairs image scan, rows (k_neighbors<true>)
 void xr_launch_scan(const XrWork& w, cudaStream_t st);
 void xr_launch_topology_fill(const XrWork& w, cudaStream_t st);
+// Candidate list at the cutoff of w.sys (descriptors at rc + 2 skin): fill=false counts into cand_cnt
+// and scans it (total into counts[5]); fill=true writes cand_edge.
+void xr_launch_candidates(const XrWork& w, bool fill, cudaStream_t st);
+// The edges within the cutoff of the candidate list: fill=false counts into cnt (scanned by
+// xr_launch_scan), fill=true writes the rows, pairs and bonds.
+void xr_launch_filter(const XrWork& w, bool fill, cudaStream_t st);
+void xr_launch_reverse(const XrWork& w, cudaStream_t st);
 void xr_launch_pairs(const XrWork& w, const XrFF& ff, cudaStream_t st);
 int xr_launch_qeq(const XrWork& w, const XrFF& ff, cudaStream_t st, int nblocks, const int4* map, int nteam,
                   const int* small, int nsmall, bool adjoint = false);

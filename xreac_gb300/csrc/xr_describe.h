@@ -34,6 +34,10 @@ inline void inverse3(const double m[9], double inv[9], double* det_out) {
 // has_guess are left to the caller. xpack (may be null) receives the positions as double4.
 // Returns XR_OK, or XR_EINPUT with *msg set to xreac's message for the failed check.
 //
+// The error band covers every candidate image near a threshold, whichever list it comes from (the
+// scan's images, a skin list, a caller's list): for such a candidate the image offset s in the
+// wrapped frame has |s_k| < rc / h_k + 1 (h_k the cell height), which the reach below bounds.
+//
 // Cell rule of xreac's Boundary (src/xreac/geometry.py:37-39): det(cell) must exceed
 // 1e-12 * |a1| |a2| |a3| ("nonsingular and right-handed").
 // Image reach: where the cell height exceeds 2 rc only the nearest image can be within rc;

@@ -13,6 +13,7 @@
 
 #include "xr_common.cuh"
 #include "xr_describe.h"
+#include "xr_lists.h"
 #include "xreac_gb300.h"
 
 namespace {
@@ -51,6 +52,32 @@ struct xr_ctx {
   int cg_max = 2000;
   long long wait_polls = 0;  // QEq team waits: poll limit (0: defaults) and the wait a test makes run out
   int wait_fail_at = 0;
+  // Candidate lists (a superset of each atom's edges, {j, shift bits} rows in canonical order): the
+  // skin list kept for reuse, or the rows of a caller-supplied list.
+  int* cand_cnt = nullptr;  // [A+1] row offsets
+  size_t ccand_cnt = 0;
+  int2* cand_edge = nullptr;
+  size_t ccand_edge = 0;
+  XrSystem* sys_list = nullptr;  // descriptors at the list cutoff rc + 2 skin (builds only)
+  size_t csys_list = 0;
+  int* h_cand_cnt = nullptr;  // pinned staging of a supplied list
+  size_t ch_cand_cnt = 0;
+  int2* h_cand_edge = nullptr;
+  size_t ch_cand_edge = 0;
+  XrSystem* h_sys_list = nullptr;
+  size_t ch_sys_list = 0;
+  // Skin reuse (xr_ctx_set_skin): the list of the last call is reused by a call on the same systems
+  // (atom counts, types, cells, pbc, cutoff) in which no atom moved more than `skin` from where it was
+  // when the list was built; the list holds every image within rc + 2 skin then (ASE's convention).
+  double skin = 0.0;
+  bool cache_valid = false;
+  double cache_rc = 0.0, cache_skin = 0.0;
+  std::vector<double> cache_x0;   // [3A] positions at the build
+  std::vector<int> cache_types;   // [A]
+  std::vector<int> cache_shape;   // per system: natoms, pbc[3]
+  std::vector<double> cache_cell; // per system: 9 cell entries (identity when not periodic)
+  long long list_builds = 0;      // candidate lists built since the context was made
+  int list_mode = 0;              // of the last call: 0 scanned, 1 list built, 2 list reused, 3 supplied
   int nsm = 0;
   int coop_per_sm = 0;
   int max_clusters = 0;  // resident thread-block clusters of the cluster QEq solver (0: unavailable),
@@ -214,11 +241,6 @@ struct xr_ctx {
 };
 
 namespace {
-
-bool set_err(xr_ctx* c, const std::string& m) {
-  c->err = m;
-  return false;
-}
 
 int cuda_fail(xr_ctx* c, cudaError_t e, const char* where) {
   c->err = std::string("CUDA error in ") + where + ": " + cudaGetErrorString(e);
@@ -388,6 +410,8 @@ void fill_work(xr_ctx* c, XrWork& w, int A, int S, unsigned flags) {
 }
 
 void attach_lists(xr_ctx* c, XrWork& w) {
+  w.cand_cnt = c->cand_cnt;
+  w.cand_edge = c->cand_edge;
   w.cap_E = (long long)c->cedge;
   w.cap_P = (long long)c->cpair_edge;
   w.cap_B = (long long)c->capB;
@@ -609,9 +633,63 @@ bool plan_qeq_cluster(xr_ctx* c, const xr_system* sys, int nsys, int* csize, int
   return true;
 }
 
-int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsigned flags, xr_result* out) {
+// Whether the kept skin list serves this call: the same systems (atom counts, types, pbc, cells) at
+// the same cutoff and skin, and no atom further than `skin` from its position at the build (the rule
+// of ASE's PrimitiveNeighborList.update: a rebuild once any atom moved more than the skin).
+bool skin_list_valid(const xr_ctx* c, int nsys, int A, double rc) {
+  if (!c->cache_valid || c->cache_rc != rc || c->cache_skin != c->skin || (int)c->cache_types.size() != A ||
+      (int)c->cache_shape.size() != 4 * nsys)
+    return false;
+  for (int s = 0; s < nsys; ++s) {
+    const XrSystem& S = c->host_sys[s];
+    const int* sh = c->cache_shape.data() + 4 * s;
+    if (sh[0] != S.natoms || sh[1] != S.periodic[0] || sh[2] != S.periodic[1] || sh[3] != S.periodic[2]) return false;
+    if (std::memcmp(c->cache_cell.data() + 9 * s, S.cell, 9 * sizeof(double)) != 0) return false;
+  }
+  if (std::memcmp(c->cache_types.data(), c->h_types, sizeof(int) * (size_t)A) != 0) return false;
+  const double lim = c->skin * c->skin;
+  for (int a = 0; a < A; ++a) {
+    const double dx = c->h_x[a].x - c->cache_x0[3 * a], dy = c->h_x[a].y - c->cache_x0[3 * a + 1],
+                 dz = c->h_x[a].z - c->cache_x0[3 * a + 2];
+    if (dx * dx + dy * dy + dz * dz > lim) return false;
+  }
+  return true;
+}
+
+void keep_skin_list(xr_ctx* c, int nsys, int A, double rc) {
+  c->cache_rc = rc;
+  c->cache_skin = c->skin;
+  c->cache_types.assign(c->h_types, c->h_types + A);
+  c->cache_x0.resize(3 * (size_t)A);
+  for (int a = 0; a < A; ++a) {
+    c->cache_x0[3 * a] = c->h_x[a].x;
+    c->cache_x0[3 * a + 1] = c->h_x[a].y;
+    c->cache_x0[3 * a + 2] = c->h_x[a].z;
+  }
+  c->cache_shape.resize(4 * (size_t)nsys);
+  c->cache_cell.resize(9 * (size_t)nsys);
+  for (int s = 0; s < nsys; ++s) {
+    const XrSystem& S = c->host_sys[s];
+    int* sh = c->cache_shape.data() + 4 * s;
+    sh[0] = S.natoms;
+    sh[1] = S.periodic[0];
+    sh[2] = S.periodic[1];
+    sh[3] = S.periodic[2];
+    std::memcpy(c->cache_cell.data() + 9 * s, S.cell, 9 * sizeof(double));
+  }
+  c->cache_valid = true;
+}
+
+enum ListMode { kScan = 0, kBuild = 1, kReuse = 2, kSupplied = 3 };
+
+int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsigned flags, xr_result* out,
+              const xr_neighbors* nb = nullptr) {
   if (!c || !ff || nsys < 1 || !sys) {
     if (c) c->err = "invalid arguments";
+    return XR_EINPUT;
+  }
+  if (nb && nsys != 1) {
+    c->err = "a supplied neighbour list belongs to a single-system call";
     return XR_EINPUT;
   }
   const bool dev_io = (flags & XR_FLAG_DEVICE_IO) != 0;
@@ -693,6 +771,56 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
     }
     off += in.natoms;
   }
+  // Where the rows come from: the all-pairs image scan, a skin list (built now, or kept from an
+  // earlier call), or the caller's list.
+  ListMode mode = kScan;
+  if (nb) {
+    std::vector<int> start;
+    std::vector<int2> rows;
+    int maxs[3];
+    std::string msg;
+    const int code = xr_host::canonical_list(sys[0].natoms, sys[0].pbc, *nb, start, rows, maxs, msg);
+    if (code != XR_OK) {
+      c->err = msg;
+      return code;
+    }
+    if (!grow(&c->cand_cnt, &c->ccand_cnt, (size_t)A + 1) || !grow(&c->cand_edge, &c->ccand_edge, std::max<size_t>(rows.size(), 1)) ||
+        !host_grow(&c->h_cand_cnt, &c->ch_cand_cnt, (size_t)A + 1) ||
+        !host_grow(&c->h_cand_edge, &c->ch_cand_edge, std::max<size_t>(rows.size(), 1)))
+      return cuda_fail(c, cudaErrorMemoryAllocation, "allocation");
+    std::memcpy(c->h_cand_cnt, start.data(), sizeof(int) * ((size_t)A + 1));
+    if (!rows.empty()) std::memcpy(c->h_cand_edge, rows.data(), sizeof(int2) * rows.size());
+    c->cache_valid = false;  // the candidate arrays now hold the caller's list
+    mode = kSupplied;
+  } else if (c->skin > 0.0) {
+    mode = skin_list_valid(c, nsys, A, rc) ? kReuse : kBuild;
+    if (mode == kBuild) {
+      if (!host_grow(&c->h_sys_list, &c->ch_sys_list, (size_t)nsys) || !grow(&c->sys_list, &c->csys_list, (size_t)nsys) ||
+          !grow(&c->cand_cnt, &c->ccand_cnt, (size_t)A + 1))
+        return cuda_fail(c, cudaErrorMemoryAllocation, "allocation");
+      const double rl = rc + 2.0 * c->skin;
+      for (int s = 0, o = 0; s < nsys; o += sys[s].natoms, ++s) {
+        const char* msg = "";
+        xr_system in = sys[s];
+        in.positions = nullptr;  // positions come from the packed copy below
+        XrSystem& L = c->h_sys_list[s];
+        // the list cutoff's descriptor: the same cell and wrap, the list cutoff's reach and band
+        std::vector<double> px(3 * (size_t)in.natoms);
+        for (int a = 0; a < in.natoms; ++a) {
+          px[3 * a] = c->h_x[o + a].x;
+          px[3 * a + 1] = c->h_x[o + a].y;
+          px[3 * a + 2] = c->h_x[o + a].z;
+        }
+        in.positions = px.data();
+        const int code = xr_host::describe_system(in, o, rl, L, nullptr, &msg);
+        if (code != XR_OK) {
+          c->err = msg;
+          return code;
+        }
+      }
+      c->cache_valid = false;  // rebuilt below
+    }
+  }
   size_t nchunk = 0;
   for (int s = 0; s < nsys; ++s) nchunk += (size_t)(sys[s].natoms + XR_CHUNK_ATOMS - 1) / XR_CHUNK_ATOMS;
   if (!host_grow(&c->h_chunks, &c->ch_chunks, nchunk) || !host_grow(&c->h_syschunks, &c->ch_syschunks, (size_t)nsys) ||
@@ -752,8 +880,49 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
   }
   attach_lists(c, w);
   stage(c, 0, st);
-  xr_launch_topology(w, st);
-  launches += 2;
+  xr_launch_prep(w, st);
+  launches += 1;
+  if (mode == kScan || mode == kSupplied) {
+    // the image scan; for a supplied list only its coincident-atom check counts (xreac checks every
+    // pair's minimum image whatever list it is given), and the filter's counts replace its own
+    xr_launch_count(w, st);
+    launches += 1;
+  }
+  if (mode == kSupplied) {
+    cudaMemcpyAsync(c->cand_cnt, c->h_cand_cnt, sizeof(int) * ((size_t)A + 1), cudaMemcpyHostToDevice, st);
+    const long long m = c->h_cand_cnt[A];
+    if (m > 0) cudaMemcpyAsync(c->cand_edge, c->h_cand_edge, sizeof(int2) * (size_t)m, cudaMemcpyHostToDevice, st);
+    h2d += sizeof(int) * ((long long)A + 1) + sizeof(int2) * m;
+  }
+  if (mode == kBuild) {
+    // every image within rc + 2 skin, with the list cutoff's descriptors
+    cudaMemcpyAsync(c->sys_list, c->h_sys_list, sizeof(XrSystem) * nsys, cudaMemcpyHostToDevice, st);
+    cudaMemsetAsync(c->cand_cnt, 0, sizeof(int) * ((size_t)A + 1), st);
+    h2d += sizeof(XrSystem) * (long long)nsys;
+    XrWork wl = w;
+    wl.sys = c->sys_list;
+    wl.cand_cnt = c->cand_cnt;
+    xr_launch_candidates(wl, false, st);
+    launches += 4;
+    cudaMemcpyAsync(c->h_small + 9, c->counts + 5, sizeof(int), cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(c->h_small + 4, c->status, sizeof(int), cudaMemcpyDeviceToHost, st);
+    d2h += 2 * sizeof(int);
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(c, e, "neighbour list count");
+    if (int code = status_to_code(c, c->h_small[4])) return code;
+    const int m = c->h_small[9];
+    if (!grow(&c->cand_edge, &c->ccand_edge, std::max<size_t>((size_t)m, 1)))
+      return cuda_fail(c, cudaErrorMemoryAllocation, "list allocation");
+    wl.cand_edge = w.cand_edge = c->cand_edge;
+    xr_launch_candidates(wl, true, st);
+    launches += 1;
+    ++c->list_builds;
+  }
+  if (mode != kScan) {
+    w.cand_cnt = c->cand_cnt;
+    w.cand_edge = c->cand_edge;
+    xr_launch_filter(w, false, st);
+    launches += 1;
+  }
   xr_launch_scan(w, st);
   launches += 3;
   cudaMemcpyAsync(c->h_small, c->counts, 4 * sizeof(int), cudaMemcpyDeviceToHost, st);
@@ -762,6 +931,8 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
   if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(c, e, "neighbour count");
   const int nE = c->h_small[0], nP = c->h_small[1], nB = c->h_small[2], nD = c->h_small[3];
   if (int code = status_to_code(c, c->h_small[4])) return code;
+  if (mode == kBuild) keep_skin_list(c, nsys, A, rc);
+  c->list_mode = mode;
   if (!ensure_lists(c, nE, nP, nB)) return cuda_fail(c, cudaErrorMemoryAllocation, "list allocation");
   attach_lists(c, w);
   w.nE = nE;
@@ -769,7 +940,11 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
   w.nB = nB;
   w.nD = nD;
   stage(c, 1, st);
-  xr_launch_topology_fill(w, st);
+  if (mode == kScan)
+    xr_launch_rows(w, st);
+  else
+    xr_launch_filter(w, true, st);
+  xr_launch_reverse(w, st);
   launches += 2;
   cudaMemsetAsync(c->a_adj, 0, sizeof(double) * (size_t)AJ_N * A, st);
   cudaMemsetAsync(c->f, 0, sizeof(double) * 3 * (size_t)A, st);
@@ -1126,7 +1301,8 @@ void xr_ctx_destroy(xr_ctx* c) {
                   c->pair_bond, c->p_r, c->p_shield, c->p_dshield, c->p_g, c->p_evdw, c->p_ecoul, c->bond_pair,
                   c->bond_i, c->bond_j, c->b_r, c->b_v, c->b_fwd, c->b_adj, c->b_e, c->dbrow, c->sys, c->energy,
                   c->props, c->status, c->counts, c->barrier, c->qmap, c->qsmall, c->qiters, c->red, c->qguess, c->qrhs, c->qadj, c->pgrad, c->bx_meta, c->bx_bo, c->bx_count,
-                  c->esum, c->arow, c->nact, c->nzrow, c->nnz, c->chunks, c->sys_chunks, c->chunk_part, c->mids, c->nmids, c->mlist};
+                  c->esum, c->arow, c->nact, c->nzrow, c->nnz, c->chunks, c->sys_chunks, c->chunk_part, c->mids, c->nmids, c->mlist,
+                  c->cand_cnt, c->cand_edge, c->sys_list};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (c->h_x) cudaFreeHost(c->h_x);
@@ -1134,7 +1310,7 @@ void xr_ctx_destroy(xr_ctx* c) {
   if (c->h_guess) cudaFreeHost(c->h_guess);
   for (void* hp : {(void*)c->h_types, (void*)c->h_sysof, (void*)c->h_sysd, (void*)c->h_chunks, (void*)c->h_syschunks,
                    (void*)c->h_qmap_p, (void*)c->h_qsmall_p, (void*)c->h_cnt, (void*)c->h_bxm, (void*)c->h_bxb,
-                   (void*)c->h_qit, (void*)c->h_pg})
+                   (void*)c->h_qit, (void*)c->h_pg, (void*)c->h_cand_cnt, (void*)c->h_cand_edge, (void*)c->h_sys_list})
     if (hp) cudaFreeHost(hp);
   if (c->h_small) cudaFreeHost(c->h_small);
   for (int k = 0; k <= xr_ctx::kStages; ++k)
@@ -1161,6 +1337,29 @@ int xr_ctx_set_wait_test(xr_ctx* c, long long polls, int fail_at) {
 
 int xr_eval(xr_ctx* c, const xr_ff* ff, const xr_system* sys, unsigned flags, xr_result* out) {
   return run_batch(c, ff, 1, sys, flags, out);
+}
+
+int xr_eval_neighbors(xr_ctx* c, const xr_ff* ff, const xr_system* sys, const xr_neighbors* nb, unsigned flags,
+                      xr_result* out) {
+  if (c && !nb) {
+    c->err = "neighbors must be a tuple (i, j, S)";
+    return XR_EINPUT;
+  }
+  return run_batch(c, ff, 1, sys, flags, out, nb);
+}
+
+int xr_ctx_set_skin(xr_ctx* c, double skin) {
+  if (!c || !(skin >= 0.0) || !std::isfinite(skin)) return XR_EINPUT;
+  c->cache_valid = false;  // setting the skin, even to its current value, drops the kept list
+  c->skin = skin;
+  return XR_OK;
+}
+
+int xr_last_list_info(const xr_ctx* c, int* mode, long long* builds) {
+  if (!c) return XR_EINPUT;
+  if (mode) *mode = c->list_mode;
+  if (builds) *builds = c->list_builds;
+  return XR_OK;
 }
 
 int xr_eval_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsigned flags, xr_result* out) {

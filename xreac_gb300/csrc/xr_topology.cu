@@ -112,6 +112,30 @@ __device__ inline int classify(const XrWork& w, const XrSystem& S, const ScreenC
                          (half ? XR_CODE_HALF : 0u));
 }
 
+// Writes edge e = (i -> j, code c) of the list and, for its flags, its pair p (half edges), bond b
+// (half bond edges) and bond-row slot (bond edges); the other indices are -1.
+__device__ inline void emit_edge(const XrWork& w, int i, int j, uint32_t c, int e, int p, int b, int slot) {
+  w.edge[e] = make_int2(j, (int)c);
+  w.edge_dbslot[e] = slot;
+  if (p >= 0) {
+    w.edge_pair[e] = p;
+    w.pair_edge[p] = e;
+    w.pair_i[p] = i;
+    if (b >= 0) {
+      w.pair_bond[p] = b;
+      w.bond_pair[b] = p;
+      w.bond_i[b] = i;
+      w.bond_j[b] = j;
+      w.dbrow[slot] = make_int2(b, 1);
+    } else {
+      w.pair_bond[p] = -1;
+    }
+  } else {
+    w.edge_pair[e] = -1;
+    if (slot >= 0) w.dbrow[slot] = make_int2(-1, -1);
+  }
+}
+
 __device__ inline int warp_excl_scan(int v, int lane, int* total) {
   int x = v;
 #pragma unroll
@@ -207,35 +231,127 @@ __global__ void k_neighbors(XrWork w) {
             const uint32_t c = (uint32_t)code & ~(uint32_t)kHitBit;
             const bool half = c & XR_CODE_HALF, bond = c & XR_CODE_BOND;
             const int e = be + n_e + o_e + k_e++;
-            w.edge[e] = make_int2(j, (int)c);
-            int slot = -1;
-            if (bond) slot = bd + n_ba + o_ba + k_ba++;
-            w.edge_dbslot[e] = slot;
-            if (half) {
-              const int p = bp + n_h + o_h + k_h++;
-              w.edge_pair[e] = p;
-              w.pair_edge[p] = e;
-              w.pair_i[p] = i;
-              if (bond) {
-                const int b = bb + n_bh + o_bh + k_bh++;
-                w.pair_bond[p] = b;
-                w.bond_pair[b] = p;
-                w.bond_i[b] = i;
-                w.bond_j[b] = j;
-                w.dbrow[slot] = make_int2(b, 1);
-              } else {
-                w.pair_bond[p] = -1;
-              }
-            } else {
-              w.edge_pair[e] = -1;
-              if (bond) w.dbrow[slot] = make_int2(-1, -1);
-            }
+            const int slot = bond ? bd + n_ba + o_ba + k_ba++ : -1;
+            const int p = half ? bp + n_h + o_h + k_h++ : -1;
+            const int b = half && bond ? bb + n_bh + o_bh + k_bh++ : -1;
+            emit_edge(w, i, j, c, e, p, b, slot);
           }
     }
     n_e += t_e;
     n_h += t_h;
     n_bh += t_bh;
     n_ba += t_ba;
+  }
+  if (!FILL && lane == 0) {
+    w.cnt[0 * L + i] = n_e;
+    w.cnt[1 * L + i] = n_h;
+    w.cnt[2 * L + i] = n_bh;
+    w.cnt[3 * L + i] = n_ba;
+  }
+}
+
+// Candidate list: every image (j, S) within the descriptor's cutoff (the list cutoff rc + 2 skin,
+// from a second set of descriptors), in canonical order, without flags: one counter per atom
+// (FILL=false, into cand_cnt) or the rows (FILL=true, cand_edge = {j, shift bits}).
+template <bool FILL>
+__global__ void k_candidates(XrWork w) {
+  const int lane = threadIdx.x & 31;
+  const int i = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
+  if (i >= w.A) return;
+  const XrSystem& S = w.sys[w.sys_of[i]];
+  const float4 pi = w.xw[i], fi = w.fw[i];
+  const int4 wi = w.wrap[i];
+  const double4_32a xi = w.x[i];
+  const int r0 = S.reach[0], r1 = S.reach[1], r2 = S.reach[2];
+  const ScreenConsts K = screen_consts(S);
+  const int natoms = S.natoms, atom_off = S.atom_off;
+  const bool per0 = S.periodic[0] != 0, per1 = S.periodic[1] != 0, per2 = S.periodic[2] != 0;
+  int n_e = FILL ? w.cand_cnt[i] : 0;
+  for (int jb = 0; jb < natoms; jb += 32) {
+    const int jl = jb + lane;
+    const bool valid = jl < natoms;
+    const int j = atom_off + (valid ? jl : 0);
+    const float4 pj = w.xw[j], fj = w.fw[j];
+    const int4 wj = w.wrap[j];
+    const int b0 = per0 ? -__float2int_rn(fj.x - fi.x) : 0;
+    const int b1 = per1 ? -__float2int_rn(fj.y - fi.y) : 0;
+    const int b2 = per2 ? -__float2int_rn(fj.z - fi.z) : 0;
+    int c_e = 0;
+    if (valid)
+      for (int o0 = -r0; o0 <= r0; ++o0)
+        for (int o1 = -r1; o1 <= r1; ++o1)
+          for (int o2 = -r2; o2 <= r2; ++o2) c_e += classify(w, S, K, i, j, pi, pj, wi, wj, b0 + o0, b1 + o1, b2 + o2, xi) != 0;
+    int t_e, o_e = 0;
+    if (!FILL) {
+      t_e = __reduce_add_sync(0xffffffffu, c_e);
+    } else {
+      o_e = warp_excl_scan(c_e, lane, &t_e);
+      if (c_e) {
+        int k = n_e + o_e;
+        for (int o0 = -r0; o0 <= r0; ++o0)
+          for (int o1 = -r1; o1 <= r1; ++o1)
+            for (int o2 = -r2; o2 <= r2; ++o2) {
+              const int code = classify(w, S, K, i, j, pi, pj, wi, wj, b0 + o0, b1 + o1, b2 + o2, xi);
+              if (code) w.cand_edge[k++] = make_int2(j, (int)((uint32_t)code & XR_SHIFT_MASK));
+            }
+      }
+    }
+    n_e += t_e;
+  }
+  if (!FILL && lane == 0) w.cand_cnt[i] = n_e;
+}
+
+// The edges within the cutoff of a candidate list (rows of {j, shift bits} in canonical order, a
+// superset of the edges: a skin list of an earlier step, or a caller-supplied list), with their
+// flags, classified exactly as k_neighbors classifies an image. One warp per source atom, 32
+// candidates at a time; the kept candidates stay in row order, so the rows remain canonical.
+// FILL=false counts per atom as k_neighbors<false> does; FILL=true writes the rows.
+template <bool FILL>
+__global__ void k_filter(XrWork w) {
+  const int lane = threadIdx.x & 31;
+  const int i = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
+  if (i >= w.A) return;
+  const XrSystem& S = w.sys[w.sys_of[i]];
+  const float4 pi = w.xw[i];
+  const int4 wi = w.wrap[i];
+  const double4_32a xi = w.x[i];
+  const ScreenConsts K = screen_consts(S);
+  const int L = w.A + 1;
+  const int beg = w.cand_cnt[i], end = w.cand_cnt[i + 1];
+  int n_e = 0, n_h = 0, n_bh = 0, n_ba = 0;
+  if (FILL) {
+    n_e = w.cnt[0 * L + i];
+    n_h = w.cnt[1 * L + i];
+    n_bh = w.cnt[2 * L + i];
+    n_ba = w.cnt[3 * L + i];
+  }
+  const unsigned below = (1u << lane) - 1u;
+  for (int k0 = beg; k0 < end; k0 += 32) {
+    const int k = k0 + lane;
+    int code = 0, j = 0;
+    if (k < end) {
+      const int2 cand = w.cand_edge[k];
+      j = cand.x;
+      const uint32_t sh = (uint32_t)cand.y;
+      const int4 wj = w.wrap[j];
+      code = classify(w, S, K, i, j, pi, w.xw[j], wi, wj, xr_sx(sh) + wj.x - wi.x, xr_sy(sh) + wj.y - wi.y,
+                      xr_sz(sh) + wj.z - wi.z, xi);
+    }
+    const uint32_t c = (uint32_t)code & ~(uint32_t)kHitBit;
+    const bool hit = code != 0, half = hit && (c & XR_CODE_HALF), bond = hit && (c & XR_CODE_BOND);
+    const unsigned m_e = __ballot_sync(0xffffffffu, hit), m_h = __ballot_sync(0xffffffffu, half);
+    const unsigned m_bh = __ballot_sync(0xffffffffu, half && bond), m_ba = __ballot_sync(0xffffffffu, bond);
+    if (FILL && hit) {
+      const int e = n_e + __popc(m_e & below);
+      const int slot = bond ? n_ba + __popc(m_ba & below) : -1;
+      const int p = half ? n_h + __popc(m_h & below) : -1;
+      const int b = half && bond ? n_bh + __popc(m_bh & below) : -1;
+      emit_edge(w, i, j, c, e, p, b, slot);
+    }
+    n_e += __popc(m_e);
+    n_h += __popc(m_h);
+    n_bh += __popc(m_bh);
+    n_ba += __popc(m_ba);
   }
   if (!FILL && lane == 0) {
     w.cnt[0 * L + i] = n_e;
@@ -323,68 +439,109 @@ __device__ inline int block_excl_scan(int v, int* smem, int* total) {
   return r;
 }
 
-__global__ void k_scan_blocks(XrWork w, int* block_sums, int nblocks) {
+__global__ void k_scan_blocks(int* base, int L, int* block_sums, int nblocks) {
   __shared__ int smem[33];
-  const int k = blockIdx.y, L = w.A + 1;
-  int* a = w.cnt + (size_t)k * L;
-  const int base = blockIdx.x * kScanTile + threadIdx.x * kScanPer;
+  const int k = blockIdx.y;
+  int* a = base + (size_t)k * L;
+  const int first = blockIdx.x * kScanTile + threadIdx.x * kScanPer;
   int s = 0;
-  for (int t = 0; t < kScanPer; ++t) s += (base + t < L) ? a[base + t] : 0;
+  for (int t = 0; t < kScanPer; ++t) s += (first + t < L) ? a[first + t] : 0;
   int total;
   block_excl_scan(s, smem, &total);
   if (threadIdx.x == 0) block_sums[k * nblocks + blockIdx.x] = total;
 }
 
-__global__ void k_scan_sums(XrWork w, int* block_sums, int nblocks) {
+__global__ void k_scan_sums(int* block_sums, int nblocks, int* totals) {
   __shared__ int smem[33];
   const int k = blockIdx.x;
   int carry = 0;
-  for (int base = 0; base < nblocks; base += kScanThreads) {
-    const int idx = base + threadIdx.x;
+  for (int b0 = 0; b0 < nblocks; b0 += kScanThreads) {
+    const int idx = b0 + threadIdx.x;
     const int v = idx < nblocks ? block_sums[k * nblocks + idx] : 0;
     int total;
     const int ex = block_excl_scan(v, smem, &total);
     if (idx < nblocks) block_sums[k * nblocks + idx] = ex + carry;
     carry += total;
   }
-  if (threadIdx.x == 0) w.counts[k] = carry;
+  if (threadIdx.x == 0) totals[k] = carry;
 }
 
-__global__ void k_scan_apply(XrWork w, const int* block_sums, int nblocks) {
+__global__ void k_scan_apply(int* base, int L, const int* block_sums, int nblocks) {
   __shared__ int smem[33];
-  const int k = blockIdx.y, L = w.A + 1;
-  int* a = w.cnt + (size_t)k * L;
-  const int base = blockIdx.x * kScanTile + threadIdx.x * kScanPer;
+  const int k = blockIdx.y;
+  int* a = base + (size_t)k * L;
+  const int first = blockIdx.x * kScanTile + threadIdx.x * kScanPer;
   int v[kScanPer];
   int s = 0;
   for (int t = 0; t < kScanPer; ++t) {
-    v[t] = (base + t < L) ? a[base + t] : 0;
+    v[t] = (first + t < L) ? a[first + t] : 0;
     s += v[t];
   }
   int total;
   int ex = block_excl_scan(s, smem, &total) + block_sums[k * nblocks + blockIdx.x];
   for (int t = 0; t < kScanPer; ++t) {
-    if (base + t < L) a[base + t] = ex;
+    if (first + t < L) a[first + t] = ex;
     ex += v[t];
   }
 }
 
+// Exclusive scans in place of `narrays` arrays of length L laid out one after another (the last
+// slot of each holds 0 on entry and the total on exit); totals[k] receives each total. block_sums
+// needs narrays * ceil(L / kScanTile) ints.
+void scan_arrays(int* base, int L, int narrays, int* block_sums, int* totals, cudaStream_t st) {
+  const int nblocks = (L + kScanTile - 1) / kScanTile;
+  k_scan_blocks<<<dim3(nblocks, narrays), kScanThreads, 0, st>>>(base, L, block_sums, nblocks);
+  k_scan_sums<<<narrays, kScanThreads, 0, st>>>(block_sums, nblocks, totals);
+  k_scan_apply<<<dim3(nblocks, narrays), kScanThreads, 0, st>>>(base, L, block_sums, nblocks);
+}
+
 }  // namespace
 
-void xr_launch_topology(const XrWork& w, cudaStream_t st) {
-  k_prep<<<(w.A + 255) / 256, 256, 0, st>>>(w);
+void xr_launch_prep(const XrWork& w, cudaStream_t st) { k_prep<<<(w.A + 255) / 256, 256, 0, st>>>(w); }
+
+void xr_launch_count(const XrWork& w, cudaStream_t st) {
   const int warps_per_block = 8;
   k_neighbors<false><<<(w.A + warps_per_block - 1) / warps_per_block, 32 * warps_per_block, 0, st>>>(w);
 }
 
+void xr_launch_topology(const XrWork& w, cudaStream_t st) {
+  xr_launch_prep(w, st);
+  xr_launch_count(w, st);
+}
+
+void xr_launch_rows(const XrWork& w, cudaStream_t st) {
+  const int warps_per_block = 8;
+  k_neighbors<true><<<(w.A + warps_per_block - 1) / warps_per_block, 32 * warps_per_block, 0, st>>>(w);
+}
+
 // Needs w.red to hold at least 4 * ceil((A+1)/4096) ints.
 void xr_launch_scan(const XrWork& w, cudaStream_t st) {
-  const int L = w.A + 1;
-  const int nblocks = (L + kScanTile - 1) / kScanTile;
-  int* sums = reinterpret_cast<int*>(w.red);
-  k_scan_blocks<<<dim3(nblocks, 4), kScanThreads, 0, st>>>(w, sums, nblocks);
-  k_scan_sums<<<4, kScanThreads, 0, st>>>(w, sums, nblocks);
-  k_scan_apply<<<dim3(nblocks, 4), kScanThreads, 0, st>>>(w, sums, nblocks);
+  scan_arrays(w.cnt, w.A + 1, 4, reinterpret_cast<int*>(w.red), w.counts, st);
+}
+
+void xr_launch_candidates(const XrWork& w, bool fill, cudaStream_t st) {
+  const int warps_per_block = 8;
+  const int blocks = (w.A + warps_per_block - 1) / warps_per_block;
+  if (fill) {
+    k_candidates<true><<<blocks, 32 * warps_per_block, 0, st>>>(w);
+  } else {
+    k_candidates<false><<<blocks, 32 * warps_per_block, 0, st>>>(w);
+    scan_arrays(w.cand_cnt, w.A + 1, 1, reinterpret_cast<int*>(w.red), w.counts + 5, st);
+  }
+}
+
+void xr_launch_filter(const XrWork& w, bool fill, cudaStream_t st) {
+  const int warps_per_block = 8;
+  const int blocks = (w.A + warps_per_block - 1) / warps_per_block;
+  if (fill)
+    k_filter<true><<<blocks, 32 * warps_per_block, 0, st>>>(w);
+  else
+    k_filter<false><<<blocks, 32 * warps_per_block, 0, st>>>(w);
+}
+
+void xr_launch_reverse(const XrWork& w, cudaStream_t st) {
+  const int warps_per_block = 8;
+  k_reverse<<<(w.A + warps_per_block - 1) / warps_per_block, 32 * warps_per_block, 0, st>>>(w);
 }
 
 void xr_launch_topology_fill(const XrWork& w, cudaStream_t st) {
