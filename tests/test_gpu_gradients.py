@@ -3,7 +3,9 @@
 dE/dtheta for bond, angle and vdW parameters and the gradient of an energy + force squared-error
 loss are checked against central differences of the device energies with the parameter moved by
 +-h (relative h = 1e-6), on a water cluster and on the TiO2/water slab of the differentiation
-workload (ffield.reax.TiOH.Kim2013).
+workload (ffield.reax.TiOH.Kim2013), and against central differences of the CPU oracle's energies
+(the reference's algorithm restated and pinned to reference-written fixtures) under the same
+modified force field.
 """
 
 import numpy as np
@@ -137,3 +139,54 @@ def test_energy_force_loss_gradient():
 
         fd = (loss_of(make_ff(shifted(h))) - loss_of(make_ff(shifted(-h)))) / (2 * h)
         assert grad.pairs[s, t][name] == pytest.approx(fd, rel=1e-4, abs=1e-4 * max(1.0, abs(fd))), (s, t, name)
+
+
+def _oracle_fd(system, setter, h):
+    """Central difference of the oracle's energy with a force-field parameter moved by +-h."""
+    import oracle
+    from xreac_gb300 import ForceField
+
+    vals = []
+    for sgn in (1, -1):
+        ff = ForceField.bundled(system.force_field)
+        setter(ff, sgn * h)
+        vals.append(oracle.evaluate(ff, system.symbols, system.positions, cell=system.cell, pbc=system.pbc,
+                                    need_forces=False, dense_bond_orders=False)["energy"])
+    return (vals[0] - vals[1]) / (2 * h)
+
+
+ORACLE_PAIRS = [("O", "H", "De_s"), ("O", "H", "p_be1"), ("O", "H", "p_ovun1"), ("O", "H", "p_bo1"),
+                ("O", "H", "p_bo2"), ("O", "H", "r_s"), ("O", "H", "D"), ("O", "H", "alpha"), ("O", "H", "gamma_w"),
+                ("O", "O", "r_vdW"), ("O", "O", "p_bo3"), ("H", "H", "alpha")]
+
+
+@pytest.mark.parametrize("s,t,name", ORACLE_PAIRS)
+def test_pair_parameter_gradient_against_oracle(s, t, name):
+    """The device adjoint dE/dtheta against central differences of the oracle on 5 H2O (15 atoms)."""
+    from xreac_gb300 import Calculator, ForceField
+
+    system = _water(n_mol=5, seed=9)
+    ff = ForceField.bundled(system.force_field)
+    _, grad = Calculator(ff).parameter_gradient(system.symbols, system.positions)
+    base = ff.pairs[s, t][name]
+    h = 1e-6 * max(abs(base), 1e-3)
+    fd = _oracle_fd(system, _pair_setter(s, t, name, base), h)
+    assert grad.pairs[s, t][name] == pytest.approx(fd, rel=2e-5, abs=2e-6), (s, t, name)
+
+
+def test_angle_parameter_gradient_against_oracle():
+    from xreac_gb300 import Calculator, ForceField
+
+    system = _water(n_mol=5, seed=9)
+    ff = ForceField.bundled(system.force_field)
+    _, grad = Calculator(ff).parameter_gradient(system.symbols, system.positions)
+    key = ("H", "O", "H")
+    checked = 0
+    for k in range(7):
+        base = float(ff.angles[key][0][k])
+        if base == 0.0:
+            continue
+        fd = _oracle_fd(system, _angle_setter(key, 0, k, base), 1e-6 * abs(base))
+        assert grad.angles[key][0][k] == pytest.approx(fd, rel=2e-5, abs=2e-6), k
+        checked += 1
+    assert checked >= 4

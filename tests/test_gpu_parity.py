@@ -175,17 +175,60 @@ def test_full_size_properties(water_4608):
     np.testing.assert_allclose(p.forces, a.forces[order], atol=1e-8, rtol=0)
 
 
-def test_cho_mixture_full_size():
-    """The 3,300-atom C/H/O mixture: all terms active, momentum and charge conservation, FD check."""
-    from xreac_gb300 import workloads
+def test_cho_mixture_full_size_against_oracle():
+    """The 3,300-atom C/H/O mixture box (300 CH4, 300 O2, 300 H2O, 100 CO2 at 0.6 g/cm3, CHO.2008)
+    against the CPU oracle at the evaluation path's stated limits (energy 1e-8 relative, components
+    1e-9 per atom, forces 1e-6 kcal/mol/A, charges 1e-8 e, exact neighbour arrays); every term active."""
+    from oracle import evaluate as oracle_evaluate
+    from xreac_gb300 import ForceField, workloads
 
     s = workloads.cho_mixture()
     c = calc(s.force_field)
     r = c.evaluate(s.symbols, s.positions, cell=s.cell, pbc=s.pbc)
-    for k in ("angle", "torsion", "hydrogen_bond", "bond", "lone_pair", "atom", "vdw", "coulomb"):
+    o = oracle_evaluate(ForceField.bundled(s.force_field), s.symbols, s.positions, cell=s.cell, pbc=s.pbc,
+                        dense_bond_orders=False)
+    n = len(s.symbols)
+    assert n == 3300
+    assert abs(r.energy - o["energy"]) <= 1e-8 * abs(o["energy"])
+    comps = np.array([r.components[k] for k in COMP])
+    ocomps = np.array([o["components"][k] for k in COMP])
+    assert np.max(np.abs(comps - ocomps)) / n <= 1e-9
+    np.testing.assert_allclose(r.forces, o["forces"], atol=1e-6, rtol=0)
+    np.testing.assert_allclose(r.charges, o["charges"], atol=1e-8, rtol=0)
+    np.testing.assert_allclose(r.total_bond_orders, o["total_bond_orders"], atol=1e-10, rtol=0)
+    np.testing.assert_array_equal(r.bond_counts, o["bond_counts"])
+    i, j, S = c.neighbor_list()
+    oi, oj, oS = o["neighbors"]
+    np.testing.assert_array_equal(i, oi)
+    np.testing.assert_array_equal(j, oj)
+    np.testing.assert_array_equal(S, oS)
+    for k in ("angle", "torsion", "hydrogen_bond", "bond", "lone_pair", "atom", "vdw", "coulomb", "penalty",
+              "conjugation"):
         assert r.components[k] != 0.0, k
     assert abs(r.charges.sum()) < 1e-10
     np.testing.assert_allclose(r.forces.sum(axis=0), 0.0, atol=1e-7)
+
+
+def test_cho_mixture_charge_response_forces_by_finite_differences():
+    """Central differences of the device energy (charges re-solved at every point) against the
+    charge-response forces of the 3,300-atom box, on a C, an O and an H coordinate. h = 1e-4 A; the
+    difference's own error (h^2 times the third derivative, plus energy rounding over 2h) stays below
+    the 1e-4 kcal/mol/A allowed."""
+    from xreac_gb300 import workloads
+
+    s = workloads.cho_mixture()
+    c = calc(s.force_field)
+    full = c.evaluate(s.symbols, s.positions, cell=s.cell, pbc=s.pbc, full_derivative=True)
+    x = np.array(s.positions, dtype=float)
+    picks = [s.symbols.index("C"), s.symbols.index("O") + 1, s.symbols.index("H") + 2]
+    h = 1e-4
+    for a, d in zip(picks, (0, 1, 2)):
+        xp, xm = x.copy(), x.copy()
+        xp[a, d] += h
+        xm[a, d] -= h
+        fd = -(c.evaluate(s.symbols, xp, cell=s.cell, pbc=s.pbc).energy
+               - c.evaluate(s.symbols, xm, cell=s.cell, pbc=s.pbc).energy) / (2 * h)
+        assert abs(full.forces[a, d] - fd) < 1e-4, (a, d, full.forces[a, d], fd)
 
 
 def test_batch_matches_single_evaluations():

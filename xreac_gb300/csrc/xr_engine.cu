@@ -561,6 +561,10 @@ int status_to_code(xr_ctx* c, int st) {
 // scaled down when they do not fit; the other systems are taken, largest first, by whichever block
 // is free. A one-block team is no team: such a system joins the small ones.
 constexpr int kQeqSmall = 160;
+#ifndef XR_QEQ_TEAM_ROWS
+#define XR_QEQ_TEAM_ROWS 32
+#endif
+constexpr int kQeqTeamRows = XR_QEQ_TEAM_ROWS;  // rows per block of a grid-wide team (a multiple of 32)
 constexpr int kQeqBatchBlock = 1024;
 constexpr int kQeqBlocks = 2048;
 
@@ -576,10 +580,10 @@ void plan_qeq(xr_ctx* c, const xr_system* sys, int nsys, int* nblocks, int* ntea
                                                                  : std::min<int>((int)small.size(), std::max(1, budget / 4)));
     const int avail = budget - small_blocks;
     long long want = 0;
-    for (size_t k = 0; k < large.size(); ++k) want += (sys[large[k]].natoms + 31) / 32;
+    for (size_t k = 0; k < large.size(); ++k) want += (sys[large[k]].natoms + kQeqTeamRows - 1) / kQeqTeamRows;
     long long have = 0;
     for (size_t k = 0; k < large.size(); ++k) {
-      const long long d = (sys[large[k]].natoms + 31) / 32;
+      const long long d = (sys[large[k]].natoms + kQeqTeamRows - 1) / kQeqTeamRows;
       team[k] = (int)std::max<long long>(2, want > avail ? d * avail / std::max<long long>(want, 1) : d);
       have += team[k];
     }
