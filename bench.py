@@ -555,37 +555,33 @@ def water_box_numbers(lib, nat, local, steps, warmup):
 
 
 def differentiation_numbers(local, copies=256):
-    """The differentiation workload: per perturbed copy, the unperturbed reference (E, F), then the
-    E+F squared-error loss and its parameter gradient (three adjoint evaluations)."""
+    """The differentiation workload: per perturbed copy, the E+F squared-error loss against the
+    unperturbed force field's E, F and its parameter gradient (device adjoint). The copies' force
+    fields are parameter sets of one device force field, so the workload is three batched device
+    calls: the reference E, F of every copy, the copies at x with a gradient per system, and the
+    copies at x +- h v (the force term's central difference)."""
     import torch
     from xreac_gb300 import Calculator, ForceField, workloads
-    from xreac_gb300.differentiation import energy_force_loss
+    from xreac_gb300.differentiation import perturbed_copies_loss
 
-    ref_calc = Calculator(ForceField.bundled("ffield.reax.TiOH.Kim2013"), device=local)
-    gen = workloads.perturbed_copies(n_copies=copies)
-    first = next(gen)
-    ref = ref_calc.evaluate(first[0].symbols, first[0].positions, cell=first[0].cell, pbc=first[0].pbc)
-    energy_force_loss(Calculator(first[1], device=local), first[0].symbols, first[0].positions, ref.energy,
-                      ref.forces, cell=first[0].cell, pbc=first[0].pbc)
+    base = ForceField.bundled("ffield.reax.TiOH.Kim2013")
+    pairs = list(workloads.perturbed_copies(n_copies=copies))
+    calc = Calculator(base, device=local)
+    perturbed_copies_loss(pairs, base, calculator=calc)  # warm-up: context, buffers, parameter sets
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    n = 0
-    losses = []
-    for system, ff in workloads.perturbed_copies(n_copies=copies):
-        ref = ref_calc.evaluate(system.symbols, system.positions, cell=system.cell, pbc=system.pbc)
-        loss, grad, _ = energy_force_loss(Calculator(ff, device=local), system.symbols, system.positions, ref.energy,
-                                          ref.forces, cell=system.cell, pbc=system.pbc)
-        losses.append(loss)
-        n += 1
+    out = perturbed_copies_loss(pairs, base, calculator=calc)
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
+    n = len(out.losses)
     return {"workload": f"{copies} perturbed copies of the anatase TiO2 4x4x1 slab + 32 H2O (288 atoms), "
                         "ffield.reax.TiOH.Kim2013, +-2% bond/angle/vdW parameters, 0.05 A displacements",
             "copies": n, "seconds": wall, "ms_per_copy": 1e3 * wall / n,
             "evaluations_per_copy": 4, "atoms_evals_per_s": 4 * 288 * n / wall,
-            "mean_loss": float(np.mean(losses)),
-            "note": "per copy: force-field upload, reference E+F, loss gradient by the device adjoint plus a "
-                    "positional central difference of it (force term)"}
+            "mean_loss": float(np.mean(out.losses)), "parameters": len(out.vector),
+            "note": "each copy's force field is a parameter set of one device force field; three batched calls: "
+                    "reference E+F of all copies, the copies at x with per-system parameter gradients, the copies "
+                    "at x +- h v (force term's central difference) with per-system gradients"}
 
 
 # Server shape: six worker contexts keep enough batches in flight to fill the GPU (measured on one GB300:

@@ -98,6 +98,36 @@ int xr_ff_create(const double* general, int ntypes, const double* atom, const do
                  xr_ff** out);
 void xr_ff_destroy(xr_ff* ff);
 
+/* Replace the parameter values of a force field in place (no reference counterpart; the reference
+ * rebuilds its per-edge parameter arrays on every evaluation): the same table shapes as at
+ * xr_ff_create (ntypes, angle, torsion and hydrogen-bond record counts), new values; one host-to-
+ * device copy, no allocation. No evaluation that uses this force field may be in flight. For
+ * parameter fitting and perturbation studies that evaluate many variants of one force field. */
+int xr_ff_update(xr_ff* ff, const double* general, const double* atom, const double* pair, const int* is_carbon,
+                 int vdw_type, const int* angle_index, const double* angle, const int* torsion_index,
+                 const double* torsion, const int* hbond_index, const double* hbond);
+
+/* Parameter sets (no reference counterpart; the reference evaluates one force field per call).
+ * A force field can hold nsets variants of its parameters, each with the elements and records of
+ * xr_ff_create: the general parameters and the angle / torsion / hydrogen-bond index tables are
+ * shared, while the atom, pair, angle, torsion and hydrogen-bond values (and the tables derived
+ * from them) are per set. xr_eval_batch_sets then evaluates every system with its own set, so many
+ * perturbed or fitted copies of a force field run in one batch. Set 0 is the force field of
+ * xr_ff_create / xr_ff_update; xr_ff_update returns the force field to that single set.
+ *
+ * xr_ff_set_count: resize to nsets (1 <= nsets <= XR_MAX_PARAMETER_SETS); sets kept keep their
+ * values, new ones start as copies of set 0. Reallocates the device tables: no evaluation that uses
+ * this force field may be in flight.
+ * xr_ff_update_sets: values of sets first .. first + count - 1, one host-to-device copy. Each table
+ * pointer is NULL (every one of these sets takes set 0's values) or holds count consecutive tables of
+ * the xr_ff_create shapes: atom count x ntypes x 24, pair count x ntypes^2 x 28, angle count x
+ * nangle x 7, torsion count x ntorsion x 5, hbond count x nhbond x 4. */
+#define XR_MAX_PARAMETER_SETS 65536
+int xr_ff_set_count(xr_ff* ff, int nsets);
+int xr_ff_set_count_of(const xr_ff* ff);
+int xr_ff_update_sets(xr_ff* ff, int first, int count, const double* atom, const double* pair, const double* angle,
+                      const double* torsion, const double* hbond);
+
 /* Context: device work buffers (grown on demand, reused across calls) and a CUDA stream.
  * stream may be NULL (the context creates its own) or a cudaStream_t owned by the caller.
  * A context is used by one host thread at a time. */
@@ -156,6 +186,11 @@ int xr_last_list_info(const xr_ctx* ctx, int* mode, long long* builds);
 /* Evaluate nsys independent systems in one ragged batch with per-system offsets. */
 int xr_eval_batch(xr_ctx* ctx, const xr_ff* ff, int nsys, const xr_system* sys, unsigned flags, xr_result* out);
 
+/* As xr_eval_batch, system s evaluated with parameter set sets[s] of ff (0 <= sets[s] < the set
+ * count). With XR_FLAG_PARAM_GRADIENT each system's gradient is with respect to its own set. */
+int xr_eval_batch_sets(xr_ctx* ctx, const xr_ff* ff, int nsys, const xr_system* sys, const int* sets, unsigned flags,
+                       xr_result* out);
+
 /* Neighbour list of the last evaluation of system `index` of the last batch, in canonical
  * (i, j, Sx, Sy, Sz) order: i, j (capacity entries each), S (capacity x 3). *count receives the
  * number of directed edges; nothing is written when capacity is too small. Host pointers. */
@@ -177,6 +212,16 @@ int xr_get_bonds(xr_ctx* ctx, int index, int* i, int* j, int* S, double* bo, lon
  * depend on these parameters, so this is the total derivative. npair = ntypes^2 * 28 and
  * nangle = 7 * (angle records) must match. */
 int xr_get_param_gradient(const xr_ctx* ctx, double* pair_grad, long long npair, double* angle_grad, long long nangle);
+
+/* As xr_get_param_gradient for the energy of system `index` of that call alone (index -1: the sum
+ * over its systems, which is xr_get_param_gradient). Every system of a call keeps its own gradient,
+ * so several evaluations (e.g. the displaced geometries of a finite difference) share one call. */
+int xr_get_param_gradient_system(const xr_ctx* ctx, int index, double* pair_grad, long long npair, double* angle_grad,
+                                 long long nangle);
+
+/* Every system's gradient block of that call at once: out[s * (npair + nangle) + k], the pair
+ * columns (k < npair) then the angle records, for s in call order; count = systems x (npair + nangle). */
+int xr_get_param_gradient_blocks(const xr_ctx* ctx, double* out, long long count);
 
 /* Number of CUDA kernels the last xr_eval / xr_eval_batch call launched. */
 long long xr_last_launches(const xr_ctx* ctx);

@@ -35,6 +35,10 @@ XR_FLAG_PARAM_GRADIENT = 4
 EXPORTED = (
     "xr_ff_create",
     "xr_ff_destroy",
+    "xr_ff_update",
+    "xr_ff_set_count",
+    "xr_ff_set_count_of",
+    "xr_ff_update_sets",
     "xr_ctx_create",
     "xr_ctx_destroy",
     "xr_last_error",
@@ -43,6 +47,7 @@ EXPORTED = (
     "xr_ctx_set_wait_test",
     "xr_eval",
     "xr_eval_batch",
+    "xr_eval_batch_sets",
     "xr_eval_neighbors",
     "xr_neighbors_check",
     "xr_ctx_set_skin",
@@ -57,11 +62,14 @@ EXPORTED = (
     "xr_last_qeq_iterations",
     "xr_last_qeq_work",
     "xr_get_param_gradient",
+    "xr_get_param_gradient_system",
+    "xr_get_param_gradient_blocks",
     "xr_count_neighbors_static",
     "xr_static_last_error",
 )
 
 XR_STATIC_MAX_ATOMS = 16384
+XR_MAX_PARAMETER_SETS = 65536
 
 
 # Pointer members are declared as void* (the C layout is the same); assign addresses with addr().
@@ -117,6 +125,18 @@ def load():
         POINTER(c_int), POINTER(c_double), c_int, POINTER(c_void_p),
     ]
     lib.xr_ff_create.restype = c_int
+    lib.xr_ff_update.argtypes = [
+        c_void_p, POINTER(c_double), POINTER(c_double), POINTER(c_double), POINTER(c_int), c_int, POINTER(c_int),
+        POINTER(c_double), POINTER(c_int), POINTER(c_double), POINTER(c_int), POINTER(c_double),
+    ]
+    lib.xr_ff_update.restype = c_int
+    lib.xr_ff_set_count.argtypes = [c_void_p, c_int]
+    lib.xr_ff_set_count.restype = c_int
+    lib.xr_ff_set_count_of.argtypes = [c_void_p]
+    lib.xr_ff_set_count_of.restype = c_int
+    lib.xr_ff_update_sets.argtypes = [c_void_p, c_int, c_int, POINTER(c_double), POINTER(c_double), POINTER(c_double),
+                                      POINTER(c_double), POINTER(c_double)]
+    lib.xr_ff_update_sets.restype = c_int
     lib.xr_ff_destroy.argtypes = [c_void_p]
     lib.xr_ff_destroy.restype = None
     lib.xr_ctx_create.argtypes = [c_int, c_void_p, POINTER(c_void_p)]
@@ -135,6 +155,9 @@ def load():
     lib.xr_eval.restype = c_int
     lib.xr_eval_batch.argtypes = [c_void_p, c_void_p, c_int, POINTER(System), c_uint, POINTER(Result)]
     lib.xr_eval_batch.restype = c_int
+    lib.xr_eval_batch_sets.argtypes = [c_void_p, c_void_p, c_int, POINTER(System), POINTER(c_int), c_uint,
+                                       POINTER(Result)]
+    lib.xr_eval_batch_sets.restype = c_int
     lib.xr_eval_neighbors.argtypes = [c_void_p, c_void_p, POINTER(System), POINTER(Neighbors), c_uint, POINTER(Result)]
     lib.xr_eval_neighbors.restype = c_int
     lib.xr_neighbors_check.argtypes = [c_int, POINTER(c_int), POINTER(Neighbors), c_char_p, c_int]
@@ -165,6 +188,11 @@ def load():
     lib.xr_last_qeq_work.restype = c_int
     lib.xr_get_param_gradient.argtypes = [c_void_p, POINTER(c_double), c_longlong, POINTER(c_double), c_longlong]
     lib.xr_get_param_gradient.restype = c_int
+    lib.xr_get_param_gradient_system.argtypes = [c_void_p, c_int, POINTER(c_double), c_longlong, POINTER(c_double),
+                                                 c_longlong]
+    lib.xr_get_param_gradient_system.restype = c_int
+    lib.xr_get_param_gradient_blocks.argtypes = [c_void_p, POINTER(c_double), c_longlong]
+    lib.xr_get_param_gradient_blocks.restype = c_int
     lib.xr_count_neighbors_static.argtypes = [POINTER(System), c_double, c_void_p, POINTER(c_int), POINTER(c_longlong)]
     lib.xr_count_neighbors_static.restype = c_int
     lib.xr_static_last_error.argtypes = []
@@ -216,6 +244,59 @@ class ForceFieldHandle:
         if code != XR_OK:
             raise RuntimeError(f"xr_ff_create failed with code {code}")
         self.handle = handle
+        self._shape = {k: v.shape for k, v in keep.items()}
+        self.nsets = 1
+
+    def update(self, tables, is_carbon, vdw_type):
+        """New values for the same table shapes (``xr_ff_update``), written into the device tables."""
+        t = tables
+        keep = dict(
+            general=np.ascontiguousarray(t["general"], dtype=np.float64),
+            atom=np.ascontiguousarray(t["atom"], dtype=np.float64),
+            pair=np.ascontiguousarray(t["pair"], dtype=np.float64),
+            is_carbon=np.ascontiguousarray(is_carbon, dtype=np.int32),
+            angle_index=np.ascontiguousarray(t["angle_index"], dtype=np.int32),
+            angle=np.ascontiguousarray(t["angle"], dtype=np.float64),
+            torsion_index=np.ascontiguousarray(t["torsion_index"], dtype=np.int32),
+            torsion=np.ascontiguousarray(t["torsion"], dtype=np.float64),
+            hbond_index=np.ascontiguousarray(t["hbond_index"], dtype=np.int32),
+            hbond=np.ascontiguousarray(t["hbond"], dtype=np.float64),
+        )
+        if {k: v.shape for k, v in keep.items()} != self._shape:
+            raise ValueError("an updated force field must have the same elements and parameter records")
+        code = self._lib.xr_ff_update(
+            self.handle, ptr(keep["general"], c_double), ptr(keep["atom"], c_double), ptr(keep["pair"], c_double),
+            ptr(keep["is_carbon"], c_int), int(vdw_type), ptr(keep["angle_index"], c_int), ptr(keep["angle"], c_double),
+            ptr(keep["torsion_index"], c_int), ptr(keep["torsion"], c_double), ptr(keep["hbond_index"], c_int),
+            ptr(keep["hbond"], c_double))
+        if code != XR_OK:
+            raise RuntimeError(f"xr_ff_update failed with code {code}")
+        self.nsets = 1
+
+    def set_count(self, nsets):
+        """Resize to ``nsets`` parameter sets (``xr_ff_set_count``); new sets start as set 0."""
+        code = self._lib.xr_ff_set_count(self.handle, int(nsets))
+        if code != XR_OK:
+            raise (ValueError if code == XR_EINPUT else RuntimeError)(f"xr_ff_set_count failed with code {code}")
+        self.nsets = int(nsets)
+
+    def update_sets(self, first, count, atom=None, pair=None, angle=None, torsion=None, hbond=None):
+        """Values of sets ``first .. first + count - 1`` (``xr_ff_update_sets``): each table None (set
+        0's values) or ``count`` stacked tables of the force field's shapes."""
+        keep = {}
+        for name, a in (("atom", atom), ("pair", pair), ("angle", angle), ("torsion", torsion), ("hbond", hbond)):
+            if a is None:
+                keep[name] = None
+                continue
+            a = np.ascontiguousarray(a, dtype=np.float64)
+            if a.shape != (int(count),) + self._shape[name]:
+                raise ValueError(f"{name} tables of the parameter sets must have shape (count,) + {self._shape[name]}")
+            keep[name] = a
+        code = self._lib.xr_ff_update_sets(self.handle, int(first), int(count), ptr(keep["atom"], c_double),
+                                           ptr(keep["pair"], c_double), ptr(keep["angle"], c_double),
+                                           ptr(keep["torsion"], c_double), ptr(keep["hbond"], c_double))
+        if code != XR_OK:
+            raise (ValueError if code == XR_EINPUT else RuntimeError)(f"xr_ff_update_sets failed with code {code}")
 
     def __del__(self):
         h = getattr(self, "handle", None)

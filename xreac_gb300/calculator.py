@@ -252,6 +252,86 @@ class Calculator:
         except (ValueError, KeyError):
             self._all_valid = False
 
+    def update_force_field(self, force_field):
+        """Evaluate with another parameter set of the same force field from now on (an extension).
+
+        ``force_field`` must have the same elements and parameter records as the current one
+        (e.g. a copy with perturbed or fitted values); its tables are written into the device
+        tables in place (``xr_ff_update``), so the device context, its buffers and any kept
+        neighbour list stay as they are.
+        """
+        if tuple(force_field.elements) != tuple(self.force_field.elements):
+            raise ValueError("an updated force field must have the same elements and parameter records")
+        force_field.validate_model()
+        if force_field.angle_row_keys() != self._angle_rows:
+            raise ValueError("an updated force field must have the same elements and parameter records")
+        self._ff.update(force_field.tables(), _is_carbon(force_field), force_field.vdw_type)
+        self.force_field = force_field
+        self._base_tables = None
+
+    # ------------------------------------------------------------------ parameter sets
+    @property
+    def parameter_set_count(self):
+        """Parameter sets on the device: 1 (the calculator's force field) plus those loaded."""
+        return self._ff.nsets
+
+    def _tables0(self):
+        t = getattr(self, "_base_tables", None)
+        if t is None:
+            t = self._base_tables = self.force_field.tables()
+        return t
+
+    def load_parameter_sets(self, force_fields):
+        """Load variants of the force field as parameter sets 1 .. len(force_fields) (an extension;
+        xreac evaluates one force field per call). Each must have the calculator's elements, general
+        parameters and parameter records; its atom, pair, angle, torsion and hydrogen-bond values
+        may differ. Set 0 stays the calculator's own force field. ``evaluate_many`` and
+        ``parameter_gradient_many`` then take ``parameter_sets=[...]``, one set per system, and
+        evaluate every system with its own set in one device batch."""
+        force_fields = list(force_fields)
+        base = self._tables0()
+        stacks = {k: [] for k in ("atom", "pair", "angle", "torsion", "hbond")}
+        for ff in force_fields:
+            if tuple(ff.elements) != tuple(self.force_field.elements):
+                raise ValueError("parameter sets must have the calculator's elements and parameter records")
+            ff.validate_model()
+            t = ff.tables()
+            if not np.array_equal(np.asarray(t["general"]), np.asarray(base["general"])):
+                raise ValueError("parameter sets share the general parameters of the calculator's force field")
+            for k in ("angle_index", "torsion_index", "hbond_index"):
+                if not np.array_equal(t[k], base[k]):
+                    raise ValueError("parameter sets must have the calculator's elements and parameter records")
+            for k in stacks:
+                stacks[k].append(t[k])
+        self.load_parameter_tables(**{k: (np.stack(v) if v else None) for k, v in stacks.items()},
+                                   count=len(force_fields))
+
+    def load_parameter_tables(self, atom=None, pair=None, angle=None, torsion=None, hbond=None, *, count=None):
+        """``load_parameter_sets`` from stacked tables: each argument None (every set takes the
+        calculator's own values for it) or an array of ``count`` tables in the shapes of
+        ``ForceField.tables()``; the values are used as given. Replaces any sets loaded before."""
+        given = [a for a in (atom, pair, angle, torsion, hbond) if a is not None]
+        if count is None:
+            if not given:
+                raise ValueError("the number of parameter sets is required when no table is given")
+            count = len(given[0])
+        count = int(count)
+        if count < 0 or count + 1 > nat.XR_MAX_PARAMETER_SETS:
+            raise ValueError(f"between 0 and {nat.XR_MAX_PARAMETER_SETS - 1} parameter sets can be loaded")
+        self._ff.set_count(count + 1)
+        if count:
+            self._ff.update_sets(1, count, atom=atom, pair=pair, angle=angle, torsion=torsion, hbond=hbond)
+
+    def _sets(self, parameter_sets, n_sys):
+        if parameter_sets is None:
+            return None
+        sets = np.ascontiguousarray(parameter_sets, dtype=np.int32)
+        if sets.shape != (n_sys,):
+            raise ValueError("parameter_sets must give one parameter set per system")
+        if len(sets) and (sets.min() < 0 or sets.max() >= self._ff.nsets):
+            raise ValueError("parameter set index out of range")
+        return sets
+
     def set_qeq(self, tolerance=1e-13, max_iterations=2000):
         """QEq solver tolerance and iteration limit.
 
@@ -401,50 +481,75 @@ class Calculator:
                                                            full_derivative, replicate=False)
         return self._run([(types, x, flags, cellm, float(total_charge), None)], full_derivative, [(1, 1, 1)], "ase")[0]
 
-    def parameter_gradient(self, symbols, positions, *, total_charge=0, cell=None, pbc=None, initial_charges=None):
+    def parameter_gradient(self, symbols, positions, *, total_charge=0, cell=None, pbc=None, initial_charges=None,
+                           full_derivative=False):
         """Energy, forces and dE/dtheta for the bond, angle and vdW parameters (an extension; xreac
         has no parameter derivatives). Returns ``(Evaluation, ParameterGradient)``.
 
         The gradient comes from the same hand-written adjoint as the forces: each energy kernel adds
         its parameter sensitivities, the bond-order parameters get theirs through the bond-order
         chain's adjoints. Charges do not depend on these parameters, so it is the total derivative.
+        ``full_derivative`` selects the charge-response forces, as in :meth:`evaluate`.
         """
         return self.parameter_gradient_many([dict(symbols=symbols, positions=positions, total_charge=total_charge,
-                                                  cell=cell, pbc=pbc, initial_charges=initial_charges)])
+                                                  cell=cell, pbc=pbc, initial_charges=initial_charges)],
+                                            full_derivative=full_derivative)
 
-    def parameter_gradient_many(self, systems):
-        """As :meth:`parameter_gradient` for a batch: a list of evaluations and the gradient of their
-        summed energy."""
+    def parameter_gradient_many(self, systems, *, per_system=False, full_derivative=False, parameter_sets=None,
+                                raw=False):
+        """As :meth:`parameter_gradient` for a batch, in one device call: the evaluations, and the
+        gradient of their summed energy, or (``per_system``) one gradient per system. With
+        ``parameter_sets`` (see :meth:`load_parameter_sets`) system k is evaluated with set
+        ``parameter_sets[k]`` and its gradient is with respect to that set. ``raw`` returns the
+        gradients as table rows instead: ``(evaluations, pair (S, T*T, 28), angle (S, R, 7))``, one
+        block per system, each row the derivative with respect to that table entry."""
+        sets = self._sets(parameter_sets, len(systems))
         results = self._evaluate_items([(s["symbols"], s["positions"], s.get("total_charge", 0), s.get("cell"),
-                                         s.get("pbc"), s.get("initial_charges")) for s in systems], False,
-                                       nat.XR_FLAG_PARAM_GRADIENT)
+                                         s.get("pbc"), s.get("initial_charges")) for s in systems], full_derivative,
+                                       nat.XR_FLAG_PARAM_GRADIENT, sets)
         T = len(self.force_field.elements)
-        pair = np.zeros(T * T * 28)
-        angle = np.zeros(7 * len(self._angle_rows))
-        code = self._lib.xr_get_param_gradient(self._ctx.handle, nat.ptr(pair, nat.c_double), len(pair),
-                                               nat.ptr(angle, nat.c_double) if len(angle) else None, len(angle))
-        if code != nat.XR_OK:
-            raise RuntimeError("parameter gradient unavailable")
-        grad = ParameterGradient.from_rows(self.force_field, pair.reshape(T * T, 28), angle.reshape(-1, 7),
-                                           self._angle_rows)
-        return (results[0] if len(systems) == 1 else results), grad
+        if raw:
+            np_, na = T * T * 28, 7 * len(self._angle_rows)
+            blocks = np.empty((len(systems), np_ + na))
+            code = self._lib.xr_get_param_gradient_blocks(self._ctx.handle, nat.ptr(blocks, nat.c_double), blocks.size)
+            if code != nat.XR_OK:
+                raise RuntimeError("parameter gradient unavailable")
+            return results, blocks[:, :np_].reshape(-1, T * T, 28), blocks[:, np_:].reshape(-1, na // 7, 7)
+        grads = []
+        for index in (range(len(systems)) if per_system else (-1,)):
+            pair = np.zeros(T * T * 28)
+            angle = np.zeros(7 * len(self._angle_rows))
+            code = self._lib.xr_get_param_gradient_system(self._ctx.handle, index, nat.ptr(pair, nat.c_double),
+                                                          len(pair), nat.ptr(angle, nat.c_double) if len(angle) else None,
+                                                          len(angle))
+            if code != nat.XR_OK:
+                raise RuntimeError("parameter gradient unavailable")
+            grads.append(ParameterGradient.from_rows(self.force_field, pair.reshape(T * T, 28), angle.reshape(-1, 7),
+                                                     self._angle_rows))
+        if per_system:
+            return results, grads
+        return (results[0] if len(systems) == 1 else results), grads[0]
 
-    def evaluate_many(self, systems, *, full_derivative=False):
+    def evaluate_many(self, systems, *, full_derivative=False, parameter_sets=None):
         """Evaluate independent systems in one ragged device batch.
 
         ``systems`` is a sequence of dicts with the keyword arguments of :meth:`evaluate`
         (``symbols``, ``positions`` and optionally ``total_charge``, ``cell``, ``pbc``,
         ``initial_charges``). Returns a list of :class:`Evaluation` in the same order.
+        ``parameter_sets`` (an extension): one parameter set per system, see
+        :meth:`load_parameter_sets`.
         """
+        sets = self._sets(parameter_sets, len(systems))
         return self._evaluate_items([(s["symbols"], s["positions"], s.get("total_charge", 0), s.get("cell"),
-                                      s.get("pbc"), s.get("initial_charges")) for s in systems], full_derivative)
+                                      s.get("pbc"), s.get("initial_charges")) for s in systems], full_derivative,
+                                    0, sets)
 
-    def _evaluate_items(self, items, full_derivative=False, extra_flags=0):
+    def _evaluate_items(self, items, full_derivative=False, extra_flags=0, sets=None):
         """``evaluate_many`` on tuples (symbols, positions, total_charge, cell, pbc, initial_charges)."""
         if _host is not None and self._all_valid and type(items) is list and items:
             packed = self._pack(items, full_derivative)
             if packed is not None:
-                return self._run_packed(*packed, full_derivative, "replicated", extra_flags)
+                return self._run_packed(*packed, full_derivative, "replicated", extra_flags, sets=sets)
         batch, reps = [], []
         prepare = self._prepare
         for symbols, positions, total_charge, cell, pbc, initial in items:
@@ -452,7 +557,7 @@ class Calculator:
             guess = None if initial is None else _guess(initial, len(sym))
             batch.append((types, x, flags, cellm, float(total_charge), guess))
             reps.append(rp)
-        return self._run(batch, full_derivative, reps, "replicated", extra_flags)
+        return self._run(batch, full_derivative, reps, "replicated", extra_flags, sets=sets)
 
     def _pack(self, items, full_derivative):
         """The batch's types and positions packed by the host module (one C pass over the requests);
@@ -511,7 +616,7 @@ class Calculator:
         charges = [float(it[2]) for it in items]
         return types, x, offsets, flags_l, cells, charges, _GuessAddresses(guess_addr, keep), reps
 
-    def _run(self, batch, full_derivative, reps, backend, extra_flags=0, supplied=None):
+    def _run(self, batch, full_derivative, reps, backend, extra_flags=0, supplied=None, sets=None):
         """One ``xr_eval_batch`` call over ``batch`` = [(types, positions, pbc flags, cell, total
         charge, initial charges)]: the inputs are packed into one array per kind, then as
         ``_run_packed`` (``xr_eval_neighbors`` with a supplied list for a single system)."""
@@ -523,10 +628,10 @@ class Calculator:
         types = np.concatenate(types_l) if n_sys > 1 else types_l[0]
         x = np.concatenate(xs) if n_sys > 1 else xs[0]
         return self._run_packed(types, x, offsets, flags_l, cells, charges, guesses, reps, full_derivative, backend,
-                                extra_flags, supplied)
+                                extra_flags, supplied, sets)
 
     def _run_packed(self, types, x, offsets, flags_l, cells, charges, guesses, reps, full_derivative, backend,
-                    extra_flags=0, supplied=None):
+                    extra_flags=0, supplied=None, sets=None):
         """One ``xr_eval_batch`` call: the per-system descriptors are filled column-wise over the
         packed types and positions, so the host cost per system is a handful of numpy operations;
         each ``Evaluation`` gets views of the batch's result arrays."""
@@ -575,6 +680,9 @@ class Calculator:
         if supplied is not None:
             code = lib.xr_eval_neighbors(self._ctx.handle, self._ff.handle, sys_arr.ctypes.data_as(_SYSTEM_P),
                                          nat.byref(supplied), flags_, res_arr.ctypes.data_as(_RESULT_P))
+        elif sets is not None:
+            code = lib.xr_eval_batch_sets(self._ctx.handle, self._ff.handle, n_sys, sys_arr.ctypes.data_as(_SYSTEM_P),
+                                          nat.ptr(sets, nat.c_int), flags_, res_arr.ctypes.data_as(_RESULT_P))
         else:
             code = lib.xr_eval_batch(self._ctx.handle, self._ff.handle, n_sys, sys_arr.ctypes.data_as(_SYSTEM_P),
                                      flags_, res_arr.ctypes.data_as(_RESULT_P))

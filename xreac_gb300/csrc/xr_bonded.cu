@@ -65,12 +65,13 @@ __device__ inline uint32_t bond_shift(const XrWork& w, int b, int dir) {
 // ------------------------------------------------------------------ uncorrected bond orders
 // sigma' = (1+cut) exp(p_bo1 (r/r_s)^p_bo2), pi' = exp(p_bo3 (r/r_p)^p_bo4), pp' likewise;
 // raw = sum; active when raw >= cut; bo0 = raw - cut (src/xreac/energy.py:130-149).
-__global__ void k_bo1(XrWork w, XrFF ff) {
+__global__ void k_bo1(XrWork w, XrFF ff0) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   bool mask = false;
   if (b < w.nB) {
     const int i = w.bond_i[b], j = w.bond_j[b];
+    const XrFF ff = xr_ff_of(ff0, w, i);
     const uint32_t code = (uint32_t)w.edge[w.pair_edge[w.bond_pair[b]]].y;
     const XrSystem& S = w.sys[w.sys_of[i]];
     const int sx = xr_sx(code), sy = xr_sy(code), sz = xr_sz(code);
@@ -172,8 +173,9 @@ __global__ void k_deltap(XrWork w) {
 }
 
 // Corrected bond orders (src/xreac/energy.py:150-165).
-__device__ inline void k_bo2_one(const XrWork& w, const XrFF& ff, int b) {
+__device__ inline void k_bo2_one(const XrWork& w, const XrFF& ff0, int b) {
   const int i = w.bond_i[b], j = w.bond_j[b];
+  const XrFF ff = xr_ff_of(ff0, w, i);
   const int ti = w.type[i], tj = w.type[j], T = ff.ntypes, pt = ti * T + tj;
   const double* g = ff.g;
   const double bo0 = BFV(BF_BO0, b), pi0 = BFV(BF_PI0, b), pp0 = BFV(BF_PP0, b);
@@ -227,9 +229,10 @@ __global__ void k_bo2(XrWork w, XrFF ff) {
 
 // Per-atom sums of corrected bond orders and the lone-pair quantities
 // (src/xreac/energy.py:185-199, 295-296).
-__global__ void k_atom1(XrWork w, XrFF ff) {
+__global__ void k_atom1(XrWork w, XrFF ff0) {
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= w.A) return;
+  const XrFF ff = xr_ff_of(ff0, w, a);
   const int L = w.A + 1, T = ff.ntypes, ta = w.type[a];
   const double* g = ff.g;
   double total = 0, sumpi = 0, prodsum = 0, ov1 = 0, n30 = 0;
@@ -288,9 +291,10 @@ __device__ inline double dsbo2_of(double sbo, double p) {
 }
 
 // Over/under-coordination and sbo (src/xreac/energy.py:201-212, 295-301), with their local adjoints.
-__global__ void k_atom2(XrWork w, XrFF ff) {
+__global__ void k_atom2(XrWork w, XrFF ff0) {
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= w.A) return;
+  const XrFF ff = xr_ff_of(ff0, w, a);
   const int L = w.A + 1, ta = w.type[a];
   const double* g = ff.g;
   const double dfvl = atom_prm(ff, ta, A_MASS) <= 21 ? 1.0 : 0.0;
@@ -335,8 +339,9 @@ __global__ void k_atom2(XrWork w, XrFF ff) {
 
 // Bond energy, C2 correction and triple-bond stabilisation, per half bond
 // (src/xreac/energy.py:194-198, 231-246).
-__device__ inline void k_bond_energy_one(const XrWork& w, const XrFF& ff, int b) {
+__device__ inline void k_bond_energy_one(const XrWork& w, const XrFF& ff0, int b) {
   const int i = w.bond_i[b], j = w.bond_j[b];
+  const XrFF ff = xr_ff_of(ff0, w, i);
   const int ti = w.type[i], tj = w.type[j], T = ff.ntypes, pt = ti * T + tj;
   const double* g = ff.g;
   const double bo = BFV(BF_BO, b), pi = BFV(BF_PI, b), pp = BFV(BF_PP, b), sig = BFV(BF_SIG, b);
@@ -347,7 +352,7 @@ __device__ inline void k_bond_energy_one(const XrWork& w, const XrFF& ff, int b)
   double e_bond = -(Des * sig * ex + Dep * pi + Depp * pp);
   BJV(BJ_SIG, b) = -Des * ex * (1.0 - be1 * be2 * powv);
   if (w.pgrad) {  // dE/d(De_s, De_p, De_pp, p_be1, p_be2)
-    double* gp = w.pgrad + (size_t)pt * XR_NPAIR_COLS;
+    double* gp = xr_pgrad(w, i) + (size_t)pt * XR_NPAIR_COLS;
     atomicAdd(gp + P_DE_S, -sig * ex);
     if (pi != 0.0) atomicAdd(gp + P_DE_P, -pi);
     if (pp != 0.0) atomicAdd(gp + P_DE_PP, -pp);
@@ -462,7 +467,7 @@ __device__ inline void push_items(uint32_t* buf, int& nbuf, bool ok, uint32_t it
 
 // Valence angle, penalty and coalition terms (src/xreac/energy.py:278-318 with the angle rule of
 // src/xreac/energy.py:49-55): units are centres j, items the pairs of j's active bonds.
-__global__ void __launch_bounds__(32 * kBondedWarps) k_angles(XrWork w, XrFF ff) {
+__global__ void __launch_bounds__(32 * kBondedWarps) k_angles(XrWork w, XrFF ff0) {
   constexpr int NC = 8, NV = 10;
   __shared__ double ucon[kBondedWarps][kUnits][NC];
   __shared__ double uacc[kBondedWarps][kUnits][NV];
@@ -473,13 +478,14 @@ __global__ void __launch_bounds__(32 * kBondedWarps) k_angles(XrWork w, XrFF ff)
   const int j0 = chunk * kUnits;
   if (j0 >= w.A) return;
   const int nu = min(kUnits, w.A - j0);
-  const int L = w.A + 1, T = ff.ntypes;
-  const double* g = ff.g;
+  const int L = w.A + 1, T = ff0.ntypes;
+  const double* g = ff0.g;
   const bool lammps = !w.full_derivative;
   const double k180 = 3.14159265 / 180;
   // unit constants, one centre per lane
   if (lane < nu) {
     const int j = j0 + lane, tj = w.type[j];
+    const XrFF ff = xr_ff_of(ff0, w, j);
     const double total_j = AFV(AF_TOTAL, j);
     const double d_j = total_j - atom_prm(ff, tj, A_VALENCY);
     const double sbo2 = AFV(AF_SBO2, j);
@@ -513,6 +519,7 @@ __global__ void __launch_bounds__(32 * kBondedWarps) k_angles(XrWork w, XrFF ff)
       const int u = item_unit(it), a = item_a(it), c = item_c(it);
       key = u;
       const int j = j0 + u, tj = w.type[j];
+      const XrFF ff = xr_ff_of(ff0, w, j);
       const double* cj = ucon[wl][u];
       const double e17 = cj[0], Fp = cj[1], dFp_dd = cj[2], K1 = cj[3], dK1_dt = cj[4], db_j = cj[5];
       const double pv3 = cj[6], pv5 = cj[7];
@@ -575,7 +582,7 @@ __global__ void __launch_bounds__(32 * kBondedWarps) k_angles(XrWork w, XrFF ff)
         const double ep = pen1 * Fp * Gp;
         if (w.pgrad) {
           // dE/d(theta00, v1, v2, coa1, v7, pen1, v4) of this record
-          double* ga = w.pgrad + w.pgrad_angle_off + 7 * (size_t)(first + q);
+          double* ga = xr_pgrad(w, j) + w.pgrad_angle_off + 7 * (size_t)(first + q);
           const double sgn_dt2 = dt * dt * exang;  // d branch / d v2 (either sign of v1)
           const double df7_dv4 = pv3 * pij * lbij * A1 * (1 - A2) + (1 - A1) * pv3 * pjk * lbjk * A2;
           const double df8_dv7 = (pv5 - 1) * (2 + ex6) / (den8 * den8) * (-db_j * ex7);
@@ -593,7 +600,7 @@ __global__ void __launch_bounds__(32 * kBondedWarps) k_angles(XrWork w, XrFF ff)
         const double K2 = exp(-g[38] * (ti_b * ti_b + tk_b * tk_b));
         const double K3 = exp(-g[30] * ((bij - 1.5) * (bij - 1.5) + (bjk - 1.5) * (bjk - 1.5)));
         const double ec_ = coa1 * K1 * K2 * K3;
-        if (w.pgrad) atomicAdd(w.pgrad + w.pgrad_angle_off + 7 * (size_t)(first + q) + 3, K1 * K2 * K3);
+        if (w.pgrad) atomicAdd(xr_pgrad(w, j) + w.pgrad_angle_off + 7 * (size_t)(first + q) + 3, K1 * K2 * K3);
         v[2] += ec_;
         v[6] += coa1 * dK1_dt * K2 * K3;
         dtot_i += ec_ * (-2 * g[38] * ti_b);
@@ -638,7 +645,7 @@ __global__ void __launch_bounds__(32 * kBondedWarps) k_angles(XrWork w, XrFF ff)
         if (BFV(BF_BO, ea.x) * BFV(BF_BO, ec.x) > THB_PRODUCT_CUT) {
           const int i = bond_other(w, ea.x, ea.y), k = bond_other(w, ec.x, ec.y);
           const int key3 = (w.type[i] * T + tj) * T + w.type[k];
-          ok = __ldg(ff.angle_index + 2 * key3 + 1) > 0;
+          ok = __ldg(ff0.angle_index + 2 * key3 + 1) > 0;
         }
         item = pack_item(u, a, c);
       }
@@ -684,7 +691,7 @@ __global__ void k_torsion_middles(XrWork w) {
 
 // Torsion and four-body conjugation (src/xreac/energy.py:320-370): units are middle bonds j -> k
 // (the half direction), items the (left, right) combinations of the two ends' active bond rows.
-__global__ void __launch_bounds__(32 * kBondedWarps) k_torsions(XrWork w, XrFF ff) {
+__global__ void __launch_bounds__(32 * kBondedWarps) k_torsions(XrWork w, XrFF ff0) {
   constexpr int NC = 10, NV = 11;
   struct UnitInt {
     int m, j, k, tj, tk, jb, kb, jn, kn;
@@ -697,9 +704,9 @@ __global__ void __launch_bounds__(32 * kBondedWarps) k_torsions(XrWork w, XrFF f
   const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
   const int warp = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
   const int nwarps = (int)((gridDim.x * blockDim.x) >> 5);
-  const int T = ff.ntypes;
+  const int T = ff0.ntypes;
   const int L = w.A + 1;
-  const double* g = ff.g;
+  const double* g = ff0.g;
   const int nm = *w.nmids;
   double* acc = &uacc[wl][0][0];
   for (int q0 = warp * kUnits; q0 < nm; q0 += nwarps * kUnits) {
@@ -709,6 +716,7 @@ __global__ void __launch_bounds__(32 * kBondedWarps) k_torsions(XrWork w, XrFF f
       const int m = w.mids[q0 + lane];
       const int j = w.bond_i[m], k = w.bond_j[m];
       const int tj = w.type[j], tk = w.type[k];
+      const XrFF ff = xr_ff_of(ff0, w, j);
       ui.m = m;
       ui.j = j;
       ui.k = k;
@@ -759,7 +767,7 @@ __global__ void __launch_bounds__(32 * kBondedWarps) k_torsions(XrWork w, XrFF f
         const int2 er = w.arow[ui.kb + item_c(it)];
         const double bo_l = BFV(BF_BO, el.x), bo_r = BFV(BF_BO, er.x);
         const int i = bond_other(w, el.x, el.y), l = bond_other(w, er.x, er.y);
-        const int row = __ldg(ff.torsion_index + ((w.type[i] * T + ui.tj) * T + ui.tk) * T + w.type[l]);
+        const int row = __ldg(ff0.torsion_index + ((w.type[i] * T + ui.tj) * T + ui.tk) * T + w.type[l]);
         double u3[3], wv[3];
         bond_vec(w, el.x, el.y, u3);
         bond_vec(w, er.x, er.y, wv);
@@ -779,7 +787,7 @@ __global__ void __launch_bounds__(32 * kBondedWarps) k_torsions(XrWork w, XrFF f
           const double iA1 = 1.0 / A1, iA2 = 1.0 / A2;
           const double P = n1[0] * n2[0] + n1[1] * n2[1] + n1[2] * n2[2];
           const double cw = P * isq;
-          const double* prm = ff.torsion + 5 * row;
+          const double* prm = xr_ff_of(ff0, w, ui.j).torsion + 5 * row;
           const double V1 = __ldg(prm + 0), V2 = __ldg(prm + 1), V3 = __ldg(prm + 2), tor1 = __ldg(prm + 3),
                        cot1 = __ldg(prm + 4);
           const double b1 = bo_l - THB_CUT, b3 = bo_r - THB_CUT;
@@ -846,7 +854,7 @@ __global__ void __launch_bounds__(32 * kBondedWarps) k_torsions(XrWork w, XrFF f
           ok = !(el.x == ui.m && el.y > 0) && !(er.x == ui.m && er.y < 0);  // left == middle, right == reverse
           if (ok) {
             const int i = bond_other(w, el.x, el.y), l = bond_other(w, er.x, er.y);
-            ok = __ldg(ff.torsion_index + ((w.type[i] * T + ui.tj) * T + ui.tk) * T + w.type[l]) >= 0 &&
+            ok = __ldg(ff0.torsion_index + ((w.type[i] * T + ui.tj) * T + ui.tk) * T + w.type[l]) >= 0 &&
                  BFV(BF_BO, el.x) * bo_m * BFV(BF_BO, er.x) > THB_CUT;
             if (ok && i == l) {
               const uint32_t sl = bond_shift(w, el.x, el.y), sr = bond_shift(w, er.x, er.y);
@@ -896,12 +904,13 @@ struct HbDonor {
 // each lane one candidate, so the FP64 work runs on full warps (an FP64 instruction costs the pipe
 // the same for one active lane as for 32). Reciprocals are formed once per acceptor, per donor and
 // per parameter row instead of once per (donor, acceptor) pair.
-__global__ void k_hbonds(XrWork w, XrFF ff) {
+__global__ void __launch_bounds__(32 * kHbWarps, 4) k_hbonds(XrWork w, XrFF ff0) {
   __shared__ HbDonor don[kHbWarps][kHbDonors];
   __shared__ int2 cand[kHbWarps][kHbBuf];
   const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
   const int h = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
   if (h >= w.A) return;
+  const XrFF ff = xr_ff_of(ff0, w, h);
   const int th = w.type[h], T = ff.ntypes;
   if (__ldg(ff.hb_role + th) != 1) {
     if (lane == 0) AEV(5, h) = 0.0;
@@ -1074,9 +1083,10 @@ __global__ void k_hbonds(XrWork w, XrFF ff) {
 }
 
 // Per-atom chain: neighbours' over-coordination cross terms, lone pair, sbo, then dE/d total.
-__global__ void k_chain_atom(XrWork w, XrFF ff) {
+__global__ void k_chain_atom(XrWork w, XrFF ff0) {
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= w.A) return;
+  const XrFF ff = xr_ff_of(ff0, w, a);
   const int L = w.A + 1, ta = w.type[a];
   const double* g = ff.g;
   double A_d = AJV(AJ_D, a), A_dlpt = AJV(AJ_DLPT, a);
@@ -1107,8 +1117,9 @@ __global__ void k_chain_atom(XrWork w, XrFF ff) {
 }
 
 // Per-bond chain: from the thresholded outputs back through f1, f4, f5 to the uncorrected orders.
-__device__ inline void k_chain_bond_one(const XrWork& w, const XrFF& ff, int b) {
+__device__ inline void k_chain_bond_one(const XrWork& w, const XrFF& ff0, int b) {
   const int i = w.bond_i[b], j = w.bond_j[b];
+  const XrFF ff = xr_ff_of(ff0, w, i);
   const int ti = w.type[i], tj = w.type[j], T = ff.ntypes, pt = ti * T + tj;
   const double bo = BFV(BF_BO, b), pi = BFV(BF_PI, b), pp = BFV(BF_PP, b), sig = BFV(BF_SIG, b);
   const double b2 = bo * bo, b4 = b2 * b2, b7 = b4 * b2 * bo;
@@ -1117,7 +1128,7 @@ __device__ inline void k_chain_bond_one(const XrWork& w, const XrFF& ff, int b) 
                 (AJV(AJ_PRODSUM, i) + AJV(AJ_PRODSUM, j)) * 8.0 * b7;
   if (w.pgrad && bo != 0.0) {
     // De_s and p_ovun1 also weight the over-coordination sum ov1 = sum p_ovun1 De_s bo of both ends
-    double* gp = w.pgrad + (size_t)pt * XR_NPAIR_COLS;
+    double* gp = xr_pgrad(w, i) + (size_t)pt * XR_NPAIR_COLS;
     const double a_ov = (AJV(AJ_OV1, i) + AJV(AJ_OV1, j)) * bo;
     atomicAdd(gp + P_DE_S, a_ov * pair_prm(ff, pt, P_OVUN1));
     atomicAdd(gp + P_OVUN1, a_ov * pair_prm(ff, pt, P_DE_S));
@@ -1178,7 +1189,7 @@ __global__ void k_chain_deltap(XrWork w) {
 }
 
 // dE/dr of each bond from the uncorrected bond orders; added to the pair's radial accumulator.
-__device__ inline void k_chain_radial_one(const XrWork& w, const XrFF& ff, int b) {
+__device__ inline void k_chain_radial_one(const XrWork& w, const XrFF& ff0, int b) {
   if (BFV(BF_MASK, b) == 0.0) return;
   const double d_bo0 = BJV(BJ_BO0, b) + AJV(AJ_DELTAP, w.bond_i[b]) + AJV(AJ_DELTAP, w.bond_j[b]);
   const double G = d_bo0 * BFV(BF_DSIG, b) + (d_bo0 + BJV(BJ_PI0, b)) * BFV(BF_DPI, b) +
@@ -1187,8 +1198,9 @@ __device__ inline void k_chain_radial_one(const XrWork& w, const XrFF& ff, int b
   if (w.pgrad) {
     // dE/d(p_bo1..6, r_s, r_p, r_pp): the uncorrected orders' parameters, through the same chain
     // adjoints (dE/dsigma' = dE/dBO0, dE/dpi' = dE/dBO0 + dE/dPI0, dE/dpipi' = dE/dBO0 + dE/dPP0)
+    const XrFF ff = xr_ff_of(ff0, w, w.bond_i[b]);
     const int ti = w.type[w.bond_i[b]], tj = w.type[w.bond_j[b]], T = ff.ntypes, pt = ti * T + tj;
-    double* gp = w.pgrad + (size_t)pt * XR_NPAIR_COLS;
+    double* gp = xr_pgrad(w, w.bond_i[b]) + (size_t)pt * XR_NPAIR_COLS;
     const double r = w.b_r[b], lr = log(r), cut = 0.01 * ff.g[29];
     const double adj[3] = {d_bo0, d_bo0 + BJV(BJ_PI0, b), d_bo0 + BJV(BJ_PP0, b)};
     const int cr[3] = {A_R_S, A_R_PI, A_R_PI_PI};

@@ -84,6 +84,7 @@ struct XrSystem {
   double origin[3];      // reference point subtracted before FP32 rounding
   double total_charge;
   int has_guess;         // QEq starts from w.qguess (charges of an earlier step) instead of Q/n
+  int ff_set;            // parameter set of the force field this system is evaluated with
   double rc, rc2, bond_cut, hb_cut;     // cutoff, cutoff^2, min(5, rc), min(7.5, rc)
   double inv_rc;                        // 1 / rc
   float cellf[9];
@@ -91,10 +92,15 @@ struct XrSystem {
   float rc2f, bc2f, hc2f;  // FP32 squared cutoff, bond cutoff and hydrogen-bond cutoff
 };
 
-// Force-field tables on the device (uploaded once per force field).
+// Force-field tables on the device (uploaded once per force field). A force field holds one or more
+// parameter sets of the same elements and records: the general parameters and the three index tables
+// (angle_index, torsion_index, hbond_index) are shared, every other table is per set. The pointers
+// below are set 0's; set s's tables sit s * set_stride bytes after them (xr_ff_at).
 struct XrFF {
   int ntypes;
   int vdw_type;
+  int nsets;                  // parameter sets (1 unless the host loaded more)
+  long long set_stride;       // bytes from one set's tables to the next set's
   double g[XR_NGENERAL];
   const double* atom;         // [T][XR_NATOM_COLS]
   const double* pair;         // [T*T][XR_NPAIR_COLS]
@@ -192,6 +198,7 @@ struct XrWork {
   // [T*T][XR_NPAIR_COLS] pair-table columns, then [R][7] angle records.
   double* pgrad;
   int pgrad_angle_off;
+  long long pgrad_stride;     // doubles per system: each system accumulates its own gradient
   double* f;                  // [A][3] gradient dE/dx accumulator (forces = -f)
   double* qwork;              // [XR_QW_N][A] QEq solver vectors
   double* red;                // reduction scratch for solvers
@@ -206,6 +213,42 @@ struct XrWork {
   double* chunk_part;         // [nchunks][XR_PART_N]
   int nchunks;
 };
+
+// The parameter-gradient block of the system of `atom` (pair table, then angle records).
+__device__ inline double* xr_pgrad(const XrWork& w, int atom) { return w.pgrad + (size_t)w.sys_of[atom] * w.pgrad_stride; }
+
+template <class P>
+__device__ __forceinline__ const P* xr_byte_offset(const P* p, long long bytes) {
+  return reinterpret_cast<const P*>(reinterpret_cast<const char*>(p) + bytes);
+}
+
+// The force field as seen by one parameter set: the per-set table pointers moved to that set.
+__device__ __forceinline__ XrFF xr_ff_at(const XrFF& ff, int set) {
+  XrFF f = ff;
+  const long long o = (long long)set * ff.set_stride;
+  f.atom = xr_byte_offset(ff.atom, o);
+  f.pair = xr_byte_offset(ff.pair, o);
+  f.pair_gw = xr_byte_offset(ff.pair_gw, o);
+  f.pair_logr = xr_byte_offset(ff.pair_logr, o);
+  f.pair_rmax = xr_byte_offset(ff.pair_rmax, o);
+  f.pair_inv = xr_byte_offset(ff.pair_inv, o);
+  f.is_carbon = xr_byte_offset(ff.is_carbon, o);
+  f.hb_role = xr_byte_offset(ff.hb_role, o);
+  f.angle = xr_byte_offset(ff.angle, o);
+  f.torsion = xr_byte_offset(ff.torsion, o);
+  f.hbond = xr_byte_offset(ff.hbond, o);
+  return f;
+}
+
+// Parameter set of the system that `atom` belongs to (0 when the force field has one set).
+__device__ __forceinline__ int xr_set_of(const XrFF& ff, const XrWork& w, int atom) {
+  return ff.nsets > 1 ? w.sys[w.sys_of[atom]].ff_set : 0;
+}
+
+// The force field of the system that `atom` belongs to.
+__device__ __forceinline__ XrFF xr_ff_of(const XrFF& ff, const XrWork& w, int atom) {
+  return xr_ff_at(ff, xr_set_of(ff, w, atom));
+}
 
 // Per-atom forward slots in a_fwd.
 enum AF { AF_DELTAP = 0, AF_TOTAL, AF_NLP, AF_VLPEX, AF_DLP, AF_DLPT, AF_SUMPI, AF_PROD, AF_OV1, AF_OV2, AF_DC,

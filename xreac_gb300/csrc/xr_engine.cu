@@ -36,11 +36,23 @@ bool grow(T** p, size_t* cap, size_t need) {
 
 }  // namespace
 
+// Per-set tables of a force field, in their order inside a set's block.
+enum FFPart { FP_ATOM = 0, FP_PAIR, FP_GW, FP_LOGR, FP_RMAX, FP_PINV, FP_CARBON, FP_HBROLE, FP_ANGLE, FP_TORSION, FP_HBOND,
+              FP_N };
+
 struct xr_ff {
   XrFF d{};
-  std::vector<void*> allocs;
+  // Device layout (one allocation): nsets blocks of set_bytes, one per parameter set, then the shared
+  // index tables (angle, torsion, hydrogen bond) in shared_bytes.
+  void* blob = nullptr;
+  size_t blob_bytes = 0;
+  size_t set_bytes = 0, shared_bytes = 0;
+  size_t part_off[FP_N] = {};        // offsets of the per-set tables inside a block
+  size_t shared_off[3] = {};         // offsets of the index tables inside the shared region
+  std::vector<unsigned char> set0;   // host copy of set 0's block (the default for tables not given)
+  int nsets = 1;
   int device = 0;
-  int nangle = 0;
+  int nangle = 0, ntorsion = 0, nhbond = 0;
 };
 
 struct xr_ctx {
@@ -125,6 +137,7 @@ struct xr_ctx {
   size_t cpgrad = 0;
   std::vector<double> h_pgrad;
   long long pgrad_pairs = 0, pgrad_angles = 0;
+  int pgrad_systems = 0;  // systems of the last call with XR_FLAG_PARAM_GRADIENT (one block each)
   double* qadj = nullptr;
   size_t cqadj = 0;
   double* f = nullptr;
@@ -687,11 +700,17 @@ void keep_skin_list(xr_ctx* c, int nsys, int A, double rc) {
 enum ListMode { kScan = 0, kBuild = 1, kReuse = 2, kSupplied = 3 };
 
 int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsigned flags, xr_result* out,
-              const xr_neighbors* nb = nullptr) {
+              const xr_neighbors* nb = nullptr, const int* sets = nullptr) {
   if (!c || !ff || nsys < 1 || !sys) {
     if (c) c->err = "invalid arguments";
     return XR_EINPUT;
   }
+  if (sets)
+    for (int s = 0; s < nsys; ++s)
+      if (sets[s] < 0 || sets[s] >= ff->nsets) {
+        c->err = "parameter set index out of range";
+        return XR_EINPUT;
+      }
   if (nb && nsys != 1) {
     c->err = "a supplied neighbour list belongs to a single-system call";
     return XR_EINPUT;
@@ -742,6 +761,7 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
       int rcode = build_system(c, in, off, rc, c->host_sys[s], c->h_x + off);
       if (rcode) return rcode;
     }
+    c->host_sys[s].ff_set = sets ? sets[s] : 0;
     for (int a = 0; a < in.natoms; ++a) {
       const int t = in.types[a];
       if (t < 0 || t >= ff->d.ntypes) {
@@ -874,13 +894,17 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
   w.nchunks = (int)nchunk;
   c->pgrad_pairs = c->pgrad_angles = 0;
   if (flags & XR_FLAG_PARAM_GRADIENT) {
+    // one gradient block per system: [pair table][angle records]
     const long long np = (long long)ff->d.ntypes * ff->d.ntypes * XR_NPAIR_COLS, na = 7ll * ff->nangle;
-    if (!grow(&c->pgrad, &c->cpgrad, (size_t)(np + na + 1))) return cuda_fail(c, cudaErrorMemoryAllocation, "allocation");
-    cudaMemsetAsync(c->pgrad, 0, sizeof(double) * (size_t)(np + na), st);
+    const size_t all = (size_t)(np + na) * nsys;
+    if (!grow(&c->pgrad, &c->cpgrad, all + 1)) return cuda_fail(c, cudaErrorMemoryAllocation, "allocation");
+    cudaMemsetAsync(c->pgrad, 0, sizeof(double) * all, st);
     w.pgrad = c->pgrad;
     w.pgrad_angle_off = (int)np;
+    w.pgrad_stride = np + na;
     c->pgrad_pairs = np;
     c->pgrad_angles = na;
+    c->pgrad_systems = nsys;
   }
   attach_lists(c, w);
   stage(c, 0, st);
@@ -1028,11 +1052,10 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
   cudaMemcpyAsync(c->h_cnt, c->cnt, sizeof(int) * 4 * (size_t)(A + 1), cudaMemcpyDeviceToHost, st);
   d2h += sizeof(int) * 4 * (long long)(A + 1);
   if (c->pgrad_pairs > 0) {
-    if (!host_grow(&c->h_pg, &c->ch_pg, (size_t)(c->pgrad_pairs + c->pgrad_angles)))
-      return cuda_fail(c, cudaErrorMemoryAllocation, "allocation");
-    cudaMemcpyAsync(c->h_pg, c->pgrad, sizeof(double) * (size_t)(c->pgrad_pairs + c->pgrad_angles),
-                    cudaMemcpyDeviceToHost, st);
-    d2h += sizeof(double) * (c->pgrad_pairs + c->pgrad_angles);
+    const size_t all = (size_t)(c->pgrad_pairs + c->pgrad_angles) * nsys;
+    if (!host_grow(&c->h_pg, &c->ch_pg, all)) return cuda_fail(c, cudaErrorMemoryAllocation, "allocation");
+    cudaMemcpyAsync(c->h_pg, c->pgrad, sizeof(double) * all, cudaMemcpyDeviceToHost, st);
+    d2h += (long long)(sizeof(double) * all);
   }
   d2h += 3 * sizeof(int);
   if (dev_io) {
@@ -1086,7 +1109,7 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
   c->list_sizes[3] = nD;
   c->list_sizes[4] = c->h_small[8];  // active bonds (uncorrected order passed the cut)
   c->list_sizes[5] = c->h_small[7];  // torsion middles (bo > 0.001)
-  if (c->pgrad_pairs > 0) c->h_pgrad.assign(c->h_pg, c->h_pg + (c->pgrad_pairs + c->pgrad_angles));
+  if (c->pgrad_pairs > 0) c->h_pgrad.assign(c->h_pg, c->h_pg + (c->pgrad_pairs + c->pgrad_angles) * nsys);
   c->last_A = A;
   // keep the scans for export
   c->host_cnt.assign(c->h_cnt, c->h_cnt + 4 * (size_t)(A + 1));
@@ -1140,6 +1163,179 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
   return XR_OK;
 }
 
+// Derived per-set tables of one parameter set (host): the vdW shielding term, log radii, bond-order
+// distance bound and reciprocal radii per pair type, and the hydrogen-bond role per element.
+void ff_derive(int T, const double* general, const double* atom, const double* pair, double* gw, double* logr,
+               double* rmax, double* pinv, int* hb_role) {
+  for (int pt = 0; pt < T * T; ++pt) {
+    const double* p = pair + pt * XR_NPAIR_COLS;
+    gw[pt] = std::pow(1.0 / p[P_GAMMA_W], general[28]);
+    logr[3 * pt + 0] = p[P_RS] > 0 ? std::log(p[P_RS]) : 0.0;
+    logr[3 * pt + 1] = p[P_RP] > 0 ? std::log(p[P_RP]) : 0.0;
+    logr[3 * pt + 2] = p[P_RPP] > 0 ? std::log(p[P_RPP]) : 0.0;
+    pinv[2 * pt] = 1.0 / p[P_RVDW];
+    pinv[2 * pt + 1] = 1.0 / p[P_RCORE];
+  }
+  // Per pair type, a distance beyond which the uncorrected bond order sigma' + pi' + pi-pi' stays
+  // below a quarter of the cut (k_bo1 skips the terms there: the bond is inactive either way). Each
+  // used term c exp(p_odd (r / r0)^p_even) decreases with r when p_odd < 0 < p_even, and stays below
+  // target / n (n used terms) for r > r0 (ln(target / (n c)) / p_odd)^(1 / p_even); the largest of
+  // these bounds the sum. Otherwise no bound is used (infinity) and every candidate is evaluated.
+  const double cut = 0.01 * general[29];
+  for (int pt = 0; pt < T * T; ++pt) {
+    const double* p = pair + pt * XR_NPAIR_COLS;
+    const double* ai = atom + (pt / T) * XR_NATOM_COLS;
+    const double* aj = atom + (pt % T) * XR_NATOM_COLS;
+    const bool use[3] = {ai[A_R_S] > 0 && aj[A_R_S] > 0, ai[A_R_PI] > 0 && aj[A_R_PI] > 0,
+                         ai[A_R_PI_PI] > 0 && aj[A_R_PI_PI] > 0};
+    const double pa[3] = {p[P_BO1], p[P_BO3], p[P_BO5]}, pb[3] = {p[P_BO2], p[P_BO4], p[P_BO6]};
+    const double r0[3] = {p[P_RS], p[P_RP], p[P_RPP]};
+    bool monotone = cut > 0;
+    int n = 0;
+    for (int k = 0; k < 3; ++k) {
+      if (!use[k]) continue;
+      ++n;
+      if (!(pa[k] < 0 && pb[k] > 0 && r0[k] > 0 && std::isfinite(pa[k]) && std::isfinite(pb[k]))) monotone = false;
+    }
+    double bound = INFINITY;
+    if (monotone) {
+      const double share = 0.25 * cut / std::max(n, 1);
+      bound = 1e-6;
+      for (int k = 0; k < 3; ++k) {
+        if (!use[k]) continue;
+        const double c = k == 0 ? 1.0 + cut : 1.0;
+        if (c <= share) continue;  // the term never reaches its share
+        const double u = std::log(share / c) / pa[k];  // > 0: (r / r0)^p_even must exceed it
+        bound = std::max(bound, r0[k] * std::pow(u, 1.0 / pb[k]) * (1.0 + 1e-12));
+      }
+      if (!std::isfinite(bound)) bound = INFINITY;
+    }
+    rmax[pt] = bound;
+  }
+  for (int t = 0; t < T; ++t) {
+    const double ph = atom[t * XR_NATOM_COLS + A_P_HBOND];
+    hb_role[t] = ph == 1.0 ? 1 : (ph == 2.0 ? 2 : 0);  // the reference compares p_hbond exactly
+  }
+}
+
+// Sizes in bytes of the per-set tables and of the shared index tables.
+void ff_part_bytes(const xr_ff* f, size_t bytes[FP_N], size_t shared[3]) {
+  const size_t T = (size_t)f->d.ntypes, TT = T * T;
+  bytes[FP_ATOM] = sizeof(double) * T * XR_NATOM_COLS;
+  bytes[FP_PAIR] = sizeof(double) * TT * XR_NPAIR_COLS;
+  bytes[FP_GW] = sizeof(double) * TT;
+  bytes[FP_LOGR] = sizeof(double) * 3 * TT;
+  bytes[FP_RMAX] = sizeof(double) * TT;
+  bytes[FP_PINV] = sizeof(double) * 2 * TT;
+  bytes[FP_CARBON] = sizeof(int) * T;
+  bytes[FP_HBROLE] = sizeof(int) * T;
+  bytes[FP_ANGLE] = sizeof(double) * 7 * (size_t)f->nangle;
+  bytes[FP_TORSION] = sizeof(double) * 5 * (size_t)f->ntorsion;
+  bytes[FP_HBOND] = sizeof(double) * 4 * (size_t)f->nhbond;
+  shared[0] = sizeof(int) * 2 * TT * T;
+  shared[1] = sizeof(int) * TT * TT;
+  shared[2] = sizeof(int) * TT * T;
+}
+
+inline size_t round256(size_t n) { return (n + 255) / 256 * 256; }
+
+// Writes one set's block (host, set_bytes long): the given tables, set 0's where a table is null
+// (is_carbon always set 0's), and the tables derived from this set's atom and pair values.
+void ff_fill_set(const xr_ff* f, const double* general, const double* atom, const double* pair, const int* is_carbon,
+                 const double* angle, const double* torsion, const double* hbond, unsigned char* block) {
+  size_t bytes[FP_N], shared[3];
+  ff_part_bytes(f, bytes, shared);
+  const unsigned char* base = f->set0.empty() ? nullptr : f->set0.data();
+  auto put = [&](int part, const void* src) {
+    const void* from = src ? src : (base ? base + f->part_off[part] : nullptr);
+    if (from && bytes[part]) std::memcpy(block + f->part_off[part], from, bytes[part]);
+  };
+  put(FP_ATOM, atom);
+  put(FP_PAIR, pair);
+  put(FP_CARBON, is_carbon);
+  put(FP_ANGLE, angle);
+  put(FP_TORSION, torsion);
+  put(FP_HBOND, hbond);
+  const int T = f->d.ntypes;
+  ff_derive(T, general, reinterpret_cast<const double*>(block + f->part_off[FP_ATOM]),
+            reinterpret_cast<const double*>(block + f->part_off[FP_PAIR]),
+            reinterpret_cast<double*>(block + f->part_off[FP_GW]), reinterpret_cast<double*>(block + f->part_off[FP_LOGR]),
+            reinterpret_cast<double*>(block + f->part_off[FP_RMAX]), reinterpret_cast<double*>(block + f->part_off[FP_PINV]),
+            reinterpret_cast<int*>(block + f->part_off[FP_HBROLE]));
+}
+
+// Points the device view at the blob: set 0's tables, the shared index tables, the set stride.
+void ff_bind(xr_ff* f) {
+  unsigned char* b = static_cast<unsigned char*>(f->blob);
+  XrFF& d = f->d;
+  d.nsets = f->nsets;
+  d.set_stride = (long long)f->set_bytes;
+  d.atom = reinterpret_cast<const double*>(b + f->part_off[FP_ATOM]);
+  d.pair = reinterpret_cast<const double*>(b + f->part_off[FP_PAIR]);
+  d.pair_gw = reinterpret_cast<const double*>(b + f->part_off[FP_GW]);
+  d.pair_logr = reinterpret_cast<const double*>(b + f->part_off[FP_LOGR]);
+  d.pair_rmax = reinterpret_cast<const double*>(b + f->part_off[FP_RMAX]);
+  d.pair_inv = reinterpret_cast<const double*>(b + f->part_off[FP_PINV]);
+  d.is_carbon = reinterpret_cast<const int*>(b + f->part_off[FP_CARBON]);
+  d.hb_role = reinterpret_cast<const int*>(b + f->part_off[FP_HBROLE]);
+  d.angle = reinterpret_cast<const double*>(b + f->part_off[FP_ANGLE]);
+  d.torsion = reinterpret_cast<const double*>(b + f->part_off[FP_TORSION]);
+  d.hbond = reinterpret_cast<const double*>(b + f->part_off[FP_HBOND]);
+  unsigned char* sh = b + (size_t)f->nsets * f->set_bytes;
+  d.angle_index = reinterpret_cast<const int*>(sh + f->shared_off[0]);
+  d.torsion_index = reinterpret_cast<const int*>(sh + f->shared_off[1]);
+  d.hbond_index = reinterpret_cast<const int*>(sh + f->shared_off[2]);
+}
+
+// The force field's device tables with one parameter set: set 0's block and the shared index tables,
+// laid out in one allocation (each table 256-byte aligned) and filled with one copy. The first call
+// allocates; later calls (xr_ff_update) overwrite the same layout and drop any further sets.
+int ff_pack(xr_ff* f, const double* general, const double* atom, const double* pair, const int* is_carbon, int vdw_type,
+            const int* angle_index, const double* angle, const int* torsion_index, const double* torsion,
+            const int* hbond_index, const double* hbond) {
+  XrFF& d = f->d;
+  size_t bytes[FP_N], shared[3];
+  ff_part_bytes(f, bytes, shared);
+  size_t set_bytes = 0, shared_bytes = 0;
+  for (int k = 0; k < FP_N; ++k) {
+    f->part_off[k] = set_bytes;
+    set_bytes += round256(bytes[k]);
+  }
+  for (int k = 0; k < 3; ++k) {
+    f->shared_off[k] = shared_bytes;
+    shared_bytes += round256(shared[k]);
+  }
+  if (f->blob && (set_bytes != f->set_bytes || shared_bytes != f->shared_bytes)) return XR_EINPUT;
+  const size_t total = std::max<size_t>(set_bytes + shared_bytes, 256);
+  if (f->blob && f->nsets != 1) {  // back to one set
+    cudaFree(f->blob);
+    f->blob = nullptr;
+  }
+  if (!f->blob) {
+    if (cudaMalloc(&f->blob, total) != cudaSuccess) {
+      f->blob = nullptr;
+      return XR_ECUDA;
+    }
+    f->blob_bytes = total;
+  }
+  f->set_bytes = set_bytes;
+  f->shared_bytes = shared_bytes;
+  f->nsets = 1;
+  d.vdw_type = vdw_type;
+  for (int k = 0; k < XR_NGENERAL; ++k) d.g[k] = general[k];
+  d.inv_g28 = 1.0 / d.g[28];
+  std::vector<unsigned char> host(total, 0);
+  f->set0.clear();
+  ff_fill_set(f, general, atom, pair, is_carbon, angle, torsion, hbond, host.data());
+  const int* idx[3] = {angle_index, torsion_index, hbond_index};
+  for (int k = 0; k < 3; ++k)
+    if (shared[k]) std::memcpy(host.data() + set_bytes + f->shared_off[k], idx[k], shared[k]);
+  f->set0.assign(host.begin(), host.begin() + set_bytes);
+  if (cudaMemcpy(f->blob, host.data(), total, cudaMemcpyHostToDevice) != cudaSuccess) return XR_ECUDA;
+  ff_bind(f);
+  return XR_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1150,112 +1346,90 @@ int xr_ff_create(const double* general, int ntypes, const double* atom, const do
                  xr_ff** out) {
   if (!out || !general || ntypes < 1 || !atom || !pair || !is_carbon || !angle_index || !torsion_index || !hbond_index)
     return XR_EINPUT;
-  if (vdw_type < 1 || vdw_type > 3) return XR_EINPUT;
+  if (vdw_type < 1 || vdw_type > 3 || nangle < 0 || ntorsion < 0 || nhbond < 0) return XR_EINPUT;
   xr_ff* f = new xr_ff();
   cudaGetDevice(&f->device);
   f->nangle = nangle;
-  const int T = ntypes;
-  XrFF& d = f->d;
-  d.ntypes = T;
-  d.vdw_type = vdw_type;
-  for (int k = 0; k < XR_NGENERAL; ++k) d.g[k] = general[k];
-  // derived per-pair constants
-  std::vector<double> gw(T * T), logr(3 * T * T);
-  for (int pt = 0; pt < T * T; ++pt) {
-    const double* p = pair + pt * XR_NPAIR_COLS;
-    gw[pt] = std::pow(1.0 / p[P_GAMMA_W], general[28]);
-    logr[3 * pt + 0] = p[P_RS] > 0 ? std::log(p[P_RS]) : 0.0;
-    logr[3 * pt + 1] = p[P_RP] > 0 ? std::log(p[P_RP]) : 0.0;
-    logr[3 * pt + 2] = p[P_RPP] > 0 ? std::log(p[P_RPP]) : 0.0;
+  f->ntorsion = ntorsion;
+  f->nhbond = nhbond;
+  f->d.ntypes = ntypes;
+  const int code = ff_pack(f, general, atom, pair, is_carbon, vdw_type, angle_index, angle, torsion_index, torsion,
+                           hbond_index, hbond);
+  if (code != XR_OK) {
+    xr_ff_destroy(f);
+    return code;
   }
-  // Per pair type, the distance beyond which the uncorrected bond order sigma' + pi' + pi-pi' stays
-  // below a quarter of the cut. Each term exp(p_odd (r / r0)^p_even) decreases with r when
-  // p_odd < 0 < p_even; otherwise no bound is used (infinity) and every candidate is evaluated.
-  std::vector<double> rmax(T * T);
-  {
-    const double cut = 0.01 * general[29];
-    for (int pt = 0; pt < T * T; ++pt) {
-      const double* p = pair + pt * XR_NPAIR_COLS;
-      const double* ai = atom + (pt / T) * XR_NATOM_COLS;
-      const double* aj = atom + (pt % T) * XR_NATOM_COLS;
-      const bool use[3] = {ai[A_R_S] > 0 && aj[A_R_S] > 0, ai[A_R_PI] > 0 && aj[A_R_PI] > 0,
-                           ai[A_R_PI_PI] > 0 && aj[A_R_PI_PI] > 0};
-      const double pa[3] = {p[P_BO1], p[P_BO3], p[P_BO5]}, pb[3] = {p[P_BO2], p[P_BO4], p[P_BO6]};
-      const double r0[3] = {p[P_RS], p[P_RP], p[P_RPP]};
-      bool monotone = cut > 0;
-      for (int k = 0; k < 3; ++k)
-        if (use[k] && !(pa[k] < 0 && pb[k] > 0 && r0[k] > 0 && std::isfinite(pa[k]) && std::isfinite(pb[k])))
-          monotone = false;
-      auto raw = [&](double r) {
-        double v = 0;
-        for (int k = 0; k < 3; ++k)
-          if (use[k]) v += (k == 0 ? 1.0 + cut : 1.0) * std::exp(pa[k] * std::pow(r / r0[k], pb[k]));
-        return v;
-      };
-      double bound = INFINITY;
-      if (monotone) {
-        const double target = 0.25 * cut;
-        double lo = 1e-6, hi = 64.0;
-        if (raw(hi) < target) {
-          if (raw(lo) < target) {
-            bound = lo;
-          } else {
-            for (int it = 0; it < 200; ++it) {
-              const double mid = 0.5 * (lo + hi);
-              (raw(mid) < target ? hi : lo) = mid;
-            }
-            bound = hi;
-          }
-        }
-      }
-      rmax[pt] = bound;
-    }
-  }
-  auto up = [&](const void* src, size_t bytes) -> void* {
-    void* dst = nullptr;
-    if (cudaMalloc(&dst, std::max<size_t>(bytes, 16)) != cudaSuccess) return nullptr;
-    if (bytes) cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice);
-    f->allocs.push_back(dst);
-    return dst;
-  };
-  d.atom = (const double*)up(atom, sizeof(double) * T * XR_NATOM_COLS);
-  d.pair = (const double*)up(pair, sizeof(double) * T * T * XR_NPAIR_COLS);
-  d.pair_gw = (const double*)up(gw.data(), sizeof(double) * T * T);
-  d.pair_logr = (const double*)up(logr.data(), sizeof(double) * 3 * T * T);
-  d.pair_rmax = (const double*)up(rmax.data(), sizeof(double) * T * T);
-  std::vector<double> pinv(2 * (size_t)T * T);
-  for (int pt = 0; pt < T * T; ++pt) {
-    pinv[2 * pt] = 1.0 / pair[pt * XR_NPAIR_COLS + P_RVDW];
-    pinv[2 * pt + 1] = 1.0 / pair[pt * XR_NPAIR_COLS + P_RCORE];
-  }
-  d.pair_inv = (const double*)up(pinv.data(), sizeof(double) * 2 * T * T);
-  d.inv_g28 = 1.0 / d.g[28];
-  d.is_carbon = (const int*)up(is_carbon, sizeof(int) * T);
-  std::vector<int> hb_role(T);
-  for (int t = 0; t < T; ++t) {
-    const double ph = atom[t * XR_NATOM_COLS + A_P_HBOND];
-    hb_role[t] = ph == 1.0 ? 1 : (ph == 2.0 ? 2 : 0);  // the reference compares p_hbond exactly
-  }
-  d.hb_role = (const int*)up(hb_role.data(), sizeof(int) * T);
-  d.angle_index = (const int*)up(angle_index, sizeof(int) * 2 * T * T * T);
-  d.angle = (const double*)up(angle, sizeof(double) * 7 * (size_t)nangle);
-  d.torsion_index = (const int*)up(torsion_index, sizeof(int) * (size_t)T * T * T * T);
-  d.torsion = (const double*)up(torsion, sizeof(double) * 5 * (size_t)ntorsion);
-  d.hbond_index = (const int*)up(hbond_index, sizeof(int) * T * T * T);
-  d.hbond = (const double*)up(hbond, sizeof(double) * 4 * (size_t)nhbond);
-  for (void* p : f->allocs)
-    if (!p) {
-      xr_ff_destroy(f);
-      return XR_ECUDA;
-    }
   *out = f;
+  return XR_OK;
+}
+
+int xr_ff_update(xr_ff* f, const double* general, const double* atom, const double* pair, const int* is_carbon,
+                 int vdw_type, const int* angle_index, const double* angle, const int* torsion_index,
+                 const double* torsion, const int* hbond_index, const double* hbond) {
+  if (!f || !general || !atom || !pair || !is_carbon || !angle_index || !torsion_index || !hbond_index || vdw_type < 1 ||
+      vdw_type > 3)
+    return XR_EINPUT;
+  cudaSetDevice(f->device);
+  return ff_pack(f, general, atom, pair, is_carbon, vdw_type, angle_index, angle, torsion_index, torsion, hbond_index,
+                 hbond);
+}
+
+int xr_ff_set_count(xr_ff* f, int nsets) {
+  if (!f || nsets < 1 || nsets > XR_MAX_PARAMETER_SETS) return XR_EINPUT;
+  if (nsets == f->nsets) return XR_OK;
+  cudaSetDevice(f->device);
+  const size_t total = std::max<size_t>((size_t)nsets * f->set_bytes + f->shared_bytes, 256);
+  void* blob = nullptr;
+  if (cudaMalloc(&blob, total) != cudaSuccess) return XR_ECUDA;
+  unsigned char* nb = static_cast<unsigned char*>(blob);
+  const unsigned char* ob = static_cast<const unsigned char*>(f->blob);
+  const int keep = std::min(nsets, f->nsets);
+  cudaError_t e = cudaMemcpy(nb, ob, (size_t)keep * f->set_bytes, cudaMemcpyDeviceToDevice);
+  for (int s = keep; s < nsets && e == cudaSuccess; ++s)
+    e = cudaMemcpy(nb + (size_t)s * f->set_bytes, ob, f->set_bytes, cudaMemcpyDeviceToDevice);
+  if (e == cudaSuccess && f->shared_bytes)
+    e = cudaMemcpy(nb + (size_t)nsets * f->set_bytes, ob + (size_t)f->nsets * f->set_bytes, f->shared_bytes,
+                   cudaMemcpyDeviceToDevice);
+  if (e != cudaSuccess) {
+    cudaFree(blob);
+    return XR_ECUDA;
+  }
+  cudaFree(f->blob);
+  f->blob = blob;
+  f->blob_bytes = total;
+  f->nsets = nsets;
+  ff_bind(f);
+  return XR_OK;
+}
+
+int xr_ff_set_count_of(const xr_ff* f) { return f ? f->nsets : 0; }
+
+int xr_ff_update_sets(xr_ff* f, int first, int count, const double* atom, const double* pair, const double* angle,
+                      const double* torsion, const double* hbond) {
+  if (!f || first < 0 || count < 0 || first > f->nsets - count) return XR_EINPUT;
+  if (count == 0) return XR_OK;
+  cudaSetDevice(f->device);
+  size_t bytes[FP_N], shared[3];
+  ff_part_bytes(f, bytes, shared);
+  const size_t T = (size_t)f->d.ntypes;
+  const size_t stride[FP_N] = {T * XR_NATOM_COLS, T * T * XR_NPAIR_COLS, 0, 0, 0, 0, 0, 0, 7 * (size_t)f->nangle,
+                               5 * (size_t)f->ntorsion, 4 * (size_t)f->nhbond};
+  std::vector<unsigned char> host((size_t)count * f->set_bytes, 0);
+  for (int s = 0; s < count; ++s)
+    ff_fill_set(f, f->d.g, atom ? atom + s * stride[FP_ATOM] : nullptr, pair ? pair + s * stride[FP_PAIR] : nullptr,
+                nullptr, angle ? angle + s * stride[FP_ANGLE] : nullptr,
+                torsion ? torsion + s * stride[FP_TORSION] : nullptr, hbond ? hbond + s * stride[FP_HBOND] : nullptr,
+                host.data() + (size_t)s * f->set_bytes);
+  if (first == 0) f->set0.assign(host.begin(), host.begin() + f->set_bytes);
+  if (cudaMemcpy(static_cast<unsigned char*>(f->blob) + (size_t)first * f->set_bytes, host.data(), host.size(),
+                 cudaMemcpyHostToDevice) != cudaSuccess)
+    return XR_ECUDA;
   return XR_OK;
 }
 
 void xr_ff_destroy(xr_ff* ff) {
   if (!ff) return;
-  for (void* p : ff->allocs)
-    if (p) cudaFree(p);
+  if (ff->blob) cudaFree(ff->blob);
   delete ff;
 }
 
@@ -1370,6 +1544,15 @@ int xr_eval_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, un
   return run_batch(c, ff, nsys, sys, flags, out);
 }
 
+int xr_eval_batch_sets(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, const int* sets, unsigned flags,
+                       xr_result* out) {
+  if (c && !sets) {
+    c->err = "parameter sets require one set index per system";
+    return XR_EINPUT;
+  }
+  return run_batch(c, ff, nsys, sys, flags, out, nullptr, sets);
+}
+
 long long xr_last_launches(const xr_ctx* c) { return c ? c->launches : 0; }
 
 int xr_last_list_sizes(const xr_ctx* c, long long* sizes, int n) {
@@ -1380,12 +1563,32 @@ int xr_last_list_sizes(const xr_ctx* c, long long* sizes, int n) {
 
 int xr_last_qeq_iterations(const xr_ctx* c) { return c ? c->qeq_iterations : 0; }
 
-int xr_get_param_gradient(const xr_ctx* c, double* pair_grad, long long npair, double* angle_grad, long long nangle) {
-  if (!c || c->pgrad_pairs == 0) return XR_EINPUT;
+int xr_get_param_gradient_system(const xr_ctx* c, int index, double* pair_grad, long long npair, double* angle_grad,
+                                 long long nangle) {
+  if (!c || c->pgrad_pairs == 0 || index < -1 || index >= c->pgrad_systems) return XR_EINPUT;
   if (npair != c->pgrad_pairs || nangle != c->pgrad_angles || !pair_grad || (nangle > 0 && !angle_grad)) return XR_EINPUT;
-  std::memcpy(pair_grad, c->h_pgrad.data(), sizeof(double) * (size_t)npair);
-  if (nangle > 0) std::memcpy(angle_grad, c->h_pgrad.data() + npair, sizeof(double) * (size_t)nangle);
+  const long long stride = npair + nangle;
+  const int s0 = index < 0 ? 0 : index, s1 = index < 0 ? c->pgrad_systems : index + 1;
+  for (long long k = 0; k < npair; ++k) pair_grad[k] = 0.0;
+  for (long long k = 0; k < nangle; ++k) angle_grad[k] = 0.0;
+  for (int sy = s0; sy < s1; ++sy) {  // systems in call order: the same sum on every call
+    const double* g = c->h_pgrad.data() + (size_t)sy * stride;
+    for (long long k = 0; k < npair; ++k) pair_grad[k] += g[k];
+    for (long long k = 0; k < nangle; ++k) angle_grad[k] += g[npair + k];
+  }
   return XR_OK;
+}
+
+int xr_get_param_gradient_blocks(const xr_ctx* c, double* out, long long count) {
+  if (!c || c->pgrad_pairs == 0 || !out) return XR_EINPUT;
+  const long long all = (c->pgrad_pairs + c->pgrad_angles) * (long long)c->pgrad_systems;
+  if (count != all) return XR_EINPUT;
+  std::memcpy(out, c->h_pgrad.data(), sizeof(double) * (size_t)all);
+  return XR_OK;
+}
+
+int xr_get_param_gradient(const xr_ctx* c, double* pair_grad, long long npair, double* angle_grad, long long nangle) {
+  return xr_get_param_gradient_system(c, -1, pair_grad, npair, angle_grad, nangle);
 }
 
 int xr_last_qeq_work(const xr_ctx* c, long long* iterations, double* matvec_bytes) {

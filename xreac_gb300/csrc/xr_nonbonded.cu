@@ -25,6 +25,11 @@ constexpr double SELF_CONVERSION = 23.02;
 
 __device__ inline double pair_prm(const XrFF& ff, int pt, int col) { return __ldg(ff.pair + pt * XR_NPAIR_COLS + col); }
 __device__ inline double atom_prm(const XrFF& ff, int t, int col) { return __ldg(ff.atom + t * XR_NATOM_COLS + col); }
+// The QEq solver sees one system at a time and reads only its parameter set's atom table.
+__device__ inline double atom_prm(const double* atab, int t, int col) { return __ldg(atab + t * XR_NATOM_COLS + col); }
+__device__ inline const double* atoms_of_system(const XrFF& ff, const XrSystem& S) {
+  return xr_ff_at(ff, ff.nsets > 1 ? S.ff_set : 0).atom;
+}
 
 __device__ inline void edge_vector(const XrSystem& S, const double4_32a& xi, const double4_32a& xj, uint32_t code, double v[3]) {
   const int sx = xr_sx(code), sy = xr_sy(code), sz = xr_sz(code);
@@ -47,13 +52,14 @@ __device__ inline double inv_cbrt(double t) {
 }
 
 // ------------------------------------------------------------------------------ pair kernel
-__global__ void k_pairs(XrWork w, XrFF ff) {
+__global__ void k_pairs(XrWork w, XrFF ff0) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= w.nP) return;
   const int e = w.pair_edge[p], i = w.pair_i[p];
   const int2 ed = w.edge[e];
   const int j = ed.x;
   const XrSystem& S = w.sys[w.sys_of[i]];
+  const XrFF ff = xr_ff_at(ff0, ff0.nsets > 1 ? S.ff_set : 0);
   double v[3];
   edge_vector(S, w.x[i], w.x[j], (uint32_t)ed.y, v);
   const double r = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(v[0], v[0]), __dmul_rn(v[1], v[1])), __dmul_rn(v[2], v[2])));
@@ -100,7 +106,7 @@ __global__ void k_pairs(XrWork w, XrFF ff) {
   if (w.pgrad && taper != 0.0) {
     // dE/d(D, alpha, r_vdW, gamma_w) of this pair's tapered vdW term (and the inner core's)
     const double rvdw = pair_prm(ff, pt, P_RVDW);
-    double* gp = w.pgrad + (size_t)pt * XR_NPAIR_COLS;
+    double* gp = xr_pgrad(w, i) + (size_t)pt * XR_NPAIR_COLS;
     const double m = taper * D * (2 * ev - 2) * ev;  // dE/d(log ev) per unit of the exponent's argument
     atomicAdd(gp + P_D, taper * (ev * ev - 2 * ev));
     atomicAdd(gp + P_ALPHA, m * 0.5 * (1 - f13 / rvdw));
@@ -536,7 +542,7 @@ struct QeqMatrix {
 // Per iteration: one product and two team-wide reductions. Returns the iterations taken, or -1
 // when a team barrier gave up.
 template <class Team, class T>
-__device__ int qeq_cg(const XrWork& w, const XrFF& ff, const Team& team, QeqShared& sh, int a0, int n, int r0,
+__device__ int qeq_cg(const XrWork& w, const double* atab, const Team& team, QeqShared& sh, int a0, int n, int r0,
                       int r1, QeqVecs<T> v, const QeqMatrix<T>& M, double s1, double gz_start, double stop,
                       double gfloor, int max_it, bool flag_limit, int& slot) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -562,7 +568,7 @@ __device__ int qeq_cg(const XrWork& w, const XrFF& ff, const Team& team, QeqShar
     R.hp[lane] = T(0);
     R.di[lane] = T(di);
     R.c[lane] = T(Cr[a]);
-    R.eta_di[lane] = T(atom_prm(ff, w.type[a], A_ETA) * di);
+    R.eta_di[lane] = T(atom_prm(atab, w.type[a], A_ETA) * di);
     R.g[lane] = v.g[a];
   }
   __syncthreads();
@@ -615,7 +621,7 @@ __device__ int qeq_cg(const XrWork& w, const XrFF& ff, const Team& team, QeqShar
         T h = (part4[0][lane] + part4[1][lane]) + (part4[2][lane] + part4[3][lane]);
         const T ga = row_smem ? R.g[lane] : (M.gstage ? M.gstage[rr] : G[a]);
         const T di = row_smem ? R.di[lane] : (v.di ? v.di[a] : T(DI[a]));
-        const T etadi = row_smem ? R.eta_di[lane] : (v.etadi ? v.etadi[a] : T(atom_prm(ff, w.type[a], A_ETA) * DI[a]));
+        const T etadi = row_smem ? R.eta_di[lane] : (v.etadi ? v.etadi[a] : T(atom_prm(atab, w.type[a], A_ETA) * DI[a]));
         const T cr = row_smem ? R.c[lane] : (v.c ? v.c[a] : T(Cr[a]));
         const T p_old = row_smem ? R.p[lane] : v.p[a];
         const T hp_old = row_smem ? R.hp[lane] : v.hp[a];
@@ -832,7 +838,7 @@ __host__ __device__ constexpr size_t rows32_bytes(int n, int m) {
 // row starts, s1 = <1, w> (team total, into sh.sd_s1w) and c = H w. Returns false when a team
 // exchange gave up.
 template <class Team>
-__device__ __noinline__ bool qeq_rows32_setup(const XrWork& w, const XrFF& ff, const Team& team, QeqShared& sh, int a0,
+__device__ __noinline__ bool qeq_rows32_setup(const XrWork& w, const double* atab, const Team& team, QeqShared& sh, int a0,
                                               int n, int r0, int r1, const QeqMatrix<float>& M, float* gyt) {
   extern __shared__ __align__(16) unsigned char qeq_dyn[];
   constexpr bool kCluster = std::is_same<Team, ClusterTeam>::value;
@@ -964,7 +970,7 @@ __device__ __noinline__ bool qeq_rows32_setup(const XrWork& w, const XrFF& ff, c
     }
     R.wv[i] = wsum;
     R.dd[i] = float(1.0 / di);
-    R.etadi[i] = float(atom_prm(ff, w.type[a], A_ETA) * di);
+    R.etadi[i] = float(atom_prm(atab, w.type[a], A_ETA) * di);
     R.rp[i] = w.cnt[a] - M.ebeg;
     s1[0] += double(wsum);
   }
@@ -1177,7 +1183,7 @@ __device__ __noinline__ int qeq_cg_rows32(const XrWork& w, const Team& team, Qeq
 // sum q = Q: g = H x + chi, lambda = <D^-1, g> / <D^-1, 1>, G = g - lambda, and its norm
 // <D^-1, G^2> (from the projected values, so free of cancellation). Two team reductions.
 template <class Team>
-__device__ bool qeq_residual(const XrWork& w, const XrFF& ff, const Team& team, QeqShared& sh, int a0, int r0, int r1,
+__device__ bool qeq_residual(const XrWork& w, const double* atab, const Team& team, QeqShared& sh, int a0, int r0, int r1,
                              double s1, double target, double* gz_out, int& slot, bool adjoint) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   double* X = &QW(Q_X, 0);
@@ -1212,7 +1218,7 @@ __device__ bool qeq_residual(const XrWork& w, const XrFF& ff, const Team& team, 
   __syncthreads();
   for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
     const int a = a0 + r, t = w.type[a];
-    const double g = G[a] + atom_prm(ff, t, A_ETA) * X[a] + (adjoint ? w.qrhs[a] : atom_prm(ff, t, A_CHI));
+    const double g = G[a] + atom_prm(atab, t, A_ETA) * X[a] + (adjoint ? w.qrhs[a] : atom_prm(atab, t, A_CHI));
     G[a] = g;
     acc[0] += DI[a] * g;
   }
@@ -1255,7 +1261,7 @@ __device__ bool qeq_residual(const XrWork& w, const XrFF& ff, const Team& team, 
 // When `cache_j` is non-null the block's matrix rows are kept in shared memory (FP32 in the mixed
 // mode, else FP64); when `gstage` is non-null the whole gradient is staged in shared memory.
 template <class Team>
-__device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int a0, int n, int r0, int r1,
+__device__ void qeq_solve(const XrWork& w, const double* atab, const Team& team, int a0, int n, int r0, int r1,
                           double Q, bool warm, QeqShared& sh, unsigned char* dyn, int dyn_bytes, bool adjoint) {
   double* smem = sh.red;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -1330,7 +1336,7 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
   __syncthreads();
   for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
     const int a = a0 + r;
-    const double di = 1.0 / (atom_prm(ff, w.type[a], A_ETA) + DI[a]);
+    const double di = 1.0 / (atom_prm(atab, w.type[a], A_ETA) + DI[a]);
     DI[a] = di;
     F[5 * w.A + a] = float(di);
     X[a] = warm ? w.qguess[a] : x0;
@@ -1433,7 +1439,7 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
   double acc[5] = {0, 0, 0, 0, 0};
   for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
     const int a = a0 + r, t = w.type[a];
-    const double eta = atom_prm(ff, t, A_ETA), di = DI[a], chi = adjoint ? w.qrhs[a] : atom_prm(ff, t, A_CHI);
+    const double eta = atom_prm(atab, t, A_ETA), di = DI[a], chi = adjoint ? w.qrhs[a] : atom_prm(atab, t, A_CHI);
     const double gu = need_rs ? x0 * (QW(Q_HP, a) + eta) + chi : chi;
     const double g = warm ? G[a] + eta * X[a] + chi : gu;
     if (need_cs) Cr[a] = Cr[a] + eta * di;
@@ -1490,12 +1496,12 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
     for (int r = r0 + threadIdx.x; r < r1 && !small_rows; r += blockDim.x) {
       const int a = a0 + r;
       F[5 * A + a] = float(DI[a]);
-      F[6 * A + a] = float(atom_prm(ff, w.type[a], A_ETA) * DI[a]);
+      F[6 * A + a] = float(atom_prm(atab, w.type[a], A_ETA) * DI[a]);
       F[7 * A + a] = float(Cr[a]);
     }
     QeqMatrix<float> M32{reinterpret_cast<const float*>(cache_h), cache_j, true, true, ebeg,
                          reinterpret_cast<float*>(gstage)};
-    if (small_rows && gz > target && gz > gfloor && n >= 2 && !qeq_rows32_setup(w, ff, team, sh, a0, n, r0, r1, M32, v32.g))
+    if (small_rows && gz > target && gz > gfloor && n >= 2 && !qeq_rows32_setup(w, atab, team, sh, a0, n, r0, r1, M32, v32.g))
       return;
     for (int sweep = 0; sweep < 8; ++sweep) {
       if (!(gz > target) || !(gz > gfloor) || n < 2) break;
@@ -1516,7 +1522,7 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
       // the correction's own projected norm starts at gz; 1e-10 of it (1e-5 in norm) per sweep,
       // and no further than a hundredth of the final target (sd_ratio: that stop over gz)
       const int it = small_rows ? qeq_cg_rows32(w, team, sh, a0, n, r0, r1, M32, v32.y, sh.sd_ratio, budget, v32.g, &slot)
-                                : qeq_cg<Team, float>(w, ff, team, sh, a0, n, r0, r1, v32, M32, s1, gz,
+                                : qeq_cg<Team, float>(w, atab, team, sh, a0, n, r0, r1, v32, M32, s1, gz,
                                                       fmax(1e-10 * gz, 0.01 * target), 0.0, budget, false, slot);
       if (it < 0) return;
       iters += it;
@@ -1536,7 +1542,7 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
       for (int r = r0 + threadIdx.x; r < r1; r += blockDim.x) X[a0 + r] += shift;
       if (!team.sync(w)) return;
       double gz_new = 0.0;
-      if (!qeq_residual(w, ff, team, sh, a0, r0, r1, s1, target, &gz_new, slot, adjoint)) return;
+      if (!qeq_residual(w, atab, team, sh, a0, r0, r1, s1, target, &gz_new, slot, adjoint)) return;
       const bool stalled = gz_new > 1e-3 * gz;
       gz = gz_new;
       if (stalled && gz > target) {
@@ -1555,7 +1561,7 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
         if (r < r1)
           for (int e = w.cnt[a] + sub; e < w.cnt[a + 1]; e += gs) cs += w.hval[e] * __ldcg(DI + w.edge[e].x);
         for (int o = gs / 2; o > 0; o >>= 1) cs += __shfl_xor_sync(0xffffffffu, cs, o);
-        if (sub == 0 && r < r1) Cr[a] = cs + atom_prm(ff, w.type[a], A_ETA) * DI[a];
+        if (sub == 0 && r < r1) Cr[a] = cs + atom_prm(atab, w.type[a], A_ETA) * DI[a];
       }
       __syncthreads();
     }
@@ -1568,7 +1574,7 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
     }
     __syncthreads();
     // what the FP32 sweeps left of the iteration limit (none: the limit is flagged unless converged)
-    const int it = qeq_cg<Team, double>(w, ff, team, sh, a0, n, r0, r1, v64, M64, s1, gz, target, gfloor,
+    const int it = qeq_cg<Team, double>(w, atab, team, sh, a0, n, r0, r1, v64, M64, s1, gz, target, gfloor,
                                         max(0, w.cg_max_iter - iters), true, slot);
     if (it < 0) return;
     iters += it;
@@ -1592,7 +1598,7 @@ __device__ void qeq_solve(const XrWork& w, const XrFF& ff, const Team& team, int
     }
     w.q[a] = q;
     const int t = w.type[a];
-    AEV(6, a) = SELF_CONVERSION * (atom_prm(ff, t, A_CHI) * q + 0.5 * atom_prm(ff, t, A_ETA) * q * q);
+    AEV(6, a) = SELF_CONVERSION * (atom_prm(atab, t, A_CHI) * q + 0.5 * atom_prm(atab, t, A_ETA) * q * q);
   }
 }
 
@@ -1612,7 +1618,7 @@ __device__ void qeq_small_systems(const XrWork& w, const XrFF& ff, const int* sm
     if (k >= nsmall) return;
     const XrSystem& S = w.sys[small[k]];
     BlockTeam team;
-    qeq_solve(w, ff, team, S.atom_off, S.natoms, 0, S.natoms, adjoint ? 0.0 : S.total_charge,
+    qeq_solve(w, atoms_of_system(ff, S), team, S.atom_off, S.natoms, 0, S.natoms, adjoint ? 0.0 : S.total_charge,
               !adjoint && S.has_guess != 0, sh, dyn, kQeqMaxDyn, adjoint != 0);
     __syncthreads();
   }
@@ -1633,8 +1639,8 @@ __global__ void __launch_bounds__(1024, 1) k_qeq_grid(XrWork w, XrFF ff, const i
     const int per = ((S.natoms + m.z - 1) / m.z + 31) / 32 * 32;
     const int r0 = min(S.natoms, m.y * per), r1 = min(S.natoms, r0 + per);
     GridTeam team{w.barrier + m.w, w.red + (size_t)32 * m.w, m.z, m.y};
-    qeq_solve(w, ff, team, S.atom_off, S.natoms, r0, r1, adjoint ? 0.0 : S.total_charge, !adjoint && S.has_guess != 0,
-              sh, dyn, kQeqMaxDyn, adjoint != 0);
+    qeq_solve(w, atoms_of_system(ff, S), team, S.atom_off, S.natoms, r0, r1, adjoint ? 0.0 : S.total_charge,
+              !adjoint && S.has_guess != 0, sh, dyn, kQeqMaxDyn, adjoint != 0);
     __syncthreads();
   }
   qeq_small_systems(w, ff, small, nsmall, w.barrier + nteam, adjoint, sh, dyn);
@@ -1679,8 +1685,8 @@ __global__ void __launch_bounds__(1024, 1) k_qeq_cluster(XrWork w, XrFF ff, cons
       return q == (int)nb ? S.natoms : lo;
     };
     const int r0 = split((int)rank), r1 = split((int)rank + 1);
-    qeq_solve(w, ff, team, S.atom_off, S.natoms, r0, r1, adjoint ? 0.0 : S.total_charge, !adjoint && S.has_guess != 0,
-              sh, dyn, kQeqMaxDyn, adjoint != 0);
+    qeq_solve(w, atoms_of_system(ff, S), team, S.atom_off, S.natoms, r0, r1, adjoint ? 0.0 : S.total_charge,
+              !adjoint && S.has_guess != 0, sh, dyn, kQeqMaxDyn, adjoint != 0);
     __syncthreads();
     if (*(volatile int*)w.status & XR_S_BARRIER) break;
   }
@@ -1693,7 +1699,7 @@ __global__ void __launch_bounds__(1024, 1) k_qeq_block(XrWork w, XrFF ff, int ad
   __shared__ QeqShared sh;
   const XrSystem& S = w.sys[blockIdx.x];
   BlockTeam team;
-  qeq_solve(w, ff, team, S.atom_off, S.natoms, 0, S.natoms, adjoint ? 0.0 : S.total_charge,
+  qeq_solve(w, atoms_of_system(ff, S), team, S.atom_off, S.natoms, 0, S.natoms, adjoint ? 0.0 : S.total_charge,
             !adjoint && S.has_guess != 0, sh, nullptr, 0, adjoint != 0);
 }
 
@@ -1783,12 +1789,13 @@ __global__ void k_energy_gather(XrWork w) {
 __global__ void k_reduce_chunk(XrWork w, XrFF ff) {
   __shared__ double smem[XR_PART_N * 32];
   const int4 ch = w.chunks[blockIdx.x];
+  const double* atab = atoms_of_system(ff, w.sys[ch.x]);
   double v[XR_PART_N];
   for (int k = 0; k < XR_PART_N; ++k) v[k] = 0.0;
   double finite = 1.0;
   for (int a = ch.y + threadIdx.x; a < ch.z; a += blockDim.x) {
     for (int k = 0; k < XR_NCOMP; ++k) v[k] += ESUM(k, a);
-    const double m = atom_prm(ff, w.type[a], A_MASS);
+    const double m = atom_prm(atab, w.type[a], A_MASS);
     const double4_32a x = w.x[a];
     const double q = w.q[a];
     v[14] += m;
@@ -1862,7 +1869,8 @@ __global__ void k_qeq_rhs(XrWork w, XrFF ff) {
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
   if (lane == 0) {
     const int t = w.type[a];
-    const double dEdq = C_ELE * s + SELF_CONVERSION * (atom_prm(ff, t, A_CHI) + atom_prm(ff, t, A_ETA) * w.q[a]);
+    const double* atab = atoms_of_system(ff, w.sys[w.sys_of[a]]);
+    const double dEdq = C_ELE * s + SELF_CONVERSION * (atom_prm(atab, t, A_CHI) + atom_prm(atab, t, A_ETA) * w.q[a]);
     w.qrhs[a] = -dEdq;
   }
 }

@@ -381,17 +381,21 @@ class ForceField:
             k = (pos[a] * T + pos[b]) * T + pos[c]
             angle_index[k] = (len(angle_rows), len(records))
             angle_rows.extend(records)
+        # torsion records in dict order; only those with a nonzero V1, V2, V3 or V_conj get a row
         torsion_index = np.full(T**4, -1, dtype=np.int32)
-        torsion_rows = []
-        for (a, b, c, d), prm in self.torsions.items():
-            if np.any(np.asarray(prm)[[0, 1, 2, 4]] != 0):
-                torsion_index[((pos[a] * T + pos[b]) * T + pos[c]) * T + pos[d]] = len(torsion_rows)
-                torsion_rows.append(prm)
+        torsion_rows = np.zeros((0, 5))
+        if self.torsions:
+            vals = np.array([np.asarray(v, dtype=np.float64).reshape(5) for v in self.torsions.values()])
+            where = np.array([((pos[a] * T + pos[b]) * T + pos[c]) * T + pos[d] for a, b, c, d in self.torsions])
+            keep = np.any(vals[:, [0, 1, 2, 4]] != 0, axis=1)
+            torsion_index[where[keep]] = np.arange(int(keep.sum()), dtype=np.int32)
+            torsion_rows = vals[keep]
         hbond_index = np.full(T**3, -1, dtype=np.int32)
-        hbond_rows = []
-        for (a, b, c), prm in self.hydrogen_bonds.items():
-            hbond_index[(pos[a] * T + pos[b]) * T + pos[c]] = len(hbond_rows)
-            hbond_rows.append(prm)
+        hbond_rows = np.zeros((0, 4))
+        if self.hydrogen_bonds:
+            hbond_rows = np.array([np.asarray(v, dtype=np.float64).reshape(4) for v in self.hydrogen_bonds.values()])
+            where = np.array([(pos[a] * T + pos[b]) * T + pos[c] for a, b, c in self.hydrogen_bonds])
+            hbond_index[where] = np.arange(len(where), dtype=np.int32)
         return dict(
             general=np.ascontiguousarray(self.general, dtype=np.float64),
             atom=np.ascontiguousarray(atom),
