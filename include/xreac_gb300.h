@@ -178,9 +178,16 @@ int xr_neighbors_check(int natoms, const int* pbc, const xr_neighbors* nb, char*
  * current value, drops the kept list. */
 int xr_ctx_set_skin(xr_ctx* ctx, double skin);
 
+/* Cell-list neighbour search (no reference counterpart; xreac enumerates every atom pair over the
+ * replicated images, src/xreac/neighbors.py:17-53). mode 0 (the default) uses it for a call whose
+ * largest system has at least 1,024 atoms when it halves the expected image tests; 1 always; -1
+ * never. Either way the list is the image scan's, in the same canonical order: the cell search
+ * yields the same candidate images, each row is then sorted. */
+int xr_ctx_set_cell_list(xr_ctx* ctx, int mode);
+
 /* How the last call got its neighbour rows (mode: 0 image scan, 1 skin list built, 2 skin list
- * reused, 3 supplied list) and how many skin lists the context has built (no reference counterpart;
- * instrumentation). */
+ * reused, 3 supplied list, 4 cell-list search, 5 skin list built from the cell list) and how many
+ * skin lists the context has built (no reference counterpart; instrumentation). */
 int xr_last_list_info(const xr_ctx* ctx, int* mode, long long* builds);
 
 /* Evaluate nsys independent systems in one ragged batch with per-system offsets. */

@@ -51,6 +51,7 @@ EXPORTED = (
     "xr_eval_neighbors",
     "xr_neighbors_check",
     "xr_ctx_set_skin",
+    "xr_ctx_set_cell_list",
     "xr_last_list_info",
     "xr_get_neighbors",
     "xr_get_bonds",
@@ -164,6 +165,8 @@ def load():
     lib.xr_neighbors_check.restype = c_int
     lib.xr_ctx_set_skin.argtypes = [c_void_p, c_double]
     lib.xr_ctx_set_skin.restype = c_int
+    lib.xr_ctx_set_cell_list.argtypes = [c_void_p, c_int]
+    lib.xr_ctx_set_cell_list.restype = c_int
     lib.xr_last_list_info.argtypes = [c_void_p, POINTER(c_int), POINTER(c_longlong)]
     lib.xr_last_list_info.restype = c_int
     lib.xr_get_neighbors.argtypes = [c_void_p, c_int, POINTER(c_int), POINTER(c_int), POINTER(c_int), c_longlong,

@@ -363,12 +363,22 @@ class Calculator:
         return getattr(self, "_skin", 0.0)
 
     def list_info(self):
-        """(how the last call got its neighbour rows: "scan", "built", "reused" or "supplied", skin
-        lists built so far)."""
+        """(how the last call got its neighbour rows: "scan", "built", "reused", "supplied", "cells"
+        (a cell-list search) or "built-cells" (a skin list built from the cell list), skin lists built
+        so far)."""
         mode = nat.c_int()
         builds = nat.c_longlong()
         self._lib.xr_last_list_info(self._ctx.handle, nat.byref(mode), nat.byref(builds))
-        return ("scan", "built", "reused", "supplied")[mode.value], int(builds.value)
+        return ("scan", "built", "reused", "supplied", "cells", "built-cells")[mode.value], int(builds.value)
+
+    def set_cell_list(self, enabled=None):
+        """Neighbour search by cell list (``xr_ctx_set_cell_list``, an extension): None chooses per
+        call (large systems where it halves the image tests), True always, False never. The list and
+        the results are the same either way."""
+        mode = 0 if enabled is None else (1 if enabled else -1)
+        if enabled is not None and not isinstance(enabled, bool):
+            raise ValueError("enabled must be None, True or False")
+        self._lib.xr_ctx_set_cell_list(self._ctx.handle, mode)
 
     def set_wait_test(self, polls=0, fail_at=0):
         """For tests of the QEq solver's failure path (``xr_ctx_set_wait_test``): ``polls`` > 0

@@ -85,6 +85,15 @@ struct XrSystem {
   double total_charge;
   int has_guess;         // QEq starts from w.qguess (charges of an earlier step) instead of Q/n
   int ff_set;            // parameter set of the force field this system is evaluated with
+  // Cell list (when the call bins its atoms): cells per lattice direction (0: not binned), cell
+  // offsets searched per direction, the system's first cell in the batch's cell arrays, and the map
+  // of a fractional coordinate f to its cell, floor((f - cell_f0) * cell_scale) (wrapped f in
+  // periodic directions, where cell_f0 = 0 and cell_scale = cells).
+  int cell_n[3];
+  int cell_reach[3];
+  int cell_base;
+  double cell_f0[3];
+  double cell_scale[3];
   double rc, rc2, bond_cut, hb_cut;     // cutoff, cutoff^2, min(5, rc), min(7.5, rc)
   double inv_rc;                        // 1 / rc
   float cellf[9];
@@ -135,7 +144,8 @@ struct XrWork {
   int wait_fail_at;
   const XrSystem* sys;
   int* status;                // one int of XR_S_* bits
-  int* counts;                // [8]: E, P, B, D totals (last entries of the scans), [4] QEq iterations, [5] candidates
+  int* counts;                // [8]: E, P, B, D totals (last entries of the scans), [4] QEq iterations, [5] candidates,
+                              // [6] the longest candidate row of a cell-list build, [7] binned atoms
   // atoms
   const double4_32a* x;           // positions (w unused)
   const int* type;
@@ -149,6 +159,13 @@ struct XrWork {
   // list kept from an earlier call, or a caller-supplied list); CSR by cand_cnt [A+1]
   int* cand_cnt;
   int2* cand_edge;
+  // cell list of the call's atoms: atom_cell [A] (global cell index, -1 unbinned), atom_slot [A], the
+  // cells' atom ranges cell_cnt [ncells + 1] (counts, then their exclusive scan) and cell_atoms [A]
+  int* atom_cell;
+  int* atom_slot;
+  int* cell_cnt;
+  int* cell_atoms;
+  int ncells;
   // edges
   int2* edge;                 // {j, code}
   int* edge_pair;             // pair id of every edge (its own or its reverse's)
@@ -283,6 +300,16 @@ void xr_launch_candidates(const XrWork& w, bool fill, cudaStream_t st);
 // The edges within the cutoff of the candidate list: fill=false counts into cnt (scanned by
 // xr_launch_scan), fill=true writes the rows, pairs and bonds.
 void xr_launch_filter(const XrWork& w, bool fill, cudaStream_t st);
+// Cell list of the atoms binned by k_prep (atom_cell): counts per cell, their scan, cell_atoms.
+void xr_launch_cells(const XrWork& w, cudaStream_t st);
+// Candidate list at the cutoff of w.sys from the cell list, in no particular order within a row:
+// fill=false counts into cand_cnt, scans it (total into counts[5]) and records the longest row in
+// counts[6]; fill=true writes cand_edge.
+void xr_launch_cell_candidates(const XrWork& w, bool fill, cudaStream_t st);
+// Sorts every candidate row into canonical (j, Sx, Sy, Sz) order; rows hold at most max_row entries
+// (at most XR_ROW_SORT_MAX).
+void xr_launch_row_sort(const XrWork& w, int max_row, cudaStream_t st);
+#define XR_ROW_SORT_MAX 8192
 void xr_launch_reverse(const XrWork& w, cudaStream_t st);
 void xr_launch_pairs(const XrWork& w, const XrFF& ff, cudaStream_t st);
 int xr_launch_qeq(const XrWork& w, const XrFF& ff, cudaStream_t st, int nblocks, const int4* map, int nteam,

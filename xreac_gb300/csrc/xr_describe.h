@@ -125,4 +125,66 @@ inline int describe_system(const xr_system& in, int atom_off, double rc, XrSyste
   return XR_OK;
 }
 
+// Cell grid of system S (already described) for a search within rl: cells at least rl / 2 high
+// along each lattice direction (coarser where that would exceed max_cells cells), the cell offsets a
+// search must visit, and the map from fractional coordinates to cells (wrapped coordinates in
+// periodic directions; the range of the positions, from x, in the others). Fills S.cell_n,
+// S.cell_reach, S.cell_f0 and S.cell_scale (S.cell_base is the caller's). Returns the number of cells
+// and, in *visits, the expected image tests per atom pair of the system relative to the image scan
+// (the fraction of the system's cells a search visits, over the scan's images per pair).
+inline long long cell_grid(XrSystem& S, const double4_32a* x, int natoms, double rl, long long max_cells,
+                           double* visits) {
+  double h[3], fmin[3] = {0, 0, 0}, fmax[3] = {0, 0, 0};
+  for (int k = 0; k < 3; ++k)
+    h[k] = 1.0 / std::sqrt(S.inv[k] * S.inv[k] + S.inv[3 + k] * S.inv[3 + k] + S.inv[6 + k] * S.inv[6 + k]);
+  for (int k = 0; k < 3; ++k) {
+    if (S.periodic[k]) continue;
+    double lo = INFINITY, hi = -INFINITY;
+    for (int a = 0; a < natoms; ++a) {
+      const double f = x[a].x * S.inv[k] + x[a].y * S.inv[3 + k] + x[a].z * S.inv[6 + k];
+      lo = std::min(lo, f);
+      hi = std::max(hi, f);
+    }
+    fmin[k] = lo;
+    fmax[k] = hi;
+  }
+  double grow = 1.0;  // cell height multiplier, raised until the grid fits max_cells
+  long long total = 1;
+  for (int attempt = 0; attempt < 200; ++attempt) {
+    total = 1;
+    for (int k = 0; k < 3; ++k) {
+      const double height = 0.5 * rl * grow;  // target cell height (A)
+      if (S.periodic[k]) {
+        const int n = std::max(1, (int)std::min(std::floor(h[k] / height), 1.0e6));
+        S.cell_n[k] = n;
+        S.cell_scale[k] = n;
+        S.cell_f0[k] = 0.0;
+      } else {
+        // cells slightly wider than the target, so that the reach below is not one cell more by rounding
+        const double wf = height / h[k] * (1.0 + 1e-6);
+        const double f0 = fmin[k] - 1e-3 * wf;
+        const double span = std::max(fmax[k] - f0, 0.0);
+        const int n = (int)std::min(std::floor(span / wf) + 1.0, 1.0e6);
+        S.cell_n[k] = n;
+        S.cell_scale[k] = 1.0 / wf;
+        S.cell_f0[k] = f0;
+      }
+      total *= S.cell_n[k];
+    }
+    if (total <= max_cells) break;
+    grow *= 1.25;
+  }
+  double frac = 1.0;
+  for (int k = 0; k < 3; ++k) {
+    // an image within rl differs by at most rl / h_k in fractional coordinate k
+    const double span = rl / h[k] * S.cell_scale[k] * (1.0 + 1e-9);
+    S.cell_reach[k] = (int)std::min(std::ceil(span), 1.0e6);
+    const int visited = 2 * S.cell_reach[k] + 1;
+    frac *= (S.periodic[k] ? (double)visited : (double)std::min(visited, S.cell_n[k])) / S.cell_n[k];
+    frac /= (2.0 * S.reach[k] + 1.0);
+  }
+  *visits = frac;
+  return total;
+}
+
 }  // namespace xr_host

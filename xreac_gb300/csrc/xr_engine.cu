@@ -78,6 +78,16 @@ struct xr_ctx {
   size_t ch_cand_edge = 0;
   XrSystem* h_sys_list = nullptr;
   size_t ch_sys_list = 0;
+  // Cell list (xr_ctx_set_cell_list): 0 chooses per call, 1 always, -1 never.
+  int cell_mode = 0;
+  int* atom_cell = nullptr;
+  size_t catom_cell = 0;
+  int* atom_slot = nullptr;
+  size_t catom_slot = 0;
+  int* cell_cnt = nullptr;
+  size_t ccell_cnt = 0;
+  int* cell_atoms = nullptr;
+  size_t ccell_atoms = 0;
   // Skin reuse (xr_ctx_set_skin): the list of the last call is reused by a call on the same systems
   // (atom counts, types, cells, pbc, cutoff) in which no atom moved more than `skin` from where it was
   // when the list was built; the list holds every image within rc + 2 skin then (ASE's convention).
@@ -89,7 +99,8 @@ struct xr_ctx {
   std::vector<int> cache_shape;   // per system: natoms, pbc[3]
   std::vector<double> cache_cell; // per system: 9 cell entries (identity when not periodic)
   long long list_builds = 0;      // candidate lists built since the context was made
-  int list_mode = 0;              // of the last call: 0 scanned, 1 list built, 2 list reused, 3 supplied
+  int list_mode = 0;              // of the last call: 0 scanned, 1 list built, 2 list reused, 3 supplied,
+                                  // 4 cell-list search, 5 list built from the cell list
   int nsm = 0;
   int coop_per_sm = 0;
   int max_clusters = 0;  // resident thread-block clusters of the cluster QEq solver (0: unavailable),
@@ -697,7 +708,51 @@ void keep_skin_list(xr_ctx* c, int nsys, int A, double rc) {
   c->cache_valid = true;
 }
 
-enum ListMode { kScan = 0, kBuild = 1, kReuse = 2, kSupplied = 3 };
+enum ListMode { kScan = 0, kBuild = 1, kReuse = 2, kSupplied = 3, kCell = 4 };
+
+// Cell-list choice of a call whose list comes from a search (an image scan, or a skin-list build at
+// rl): per system, the grid of cell_grid stored in both descriptor sets; used when the searches'
+// expected image tests fall below half of the image scan's (or when the context forces it).
+// Systems smaller than kCellMinAtoms cost little either way. Returns the batch's number of cells
+// (0: no cell list).
+constexpr int kCellMinAtoms = 1024;
+
+long long plan_cells(xr_ctx* c, int nsys, const xr_system* sys, double rl, XrSystem* list_desc) {
+  if (c->cell_mode < 0) return 0;
+  double scan = 0.0, cells = 0.0;
+  long long total = 0;
+  int largest = 0;
+  for (int s = 0, o = 0; s < nsys; o += sys[s].natoms, ++s) {
+    XrSystem& S = list_desc ? list_desc[s] : c->host_sys[s];
+    const int n = sys[s].natoms;
+    largest = std::max(largest, n);
+    double visits = 1.0;
+    const long long nc = xr_host::cell_grid(S, c->h_x + o, n, rl, std::max<long long>(64, 2ll * n), &visits);
+    S.cell_base = (int)total;
+    total += nc;
+    double images = 1.0;
+    for (int k = 0; k < 3; ++k) images *= 2.0 * S.reach[k] + 1.0;
+    scan += (double)n * n * images;
+    cells += (double)n * n * images * visits + 64.0 * n;  // plus the row sort
+    if (total > (1ll << 30)) return 0;
+  }
+  const bool use = c->cell_mode > 0 || (largest >= kCellMinAtoms && cells < 0.5 * scan);
+  for (int s = 0; s < nsys; ++s) {
+    XrSystem& S = list_desc ? list_desc[s] : c->host_sys[s];
+    if (!use) S.cell_n[0] = S.cell_n[1] = S.cell_n[2] = 0;
+    if (list_desc) {  // k_prep bins with the main descriptors: the same grid in both sets
+      XrSystem& M = c->host_sys[s];
+      for (int k = 0; k < 3; ++k) {
+        M.cell_n[k] = S.cell_n[k];
+        M.cell_reach[k] = S.cell_reach[k];
+        M.cell_f0[k] = S.cell_f0[k];
+        M.cell_scale[k] = S.cell_scale[k];
+      }
+      M.cell_base = S.cell_base;
+    }
+  }
+  return use ? total : 0;
+}
 
 int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsigned flags, xr_result* out,
               const xr_neighbors* nb = nullptr, const int* sets = nullptr) {
@@ -845,6 +900,17 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
       c->cache_valid = false;  // rebuilt below
     }
   }
+  long long ncells = 0;
+  if (mode == kScan || mode == kBuild) {
+    ncells = plan_cells(c, nsys, sys, mode == kBuild ? rc + 2.0 * c->skin : rc, mode == kBuild ? c->h_sys_list : nullptr);
+    if (ncells > 0) {
+      if (!grow(&c->atom_cell, &c->catom_cell, (size_t)A) || !grow(&c->atom_slot, &c->catom_slot, (size_t)A) ||
+          !grow(&c->cell_atoms, &c->ccell_atoms, (size_t)A) || !grow(&c->cell_cnt, &c->ccell_cnt, (size_t)ncells + 1) ||
+          !grow(&c->cand_cnt, &c->ccand_cnt, (size_t)A + 1))
+        return cuda_fail(c, cudaErrorMemoryAllocation, "allocation");
+      if (mode == kScan) mode = kCell;
+    }
+  }
   size_t nchunk = 0;
   for (int s = 0; s < nsys; ++s) nchunk += (size_t)(sys[s].natoms + XR_CHUNK_ATOMS - 1) / XR_CHUNK_ATOMS;
   if (!host_grow(&c->h_chunks, &c->ch_chunks, nchunk) || !host_grow(&c->h_syschunks, &c->ch_syschunks, (size_t)nsys) ||
@@ -907,8 +973,15 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
     c->pgrad_systems = nsys;
   }
   attach_lists(c, w);
+  if (ncells > 0) {
+    w.atom_cell = c->atom_cell;
+    w.atom_slot = c->atom_slot;
+    w.cell_cnt = c->cell_cnt;
+    w.cell_atoms = c->cell_atoms;
+    w.ncells = (int)ncells;
+  }
   stage(c, 0, st);
-  xr_launch_prep(w, st);
+  xr_launch_prep(w, st);  // also assigns every atom its cell when the call uses the cell list
   launches += 1;
   if (mode == kScan || mode == kSupplied) {
     // the image scan; for a supplied list only its coincident-atom check counts (xreac checks every
@@ -922,28 +995,45 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
     if (m > 0) cudaMemcpyAsync(c->cand_edge, c->h_cand_edge, sizeof(int2) * (size_t)m, cudaMemcpyHostToDevice, st);
     h2d += sizeof(int) * ((long long)A + 1) + sizeof(int2) * m;
   }
-  if (mode == kBuild) {
-    // every image within rc + 2 skin, with the list cutoff's descriptors
-    cudaMemcpyAsync(c->sys_list, c->h_sys_list, sizeof(XrSystem) * nsys, cudaMemcpyHostToDevice, st);
-    cudaMemsetAsync(c->cand_cnt, 0, sizeof(int) * ((size_t)A + 1), st);
-    h2d += sizeof(XrSystem) * (long long)nsys;
+  if (mode == kBuild || mode == kCell) {
+    // every image within the list cutoff (rc + 2 skin for a skin list, with its descriptors; rc for
+    // a cell-list search), from the cell list or the image scan
     XrWork wl = w;
-    wl.sys = c->sys_list;
+    if (mode == kBuild) {
+      cudaMemcpyAsync(c->sys_list, c->h_sys_list, sizeof(XrSystem) * nsys, cudaMemcpyHostToDevice, st);
+      h2d += sizeof(XrSystem) * (long long)nsys;
+      wl.sys = c->sys_list;
+    }
+    cudaMemsetAsync(c->cand_cnt, 0, sizeof(int) * ((size_t)A + 1), st);
     wl.cand_cnt = c->cand_cnt;
-    xr_launch_candidates(wl, false, st);
-    launches += 4;
-    cudaMemcpyAsync(c->h_small + 9, c->counts + 5, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (ncells > 0) {
+      xr_launch_cells(wl, st);
+      xr_launch_cell_candidates(wl, false, st);
+      launches += 8;
+    } else {
+      xr_launch_candidates(wl, false, st);
+      launches += 4;
+    }
+    cudaMemcpyAsync(c->h_small + 9, c->counts + 5, 2 * sizeof(int), cudaMemcpyDeviceToHost, st);
     cudaMemcpyAsync(c->h_small + 4, c->status, sizeof(int), cudaMemcpyDeviceToHost, st);
-    d2h += 2 * sizeof(int);
+    d2h += 3 * sizeof(int);
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(c, e, "neighbour list count");
     if (int code = status_to_code(c, c->h_small[4])) return code;
-    const int m = c->h_small[9];
+    const int m = c->h_small[9], longest = c->h_small[10];
     if (!grow(&c->cand_edge, &c->ccand_edge, std::max<size_t>((size_t)m, 1)))
       return cuda_fail(c, cudaErrorMemoryAllocation, "list allocation");
     wl.cand_edge = w.cand_edge = c->cand_edge;
-    xr_launch_candidates(wl, true, st);
-    launches += 1;
-    ++c->list_builds;
+    if (ncells > 0 && longest <= XR_ROW_SORT_MAX) {
+      xr_launch_cell_candidates(wl, true, st);
+      xr_launch_row_sort(wl, longest, st);
+      launches += 2;
+    } else {
+      // the image scan finds the same candidates (its rows come out in canonical order): used where
+      // a row is too long for the shared-memory sort
+      xr_launch_candidates(wl, true, st);
+      launches += 1;
+    }
+    if (mode == kBuild) ++c->list_builds;
   }
   if (mode != kScan) {
     w.cand_cnt = c->cand_cnt;
@@ -960,7 +1050,7 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
   const int nE = c->h_small[0], nP = c->h_small[1], nB = c->h_small[2], nD = c->h_small[3];
   if (int code = status_to_code(c, c->h_small[4])) return code;
   if (mode == kBuild) keep_skin_list(c, nsys, A, rc);
-  c->list_mode = mode;
+  c->list_mode = mode == kBuild && ncells > 0 ? 5 : (int)mode;
   if (!ensure_lists(c, nE, nP, nB)) return cuda_fail(c, cudaErrorMemoryAllocation, "list allocation");
   attach_lists(c, w);
   w.nE = nE;
@@ -1480,7 +1570,7 @@ void xr_ctx_destroy(xr_ctx* c) {
                   c->bond_i, c->bond_j, c->b_r, c->b_v, c->b_fwd, c->b_adj, c->b_e, c->dbrow, c->sys, c->energy,
                   c->props, c->status, c->counts, c->barrier, c->qmap, c->qsmall, c->qiters, c->red, c->qguess, c->qrhs, c->qadj, c->pgrad, c->bx_meta, c->bx_bo, c->bx_count,
                   c->esum, c->arow, c->nact, c->nzrow, c->nnz, c->chunks, c->sys_chunks, c->chunk_part, c->mids, c->nmids, c->mlist,
-                  c->cand_cnt, c->cand_edge, c->sys_list};
+                  c->cand_cnt, c->cand_edge, c->sys_list, c->atom_cell, c->atom_slot, c->cell_cnt, c->cell_atoms};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (c->h_x) cudaFreeHost(c->h_x);
@@ -1530,6 +1620,12 @@ int xr_ctx_set_skin(xr_ctx* c, double skin) {
   if (!c || !(skin >= 0.0) || !std::isfinite(skin)) return XR_EINPUT;
   c->cache_valid = false;  // setting the skin, even to its current value, drops the kept list
   c->skin = skin;
+  return XR_OK;
+}
+
+int xr_ctx_set_cell_list(xr_ctx* c, int mode) {
+  if (!c || mode < -1 || mode > 1) return XR_EINPUT;
+  c->cell_mode = mode;
   return XR_OK;
 }
 

@@ -37,6 +37,19 @@ __global__ void k_prep(XrWork w) {
   w.wrap[a] = make_int4(wr[0], wr[1], wr[2], 0);
   w.xw[a] = make_float4((float)xw[0], (float)xw[1], (float)xw[2], 0.f);
   w.fw[a] = make_float4((float)f[0], (float)f[1], (float)f[2], 0.f);
+  if (w.atom_cell) {
+    // the cell of the wrapped position, from the same FP64 fractional coordinates as the wrap
+    int cell = -1;
+    if (S.cell_n[0] > 0) {
+      int c[3];
+      for (int k = 0; k < 3; ++k) {
+        const double g = (S.periodic[k] ? f[k] : f[k] - S.cell_f0[k]) * S.cell_scale[k];
+        c[k] = (int)fmin(fmax(floor(g), 0.0), (double)(S.cell_n[k] - 1));
+      }
+      cell = S.cell_base + (c[0] * S.cell_n[1] + c[1]) * S.cell_n[2] + c[2];
+    }
+    w.atom_cell[a] = cell;
+  }
 }
 
 // Exact FP64 edge vector with the reference's association: (x_j - x_i) + S @ cell.
@@ -301,6 +314,136 @@ __global__ void k_candidates(XrWork w) {
   if (!FILL && lane == 0) w.cand_cnt[i] = n_e;
 }
 
+// ------------------------------------------------------------------------------ cell list
+// Atoms binned into the cells k_prep assigned (order within a cell is that of the atomics; rows are
+// sorted afterwards, so results do not depend on it).
+__global__ void k_cell_count(XrWork w) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= w.A) return;
+  const int c = w.atom_cell[a];
+  if (c >= 0) w.atom_slot[a] = atomicAdd(w.cell_cnt + c, 1);
+}
+
+__global__ void k_cell_fill(XrWork w) {
+  const int a = blockIdx.x * blockDim.x + threadIdx.x;
+  if (a >= w.A) return;
+  const int c = w.atom_cell[a];
+  if (c >= 0) w.cell_atoms[w.cell_cnt[c] + w.atom_slot[a]] = a;
+}
+
+__device__ inline int floor_div(int a, int n) { return a >= 0 ? a / n : -((-a + n - 1) / n); }
+
+// Candidate images within the descriptor's cutoff from the cell list: one warp per source atom
+// visits the cells within cell_reach of its own. Any image within the cutoff lies there: its
+// fractional coordinates differ by at most cutoff / h_k (h_k the cell height), which is at most
+// cell_reach cells. For fixed offsets in the first two directions the cells along the third are
+// consecutive in cell_atoms, so their atoms are streamed as one range per image shift and the
+// lanes stay busy however few atoms a cell holds. Each image is visited once: a cell offset fixes
+// the wrapped cell and its shift. FILL=false counts (cand_cnt, and the longest row into counts[6]);
+// FILL=true writes {j, shift bits} in visiting order.
+template <bool FILL>
+__global__ void k_cell_candidates(XrWork w) {
+  const int lane = threadIdx.x & 31;
+  const int i = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
+  if (i >= w.A) return;
+  const XrSystem& S = w.sys[w.sys_of[i]];
+  const float4 pi = w.xw[i];
+  const int4 wi = w.wrap[i];
+  const double4_32a xi = w.x[i];
+  const ScreenConsts K = screen_consts(S);
+  const int n0 = S.cell_n[0], n1 = S.cell_n[1], n2 = S.cell_n[2];
+  const int m0 = S.cell_reach[0], m1 = S.cell_reach[1], m2 = S.cell_reach[2];
+  const bool per0 = S.periodic[0] != 0, per1 = S.periodic[1] != 0, per2 = S.periodic[2] != 0;
+  const int local = w.atom_cell[i] - S.cell_base;
+  const int c2 = local % n2, c1 = (local / n2) % n1, c0 = local / (n1 * n2);
+  const unsigned below = (1u << lane) - 1u;
+  int n_e = FILL ? w.cand_cnt[i] : 0;
+  for (int d0 = -m0; d0 <= m0; ++d0) {
+    int e0 = c0 + d0, s0 = 0;
+    if (per0) {
+      s0 = floor_div(e0, n0);
+      e0 -= s0 * n0;
+    } else if (e0 < 0 || e0 >= n0) {
+      continue;
+    }
+    for (int d1 = -m1; d1 <= m1; ++d1) {
+      int e1 = c1 + d1, s1 = 0;
+      if (per1) {
+        s1 = floor_div(e1, n1);
+        e1 -= s1 * n1;
+      } else if (e1 < 0 || e1 >= n1) {
+        continue;
+      }
+      const int rowbase = S.cell_base + (e0 * n1 + e1) * n2;
+      int lo = c2 - m2, hi = c2 + m2;
+      if (!per2) {
+        lo = max(lo, 0);
+        hi = min(hi, n2 - 1);
+      }
+      for (int e = lo; e <= hi;) {
+        const int s2 = per2 ? floor_div(e, n2) : 0;
+        const int seg_end = per2 ? min(hi, (s2 + 1) * n2 - 1) : hi;
+        const int abeg = w.cell_cnt[rowbase + (e - s2 * n2)], aend = w.cell_cnt[rowbase + (seg_end - s2 * n2) + 1];
+        for (int k0 = abeg; k0 < aend; k0 += 32) {
+          const int k = k0 + lane;
+          int code = 0, j = 0;
+          if (k < aend) {
+            j = w.cell_atoms[k];
+            code = classify(w, S, K, i, j, pi, w.xw[j], wi, w.wrap[j], s0, s1, s2, xi);
+          }
+          const unsigned m = __ballot_sync(0xffffffffu, code != 0);
+          if (FILL && code) w.cand_edge[n_e + __popc(m & below)] = make_int2(j, (int)((uint32_t)code & XR_SHIFT_MASK));
+          n_e += __popc(m);
+        }
+        e = seg_end + 1;
+      }
+    }
+  }
+  if (!FILL && lane == 0) {
+    w.cand_cnt[i] = n_e;
+    atomicMax(w.counts + 6, n_e);
+  }
+}
+
+// One block per candidate row: bitonic sort of the row's keys (j << 27 | shift bits, the canonical
+// order) in shared memory, padded to a power of two.
+__global__ void k_row_sort(XrWork w, int cap) {
+  extern __shared__ unsigned long long keys[];
+  const int i = blockIdx.x;
+  const int beg = w.cand_cnt[i], len = w.cand_cnt[i + 1] - beg;
+  if (len < 2) return;
+  if (len > cap) {  // cannot happen: the host sized the buffer for the longest row
+    if (threadIdx.x == 0) atomicOr(w.status, XR_S_LIMIT);
+    return;
+  }
+  int P = 2;
+  while (P < len) P <<= 1;
+  for (int t = threadIdx.x; t < P; t += blockDim.x) {
+    if (t < len) {
+      const int2 c = w.cand_edge[beg + t];
+      keys[t] = ((unsigned long long)(uint32_t)c.x << 27) | ((uint32_t)c.y & XR_SHIFT_MASK);
+    } else {
+      keys[t] = ~0ull;
+    }
+  }
+  __syncthreads();
+  for (int k = 2; k <= P; k <<= 1)
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int t = threadIdx.x; t < (P >> 1); t += blockDim.x) {
+        const int lo = 2 * t - (t & (j - 1)), hi = lo + j;
+        const bool up = (lo & k) == 0;
+        const unsigned long long a = keys[lo], b = keys[hi];
+        if ((a > b) == up) {
+          keys[lo] = b;
+          keys[hi] = a;
+        }
+      }
+      __syncthreads();
+    }
+  for (int t = threadIdx.x; t < len; t += blockDim.x)
+    w.cand_edge[beg + t] = make_int2((int)(keys[t] >> 27), (int)(keys[t] & XR_SHIFT_MASK));
+}
+
 // The edges within the cutoff of a candidate list (rows of {j, shift bits} in canonical order, a
 // superset of the edges: a skin list of an earlier step, or a caller-supplied list), with their
 // flags, classified exactly as k_neighbors classifies an image. One warp per source atom, 32
@@ -537,6 +680,33 @@ void xr_launch_filter(const XrWork& w, bool fill, cudaStream_t st) {
     k_filter<true><<<blocks, 32 * warps_per_block, 0, st>>>(w);
   else
     k_filter<false><<<blocks, 32 * warps_per_block, 0, st>>>(w);
+}
+
+void xr_launch_cells(const XrWork& w, cudaStream_t st) {
+  cudaMemsetAsync(w.cell_cnt, 0, sizeof(int) * ((size_t)w.ncells + 1), st);
+  k_cell_count<<<(w.A + 255) / 256, 256, 0, st>>>(w);
+  scan_arrays(w.cell_cnt, w.ncells + 1, 1, reinterpret_cast<int*>(w.red), w.counts + 7, st);
+  k_cell_fill<<<(w.A + 255) / 256, 256, 0, st>>>(w);
+}
+
+void xr_launch_cell_candidates(const XrWork& w, bool fill, cudaStream_t st) {
+  const int warps_per_block = 8;
+  const int blocks = (w.A + warps_per_block - 1) / warps_per_block;
+  if (fill) {
+    k_cell_candidates<true><<<blocks, 32 * warps_per_block, 0, st>>>(w);
+  } else {
+    k_cell_candidates<false><<<blocks, 32 * warps_per_block, 0, st>>>(w);
+    scan_arrays(w.cand_cnt, w.A + 1, 1, reinterpret_cast<int*>(w.red), w.counts + 5, st);
+  }
+}
+
+void xr_launch_row_sort(const XrWork& w, int max_row, cudaStream_t st) {
+  int cap = 2;
+  while (cap < max_row) cap <<= 1;
+  if (max_row < 2) return;
+  const size_t bytes = sizeof(unsigned long long) * cap;
+  if (bytes > 48 * 1024) cudaFuncSetAttribute(k_row_sort, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  k_row_sort<<<w.A, 128, bytes, st>>>(w, cap);
 }
 
 void xr_launch_reverse(const XrWork& w, cudaStream_t st) {
