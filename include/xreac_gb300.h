@@ -230,6 +230,16 @@ int xr_get_param_gradient_system(const xr_ctx* ctx, int index, double* pair_grad
  * columns (k < npair) then the angle records, for s in call order; count = systems x (npair + nangle). */
 int xr_get_param_gradient_blocks(const xr_ctx* ctx, double* out, long long count);
 
+/* Device memory of a context (no reference counterpart; for admission by footprint): the bytes its
+ * buffers hold, and their capacities caps[0..n) = atoms, systems, directed edges, pairs, bonds,
+ * candidate edges (a call within them allocates nothing). */
+int xr_ctx_memory(const xr_ctx* ctx, long long* device_bytes, long long* caps, int n);
+
+/* Device bytes a context needs for calls of up to `atoms` atoms in `systems` systems with `edges`
+ * directed edges and `bonds` bond candidates (what xr_ctx_reserve would allocate), or -1 for invalid
+ * sizes. Needs no device. */
+long long xr_footprint_bytes(int atoms, int systems, long long edges, long long bonds);
+
 /* Number of CUDA kernels the last xr_eval / xr_eval_batch call launched. */
 long long xr_last_launches(const xr_ctx* ctx);
 

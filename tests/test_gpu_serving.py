@@ -127,3 +127,40 @@ def test_batches_are_deterministic():
         assert x.energy == y.energy
         np.testing.assert_array_equal(x.charges, y.charges)
         np.testing.assert_allclose(x.forces, y.forces, rtol=1e-13, atol=1e-12)
+
+
+def test_footprint_admission_keeps_dense_periodic_batches_within_the_reservation():
+    """Dense periodic requests (liquid water at 1 g/cm^3, about 400 directed edges per atom) served
+    within a device-memory budget: the contexts' reservations fit the budget, no batch reallocates
+    device memory, and each result equals its evaluation alone."""
+    from xreac_gb300 import Calculator, ForceField, workloads
+    from xreac_gb300.serving import Request, Server, replay
+
+    ff = ForceField.bundled("ffield.reax.HO.2015")
+    boxes = [workloads.water_box(n_mol=100, box=14.42, seed=40 + k) for k in range(12)]
+    reqs = [Request(b.symbols, b.positions, "ff", b.cell, True) for b in boxes]
+    budget = 2 * Calculator.footprint_bytes(1200, 64, 1200 * 450, 1200 * 30)
+    with Server({"ff": ff}, workers=2, max_batch_atoms=8192, max_batch_requests=64, memory_budget=budget) as srv:
+        assert srv.max_batch_atoms <= 1200
+        served, _ = replay(srv, reqs)
+        report = srv.memory_report()
+        batches = list(srv.batches)
+    assert report["reallocations"] == 0
+    assert sum(c["device_bytes"] for c in report["contexts"]) <= budget
+    assert max(b.requests for b in batches) >= 2 and all(b.edges <= 1.25 * b.est_edges for b in batches)
+    alone = Calculator(ff)
+    for req, out in zip(reqs, served):
+        assert not isinstance(out, Exception), out
+        _close(out.evaluation, alone.evaluate(req.symbols, req.positions, cell=req.cell, pbc=True))
+
+
+def test_footprint_bytes_match_a_reservation():
+    from xreac_gb300 import Calculator, ForceField
+
+    calc = Calculator(ForceField.bundled("ffield.reax.HO.2015"))
+    before = calc.memory()["device_bytes"]
+    calc.reserve(4096, 128, edges_per_atom=450, bonds_per_atom=30)
+    m = calc.memory()
+    est = Calculator.footprint_bytes(4096, 128, 4096 * 450, 4096 * 30)
+    assert m["atoms"] >= 4096 and m["systems"] >= 128 and m["edges"] >= 4096 * 450 and m["bonds"] >= 4096 * 30
+    assert 0.8 * est <= m["device_bytes"] - before <= 1.2 * est

@@ -65,6 +65,8 @@ EXPORTED = (
     "xr_get_param_gradient",
     "xr_get_param_gradient_system",
     "xr_get_param_gradient_blocks",
+    "xr_ctx_memory",
+    "xr_footprint_bytes",
     "xr_count_neighbors_static",
     "xr_static_last_error",
 )
@@ -196,6 +198,10 @@ def load():
     lib.xr_get_param_gradient_system.restype = c_int
     lib.xr_get_param_gradient_blocks.argtypes = [c_void_p, POINTER(c_double), c_longlong]
     lib.xr_get_param_gradient_blocks.restype = c_int
+    lib.xr_ctx_memory.argtypes = [c_void_p, POINTER(c_longlong), POINTER(c_longlong), c_int]
+    lib.xr_ctx_memory.restype = c_int
+    lib.xr_footprint_bytes.argtypes = [c_int, c_int, c_longlong, c_longlong]
+    lib.xr_footprint_bytes.restype = c_longlong
     lib.xr_count_neighbors_static.argtypes = [POINTER(System), c_double, c_void_p, POINTER(c_int), POINTER(c_longlong)]
     lib.xr_count_neighbors_static.restype = c_int
     lib.xr_static_last_error.argtypes = []

@@ -854,6 +854,23 @@ class Calculator:
         self._lib.xr_ctx_stage_times(self._ctx.handle, ms, 8, nat.byref(calls))
         return np.array(ms[:8]), int(calls.value)
 
+    def memory(self):
+        """The context's device memory (``xr_ctx_memory``): bytes held and the capacities a call can
+        use without allocating (atoms, systems, directed edges, pairs, bonds, candidate edges)."""
+        b = nat.c_longlong()
+        caps = (nat.c_longlong * 6)()
+        self._lib.xr_ctx_memory(self._ctx.handle, nat.byref(b), caps, 6)
+        names = ("atoms", "systems", "edges", "pairs", "bonds", "candidates")
+        return dict(device_bytes=int(b.value), **{k: int(v) for k, v in zip(names, caps)})
+
+    @staticmethod
+    def footprint_bytes(atoms, systems=1, edges=0, bonds=0):
+        """Device bytes a context needs for calls of up to these sizes (``xr_footprint_bytes``)."""
+        v = nat.load().xr_footprint_bytes(int(atoms), int(systems), int(edges), int(bonds))
+        if v < 0:
+            raise ValueError("atoms and systems must be positive, edges and bonds nonnegative")
+        return int(v)
+
     def list_sizes(self):
         """Sizes of the last call's lists: directed edges, pairs, bond candidates, bond-row entries,
         active bonds, torsion middles (summed over its systems)."""

@@ -78,6 +78,8 @@ struct xr_ctx {
   size_t ch_cand_edge = 0;
   XrSystem* h_sys_list = nullptr;
   size_t ch_sys_list = 0;
+  // Device bytes the context holds (its buffers, as grown; xr_ctx_memory).
+  long long dev_bytes = 0;
   // Cell list (xr_ctx_set_cell_list): 0 chooses per call, 1 always, -1 never.
   int cell_mode = 0;
   int* atom_cell = nullptr;
@@ -266,6 +268,15 @@ struct xr_ctx {
 
 namespace {
 
+// grow() for a context's buffer, keeping the context's device-byte count.
+template <class T>
+bool grow(xr_ctx* c, T** p, size_t* cap, size_t need) {
+  const long long before = *p ? (long long)(*cap * sizeof(T)) : 0;
+  const bool ok = grow(p, cap, need);
+  c->dev_bytes += (*p ? (long long)(*cap * sizeof(T)) : 0) - before;
+  return ok;
+}
+
 int cuda_fail(xr_ctx* c, cudaError_t e, const char* where) {
   c->err = std::string("CUDA error in ") + where + ": " + cudaGetErrorString(e);
   return XR_ECUDA;
@@ -301,7 +312,7 @@ int build_system(xr_ctx* c, const xr_system& in, int atom_off, double rc, XrSyst
 
 #define GROW(field, n)                                      \
   do {                                                      \
-    if (!grow(&c->field, &c->c##field, (size_t)(n))) return false; \
+    if (!grow(c, &c->field, &c->c##field, (size_t)(n))) return false; \
   } while (0)
 
 bool ensure_atoms(xr_ctx* c, int A, int S) {
@@ -337,6 +348,10 @@ bool ensure_atoms(xr_ctx* c, int A, int S) {
   return true;
 }
 
+// Device bytes per bond slot of the bond arrays (structures of arrays with stride capB).
+constexpr long long kBondBytes = 3 * sizeof(int) + 4 * sizeof(double) + (BF_N + BJ_N + 4) * sizeof(double) +
+                                 6 * sizeof(int2) + 2 * sizeof(int);
+
 bool ensure_lists(xr_ctx* c, long long E, long long P, long long B) {
   GROW(edge, E);
   GROW(edge_pair, E);
@@ -357,6 +372,7 @@ bool ensure_lists(xr_ctx* c, long long E, long long P, long long B) {
   if (c->capB < (size_t)B || !c->b_fwd) {
     size_t nb = std::max<size_t>((size_t)B, 1);
     nb = nb + nb / 4 + 64;
+    c->dev_bytes -= (long long)(c->b_fwd ? c->capB : 0) * kBondBytes;
     cudaFree(c->bond_pair);
     cudaFree(c->bond_i);
     cudaFree(c->bond_j);
@@ -392,6 +408,7 @@ bool ensure_lists(xr_ctx* c, long long E, long long P, long long B) {
               cudaMalloc((void**)&c->mlist, nb * sizeof(int)) == cudaSuccess;
     if (!ok) return false;
     c->capB = nb;
+    c->dev_bytes += (long long)nb * kBondBytes;
   }
   return true;
 }
@@ -863,7 +880,7 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
       c->err = msg;
       return code;
     }
-    if (!grow(&c->cand_cnt, &c->ccand_cnt, (size_t)A + 1) || !grow(&c->cand_edge, &c->ccand_edge, std::max<size_t>(rows.size(), 1)) ||
+    if (!grow(c, &c->cand_cnt, &c->ccand_cnt, (size_t)A + 1) || !grow(c, &c->cand_edge, &c->ccand_edge, std::max<size_t>(rows.size(), 1)) ||
         !host_grow(&c->h_cand_cnt, &c->ch_cand_cnt, (size_t)A + 1) ||
         !host_grow(&c->h_cand_edge, &c->ch_cand_edge, std::max<size_t>(rows.size(), 1)))
       return cuda_fail(c, cudaErrorMemoryAllocation, "allocation");
@@ -874,8 +891,8 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
   } else if (c->skin > 0.0) {
     mode = skin_list_valid(c, nsys, A, rc) ? kReuse : kBuild;
     if (mode == kBuild) {
-      if (!host_grow(&c->h_sys_list, &c->ch_sys_list, (size_t)nsys) || !grow(&c->sys_list, &c->csys_list, (size_t)nsys) ||
-          !grow(&c->cand_cnt, &c->ccand_cnt, (size_t)A + 1))
+      if (!host_grow(&c->h_sys_list, &c->ch_sys_list, (size_t)nsys) || !grow(c, &c->sys_list, &c->csys_list, (size_t)nsys) ||
+          !grow(c, &c->cand_cnt, &c->ccand_cnt, (size_t)A + 1))
         return cuda_fail(c, cudaErrorMemoryAllocation, "allocation");
       const double rl = rc + 2.0 * c->skin;
       for (int s = 0, o = 0; s < nsys; o += sys[s].natoms, ++s) {
@@ -904,9 +921,9 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
   if (mode == kScan || mode == kBuild) {
     ncells = plan_cells(c, nsys, sys, mode == kBuild ? rc + 2.0 * c->skin : rc, mode == kBuild ? c->h_sys_list : nullptr);
     if (ncells > 0) {
-      if (!grow(&c->atom_cell, &c->catom_cell, (size_t)A) || !grow(&c->atom_slot, &c->catom_slot, (size_t)A) ||
-          !grow(&c->cell_atoms, &c->ccell_atoms, (size_t)A) || !grow(&c->cell_cnt, &c->ccell_cnt, (size_t)ncells + 1) ||
-          !grow(&c->cand_cnt, &c->ccand_cnt, (size_t)A + 1))
+      if (!grow(c, &c->atom_cell, &c->catom_cell, (size_t)A) || !grow(c, &c->atom_slot, &c->catom_slot, (size_t)A) ||
+          !grow(c, &c->cell_atoms, &c->ccell_atoms, (size_t)A) || !grow(c, &c->cell_cnt, &c->ccell_cnt, (size_t)ncells + 1) ||
+          !grow(c, &c->cand_cnt, &c->ccand_cnt, (size_t)A + 1))
         return cuda_fail(c, cudaErrorMemoryAllocation, "allocation");
       if (mode == kScan) mode = kCell;
     }
@@ -914,7 +931,7 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
   size_t nchunk = 0;
   for (int s = 0; s < nsys; ++s) nchunk += (size_t)(sys[s].natoms + XR_CHUNK_ATOMS - 1) / XR_CHUNK_ATOMS;
   if (!host_grow(&c->h_chunks, &c->ch_chunks, nchunk) || !host_grow(&c->h_syschunks, &c->ch_syschunks, (size_t)nsys) ||
-      !grow(&c->chunks, &c->cchunks, nchunk) || !grow(&c->chunk_part, &c->cchunk_part, nchunk * (size_t)XR_PART_N))
+      !grow(c, &c->chunks, &c->cchunks, nchunk) || !grow(c, &c->chunk_part, &c->cchunk_part, nchunk * (size_t)XR_PART_N))
     return cuda_fail(c, cudaErrorMemoryAllocation, "allocation");
   int4* chunk_tab = c->h_chunks;
   int2* sys_chunk_tab = c->h_syschunks;
@@ -963,7 +980,7 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
     // one gradient block per system: [pair table][angle records]
     const long long np = (long long)ff->d.ntypes * ff->d.ntypes * XR_NPAIR_COLS, na = 7ll * ff->nangle;
     const size_t all = (size_t)(np + na) * nsys;
-    if (!grow(&c->pgrad, &c->cpgrad, all + 1)) return cuda_fail(c, cudaErrorMemoryAllocation, "allocation");
+    if (!grow(c, &c->pgrad, &c->cpgrad, all + 1)) return cuda_fail(c, cudaErrorMemoryAllocation, "allocation");
     cudaMemsetAsync(c->pgrad, 0, sizeof(double) * all, st);
     w.pgrad = c->pgrad;
     w.pgrad_angle_off = (int)np;
@@ -1020,7 +1037,7 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
     if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(c, e, "neighbour list count");
     if (int code = status_to_code(c, c->h_small[4])) return code;
     const int m = c->h_small[9], longest = c->h_small[10];
-    if (!grow(&c->cand_edge, &c->ccand_edge, std::max<size_t>((size_t)m, 1)))
+    if (!grow(c, &c->cand_edge, &c->ccand_edge, std::max<size_t>((size_t)m, 1)))
       return cuda_fail(c, cudaErrorMemoryAllocation, "list allocation");
     wl.cand_edge = w.cand_edge = c->cand_edge;
     if (ncells > 0 && longest <= XR_ROW_SORT_MAX) {
@@ -1120,7 +1137,7 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
   launches += 1;
   xr_launch_reduce(w, ff->d, st);
   launches += 3;
-  if (!grow(&c->bx_meta, &c->cbx_meta, (size_t)std::max(nB, 1)) || !grow(&c->bx_bo, &c->cbx_bo, (size_t)std::max(nB, 1)))
+  if (!grow(c, &c->bx_meta, &c->cbx_meta, (size_t)std::max(nB, 1)) || !grow(c, &c->bx_bo, &c->cbx_bo, (size_t)std::max(nB, 1)))
     return cuda_fail(c, cudaErrorMemoryAllocation, "bond export");
   cudaMemsetAsync(c->bx_count, 0, sizeof(int), st);
   if (nB > 0) {
@@ -1768,12 +1785,46 @@ int xr_ctx_reserve(xr_ctx* c, int atoms, int systems, long long edges, long long
   if (!ensure_atoms(c, atoms, systems) || !host_grow(&c->h_x, &c->ch_x, (size_t)atoms) ||
       !host_grow(&c->h_out, &c->ch_out, 8 * (size_t)atoms + 32 * (size_t)systems + 8) ||
       !host_grow(&c->h_guess, &c->ch_guess, (size_t)atoms) || !ensure_lists(c, edges, edges / 2, bonds) ||
-      !grow(&c->chunks, &c->cchunks, (size_t)chunks) ||
-      !grow(&c->chunk_part, &c->cchunk_part, (size_t)chunks * XR_PART_N) ||
-      !grow(&c->bx_meta, &c->cbx_meta, (size_t)std::max<long long>(bonds, 1)) ||
-      !grow(&c->bx_bo, &c->cbx_bo, (size_t)std::max<long long>(bonds, 1)))
+      !grow(c, &c->chunks, &c->cchunks, (size_t)chunks) ||
+      !grow(c, &c->chunk_part, &c->cchunk_part, (size_t)chunks * XR_PART_N) ||
+      !grow(c, &c->bx_meta, &c->cbx_meta, (size_t)std::max<long long>(bonds, 1)) ||
+      !grow(c, &c->bx_bo, &c->cbx_bo, (size_t)std::max<long long>(bonds, 1)) ||
+      // candidate rows and the cell list, for calls that search by cells
+      !grow(c, &c->cand_cnt, &c->ccand_cnt, (size_t)atoms + 1) ||
+      !grow(c, &c->cand_edge, &c->ccand_edge, (size_t)std::max<long long>(edges, 1)) ||
+      !grow(c, &c->atom_cell, &c->catom_cell, (size_t)atoms) || !grow(c, &c->atom_slot, &c->catom_slot, (size_t)atoms) ||
+      !grow(c, &c->cell_atoms, &c->ccell_atoms, (size_t)atoms) ||
+      !grow(c, &c->cell_cnt, &c->ccell_cnt, 2 * (size_t)atoms + 64 * (size_t)systems + 1))
     return cuda_fail(c, cudaErrorMemoryAllocation, "reservation");
   return XR_OK;
+}
+
+int xr_ctx_memory(const xr_ctx* c, long long* device_bytes, long long* caps, int n) {
+  if (!c || n < 0 || (n > 0 && !caps)) return XR_EINPUT;
+  if (device_bytes) *device_bytes = c->dev_bytes;
+  const long long v[6] = {(long long)c->cx, (long long)c->csys, (long long)c->cedge, (long long)c->cpair_edge,
+                          (long long)c->capB, (long long)c->ccand_edge};
+  for (int k = 0; k < n && k < 6; ++k) caps[k] = v[k];
+  return XR_OK;
+}
+
+long long xr_footprint_bytes(int atoms, int systems, long long edges, long long bonds) {
+  if (atoms < 1 || systems < 1 || edges < 0 || bonds < 0) return -1;
+  // the buffers of ensure_atoms, ensure_lists and xr_ctx_reserve, per element
+  const long long per_atom = sizeof(double4_32a) + 2 * sizeof(int) + sizeof(int4) + 2 * sizeof(float4) + 4 * sizeof(int) +
+                             (AF_N + AJ_N + 8 + 4 + 3 + XR_QW_N + 8 + XR_ESUM_N) * sizeof(double) + 2 * sizeof(int);
+  const long long per_system = sizeof(int2) + 2 * sizeof(int) + sizeof(XrSystem) + 20 * sizeof(double);
+  const long long per_edge = sizeof(int2) + 2 * sizeof(int) + sizeof(double) + sizeof(float) + sizeof(unsigned short);
+  const long long per_pair = 3 * sizeof(int) + 6 * sizeof(double);
+  const long long per_bond = kBondBytes + sizeof(int4) + sizeof(double);
+  const long long chunks = (long long)systems + atoms / XR_CHUNK_ATOMS + 1;
+  const long long per_cells = 4 * sizeof(int) + 2 * sizeof(int);  // cand_cnt, atom_cell, atom_slot, cell_atoms, cell_cnt
+  const long long base = (long long)atoms * (per_atom + per_cells) + (long long)systems * (per_system + 64 * sizeof(int)) +
+                         edges * (per_edge + sizeof(int2)) + (edges / 2) * per_pair + bonds * per_bond +
+                         chunks * (sizeof(int4) + XR_PART_N * sizeof(double));
+  const long long red = (long long)sizeof(double) * 4 * 8 * 2048;  // reduction scratch, at least this
+  // grow()'s headroom (n + n/4 + 64 elements per buffer), rounded up by 2 %
+  return (base + red) * 5 / 4 + (base + red) / 50 + 64ll * 64 * 16;
 }
 
 int xr_ctx_set_profiling(xr_ctx* c, int enable) {

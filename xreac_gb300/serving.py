@@ -9,6 +9,14 @@ the previous one is still on the GPU, so requests that arrive during a batch joi
 the batches' work overlaps on the device. The C library releases the Python GIL for the duration
 of a batch.
 
+Admission by device footprint: every worker context is reserved at start-up (atoms, systems,
+directed edges, bond candidates), within ``memory_budget`` when one is given, so that no batch
+allocates device memory while others run (a reallocation synchronises the device). A batch takes
+requests, oldest first, while its estimated lists still fit the context: a request of n atoms is
+estimated at n * min(n - 1, K) directed edges (n * K when periodic) and n * min((n - 1) / 2, K_b)
+bond candidates, where K and K_b per force field start at ``edges_per_atom`` and
+``bonds_per_atom`` and rise whenever a batch's lists turn out larger than estimated.
+
 Sessions: requests that carry the same ``session`` key are successive steps of one system (a
 relaxation or MD trajectory). The server keeps the last QEq charges of each session and starts the
 next step's solve from them (a warm start); results meet the same tolerance either way.
@@ -116,6 +124,34 @@ class Batch:
     qeq_bytes: float     # algorithmic matrix-free bytes of those iterations
     h2d_bytes: int = 0   # host-to-device bytes of the batch call
     d2h_bytes: int = 0   # device-to-host bytes of the batch call
+    est_edges: int = 0   # directed edges the admission estimated
+    edges: int = 0       # directed edges of the batch's lists
+    device_bytes: int = 0  # the worker context's device bytes after the batch
+
+
+class Footprint:
+    """Per-force-field density model of the admission: directed edges and bond candidates per atom
+    (K, K_b), raised when a batch exceeds its estimate."""
+
+    __slots__ = ("edges_per_atom", "bonds_per_atom")
+
+    def __init__(self, edges_per_atom, bonds_per_atom):
+        self.edges_per_atom = float(edges_per_atom)
+        self.bonds_per_atom = float(bonds_per_atom)
+
+    def estimate(self, natoms, periodic):
+        """(directed edges, bond candidates) expected for one request."""
+        if periodic:
+            return natoms * self.edges_per_atom, natoms * self.bonds_per_atom
+        return natoms * min(natoms - 1, self.edges_per_atom), natoms * min(0.5 * (natoms - 1), self.bonds_per_atom)
+
+    def observe(self, est_edges, edges, est_bonds, bonds):
+        """A batch's actual list sizes against their estimate: raise the densities (5 % above the
+        observed ratio) where the estimate fell short."""
+        if est_edges > 0 and edges > est_edges:
+            self.edges_per_atom *= 1.05 * edges / est_edges
+        if est_bonds > 0 and bonds > est_bonds:
+            self.bonds_per_atom *= 1.05 * bonds / est_bonds
 
 
 class Server:
@@ -124,17 +160,26 @@ class Server:
     ``force_fields`` maps names to ``ForceField`` objects. ``workers`` device contexts run batches
     concurrently; ``max_batch_atoms`` and ``max_batch_requests`` bound one batch, and every context
     is sized for that bound at start-up (``reserve``), so admission never waits on a device
-    allocation. ``warm_start`` enables the per-session QEq warm start.
+    allocation. ``memory_budget`` (bytes, optional) caps the device memory of all contexts together:
+    the atom bound is lowered until every context's reservation fits its share. ``edges_per_atom``
+    and ``bonds_per_atom`` are the admission's starting densities (see the module docstring).
+    ``warm_start`` enables the per-session QEq warm start.
     """
 
     def __init__(self, force_fields, *, workers=4, max_batch_atoms=16384, max_batch_requests=512, device=0,
-                 warm_start=True, max_expanded_atoms=512, reserve=True):
+                 warm_start=True, max_expanded_atoms=512, reserve=True, memory_budget=None, edges_per_atom=450.0,
+                 bonds_per_atom=30.0):
         if workers < 1:
             raise ValueError("workers must be at least 1")
         self.force_fields = dict(force_fields)
         self.max_batch_atoms = int(max_batch_atoms)
         self.max_batch_requests = int(max_batch_requests)
         self.warm_start = warm_start
+        self.footprints = {name: Footprint(edges_per_atom, bonds_per_atom) for name in self.force_fields}
+        self.reallocations = 0  # batches after which a context held more device memory than before
+        if memory_budget is not None:
+            share = float(memory_budget) / (workers * max(1, len(self.force_fields)))
+            self.max_batch_atoms = self._atoms_within(share, edges_per_atom, bonds_per_atom)
         self._queues = {name: collections.deque() for name in self.force_fields}
         self._cv = threading.Condition()
         self._done_cv = threading.Condition()  # signalled once per finished batch
@@ -147,12 +192,16 @@ class Server:
              for name, ff in self.force_fields.items()}
             for _ in range(workers)
         ]
+        self._reserved = bool(reserve)
         if reserve:
             # size every context for the largest admissible batch up front: a buffer growth during
             # serving would reallocate device memory and stall the other workers' batches
             for calcs in self._calcs:
                 for calc in calcs.values():
-                    calc.reserve(self.max_batch_atoms, self.max_batch_requests)
+                    calc.reserve(self.max_batch_atoms, self.max_batch_requests, edges_per_atom=edges_per_atom,
+                                 bonds_per_atom=bonds_per_atom)
+        # what each context holds without allocating: (atoms, systems, edges, bonds)
+        self._caps = [{name: self._capacity(calc) for name, calc in calcs.items()} for calcs in self._calcs]
         self._threads = [threading.Thread(target=self._worker, args=(k,), daemon=True) for k in range(workers)]
         for t in self._threads:
             t.start()
@@ -204,6 +253,44 @@ class Server:
     def __exit__(self, *exc):
         self.close()
 
+    def _atoms_within(self, share, edges_per_atom, bonds_per_atom):
+        """The largest atom bound (at most max_batch_atoms) whose reservation fits ``share`` bytes."""
+        def need(a):
+            return Calculator.footprint_bytes(a, self.max_batch_requests, int(a * edges_per_atom),
+                                              int(a * bonds_per_atom))
+
+        if need(1) > share:
+            raise ValueError("memory_budget is too small for a single-atom batch on every worker")
+        lo, hi = 1, self.max_batch_atoms
+        while lo < hi:
+            mid = (lo + hi + 1) // 2
+            if need(mid) <= share:
+                lo = mid
+            else:
+                hi = mid - 1
+        return lo
+
+    def _capacity(self, calc):
+        mem = getattr(calc, "memory", None)
+        if mem is None or not self._reserved:
+            # unreserved contexts grow on demand, and a calculator without memory reporting has only
+            # the configured bounds
+            return (self.max_batch_atoms, self.max_batch_requests, float("inf"), float("inf"))
+        m = mem()
+        return (min(m["atoms"], self.max_batch_atoms), min(m["systems"], self.max_batch_requests), m["edges"],
+                m["bonds"])
+
+    def memory_report(self):
+        """Device memory of every worker context: bytes and capacities, the admission's densities per
+        force field and the number of reallocations during serving."""
+        contexts = []
+        for k, calcs in enumerate(self._calcs):
+            for name, calc in calcs.items():
+                if hasattr(calc, "memory"):
+                    contexts.append(dict(worker=k, force_field=name, **calc.memory()))
+        densities = {name: (f.edges_per_atom, f.bonds_per_atom) for name, f in self.footprints.items()}
+        return dict(contexts=contexts, densities=densities, reallocations=self.reallocations)
+
     # ------------------------------------------------------------------ instrumentation
     def set_profiling(self, enable=True):
         """Per-stage CUDA-event timing on every worker context (resets the accumulators)."""
@@ -222,23 +309,29 @@ class Server:
         return total, calls
 
     # ------------------------------------------------------------------ worker side
-    def _take_batch(self):
-        """Oldest-first: the force field whose head request waited longest, then FIFO up to the budget."""
+    def _take_batch(self, k=0):
+        """Oldest-first: the force field whose head request waited longest, then FIFO while the
+        batch's estimated footprint fits worker k's context (the first request always goes)."""
         best = None
         for name, q in self._queues.items():
             if q and (best is None or q[0][0].arrival < self._queues[best][0][0].arrival):
                 best = name
         if best is None:
-            return None, []
+            return None, [], (0, 0)
         q = self._queues[best]
-        batch, atoms = [], 0
-        while q and len(batch) < self.max_batch_requests:
-            n = q[0][0].natoms
-            if batch and atoms + n > self.max_batch_atoms:
+        cap_atoms, cap_sys, cap_edges, cap_bonds = self._caps[k][best]
+        fp = self.footprints[best]
+        batch, atoms, edges, bonds = [], 0, 0.0, 0.0
+        while q and len(batch) < cap_sys:
+            req = q[0][0]
+            n = req.natoms
+            p = req.pbc
+            e, b = fp.estimate(n, False if p is None or p is False else (True if p is True else bool(np.any(p))))
+            if batch and (atoms + n > cap_atoms or edges + e > cap_edges or bonds + b > cap_bonds):
                 break
             batch.append(q.popleft())
-            atoms += n
-        return best, batch
+            atoms, edges, bonds = atoms + n, edges + e, bonds + b
+        return best, batch, (edges, bonds)
 
     def _worker(self, k):
         calcs = self._calcs[k]
@@ -246,13 +339,13 @@ class Server:
             with self._cv:
                 while not self._closed and not any(self._queues.values()):
                     self._cv.wait()
-                name, batch = self._take_batch()
+                name, batch, est = self._take_batch(k)
                 if not batch:
                     if self._closed:
                         return
                     continue
             try:
-                self._run(calcs[name], name, batch)
+                self._run(calcs[name], name, batch, est, k)
             except BaseException as err:  # noqa: BLE001 - an unexpected failure fails the batch, not the worker
                 for _, fut in batch:
                     if not fut._done:
@@ -261,7 +354,7 @@ class Server:
                 with self._done_cv:
                     self._done_cv.notify_all()
 
-    def _run(self, calc, name, batch):
+    def _run(self, calc, name, batch, est=(0, 0), k=0):
         charges = self._charges
         warm = self.warm_start
         items = []
@@ -286,8 +379,20 @@ class Server:
         done = time.perf_counter()
         its, qbytes = calc.qeq_work()
         h2d, d2h = calc.transfer_bytes()
+        edges, dev_bytes = 0, 0
+        if hasattr(calc, "memory"):
+            sizes = calc.list_sizes()
+            edges = sizes[0]
+            before = self._caps[k][name]
+            cap = self._capacity(calc)
+            dev_bytes = calc.memory()["device_bytes"]
+            with self._cv:
+                self.footprints[name].observe(est[0], sizes[0], est[1], sizes[2])
+                if cap != before:
+                    self.reallocations += 1
+                    self._caps[k][name] = cap
         self.batches.append(Batch(name, len(batch), sum(len(it[0]) for it in items), done - t0, calc.last_launches,
-                                  its, qbytes, h2d, d2h))
+                                  its, qbytes, h2d, d2h, int(est[0]), edges, dev_bytes))
         nb = len(batch)
         with self._charges_lock:
             for (req, fut), res in zip(batch, results):
