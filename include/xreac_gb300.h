@@ -178,6 +178,16 @@ int xr_neighbors_check(int natoms, const int* pbc, const xr_neighbors* nb, char*
  * current value, drops the kept list. */
 int xr_ctx_set_skin(xr_ctx* ctx, double skin);
 
+/* CUDA graphs (no reference counterpart): with enable != 0 (the default) a call that repeats the
+ * previous call's launch sequence (the same systems' sizes and periodicity, force field, flags and
+ * buffers, as in relaxation or MD steps) records the kernels after the neighbour count as a CUDA
+ * graph, and later calls with the same sequence replay it as one launch. The kernels read the list
+ * sizes from device memory, so a replay is the same computation. Not used with stage timing
+ * (xr_ctx_set_profiling) or with grid-wide QEq teams. xr_last_graph: 0 launched directly, 1
+ * recorded, 2 replayed (-1 for a null context). */
+int xr_ctx_set_graphs(xr_ctx* ctx, int enable);
+int xr_last_graph(const xr_ctx* ctx);
+
 /* Cell-list neighbour search (no reference counterpart; xreac enumerates every atom pair over the
  * replicated images, src/xreac/neighbors.py:17-53). mode 0 (the default) uses it for a call whose
  * largest system has at least 1,024 atoms when it halves the expected image tests; 1 always; -1

@@ -52,6 +52,8 @@ EXPORTED = (
     "xr_neighbors_check",
     "xr_ctx_set_skin",
     "xr_ctx_set_cell_list",
+    "xr_ctx_set_graphs",
+    "xr_last_graph",
     "xr_last_list_info",
     "xr_get_neighbors",
     "xr_get_bonds",
@@ -169,6 +171,10 @@ def load():
     lib.xr_ctx_set_skin.restype = c_int
     lib.xr_ctx_set_cell_list.argtypes = [c_void_p, c_int]
     lib.xr_ctx_set_cell_list.restype = c_int
+    lib.xr_ctx_set_graphs.argtypes = [c_void_p, c_int]
+    lib.xr_ctx_set_graphs.restype = c_int
+    lib.xr_last_graph.argtypes = [c_void_p]
+    lib.xr_last_graph.restype = c_int
     lib.xr_last_list_info.argtypes = [c_void_p, POINTER(c_int), POINTER(c_longlong)]
     lib.xr_last_list_info.restype = c_int
     lib.xr_get_neighbors.argtypes = [c_void_p, c_int, POINTER(c_int), POINTER(c_int), POINTER(c_int), c_longlong,

@@ -371,6 +371,18 @@ class Calculator:
         self._lib.xr_last_list_info(self._ctx.handle, nat.byref(mode), nat.byref(builds))
         return ("scan", "built", "reused", "supplied", "cells", "built-cells")[mode.value], int(builds.value)
 
+    def set_graphs(self, enabled=True):
+        """CUDA graphs for repeated launch sequences (``xr_ctx_set_graphs``, an extension; on by
+        default): a call that repeats the previous call's systems and settings records its kernels
+        as a graph, and later such calls replay it."""
+        self._lib.xr_ctx_set_graphs(self._ctx.handle, 1 if enabled else 0)
+
+    @property
+    def last_graph(self):
+        """How the last call launched its kernels after the neighbour count: "direct", "recorded"
+        or "replayed"."""
+        return ("direct", "recorded", "replayed")[self._lib.xr_last_graph(self._ctx.handle)]
+
     def set_cell_list(self, enabled=None):
         """Neighbour search by cell list (``xr_ctx_set_cell_list``, an extension): None chooses per
         call (large systems where it halves the image tests), True always, False never. The list and

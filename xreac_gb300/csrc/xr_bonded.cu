@@ -65,11 +65,11 @@ __device__ inline uint32_t bond_shift(const XrWork& w, int b, int dir) {
 // ------------------------------------------------------------------ uncorrected bond orders
 // sigma' = (1+cut) exp(p_bo1 (r/r_s)^p_bo2), pi' = exp(p_bo3 (r/r_p)^p_bo4), pp' likewise;
 // raw = sum; active when raw >= cut; bo0 = raw - cut (src/xreac/energy.py:130-149).
-__global__ void k_bo1(XrWork w, XrFF ff0) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+// One block-wide tile of bonds b (the whole warp takes part: the active ones are compacted with ballots).
+__device__ inline void bo1_tile(const XrWork& w, const XrFF& ff0, int b, int nb) {
   const int lane = threadIdx.x & 31;
   bool mask = false;
-  if (b < w.nB) {
+  if (b < nb) {
     const int i = w.bond_i[b], j = w.bond_j[b];
     const XrFF ff = xr_ff_of(ff0, w, i);
     const uint32_t code = (uint32_t)w.edge[w.pair_edge[w.bond_pair[b]]].y;
@@ -138,6 +138,12 @@ __global__ void k_bo1(XrWork w, XrFF ff0) {
   if (lane == 0 && m) base = atomicAdd(w.nmask, __popc(m));
   base = __shfl_sync(0xffffffffu, base, 0);
   if (mask) w.mlist[base + __popc(m & ((1u << lane) - 1u))] = b;
+}
+
+__global__ void k_bo1(XrWork w, XrFF ff0) {
+  const int nb = xr_num_bonds(w);
+  for (int b0 = blockIdx.x * blockDim.x; b0 < nb; b0 += gridDim.x * blockDim.x)  // uniform per block
+    bo1_tile(w, ff0, b0 + threadIdx.x, nb);
 }
 
 // Delta'_a = sum of uncorrected bond orders over the atom's directed bond edges, one warp per atom.
@@ -675,18 +681,21 @@ __device__ inline void cross3(const double a[3], const double b[3], double c[3])
 
 // Bonds with bo > 0.001 (the middles of torsion chains), compacted with warp-aggregated atomics.
 __global__ void k_torsion_middles(XrWork w) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nb = xr_num_bonds(w);
   const int lane = threadIdx.x & 31;
-  const bool keep = b < w.nB && BFV(BF_BO, b) > THB_CUT;
-  if (b < w.nB && !keep) {
-    BEV(2, b) = 0.0;
-    BEV(3, b) = 0.0;
+  for (int b0 = blockIdx.x * blockDim.x; b0 < nb; b0 += gridDim.x * blockDim.x) {  // uniform per block
+    const int b = b0 + threadIdx.x;
+    const bool keep = b < nb && BFV(BF_BO, b) > THB_CUT;
+    if (b < nb && !keep) {
+      BEV(2, b) = 0.0;
+      BEV(3, b) = 0.0;
+    }
+    const unsigned msk = __ballot_sync(0xffffffffu, keep);
+    int base = 0;
+    if (lane == 0 && msk) base = atomicAdd(w.nmids, __popc(msk));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (keep) w.mids[base + __popc(msk & ((1u << lane) - 1u))] = b;
   }
-  const unsigned msk = __ballot_sync(0xffffffffu, keep);
-  int base = 0;
-  if (lane == 0 && msk) base = atomicAdd(w.nmids, __popc(msk));
-  base = __shfl_sync(0xffffffffu, base, 0);
-  if (keep) w.mids[base + __popc(msk & ((1u << lane) - 1u))] = b;
 }
 
 // Torsion and four-body conjugation (src/xreac/energy.py:320-370): units are middle bonds j -> k

@@ -231,6 +231,14 @@ struct XrWork {
   int nchunks;
 };
 
+// List sizes of the call as the device holds them (the totals of the count scans, counts[0..2]).
+// Kernels over edges, pairs and bonds read these and stride over them, so a launch sequence
+// recorded for one call (a CUDA graph) stays correct when it is replayed for a call whose lists
+// have other sizes.
+__device__ __forceinline__ int xr_num_edges(const XrWork& w) { return *(volatile const int*)(w.counts + 0); }
+__device__ __forceinline__ int xr_num_pairs(const XrWork& w) { return *(volatile const int*)(w.counts + 1); }
+__device__ __forceinline__ int xr_num_bonds(const XrWork& w) { return *(volatile const int*)(w.counts + 2); }
+
 // The parameter-gradient block of the system of `atom` (pair table, then angle records).
 __device__ inline double* xr_pgrad(const XrWork& w, int atom) { return w.pgrad + (size_t)w.sys_of[atom] * w.pgrad_stride; }
 

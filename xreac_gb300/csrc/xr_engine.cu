@@ -80,6 +80,14 @@ struct xr_ctx {
   size_t ch_sys_list = 0;
   // Device bytes the context holds (its buffers, as grown; xr_ctx_memory).
   long long dev_bytes = 0;
+  // CUDA graph of the launch sequence after the list count (xr_ctx_set_graphs): recorded when a
+  // call repeats the previous call's launch key, replayed while the key stays the same.
+  bool graphs = true;
+  cudaGraphExec_t gexec = nullptr;
+  std::vector<unsigned char> gkey;     // key of the recorded sequence
+  std::vector<unsigned char> last_key; // key of the previous call
+  long long glaunches = 0;             // kernels in the recorded sequence
+  int last_graph = 0;                  // of the last call: 0 launched directly, 1 recorded, 2 replayed
   // Cell list (xr_ctx_set_cell_list): 0 chooses per call, 1 always, -1 never.
   int cell_mode = 0;
   int* atom_cell = nullptr;
@@ -529,19 +537,23 @@ __global__ void k_positions_from_device(const double* pos, double4_32a* x, int n
 
 // Nonzero corrected bond orders, compacted with warp-aggregated atomics; the host restores bond order.
 __global__ void k_bond_export(XrWork w, int4* meta, double* bo_out, int* counter) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nb = xr_num_bonds(w);
   const int lane = threadIdx.x & 31;
-  const double bo = b < w.nB ? w.b_fwd[(size_t)BF_BO * w.cap_B + b] : 0.0;
-  const bool keep = b < w.nB && bo != 0.0;
-  const unsigned m = __ballot_sync(0xffffffffu, keep);
-  int base = 0;
-  if (lane == 0 && m) base = atomicAdd(counter, __popc(m));
-  base = __shfl_sync(0xffffffffu, base, 0);
-  if (!keep) return;
-  const int slot = base + __popc(m & ((1u << lane) - 1u));
-  const int code = w.edge[w.pair_edge[w.bond_pair[b]]].y;
-  meta[slot] = make_int4(b, w.bond_i[b], w.bond_j[b], code);
-  bo_out[slot] = bo;
+  for (int b0 = blockIdx.x * blockDim.x; b0 < nb; b0 += gridDim.x * blockDim.x) {  // uniform per block
+    const int b = b0 + threadIdx.x;
+    const double bo = b < nb ? w.b_fwd[(size_t)BF_BO * w.cap_B + b] : 0.0;
+    const bool keep = b < nb && bo != 0.0;
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    int base = 0;
+    if (lane == 0 && m) base = atomicAdd(counter, __popc(m));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (keep) {
+      const int slot = base + __popc(m & ((1u << lane) - 1u));
+      const int code = w.edge[w.pair_edge[w.bond_pair[b]]].y;
+      meta[slot] = make_int4(b, w.bond_i[b], w.bond_j[b], code);
+      bo_out[slot] = bo;
+    }
+  }
 }
 
 void stage(xr_ctx* c, int k, cudaStream_t st) {
@@ -769,6 +781,22 @@ long long plan_cells(xr_ctx* c, int nsys, const xr_system* sys, double rl, XrSys
     }
   }
   return use ? total : 0;
+}
+
+// Everything the launch sequence after the list count depends on, other than data in device memory:
+// the work descriptor (pointers, capacities, atom and system counts; the list sizes are read from
+// the device), the force field's view, and the host-side launch choices.
+std::vector<unsigned char> launch_key(const XrWork& w, const XrFF& ff, const int* ints, int nints, const void* const* ptrs,
+                                      int nptrs) {
+  XrWork wk = w;  // padding is zero: fill_work clears the whole structure
+  wk.nE = wk.nP = wk.nB = wk.nD = 0;
+  std::vector<unsigned char> k(sizeof(XrWork) + sizeof(XrFF) + sizeof(int) * nints + sizeof(void*) * nptrs);
+  unsigned char* q = k.data();
+  std::memcpy(q, &wk, sizeof(XrWork));
+  std::memcpy(q + sizeof(XrWork), &ff, sizeof(XrFF));
+  std::memcpy(q + sizeof(XrWork) + sizeof(XrFF), ints, sizeof(int) * nints);
+  std::memcpy(q + sizeof(XrWork) + sizeof(XrFF) + sizeof(int) * nints, ptrs, sizeof(void*) * nptrs);
+  return k;
 }
 
 int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsigned flags, xr_result* out,
@@ -1074,76 +1102,127 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
   w.nP = nP;
   w.nB = nB;
   w.nD = nD;
-  stage(c, 1, st);
-  if (mode == kScan)
-    xr_launch_rows(w, st);
-  else
-    xr_launch_filter(w, true, st);
-  xr_launch_reverse(w, st);
-  launches += 2;
-  cudaMemsetAsync(c->a_adj, 0, sizeof(double) * (size_t)AJ_N * A, st);
-  cudaMemsetAsync(c->f, 0, sizeof(double) * 3 * (size_t)A, st);
-  cudaMemsetAsync(c->b_adj, 0, sizeof(double) * (size_t)BJ_N * c->capB, st);
-  cudaMemsetAsync(c->b_e, 0, sizeof(double) * 4 * c->capB, st);
-  stage(c, 2, st);
-  xr_launch_pairs(w, ff->d, st);
-  launches += 2;
-  stage(c, 3, st);
-  int qblocks = 0, qteam = 0, qsmall = 0, qbig = 0, qcsize = 0;
+  // Host-side choices of the launch sequence, made before it so that it can be recorded: the QEq
+  // plan (its tables go through pinned buffers that a replay copies again) and the bond export.
+  int qblocks = 0, qteam = 0, qsmall = 0, qbig = 0, qcsize = 0, nlist = 0;
   bool qcluster = false;
   if (c->coop_per_sm > 0) {
     qcluster = plan_qeq_cluster(c, sys, nsys, &qcsize, &qblocks, &qbig, &qsmall);
     if (!qcluster) plan_qeq(c, sys, nsys, &qblocks, &qteam, &qsmall);
-    const int nlist = qbig + qsmall;
+    nlist = qbig + qsmall;
     if (!host_grow(&c->h_qmap_p, &c->ch_qmap_p, (size_t)std::max(qteam, 1)) ||
         !host_grow(&c->h_qsmall_p, &c->ch_qsmall_p, (size_t)std::max(nlist, 1)))
       return cuda_fail(c, cudaErrorMemoryAllocation, "allocation");
-    if (qteam > 0) {
-      std::memcpy(c->h_qmap_p, c->h_qmap.data(), sizeof(int4) * qteam);
-      cudaMemcpyAsync(c->qmap, c->h_qmap_p, sizeof(int4) * qteam, cudaMemcpyHostToDevice, st);
-    }
-    if (nlist > 0) {
-      std::memcpy(c->h_qsmall_p, c->h_qsmall.data(), sizeof(int) * nlist);
-      cudaMemcpyAsync(c->qsmall, c->h_qsmall_p, sizeof(int) * nlist, cudaMemcpyHostToDevice, st);
-    }
+    if (qteam > 0) std::memcpy(c->h_qmap_p, c->h_qmap.data(), sizeof(int4) * qteam);
+    if (nlist > 0) std::memcpy(c->h_qsmall_p, c->h_qsmall.data(), sizeof(int) * nlist);
     h2d += sizeof(int4) * (long long)qteam + sizeof(int) * (long long)nlist;
   }
+  if (!grow(c, &c->bx_meta, &c->cbx_meta, (size_t)std::max(nB, 1)) || !grow(c, &c->bx_bo, &c->cbx_bo, (size_t)std::max(nB, 1)))
+    return cuda_fail(c, cudaErrorMemoryAllocation, "bond export");
   auto launch_qeq = [&](bool adjoint) {
     return qcluster ? xr_launch_qeq_cluster(w, ff->d, st, qcsize, qblocks, c->qsmall, qbig, qsmall, adjoint)
                     : xr_launch_qeq(w, ff->d, st, qblocks, c->qmap, qteam, c->qsmall, qsmall, adjoint);
   };
-  if (int le = launch_qeq(false))
-    return cuda_fail(c, (cudaError_t)le, "QEq launch");
-  launches += 1;
-  stage(c, 4, st);
-  xr_launch_coulomb(w, ff->d, st);
-  launches += 1;
-  if (w.full_derivative) {
-    // charge-response forces: adjoint QEq solve with the same plan, then its radial pair terms
-    xr_launch_charge_response(w, ff->d, st, 0);
-    if (int le = launch_qeq(true))
-      return cuda_fail(c, (cudaError_t)le, "adjoint QEq launch");
-    xr_launch_charge_response(w, ff->d, st, 1);
-    launches += 4;
+  // The launch sequence: rows, pairs, QEq, Coulomb, bond orders, bonded terms, forces, reductions,
+  // bond export. Returns 0 or a CUDA error of a launch.
+  auto sequence = [&]() -> int {
+    stage(c, 1, st);
+    if (mode == kScan)
+      xr_launch_rows(w, st);
+    else
+      xr_launch_filter(w, true, st);
+    xr_launch_reverse(w, st);
+    launches += 2;
+    cudaMemsetAsync(c->a_adj, 0, sizeof(double) * (size_t)AJ_N * A, st);
+    cudaMemsetAsync(c->f, 0, sizeof(double) * 3 * (size_t)A, st);
+    cudaMemsetAsync(c->b_adj, 0, sizeof(double) * (size_t)BJ_N * c->capB, st);
+    cudaMemsetAsync(c->b_e, 0, sizeof(double) * 4 * c->capB, st);
+    stage(c, 2, st);
+    xr_launch_pairs(w, ff->d, st);
+    launches += 2;
+    stage(c, 3, st);
+    if (qteam > 0) cudaMemcpyAsync(c->qmap, c->h_qmap_p, sizeof(int4) * qteam, cudaMemcpyHostToDevice, st);
+    if (nlist > 0) cudaMemcpyAsync(c->qsmall, c->h_qsmall_p, sizeof(int) * nlist, cudaMemcpyHostToDevice, st);
+    if (int le = launch_qeq(false)) return le;
+    launches += 1;
+    stage(c, 4, st);
+    xr_launch_coulomb(w, ff->d, st);
+    launches += 1;
+    if (w.full_derivative) {
+      // charge-response forces: adjoint QEq solve with the same plan, then its radial pair terms
+      xr_launch_charge_response(w, ff->d, st, 0);
+      if (int le = launch_qeq(true)) return le;
+      xr_launch_charge_response(w, ff->d, st, 1);
+      launches += 4;
+    }
+    stage(c, 5, st);
+    xr_launch_bond_orders(w, ff->d, st);
+    launches += 3;
+    stage(c, 6, st);
+    xr_launch_bonded(w, ff->d, st);
+    launches += 11;
+    stage(c, 7, st);
+    xr_launch_forces(w, ff->d, st);
+    launches += 1;
+    xr_launch_reduce(w, ff->d, st);
+    launches += 3;
+    cudaMemsetAsync(c->bx_count, 0, sizeof(int), st);
+    if (nB > 0) {
+      k_bond_export<<<(nB + 255) / 256, 256, 0, st>>>(w, c->bx_meta, c->bx_bo, c->bx_count);
+      ++launches;
+    }
+    return (int)cudaGetLastError();
+  };
+  // A sequence is recorded as a CUDA graph when a call repeats the previous call's launch key (a
+  // relaxation or MD step, a repeated request), and replayed while the key stays the same: one
+  // launch instead of about 30 kernel launches and their memsets. Not with stage timing, nor with
+  // grid-wide QEq teams (their co-residency needs a cooperative launch).
+  c->last_graph = 0;
+  bool done = false;
+  if (c->graphs && !c->profile && qteam == 0) {
+    const int ints[] = {(int)mode, qcluster ? 1 : 0, qcsize, qblocks, qteam, qsmall, qbig, nlist, nE > 0, nP > 0, nB > 0};
+    const void* ptrs[] = {c->h_qmap_p, c->h_qsmall_p, c->bx_meta, c->bx_bo, c->bx_count};
+    std::vector<unsigned char> key = launch_key(w, ff->d, ints, (int)(sizeof(ints) / sizeof(int)), ptrs, 5);
+    if (c->gexec && key == c->gkey) {
+      if (cudaGraphLaunch(c->gexec, st) == cudaSuccess) {
+        launches += c->glaunches;
+        c->last_graph = 2;
+        done = true;
+      } else {
+        cudaGetLastError();
+      }
+    } else if (key == c->last_key) {
+      const long long before = launches;
+      cudaGraph_t g = nullptr;
+      if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+        const int rc = sequence();
+        const cudaError_t ce = cudaStreamEndCapture(st, &g);
+        cudaGraphExec_t ex = nullptr;
+        if (rc == 0 && ce == cudaSuccess && g && cudaGraphInstantiate(&ex, g, 0) == cudaSuccess) {
+          if (c->gexec) cudaGraphExecDestroy(c->gexec);
+          c->gexec = ex;
+          c->gkey = key;
+          c->glaunches = launches - before;
+          if (cudaGraphLaunch(ex, st) == cudaSuccess) {
+            c->last_graph = 1;
+            done = true;
+          }
+        }
+        if (g) cudaGraphDestroy(g);
+      }
+      if (!done) {  // not recordable here: launch directly, and do not try this key again
+        cudaGetLastError();
+        launches = before;
+        if (c->gexec) cudaGraphExecDestroy(c->gexec);
+        c->gexec = nullptr;
+        c->gkey.clear();
+        key.clear();
+      }
+    }
+    c->last_key = std::move(key);
   }
-  stage(c, 5, st);
-  xr_launch_bond_orders(w, ff->d, st);
-  launches += 3;
-  stage(c, 6, st);
-  xr_launch_bonded(w, ff->d, st);
-  launches += 11;
-  stage(c, 7, st);
-  xr_launch_forces(w, ff->d, st);
-  launches += 1;
-  xr_launch_reduce(w, ff->d, st);
-  launches += 3;
-  if (!grow(c, &c->bx_meta, &c->cbx_meta, (size_t)std::max(nB, 1)) || !grow(c, &c->bx_bo, &c->cbx_bo, (size_t)std::max(nB, 1)))
-    return cuda_fail(c, cudaErrorMemoryAllocation, "bond export");
-  cudaMemsetAsync(c->bx_count, 0, sizeof(int), st);
-  if (nB > 0) {
-    k_bond_export<<<(nB + 255) / 256, 256, 0, st>>>(w, c->bx_meta, c->bx_bo, c->bx_count);
-    ++launches;
-  }
+  if (!done)
+    if (int le = sequence()) return cuda_fail(c, (cudaError_t)le, "launch");
   cudaMemcpyAsync(c->h_small + 5, c->bx_count, sizeof(int), cudaMemcpyDeviceToHost, st);
   cudaMemcpyAsync(c->h_small + 6, c->counts + 4, sizeof(int), cudaMemcpyDeviceToHost, st);
   cudaMemcpyAsync(c->h_qit, c->qiters, sizeof(int) * nsys, cudaMemcpyDeviceToHost, st);
@@ -1581,6 +1660,7 @@ void xr_ctx_destroy(xr_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
+  if (c->gexec) cudaGraphExecDestroy(c->gexec);
   void* bufs[] = {c->x, c->type, c->sys_of, c->wrap, c->xw, c->fw, c->cnt, c->a_fwd, c->a_adj, c->a_e, c->q, c->f,
                   c->qwork, c->outbuf, c->edge, c->edge_pair, c->edge_dbslot, c->hval, c->qch, c->qcj, c->pair_edge, c->pair_i,
                   c->pair_bond, c->p_r, c->p_shield, c->p_dshield, c->p_g, c->p_evdw, c->p_ecoul, c->bond_pair,
@@ -1639,6 +1719,21 @@ int xr_ctx_set_skin(xr_ctx* c, double skin) {
   c->skin = skin;
   return XR_OK;
 }
+
+int xr_ctx_set_graphs(xr_ctx* c, int enable) {
+  if (!c) return XR_EINPUT;
+  c->graphs = enable != 0;
+  if (!c->graphs && c->gexec) {
+    cudaSetDevice(c->device);
+    cudaGraphExecDestroy(c->gexec);
+    c->gexec = nullptr;
+    c->gkey.clear();
+  }
+  c->last_key.clear();
+  return XR_OK;
+}
+
+int xr_last_graph(const xr_ctx* c) { return c ? c->last_graph : -1; }
 
 int xr_ctx_set_cell_list(xr_ctx* c, int mode) {
   if (!c || mode < -1 || mode > 1) return XR_EINPUT;

@@ -52,9 +52,7 @@ __device__ inline double inv_cbrt(double t) {
 }
 
 // ------------------------------------------------------------------------------ pair kernel
-__global__ void k_pairs(XrWork w, XrFF ff0) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= w.nP) return;
+__device__ inline void pair_one(const XrWork& w, const XrFF& ff0, int p) {
   const int e = w.pair_edge[p], i = w.pair_i[p];
   const int2 ed = w.edge[e];
   const int j = ed.x;
@@ -129,11 +127,12 @@ __global__ void k_pairs(XrWork w, XrFF ff0) {
 }
 
 __global__ void k_hval(XrWork w) {
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= w.nE) return;
-  const double h = QEQ_COULOMB * w.p_shield[w.edge_pair[e]];
-  w.hval[e] = h;
-  w.qch[e] = float(h);  // FP32 copy for the solver's row cache (which may overwrite it, scaled)
+  const int ne = xr_num_edges(w);
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += gridDim.x * blockDim.x) {
+    const double h = QEQ_COULOMB * w.p_shield[w.edge_pair[e]];
+    w.hval[e] = h;
+    w.qch[e] = float(h);  // FP32 copy for the solver's row cache (which may overwrite it, scaled)
+  }
 }
 
 // ---------------------------------------------------------------------------------- QEq
@@ -1703,22 +1702,26 @@ __global__ void __launch_bounds__(1024, 1) k_qeq_block(XrWork w, XrFF ff, int ad
             !adjoint && S.has_guess != 0, sh, nullptr, 0, adjoint != 0);
 }
 
+__global__ void k_pairs(XrWork w, XrFF ff0) {
+  const int np = xr_num_pairs(w);
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) pair_one(w, ff0, p);
+}
+
 // ------------------------------------------------------------------------------ Coulomb
 __global__ void k_coulomb(XrWork w) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= w.nP) return;
-  const int i = w.pair_i[p], j = w.edge[w.pair_edge[p]].x;
-  const double qq = C_ELE * w.q[i] * w.q[j];
-  w.p_ecoul[p] = qq * w.p_shield[p];
-  w.p_g[p] += qq * w.p_dshield[p];
+  const int np = xr_num_pairs(w);
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
+    const int i = w.pair_i[p], j = w.edge[w.pair_edge[p]].x;
+    const double qq = C_ELE * w.q[i] * w.q[j];
+    w.p_ecoul[p] = qq * w.p_shield[p];
+    w.p_g[p] += qq * w.p_dshield[p];
+  }
 }
 
 // ------------------------------------------------------------------------ force assembly
 // Every radial sensitivity (vdW, Coulomb, bond-order chain) sits on its pair: dE/dx_j += G v/r,
 // dE/dx_i -= G v/r.
-__global__ void k_pair_forces(XrWork w) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= w.nP) return;
+__device__ inline void pair_force_one(const XrWork& w, int p) {
   const double G = w.p_g[p];
   if (G == 0.0) return;
   const int i = w.pair_i[p];
@@ -1733,6 +1736,11 @@ __global__ void k_pair_forces(XrWork w) {
     atomicAdd(w.f + 3 * j + c, s * v[c]);
     atomicAdd(w.f + 3 * i + c, -s * v[c]);
   }
+}
+
+__global__ void k_pair_forces(XrWork w) {
+  const int np = xr_num_pairs(w);
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) pair_force_one(w, p);
 }
 
 // ------------------------------------------------------------------------ reductions
@@ -1876,10 +1884,11 @@ __global__ void k_qeq_rhs(XrWork w, XrFF ff) {
 }
 
 __global__ void k_charge_response_radial(XrWork w) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= w.nP) return;
-  const int i = w.pair_i[p], j = w.edge[w.pair_edge[p]].x;
-  w.p_g[p] += -QEQ_COULOMB * (w.qadj[i] * w.q[j] + w.qadj[j] * w.q[i]) * w.p_dshield[p];
+  const int np = xr_num_pairs(w);
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
+    const int i = w.pair_i[p], j = w.edge[w.pair_edge[p]].x;
+    w.p_g[p] += -QEQ_COULOMB * (w.qadj[i] * w.q[j] + w.qadj[j] * w.q[i]) * w.p_dshield[p];
+  }
 }
 
 }  // namespace
