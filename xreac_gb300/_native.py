@@ -180,8 +180,8 @@ def load():
     lib.xr_get_neighbors.argtypes = [c_void_p, c_int, POINTER(c_int), POINTER(c_int), POINTER(c_int), c_longlong,
                                      POINTER(c_longlong)]
     lib.xr_get_neighbors.restype = c_int
-    lib.xr_get_bonds.argtypes = [c_void_p, c_int, POINTER(c_int), POINTER(c_int), POINTER(c_int), POINTER(c_double),
-                                 c_longlong, POINTER(c_longlong)]
+    lib.xr_get_bonds.argtypes = [c_void_p, c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_longlong,
+                                 POINTER(c_longlong)]  # i, j, S, bo: int*, int*, int*, double*
     lib.xr_get_bonds.restype = c_int
     lib.xr_last_launches.argtypes = [c_void_p]
     lib.xr_last_launches.restype = c_longlong

@@ -488,8 +488,7 @@ class Calculator:
             nb = nat.Neighbors(len(i), nat.addr(i), nat.addr(j), nat.addr(shifts))
             return self._run([(types, x, flags, cellm, float(total_charge), guess)], full_derivative, [(1, 1, 1)],
                              "provided", supplied=nb)[0]
-        return self._run([(types, x, flags, cellm, float(total_charge), guess)], full_derivative, [reps],
-                         "replicated")[0]
+        return self._run_one(types, x, flags, cellm, float(total_charge), guess, full_derivative, reps, "replicated")
 
     def _evaluate_backend(self, symbols, positions, *, total_charge=0, cell=None, pbc=None, full_derivative=False,
                           backend="replicated"):
@@ -638,6 +637,47 @@ class Calculator:
         charges = [float(it[2]) for it in items]
         return types, x, offsets, flags_l, cells, charges, _GuessAddresses(guess_addr, keep), reps
 
+    def _run_one(self, types, x, flags, cellm, total_charge, guess, full_derivative, rep, backend):
+        """``_run`` for one system (``xr_eval``) with a reused pair of C descriptors and one output
+        block, instead of the batch's structured arrays: the plain path's host cost."""
+        n = len(types)
+        if not np.isfinite(x).all():
+            raise ValueError("positions must be a finite (N, 3) array in Angstrom")
+        one = self.__dict__.get("_one")
+        if one is None:
+            one = self._one = (nat.System(), nat.Result())
+        sd, rd = one
+        sd.natoms = n
+        sd.types = nat.addr(types)
+        sd.positions = nat.addr(x)
+        sd.cell = None if cellm is None else nat.addr(cellm)
+        sd.pbc[0], sd.pbc[1], sd.pbc[2] = int(flags[0]), int(flags[1]), int(flags[2])
+        sd.total_charge = total_charge
+        sd.charges_guess = None if guess is None else nat.addr(guess)
+        # one block: energy (15) | dipole (3) | forces (3n) | charges, total bond orders, lone pairs (3n)
+        block = np.empty(18 + 6 * n)
+        counts = np.empty(n, dtype=np.int32)
+        base = nat.addr(block)
+        rd.energy = base
+        rd.dipole = base + 120
+        rd.forces = base + 144
+        rd.charges = base + 144 + 24 * n
+        rd.total_bond_orders = base + 144 + 32 * n
+        rd.lone_pairs = base + 144 + 40 * n
+        rd.bond_counts = nat.addr(counts)
+        code = self._lib.xr_eval(self._ctx.handle, self._ff.handle, nat.byref(sd),
+                                 nat.XR_FLAG_FULL_DERIVATIVE if full_derivative else 0, nat.byref(rd))
+        if code != nat.XR_OK:
+            self._raise(code)
+        bonds = self._bonds(0)
+        held = _BatchResults(block[:15].reshape(1, 15), block[18:18 + 3 * n].reshape(n, 3),
+                             block[18 + 3 * n:].reshape(3, n), counts, block[15:18].reshape(1, 3), [0, n], bonds,
+                             [0, len(bonds[0])])
+        ev = object.__new__(Evaluation)
+        ev.__dict__.update(energy=float(block[14]), full_derivative=full_derivative, cell_repetitions=rep,
+                           neighbor_backend=backend, _batch=held, _index=0)
+        return ev
+
     def _run(self, batch, full_derivative, reps, backend, extra_flags=0, supplied=None, sets=None):
         """One ``xr_eval_batch`` call over ``batch`` = [(types, positions, pbc flags, cell, total
         charge, initial charges)]: the inputs are packed into one array per kind, then as
@@ -734,13 +774,11 @@ class Calculator:
         count = nat.c_longlong()
         lib.xr_get_bonds(h, index, None, None, None, None, 0, nat.byref(count))
         m = count.value
-        i = np.zeros(m, dtype=np.int32)
-        j = np.zeros(m, dtype=np.int32)
-        S = np.zeros((m, 3), dtype=np.int32)
-        bo = np.zeros(m)
-        lib.xr_get_bonds(h, index, nat.ptr(i, nat.c_int), nat.ptr(j, nat.c_int), nat.ptr(S, nat.c_int),
-                         nat.ptr(bo, nat.c_double), m, nat.byref(count))
-        return i, j, S, bo
+        ints = np.empty(5 * m, dtype=np.int32)  # i | j | S
+        bo = np.empty(m)
+        base = nat.addr(ints)
+        lib.xr_get_bonds(h, index, base, base + 4 * m, base + 8 * m, nat.addr(bo), m, nat.byref(count))
+        return ints[:m], ints[m:2 * m], ints[2 * m:].reshape(m, 3), bo
 
     def relax(self, symbols, positions, *, force_tolerance=1e-4, max_iterations=500, total_charge=0, cell=None,
               pbc=None, backend="ase"):
