@@ -43,6 +43,8 @@ enum xr_status {
 #define XR_FLAG_FULL_DERIVATIVE 1u /* charge-response forces (xreac full_derivative=True) */
 #define XR_FLAG_DEVICE_IO 2u       /* positions and result arrays are device pointers */
 #define XR_FLAG_PARAM_GRADIENT 4u  /* also dE/dtheta for bond, angle and vdW parameters (xr_get_param_gradient) */
+#define XR_FLAG_QEQ_GRADIENT 8u    /* with XR_FLAG_PARAM_GRADIENT: also chi, eta (xr_get_param_gradient_atoms) and the
+                                    * pair table's gamma, through an adjoint QEq solve */
 
 typedef struct xr_ff xr_ff;
 typedef struct xr_ctx xr_ctx;
@@ -236,8 +238,17 @@ int xr_get_param_gradient(const xr_ctx* ctx, double* pair_grad, long long npair,
 int xr_get_param_gradient_system(const xr_ctx* ctx, int index, double* pair_grad, long long npair, double* angle_grad,
                                  long long nangle);
 
-/* Every system's gradient block of that call at once: out[s * (npair + nangle) + k], the pair
- * columns (k < npair) then the angle records, for s in call order; count = systems x (npair + nangle). */
+/* The atom-table part of that gradient: atom_grad[t*24 + column] over the atom-table columns of
+ * xr_ff_create, filled for chi and eta when the call had XR_FLAG_QEQ_GRADIENT (then the pair table's
+ * gamma column is filled too); natom = ntypes * 24. The QEq parameters change the charges, so these
+ * total derivatives come from an adjoint QEq solve: dE/dchi = 23.02 q - lambda, dE/deta = 11.51 q^2 -
+ * lambda q per atom, with lambda the solution of H lambda = dE/dq on sum lambda = 0 (no reference
+ * counterpart). index as for xr_get_param_gradient_system. */
+int xr_get_param_gradient_atoms(const xr_ctx* ctx, int index, double* atom_grad, long long natom);
+
+/* Every system's gradient block of that call at once: out[s * (npair + nangle + natom) + k], the pair
+ * columns (k < npair), the angle records, then the atom-table columns, for s in call order;
+ * count = systems x (npair + nangle + natom). */
 int xr_get_param_gradient_blocks(const xr_ctx* ctx, double* out, long long count);
 
 /* Device memory of a context (no reference counterpart; for admission by footprint): the bytes its

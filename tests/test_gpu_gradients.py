@@ -190,3 +190,56 @@ def test_angle_parameter_gradient_against_oracle():
         assert grad.angles[key][0][k] == pytest.approx(fd, rel=2e-5, abs=2e-6), k
         checked += 1
     assert checked >= 4
+
+
+def _atom_setter(s, name, base):
+    def setter(ff, d):
+        ff.atoms[s][name] = base + d
+    return setter
+
+
+@pytest.mark.parametrize("periodic", [False, True])
+def test_qeq_parameter_gradients_against_oracle(periodic):
+    """chi and eta of each element and the pair table's gamma (qeq=True: the charges' response
+    through an adjoint QEq solve) against central differences of the oracle's energies, whose dense
+    KKT solve re-solves the charges for every modified force field. A charged water cluster, and a
+    periodic water box."""
+    from xreac_gb300 import Calculator, ForceField, workloads
+    from xreac_gb300.workloads import System
+
+    if periodic:
+        system = workloads.water_box(n_mol=64, box=12.4, seed=11)
+    else:
+        base_sys = _water(n_mol=5, seed=9)
+        system = System(base_sys.symbols, base_sys.positions, None, False, 1.0, base_sys.force_field)
+    ff = ForceField.bundled(system.force_field)
+    calc = Calculator(ff)
+    ev, grad = calc.parameter_gradient(system.symbols, system.positions, cell=system.cell, pbc=system.pbc,
+                                       total_charge=system.total_charge, qeq=True)
+    _, plain = calc.parameter_gradient(system.symbols, system.positions, cell=system.cell, pbc=system.pbc,
+                                       total_charge=system.total_charge)
+    assert plain.atoms == {} and "gamma" not in plain.pairs["O", "H"]
+
+    def oracle_fd(setter, h):
+        import oracle
+
+        vals = []
+        for sgn in (1, -1):
+            f = ForceField.bundled(system.force_field)
+            setter(f, sgn * h)
+            vals.append(oracle.evaluate(f, system.symbols, system.positions, cell=system.cell, pbc=system.pbc,
+                                        total_charge=system.total_charge, need_forces=False,
+                                        dense_bond_orders=False)["energy"])
+        return (vals[0] - vals[1]) / (2 * h)
+
+    for s in ("O", "H"):
+        for name in ("chi", "eta"):
+            base = ff.atoms[s][name]
+            fd = oracle_fd(_atom_setter(s, name, base), 1e-6 * abs(base))
+            assert grad.atoms[s][name] == pytest.approx(fd, rel=1e-5, abs=1e-5), (s, name)
+    for s, t in (("O", "H"), ("O", "O"), ("H", "H")):
+        base = ff.pairs[s, t]["gamma"]
+        fd = oracle_fd(_pair_setter(s, t, "gamma", base), 1e-6 * abs(base))
+        assert grad.pairs[s, t]["gamma"] == pytest.approx(fd, rel=1e-5, abs=1e-5), (s, t)
+    # the other parameters' gradients do not change with qeq=True
+    assert grad.pairs["O", "H"]["De_s"] == pytest.approx(plain.pairs["O", "H"]["De_s"], rel=1e-12)

@@ -31,6 +31,7 @@ XR_EWAIT = 12
 XR_FLAG_FULL_DERIVATIVE = 1
 XR_FLAG_DEVICE_IO = 2
 XR_FLAG_PARAM_GRADIENT = 4
+XR_FLAG_QEQ_GRADIENT = 8
 
 EXPORTED = (
     "xr_ff_create",
@@ -67,6 +68,7 @@ EXPORTED = (
     "xr_get_param_gradient",
     "xr_get_param_gradient_system",
     "xr_get_param_gradient_blocks",
+    "xr_get_param_gradient_atoms",
     "xr_ctx_memory",
     "xr_footprint_bytes",
     "xr_count_neighbors_static",
@@ -204,6 +206,8 @@ def load():
     lib.xr_get_param_gradient_system.restype = c_int
     lib.xr_get_param_gradient_blocks.argtypes = [c_void_p, POINTER(c_double), c_longlong]
     lib.xr_get_param_gradient_blocks.restype = c_int
+    lib.xr_get_param_gradient_atoms.argtypes = [c_void_p, c_int, POINTER(c_double), c_longlong]
+    lib.xr_get_param_gradient_atoms.restype = c_int
     lib.xr_ctx_memory.argtypes = [c_void_p, POINTER(c_longlong), POINTER(c_longlong), c_int]
     lib.xr_ctx_memory.restype = c_int
     lib.xr_footprint_bytes.argtypes = [c_int, c_int, c_longlong, c_longlong]

@@ -150,6 +150,9 @@ GRADIENT_PAIR_COLUMNS = ("De_s", "De_p", "De_pp", "p_be1", "p_be2", "p_ovun1", "
                          "p_bo5", "p_bo6", "r_s", "r_p", "r_pp", "D", "alpha", "gamma_w", "r_vdW", "rcore", "ecore",
                          "acore")
 ANGLE_PARAMETERS = ("theta_00", "p_val1", "p_val2", "p_coa1", "p_val7", "p_pen1", "p_val4")
+# QEq parameters with a gradient (through the adjoint QEq solve): atom-table and pair-table columns.
+QEQ_ATOM_COLUMNS = ("chi", "eta")
+QEQ_PAIR_COLUMNS = ("gamma",)
 
 
 @dataclass
@@ -171,19 +174,23 @@ class ParameterGradient:
     ``pairs[(s, t)][name]`` and ``angles[(a, b, c)][record][k]`` (k in ``ANGLE_PARAMETERS`` order).
     A parameter the force field stores once for several keys (a pair's two orders, an angle's two
     ends) appears under each of them with the summed gradient of all its table rows, i.e. the
-    derivative with respect to that single stored value.
+    derivative with respect to that single stored value. With the QEq parameters (``qeq=True``),
+    ``atoms[s]["chi"]``, ``atoms[s]["eta"]`` and ``pairs[(s, t)]["gamma"]`` (the pair table's shielding
+    parameter) hold their total derivatives, charges' response included.
     """
 
     pairs: dict
     angles: dict
+    atoms: dict = field(default_factory=dict)
 
     @classmethod
-    def from_rows(cls, ff, pair_rows, angle_rows, angle_keys):
-        from .forcefield import PAIR_COLUMNS
+    def from_rows(cls, ff, pair_rows, angle_rows, angle_keys, atom_rows=None):
+        from .forcefield import ATOM_COLUMNS, PAIR_COLUMNS
 
         names = ff.elements
         T = len(names)
-        cols = [PAIR_COLUMNS.index(c) for c in GRADIENT_PAIR_COLUMNS]
+        pair_names = GRADIENT_PAIR_COLUMNS + (QEQ_PAIR_COLUMNS if atom_rows is not None else ())
+        cols = [PAIR_COLUMNS.index(c) for c in pair_names]
         by_obj = {}
         for si, s in enumerate(names):
             for ti, t in enumerate(names):
@@ -196,7 +203,7 @@ class ParameterGradient:
                 acc[1].append(key)
         pairs = {}
         for vec, keys in by_obj.values():
-            d = dict(zip(GRADIENT_PAIR_COLUMNS, map(float, vec)))
+            d = dict(zip(pair_names, map(float, vec)))
             for key in keys:
                 pairs[key] = d
         rec = {}
@@ -207,7 +214,12 @@ class ParameterGradient:
         angles = {}
         for key, records in ff.angles.items():
             angles[key] = [rec.get(id(r), np.zeros(7)).copy() for r in records]
-        return cls(pairs, angles)
+        atoms = {}
+        if atom_rows is not None:
+            acols = [ATOM_COLUMNS.index(c) for c in QEQ_ATOM_COLUMNS]
+            for k, s_ in enumerate(names):
+                atoms[s_] = dict(zip(QEQ_ATOM_COLUMNS, map(float, atom_rows[k, acols])))
+        return cls(pairs, angles, atoms)
 
 
 class _GuessAddresses(NamedTuple):
@@ -503,39 +515,44 @@ class Calculator:
         return self._run([(types, x, flags, cellm, float(total_charge), None)], full_derivative, [(1, 1, 1)], "ase")[0]
 
     def parameter_gradient(self, symbols, positions, *, total_charge=0, cell=None, pbc=None, initial_charges=None,
-                           full_derivative=False):
+                           full_derivative=False, qeq=False):
         """Energy, forces and dE/dtheta for the bond, angle and vdW parameters (an extension; xreac
         has no parameter derivatives). Returns ``(Evaluation, ParameterGradient)``.
 
         The gradient comes from the same hand-written adjoint as the forces: each energy kernel adds
         its parameter sensitivities, the bond-order parameters get theirs through the bond-order
         chain's adjoints. Charges do not depend on these parameters, so it is the total derivative.
-        ``full_derivative`` selects the charge-response forces, as in :meth:`evaluate`.
+        ``full_derivative`` selects the charge-response forces, as in :meth:`evaluate`. ``qeq``
+        adds the QEq parameters (chi, eta per element, the pair table's gamma), which change the
+        charges: their total derivatives take one adjoint QEq solve more.
         """
         return self.parameter_gradient_many([dict(symbols=symbols, positions=positions, total_charge=total_charge,
                                                   cell=cell, pbc=pbc, initial_charges=initial_charges)],
-                                            full_derivative=full_derivative)
+                                            full_derivative=full_derivative, qeq=qeq)
 
     def parameter_gradient_many(self, systems, *, per_system=False, full_derivative=False, parameter_sets=None,
-                                raw=False):
+                                raw=False, qeq=False):
         """As :meth:`parameter_gradient` for a batch, in one device call: the evaluations, and the
         gradient of their summed energy, or (``per_system``) one gradient per system. With
         ``parameter_sets`` (see :meth:`load_parameter_sets`) system k is evaluated with set
         ``parameter_sets[k]`` and its gradient is with respect to that set. ``raw`` returns the
         gradients as table rows instead: ``(evaluations, pair (S, T*T, 28), angle (S, R, 7))``, one
-        block per system, each row the derivative with respect to that table entry."""
+        block per system, each row the derivative with respect to that table entry, and with ``qeq``
+        the atom-table rows ``(S, T, 24)`` as a fourth item. ``qeq``: see :meth:`parameter_gradient`."""
         sets = self._sets(parameter_sets, len(systems))
+        flags_ = nat.XR_FLAG_PARAM_GRADIENT | (nat.XR_FLAG_QEQ_GRADIENT if qeq else 0)
         results = self._evaluate_items([(s["symbols"], s["positions"], s.get("total_charge", 0), s.get("cell"),
                                          s.get("pbc"), s.get("initial_charges")) for s in systems], full_derivative,
-                                       nat.XR_FLAG_PARAM_GRADIENT, sets)
+                                       flags_, sets)
         T = len(self.force_field.elements)
         if raw:
-            np_, na = T * T * 28, 7 * len(self._angle_rows)
-            blocks = np.empty((len(systems), np_ + na))
+            np_, na, nat_ = T * T * 28, 7 * len(self._angle_rows), T * 24
+            blocks = np.empty((len(systems), np_ + na + nat_))
             code = self._lib.xr_get_param_gradient_blocks(self._ctx.handle, nat.ptr(blocks, nat.c_double), blocks.size)
             if code != nat.XR_OK:
                 raise RuntimeError("parameter gradient unavailable")
-            return results, blocks[:, :np_].reshape(-1, T * T, 28), blocks[:, np_:].reshape(-1, na // 7, 7)
+            out = (results, blocks[:, :np_].reshape(-1, T * T, 28), blocks[:, np_:np_ + na].reshape(-1, na // 7, 7))
+            return out + (blocks[:, np_ + na:].reshape(-1, T, 24),) if qeq else out
         grads = []
         for index in (range(len(systems)) if per_system else (-1,)):
             pair = np.zeros(T * T * 28)
@@ -543,10 +560,16 @@ class Calculator:
             code = self._lib.xr_get_param_gradient_system(self._ctx.handle, index, nat.ptr(pair, nat.c_double),
                                                           len(pair), nat.ptr(angle, nat.c_double) if len(angle) else None,
                                                           len(angle))
+            atom = None
+            if code == nat.XR_OK and qeq:
+                atom = np.zeros(T * 24)
+                code = self._lib.xr_get_param_gradient_atoms(self._ctx.handle, index, nat.ptr(atom, nat.c_double),
+                                                             len(atom))
+                atom = atom.reshape(T, 24)
             if code != nat.XR_OK:
                 raise RuntimeError("parameter gradient unavailable")
             grads.append(ParameterGradient.from_rows(self.force_field, pair.reshape(T * T, 28), angle.reshape(-1, 7),
-                                                     self._angle_rows))
+                                                     self._angle_rows, atom))
         if per_system:
             return results, grads
         return (results[0] if len(systems) == 1 else results), grads[0]

@@ -679,22 +679,90 @@ __device__ inline void cross3(const double a[3], const double b[3], double c[3])
   c[2] = a[0] * b[1] - a[1] * b[0];
 }
 
-// Bonds with bo > 0.001 (the middles of torsion chains), compacted with warp-aggregated atomics.
-__global__ void k_torsion_middles(XrWork w) {
-  const int nb = xr_num_bonds(w);
-  const int lane = threadIdx.x & 31;
-  for (int b0 = blockIdx.x * blockDim.x; b0 < nb; b0 += gridDim.x * blockDim.x) {  // uniform per block
-    const int b = b0 + threadIdx.x;
+// Bonds with bo > 0.001 (the middles of torsion chains), compacted in bond order: the count of every
+// tile of kMidTile bonds (k_mid_count), an exclusive scan of the tile counts in one block
+// (k_mid_scan, which also stores the total in nmids), then each tile's middles at its offset
+// (k_mid_fill). The order of mids decides which middles a warp of k_torsions takes together, and with
+// that how each middle's items fall into the warp's batches of 32, i.e. the order in which they are
+// summed: a fixed order keeps the torsion and conjugation energies the same bit for bit on every
+// call. Launched with 128-thread blocks.
+constexpr int kMidTile = 128;
+
+__global__ void k_mid_count(XrWork w) {
+  __shared__ int wc[kMidTile / 32];
+  const int nb = xr_num_bonds(w), ntiles = (nb + kMidTile - 1) / kMidTile;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int b = t * kMidTile + threadIdx.x;
     const bool keep = b < nb && BFV(BF_BO, b) > THB_CUT;
     if (b < nb && !keep) {
       BEV(2, b) = 0.0;
       BEV(3, b) = 0.0;
     }
     const unsigned msk = __ballot_sync(0xffffffffu, keep);
-    int base = 0;
-    if (lane == 0 && msk) base = atomicAdd(w.nmids, __popc(msk));
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if (keep) w.mids[base + __popc(msk & ((1u << lane) - 1u))] = b;
+    if (lane == 0) wc[wid] = __popc(msk);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int c = 0;
+      for (int k = 0; k < kMidTile / 32; ++k) c += wc[k];
+      w.mid_tiles[t] = c;
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void k_mid_scan(XrWork w) {  // one block of 1024 threads
+  __shared__ int part[32];
+  __shared__ int carry_s;
+  const int nb = xr_num_bonds(w), ntiles = (nb + kMidTile - 1) / kMidTile;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (threadIdx.x == 0) carry_s = 0;
+  __syncthreads();
+  for (int base = 0; base < ntiles; base += blockDim.x) {
+    const int t = base + threadIdx.x;
+    const int v = t < ntiles ? w.mid_tiles[t] : 0;
+    int x = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, d);
+      if (lane >= d) x += y;
+    }
+    if (lane == 31) part[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+      const int p = part[lane];
+      int q = p;
+#pragma unroll
+      for (int d = 1; d < 32; d <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, q, d);
+        if (lane >= d) q += y;
+      }
+      part[lane] = q - p;  // exclusive over warps
+    }
+    __syncthreads();
+    const int carry = carry_s;
+    if (t < ntiles) w.mid_tiles[t] = carry + part[wid] + x - v;
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) carry_s = carry + part[wid] + x;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *w.nmids = carry_s;
+}
+
+__global__ void k_mid_fill(XrWork w) {
+  __shared__ int wc[kMidTile / 32];
+  const int nb = xr_num_bonds(w), ntiles = (nb + kMidTile - 1) / kMidTile;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int b = t * kMidTile + threadIdx.x;
+    const bool keep = b < nb && BFV(BF_BO, b) > THB_CUT;
+    const unsigned msk = __ballot_sync(0xffffffffu, keep);
+    if (lane == 0) wc[wid] = __popc(msk);
+    __syncthreads();
+    int off = w.mid_tiles[t];
+    for (int k = 0; k < wid; ++k) off += wc[k];
+    if (keep) w.mids[off + __popc(msk & ((1u << lane) - 1u))] = b;
+    __syncthreads();
   }
 }
 
@@ -1261,7 +1329,10 @@ void xr_launch_bonded(const XrWork& w, const XrFF& ff, cudaStream_t st) {
     k_angles<<<(chunks + kBondedWarps - 1) / kBondedWarps, 32 * kBondedWarps, 0, st>>>(w, ff);
   }
   if (w.nB > 0) {
-    k_torsion_middles<<<gB, tb, 0, st>>>(w);
+    const int gT = std::min((w.nB + kMidTile - 1) / kMidTile, 152 * 16);
+    k_mid_count<<<gT, kMidTile, 0, st>>>(w);
+    k_mid_scan<<<1, 1024, 0, st>>>(w);
+    k_mid_fill<<<gT, kMidTile, 0, st>>>(w);
     const int chunks = (w.nB + kUnits - 1) / kUnits;
     const int blocks = std::min((chunks + kBondedWarps - 1) / kBondedWarps, 152 * 16);
     k_torsions<<<blocks, 32 * kBondedWarps, 0, st>>>(w, ff);

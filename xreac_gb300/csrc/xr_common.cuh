@@ -199,6 +199,7 @@ struct XrWork {
   int* nnz;                   // [A] number of such entries per atom (every other entry has zero bond orders)
   int* mids;                  // [B] bonds with bo > 0.001 (torsion middles), compacted
   int* nmids;                 // device count of mids
+  int* mid_tiles;             // [ceil(cap_B / 128)] per-tile counts, then offsets, of the middles
   int* mlist;                 // [B] active bonds (uncorrected order passed the cut), in any order
   int* nmask;                 // length of mlist (device)
   // per-atom forward intermediates [AF_N][A] and adjoints [AJ_N][A] (structure of arrays)
@@ -215,6 +216,7 @@ struct XrWork {
   // [T*T][XR_NPAIR_COLS] pair-table columns, then [R][7] angle records.
   double* pgrad;
   int pgrad_angle_off;
+  int pgrad_atom_off;         // [T][XR_NATOM_COLS] atom-table columns after the angle records (chi, eta)
   long long pgrad_stride;     // doubles per system: each system accumulates its own gradient
   double* f;                  // [A][3] gradient dE/dx accumulator (forces = -f)
   double* qwork;              // [XR_QW_N][A] QEq solver vectors
@@ -323,6 +325,9 @@ void xr_launch_pairs(const XrWork& w, const XrFF& ff, cudaStream_t st);
 int xr_launch_qeq(const XrWork& w, const XrFF& ff, cudaStream_t st, int nblocks, const int4* map, int nteam,
                   const int* small, int nsmall, bool adjoint = false);
 void xr_launch_charge_response(const XrWork& w, const XrFF& ff, cudaStream_t st, int stage);
+// Parameter gradient of the QEq parameters from the charges and the adjoint solution (qadj):
+// chi and eta of every atom's type, the pair table's gamma of every pair's type.
+void xr_launch_qeq_param_gradient(const XrWork& w, const XrFF& ff, cudaStream_t st);
 int xr_qeq_coop_blocks_per_sm();
 // Thread-block-cluster QEq solver: `csize` blocks per cluster (kQeqClusterBatch for batches, whose
 // many systems share the SMs; kQeqClusterSingle for a single system, whose solve time is the call's

@@ -157,7 +157,7 @@ struct xr_ctx {
   double* pgrad = nullptr;  // force-field parameter gradient of the last call (when requested)
   size_t cpgrad = 0;
   std::vector<double> h_pgrad;
-  long long pgrad_pairs = 0, pgrad_angles = 0;
+  long long pgrad_pairs = 0, pgrad_angles = 0, pgrad_atoms = 0;
   int pgrad_systems = 0;  // systems of the last call with XR_FLAG_PARAM_GRADIENT (one block each)
   double* qadj = nullptr;
   size_t cqadj = 0;
@@ -176,6 +176,8 @@ struct xr_ctx {
   size_t cnnz = 0;
   int* mids = nullptr;
   int* nmids = nullptr;  // [2] torsion middles, active bonds
+  int* mid_tiles = nullptr;  // per 128-bond tile: middles counts, then offsets
+  size_t cmid_tiles = 0;
   int* mlist = nullptr;
   int* nact = nullptr;
   size_t cnact = 0;
@@ -361,6 +363,7 @@ constexpr long long kBondBytes = 3 * sizeof(int) + 4 * sizeof(double) + (BF_N + 
                                  6 * sizeof(int2) + 2 * sizeof(int);
 
 bool ensure_lists(xr_ctx* c, long long E, long long P, long long B) {
+  GROW(mid_tiles, B / 128 + 2);
   GROW(edge, E);
   GROW(edge_pair, E);
   GROW(edge_dbslot, E);
@@ -491,6 +494,7 @@ void attach_lists(xr_ctx* c, XrWork& w) {
   w.arow = c->arow;
   w.nzrow = c->nzrow;
   w.mids = c->mids;
+  w.mid_tiles = c->mid_tiles;
   w.nmids = c->nmids;
   w.nmask = c->nmids + 1;
   w.qguess = c->qguess;
@@ -1005,16 +1009,19 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
   w.nchunks = (int)nchunk;
   c->pgrad_pairs = c->pgrad_angles = 0;
   if (flags & XR_FLAG_PARAM_GRADIENT) {
-    // one gradient block per system: [pair table][angle records]
+    // one gradient block per system: [pair table][angle records][atom table]
     const long long np = (long long)ff->d.ntypes * ff->d.ntypes * XR_NPAIR_COLS, na = 7ll * ff->nangle;
-    const size_t all = (size_t)(np + na) * nsys;
+    const long long nat = (long long)ff->d.ntypes * XR_NATOM_COLS;
+    const size_t all = (size_t)(np + na + nat) * nsys;
     if (!grow(c, &c->pgrad, &c->cpgrad, all + 1)) return cuda_fail(c, cudaErrorMemoryAllocation, "allocation");
     cudaMemsetAsync(c->pgrad, 0, sizeof(double) * all, st);
     w.pgrad = c->pgrad;
     w.pgrad_angle_off = (int)np;
-    w.pgrad_stride = np + na;
+    w.pgrad_atom_off = (int)(np + na);
+    w.pgrad_stride = np + na + nat;
     c->pgrad_pairs = np;
     c->pgrad_angles = na;
+    c->pgrad_atoms = nat;
     c->pgrad_systems = nsys;
   }
   attach_lists(c, w);
@@ -1148,19 +1155,28 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
     stage(c, 4, st);
     xr_launch_coulomb(w, ff->d, st);
     launches += 1;
-    if (w.full_derivative) {
-      // charge-response forces: adjoint QEq solve with the same plan, then its radial pair terms
+    const bool qeq_grad = w.pgrad && (flags & XR_FLAG_QEQ_GRADIENT);
+    if (w.full_derivative || qeq_grad) {
+      // the adjoint QEq solve with the same plan: charge-response forces (its radial pair terms)
+      // and the QEq parameters' gradient
       xr_launch_charge_response(w, ff->d, st, 0);
       if (int le = launch_qeq(true)) return le;
-      xr_launch_charge_response(w, ff->d, st, 1);
-      launches += 4;
+      launches += 3;
+      if (w.full_derivative) {
+        xr_launch_charge_response(w, ff->d, st, 1);
+        launches += 1;
+      }
+      if (qeq_grad) {
+        xr_launch_qeq_param_gradient(w, ff->d, st);
+        launches += 1;
+      }
     }
     stage(c, 5, st);
     xr_launch_bond_orders(w, ff->d, st);
     launches += 3;
     stage(c, 6, st);
     xr_launch_bonded(w, ff->d, st);
-    launches += 11;
+    launches += 13;
     stage(c, 7, st);
     xr_launch_forces(w, ff->d, st);
     launches += 1;
@@ -1180,7 +1196,8 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
   c->last_graph = 0;
   bool done = false;
   if (c->graphs && !c->profile && qteam == 0) {
-    const int ints[] = {(int)mode, qcluster ? 1 : 0, qcsize, qblocks, qteam, qsmall, qbig, nlist, nE > 0, nP > 0, nB > 0};
+    const int ints[] = {(int)mode, qcluster ? 1 : 0, qcsize, qblocks, qteam, qsmall, qbig, nlist, nE > 0, nP > 0, nB > 0,
+                        (int)flags};
     const void* ptrs[] = {c->h_qmap_p, c->h_qsmall_p, c->bx_meta, c->bx_bo, c->bx_count};
     std::vector<unsigned char> key = launch_key(w, ff->d, ints, (int)(sizeof(ints) / sizeof(int)), ptrs, 5);
     if (c->gexec && key == c->gkey) {
@@ -1238,7 +1255,7 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
   cudaMemcpyAsync(c->h_cnt, c->cnt, sizeof(int) * 4 * (size_t)(A + 1), cudaMemcpyDeviceToHost, st);
   d2h += sizeof(int) * 4 * (long long)(A + 1);
   if (c->pgrad_pairs > 0) {
-    const size_t all = (size_t)(c->pgrad_pairs + c->pgrad_angles) * nsys;
+    const size_t all = (size_t)(c->pgrad_pairs + c->pgrad_angles + c->pgrad_atoms) * nsys;
     if (!host_grow(&c->h_pg, &c->ch_pg, all)) return cuda_fail(c, cudaErrorMemoryAllocation, "allocation");
     cudaMemcpyAsync(c->h_pg, c->pgrad, sizeof(double) * all, cudaMemcpyDeviceToHost, st);
     d2h += (long long)(sizeof(double) * all);
@@ -1295,7 +1312,8 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
   c->list_sizes[3] = nD;
   c->list_sizes[4] = c->h_small[8];  // active bonds (uncorrected order passed the cut)
   c->list_sizes[5] = c->h_small[7];  // torsion middles (bo > 0.001)
-  if (c->pgrad_pairs > 0) c->h_pgrad.assign(c->h_pg, c->h_pg + (c->pgrad_pairs + c->pgrad_angles) * nsys);
+  if (c->pgrad_pairs > 0)
+    c->h_pgrad.assign(c->h_pg, c->h_pg + (c->pgrad_pairs + c->pgrad_angles + c->pgrad_atoms) * nsys);
   c->last_A = A;
   // keep the scans for export
   c->host_cnt.assign(c->h_cnt, c->h_cnt + 4 * (size_t)(A + 1));
@@ -1667,7 +1685,8 @@ void xr_ctx_destroy(xr_ctx* c) {
                   c->bond_i, c->bond_j, c->b_r, c->b_v, c->b_fwd, c->b_adj, c->b_e, c->dbrow, c->sys, c->energy,
                   c->props, c->status, c->counts, c->barrier, c->qmap, c->qsmall, c->qiters, c->red, c->qguess, c->qrhs, c->qadj, c->pgrad, c->bx_meta, c->bx_bo, c->bx_count,
                   c->esum, c->arow, c->nact, c->nzrow, c->nnz, c->chunks, c->sys_chunks, c->chunk_part, c->mids, c->nmids, c->mlist,
-                  c->cand_cnt, c->cand_edge, c->sys_list, c->atom_cell, c->atom_slot, c->cell_cnt, c->cell_atoms};
+                  c->cand_cnt, c->cand_edge, c->sys_list, c->atom_cell, c->atom_slot, c->cell_cnt, c->cell_atoms,
+                  c->mid_tiles};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (c->h_x) cudaFreeHost(c->h_x);
@@ -1775,7 +1794,7 @@ int xr_get_param_gradient_system(const xr_ctx* c, int index, double* pair_grad, 
                                  long long nangle) {
   if (!c || c->pgrad_pairs == 0 || index < -1 || index >= c->pgrad_systems) return XR_EINPUT;
   if (npair != c->pgrad_pairs || nangle != c->pgrad_angles || !pair_grad || (nangle > 0 && !angle_grad)) return XR_EINPUT;
-  const long long stride = npair + nangle;
+  const long long stride = npair + nangle + c->pgrad_atoms;
   const int s0 = index < 0 ? 0 : index, s1 = index < 0 ? c->pgrad_systems : index + 1;
   for (long long k = 0; k < npair; ++k) pair_grad[k] = 0.0;
   for (long long k = 0; k < nangle; ++k) angle_grad[k] = 0.0;
@@ -1787,9 +1806,22 @@ int xr_get_param_gradient_system(const xr_ctx* c, int index, double* pair_grad, 
   return XR_OK;
 }
 
+int xr_get_param_gradient_atoms(const xr_ctx* c, int index, double* atom_grad, long long natom) {
+  if (!c || c->pgrad_pairs == 0 || index < -1 || index >= c->pgrad_systems || natom != c->pgrad_atoms || !atom_grad)
+    return XR_EINPUT;
+  const long long stride = c->pgrad_pairs + c->pgrad_angles + c->pgrad_atoms;
+  const int s0 = index < 0 ? 0 : index, s1 = index < 0 ? c->pgrad_systems : index + 1;
+  for (long long k = 0; k < natom; ++k) atom_grad[k] = 0.0;
+  for (int sy = s0; sy < s1; ++sy) {
+    const double* g = c->h_pgrad.data() + (size_t)sy * stride + c->pgrad_pairs + c->pgrad_angles;
+    for (long long k = 0; k < natom; ++k) atom_grad[k] += g[k];
+  }
+  return XR_OK;
+}
+
 int xr_get_param_gradient_blocks(const xr_ctx* c, double* out, long long count) {
   if (!c || c->pgrad_pairs == 0 || !out) return XR_EINPUT;
-  const long long all = (c->pgrad_pairs + c->pgrad_angles) * (long long)c->pgrad_systems;
+  const long long all = (c->pgrad_pairs + c->pgrad_angles + c->pgrad_atoms) * (long long)c->pgrad_systems;
   if (count != all) return XR_EINPUT;
   std::memcpy(out, c->h_pgrad.data(), sizeof(double) * (size_t)all);
   return XR_OK;

@@ -1891,7 +1891,41 @@ __global__ void k_charge_response_radial(XrWork w) {
   }
 }
 
+// dE/d(chi, eta, gamma) through the charges: with the KKT system H q + chi = mu 1, sum q = Q and the
+// adjoint lambda (H lambda = dE/dq - nu 1, sum lambda = 0, from the adjoint solve), the total
+// derivative of a parameter theta is dE/dtheta|_q - lambda' (dH/dtheta q + dchi/dtheta). So
+// dE/dchi_i = 23.02 q_i - lambda_i, dE/deta_i = 11.51 q_i^2 - lambda_i q_i (H_ii = eta_i + self
+// images), and for a pair's gamma (shield = taper (r^3 + gamma)^(-1/3), H_ij = 14.4 shield),
+// (332.06371 q_i q_j - 14.4 (lambda_i q_j + lambda_j q_i)) dshield/dgamma with
+// dshield/dgamma = -shield / (3 (r^3 + gamma)). Summed per element and per pair type.
+__global__ void k_qeq_param_grad(XrWork w, XrFF ff0) {
+  const int stride = gridDim.x * blockDim.x;
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < w.A; a += stride) {
+    const double q = w.q[a], lam = w.qadj[a];
+    double* ga = xr_pgrad(w, a) + w.pgrad_atom_off + (size_t)w.type[a] * XR_NATOM_COLS;
+    atomicAdd(ga + A_CHI, SELF_CONVERSION * q - lam);
+    atomicAdd(ga + A_ETA, 0.5 * SELF_CONVERSION * q * q - lam * q);
+  }
+  const int np = xr_num_pairs(w);
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += stride) {
+    const int i = w.pair_i[p], j = w.edge[w.pair_edge[p]].x;
+    const double sh = w.p_shield[p];
+    if (sh == 0.0) continue;
+    const XrFF ff = xr_ff_of(ff0, w, i);
+    const int pt = w.type[i] * ff.ntypes + w.type[j];
+    const double r = w.p_r[p], gam = pair_prm(ff, pt, P_GAMMA);
+    const double dsh = -sh / (3.0 * (r * r * r + gam));
+    const double c = C_ELE * w.q[i] * w.q[j] - QEQ_COULOMB * (w.qadj[i] * w.q[j] + w.qadj[j] * w.q[i]);
+    atomicAdd(xr_pgrad(w, i) + (size_t)pt * XR_NPAIR_COLS + P_GAMMA, c * dsh);
+  }
+}
+
 }  // namespace
+
+void xr_launch_qeq_param_gradient(const XrWork& w, const XrFF& ff, cudaStream_t st) {
+  const int n = std::max(w.A, std::max(w.nP, 1));
+  k_qeq_param_grad<<<std::min((n + 255) / 256, 152 * 8), 256, 0, st>>>(w, ff);
+}
 
 void xr_launch_charge_response(const XrWork& w, const XrFF& ff, cudaStream_t st, int stage) {
   if (stage == 0) {
