@@ -386,11 +386,12 @@ class Server:
             before = self._caps[k][name]
             cap = self._capacity(calc)
             dev_bytes = calc.memory()["device_bytes"]
-            with self._cv:
-                self.footprints[name].observe(est[0], sizes[0], est[1], sizes[2])
-                if cap != before:
-                    self.reallocations += 1
-                    self._caps[k][name] = cap
+            # no server lock: the densities only rise (a lost update between two workers is re-learned
+            # on a later batch), and worker k alone reads and writes its contexts' capacities
+            self.footprints[name].observe(est[0], sizes[0], est[1], sizes[2])
+            if cap != before:
+                self.reallocations += 1
+                self._caps[k][name] = cap
         self.batches.append(Batch(name, len(batch), sum(len(it[0]) for it in items), done - t0, calc.last_launches,
                                   its, qbytes, h2d, d2h, int(est[0]), edges, dev_bytes))
         nb = len(batch)
