@@ -222,6 +222,7 @@ struct XrWork {
   double* qwork;              // [XR_QW_N][A] QEq solver vectors
   double* red;                // reduction scratch for solvers
   unsigned* barrier;          // [2048] arrival counters of the QEq teams (indexed by a team's first block)
+  int* qsplit;                // row splits of the cluster teams' systems (k_qeq_splits)
   // outputs
   double* energy;             // [S][16]: 14 components, total, pad
   double* props;              // [S][4]: dipole xyz, pad

@@ -18,6 +18,9 @@
 
 namespace {
 
+// Most co-resident blocks of the QEq solver kernel (its team map and barrier counters).
+constexpr int kQeqBlocks = 2048;
+
 template <class T>
 bool grow(T** p, size_t* cap, size_t need) {
   if (*p && *cap >= need) return true;
@@ -178,6 +181,8 @@ struct xr_ctx {
   int* nmids = nullptr;  // [2] torsion middles, active bonds
   int* mid_tiles = nullptr;  // per 128-bond tile: middles counts, then offsets
   size_t cmid_tiles = 0;
+  int* qsplit = nullptr;     // row splits of the cluster teams' systems
+  size_t cqsplit = 0;
   int* mlist = nullptr;
   int* nact = nullptr;
   size_t cnact = 0;
@@ -350,6 +355,7 @@ bool ensure_atoms(xr_ctx* c, int A, int S) {
   GROW(qsmall, S);
   GROW(qiters, S);
   GROW(sys, S);
+  GROW(qsplit, 9 * (size_t)S + 2 * (size_t)kQeqBlocks + 9);  // cluster teams' splits, or two per grid-team block
   GROW(energy, 16 * (size_t)S);
   GROW(props, 4 * (size_t)S);
   const size_t scan_ints = 4 * ((size_t)(A + 1) / 4096 + 2);
@@ -451,6 +457,7 @@ void fill_work(xr_ctx* c, XrWork& w, int A, int S, unsigned flags) {
   w.qwork = c->qwork;
   w.red = c->red;
   w.barrier = c->barrier;
+  w.qsplit = c->qsplit;
   w.energy = c->energy;
   w.props = c->props;
   w.esum = c->esum;
@@ -623,7 +630,6 @@ constexpr int kQeqSmall = 160;
 #endif
 constexpr int kQeqTeamRows = XR_QEQ_TEAM_ROWS;  // rows per block of a grid-wide team (a multiple of 32)
 constexpr int kQeqBatchBlock = 1024;
-constexpr int kQeqBlocks = 2048;
 
 void plan_qeq(xr_ctx* c, const xr_system* sys, int nsys, int* nblocks, int* nteam, int* nsmall) {
   const int budget = std::min(c->nsm * c->coop_per_sm, kQeqBlocks);
@@ -1151,7 +1157,7 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
     if (qteam > 0) cudaMemcpyAsync(c->qmap, c->h_qmap_p, sizeof(int4) * qteam, cudaMemcpyHostToDevice, st);
     if (nlist > 0) cudaMemcpyAsync(c->qsmall, c->h_qsmall_p, sizeof(int) * nlist, cudaMemcpyHostToDevice, st);
     if (int le = launch_qeq(false)) return le;
-    launches += 1;
+    launches += (qcluster ? qbig > 0 : qteam > 0) ? 2 : 1;  // the teams' row splits, then the solver
     stage(c, 4, st);
     xr_launch_coulomb(w, ff->d, st);
     launches += 1;
@@ -1161,7 +1167,7 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
       // and the QEq parameters' gradient
       xr_launch_charge_response(w, ff->d, st, 0);
       if (int le = launch_qeq(true)) return le;
-      launches += 3;
+      launches += (qcluster ? qbig > 0 : qteam > 0) ? 4 : 3;
       if (w.full_derivative) {
         xr_launch_charge_response(w, ff->d, st, 1);
         launches += 1;
@@ -1686,7 +1692,7 @@ void xr_ctx_destroy(xr_ctx* c) {
                   c->props, c->status, c->counts, c->barrier, c->qmap, c->qsmall, c->qiters, c->red, c->qguess, c->qrhs, c->qadj, c->pgrad, c->bx_meta, c->bx_bo, c->bx_count,
                   c->esum, c->arow, c->nact, c->nzrow, c->nnz, c->chunks, c->sys_chunks, c->chunk_part, c->mids, c->nmids, c->mlist,
                   c->cand_cnt, c->cand_edge, c->sys_list, c->atom_cell, c->atom_slot, c->cell_cnt, c->cell_atoms,
-                  c->mid_tiles};
+                  c->mid_tiles, c->qsplit};
   for (void* p : bufs)
     if (p) cudaFree(p);
   if (c->h_x) cudaFreeHost(c->h_x);
