@@ -446,7 +446,7 @@ struct QeqRows {
 struct QeqShared {
   double red[kRedSmem];
   double sc_lam, sc_alpha, sc_step, sc_beta;
-  float sf_lam, sf_alpha, sf_step, sf_beta, sf_gz, sf_stop;
+  float sf_lam, sf_alpha, sf_step, sf_beta, sf_gz, sf_stop, sf_shift, sf_aold;
   double sd_s1w;  // <1, M^-1 1> of the FP32 row solver's block-Jacobi preconditioner
   // Scalars of the solve formed once, by the thread that runs a reduction's post hook (a division
   // done by every warp would cost the FP64 pipe once per warp): the start multipliers, the target,
@@ -736,71 +736,81 @@ __device__ inline int row_group(int m) {
   return g;
 }
 
-// Sum of two floats over the team: every thread passes its values; the block totals are formed in
-// warp 0 and, for a cluster team, exchanged and added in rank order; thread 0 of each block runs
-// post() on the totals (bit-identical in every block) and the block waits for it. Returns false
-// when a cluster exchange gave up.
-template <class Team, class Post>
-__device__ inline bool team_sum2f(const Team& team, const XrWork& w, float a, float b, float* smem, Post post,
-                                  int* slot = nullptr) {
+// Sum of NV floats over the team: every thread passes its values; the block totals are formed in
+// warp 0 and, for a cluster or grid team, exchanged and added in rank order; thread 0 of each block
+// runs post(t) on the totals t[0..NV) (bit-identical in every block) and the block waits for it.
+// Returns false when a team exchange gave up.
+template <int NV, class Team, class Post>
+__device__ inline bool team_sumf(const Team& team, const XrWork& w, float* v, float* smem, Post post, int* slot) {
   constexpr bool kCluster = std::is_same<Team, ClusterTeam>::value;
   constexpr bool kGrid = std::is_same<Team, GridTeam>::value;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  a = warp_total_t<float>(a);
-  b = warp_total_t<float>(b);
-  if (lane == 0) {
-    smem[wid] = a;
-    smem[32 + wid] = b;
-  }
+#pragma unroll
+  for (int k = 0; k < NV; ++k) v[k] = warp_total_t<float>(v[k]);
+  if (lane == 0)
+#pragma unroll
+    for (int k = 0; k < NV; ++k) smem[32 * k + wid] = v[k];
   __syncthreads();
-  if constexpr (kGrid) {  // a grid-wide reduction of the block totals (FP64 slots, alternating)
-    double v[2] = {0.0, 0.0};
-    if (wid == 0) {
-      v[0] = double(warp_total_t<float>(lane < nw ? smem[lane] : 0.0f));
-      v[1] = double(warp_total_t<float>(lane < nw ? smem[32 + lane] : 0.0f));
-    }
-    const bool ok = team.template reduce<2>(w, v, reinterpret_cast<double*>(smem), *slot,
-                                            [&](double* t) { post(float(t[0]), float(t[1])); });
+  if constexpr (kGrid) {
+    double d[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) d[k] = wid == 0 ? double(warp_total_t<float>(lane < nw ? smem[32 * k + lane] : 0.0f)) : 0.0;
+    const bool ok = team.template reduce<NV>(w, d, reinterpret_cast<double*>(smem), *slot, [&](double* t) {
+      float f[NV];
+#pragma unroll
+      for (int k = 0; k < NV; ++k) f[k] = float(t[k]);
+      post(f);
+    });
     *slot = *slot == 1 ? 2 : 1;
     return ok;
   }
   bool good = true;
   if (wid == 0) {
-    float x = lane < nw ? smem[lane] : 0.0f, y = lane < nw ? smem[32 + lane] : 0.0f;
-    x = warp_total_t<float>(x);
-    y = warp_total_t<float>(y);
+    float x[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) x[k] = warp_total_t<float>(lane < nw ? smem[32 * k + lane] : 0.0f);
     if constexpr (kCluster) {
       const unsigned par = ++team.count & 1;
-      const double v[2] = {double(x), double(y)};
-      double t[2];
-      good = team.template exchange<2>(w, v, par, t);
-      x = float(ClusterTeam::rank_total(t[0]));
-      y = float(ClusterTeam::rank_total(t[1]));
+      double dv[NV], t[NV];
+#pragma unroll
+      for (int k = 0; k < NV; ++k) dv[k] = double(x[k]);
+      good = team.template exchange<NV>(w, dv, par, t);
+#pragma unroll
+      for (int k = 0; k < NV; ++k) x[k] = float(ClusterTeam::rank_total(t[k]));
     }
     if (lane == 0) {
-      post(x, y);
-      if (!good) smem[64] = -1.0f;
+      post(x);
+      if (!good) smem[32 * NV] = -1.0f;
     }
   }
   if constexpr (kCluster) {
-    if (threadIdx.x == 0 && good) smem[64] = 0.0f;
+    if (threadIdx.x == 0 && good) smem[32 * NV] = 0.0f;
   }
   __syncthreads();
-  if constexpr (kCluster) return smem[64] == 0.0f;
+  if constexpr (kCluster) return smem[32 * NV] == 0.0f;
   return true;
 }
 
 // Shared-memory layout of the FP32 row solver, at the start of the kernel's dynamic shared memory,
 // for a system of n atoms of which this block owns m rows (r0 .. r1):
-//   yt[n4]  D y for every row of the system (y = M^-1 g), the vector the product gathers; n4 = n
-//           rounded up to a multiple of 4
-//   own rows, m floats each: p, Hp, x (the correction), D_ii, eta D^-1, c = H w, w = M^-1 1, g, y
+//   yt[n4]  D v for every row of the system (v = M^-1 of the vector being multiplied), the vector the
+//           product gathers; n4 = n rounded up to a multiple of 4; two such buffers for a cluster
+//   own rows, m floats each: the constants D_ii, eta D^-1, c = H w1, w1 = M^-1 1, then the solver's
+//           x (the correction), p, s, q, z, r, u, w, m~ (qeq_cg_rows32_pipelined; qeq_cg_rows32
+//           uses x, p, s, r, u)
 //   binv[8m] row r of its group's inverse block (columns: the group's rows in order)
 //   rp[m + 1] row starts relative to the cache; first[m], size[m] the group of each row (16-bit)
 // M is block-Jacobi: groups of at most 8 consecutive own rows whose atoms are joined by distances
 // below 1.3 A (molecules), each block H restricted to the group. One-row groups are Jacobi.
 constexpr int kGroupMax = 8;
 constexpr double kGroupBond = 1.3;
+// Stop of an FP32 sweep of the row solver: its squared preconditioned norm falls by this factor, or to
+// a hundredth of the final target. 1e-10 (1e-5 in norm) for the textbook CG of blocks and clusters,
+// 1e-7 (about 3e-4) for the pipelined CG of grid teams.
+template <class Team>
+__host__ __device__ constexpr double sweep_ratio32() {
+  return std::is_same<Team, GridTeam>::value ? 1e-7 : 1e-10;
+}
 
 // A team splits a system's rows between its blocks, and each block forms its block-Jacobi groups from
 // its own rows. A split between local rows r - 1 and r cuts no group when no bond shorter than
@@ -843,32 +853,47 @@ __device__ inline int qeq_aligned_split_warp(const XrWork& w, int a0, int n, int
 }
 
 struct Rows32 {
-  float *yt, *p, *hp, *x, *dd, *etadi, *cw, *wv, *gl, *yl, *binv;
+  float *yt, *dd, *etadi, *cw, *wv, *x, *p, *s, *q, *z, *rr, *u, *wq, *mt, *binv;
   int* rp;
   unsigned short *first, *size;
-  __device__ Rows32(unsigned char* base, int n, int m) {
+  int n4;
+  __device__ Rows32(unsigned char* base, int n, int m, int nyt) {
     float* f = reinterpret_cast<float*>(base);
+    n4 = (n + 3) / 4 * 4;
     yt = f;
-    p = f + (n + 3) / 4 * 4;
-    hp = p + m;
-    x = hp + m;
-    dd = x + m;
+    dd = f + nyt * n4;
     etadi = dd + m;
     cw = etadi + m;
     wv = cw + m;
-    gl = wv + m;
-    yl = gl + m;
-    binv = yl + m;
+    x = wv + m;
+    p = x + m;
+    s = p + m;
+    q = s + m;
+    z = q + m;
+    rr = z + m;
+    u = rr + m;
+    wq = u + m;
+    mt = wq + m;
+    binv = mt + m;
     rp = reinterpret_cast<int*>(binv + kGroupMax * m);
     first = reinterpret_cast<unsigned short*>(rp + m + 1);
     size = first + m;
   }
-  // FP32 scratch of the setup, 8 per row over p .. gl
-  __device__ float* scratch32() const { return p; }
+  // FP32 scratch of the setup, 8 per row over dd .. q
+  __device__ float* scratch32() const { return dd; }
+  // buffer k of the gathered vector (a cluster team alternates two)
+  __device__ float* ytb(int k) const { return yt + (k & 1) * n4; }
 };
 
-__host__ __device__ constexpr size_t rows32_bytes(int n, int m) {
-  return (4 * (size_t)((n + 3) / 4 * 4) + 4 * (size_t)(9 + kGroupMax) * m + 4 * (size_t)(m + 1) + 4 * (size_t)m + 15) /
+// Buffers of the gathered vector: two for a cluster team, whose blocks write into each other's.
+template <class Team>
+__host__ __device__ constexpr int rows32_yt_buffers() {
+  return std::is_same<Team, ClusterTeam>::value ? 2 : 1;
+}
+
+__host__ __device__ constexpr size_t rows32_bytes(int n, int m, int nyt) {
+  return (4 * (size_t)nyt * ((n + 3) / 4 * 4) + 4 * (size_t)(13 + kGroupMax) * m + 4 * (size_t)(m + 1) + 4 * (size_t)m +
+          15) /
          16 * 16;
 }
 
@@ -884,7 +909,7 @@ __device__ __noinline__ bool qeq_rows32_setup(const XrWork& w, const double* ata
   constexpr bool kGrid = std::is_same<Team, GridTeam>::value;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5, tid = threadIdx.x;
   const int m = r1 - r0;
-  Rows32 R(qeq_dyn, n, m);
+  Rows32 R(qeq_dyn, n, m, rows32_yt_buffers<Team>());
   const double* DI = &QW(Q_DINV, 0);
   const int gs = row_group(m), sub = lane & (gs - 1), gpw = 32 / gs;
   // 1. for every own row, the latest of the kGroupMax - 1 own rows before it that is bonded to it
@@ -993,7 +1018,7 @@ __device__ __noinline__ bool qeq_rows32_setup(const XrWork& w, const double* ata
       for (int q = 0; q < kGroupMax; ++q) R.binv[kGroupMax * (f + r) + q] = q >= k ? 0.0f : ok ? a[q] : (q == r ? di : 0.0f);
     }
   }
-  __syncthreads();  // the scratch (p .. gl) is free again
+  __syncthreads();  // the scratch (dd .. q) is free again
   // 5. Jacobi rows, w = M^-1 1 (the stored inverse rows' sums), D, eta D^-1, the row starts
   double s1[1] = {0.0};
   for (int i = tid; i < m; i += blockDim.x) {
@@ -1047,30 +1072,27 @@ __device__ __noinline__ bool qeq_rows32_setup(const XrWork& w, const double* ata
   return true;
 }
 
-// The FP32 solve of a refinement sweep with every vector in shared memory (layout Rows32): a system
-// of at most 1024 atoms solved by one block (rows [0, n)) or by a thread-block cluster, or a larger
-// system by a grid-wide team (this block's rows [r0, r1)). Projected PCG with the block-Jacobi M of
-// the setup:
-// z = M^-1 (g - lambda 1) with lambda = <w, g> / <w, 1>; the product gathers yt = D M^-1 g over the
-// pre-scaled rows (H'_ij = H_ij / D_jj), so H z = H'yt - lambda c. g is kept projected (shifted
-// by the multiplier each step), so <g, z> is free of cancellation. A group of lanes per row forms
-// the product and its first lane the first update; a thread per row the second update and the
-// group products M^-1 g. In a cluster each block writes its rows' D M^-1 g into every other
-// block's yt before the second reduction, whose exchange publishes it; a grid team writes it to
-// global memory (gyt) and every block stages the whole vector after the reduction. The iteration
-// stops when
-// <g, z> falls to `ratio` times its start value. The correction x of the own rows is written to
-// y_out (global, indexed by atom).
+// The FP32 solve of a refinement sweep with every vector in shared memory (layout Rows32) for a system
+// of at most 1024 atoms solved by one block (rows [0, n)) or by a thread-block cluster. Projected
+// PCG with the block-Jacobi M of the setup: z = M^-1 (g - lambda 1) with lambda = <w1, g> / <w1, 1>;
+// the product gathers yt = D M^-1 g over the pre-scaled rows (H'_ij = H_ij / D_jj), so
+// H z = H'yt - lambda c. g is kept projected (shifted by the multiplier each step), so <g, z> is free
+// of cancellation. A group of lanes per row forms the product and its first lane the first update;
+// a thread per row the second update and the group products M^-1 g. Two team reductions per
+// iteration: p'Hp with <w1, Hp> after the product, the new norm after the preconditioner. In a
+// cluster each block writes its rows' D M^-1 g into every other block's yt before the second
+// reduction, whose exchange publishes it; the writes alternate between two yt buffers, so that
+// the first one cannot reach a block still gathering the setup's vector. Stops when <g, z> falls
+// to `ratio` times its start value (the vectors g, Hp and y of the description live in the
+// layout's r, s and u). The correction x of the own rows is written to y_out (global, by atom).
 template <class Team>
 __device__ __noinline__ int qeq_cg_rows32(const XrWork& w, const Team& team, QeqShared& sh, int a0, int n, int r0,
-                                          int r1, const QeqMatrix<float>& M, float* y_out, double ratio, int max_it,
-                                          float* gyt, int* slot) {
+                                          int r1, const QeqMatrix<float>& M, float* y_out, double ratio, int max_it, int* slot) {
   extern __shared__ __align__(16) unsigned char qeq_dyn[];
   constexpr bool kCluster = std::is_same<Team, ClusterTeam>::value;
-  constexpr bool kGrid = std::is_same<Team, GridTeam>::value;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5, tid = threadIdx.x;
   const int m = r1 - r0;
-  Rows32 R(qeq_dyn, n, m);
+  Rows32 R(qeq_dyn, n, m, rows32_yt_buffers<Team>());
   // the row cache: in this block's shared memory, or FP32 rows in global memory
   const bool cache_shared = __isShared(M.cache_h);
   const float* const ch_g = M.cache_h;
@@ -1082,48 +1104,46 @@ __device__ __noinline__ int qeq_cg_rows32(const XrWork& w, const Team& team, Qeq
   const double* G = &QW(Q_G, 0);
   float* red = reinterpret_cast<float*>(sh.red);
   const float s1 = float(sh.sd_s1w);
-  unsigned remote = 0;
-  if constexpr (kCluster) remote = smem_u32(R.yt + r0);
+  // exchange parity: the setup's product gathered buffer 0, so the first publish writes buffer 1 (a
+  // cluster's blocks write into each other's; a block alone has one buffer)
+  int buf = 1;
+  auto yt_of = [&](int k) -> float* { return kCluster ? R.ytb(k) : R.yt; };
   auto publish = [&](int i, float v) {  // D M^-1 g of own row i, here and in the other blocks
-    R.yt[r0 + i] = v;
+    float* yt = yt_of(buf);
+    yt[r0 + i] = v;
     if constexpr (kCluster) {
+      const unsigned remote = smem_u32(yt + r0 + i);
       for (int r = 0; r < team.nb; ++r)
-        if (r != team.rank) asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(cluster_map(remote + 4 * i, r)), "f"(v) : "memory");
-    }
-    if constexpr (kGrid) gyt[a0 + r0 + i] = v;  // global: the other blocks stage it after the reduction
-  };
-  auto stage = [&]() {  // a grid team's whole yt from global memory, after the reduction that published it
-    if constexpr (kGrid) {
-      for (int q = tid; q < n; q += blockDim.x) R.yt[q] = __ldcg(gyt + a0 + q);
-      __syncthreads();
+        if (r != team.rank) asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(cluster_map(remote, r)), "f"(v) : "memory");
     }
   };
   auto group_apply = [&](int i) {  // (M^-1 g)_i over the group of row i
     const int f = R.first[i], k = R.size[i];
     const float* bi = R.binv + kGroupMax * i;
     float t = 0.0f;
-    for (int b = 0; b < k; ++b) t += bi[b] * R.gl[f + b];
+    for (int b = 0; b < k; ++b) t += bi[b] * R.rr[f + b];
     return t;
   };
   for (int i = tid; i < m; i += blockDim.x) {
-    R.gl[i] = float(__ldcg(G + a0 + r0 + i));
+    R.rr[i] = float(__ldcg(G + a0 + r0 + i));
     R.p[i] = 0.0f;
-    R.hp[i] = 0.0f;
+    R.s[i] = 0.0f;
     R.x[i] = 0.0f;
   }
   __syncthreads();
   float u0 = 0.0f, u1 = 0.0f;
   for (int i = tid; i < m; i += blockDim.x) {
     const float y = group_apply(i);
-    R.yl[i] = y;
+    R.u[i] = y;
     publish(i, y * R.dd[i]);
-    u0 += R.wv[i] * R.gl[i];
-    u1 += R.gl[i] * y;
+    u0 += R.wv[i] * R.rr[i];
+    u1 += R.rr[i] * y;
   }
   // start: lambda = <w, g> / <w, 1>, and <g - lambda, M^-1 (g - lambda)> = <g, M^-1 g> - lambda <w, g>
-  if (!team_sum2f(team, w, u0, u1, red, [&](float t0, float t1) {
-        const float lam = t0 / s1;
-        const float gz = t1 - lam * t0;
+  float acc[2] = {u0, u1};
+  if (!team_sumf<2>(team, w, acc, red, [&](const float* t) {
+        const float lam = t[0] / s1;
+        const float gz = t[1] - lam * t[0];
         sh.sf_lam = lam;
         sh.sf_beta = 0.0f;
         sh.sf_gz = gz;
@@ -1131,7 +1151,7 @@ __device__ __noinline__ int qeq_cg_rows32(const XrWork& w, const Team& team, Qeq
         sh.sc_state = (!(gz > 0.0f) || n < 2) ? 1 : 0;
       }, slot))
     return -1;
-  stage();
+  const float* yt = yt_of(buf);
   const float fstop = sh.sf_stop;
   const int gs = row_group(m), sub = lane & (gs - 1), gpw = 32 / gs;
   int it = 0;
@@ -1150,12 +1170,12 @@ __device__ __noinline__ int qeq_cg_rows32(const XrWork& w, const Team& team, Qeq
       for (; e + 3 * gs < ee; e += 4 * gs) {
         const float h0 = ch[e], h1 = ch[e + gs], h2 = ch[e + 2 * gs], h3 = ch[e + 3 * gs];
         const int j0 = cj[e], j1 = cj[e + gs], j2 = cj[e + 2 * gs], j3 = cj[e + 3 * gs];
-        s += h0 * R.yt[j0];
-        s += h1 * R.yt[j1];
-        s += h2 * R.yt[j2];
-        s += h3 * R.yt[j3];
+        s += h0 * yt[j0];
+        s += h1 * yt[j1];
+        s += h2 * yt[j2];
+        s += h3 * yt[j3];
       }
-      for (; e < ee; e += gs) s += ch[e] * R.yt[cj[e]];
+      for (; e < ee; e += gs) s += ch[e] * yt[cj[e]];
       return s;
     };
     for (int ib = wid * gpw; ib < m; ib += nw * gpw) {
@@ -1165,53 +1185,259 @@ __device__ __noinline__ int qeq_cg_rows32(const XrWork& w, const Team& team, Qeq
         s = cache_shared ? row_dot(ch_s, cj_s, R.rp[i] + sub, R.rp[i + 1]) : row_dot(ch_g, cj_g, R.rp[i] + sub, R.rp[i + 1]);
       for (int o = gs / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
       if (sub == 0 && i < m) {
-        const float hz = s + R.etadi[i] * R.yt[r0 + i] - lam * R.cw[i];
-        const float z = R.yl[i] - lam * R.wv[i];
+        const float hz = s + R.etadi[i] * yt[r0 + i] - lam * R.cw[i];
+        const float z = R.u[i] - lam * R.wv[i];
         const float pv = -z + beta * R.p[i];
-        const float hpv = -hz + beta * R.hp[i];
+        const float hpv = -hz + beta * R.s[i];
         R.p[i] = pv;
-        R.hp[i] = hpv;
-        R.gl[i] -= lam;
+        R.s[i] = hpv;
+        R.rr[i] -= lam;
         php0 += pv * hpv;
         php1 += R.wv[i] * hpv;
       }
     }
-    if (!team_sum2f(team, w, php0, php1, red, [&](float t0, float t1) {
+    acc[0] = php0;
+    acc[1] = php1;
+    if (!team_sumf<2>(team, w, acc, red, [&](const float* t) {
           const float gz = sh.sf_gz;
-          if (!(fabsf(t0) > 0.0f) || !isfinite(t0)) {
+          if (!(fabsf(t[0]) > 0.0f) || !isfinite(t[0])) {
             sh.sc_state = 2;  // breakdown: the FP64 residual of the sweep decides what follows
           } else {
-            sh.sf_alpha = gz / t0;
-            sh.sf_step = sh.sf_alpha * t1 / s1;
+            sh.sf_alpha = gz / t[0];
+            sh.sf_step = sh.sf_alpha * t[1] / s1;
           }
         }, slot))
       return -1;
     if (sh.sc_state != 0) break;
     const float alpha = sh.sf_alpha, step = sh.sf_step;
     for (int i = tid; i < m; i += blockDim.x) {
-      R.gl[i] = (R.gl[i] + alpha * R.hp[i]) - step;
+      R.rr[i] = (R.rr[i] + alpha * R.s[i]) - step;
       R.x[i] += alpha * R.p[i];
     }
     __syncthreads();  // the group products read the other rows of the group
     u0 = 0.0f;
     u1 = 0.0f;
+    buf ^= 1;
     for (int i = tid; i < m; i += blockDim.x) {
       const float y = group_apply(i);
-      R.yl[i] = y;
+      R.u[i] = y;
       publish(i, y * R.dd[i]);
-      u0 += R.wv[i] * R.gl[i];
-      u1 += R.gl[i] * y;
+      u0 += R.wv[i] * R.rr[i];
+      u1 += R.rr[i] * y;
     }
-    if (!team_sum2f(team, w, u0, u1, red, [&](float t0, float t1) {
-          const float lamn = t0 / s1;
-          const float gzn = t1 - lamn * t0;
+    acc[0] = u0;
+    acc[1] = u1;
+    if (!team_sumf<2>(team, w, acc, red, [&](const float* t) {
+          const float lamn = t[0] / s1;
+          const float gzn = t[1] - lamn * t[0];
           sh.sf_lam = lamn;
           sh.sf_beta = gzn / sh.sf_gz;
           sh.sf_gz = gzn;
           if (gzn <= fstop) sh.sc_state = 1;
         }, slot))
       return -1;
+    yt = yt_of(buf);
+  }
+  for (int i = tid; i < m; i += blockDim.x) y_out[a0 + r0 + i] = R.x[i];
+  __syncthreads();
+  return it;
+}
+
+// The FP32 solve of a refinement sweep of a grid-wide team (this block's rows [r0, r1) of a system
+// above the cluster sizes), every vector in shared memory (layout Rows32).
+//
+// Pipelined projected PCG (Ghysels and Vanroose's recurrences) with the block-Jacobi M of the
+// setup, on  minimise 1/2 y'Hy + g0'y  subject to  sum y = 0,  with residual r = -g:
+//   u = P r, w = H u with P = M^-1 - w1 w1' / s1 (w1 = M^-1 1, s1 = <1, w1>: z = P r sums to zero);
+//   per iteration gamma = r'u, delta = w'u and pi = <w1, w> are reduced together, while the
+//   preconditioned m~ = M^-1 w is exchanged in the same team operation; after it m = m~ - w1 pi/s1,
+//   n = H m = H m~ - c pi/s1 (c = H w1 from the setup), beta = gamma / gamma_old,
+//   alpha = gamma / (delta - beta gamma / alpha_old), and the recurrences
+//   z = n + beta z, q = m + beta q, s = w + beta s, p = u + beta p,
+//   y += alpha p, r -= alpha s, u -= alpha q, w -= alpha z.
+// One grid-wide reduction per iteration instead of the textbook form's two (about 4 us each on the
+// water box). The extra recurrences lose accuracy in FP32 over long runs, so a sweep stops at a
+// relative norm of about 3e-4 (sweep_ratio32) and the FP64 refinement restarts it: on the water
+// box, the C/H/O box and the stream's 500-atom systems an FP32 emulation took 1-5 % more
+// iterations than the textbook form, over four sweeps instead of three. Block and cluster teams,
+// whose reductions cost far less, keep the textbook form (qeq_cg_rows32): there the extra sweep
+// cost more than the saved reductions.
+//
+// The product gathers yt = D m~ over the pre-scaled rows (H'_ij = H_ij / D_jj). A group of lanes
+// per row forms the product and its first lane the updates; a thread per row the partial sums and
+// the group products M^-1 w. Every block writes its rows' D m~ to global memory before the
+// reduction and stages the whole vector after it, alternating two global buffers (gyt0, gyt1): a
+// block writes buffer k & 1 for exchange k only after exchange k - 1, which every block entered
+// after staging exchange k - 2's buffer. (Written for any team: a cluster alternates two shared
+// buffers the same way.) The iteration stops when gamma falls to `ratio` times its start value.
+// The correction y of the own rows is written to y_out (global, indexed by atom).
+template <class Team>
+__device__ __noinline__ int qeq_cg_rows32_pipelined(const XrWork& w, const Team& team, QeqShared& sh, int a0, int n,
+                                                    int r0, int r1, const QeqMatrix<float>& M, float* y_out,
+                                                    double ratio, int max_it, float* gyt0, float* gyt1, int* slot) {
+  extern __shared__ __align__(16) unsigned char qeq_dyn[];
+  constexpr bool kCluster = std::is_same<Team, ClusterTeam>::value;
+  constexpr bool kGrid = std::is_same<Team, GridTeam>::value;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5, tid = threadIdx.x;
+  const int m = r1 - r0;
+  Rows32 R(qeq_dyn, n, m, rows32_yt_buffers<Team>());
+  // the row cache: in this block's shared memory, or FP32 rows in global memory
+  const bool cache_shared = __isShared(M.cache_h);
+  const float* const ch_g = M.cache_h;
+  const unsigned short* const cj_g = M.cache_j;
+  const float* const ch_s =
+      reinterpret_cast<const float*>(qeq_dyn + (cache_shared ? (reinterpret_cast<const unsigned char*>(M.cache_h) - qeq_dyn) : 0));
+  const unsigned short* const cj_s = reinterpret_cast<const unsigned short*>(
+      qeq_dyn + (cache_shared ? (reinterpret_cast<const unsigned char*>(M.cache_j) - qeq_dyn) : 0));
+  const double* G = &QW(Q_G, 0);
+  float* red = reinterpret_cast<float*>(sh.red);
+  const float s1 = float(sh.sd_s1w);
+  // exchange parity: the setup's product gathered buffer 0, so the first exchange writes buffer 1
+  int buf = 1;
+  auto yt_of = [&](int k) -> float* { return kCluster ? R.ytb(k) : R.yt; };
+  auto publish = [&](int i, float v) {  // D m~ of own row i, here and in the other blocks
+    float* yt = yt_of(buf);
+    yt[r0 + i] = v;
+    if constexpr (kCluster) {
+      const unsigned remote = smem_u32(yt + r0 + i);
+      for (int r = 0; r < team.nb; ++r)
+        if (r != team.rank) asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(cluster_map(remote, r)), "f"(v) : "memory");
+    }
+    if constexpr (kGrid) (buf ? gyt1 : gyt0)[a0 + r0 + i] = v;  // the other blocks stage it after the reduction
+  };
+  auto stage = [&]() {  // a grid team's whole yt from global memory, after the reduction that published it
+    if constexpr (kGrid) {
+      const float* src = buf ? gyt1 : gyt0;
+      for (int q = tid; q < n; q += blockDim.x) R.yt[q] = __ldcg(src + a0 + q);
+      __syncthreads();
+    }
+  };
+  auto group_apply = [&](const float* v, int i) {  // (M^-1 v)_i over the group of row i
+    const int f = R.first[i], k = R.size[i];
+    const float* bi = R.binv + kGroupMax * i;
+    float t = 0.0f;
+    for (int b = 0; b < k; ++b) t += bi[b] * v[f + b];
+    return t;
+  };
+  const int gs = row_group(m), sub = lane & (gs - 1), gpw = 32 / gs;
+  // The product H'yt over the cached rows (gs lanes per row, four entries per lane in flight: the rows
+  // may stream from L2 rather than shared memory); the first lane of the row's group then runs
+  // epi(i, sum) with the off-diagonal sum (the diagonal term is etadi * yt).
+  auto product = [&](auto epi) {
+    const float* yt = yt_of(buf);
+    auto row_dot = [&](const float* ch, const unsigned short* cj, int e, int ee) {
+      float t = 0.0f;
+      for (; e + 3 * gs < ee; e += 4 * gs) {
+        const float h0 = ch[e], h1 = ch[e + gs], h2 = ch[e + 2 * gs], h3 = ch[e + 3 * gs];
+        const int j0 = cj[e], j1 = cj[e + gs], j2 = cj[e + 2 * gs], j3 = cj[e + 3 * gs];
+        t += h0 * yt[j0];
+        t += h1 * yt[j1];
+        t += h2 * yt[j2];
+        t += h3 * yt[j3];
+      }
+      for (; e < ee; e += gs) t += ch[e] * yt[cj[e]];
+      return t;
+    };
+    for (int ib = wid * gpw; ib < m; ib += nw * gpw) {
+      const int i = ib + lane / gs;
+      float t = 0.0f;
+      if (i < m)
+        t = cache_shared ? row_dot(ch_s, cj_s, R.rp[i] + sub, R.rp[i + 1]) : row_dot(ch_g, cj_g, R.rp[i] + sub, R.rp[i + 1]);
+      for (int o = gs / 2; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+      if (sub == 0 && i < m) epi(i, t + R.etadi[i] * yt[r0 + i]);
+    }
+  };
+  // start: r = -g0, u~ = M^-1 r exchanged with the reduction of <w1, r> and <r, u~>; then
+  // u = u~ - w1 <w1, r>/s1 and w = H u = H u~ - c <w1, r>/s1
+  for (int i = tid; i < m; i += blockDim.x) {
+    R.rr[i] = -float(__ldcg(G + a0 + r0 + i));
+    R.x[i] = 0.0f;
+    R.p[i] = 0.0f;
+    R.s[i] = 0.0f;
+    R.q[i] = 0.0f;
+    R.z[i] = 0.0f;
+  }
+  __syncthreads();
+  float acc[3] = {0.0f, 0.0f, 0.0f};
+  for (int i = tid; i < m; i += blockDim.x) {
+    const float t = group_apply(R.rr, i);
+    R.u[i] = t;
+    publish(i, t * R.dd[i]);
+    acc[0] += R.wv[i] * R.rr[i];
+    acc[1] += R.rr[i] * t;
+  }
+  if (!team_sumf<2>(team, w, acc, red, [&](const float* t) {
+        const float shift = t[0] / s1;
+        const float gam = t[1] - shift * t[0];  // <r, P r>
+        sh.sf_shift = shift;
+        sh.sf_stop = float(ratio) * gam;
+        sh.sc_state = (!(gam > 0.0f) || n < 2) ? 1 : 0;
+      }, slot))
+    return -1;
+  stage();
+  if (sh.sc_state == 0) {
+    const float shift = sh.sf_shift;
+    product([&](int i, float hv) {
+      R.wq[i] = hv - shift * R.cw[i];
+      R.u[i] -= shift * R.wv[i];
+    });
+    __syncthreads();  // the group products read the other rows of the group
+  }
+  const float fstop = sh.sf_stop;
+  int it = 0;
+  while (sh.sc_state == 0) {
+    buf ^= 1;
+    acc[0] = acc[1] = acc[2] = 0.0f;
+    for (int i = tid; i < m; i += blockDim.x) {
+      const float t = group_apply(R.wq, i);
+      R.mt[i] = t;
+      publish(i, t * R.dd[i]);
+      acc[0] += R.rr[i] * R.u[i];
+      acc[1] += R.wq[i] * R.u[i];
+      acc[2] += R.wv[i] * R.wq[i];
+    }
+    const bool more = it < max_it;
+    if (!team_sumf<3>(team, w, acc, red, [&](const float* t) {
+          const float gam = t[0], dlt = t[1];
+          if (gam <= fstop || !more) {
+            sh.sc_state = 1;
+            return;
+          }
+          const float beta = it == 0 ? 0.0f : gam / sh.sf_gz;
+          const float php = it == 0 ? dlt : dlt - beta * gam / sh.sf_aold;  // p'Hp
+          if (!(fabsf(php) > 0.0f) || !isfinite(php) || !isfinite(gam)) {
+            sh.sc_state = 2;  // breakdown: the FP64 residual of the sweep decides what follows
+            return;
+          }
+          const float alpha = gam / php;
+          sh.sf_beta = beta;
+          sh.sf_alpha = alpha;
+          sh.sf_aold = alpha;
+          sh.sf_gz = gam;
+          sh.sf_shift = t[2] / s1;
+        }, slot))
+      return -1;
+    if (sh.sc_state != 0) break;
     stage();
+    const float alpha = sh.sf_alpha, beta = sh.sf_beta, shift = sh.sf_shift;
+    product([&](int i, float hv) {
+      const float nv = hv - shift * R.cw[i];
+      const float mv = R.mt[i] - shift * R.wv[i];
+      const float zv = nv + beta * R.z[i];
+      const float qv = mv + beta * R.q[i];
+      const float sv = R.wq[i] + beta * R.s[i];
+      const float pv = R.u[i] + beta * R.p[i];
+      R.z[i] = zv;
+      R.q[i] = qv;
+      R.s[i] = sv;
+      R.p[i] = pv;
+      R.x[i] += alpha * pv;
+      R.rr[i] -= alpha * sv;
+      R.u[i] -= alpha * qv;
+      R.wq[i] -= alpha * zv;
+    });
+    __syncthreads();  // the group products read the other rows of the group
+    ++it;
   }
   for (int i = tid; i < m; i += blockDim.x) y_out[a0 + r0 + i] = R.x[i];
   __syncthreads();
@@ -1273,8 +1499,11 @@ __device__ bool qeq_residual(const XrWork& w, const double* atab, const Team& te
     acc2[0] += DI[a] * g * g;
   }
   rows_sum_all<1>(acc2, r1 - r0);
-  // (and the stop ratio of a sweep from here: 1e-10 of the norm, no further than 1e-2 of the target)
-  auto ratio = [&](double* t) { sh.sd_ratio = t[0] > 0.0 ? fmax(1e-10 * t[0], 0.01 * target) / t[0] : 1.0; };
+  // (and the stop ratio of the row solver's next sweep from here: sweep_ratio32 of the norm, no
+  // further than 1e-2 of the target)
+  auto ratio = [&](double* t) {
+    sh.sd_ratio = t[0] > 0.0 ? fmax(sweep_ratio32<Team>() * t[0], 0.01 * target) / t[0] : 1.0;
+  };
   if (!team_sum<1>(team, w, acc2, sh.red, slot, ratio)) return false;
   slot = slot == 1 ? 2 : 1;
   *gz_out = acc2[0];
@@ -1318,7 +1547,7 @@ __device__ void qeq_solve(const XrWork& w, const double* atab, const Team& team,
   // rows fit, else FP64 values + columns (10 B), else nothing (rows read from global memory).
   // A block that solves a system of at most 1024 atoms alone keeps every row's FP32 state in shared
   // memory instead, and so does each block of a cluster team for its rows plus the whole vector the
-  // product gathers (layout Rows32: 4 B per atom of the system and 72 B per own row), and at least
+  // product gathers (layout Rows32: 4 B per atom of the system, 8 B in a cluster, and 92 B per own row), and at least
   // the n doubles of the FP64 stage of a fallback.
   constexpr bool kBlock = std::is_same<Team, BlockTeam>::value;
   constexpr bool kCluster = std::is_same<Team, ClusterTeam>::value;
@@ -1327,9 +1556,10 @@ __device__ void qeq_solve(const XrWork& w, const double* atab, const Team& team,
   int team_rows = n;  // the most rows any block of the team owns (the same value in every block)
   if constexpr (kGridTeam) team_rows = min(n, ((n + team.nb - 1) / team.nb + 31) / 32 * 32 + kGroupMax);
   const bool small_rows =
-      dyn != nullptr && ((kBlock || kCluster) ? n <= 1024 : rows32_bytes(n, team_rows) <= (size_t)dyn_bytes / 2);
+      dyn != nullptr && ((kBlock || kCluster) ? n <= 1024 : rows32_bytes(n, team_rows, 1) <= (size_t)dyn_bytes / 2);
   const int stage_n = (dyn != nullptr && (small_rows || n * 8 <= dyn_bytes / 2)) ? n : 0;
-  const size_t stage_bytes = small_rows ? std::max<size_t>(rows32_bytes(n, r1 - r0), 8 * (size_t)n) : 8 * (size_t)stage_n;
+  const size_t stage_bytes =
+      small_rows ? std::max<size_t>(rows32_bytes(n, r1 - r0, rows32_yt_buffers<Team>()), 8 * (size_t)n) : 8 * (size_t)stage_n;
   void* gstage = stage_n > 0 ? dyn : nullptr;
   unsigned char* region = dyn != nullptr ? dyn + stage_bytes : nullptr;
   const long long region_bytes = dyn != nullptr ? dyn_bytes - (long long)stage_bytes : 0;
@@ -1520,7 +1750,7 @@ __device__ void qeq_solve(const XrWork& w, const double* atab, const Team& team,
   if (!team_sum<3>(team, w, acc2, smem, 1, [&](double* t) {
         sh.sd_target = w.cg_tol * w.cg_tol * t[1];
         sh.sd_gfloor = 1e-28 * fmax(acc[2], acc[4]);
-        sh.sd_ratio = t[0] > 0.0 ? fmax(1e-10 * t[0], 0.01 * sh.sd_target) / t[0] : 1.0;
+        sh.sd_ratio = t[0] > 0.0 ? fmax(sweep_ratio32<Team>() * t[0], 0.01 * sh.sd_target) / t[0] : 1.0;
       }))
     return;
   const double target = sh.sd_target, gfloor = sh.sd_gfloor;
@@ -1558,11 +1788,19 @@ __device__ void qeq_solve(const XrWork& w, const double* atab, const Team& team,
         }
         if (!team.sync(w)) return;
       }
-      // the correction's own projected norm starts at gz; 1e-10 of it (1e-5 in norm) per sweep,
-      // and no further than a hundredth of the final target (sd_ratio: that stop over gz)
-      const int it = small_rows ? qeq_cg_rows32(w, team, sh, a0, n, r0, r1, M32, v32.y, sh.sd_ratio, budget, v32.g, &slot)
-                                : qeq_cg<Team, float>(w, atab, team, sh, a0, n, r0, r1, v32, M32, s1, gz,
-                                                      fmax(1e-10 * gz, 0.01 * target), 0.0, budget, false, slot);
+      // the correction's own projected norm starts at gz; the row solver stops at sweep_ratio32 of it
+      // per sweep (sd_ratio), the FP32 CG over global rows at 1e-10 (1e-5 in norm), both no further
+      // than a hundredth of the final target
+      int it = 0;
+      if (small_rows) {
+        if constexpr (kGridTeam)
+          it = qeq_cg_rows32_pipelined(w, team, sh, a0, n, r0, r1, M32, v32.y, sh.sd_ratio, budget, v32.g, v32.g2, &slot);
+        else
+          it = qeq_cg_rows32(w, team, sh, a0, n, r0, r1, M32, v32.y, sh.sd_ratio, budget, &slot);
+      } else {
+        it = qeq_cg<Team, float>(w, atab, team, sh, a0, n, r0, r1, v32, M32, s1, gz, fmax(1e-10 * gz, 0.01 * target), 0.0,
+                                 budget, false, slot);
+      }
       if (it < 0) return;
       iters += it;
       // x += y, then restore sum x = Q exactly: the FP32 step keeps sum y = 0 only to FP32 rounding,
