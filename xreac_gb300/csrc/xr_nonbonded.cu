@@ -270,6 +270,76 @@ struct GridTeam {
     for (int k = 0; k < NV; ++k) v[k] = res[k];
     return ok;
   }
+  // The same for NV <= 4 floats (the FP32 sweeps' scalars): slots of four floats per rank, one
+  // 16-byte load per rank, and FP32 sums. An FP64 add occupies this part's FP64 pipe for 64
+  // cycles per warp instruction, so the double form's 30 dependent adds for three values took
+  // about 1 us of the reduction.
+  template <int NV, class Post>
+  __device__ bool reducef(const XrWork& w, float* v, double* smem, int slot, Post post) const {
+    static_assert(NV <= 4, "at most four values per reduction");
+    __shared__ int ok;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    target += nb;
+    float* res = reinterpret_cast<float*>(result_slot(smem, slot));
+    float* rs = reinterpret_cast<float*>(red + (size_t)slot * 8 * nb);  // [rank][4]
+    if (wid == 0) {
+      int good = 1;
+      __syncwarp();  // orders warp 0's row writes before lane 0's release
+      if (lane == 0) {
+        float4 o = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        if (NV > 0) o.x = v[0];
+        if (NV > 1) o.y = v[1];
+        if (NV > 2) o.z = v[2];
+        if (NV > 3) o.w = v[3];
+        reinterpret_cast<float4*>(rs)[rank] = o;
+        asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(bar) : "memory");
+        const long long cap = wait_cap(w, 1ll << 24);
+        const bool poisoned = wait_poisoned(w, target / nb);
+        long long it = 0;
+        while (poisoned || ld_acquire(bar) < target) {
+          if (++it > cap || ((it & 255) == 0 && (*(volatile int*)w.status & XR_S_BARRIER))) {
+            atomicOr(w.status, XR_S_BARRIER);
+            good = 0;
+            break;
+          }
+          if (it > 256) __nanosleep(32);
+        }
+        ok = good;
+      }
+      __syncwarp();
+      // each lane adds its ranks in order, then a fixed shuffle tree: deterministic
+      float t[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+      for (int base = 0; base < nb; base += 5 * 32) {
+        float4 x[5];
+#pragma unroll
+        for (int u = 0; u < 5; ++u) {
+          const int q = base + lane + 32 * u;
+          x[u] = q < nb ? __ldcg(reinterpret_cast<const float4*>(rs) + q) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        }
+#pragma unroll
+        for (int u = 0; u < 5; ++u) {
+          t[0] += x[u].x;
+          t[1] += x[u].y;
+          t[2] += x[u].z;
+          t[3] += x[u].w;
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < NV; ++k) {
+        float s = t[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        t[k] = s;
+      }
+      if (lane == 0) {
+        for (int k = 0; k < NV; ++k) res[k] = t[k];
+        post(res);
+      }
+    }
+    __syncthreads();
+    for (int k = 0; k < NV; ++k) v[k] = res[k];
+    return ok;
+  }
 };
 
 struct BlockTeam {
@@ -752,15 +822,10 @@ __device__ inline bool team_sumf(const Team& team, const XrWork& w, float* v, fl
     for (int k = 0; k < NV; ++k) smem[32 * k + wid] = v[k];
   __syncthreads();
   if constexpr (kGrid) {
-    double d[NV];
+    float f[NV];
 #pragma unroll
-    for (int k = 0; k < NV; ++k) d[k] = wid == 0 ? double(warp_total_t<float>(lane < nw ? smem[32 * k + lane] : 0.0f)) : 0.0;
-    const bool ok = team.template reduce<NV>(w, d, reinterpret_cast<double*>(smem), *slot, [&](double* t) {
-      float f[NV];
-#pragma unroll
-      for (int k = 0; k < NV; ++k) f[k] = float(t[k]);
-      post(f);
-    });
+    for (int k = 0; k < NV; ++k) f[k] = wid == 0 ? warp_total_t<float>(lane < nw ? smem[32 * k + lane] : 0.0f) : 0.0f;
+    const bool ok = team.template reducef<NV>(w, f, reinterpret_cast<double*>(smem), *slot, post);
     *slot = *slot == 1 ? 2 : 1;
     return ok;
   }
@@ -1319,7 +1384,11 @@ __device__ __noinline__ int qeq_cg_rows32_pipelined(const XrWork& w, const Team&
     for (int b = 0; b < k; ++b) t += bi[b] * v[f + b];
     return t;
   };
-  const int gs = row_group(m), sub = lane & (gs - 1), gpw = 32 / gs;
+  // lanes per row: the fewest that take the block's rows in one pass over its warps (a block of 33
+  // rows would otherwise give its first warp a second row, and the team waits for that block)
+  int gs = 32;
+  while (gs > 4 && m * gs > (int)blockDim.x) gs >>= 1;
+  const int sub = lane & (gs - 1), gpw = 32 / gs;
   // The product H'yt over the cached rows (gs lanes per row, four entries per lane in flight: the rows
   // may stream from L2 rather than shared memory); the first lane of the row's group then runs
   // epi(i, sum) with the off-diagonal sum (the diagonal term is etadi * yt).
