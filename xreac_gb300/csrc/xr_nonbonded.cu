@@ -1372,8 +1372,23 @@ __device__ __noinline__ int qeq_cg_rows32_pipelined(const XrWork& w, const Team&
   };
   auto stage = [&]() {  // a grid team's whole yt from global memory, after the reduction that published it
     if constexpr (kGrid) {
-      const float* src = buf ? gyt1 : gyt0;
-      for (int q = tid; q < n; q += blockDim.x) R.yt[q] = __ldcg(src + a0 + q);
+      const float* src = (buf ? gyt1 : gyt0) + a0;
+      // 16-byte loads from the first 16-byte boundary on; the few elements before it and after the
+      // last whole vector one by one
+      const int head = min(n, int((16 - (reinterpret_cast<uintptr_t>(src) & 15)) & 15) / 4);
+      const int nv4 = (n - head) / 4;
+      const float4* src4 = reinterpret_cast<const float4*>(src + head);
+      for (int q = tid; q < nv4; q += blockDim.x) {
+        const float4 v = __ldcg(src4 + q);
+        float* d = R.yt + head + 4 * q;
+        d[0] = v.x;
+        d[1] = v.y;
+        d[2] = v.z;
+        d[3] = v.w;
+      }
+      const int rest = head + 4 * nv4;
+      if (tid < head) R.yt[tid] = __ldcg(src + tid);
+      if (tid < n - rest) R.yt[rest + tid] = __ldcg(src + rest + tid);
       __syncthreads();
     }
   };
