@@ -446,7 +446,61 @@ struct ClusterTeam {
     }
     return good;
   }
+  // exchange() for NV <= 8 floats (the FP32 sweeps' scalars): the same protocol on a float view of
+  // the slot arrays, so that the totals are FP32 adds (an FP64 add occupies this part's FP64 pipe for
+  // 64 cycles per warp instruction: the FP64 totals and post hook took about 0.45 us of each
+  // reduction).
+  template <int NV>
+  __device__ bool exchangef(const XrWork& w, const float* v, unsigned par, float* t) const {
+    const int lane = threadIdx.x & 31;
+    const unsigned m = count;
+    float* fslots = reinterpret_cast<float*>(slots);  // [parity][rank][16]
+    __syncwarp();
+    if (lane < nb) {
+      const unsigned dst = cluster_map(smem_u32(fslots + (par * 8 + rank) * 16), lane);
+#pragma unroll
+      for (int k = 0; k < NV; ++k) asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(dst + 4 * k), "f"(v[k]) : "memory");
+      asm volatile("st.release.cluster.shared::cluster.u32 [%0], %1;" ::"r"(cluster_map(smem_u32(seqs + par * 8 + rank), lane)),
+                   "r"(m)
+                   : "memory");
+    }
+    bool mine = lane >= nb;
+    const unsigned mine_addr = smem_u32(seqs + par * 8 + (lane & 7));
+    const long long cap = wait_cap(w, 1ll << 22);
+    const bool poisoned = wait_poisoned(w, m);
+    long long it = 0;
+    int good = 1;
+    for (;;) {
+      if (!mine) {
+        unsigned sq;
+        asm volatile("ld.acquire.cluster.shared::cta.u32 %0, [%1];" : "=r"(sq) : "r"(mine_addr) : "memory");
+        mine = sq == m && !poisoned;
+      }
+      if (__all_sync(0xffffffffu, mine)) break;
+      bool stop = ++it > cap;
+      if (lane == 0 && (it & 1023) == 0) stop = stop || (*(volatile int*)w.status & XR_S_BARRIER);
+      if (__any_sync(0xffffffffu, stop)) {
+        if (lane == 0) atomicOr(w.status, XR_S_BARRIER);
+        good = 0;
+        break;
+      }
+    }
+    if (lane < nb) {
+      const float* src = fslots + (par * 8 + lane) * 16;
+#pragma unroll
+      for (int k = 0; k < NV; ++k) t[k] = src[k];
+    } else {
+#pragma unroll
+      for (int k = 0; k < NV; ++k) t[k] = 0.0f;
+    }
+    return good;
+  }
   // Totals of the entries over lanes 0..7 of warp 0, a fixed tree (the same in every block).
+  __device__ static float rank_totalf(float t) {
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+    return t;
+  }
   __device__ static double rank_total(double t) {
 #pragma unroll
     for (int o = 4; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
@@ -836,12 +890,10 @@ __device__ inline bool team_sumf(const Team& team, const XrWork& w, float* v, fl
     for (int k = 0; k < NV; ++k) x[k] = warp_total_t<float>(lane < nw ? smem[32 * k + lane] : 0.0f);
     if constexpr (kCluster) {
       const unsigned par = ++team.count & 1;
-      double dv[NV], t[NV];
+      float t[NV];
+      good = team.template exchangef<NV>(w, x, par, t);
 #pragma unroll
-      for (int k = 0; k < NV; ++k) dv[k] = double(x[k]);
-      good = team.template exchange<NV>(w, dv, par, t);
-#pragma unroll
-      for (int k = 0; k < NV; ++k) x[k] = float(ClusterTeam::rank_total(t[k]));
+      for (int k = 0; k < NV; ++k) x[k] = ClusterTeam::rank_totalf(t[k]);
     }
     if (lane == 0) {
       post(x);
@@ -861,8 +913,7 @@ __device__ inline bool team_sumf(const Team& team, const XrWork& w, float* v, fl
 //   yt[n4]  D v for every row of the system (v = M^-1 of the vector being multiplied), the vector the
 //           product gathers; n4 = n rounded up to a multiple of 4; two such buffers for a cluster
 //   own rows, m floats each: the constants D_ii, eta D^-1, c = H w1, w1 = M^-1 1, then the solver's
-//           x (the correction), p, s, q, z, r, u, w, m~ (qeq_cg_rows32_pipelined; qeq_cg_rows32
-//           uses x, p, s, r, u)
+//           x (the correction), p, s, r, u, and for the pipelined solver of grid teams q, z, w, m~
 //   binv[8m] row r of its group's inverse block (columns: the group's rows in order)
 //   rp[m + 1] row starts relative to the cache; first[m], size[m] the group of each row (16-bit)
 // M is block-Jacobi: groups of at most 8 consecutive own rows whose atoms are joined by distances
@@ -918,11 +969,12 @@ __device__ inline int qeq_aligned_split_warp(const XrWork& w, int a0, int n, int
 }
 
 struct Rows32 {
-  float *yt, *dd, *etadi, *cw, *wv, *x, *p, *s, *q, *z, *rr, *u, *wq, *mt, *binv;
+  float *yt, *dd, *etadi, *cw, *wv, *x, *p, *s, *rr, *u, *q, *z, *wq, *mt, *binv;
   int* rp;
   unsigned short *first, *size;
   int n4;
-  __device__ Rows32(unsigned char* base, int n, int m, int nyt) {
+  // nyt gathered-vector buffers; nvec per-row vectors (rows32_vectors)
+  __device__ Rows32(unsigned char* base, int n, int m, int nyt, int nvec) {
     float* f = reinterpret_cast<float*>(base);
     n4 = (n + 3) / 4 * 4;
     yt = f;
@@ -933,18 +985,18 @@ struct Rows32 {
     x = wv + m;
     p = x + m;
     s = p + m;
-    q = s + m;
-    z = q + m;
-    rr = z + m;
+    rr = s + m;
     u = rr + m;
-    wq = u + m;
+    q = u + m;  // q, z, w, m~: the pipelined solver's only
+    z = q + m;
+    wq = z + m;
     mt = wq + m;
-    binv = mt + m;
+    binv = dd + nvec * m;
     rp = reinterpret_cast<int*>(binv + kGroupMax * m);
     first = reinterpret_cast<unsigned short*>(rp + m + 1);
     size = first + m;
   }
-  // FP32 scratch of the setup, 8 per row over dd .. q
+  // FP32 scratch of the setup, 8 per row over dd .. rr
   __device__ float* scratch32() const { return dd; }
   // buffer k of the gathered vector (a cluster team alternates two)
   __device__ float* ytb(int k) const { return yt + (k & 1) * n4; }
@@ -956,9 +1008,17 @@ __host__ __device__ constexpr int rows32_yt_buffers() {
   return std::is_same<Team, ClusterTeam>::value ? 2 : 1;
 }
 
-__host__ __device__ constexpr size_t rows32_bytes(int n, int m, int nyt) {
-  return (4 * (size_t)nyt * ((n + 3) / 4 * 4) + 4 * (size_t)(13 + kGroupMax) * m + 4 * (size_t)(m + 1) + 4 * (size_t)m +
-          15) /
+// Per-row vectors: the constants D, eta D^-1, c, w1 and the textbook solver's x, p, s, r, u; the
+// pipelined solver of grid teams adds q, z, w, m~.
+template <class Team>
+__host__ __device__ constexpr int rows32_vectors() {
+  return std::is_same<Team, GridTeam>::value ? 13 : 9;
+}
+
+template <class Team>
+__host__ __device__ constexpr size_t rows32_bytes(int n, int m) {
+  return (4 * (size_t)rows32_yt_buffers<Team>() * ((n + 3) / 4 * 4) + 4 * (size_t)(rows32_vectors<Team>() + kGroupMax) * m +
+          4 * (size_t)(m + 1) + 4 * (size_t)m + 15) /
          16 * 16;
 }
 
@@ -974,7 +1034,7 @@ __device__ __noinline__ bool qeq_rows32_setup(const XrWork& w, const double* ata
   constexpr bool kGrid = std::is_same<Team, GridTeam>::value;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5, tid = threadIdx.x;
   const int m = r1 - r0;
-  Rows32 R(qeq_dyn, n, m, rows32_yt_buffers<Team>());
+  Rows32 R(qeq_dyn, n, m, rows32_yt_buffers<Team>(), rows32_vectors<Team>());
   const double* DI = &QW(Q_DINV, 0);
   const int gs = row_group(m), sub = lane & (gs - 1), gpw = 32 / gs;
   // 1. for every own row, the latest of the kGroupMax - 1 own rows before it that is bonded to it
@@ -1083,7 +1143,7 @@ __device__ __noinline__ bool qeq_rows32_setup(const XrWork& w, const double* ata
       for (int q = 0; q < kGroupMax; ++q) R.binv[kGroupMax * (f + r) + q] = q >= k ? 0.0f : ok ? a[q] : (q == r ? di : 0.0f);
     }
   }
-  __syncthreads();  // the scratch (dd .. q) is free again
+  __syncthreads();  // the scratch (dd .. rr) is free again
   // 5. Jacobi rows, w = M^-1 1 (the stored inverse rows' sums), D, eta D^-1, the row starts
   double s1[1] = {0.0};
   for (int i = tid; i < m; i += blockDim.x) {
@@ -1157,7 +1217,7 @@ __device__ __noinline__ int qeq_cg_rows32(const XrWork& w, const Team& team, Qeq
   constexpr bool kCluster = std::is_same<Team, ClusterTeam>::value;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5, tid = threadIdx.x;
   const int m = r1 - r0;
-  Rows32 R(qeq_dyn, n, m, rows32_yt_buffers<Team>());
+  Rows32 R(qeq_dyn, n, m, rows32_yt_buffers<Team>(), rows32_vectors<Team>());
   // the row cache: in this block's shared memory, or FP32 rows in global memory
   const bool cache_shared = __isShared(M.cache_h);
   const float* const ch_g = M.cache_h;
@@ -1345,7 +1405,7 @@ __device__ __noinline__ int qeq_cg_rows32_pipelined(const XrWork& w, const Team&
   constexpr bool kGrid = std::is_same<Team, GridTeam>::value;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5, tid = threadIdx.x;
   const int m = r1 - r0;
-  Rows32 R(qeq_dyn, n, m, rows32_yt_buffers<Team>());
+  Rows32 R(qeq_dyn, n, m, rows32_yt_buffers<Team>(), rows32_vectors<Team>());
   // the row cache: in this block's shared memory, or FP32 rows in global memory
   const bool cache_shared = __isShared(M.cache_h);
   const float* const ch_g = M.cache_h;
@@ -1631,7 +1691,8 @@ __device__ void qeq_solve(const XrWork& w, const double* atab, const Team& team,
   // rows fit, else FP64 values + columns (10 B), else nothing (rows read from global memory).
   // A block that solves a system of at most 1024 atoms alone keeps every row's FP32 state in shared
   // memory instead, and so does each block of a cluster team for its rows plus the whole vector the
-  // product gathers (layout Rows32: 4 B per atom of the system, 8 B in a cluster, and 92 B per own row), and at least
+  // product gathers (layout Rows32: 4 B per atom of the system, 8 B in a cluster, and 76 B per own row, 92 B in a
+  // grid team), and at least
   // the n doubles of the FP64 stage of a fallback.
   constexpr bool kBlock = std::is_same<Team, BlockTeam>::value;
   constexpr bool kCluster = std::is_same<Team, ClusterTeam>::value;
@@ -1640,10 +1701,10 @@ __device__ void qeq_solve(const XrWork& w, const double* atab, const Team& team,
   int team_rows = n;  // the most rows any block of the team owns (the same value in every block)
   if constexpr (kGridTeam) team_rows = min(n, ((n + team.nb - 1) / team.nb + 31) / 32 * 32 + kGroupMax);
   const bool small_rows =
-      dyn != nullptr && ((kBlock || kCluster) ? n <= 1024 : rows32_bytes(n, team_rows, 1) <= (size_t)dyn_bytes / 2);
+      dyn != nullptr && ((kBlock || kCluster) ? n <= 1024 : rows32_bytes<Team>(n, team_rows) <= (size_t)dyn_bytes / 2);
   const int stage_n = (dyn != nullptr && (small_rows || n * 8 <= dyn_bytes / 2)) ? n : 0;
   const size_t stage_bytes =
-      small_rows ? std::max<size_t>(rows32_bytes(n, r1 - r0, rows32_yt_buffers<Team>()), 8 * (size_t)n) : 8 * (size_t)stage_n;
+      small_rows ? std::max<size_t>(rows32_bytes<Team>(n, r1 - r0), 8 * (size_t)n) : 8 * (size_t)stage_n;
   void* gstage = stage_n > 0 ? dyn : nullptr;
   unsigned char* region = dyn != nullptr ? dyn + stage_bytes : nullptr;
   const long long region_bytes = dyn != nullptr ? dyn_bytes - (long long)stage_bytes : 0;
