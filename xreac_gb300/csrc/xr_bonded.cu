@@ -1310,7 +1310,7 @@ static int active_grid(const XrWork& w, int tb) { return std::max(1, std::min((w
 void xr_launch_bond_orders(const XrWork& w, const XrFF& ff, cudaStream_t st) {
   const int tb = 128;
   const int gB = (w.nB + tb - 1) / tb;
-  cudaMemsetAsync(w.nmids, 0, 2 * sizeof(int), st);  // torsion middles, active bonds
+  // (the torsion-middle and active-bond counters were zeroed by k_prep)
   if (w.nB > 0) k_bo1<<<gB, tb, 0, st>>>(w, ff);
   k_deltap<<<(w.A + 3) / 4, 128, 0, st>>>(w);
   if (w.nB > 0) k_bo2<<<active_grid(w, tb), tb, 0, st>>>(w, ff);

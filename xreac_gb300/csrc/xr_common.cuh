@@ -52,6 +52,7 @@ enum XrStatusBits {
   XR_S_BARRIER = 1 << 8,      // a grid barrier wait reached its iteration limit
   XR_S_REVERSE = 1 << 9,      // an edge without its reverse (internal consistency check)
   XR_S_LIMIT = 1 << 10,       // an atom has more active bonds than the packed item indices hold
+  XR_S_BAD_PACK = 1 << 11,    // an atom's packed type and system word was out of range (internal check)
 };
 
 // Edge code: three 9-bit signed image shifts plus flags. Sx sits in the highest shift bits so the
@@ -150,6 +151,12 @@ struct XrWork {
   const double4_32a* x;           // positions (w unused)
   const int* type;
   const int* sys_of;
+  // Set when the host packed each atom's type and system into the unused 8 bytes of its position
+  // (low and high 32 bits of x[a].w): k_prep then writes type and sys_of itself, and a call uploads
+  // one array instead of three.
+  int types_in_x;
+  int prep_zero;              // k_prep zeroes the call's counters (evaluations; not the static count)
+  int* bx_count;              // exported bonds of the call (zeroed by k_prep)
   int4* wrap;                 // integer lattice wrap of each atom
   float4* xw;                 // wrapped position minus origin, FP32
   float4* fw;                 // wrapped fractional coordinates, FP32

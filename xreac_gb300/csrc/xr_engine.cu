@@ -240,10 +240,6 @@ struct xr_ctx {
   double stage_ms[kStages] = {};
   long long stage_calls = 0;
   // compact export of nonzero bonds: {bond, i, j, code} and bo
-  int4* bx_meta = nullptr;
-  size_t cbx_meta = 0;
-  double* bx_bo = nullptr;
-  size_t cbx_bo = 0;
   int* bx_count = nullptr;
   std::vector<int4> h_bx_meta;
   std::vector<double> h_bx_bo;
@@ -264,14 +260,6 @@ struct xr_ctx {
   size_t ch_qmap_p = 0;
   int* h_qsmall_p = nullptr;
   size_t ch_qsmall_p = 0;
-  int* h_cnt = nullptr;  // [4][A+1] scans of the last evaluation
-  size_t ch_cnt = 0;
-  int4* h_bxm = nullptr;
-  size_t ch_bxm = 0;
-  double* h_bxb = nullptr;
-  size_t ch_bxb = 0;
-  int* h_qit = nullptr;
-  size_t ch_qit = 0;
   double* h_pg = nullptr;
   size_t ch_pg = 0;
   double* h_out = nullptr;
@@ -445,6 +433,7 @@ void fill_work(xr_ctx* c, XrWork& w, int A, int S, unsigned flags) {
   w.x = c->x;
   w.type = c->type;
   w.sys_of = c->sys_of;
+  w.bx_count = c->bx_count;
   w.wrap = c->wrap;
   w.xw = c->xw;
   w.fw = c->fw;
@@ -511,6 +500,32 @@ void attach_lists(xr_ctx* c, XrWork& w) {
   w.mlist = c->mlist;
 }
 
+// One exported bond: (bond id, i, j, image code) and its corrected order.
+struct __align__(16) XrBondRecord {
+  int4 meta;
+  double bo;
+  double pad;
+};
+
+// The result block of a call, in doubles from the start of outbuf (device) and h_out (host): per-atom
+// values [8 A], energies [16 S], properties [4 S], the tail of ints (kTailInts counters, the systems'
+// QEq iterations [S], the scans [4 (A + 1)]), then the exported bonds as 32-byte records. Kernels
+// write all of it, so one copy brings a call's results back.
+constexpr int kTailInts = 5;  // status, exported bonds, QEq iterations, torsion middles, active bonds
+struct ResultLayout {
+  size_t energy, props, tail, bonds, end;
+};
+ResultLayout result_layout(int A, int nsys, long long nB) {
+  ResultLayout L;
+  L.energy = 8 * (size_t)A;
+  L.props = L.energy + 16 * (size_t)nsys;
+  L.tail = L.props + 4 * (size_t)nsys;
+  const size_t tail_ints = kTailInts + (size_t)nsys + 4 * (size_t)(A + 1);
+  L.bonds = (L.tail + (tail_ints + 1) / 2 + 3) / 4 * 4;
+  L.end = L.bonds + 4 * (size_t)std::max<long long>(nB, 0);
+  return L;
+}
+
 // Packs forces (-dE/dx), charges, total bond orders, lone pairs and bond counts per atom.
 __global__ void k_pack(XrWork w, double* out) {
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
@@ -540,6 +555,26 @@ __global__ void k_unpack_device(XrWork w, double* forces, double* charges, doubl
   if (counts) counts[a] = (int)w.a_fwd[(size_t)AF_COUNT30 * w.A + a];
 }
 
+// Energies, properties and the tail of ints into the result block (its layout: result_layout), after
+// every other kernel of the call.
+__global__ void k_gather_tail(XrWork w, double* block, size_t energy_off, size_t tail_off) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x, nt = gridDim.x * blockDim.x;
+  double* e = block + energy_off;
+  for (int k = t; k < 20 * w.S; k += nt) e[k] = k < 16 * w.S ? w.energy[k] : w.props[k - 16 * w.S];
+  int* ti = reinterpret_cast<int*>(block + tail_off);
+  if (t == 0) {
+    ti[0] = *w.status;
+    ti[1] = *w.bx_count;
+    ti[2] = w.counts[4];
+    ti[3] = w.nmids[0];
+    ti[4] = w.nmids[1];
+  }
+  for (int k = t; k < w.S; k += nt) ti[kTailInts + k] = w.qiters[k];
+  int* tc = ti + kTailInts + w.S;
+  const int nc = 4 * (w.A + 1);
+  for (int k = t; k < nc; k += nt) tc[k] = w.cnt[k];
+}
+
 __global__ void k_positions_from_device(const double* pos, double4_32a* x, int n) {
   const int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= n) return;
@@ -547,7 +582,7 @@ __global__ void k_positions_from_device(const double* pos, double4_32a* x, int n
 }
 
 // Nonzero corrected bond orders, compacted with warp-aggregated atomics; the host restores bond order.
-__global__ void k_bond_export(XrWork w, int4* meta, double* bo_out, int* counter) {
+__global__ void k_bond_export(XrWork w, XrBondRecord* rec, int* counter) {
   const int nb = xr_num_bonds(w);
   const int lane = threadIdx.x & 31;
   for (int b0 = blockIdx.x * blockDim.x; b0 < nb; b0 += gridDim.x * blockDim.x) {  // uniform per block
@@ -561,8 +596,11 @@ __global__ void k_bond_export(XrWork w, int4* meta, double* bo_out, int* counter
     if (keep) {
       const int slot = base + __popc(m & ((1u << lane) - 1u));
       const int code = w.edge[w.pair_edge[w.bond_pair[b]]].y;
-      meta[slot] = make_int4(b, w.bond_i[b], w.bond_j[b], code);
-      bo_out[slot] = bo;
+      XrBondRecord r;
+      r.meta = make_int4(b, w.bond_i[b], w.bond_j[b], code);
+      r.bo = bo;
+      r.pad = 0.0;
+      rec[slot] = r;
     }
   }
 }
@@ -587,6 +625,10 @@ int status_to_code(xr_ctx* c, int st) {
   if (st & XR_S_REVERSE) {
     c->err = "neighbors must include both directions: (i, j, S) and (j, i, -S)";
     return XR_EINPUT;
+  }
+  if (st & XR_S_BAD_PACK) {
+    c->err = "internal error: an atom's packed type and system were out of range";
+    return XR_ECUDA;
   }
   if (st & XR_S_BOC_NAN) {
     c->err = "Invalid p_boc mixing for an active bond-order correction";
@@ -845,13 +887,11 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
     return XR_EINPUT;
   }
   const int A = (int)A64;
-  if (!ensure_atoms(c, A, nsys) || !host_grow(&c->h_x, &c->ch_x, (size_t)A) ||
-      !host_grow(&c->h_out, &c->ch_out, 8 * (size_t)A + 32 * (size_t)nsys + 8))
+  if (!ensure_atoms(c, A, nsys) || !host_grow(&c->h_x, &c->ch_x, (size_t)A))
     return cuda_fail(c, cudaErrorMemoryAllocation, "allocation");
   c->host_sys.resize(nsys);
   if (!host_grow(&c->h_types, &c->ch_types, (size_t)A) || !host_grow(&c->h_sysof, &c->ch_sysof, (size_t)A) ||
-      !host_grow(&c->h_sysd, &c->ch_sysd, (size_t)nsys) || !host_grow(&c->h_qit, &c->ch_qit, (size_t)nsys) ||
-      !host_grow(&c->h_cnt, &c->ch_cnt, 4 * (size_t)(A + 1)))
+      !host_grow(&c->h_sysd, &c->ch_sysd, (size_t)nsys))
     return cuda_fail(c, cudaErrorMemoryAllocation, "allocation");
   int* types = c->h_types;
   int* sys_of = c->h_sysof;
@@ -880,6 +920,10 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
       }
       types[off + a] = t;
       sys_of[off + a] = s;
+      if (!dev_io) {
+        const unsigned long long bits = (unsigned long long)(unsigned)t | ((unsigned long long)(unsigned)s << 32);
+        std::memcpy(&c->h_x[off + a].w, &bits, sizeof(bits));
+      }
     }
     if (in.charges_guess) {
       // starting charges of the QEq solve (a warm start), shifted onto sum q = total_charge
@@ -999,19 +1043,21 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
     cudaMemcpyAsync(c->qguess, c->h_guess, sizeof(double) * A, cudaMemcpyHostToDevice, st);
     h2d += sizeof(double) * (long long)A;
   }
-  cudaMemcpyAsync(c->type, types, sizeof(int) * A, cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(c->sys_of, sys_of, sizeof(int) * A, cudaMemcpyHostToDevice, st);
+  if (dev_io) {  // else types and systems travel in the positions' fourth words, unpacked by k_prep
+    cudaMemcpyAsync(c->type, types, sizeof(int) * A, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(c->sys_of, sys_of, sizeof(int) * A, cudaMemcpyHostToDevice, st);
+    h2d += 2 * sizeof(int) * (long long)A;
+  }
   cudaMemcpyAsync(c->sys, c->h_sysd, sizeof(XrSystem) * nsys, cudaMemcpyHostToDevice, st);
   cudaMemcpyAsync(c->chunks, chunk_tab, sizeof(int4) * nchunk, cudaMemcpyHostToDevice, st);
   cudaMemcpyAsync(c->sys_chunks, sys_chunk_tab, sizeof(int2) * nsys, cudaMemcpyHostToDevice, st);
-  h2d += 2 * sizeof(int) * (long long)A + sizeof(XrSystem) * (long long)nsys +
-         (long long)(sizeof(int4) * nchunk + sizeof(int2) * nsys);
+  h2d += sizeof(XrSystem) * (long long)nsys + (long long)(sizeof(int4) * nchunk + sizeof(int2) * nsys);
+  // (counts, QEq iterations, scans, torsion-middle and exported-bond counters: zeroed by k_prep)
   cudaMemsetAsync(c->status, 0, sizeof(int), st);
-  cudaMemsetAsync(c->counts, 0, 8 * sizeof(int), st);
-  cudaMemsetAsync(c->qiters, 0, sizeof(int) * nsys, st);
-  cudaMemsetAsync(c->cnt, 0, sizeof(int) * 4 * (size_t)(A + 1), st);
   XrWork w;
   fill_work(c, w, A, nsys, flags);
+  w.types_in_x = dev_io ? 0 : 1;
+  w.prep_zero = 1;
   w.nchunks = (int)nchunk;
   c->pgrad_pairs = c->pgrad_angles = 0;
   if (flags & XR_FLAG_PARAM_GRADIENT) {
@@ -1130,8 +1176,10 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
     if (nlist > 0) std::memcpy(c->h_qsmall_p, c->h_qsmall.data(), sizeof(int) * nlist);
     h2d += sizeof(int4) * (long long)qteam + sizeof(int) * (long long)nlist;
   }
-  if (!grow(c, &c->bx_meta, &c->cbx_meta, (size_t)std::max(nB, 1)) || !grow(c, &c->bx_bo, &c->cbx_bo, (size_t)std::max(nB, 1)))
-    return cuda_fail(c, cudaErrorMemoryAllocation, "bond export");
+  const ResultLayout RL = result_layout(A, nsys, nB);
+  if (!grow(c, &c->outbuf, &c->coutbuf, RL.end) || !host_grow(&c->h_out, &c->ch_out, RL.end))
+    return cuda_fail(c, cudaErrorMemoryAllocation, "result block");
+  XrBondRecord* const bx_rec = reinterpret_cast<XrBondRecord*>(c->outbuf + RL.bonds);
   auto launch_qeq = [&](bool adjoint) {
     return qcluster ? xr_launch_qeq_cluster(w, ff->d, st, qcsize, qblocks, c->qsmall, qbig, qsmall, adjoint)
                     : xr_launch_qeq(w, ff->d, st, qblocks, c->qmap, qteam, c->qsmall, qsmall, adjoint);
@@ -1188,9 +1236,8 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
     launches += 1;
     xr_launch_reduce(w, ff->d, st);
     launches += 3;
-    cudaMemsetAsync(c->bx_count, 0, sizeof(int), st);
-    if (nB > 0) {
-      k_bond_export<<<(nB + 255) / 256, 256, 0, st>>>(w, c->bx_meta, c->bx_bo, c->bx_count);
+    if (nB > 0) {  // (its counter was zeroed by k_prep)
+      k_bond_export<<<(nB + 255) / 256, 256, 0, st>>>(w, bx_rec, c->bx_count);
       ++launches;
     }
     return (int)cudaGetLastError();
@@ -1204,7 +1251,7 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
   if (c->graphs && !c->profile && qteam == 0) {
     const int ints[] = {(int)mode, qcluster ? 1 : 0, qcsize, qblocks, qteam, qsmall, qbig, nlist, nE > 0, nP > 0, nB > 0,
                         (int)flags};
-    const void* ptrs[] = {c->h_qmap_p, c->h_qsmall_p, c->bx_meta, c->bx_bo, c->bx_count};
+    const void* ptrs[] = {c->h_qmap_p, c->h_qsmall_p, bx_rec, c->bx_count, c->outbuf};
     std::vector<unsigned char> key = launch_key(w, ff->d, ints, (int)(sizeof(ints) / sizeof(int)), ptrs, 5);
     if (c->gexec && key == c->gkey) {
       if (cudaGraphLaunch(c->gexec, st) == cudaSuccess) {
@@ -1246,45 +1293,35 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
   }
   if (!done)
     if (int le = sequence()) return cuda_fail(c, (cudaError_t)le, "launch");
-  cudaMemcpyAsync(c->h_small + 5, c->bx_count, sizeof(int), cudaMemcpyDeviceToHost, st);
-  cudaMemcpyAsync(c->h_small + 6, c->counts + 4, sizeof(int), cudaMemcpyDeviceToHost, st);
-  cudaMemcpyAsync(c->h_qit, c->qiters, sizeof(int) * nsys, cudaMemcpyDeviceToHost, st);
-  d2h += sizeof(int) * (long long)nsys;
-  // bond export (the nonzero bonds are a prefix of at most nB entries), the scans and the parameter
-  // gradient come back in the same stream, so the call synchronises once more only at its end
-  if (!host_grow(&c->h_bxm, &c->ch_bxm, (size_t)std::max(nB, 1)) || !host_grow(&c->h_bxb, &c->ch_bxb, (size_t)std::max(nB, 1)))
-    return cuda_fail(c, cudaErrorMemoryAllocation, "allocation");
-  if (nB > 0) {
-    cudaMemcpyAsync(c->h_bxm, c->bx_meta, sizeof(int4) * nB, cudaMemcpyDeviceToHost, st);
-    cudaMemcpyAsync(c->h_bxb, c->bx_bo, sizeof(double) * nB, cudaMemcpyDeviceToHost, st);
+  // Results: the per-atom values (k_pack, or the caller's device arrays), then energies, properties,
+  // counters, QEq iterations and scans (k_gather_tail) into the result block, where k_bond_export has
+  // written the exported bonds (at most nB records); one copy brings the block back, and the call
+  // synchronises once more only at its end. The parameter gradient, when asked for, comes separately.
+  if (dev_io) {
+    const xr_result& r = out[0];
+    k_unpack_device<<<(A + 255) / 256, 256, 0, st>>>(w, r.forces, r.charges, r.total_bond_orders, r.lone_pairs,
+                                                    r.bond_counts);
+  } else {
+    k_pack<<<(A + 255) / 256, 256, 0, st>>>(w, c->outbuf);
   }
-  cudaMemcpyAsync(c->h_cnt, c->cnt, sizeof(int) * 4 * (size_t)(A + 1), cudaMemcpyDeviceToHost, st);
-  d2h += sizeof(int) * 4 * (long long)(A + 1);
+  {
+    const long long tail_n = 20ll * nsys + 4ll * (A + 1) + nsys;
+    const int gb = (int)std::min<long long>((tail_n + 255) / 256, 152 * 4);
+    k_gather_tail<<<gb, 256, 0, st>>>(w, c->outbuf, RL.energy, RL.tail);
+  }
+  launches += 2;
+  {
+    const size_t from = dev_io ? RL.energy : 0;
+    const size_t count = RL.bonds + 4 * (size_t)std::max(nB, 0) - from;
+    cudaMemcpyAsync(c->h_out + from, c->outbuf + from, sizeof(double) * count, cudaMemcpyDeviceToHost, st);
+    d2h += (long long)(sizeof(double) * count);
+  }
   if (c->pgrad_pairs > 0) {
     const size_t all = (size_t)(c->pgrad_pairs + c->pgrad_angles + c->pgrad_atoms) * nsys;
     if (!host_grow(&c->h_pg, &c->ch_pg, all)) return cuda_fail(c, cudaErrorMemoryAllocation, "allocation");
     cudaMemcpyAsync(c->h_pg, c->pgrad, sizeof(double) * all, cudaMemcpyDeviceToHost, st);
     d2h += (long long)(sizeof(double) * all);
   }
-  d2h += 3 * sizeof(int);
-  if (dev_io) {
-    const xr_result& r = out[0];
-    k_unpack_device<<<(A + 255) / 256, 256, 0, st>>>(w, r.forces, r.charges, r.total_bond_orders, r.lone_pairs,
-                                                    r.bond_counts);
-    ++launches;
-    cudaMemcpyAsync(c->h_out, c->energy, sizeof(double) * 16, cudaMemcpyDeviceToHost, st);
-    cudaMemcpyAsync(c->h_out + 16, c->props, sizeof(double) * 4, cudaMemcpyDeviceToHost, st);
-    d2h += 20 * sizeof(double);
-  } else {
-    k_pack<<<(A + 255) / 256, 256, 0, st>>>(w, c->outbuf);
-    ++launches;
-    cudaMemcpyAsync(c->h_out, c->outbuf, sizeof(double) * 8 * A, cudaMemcpyDeviceToHost, st);
-    cudaMemcpyAsync(c->h_out + 8 * (size_t)A, c->energy, sizeof(double) * 16 * nsys, cudaMemcpyDeviceToHost, st);
-    cudaMemcpyAsync(c->h_out + 8 * (size_t)A + 16 * nsys, c->props, sizeof(double) * 4 * nsys, cudaMemcpyDeviceToHost, st);
-    d2h += sizeof(double) * (8 * (long long)A + 20 * (long long)nsys);
-  }
-  cudaMemcpyAsync(c->h_small + 4, c->status, sizeof(int), cudaMemcpyDeviceToHost, st);
-  cudaMemcpyAsync(c->h_small + 7, c->nmids, 2 * sizeof(int), cudaMemcpyDeviceToHost, st);
   stage(c, 8, st);
   if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(c, e, "evaluation");
   if (c->profile) {
@@ -1294,46 +1331,46 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
     }
     ++c->stage_calls;
   }
+  const int* tail = reinterpret_cast<const int*>(c->h_out + RL.tail);
+  const XrBondRecord* recs = reinterpret_cast<const XrBondRecord*>(c->h_out + RL.bonds);
   {
-    const int nx = c->h_small[5];
+    const int nx = std::min(tail[1], std::max(nB, 0));
     d2h += (sizeof(int4) + sizeof(double)) * (long long)nB;
     // exported in arrival order; sorted by bond id (system, then pair order) for the exporters
     std::vector<int> order(nx);
     for (int k = 0; k < nx; ++k) order[k] = k;
-    std::sort(order.begin(), order.end(), [&](int a, int b) { return c->h_bxm[a].x < c->h_bxm[b].x; });
+    std::sort(order.begin(), order.end(), [&](int a, int b) { return recs[a].meta.x < recs[b].meta.x; });
     c->h_bx_meta.resize(nx);
     c->h_bx_bo.resize(nx);
     for (int k = 0; k < nx; ++k) {
-      c->h_bx_meta[k] = c->h_bxm[order[k]];
-      c->h_bx_bo[k] = c->h_bxb[order[k]];
+      c->h_bx_meta[k] = recs[order[k]].meta;
+      c->h_bx_bo[k] = recs[order[k]].bo;
     }
   }
-  c->h_qiters.assign(c->h_qit, c->h_qit + nsys);
+  c->h_qiters.assign(tail + kTailInts, tail + kTailInts + nsys);
   if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(c, e, "kernel launch");
   c->launches = launches;
-  c->qeq_iterations = c->h_small[6];
+  c->qeq_iterations = tail[2];
   c->list_sizes[0] = nE;
   c->list_sizes[1] = nP;
   c->list_sizes[2] = nB;
   c->list_sizes[3] = nD;
-  c->list_sizes[4] = c->h_small[8];  // active bonds (uncorrected order passed the cut)
-  c->list_sizes[5] = c->h_small[7];  // torsion middles (bo > 0.001)
+  c->list_sizes[4] = tail[4];  // active bonds (uncorrected order passed the cut)
+  c->list_sizes[5] = tail[3];  // torsion middles (bo > 0.001)
   if (c->pgrad_pairs > 0)
     c->h_pgrad.assign(c->h_pg, c->h_pg + (c->pgrad_pairs + c->pgrad_angles + c->pgrad_atoms) * nsys);
   c->last_A = A;
   // keep the scans for export
-  c->host_cnt.assign(c->h_cnt, c->h_cnt + 4 * (size_t)(A + 1));
+  c->host_cnt.assign(tail + kTailInts + nsys, tail + kTailInts + nsys + 4 * (size_t)(A + 1));
   c->h2d_bytes = h2d;
   c->d2h_bytes = d2h;
-  if (int code = status_to_code(c, c->h_small[4])) return code;
+  if (int code = status_to_code(c, tail[0])) return code;
   if (dev_io) {
     const xr_result& r = out[0];
-    if (r.energy) {
-      for (int k = 0; k < 14; ++k) r.energy[k] = c->h_out[k];
-      r.energy[14] = c->h_out[14];
-    }
+    if (r.energy)
+      for (int k = 0; k < 15; ++k) r.energy[k] = c->h_out[RL.energy + k];
     if (r.dipole)
-      for (int k = 0; k < 3; ++k) r.dipole[k] = c->h_out[16 + k];
+      for (int k = 0; k < 3; ++k) r.dipole[k] = c->h_out[RL.props + k];
     return XR_OK;
   }
   off = 0;
@@ -1341,8 +1378,8 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
     const xr_result& r = out[s];
     const int n = sys[s].natoms;
     const double* pa = c->h_out + 8 * (size_t)off;
-    const double* pe = c->h_out + 8 * (size_t)A + 16 * s;
-    const double* pp = c->h_out + 8 * (size_t)A + 16 * nsys + 4 * s;
+    const double* pe = c->h_out + RL.energy + 16 * s;
+    const double* pp = c->h_out + RL.props + 4 * s;
     if (r.energy)
       for (int k = 0; k < 15; ++k) r.energy[k] = pe[k];
     if (r.dipole)
@@ -1689,7 +1726,7 @@ void xr_ctx_destroy(xr_ctx* c) {
                   c->qwork, c->outbuf, c->edge, c->edge_pair, c->edge_dbslot, c->hval, c->qch, c->qcj, c->pair_edge, c->pair_i,
                   c->pair_bond, c->p_r, c->p_shield, c->p_dshield, c->p_g, c->p_evdw, c->p_ecoul, c->bond_pair,
                   c->bond_i, c->bond_j, c->b_r, c->b_v, c->b_fwd, c->b_adj, c->b_e, c->dbrow, c->sys, c->energy,
-                  c->props, c->status, c->counts, c->barrier, c->qmap, c->qsmall, c->qiters, c->red, c->qguess, c->qrhs, c->qadj, c->pgrad, c->bx_meta, c->bx_bo, c->bx_count,
+                  c->props, c->status, c->counts, c->barrier, c->qmap, c->qsmall, c->qiters, c->red, c->qguess, c->qrhs, c->qadj, c->pgrad, c->bx_count,
                   c->esum, c->arow, c->nact, c->nzrow, c->nnz, c->chunks, c->sys_chunks, c->chunk_part, c->mids, c->nmids, c->mlist,
                   c->cand_cnt, c->cand_edge, c->sys_list, c->atom_cell, c->atom_slot, c->cell_cnt, c->cell_atoms,
                   c->mid_tiles, c->qsplit};
@@ -1699,8 +1736,7 @@ void xr_ctx_destroy(xr_ctx* c) {
   if (c->h_out) cudaFreeHost(c->h_out);
   if (c->h_guess) cudaFreeHost(c->h_guess);
   for (void* hp : {(void*)c->h_types, (void*)c->h_sysof, (void*)c->h_sysd, (void*)c->h_chunks, (void*)c->h_syschunks,
-                   (void*)c->h_qmap_p, (void*)c->h_qsmall_p, (void*)c->h_cnt, (void*)c->h_bxm, (void*)c->h_bxb,
-                   (void*)c->h_qit, (void*)c->h_pg, (void*)c->h_cand_cnt, (void*)c->h_cand_edge, (void*)c->h_sys_list})
+                   (void*)c->h_qmap_p, (void*)c->h_qsmall_p, (void*)c->h_pg, (void*)c->h_cand_cnt, (void*)c->h_cand_edge, (void*)c->h_sys_list})
     if (hp) cudaFreeHost(hp);
   if (c->h_small) cudaFreeHost(c->h_small);
   for (int k = 0; k <= xr_ctx::kStages; ++k)
@@ -1916,12 +1952,11 @@ int xr_ctx_reserve(xr_ctx* c, int atoms, int systems, long long edges, long long
   cudaSetDevice(c->device);
   const long long chunks = (long long)systems + atoms / XR_CHUNK_ATOMS + 1;
   if (!ensure_atoms(c, atoms, systems) || !host_grow(&c->h_x, &c->ch_x, (size_t)atoms) ||
-      !host_grow(&c->h_out, &c->ch_out, 8 * (size_t)atoms + 32 * (size_t)systems + 8) ||
       !host_grow(&c->h_guess, &c->ch_guess, (size_t)atoms) || !ensure_lists(c, edges, edges / 2, bonds) ||
       !grow(c, &c->chunks, &c->cchunks, (size_t)chunks) ||
       !grow(c, &c->chunk_part, &c->cchunk_part, (size_t)chunks * XR_PART_N) ||
-      !grow(c, &c->bx_meta, &c->cbx_meta, (size_t)std::max<long long>(bonds, 1)) ||
-      !grow(c, &c->bx_bo, &c->cbx_bo, (size_t)std::max<long long>(bonds, 1)) ||
+      !grow(c, &c->outbuf, &c->coutbuf, result_layout(atoms, systems, bonds).end) ||
+      !host_grow(&c->h_out, &c->ch_out, result_layout(atoms, systems, bonds).end) ||
       // candidate rows and the cell list, for calls that search by cells
       !grow(c, &c->cand_cnt, &c->ccand_cnt, (size_t)atoms + 1) ||
       !grow(c, &c->cand_edge, &c->ccand_edge, (size_t)std::max<long long>(edges, 1)) ||
@@ -1945,11 +1980,11 @@ long long xr_footprint_bytes(int atoms, int systems, long long edges, long long 
   if (atoms < 1 || systems < 1 || edges < 0 || bonds < 0) return -1;
   // the buffers of ensure_atoms, ensure_lists and xr_ctx_reserve, per element
   const long long per_atom = sizeof(double4_32a) + 2 * sizeof(int) + sizeof(int4) + 2 * sizeof(float4) + 4 * sizeof(int) +
-                             (AF_N + AJ_N + 8 + 4 + 3 + XR_QW_N + 8 + XR_ESUM_N) * sizeof(double) + 2 * sizeof(int);
-  const long long per_system = sizeof(int2) + 2 * sizeof(int) + sizeof(XrSystem) + 20 * sizeof(double);
+                             (AF_N + AJ_N + 8 + 4 + 3 + XR_QW_N + 8 + XR_ESUM_N) * sizeof(double) + 6 * sizeof(int);
+  const long long per_system = sizeof(int2) + 3 * sizeof(int) + sizeof(XrSystem) + 20 * sizeof(double);
   const long long per_edge = sizeof(int2) + 2 * sizeof(int) + sizeof(double) + sizeof(float) + sizeof(unsigned short);
   const long long per_pair = 3 * sizeof(int) + 6 * sizeof(double);
-  const long long per_bond = kBondBytes + sizeof(int4) + sizeof(double);
+  const long long per_bond = kBondBytes + 32;  // + the exported-bond record of the result block
   const long long chunks = (long long)systems + atoms / XR_CHUNK_ATOMS + 1;
   const long long per_cells = 4 * sizeof(int) + 2 * sizeof(int);  // cand_cnt, atom_cell, atom_slot, cell_atoms, cell_cnt
   const long long base = (long long)atoms * (per_atom + per_cells) + (long long)systems * (per_system + 64 * sizeof(int)) +

@@ -19,8 +19,37 @@ constexpr int kHitBit = 1 << 30;
 __global__ void k_prep(XrWork w) {
   int a = blockIdx.x * blockDim.x + threadIdx.x;
   if (a >= w.A) return;
-  const XrSystem& S = w.sys[w.sys_of[a]];
+  if (w.prep_zero) {
+    // an evaluation's counters and scans start at zero (instead of a memset each; the status word
+    // is cleared by the host before this kernel, since any block may flag it); cnt holds 4 (A + 1)
+    // ints
+    for (int k = 0; k < 4; ++k) w.cnt[4 * a + k] = 0;
+    if (a == 0) {
+      for (int k = 0; k < 4; ++k) w.cnt[4 * w.A + k] = 0;
+      for (int k = 0; k < 8; ++k) w.counts[k] = 0;
+      w.nmids[0] = 0;
+      w.nmids[1] = 0;
+      *w.bx_count = 0;
+    }
+    if (a < w.S) w.qiters[a] = 0;
+  }
   const double4_32a p = w.x[a];
+  int sys;
+  if (w.types_in_x) {
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(p.w);
+    int t = (int)(unsigned)(bits & 0xffffffffull);
+    sys = (int)(unsigned)(bits >> 32);
+    if (sys < 0 || sys >= w.S || t < 0) {  // not a packed word: flagged (the call fails), in-range indices kept
+      atomicOr(w.status, XR_S_BAD_PACK);
+      sys = 0;
+      t = 0;
+    }
+    const_cast<int*>(w.type)[a] = t;
+    const_cast<int*>(w.sys_of)[a] = sys;
+  } else {
+    sys = w.sys_of[a];
+  }
+  const XrSystem& S = w.sys[sys];
   const double xs[3] = {p.x, p.y, p.z};
   double f[3];
   int wr[3];
