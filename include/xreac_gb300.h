@@ -180,13 +180,14 @@ int xr_neighbors_check(int natoms, const int* pbc, const xr_neighbors* nb, char*
  * current value, drops the kept list. */
 int xr_ctx_set_skin(xr_ctx* ctx, double skin);
 
-/* CUDA graphs (no reference counterpart): with enable != 0 (the default) a call that repeats the
- * previous call's launch sequence (the same systems' sizes and periodicity, force field, flags and
- * buffers, as in relaxation or MD steps) records the kernels after the neighbour count as a CUDA
- * graph, and later calls with the same sequence replay it as one launch. The kernels read the list
- * sizes from device memory, so a replay is the same computation. Not used with stage timing
- * (xr_ctx_set_profiling) or with grid-wide QEq teams. xr_last_graph: 0 launched directly, 1
- * recorded, 2 replayed (-1 for a null context). */
+/* CUDA graphs (no reference counterpart): with enable != 0 (the default) the second call with a
+ * given launch sequence (the same systems' sizes and periodicity, force field, flags and buffers, as
+ * in relaxation or MD steps or a request size seen before) records the kernels after the neighbour
+ * count as a CUDA graph, and later calls with that sequence replay it as one launch; a context keeps
+ * its 128 most recently used graphs. The kernels read the list sizes from device memory, so a replay
+ * is the same computation. Not used with stage timing (xr_ctx_set_profiling) or with grid-wide QEq
+ * teams. xr_last_graph: 0 launched directly, 1 recorded, 2 replayed (-1 for a null context).
+ * xr_ctx_set_graphs(ctx, 0) releases the context's graphs. */
 int xr_ctx_set_graphs(xr_ctx* ctx, int enable);
 int xr_last_graph(const xr_ctx* ctx);
 

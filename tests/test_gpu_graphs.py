@@ -1,5 +1,5 @@
-"""CUDA-graph replay of the launch sequence: a call that repeats the previous call's systems and
-settings records its kernels after the neighbour count as a graph, later ones replay it. Every
+"""CUDA-graph replay of the launch sequence: the kernels after the neighbour count are recorded as a
+graph the second time a launch key occurs, and later calls with that key replay it. Every
 replayed result must equal that of direct launches on the same inputs (xreac's Calculator.evaluate,
 src/xreac/calculator.py:76-165, has no such state): energies and charges bit for bit, forces to the
 last bits (atomics), including steps whose lists change size between replays."""

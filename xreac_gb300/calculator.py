@@ -385,8 +385,8 @@ class Calculator:
 
     def set_graphs(self, enabled=True):
         """CUDA graphs for repeated launch sequences (``xr_ctx_set_graphs``, an extension; on by
-        default): a call that repeats the previous call's systems and settings records its kernels
-        as a graph, and later such calls replay it."""
+        default): the second call with given system sizes and settings records its kernels as a
+        graph, and later such calls replay it (the 128 most recently used graphs are kept)."""
         self._lib.xr_ctx_set_graphs(self._ctx.handle, 1 if enabled else 0)
 
     @property

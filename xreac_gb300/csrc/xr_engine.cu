@@ -9,6 +9,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "xr_common.cuh"
@@ -83,14 +84,21 @@ struct xr_ctx {
   size_t ch_sys_list = 0;
   // Device bytes the context holds (its buffers, as grown; xr_ctx_memory).
   long long dev_bytes = 0;
-  // CUDA graph of the launch sequence after the list count (xr_ctx_set_graphs): recorded when a
-  // call repeats the previous call's launch key, replayed while the key stays the same.
+  // CUDA graphs of the launch sequence after the list count (xr_ctx_set_graphs): a sequence is
+  // recorded the second time its launch key occurs and replayed whenever the key occurs again; the
+  // kGraphCache most recently used graphs are kept.
   bool graphs = true;
-  cudaGraphExec_t gexec = nullptr;
-  std::vector<unsigned char> gkey;     // key of the recorded sequence
-  std::vector<unsigned char> last_key; // key of the previous call
-  long long glaunches = 0;             // kernels in the recorded sequence
-  int last_graph = 0;                  // of the last call: 0 launched directly, 1 recorded, 2 replayed
+  struct GraphEntry {
+    cudaGraphExec_t exec;
+    long long launches;       // kernels in the recorded sequence
+    unsigned long long used;  // clock of the last use
+  };
+  std::unordered_map<std::string, GraphEntry> gcache;
+  std::unordered_map<std::string, int> gseen;  // keys not recorded yet: occurrences (-1: not recordable)
+  unsigned long long gclock = 0;
+  static constexpr size_t kGraphCache = 128;
+  static constexpr size_t kGraphSeen = 4096;
+  int last_graph = 0;  // of the last call: 0 launched directly, 1 recorded, 2 replayed
   // Cell list (xr_ctx_set_cell_list): 0 chooses per call, 1 always, -1 never.
   int cell_mode = 0;
   int* atom_cell = nullptr;
@@ -1242,54 +1250,63 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
     }
     return (int)cudaGetLastError();
   };
-  // A sequence is recorded as a CUDA graph when a call repeats the previous call's launch key (a
-  // relaxation or MD step, a repeated request), and replayed while the key stays the same: one
-  // launch instead of about 30 kernel launches and their memsets. Not with stage timing, nor with
-  // grid-wide QEq teams (their co-residency needs a cooperative launch).
+  // A sequence is recorded as a CUDA graph the second time its launch key occurs (a relaxation or MD
+  // step, a repeated request, a request size seen before) and replayed on later occurrences: one
+  // launch instead of about 30 kernel launches and their memsets. The key holds every pointer and
+  // size the recorded launches use, so a cached graph matches only calls whose buffers it addresses.
+  // Not with stage timing, nor with grid-wide QEq teams (their co-residency needs a cooperative launch).
   c->last_graph = 0;
   bool done = false;
   if (c->graphs && !c->profile && qteam == 0) {
     const int ints[] = {(int)mode, qcluster ? 1 : 0, qcsize, qblocks, qteam, qsmall, qbig, nlist, nE > 0, nP > 0, nB > 0,
                         (int)flags};
-    const void* ptrs[] = {c->h_qmap_p, c->h_qsmall_p, bx_rec, c->bx_count, c->outbuf};
-    std::vector<unsigned char> key = launch_key(w, ff->d, ints, (int)(sizeof(ints) / sizeof(int)), ptrs, 5);
-    if (c->gexec && key == c->gkey) {
-      if (cudaGraphLaunch(c->gexec, st) == cudaSuccess) {
-        launches += c->glaunches;
+    const void* ptrs[] = {c->h_qmap_p, c->h_qsmall_p, c->qmap, c->qsmall, bx_rec, c->bx_count, c->outbuf};
+    const int nptrs = (int)(sizeof(ptrs) / sizeof(ptrs[0]));
+    const std::vector<unsigned char> kv = launch_key(w, ff->d, ints, (int)(sizeof(ints) / sizeof(int)), ptrs, nptrs);
+    const std::string key(reinterpret_cast<const char*>(kv.data()), kv.size());
+    auto hit = c->gcache.find(key);
+    if (hit != c->gcache.end()) {
+      if (cudaGraphLaunch(hit->second.exec, st) == cudaSuccess) {
+        launches += hit->second.launches;
+        hit->second.used = ++c->gclock;
         c->last_graph = 2;
         done = true;
       } else {
         cudaGetLastError();
       }
-    } else if (key == c->last_key) {
-      const long long before = launches;
-      cudaGraph_t g = nullptr;
-      if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
-        const int rc = sequence();
-        const cudaError_t ce = cudaStreamEndCapture(st, &g);
+    } else {
+      int& seen = c->gseen[key];
+      if (seen >= 0 && ++seen >= 2) {
+        const long long before = launches;
+        cudaGraph_t g = nullptr;
         cudaGraphExec_t ex = nullptr;
-        if (rc == 0 && ce == cudaSuccess && g && cudaGraphInstantiate(&ex, g, 0) == cudaSuccess) {
-          if (c->gexec) cudaGraphExecDestroy(c->gexec);
-          c->gexec = ex;
-          c->gkey = key;
-          c->glaunches = launches - before;
-          if (cudaGraphLaunch(ex, st) == cudaSuccess) {
-            c->last_graph = 1;
-            done = true;
-          }
+        if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+          const int rc = sequence();
+          const cudaError_t ce = cudaStreamEndCapture(st, &g);
+          if (rc != 0 || ce != cudaSuccess || !g || cudaGraphInstantiate(&ex, g, 0) != cudaSuccess) ex = nullptr;
+          if (g) cudaGraphDestroy(g);
         }
-        if (g) cudaGraphDestroy(g);
+        if (ex && cudaGraphLaunch(ex, st) == cudaSuccess) {
+          if (c->gcache.size() >= xr_ctx::kGraphCache) {  // evict the least recently used
+            auto lru = c->gcache.begin();
+            for (auto it = c->gcache.begin(); it != c->gcache.end(); ++it)
+              if (it->second.used < lru->second.used) lru = it;
+            cudaGraphExecDestroy(lru->second.exec);
+            c->gcache.erase(lru);
+          }
+          c->gcache.emplace(key, xr_ctx::GraphEntry{ex, launches - before, ++c->gclock});
+          c->gseen.erase(key);
+          c->last_graph = 1;
+          done = true;
+        } else {  // not recordable here: launch directly, and do not try this key again
+          if (ex) cudaGraphExecDestroy(ex);
+          cudaGetLastError();
+          launches = before;
+          seen = -1;
+        }
       }
-      if (!done) {  // not recordable here: launch directly, and do not try this key again
-        cudaGetLastError();
-        launches = before;
-        if (c->gexec) cudaGraphExecDestroy(c->gexec);
-        c->gexec = nullptr;
-        c->gkey.clear();
-        key.clear();
-      }
+      if (c->gseen.size() > xr_ctx::kGraphSeen) c->gseen.clear();
     }
-    c->last_key = std::move(key);
   }
   if (!done)
     if (int le = sequence()) return cuda_fail(c, (cudaError_t)le, "launch");
@@ -1721,7 +1738,7 @@ void xr_ctx_destroy(xr_ctx* c) {
   if (!c) return;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
-  if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  for (auto& e : c->gcache) cudaGraphExecDestroy(e.second.exec);
   void* bufs[] = {c->x, c->type, c->sys_of, c->wrap, c->xw, c->fw, c->cnt, c->a_fwd, c->a_adj, c->a_e, c->q, c->f,
                   c->qwork, c->outbuf, c->edge, c->edge_pair, c->edge_dbslot, c->hval, c->qch, c->qcj, c->pair_edge, c->pair_i,
                   c->pair_bond, c->p_r, c->p_shield, c->p_dshield, c->p_g, c->p_evdw, c->p_ecoul, c->bond_pair,
@@ -1784,13 +1801,12 @@ int xr_ctx_set_skin(xr_ctx* c, double skin) {
 int xr_ctx_set_graphs(xr_ctx* c, int enable) {
   if (!c) return XR_EINPUT;
   c->graphs = enable != 0;
-  if (!c->graphs && c->gexec) {
+  if (!c->graphs && !c->gcache.empty()) {
     cudaSetDevice(c->device);
-    cudaGraphExecDestroy(c->gexec);
-    c->gexec = nullptr;
-    c->gkey.clear();
+    for (auto& e : c->gcache) cudaGraphExecDestroy(e.second.exec);
+    c->gcache.clear();
   }
-  c->last_key.clear();
+  c->gseen.clear();
   return XR_OK;
 }
 
