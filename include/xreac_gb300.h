@@ -155,6 +155,12 @@ int xr_ctx_set_qeq(xr_ctx* ctx, double tolerance, int max_iterations);
  * (a single block, no team waits) are not affected. */
 int xr_ctx_set_wait_test(xr_ctx* ctx, long long polls, int fail_at);
 
+/* Test of the device math (no reference counterpart): out[i] = f(in[i]) for n device-resident
+ * doubles on the current device's default stream, f = the double-float exp (fn 0) or log (fn 2) that
+ * the pair and bond-order kernels use, or CUDA's FP64 exp (fn 1) or log (fn 3) to compare with.
+ * Returns XR_OK, XR_EINPUT for a bad fn or n, or XR_ECUDA. */
+int xr_test_math(int fn, const double* in, double* out, int n);
+
 /* Evaluate one system (energy, fixed-charge forces, QEq charges, per-atom bond properties). */
 int xr_eval(xr_ctx* ctx, const xr_ff* ff, const xr_system* sys, unsigned flags, xr_result* out);
 

@@ -46,6 +46,7 @@ EXPORTED = (
     "xr_ctx_set_qeq",
     "xr_ctx_reserve",
     "xr_ctx_set_wait_test",
+    "xr_test_math",
     "xr_eval",
     "xr_eval_batch",
     "xr_eval_batch_sets",
@@ -158,6 +159,8 @@ def load():
     lib.xr_ctx_reserve.restype = c_int
     lib.xr_ctx_set_wait_test.argtypes = [c_void_p, c_longlong, c_int]
     lib.xr_ctx_set_wait_test.restype = c_int
+    lib.xr_test_math.argtypes = [c_int, c_void_p, c_void_p, c_int]
+    lib.xr_test_math.restype = c_int
     lib.xr_eval.argtypes = [c_void_p, c_void_p, POINTER(System), c_uint, POINTER(Result)]
     lib.xr_eval.restype = c_int
     lib.xr_eval_batch.argtypes = [c_void_p, c_void_p, c_int, POINTER(System), c_uint, POINTER(Result)]

@@ -10,9 +10,12 @@
 //   needs no atomics and is deterministic.
 // - A single large system runs the solver as one cooperative grid with a barrier whose every wait
 //   is bounded; batches of systems give each system one thread block.
+#include <algorithm>
 #include <type_traits>
 
 #include "xr_common.cuh"
+#include "xr_dfloat.cuh"
+#include "xreac_gb300.h"
 
 namespace {
 
@@ -76,23 +79,25 @@ __device__ inline void pair_one(const XrWork& w, const XrFF& ff0, int p) {
   const double shield = taper * z;
   const double dshield = dtaper * z - taper * r * r * (z2 * z2);
   double f13 = r, df13 = 1.0;
+  // exponentials and logarithms in double-float arithmetic on the FP32 pipe (xr_dfloat.cuh): they
+  // were most of this kernel's FP64 issue
   if (ff.vdw_type == 1 || ff.vdw_type == 3) {
     const double pw = ff.g[28];
-    const double rp = exp(pw * log(r));
+    const double rp = xr_exp(pw * xr_log(r));
     const double sum = rp + __ldg(ff.pair_gw + pt);
-    f13 = exp(log(sum) * ff.inv_g28);
+    f13 = xr_exp(xr_log(sum) * ff.inv_g28);
     df13 = f13 * rp / (sum * r);
   }
   // reciprocals of the pair's radii from the table: multiplies instead of FP64 divisions
   const double D = pair_prm(ff, pt, P_D), alpha = pair_prm(ff, pt, P_ALPHA);
   const double2 inv = __ldg(reinterpret_cast<const double2*>(ff.pair_inv) + pt);  // 1/r_vdW, 1/rcore
-  const double ev = exp(0.5 * alpha * (1 - f13 * inv.x));
+  const double ev = xr_exp(0.5 * alpha * (1 - f13 * inv.x));
   const double dev = ev * (-0.5 * alpha * inv.x) * df13;
   double E = taper * D * (ev * ev - 2 * ev);
   double G = dtaper * D * (ev * ev - 2 * ev) + taper * D * (2 * ev - 2) * dev;
   if (ff.vdw_type == 2 || ff.vdw_type == 3) {
     const double ecore = pair_prm(ff, pt, P_ECORE), acore = pair_prm(ff, pt, P_ACORE);
-    const double ec = ecore * exp(acore * (1 - r * inv.y));
+    const double ec = ecore * xr_exp(acore * (1 - r * inv.y));
     E += taper * ec;
     G += dtaper * ec + taper * ec * (-acore * inv.y);
   }
@@ -2490,4 +2495,21 @@ void xr_launch_reduce(const XrWork& w, const XrFF& ff, cudaStream_t st) {
   k_energy_gather<<<(w.A + 7) / 8, 256, 0, st>>>(w);
   k_reduce_chunk<<<w.nchunks, 256, 0, st>>>(w, ff);
   k_reduce_final<<<w.S, 32, 0, st>>>(w);
+}
+
+namespace {
+__global__ void k_math_test(int fn, const double* in, double* out, int n) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double x = in[i];
+    out[i] = fn == 0 ? xr_exp(x) : fn == 1 ? exp(x) : fn == 2 ? xr_log(x) : log(x);
+  }
+}
+}  // namespace
+
+extern "C" int xr_test_math(int fn, const double* in, double* out, int n) {
+  if (fn < 0 || fn > 3 || n < 0 || (n > 0 && (!in || !out))) return XR_EINPUT;
+  if (n == 0) return XR_OK;
+  k_math_test<<<std::min((n + 255) / 256, 4096), 256>>>(fn, in, out, n);
+  if (cudaGetLastError() != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) return XR_ECUDA;
+  return XR_OK;
 }
