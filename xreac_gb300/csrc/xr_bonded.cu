@@ -20,6 +20,7 @@
 #include <algorithm>
 
 #include "xr_common.cuh"
+#include "xr_dfloat.cuh"  // xr_exp, xr_log: exp and log in double-float arithmetic on the FP32 pipe
 
 namespace {
 
@@ -95,23 +96,23 @@ __device__ inline void bo1_tile(const XrWork& w, const XrFF& ff0, int b, int nb)
     // Beyond the pair type's bound the uncorrected order is below a quarter of the cut: no term is
     // evaluated, the bond is inactive with zero orders (as the full expression would give).
     if (r <= __ldg(ff.pair_rmax + pt)) {
-      const double lr = log(r);
+      const double lr = xr_log(r);
       if (atom_prm(ff, ti, A_R_S) > 0 && atom_prm(ff, tj, A_R_S) > 0) {
         const double p1 = pair_prm(ff, pt, P_BO1), p2 = pair_prm(ff, pt, P_BO2);
-        const double t = exp(p2 * (lr - __ldg(ff.pair_logr + 3 * pt + 0)));
-        sig = (1.0 + cut) * exp(p1 * t);
+        const double t = xr_exp(p2 * (lr - __ldg(ff.pair_logr + 3 * pt + 0)));
+        sig = (1.0 + cut) * xr_exp(p1 * t);
         dsig = sig * p1 * p2 * t / r;
       }
       if (atom_prm(ff, ti, A_R_PI) > 0 && atom_prm(ff, tj, A_R_PI) > 0) {
         const double p3 = pair_prm(ff, pt, P_BO3), p4 = pair_prm(ff, pt, P_BO4);
-        const double t = exp(p4 * (lr - __ldg(ff.pair_logr + 3 * pt + 1)));
-        pi = exp(p3 * t);
+        const double t = xr_exp(p4 * (lr - __ldg(ff.pair_logr + 3 * pt + 1)));
+        pi = xr_exp(p3 * t);
         dpi = pi * p3 * p4 * t / r;
       }
       if (atom_prm(ff, ti, A_R_PI_PI) > 0 && atom_prm(ff, tj, A_R_PI_PI) > 0) {
         const double p5 = pair_prm(ff, pt, P_BO5), p6 = pair_prm(ff, pt, P_BO6);
-        const double t = exp(p6 * (lr - __ldg(ff.pair_logr + 3 * pt + 2)));
-        pp = exp(p5 * t);
+        const double t = xr_exp(p6 * (lr - __ldg(ff.pair_logr + 3 * pt + 2)));
+        pp = xr_exp(p5 * t);
         dpp = pp * p5 * p6 * t / r;
       }
     }
@@ -197,11 +198,11 @@ __device__ inline void k_bo2_one(const XrWork& w, const XrFF& ff0, int b) {
   const double dbi = dpi_ - atom_prm(ff, ti, A_VALENCY_VAL), dbj = dpj - atom_prm(ff, tj, A_VALENCY_VAL);
   double f1 = 1.0, df1i = 0.0, df1j = 0.0;
   if (ovc >= 0.001) {
-    const double e2i = exp(-g[0] * di), e2j = exp(-g[0] * dj);
+    const double e2i = xr_exp(-g[0] * di), e2j = xr_exp(-g[0] * dj);
     const double f2 = e2i + e2j;
-    const double e3i = exp(-g[1] * di), e3j = exp(-g[1] * dj);
+    const double e3i = xr_exp(-g[1] * di), e3j = xr_exp(-g[1] * dj);
     const double s3 = 0.5 * (e3i + e3j);
-    const double f3 = -log(s3) / g[1];
+    const double f3 = -xr_log(s3) / g[1];
     const double Ai = vi + f2, Bi = Ai + f3, Aj = vj + f2, Bj = Aj + f3;
     f1 = 0.5 * (Ai / Bi + Aj / Bj);
     const double df1_df2 = 0.5 * (f3 / (Bi * Bi) + f3 / (Bj * Bj));
@@ -209,8 +210,8 @@ __device__ inline void k_bo2_one(const XrWork& w, const XrFF& ff0, int b) {
     df1i = df1_df2 * (-g[0] * e2i) + df1_df3 * (0.5 * e3i / s3);
     df1j = df1_df2 * (-g[0] * e2j) + df1_df3 * (0.5 * e3j / s3);
   }
-  const double f4 = 1.0 / (1.0 + exp(-(boc4 * bo0 * bo0 - dbi) * boc3 + boc5));
-  const double f5 = 1.0 / (1.0 + exp(-(boc4 * bo0 * bo0 - dbj) * boc3 + boc5));
+  const double f4 = 1.0 / (1.0 + xr_exp(-(boc4 * bo0 * bo0 - dbi) * boc3 + boc5));
+  const double f5 = 1.0 / (1.0 + xr_exp(-(boc4 * bo0 * bo0 - dbj) * boc3 + boc5));
   const double f45 = v13 >= 0.001 ? f4 * f5 : 1.0;
   const double corr = f1 * f45;
   const double bo = bo0 * corr, pi = pi0 * corr * f1, pp = pp0 * corr * f1;
@@ -261,11 +262,11 @@ __global__ void k_atom1(XrWork w, XrFF ff0) {
   const double de = total - vale;
   const double half = trunc(de / 2);
   const double vlpex = de - 2 * half;
-  const double e15 = exp(-g[15] * (2 + vlpex) * (2 + vlpex));
+  const double e15 = xr_exp(-g[15] * (2 + vlpex) * (2 + vlpex));
   const double nlp = e15 - half;
   const double dlp = 0.5 * (vale - val) - nlp;
   const double dlpt = atom_prm(ff, ta, A_MASS) > 21 ? 0.0 : dlp;
-  const double elp = exp(-75 * dlp);
+  const double elp = xr_exp(-75 * dlp);
   const double s = 1.0 / (1.0 + elp);
   const double plp2 = atom_prm(ff, ta, A_P_LP2);
   AEV(0, a) = plp2 * dlp * s;
@@ -276,7 +277,7 @@ __global__ void k_atom1(XrWork w, XrFF ff0) {
   AFV(AF_DLP, a) = dlp;
   AFV(AF_DLPT, a) = dlpt;
   AFV(AF_SUMPI, a) = sumpi;
-  AFV(AF_PROD, a) = exp(-prodsum);
+  AFV(AF_PROD, a) = xr_exp(-prodsum);
   AFV(AF_OV1, a) = ov1;
   AFV(AF_COUNT30, a) = n30;
   AFV(AF_E15, a) = e15;
@@ -285,14 +286,14 @@ __global__ void k_atom1(XrWork w, XrFF ff0) {
 
 __device__ inline double sbo2_of(double sbo, double p) {
   if (sbo <= 0) return 0.0;
-  if (sbo <= 1) return exp(p * log(sbo));
-  if (sbo < 2) return 2.0 - exp(p * log(2.0 - sbo));
+  if (sbo <= 1) return xr_exp(p * xr_log(sbo));
+  if (sbo < 2) return 2.0 - xr_exp(p * xr_log(2.0 - sbo));
   return 2.0;
 }
 __device__ inline double dsbo2_of(double sbo, double p) {
   if (sbo <= 0) return 0.0;
-  if (sbo <= 1) return p * exp((p - 1) * log(sbo));
-  if (sbo < 2) return p * exp((p - 1) * log(2.0 - sbo));
+  if (sbo <= 1) return p * xr_exp((p - 1) * xr_log(sbo));
+  if (sbo < 2) return p * xr_exp((p - 1) * xr_log(2.0 - sbo));
   return 0.0;
 }
 
@@ -314,15 +315,15 @@ __global__ void k_atom2(XrWork w, XrFF ff0) {
   const double total = AFV(AF_TOTAL, a), val = atom_prm(ff, ta, A_VALENCY);
   const double d = total - val, db = total - atom_prm(ff, ta, A_VALENCY_BOC);
   const double dlpt = AFV(AF_DLPT, a), ov1 = AFV(AF_OV1, a);
-  const double exov = exp(g[31] * ov2);
+  const double exov = xr_exp(g[31] * ov2);
   const double denc = 1.0 + g[32] * exov;
   const double dc = d - dfvl * dlpt / denc;
   const double po2 = atom_prm(ff, ta, A_P_OVUN2), p5 = atom_prm(ff, ta, A_P_OVUN5);
   const double D1 = dc + val + 1e-8;
-  const double eo = exp(po2 * dc);
+  const double eo = xr_exp(po2 * dc);
   const double D2 = 1.0 + eo;
   const double over = ov1 * dc / D1 / D2;
-  const double eu = exp(g[6] * dc), em = exp(-po2 * dc), e9 = exp(g[9] * ov2);
+  const double eu = xr_exp(g[6] * dc), em = xr_exp(-po2 * dc), e9 = xr_exp(g[9] * ov2);
   const double D3 = 1.0 + em, D4 = 1.0 + g[8] * e9;
   const double under = -p5 * (1.0 - eu) / D3 / D4;
   AEV(1, a) = over + under;
@@ -353,8 +354,8 @@ __device__ inline void k_bond_energy_one(const XrWork& w, const XrFF& ff0, int b
   const double bo = BFV(BF_BO, b), pi = BFV(BF_PI, b), pp = BFV(BF_PP, b), sig = BFV(BF_SIG, b);
   const double Des = pair_prm(ff, pt, P_DE_S), Dep = pair_prm(ff, pt, P_DE_P), Depp = pair_prm(ff, pt, P_DE_PP);
   const double be1 = pair_prm(ff, pt, P_BE1), be2 = pair_prm(ff, pt, P_BE2);
-  const double powv = sig > 0 ? exp(be2 * log(sig)) : 0.0;
-  const double ex = exp(be1 * (1.0 - powv));
+  const double powv = sig > 0 ? xr_exp(be2 * xr_log(sig)) : 0.0;
+  const double ex = xr_exp(be1 * (1.0 - powv));
   double e_bond = -(Des * sig * ex + Dep * pi + Depp * pp);
   BJV(BJ_SIG, b) = -Des * ex * (1.0 - be1 * be2 * powv);
   if (w.pgrad) {  // dE/d(De_s, De_p, De_pp, p_be1, p_be2)
@@ -364,7 +365,7 @@ __device__ inline void k_bond_energy_one(const XrWork& w, const XrFF& ff0, int b
     if (pp != 0.0) atomicAdd(gp + P_DE_PP, -pp);
     if (sig > 0) {
       atomicAdd(gp + P_BE1, -Des * sig * ex * (1.0 - powv));
-      atomicAdd(gp + P_BE2, Des * sig * ex * be1 * powv * log(sig));
+      atomicAdd(gp + P_BE2, Des * sig * ex * be1 * powv * xr_log(sig));
     }
   }
   BJV(BJ_PI, b) += -Dep;
@@ -390,10 +391,10 @@ __device__ inline void k_bond_energy_one(const XrWork& w, const XrFF& ff0, int b
   if (allowed && bo >= 1.0) {
     const double ti_ = AFV(AF_TOTAL, i), tj_ = AFV(AF_TOTAL, j);
     const double di = ti_ - atom_prm(ff, ti, A_VALENCY), dj = tj_ - atom_prm(ff, tj, A_VALENCY);
-    const double e1 = exp(-g[7] * (bo - 2.5) * (bo - 2.5));
-    const double e4 = exp(g[4] * (di + dj));
+    const double e1 = xr_exp(-g[7] * (bo - 2.5) * (bo - 2.5));
+    const double e4 = xr_exp(g[4] * (di + dj));
     const double D = 1.0 + 25.0 * e4;
-    const double ei = exp(-g[3] * (ti_ - bo)), ej = exp(-g[3] * (tj_ - bo));
+    const double ei = xr_exp(-g[3] * (ti_ - bo)), ej = xr_exp(-g[3] * (tj_ - bo));
     const double stab = g[10] * e1 / D * (ei + ej);
     e_bond += stab;
     dbo += g[10] / D * (-2.0 * g[7] * (bo - 2.5) * e1 * (ei + ej) + e1 * g[3] * (ei + ej));
@@ -495,12 +496,12 @@ __global__ void __launch_bounds__(32 * kBondedWarps) k_angles(XrWork w, XrFF ff0
     const double total_j = AFV(AF_TOTAL, j);
     const double d_j = total_j - atom_prm(ff, tj, A_VALENCY);
     const double sbo2 = AFV(AF_SBO2, j);
-    const double ex3 = exp(-g[20] * d_j), ex4 = exp(g[21] * d_j);
+    const double ex3 = xr_exp(-g[20] * d_j), ex4 = xr_exp(g[21] * d_j);
     const double den34 = 1 + ex3 + ex4;
-    const double e2 = exp(g[2] * (total_j - atom_prm(ff, tj, A_VALENCY_VAL)));
+    const double e2 = xr_exp(g[2] * (total_j - atom_prm(ff, tj, A_VALENCY_VAL)));
     const double K1 = 1.0 / (1.0 + e2);
     double* cj = ucon[wl][lane];
-    cj[0] = exp(-g[17] * (2 - sbo2));
+    cj[0] = xr_exp(-g[17] * (2 - sbo2));
     cj[1] = (2 + ex3) / den34;
     cj[2] = (-g[20] * ex3 * den34 - (2 + ex3) * (-g[20] * ex3 + g[21] * ex4)) / (den34 * den34);
     cj[3] = K1;
@@ -553,7 +554,7 @@ __global__ void __launch_bounds__(32 * kBondedWarps) k_angles(XrWork w, XrFF ff0
         dth_dcos = (cosv > lo && cosv < hi) ? -1.0 / sqrt(1.0 - cc * cc) : 0.0;
       }
       const double bij = bo_l - THB_CUT, bjk = bo_r - THB_CUT;
-      const double lbij = log(bij), lbjk = log(bjk);
+      const double lbij = xr_log(bij), lbjk = xr_log(bjk);
       const double ibij = 1.0 / bij, ibjk = 1.0 / bjk;
       // terms that do not depend on the parameter record
       const double ti_b = total_i - bij, tk_b = total_k - bjk;
@@ -565,17 +566,17 @@ __global__ void __launch_bounds__(32 * kBondedWarps) k_angles(XrWork w, XrFF ff0
         if (!(fabs(v1) > 0.001)) continue;
         const double theta0 = (180 - th00 * (1 - e17)) * k180;
         const double dth0_dsbo2 = th00 * k180 * g[17] * e17;
-        const double pij = exp(v4 * lbij), pjk = exp(v4 * lbjk);
-        const double A1 = exp(-pv3 * pij), A2 = exp(-pv3 * pjk);
+        const double pij = xr_exp(v4 * lbij), pjk = xr_exp(v4 * lbjk);
+        const double A1 = xr_exp(-pv3 * pij), A2 = xr_exp(-pv3 * pjk);
         const double f7 = (1 - A1) * (1 - A2);
         const double df7_dbij = pv3 * v4 * pij * ibij * A1 * (1 - A2);
         const double df7_dbjk = (1 - A1) * pv3 * v4 * pjk * ibjk * A2;
-        const double ex6 = exp(g[14] * db_j), ex7 = exp(-v7 * db_j);
+        const double ex6 = xr_exp(g[14] * db_j), ex7 = xr_exp(-v7 * db_j);
         const double den8 = 1 + ex6 + ex7;
         const double f8 = pv5 - (pv5 - 1) * (2 + ex6) / den8;
         const double df8_ddb = -(pv5 - 1) * (g[14] * ex6 * den8 - (2 + ex6) * (g[14] * ex6 - v7 * ex7)) / (den8 * den8);
         const double dt = theta0 - theta;
-        const double exang = exp(-v2 * dt * dt);
+        const double exang = xr_exp(-v2 * dt * dt);
         const double branch = v1 >= 0 ? 1 - exang : -exang;
         v[0] += f7 * f8 * v1 * branch;
         const double dE_ddt = f7 * f8 * v1 * 2 * v2 * dt * exang;
@@ -584,7 +585,7 @@ __global__ void __launch_bounds__(32 * kBondedWarps) k_angles(XrWork w, XrFF ff0
         dbij += f8 * v1 * branch * df7_dbij;
         dbjk += f8 * v1 * branch * df7_dbjk;
         v[4] += f7 * v1 * branch * df8_ddb;
-        const double Gp = exp(-g[19] * ((bij - 2) * (bij - 2) + (bjk - 2) * (bjk - 2)));
+        const double Gp = xr_exp(-g[19] * ((bij - 2) * (bij - 2) + (bjk - 2) * (bjk - 2)));
         const double ep = pen1 * Fp * Gp;
         if (w.pgrad) {
           // dE/d(theta00, v1, v2, coa1, v7, pen1, v4) of this record
@@ -603,8 +604,8 @@ __global__ void __launch_bounds__(32 * kBondedWarps) k_angles(XrWork w, XrFF ff0
         v[5] += pen1 * dFp_dd * Gp;
         dbij += ep * (-2 * g[19] * (bij - 2));
         dbjk += ep * (-2 * g[19] * (bjk - 2));
-        const double K2 = exp(-g[38] * (ti_b * ti_b + tk_b * tk_b));
-        const double K3 = exp(-g[30] * ((bij - 1.5) * (bij - 1.5) + (bjk - 1.5) * (bjk - 1.5)));
+        const double K2 = xr_exp(-g[38] * (ti_b * ti_b + tk_b * tk_b));
+        const double K3 = xr_exp(-g[30] * ((bij - 1.5) * (bij - 1.5) + (bjk - 1.5) * (bjk - 1.5)));
         const double ec_ = coa1 * K1 * K2 * K3;
         if (w.pgrad) atomicAdd(xr_pgrad(w, j) + w.pgrad_angle_off + 7 * (size_t)(first + q) + 3, K1 * K2 * K3);
         v[2] += ec_;
@@ -811,7 +812,7 @@ __global__ void __launch_bounds__(32 * kBondedWarps) k_torsions(XrWork w, XrFF f
       const double db_j = AFV(AF_TOTAL, j) - atom_prm(ff, tj, A_VALENCY_BOC);
       const double db_k = AFV(AF_TOTAL, k) - atom_prm(ff, tk, A_VALENCY_BOC);
       const double ds = db_j + db_k;
-      const double ex3 = exp(-g[24] * ds), ex4 = exp(g[25] * ds);
+      const double ex3 = xr_exp(-g[24] * ds), ex4 = xr_exp(g[25] * ds);
       const double den = 1 + ex3 + ex4;
       const double b2 = BFV(BF_BO, m) - THB_CUT;
       cm[0] = v[0];
@@ -822,7 +823,7 @@ __global__ void __launch_bounds__(32 * kBondedWarps) k_torsions(XrWork w, XrFF f
       cm[5] = (2 + ex3) / den;  // f11
       cm[6] = (-g[24] * ex3 * den - (2 + ex3) * (-g[24] * ex3 + g[25] * ex4)) / (den * den);
       cm[7] = b2;
-      cm[8] = exp(-g[23] * b2);
+      cm[8] = xr_exp(-g[23] * b2);
       cm[9] = BFV(BF_BO, m);
 #pragma unroll
       for (int c = 0; c < NV; ++c) uacc[wl][lane][c] = 0.0;
@@ -868,14 +869,14 @@ __global__ void __launch_bounds__(32 * kBondedWarps) k_torsions(XrWork w, XrFF f
           const double V1 = __ldg(prm + 0), V2 = __ldg(prm + 1), V3 = __ldg(prm + 2), tor1 = __ldg(prm + 3),
                        cot1 = __ldg(prm + 4);
           const double b1 = bo_l - THB_CUT, b3 = bo_r - THB_CUT;
-          const double e1 = exp(-g[23] * b1), e3 = exp(-g[23] * b3);
+          const double e1 = xr_exp(-g[23] * b1), e3 = xr_exp(-g[23] * b3);
           const double y = 2 - pi_m - f11;
-          const double ex1 = exp(tor1 * y * y);
+          const double ex1 = xr_exp(tor1 * y * y);
           const double fn10 = (1 - e1) * (1 - e2) * (1 - e3);
           const double cv = 0.5 * (V1 * (1 + cw) + V2 * ex1 * (2 - 2 * cw * cw) + V3 * (1 + 4 * cw * cw * cw - 3 * cw));
           acc_v[0] = fn10 * sinprod * cv;
           const double q1 = b1 - 1.5, q2 = b2 - 1.5, q3 = b3 - 1.5;
-          const double fn12 = exp(-g[27] * (q1 * q1 + q2 * q2 + q3 * q3));
+          const double fn12 = xr_exp(-g[27] * (q1 * q1 + q2 * q2 + q3 * q3));
           const double conj = 1 + (cw * cw - 1) * sinprod;
           acc_v[1] = cot1 * fn12 * conj;
           const double dcv_dcw = 0.5 * (V1 - 4 * V2 * ex1 * cw + V3 * (12 * cw * cw - 3));
@@ -1076,7 +1077,7 @@ __global__ void __launch_bounds__(32 * kHbWarps, 4) k_hbonds(XrWork w, XrFF ff0)
           }
           if (!(r0 > 0)) continue;
           if (ebrow_k[k] != row) {
-            eb_k[k] = exp(-hb2 * d.bo);
+            eb_k[k] = xr_exp(-hb2 * d.bo);
             ebrow_k[k] = row;
           }
           const double eb = eb_k[k];
@@ -1086,7 +1087,7 @@ __global__ void __launch_bounds__(32 * kHbWarps, 4) k_hbonds(XrWork w, XrFF ff0)
           const double omc = 1 - cc;
           const double sin4 = 0.25 * omc * omc;
           const double Fb = hb1 * (1 - eb);
-          const double E2 = exp(-hb3 * (r0 * ira + ra * ir0 - 2));
+          const double E2 = xr_exp(-hb3 * (r0 * ira + ra * ir0 - 2));
           const double FE = Fb * E2;
           E += FE * sin4;
           acc[k][3] += hb1 * hb2 * eb * E2 * sin4;
@@ -1278,7 +1279,7 @@ __device__ inline void k_chain_radial_one(const XrWork& w, const XrFF& ff0, int 
     const XrFF ff = xr_ff_of(ff0, w, w.bond_i[b]);
     const int ti = w.type[w.bond_i[b]], tj = w.type[w.bond_j[b]], T = ff.ntypes, pt = ti * T + tj;
     double* gp = xr_pgrad(w, w.bond_i[b]) + (size_t)pt * XR_NPAIR_COLS;
-    const double r = w.b_r[b], lr = log(r), cut = 0.01 * ff.g[29];
+    const double r = w.b_r[b], lr = xr_log(r), cut = 0.01 * ff.g[29];
     const double adj[3] = {d_bo0, d_bo0 + BJV(BJ_PI0, b), d_bo0 + BJV(BJ_PP0, b)};
     const int cr[3] = {A_R_S, A_R_PI, A_R_PI_PI};
     const int ca[3] = {P_BO1, P_BO3, P_BO5}, cb[3] = {P_BO2, P_BO4, P_BO6}, cr0[3] = {P_RS, P_RP, P_RPP};
@@ -1286,8 +1287,8 @@ __device__ inline void k_chain_radial_one(const XrWork& w, const XrFF& ff0, int 
       if (!(atom_prm(ff, ti, cr[k]) > 0 && atom_prm(ff, tj, cr[k]) > 0) || adj[k] == 0.0) continue;
       const double pa = pair_prm(ff, pt, ca[k]), pb = pair_prm(ff, pt, cb[k]), r0 = pair_prm(ff, pt, cr0[k]);
       const double lt = lr - __ldg(ff.pair_logr + 3 * pt + k);
-      const double t = exp(pb * lt);
-      const double bo = (k == 0 ? 1.0 + cut : 1.0) * exp(pa * t);
+      const double t = xr_exp(pb * lt);
+      const double bo = (k == 0 ? 1.0 + cut : 1.0) * xr_exp(pa * t);
       atomicAdd(gp + ca[k], adj[k] * bo * t);
       atomicAdd(gp + cb[k], adj[k] * bo * pa * t * lt);
       atomicAdd(gp + cr0[k], adj[k] * bo * pa * t * (-pb / r0));
