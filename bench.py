@@ -752,6 +752,7 @@ def main():
         "errors": errors,
         "clocks": clocks.summary(),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "pass_ms": [round(1e3 * t, 2) for t in wall],
                 "api": "xreac_gb300.serving.Server.submit_many (the whole pass at once) with host numpy arrays, "
                        "results as Evaluation objects"},
         "gpu_launches": int(sum(b.launches for b in batches)),

@@ -119,6 +119,9 @@ struct XrFF {
   const double* pair_rmax;    // [T*T] distance beyond which the uncorrected bond order stays below cut/4
   const double* pair_inv;     // [T*T][2] 1 / r_vdW, 1 / rcore (IEEE: infinite for a zero rcore)
   double inv_g28;             // 1 / g[28], the vdW shielding exponent
+  // p = g[28], 1 / p, 1 / p - 1 and p - 1 as double-floats (hi, lo) for the pair kernel's vdW
+  // shielding chain in double-float arithmetic
+  float2 vdw_p, vdw_invp, vdw_invp_m1, vdw_p_m1;
   const int* is_carbon;       // [T] label is "C" (case-insensitive): C2 correction applies
   const int* hb_role;         // [T] 1 hydrogen-bond hydrogen, 2 donor/acceptor (p_hbond), 0 otherwise
   const int* angle_index;     // [T^3][2] first, count

@@ -138,6 +138,42 @@ __device__ inline double xr_exp(double x) {
   return __longlong_as_double(__double_as_longlong(v) + ((long long)n << 52));  // v 2^n: both normal
 }
 
+// exp(x) as a double-float for a double-float x with |x| < 80 whose own 48 bits are all it has (the
+// vdW shielding chain, |x| below 5 there): the reduction in FP32 as in xr_df_exp_float, with x.lo
+// added after the exact steps; 2^n applied to both floats (exact while they stay normal, n >= -100).
+__device__ inline xr_df xr_df_exp_df(xr_df x) {
+  if (!(fabsf(x.hi) < 80.0f)) {
+    const double v = exp((double)x.hi + (double)x.lo);
+    return xr_df_from_double(v);
+  }
+  const float C1 = 0x1.63p-7f, C2 = -0x1.bdp-19f, C3 = -0x1.05c61p-35f, C4 = -0x1.950d88p-60f;
+  const float kf = rintf(__fmul_rn(x.hi, 0x1.715476p+6f));
+  xr_df r = xr_df_two_sum(__fsub_rn(x.hi, __fmul_rn(kf, C1)), -__fmul_rn(kf, C2));
+  r = xr_df_add_f(r, x.lo);
+  const float p3 = __fmul_rn(kf, C3);
+  r = xr_df_add(r, {-p3, -__fmaf_rn(kf, C3, -p3)});
+  r = xr_df_add_f(r, -__fmul_rn(kf, C4));
+  int n;
+  xr_df m = xr_df_exp_finish(r, (int)kf, &n);
+  const float s = __int_as_float((127 + n) << 23);
+  m.hi = __fmul_rn(m.hi, s);
+  m.lo = __fmul_rn(m.lo, s);
+  return m;
+}
+
+// log(a) as a double-float for a double-float a in [1e-30, 1e30] (the Newton step of xr_log).
+__device__ inline xr_df xr_df_log_df(xr_df a) {
+  if (!(a.hi >= 1e-30f && a.hi <= 1e30f)) return xr_df_from_double(log((double)a.hi + (double)a.lo));
+  const float y0 = logf(a.hi);
+  int n;
+  xr_df e = xr_df_exp_float(-y0, &n);
+  const float s = __int_as_float((127 + n) << 23);
+  e.hi = __fmul_rn(e.hi, s);
+  e.lo = __fmul_rn(e.lo, s);
+  const xr_df t = xr_df_add_f(xr_df_mul(a, e), -1.0f);
+  return xr_df_add_f(xr_df_add_f(t, y0), __fmul_rn(-0.5f, __fmul_rn(t.hi, t.hi)));
+}
+
 // log(a), FP64 in and out.
 __device__ inline double xr_log(double a) {
   const xr_df ad = xr_df_from_double(a);

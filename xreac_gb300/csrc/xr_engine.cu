@@ -1588,6 +1588,14 @@ int ff_pack(xr_ff* f, const double* general, const double* atom, const double* p
   d.vdw_type = vdw_type;
   for (int k = 0; k < XR_NGENERAL; ++k) d.g[k] = general[k];
   d.inv_g28 = 1.0 / d.g[28];
+  auto as_df = [](double v) {
+    const float h = (float)v;
+    return make_float2(h, (float)(v - (double)h));
+  };
+  d.vdw_p = as_df(d.g[28]);
+  d.vdw_invp = as_df(d.inv_g28);
+  d.vdw_invp_m1 = as_df(d.inv_g28 - 1.0);
+  d.vdw_p_m1 = as_df(d.g[28] - 1.0);
   std::vector<unsigned char> host(total, 0);
   f->set0.clear();
   ff_fill_set(f, general, atom, pair, is_carbon, angle, torsion, hbond, host.data());

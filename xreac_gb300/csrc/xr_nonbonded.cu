@@ -80,13 +80,17 @@ __device__ inline void pair_one(const XrWork& w, const XrFF& ff0, int p) {
   const double dshield = dtaper * z - taper * r * r * (z2 * z2);
   double f13 = r, df13 = 1.0;
   // exponentials and logarithms in double-float arithmetic on the FP32 pipe (xr_dfloat.cuh): they
-  // were most of this kernel's FP64 issue
+  // were most of this kernel's FP64 issue. The shielding chain stays in double-floats from r to
+  // f13 = (r^p + gw)^(1/p) and df13 / dr = r^(p-1) sum^(1/p-1) = exp((p-1) log r + (1/p-1) log sum).
   if (ff.vdw_type == 1 || ff.vdw_type == 3) {
-    const double pw = ff.g[28];
-    const double rp = xr_exp(pw * xr_log(r));
-    const double sum = rp + __ldg(ff.pair_gw + pt);
-    f13 = xr_exp(xr_log(sum) * ff.inv_g28);
-    df13 = f13 * rp / (sum * r);
+    const xr_df lr = xr_df_log_df(xr_df_from_double(r));
+    const xr_df rp = xr_df_exp_df(xr_df_mul(lr, {ff.vdw_p.x, ff.vdw_p.y}));
+    const xr_df ls = xr_df_log_df(xr_df_add(rp, xr_df_from_double(__ldg(ff.pair_gw + pt))));
+    const xr_df f = xr_df_exp_df(xr_df_mul(ls, {ff.vdw_invp.x, ff.vdw_invp.y}));
+    const xr_df d = xr_df_exp_df(xr_df_add(xr_df_mul(lr, {ff.vdw_p_m1.x, ff.vdw_p_m1.y}),
+                                           xr_df_mul(ls, {ff.vdw_invp_m1.x, ff.vdw_invp_m1.y})));
+    f13 = (double)f.hi + (double)f.lo;
+    df13 = (double)d.hi + (double)d.lo;
   }
   // reciprocals of the pair's radii from the table: multiplies instead of FP64 divisions
   const double D = pair_prm(ff, pt, P_D), alpha = pair_prm(ff, pt, P_ALPHA);
