@@ -35,8 +35,12 @@ __device__ inline const double* atoms_of_system(const XrFF& ff, const XrSystem& 
 }
 
 __device__ inline void edge_vector(const XrSystem& S, const double4_32a& xi, const double4_32a& xj, uint32_t code, double v[3]) {
-  const int sx = xr_sx(code), sy = xr_sy(code), sz = xr_sz(code);
   const double xa[3] = {xi.x, xi.y, xi.z}, xb[3] = {xj.x, xj.y, xj.z};
+  if ((code & XR_SHIFT_MASK) == xr_pack_shift(0, 0, 0)) {  // no image shift: the offset is zero
+    for (int c = 0; c < 3; ++c) v[c] = __dsub_rn(xb[c], xa[c]);
+    return;
+  }
+  const int sx = xr_sx(code), sy = xr_sy(code), sz = xr_sz(code);
   for (int c = 0; c < 3; ++c) {
     const double off = __dadd_rn(__dadd_rn(__dmul_rn((double)sx, S.cell[c]), __dmul_rn((double)sy, S.cell[3 + c])),
                                  __dmul_rn((double)sz, S.cell[6 + c]));
@@ -46,7 +50,10 @@ __device__ inline void edge_vector(const XrSystem& S, const double4_32a& xi, con
 
 // t^(-1/3) for t in the float range: an FP32 seed, then two Newton-Raphson steps on f(z) = z^-3 - t,
 // z <- z (4 - t z^3) / 3, each of which squares the relative error (about 1e-7, 1e-14, then FP64
-// rounding). Multiplies only: it replaces a double cube root and the divisions by it.
+// rounding). Multiplies only: it replaces a double cube root and the divisions by it. It stays FP64:
+// the shield builds the QEq matrix, whose solve amplifies an entry's error by the matrix's condition
+// (a double-float version, about 1e-14, moved the Coulomb energy of an ill-conditioned fixture by 2e-12
+// of its value, beyond the parity tolerance).
 __device__ inline double inv_cbrt(double t) {
   double z = (double)rcbrtf((float)t);
   z = z * (4.0 - t * z * z * z) * (1.0 / 3.0);
@@ -74,7 +81,7 @@ __device__ inline void pair_one(const XrWork& w, const XrFF& ff0, int p) {
     dtaper = 140.0 * S.inv_rc * u * u * u * um * um * um;
   }
   const double gam = pair_prm(ff, pt, P_GAMMA);
-  const double z = inv_cbrt(r * r * r + gam);  // (r^3 + gamma)^(-1/3)
+  const double z = inv_cbrt(r * r * r + gam);  // (r^3 + gamma)^(-1/3), FP64: the QEq matrix is built from it
   const double z2 = z * z;
   const double shield = taper * z;
   const double dshield = dtaper * z - taper * r * r * (z2 * z2);

@@ -85,6 +85,10 @@ __global__ void k_prep(XrWork w) {
 __device__ inline void exact_vector(const XrSystem& S, const double4_32a& xi, const double4_32a& xj, int sx, int sy, int sz,
                                     double v[3]) {
   const double xa[3] = {xi.x, xi.y, xi.z}, xb[3] = {xj.x, xj.y, xj.z};
+  if ((sx | sy | sz) == 0) {  // no image shift: the offset is zero (the same values, FP64 work saved)
+    for (int c = 0; c < 3; ++c) v[c] = __dsub_rn(xb[c], xa[c]);
+    return;
+  }
   for (int c = 0; c < 3; ++c) {
     double off = __dadd_rn(__dadd_rn(__dmul_rn((double)sx, S.cell[0 * 3 + c]), __dmul_rn((double)sy, S.cell[1 * 3 + c])),
                            __dmul_rn((double)sz, S.cell[2 * 3 + c]));
