@@ -79,10 +79,12 @@ __device__ inline void bo1_tile(const XrWork& w, const XrFF& ff0, int b, int nb)
     const double4_32a xi = w.x[i], xj = w.x[j];
     const double xa[3] = {xi.x, xi.y, xi.z}, xb[3] = {xj.x, xj.y, xj.z};
     double v[3];
+    const bool shifted = (code & XR_SHIFT_MASK) != xr_pack_shift(0, 0, 0);  // else the offset is zero
     for (int c = 0; c < 3; ++c) {
-      const double off = __dadd_rn(__dadd_rn(__dmul_rn((double)sx, S.cell[c]), __dmul_rn((double)sy, S.cell[3 + c])),
-                                   __dmul_rn((double)sz, S.cell[6 + c]));
-      v[c] = __dadd_rn(__dsub_rn(xb[c], xa[c]), off);
+      v[c] = __dsub_rn(xb[c], xa[c]);
+      if (shifted)
+        v[c] = __dadd_rn(v[c], __dadd_rn(__dadd_rn(__dmul_rn((double)sx, S.cell[c]), __dmul_rn((double)sy, S.cell[3 + c])),
+                                         __dmul_rn((double)sz, S.cell[6 + c])));
     }
     const double r = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(v[0], v[0]), __dmul_rn(v[1], v[1])), __dmul_rn(v[2], v[2])));
     w.b_r[b] = r;
@@ -1050,10 +1052,12 @@ __global__ void __launch_bounds__(32 * kHbWarps, 4) k_hbonds(XrWork w, XrFF ff0)
           const double4_32a xa = w.x[ja];
           const int sx = xr_sx(sa), sy = xr_sy(sa), sz = xr_sz(sa);
           const double p0[3] = {xh.x, xh.y, xh.z}, p1[3] = {xa.x, xa.y, xa.z};
+          const bool shifted = sa != xr_pack_shift(0, 0, 0);  // else the offset is zero
           for (int c = 0; c < 3; ++c) {
-            const double off = __dadd_rn(__dadd_rn(__dmul_rn((double)sx, S.cell[c]), __dmul_rn((double)sy, S.cell[3 + c])),
-                                         __dmul_rn((double)sz, S.cell[6 + c]));
-            va[c] = __dadd_rn(__dsub_rn(p1[c], p0[c]), off);
+            va[c] = __dsub_rn(p1[c], p0[c]);
+            if (shifted)
+              va[c] = __dadd_rn(va[c], __dadd_rn(__dadd_rn(__dmul_rn((double)sx, S.cell[c]), __dmul_rn((double)sy, S.cell[3 + c])),
+                                                 __dmul_rn((double)sz, S.cell[6 + c])));
           }
         }
         const double ra = sqrt(va[0] * va[0] + va[1] * va[1] + va[2] * va[2]);
