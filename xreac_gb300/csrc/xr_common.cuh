@@ -159,6 +159,10 @@ struct XrWork {
   // one array instead of three.
   int types_in_x;
   int prep_zero;              // k_prep zeroes the call's counters (evaluations; not the static count)
+  // [A] the QEq preconditioner's bonds: the first and the last atom j of the kGroupMax - 1 atoms
+  // before a that lies within 1.3 A of a (an image counts), or INT_MAX / -1 (set by k_pairs)
+  int* qb_first;
+  int* qb_last;
   int* bx_count;              // exported bonds of the call (zeroed by k_prep)
   int4* wrap;                 // integer lattice wrap of each atom
   float4* xw;                 // wrapped position minus origin, FP32

@@ -194,6 +194,10 @@ struct xr_ctx {
   int* mlist = nullptr;
   int* nact = nullptr;
   size_t cnact = 0;
+  int* qb_first = nullptr;
+  size_t cqb_first = 0;
+  int* qb_last = nullptr;
+  size_t cqb_last = 0;
   int4* chunks = nullptr;
   size_t cchunks = 0;
   int2* sys_chunks = nullptr;
@@ -347,6 +351,8 @@ bool ensure_atoms(xr_ctx* c, int A, int S) {
   GROW(esum, (size_t)XR_ESUM_N * A);
   GROW(nact, A);
   GROW(nnz, A);
+  GROW(qb_first, A);
+  GROW(qb_last, A);
   GROW(sys_chunks, S);
   GROW(qsmall, S);
   GROW(qiters, S);
@@ -442,6 +448,8 @@ void fill_work(xr_ctx* c, XrWork& w, int A, int S, unsigned flags) {
   w.type = c->type;
   w.sys_of = c->sys_of;
   w.bx_count = c->bx_count;
+  w.qb_first = c->qb_first;
+  w.qb_last = c->qb_last;
   w.wrap = c->wrap;
   w.xw = c->xw;
   w.fw = c->fw;
@@ -1752,7 +1760,7 @@ void xr_ctx_destroy(xr_ctx* c) {
                   c->pair_bond, c->p_r, c->p_shield, c->p_dshield, c->p_g, c->p_evdw, c->p_ecoul, c->bond_pair,
                   c->bond_i, c->bond_j, c->b_r, c->b_v, c->b_fwd, c->b_adj, c->b_e, c->dbrow, c->sys, c->energy,
                   c->props, c->status, c->counts, c->barrier, c->qmap, c->qsmall, c->qiters, c->red, c->qguess, c->qrhs, c->qadj, c->pgrad, c->bx_count,
-                  c->esum, c->arow, c->nact, c->nzrow, c->nnz, c->chunks, c->sys_chunks, c->chunk_part, c->mids, c->nmids, c->mlist,
+                  c->esum, c->arow, c->nact, c->nzrow, c->nnz, c->qb_first, c->qb_last, c->chunks, c->sys_chunks, c->chunk_part, c->mids, c->nmids, c->mlist,
                   c->cand_cnt, c->cand_edge, c->sys_list, c->atom_cell, c->atom_slot, c->cell_cnt, c->cell_atoms,
                   c->mid_tiles, c->qsplit};
   for (void* p : bufs)
@@ -2004,7 +2012,7 @@ long long xr_footprint_bytes(int atoms, int systems, long long edges, long long 
   if (atoms < 1 || systems < 1 || edges < 0 || bonds < 0) return -1;
   // the buffers of ensure_atoms, ensure_lists and xr_ctx_reserve, per element
   const long long per_atom = sizeof(double4_32a) + 2 * sizeof(int) + sizeof(int4) + 2 * sizeof(float4) + 4 * sizeof(int) +
-                             (AF_N + AJ_N + 8 + 4 + 3 + XR_QW_N + 8 + XR_ESUM_N) * sizeof(double) + 6 * sizeof(int);
+                             (AF_N + AJ_N + 8 + 4 + 3 + XR_QW_N + 8 + XR_ESUM_N) * sizeof(double) + 8 * sizeof(int);
   const long long per_system = sizeof(int2) + 3 * sizeof(int) + sizeof(XrSystem) + 20 * sizeof(double);
   const long long per_edge = sizeof(int2) + 2 * sizeof(int) + sizeof(double) + sizeof(float) + sizeof(unsigned short);
   const long long per_pair = 3 * sizeof(int) + 6 * sizeof(double);

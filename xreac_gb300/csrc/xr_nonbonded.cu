@@ -61,6 +61,11 @@ __device__ inline double inv_cbrt(double t) {
   return z;
 }
 
+// The QEq block-Jacobi groups: runs of at most kGroupMax consecutive atoms, each within kGroupBond of
+// an earlier atom of its run (molecules).
+constexpr int kGroupMax = 8;
+constexpr double kGroupBond = 1.3;
+
 // ------------------------------------------------------------------------------ pair kernel
 __device__ inline void pair_one(const XrWork& w, const XrFF& ff0, int p) {
   const int e = w.pair_edge[p], i = w.pair_i[p];
@@ -71,6 +76,11 @@ __device__ inline void pair_one(const XrWork& w, const XrFF& ff0, int p) {
   double v[3];
   edge_vector(S, w.x[i], w.x[j], (uint32_t)ed.y, v);
   const double r = __dsqrt_rn(__dadd_rn(__dadd_rn(__dmul_rn(v[0], v[0]), __dmul_rn(v[1], v[1])), __dmul_rn(v[2], v[2])));
+  if (r < kGroupBond && i != j && abs(i - j) < kGroupMax) {  // a bond for the QEq preconditioner's groups
+    const int lo = min(i, j), hi = max(i, j);
+    atomicMin(w.qb_first + hi, lo);
+    atomicMax(w.qb_last + hi, lo);
+  }
   const double rc = S.rc;
   const int T = ff.ntypes, pt = w.type[i] * T + w.type[j];
   double taper = 0.0, dtaper = 0.0;
@@ -934,8 +944,6 @@ __device__ inline bool team_sumf(const Team& team, const XrWork& w, float* v, fl
 //   rp[m + 1] row starts relative to the cache; first[m], size[m] the group of each row (16-bit)
 // M is block-Jacobi: groups of at most 8 consecutive own rows whose atoms are joined by distances
 // below 1.3 A (molecules), each block H restricted to the group. One-row groups are Jacobi.
-constexpr int kGroupMax = 8;
-constexpr double kGroupBond = 1.3;
 // Stop of an FP32 sweep of the row solver: its squared preconditioned norm falls by this factor, or to
 // a hundredth of the final target. 1e-10 (1e-5 in norm) for the textbook CG of blocks and clusters,
 // 1e-7 (about 3e-4) for the pipelined CG of grid teams.
@@ -950,20 +958,10 @@ __host__ __device__ constexpr double sweep_ratio32() {
 // only joins rows that close). A molecule cut in two loses its strong intramolecular couplings to the
 // plain Jacobi part of the preconditioner: on the 4,608-atom water box that took 84 CG iterations
 // instead of 69, on 300-atom clusters 52 instead of 39.
-// Whether row i (local) has such a bond to a row in [max(0, i - 7), r): rows are sorted by j, so
-// those edges are one range, found by bisection.
+// Whether row i (local) has such a bond to a row in [max(0, i - 7), r): the first bonded atom of that
+// window, which k_pairs recorded, lies before r.
 __device__ inline bool qeq_row_bonded_before(const XrWork& w, int a0, int i, int r) {
-  const int lo = a0 + max(0, i - (kGroupMax - 1)), hi = a0 + r;
-  int b = w.cnt[a0 + i], t = w.cnt[a0 + i + 1];
-  const int end = t;
-  while (b < t) {
-    const int mid = (b + t) >> 1;
-    if (w.edge[mid].x < lo) b = mid + 1;
-    else t = mid;
-  }
-  for (int e = b; e < end && w.edge[e].x < hi; ++e)
-    if (__ldg(w.p_r + w.edge_pair[e]) < kGroupBond) return true;
-  return false;
+  return __ldcg(w.qb_first + a0 + i) < a0 + r;
 }
 
 // The nearest split at or after r (within kGroupMax - 1 rows) that cuts no group, else r; one warp,
@@ -1054,21 +1052,11 @@ __device__ __noinline__ bool qeq_rows32_setup(const XrWork& w, const double* ata
   const double* DI = &QW(Q_DINV, 0);
   const int gs = row_group(m), sub = lane & (gs - 1), gpw = 32 / gs;
   // 1. for every own row, the latest of the kGroupMax - 1 own rows before it that is bonded to it
-  //    (distance below kGroupBond); rows further back cannot share its group. Columns come from the
-  //    row cache, and a distance is read only for a candidate column.
+  //    (distance below kGroupBond, recorded by k_pairs); rows further back cannot share its group
   int* prev = reinterpret_cast<int*>(R.binv);  // scratch until the inverses are written
-  for (int ib = wid * gpw; ib < m; ib += nw * gpw) {
-    const int i = ib + lane / gs;
-    int best = -1;
-    if (i < m) {
-      const int a = a0 + r0 + i, lo = max(0, i - (kGroupMax - 1));
-      for (int e = w.cnt[a] + sub; e < w.cnt[a + 1]; e += gs) {
-        const int c = int(M.cache_j[e - M.ebeg]) - r0;
-        if (c >= lo && c < i && c > best && __ldg(w.p_r + w.edge_pair[e]) < kGroupBond) best = c;
-      }
-    }
-    for (int o = gs / 2; o > 0; o >>= 1) best = max(best, __shfl_xor_sync(0xffffffffu, best, o));
-    if (sub == 0 && i < m) prev[i] = best;
+  for (int i = tid; i < m; i += blockDim.x) {
+    const int last = __ldcg(w.qb_last + a0 + r0 + i);
+    prev[i] = last >= a0 + r0 ? last - (a0 + r0) : -1;
   }
   __syncthreads();
   // 2. groups: runs of consecutive rows, each bonded to an earlier row of its run, at most kGroupMax

@@ -32,6 +32,8 @@ __global__ void k_prep(XrWork w) {
       *w.bx_count = 0;
     }
     if (a < w.S) w.qiters[a] = 0;
+    w.qb_first[a] = 0x7fffffff;
+    w.qb_last[a] = -1;
   }
   const double4_32a p = w.x[a];
   int sys;
