@@ -590,8 +590,8 @@ def differentiation_numbers(local, copies=256):
 SERVER_WORKERS = 6
 SERVER_BATCH_ATOMS = 8192
 
-STAGE_NAMES = ["neighbour_count_scan", "neighbour_fill_reverse", "pairs_vdw_shield", "qeq_cg", "coulomb",
-               "bond_orders", "bonded_terms_and_adjoint", "forces_reduce_pack"]
+STAGE_NAMES = ["neighbour_count_scan", "neighbour_fill_reverse", "pairs_vdw_shield", "qeq_cg", "charge_response",
+               "bond_orders", "bonded_terms_and_adjoint", "coulomb_forces_reduce_pack"]
 
 
 def main():

@@ -292,8 +292,10 @@ int xr_last_transfer_bytes(const xr_ctx* ctx, long long* h2d, long long* d2h);
 /* Per-stage device timing with CUDA events on the context stream (no reference counterpart;
  * instrumentation). enable=1 resets the accumulators. Stages: 0 neighbour count + scan (including
  * the host read of the list sizes), 1 row fill + reverse map, 2 pair kernel (vdW, shield) and QEq
- * matrix rows, 3 QEq solve, 4 Coulomb, 5 bond orders (uncorrected, Delta', corrected), 6 bonded
- * terms + adjoint chain, 7 force assembly + reductions + result packing. ms receives the summed
+ * matrix rows, 3 QEq solve, 4 charge response (the adjoint QEq solve; empty unless the call asks
+ * for the charge-response derivative or the QEq parameters' gradient), 5 bond orders (uncorrected,
+ * Delta', corrected), 6 bonded terms + adjoint chain, 7 Coulomb energy + force assembly +
+ * reductions + result packing. ms receives the summed
  * milliseconds of the first n (at most 8) stages over *calls evaluations. */
 int xr_ctx_set_profiling(xr_ctx* ctx, int enable);
 int xr_ctx_stage_times(const xr_ctx* ctx, double* ms, int n, long long* calls);

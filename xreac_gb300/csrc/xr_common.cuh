@@ -86,6 +86,7 @@ struct XrSystem {
   double total_charge;
   int has_guess;         // QEq starts from w.qguess (charges of an earlier step) instead of Q/n
   int ff_set;            // parameter set of the force field this system is evaluated with
+  int chunk0;            // the system's first energy-reduction chunk (XR_CHUNK_ATOMS atoms each) in the batch
   // Cell list (when the call bins its atoms): cells per lattice direction (0: not binned), cell
   // offsets searched per direction, the system's first cell in the batch's cell arrays, and the map
   // of a fractional coordinate f to its cell, floor((f - cell_f0) * cell_scale) (wrapped f in
@@ -240,10 +241,7 @@ struct XrWork {
   // outputs
   double* energy;             // [S][16]: 14 components, total, pad
   double* props;              // [S][4]: dipole xyz, pad
-  // deterministic per-system reductions: per-atom energy sums, then fixed atom chunks per system
-  double* esum;               // [XR_ESUM_N][A]
-  const int4* chunks;         // [nchunks] {system, first atom, end atom, 0}
-  const int2* sys_chunks;     // [S] {first chunk, end chunk}
+  // deterministic per-system reductions: fixed atom chunks per system (XrSystem::chunk0 onwards)
   double* chunk_part;         // [nchunks][XR_PART_N]
   int nchunks;
 };
@@ -308,9 +306,8 @@ enum BF { BF_BO0 = 0, BF_PI0, BF_PP0, BF_DSIG, BF_DPI, BF_DPP, BF_BO, BF_PI, BF_
 enum BJ { BJ_BO = 0, BJ_PI, BJ_PP, BJ_SIG, BJ_BO0, BJ_PI0, BJ_PP0, BJ_CI, BJ_CJ, BJ_N };
 
 #define XR_QW_N 12
-#define XR_ESUM_N 14
 #define XR_PART_N 24
-#define XR_CHUNK_ATOMS 1024
+#define XR_CHUNK_ATOMS 64
 
 // Kernel launchers (defined in the .cu files, called by the engine).
 void xr_launch_topology(const XrWork& w, cudaStream_t st);  // xr_launch_prep, then xr_launch_count
@@ -353,7 +350,6 @@ constexpr int kQeqClusterSingle = 8;
 int xr_qeq_max_clusters(int csize);
 int xr_launch_qeq_cluster(const XrWork& w, const XrFF& ff, cudaStream_t st, int csize, int nblocks, const int* list,
                           int nbig, int nsmall, bool adjoint = false);
-void xr_launch_coulomb(const XrWork& w, const XrFF& ff, cudaStream_t st);
 void xr_launch_bond_orders(const XrWork& w, const XrFF& ff, cudaStream_t st);  // k_bo1, k_deltap, k_bo2
 void xr_launch_bonded(const XrWork& w, const XrFF& ff, cudaStream_t st);       // energy terms and adjoint chain
 void xr_launch_forces(const XrWork& w, const XrFF& ff, cudaStream_t st);

@@ -2,8 +2,8 @@
 //
 // Sequence per call: upload positions and system descriptors -> count neighbour rows -> scan ->
 // (grow buffers) -> fill rows, pairs, bonds, reverse map -> pair kernel (vdW, shield) -> QEq ->
-// Coulomb -> bond orders, bonded energies and adjoints -> force assembly -> per-system reductions
-// -> one copy of the packed per-atom results back to the host (or straight into device outputs).
+// bond orders, bonded energies and adjoints -> Coulomb energy and force assembly -> per-system
+// reductions -> one copy of the packed per-atom results back to the host (or straight into device outputs).
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -178,8 +178,6 @@ struct xr_ctx {
   size_t cqwork = 0;
   double* outbuf = nullptr;
   size_t coutbuf = 0;
-  double* esum = nullptr;
-  size_t cesum = 0;
   int2* arow = nullptr;
   size_t carow = 0;
   int2* nzrow = nullptr;
@@ -198,10 +196,6 @@ struct xr_ctx {
   size_t cqb_first = 0;
   int* qb_last = nullptr;
   size_t cqb_last = 0;
-  int4* chunks = nullptr;
-  size_t cchunks = 0;
-  int2* sys_chunks = nullptr;
-  size_t csys_chunks = 0;
   double* chunk_part = nullptr;
   size_t cchunk_part = 0;
   // edge / pair / bond buffers
@@ -264,10 +258,6 @@ struct xr_ctx {
   size_t ch_sysof = 0;
   XrSystem* h_sysd = nullptr;
   size_t ch_sysd = 0;
-  int4* h_chunks = nullptr;
-  size_t ch_chunks = 0;
-  int2* h_syschunks = nullptr;
-  size_t ch_syschunks = 0;
   int4* h_qmap_p = nullptr;
   size_t ch_qmap_p = 0;
   int* h_qsmall_p = nullptr;
@@ -348,12 +338,10 @@ bool ensure_atoms(xr_ctx* c, int A, int S) {
   GROW(f, 3 * (size_t)A);
   GROW(qwork, (size_t)XR_QW_N * A);
   GROW(outbuf, 8 * (size_t)A);
-  GROW(esum, (size_t)XR_ESUM_N * A);
   GROW(nact, A);
   GROW(nnz, A);
   GROW(qb_first, A);
   GROW(qb_last, A);
-  GROW(sys_chunks, S);
   GROW(qsmall, S);
   GROW(qiters, S);
   GROW(sys, S);
@@ -465,11 +453,8 @@ void fill_work(xr_ctx* c, XrWork& w, int A, int S, unsigned flags) {
   w.qsplit = c->qsplit;
   w.energy = c->energy;
   w.props = c->props;
-  w.esum = c->esum;
   w.nact = c->nact;
   w.nnz = c->nnz;
-  w.chunks = c->chunks;
-  w.sys_chunks = c->sys_chunks;
   w.chunk_part = c->chunk_part;
 }
 
@@ -1026,23 +1011,14 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
       if (mode == kScan) mode = kCell;
     }
   }
+  // energy-reduction chunks: each system's atoms in runs of XR_CHUNK_ATOMS, numbered in system order
   size_t nchunk = 0;
-  for (int s = 0; s < nsys; ++s) nchunk += (size_t)(sys[s].natoms + XR_CHUNK_ATOMS - 1) / XR_CHUNK_ATOMS;
-  if (!host_grow(&c->h_chunks, &c->ch_chunks, nchunk) || !host_grow(&c->h_syschunks, &c->ch_syschunks, (size_t)nsys) ||
-      !grow(c, &c->chunks, &c->cchunks, nchunk) || !grow(c, &c->chunk_part, &c->cchunk_part, nchunk * (size_t)XR_PART_N))
-    return cuda_fail(c, cudaErrorMemoryAllocation, "allocation");
-  int4* chunk_tab = c->h_chunks;
-  int2* sys_chunk_tab = c->h_syschunks;
-  {
-    int k = 0;
-    for (int s = 0, a = 0; s < nsys; ++s) {
-      sys_chunk_tab[s].x = k;
-      for (int b = 0; b < sys[s].natoms; b += XR_CHUNK_ATOMS)
-        chunk_tab[k++] = make_int4(s, a + b, a + std::min(sys[s].natoms, b + XR_CHUNK_ATOMS), 0);
-      sys_chunk_tab[s].y = k;
-      a += sys[s].natoms;
-    }
+  for (int s = 0; s < nsys; ++s) {
+    c->host_sys[s].chunk0 = (int)nchunk;
+    nchunk += (size_t)(sys[s].natoms + XR_CHUNK_ATOMS - 1) / XR_CHUNK_ATOMS;
   }
+  if (!grow(c, &c->chunk_part, &c->cchunk_part, nchunk * (size_t)XR_PART_N))
+    return cuda_fail(c, cudaErrorMemoryAllocation, "allocation");
   std::memcpy(c->h_sysd, c->host_sys.data(), sizeof(XrSystem) * nsys);
   cudaStream_t st = c->stream;
   long long launches = 0;
@@ -1065,9 +1041,7 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
     h2d += 2 * sizeof(int) * (long long)A;
   }
   cudaMemcpyAsync(c->sys, c->h_sysd, sizeof(XrSystem) * nsys, cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(c->chunks, chunk_tab, sizeof(int4) * nchunk, cudaMemcpyHostToDevice, st);
-  cudaMemcpyAsync(c->sys_chunks, sys_chunk_tab, sizeof(int2) * nsys, cudaMemcpyHostToDevice, st);
-  h2d += sizeof(XrSystem) * (long long)nsys + (long long)(sizeof(int4) * nchunk + sizeof(int2) * nsys);
+  h2d += sizeof(XrSystem) * (long long)nsys;
   // (counts, QEq iterations, scans, torsion-middle and exported-bond counters: zeroed by k_prep)
   cudaMemsetAsync(c->status, 0, sizeof(int), st);
   XrWork w;
@@ -1200,8 +1174,8 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
     return qcluster ? xr_launch_qeq_cluster(w, ff->d, st, qcsize, qblocks, c->qsmall, qbig, qsmall, adjoint)
                     : xr_launch_qeq(w, ff->d, st, qblocks, c->qmap, qteam, c->qsmall, qsmall, adjoint);
   };
-  // The launch sequence: rows, pairs, QEq, Coulomb, bond orders, bonded terms, forces, reductions,
-  // bond export. Returns 0 or a CUDA error of a launch.
+  // The launch sequence: rows, pairs, QEq, bond orders, bonded terms, Coulomb energy and forces,
+  // reductions, bond export. Returns 0 or a CUDA error of a launch.
   auto sequence = [&]() -> int {
     stage(c, 1, st);
     if (mode == kScan)
@@ -1223,8 +1197,6 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
     if (int le = launch_qeq(false)) return le;
     launches += (qcluster ? qbig > 0 : qteam > 0) ? 2 : 1;  // the teams' row splits, then the solver
     stage(c, 4, st);
-    xr_launch_coulomb(w, ff->d, st);
-    launches += 1;
     const bool qeq_grad = w.pgrad && (flags & XR_FLAG_QEQ_GRADIENT);
     if (w.full_derivative || qeq_grad) {
       // the adjoint QEq solve with the same plan: charge-response forces (its radial pair terms)
@@ -1251,7 +1223,7 @@ int run_batch(xr_ctx* c, const xr_ff* ff, int nsys, const xr_system* sys, unsign
     xr_launch_forces(w, ff->d, st);
     launches += 1;
     xr_launch_reduce(w, ff->d, st);
-    launches += 3;
+    launches += 2;
     if (nB > 0) {  // (its counter was zeroed by k_prep)
       k_bond_export<<<(nB + 255) / 256, 256, 0, st>>>(w, bx_rec, c->bx_count);
       ++launches;
@@ -1760,7 +1732,7 @@ void xr_ctx_destroy(xr_ctx* c) {
                   c->pair_bond, c->p_r, c->p_shield, c->p_dshield, c->p_g, c->p_evdw, c->p_ecoul, c->bond_pair,
                   c->bond_i, c->bond_j, c->b_r, c->b_v, c->b_fwd, c->b_adj, c->b_e, c->dbrow, c->sys, c->energy,
                   c->props, c->status, c->counts, c->barrier, c->qmap, c->qsmall, c->qiters, c->red, c->qguess, c->qrhs, c->qadj, c->pgrad, c->bx_count,
-                  c->esum, c->arow, c->nact, c->nzrow, c->nnz, c->qb_first, c->qb_last, c->chunks, c->sys_chunks, c->chunk_part, c->mids, c->nmids, c->mlist,
+                  c->arow, c->nact, c->nzrow, c->nnz, c->qb_first, c->qb_last, c->chunk_part, c->mids, c->nmids, c->mlist,
                   c->cand_cnt, c->cand_edge, c->sys_list, c->atom_cell, c->atom_slot, c->cell_cnt, c->cell_atoms,
                   c->mid_tiles, c->qsplit};
   for (void* p : bufs)
@@ -1768,7 +1740,7 @@ void xr_ctx_destroy(xr_ctx* c) {
   if (c->h_x) cudaFreeHost(c->h_x);
   if (c->h_out) cudaFreeHost(c->h_out);
   if (c->h_guess) cudaFreeHost(c->h_guess);
-  for (void* hp : {(void*)c->h_types, (void*)c->h_sysof, (void*)c->h_sysd, (void*)c->h_chunks, (void*)c->h_syschunks,
+  for (void* hp : {(void*)c->h_types, (void*)c->h_sysof, (void*)c->h_sysd,
                    (void*)c->h_qmap_p, (void*)c->h_qsmall_p, (void*)c->h_pg, (void*)c->h_cand_cnt, (void*)c->h_cand_edge, (void*)c->h_sys_list})
     if (hp) cudaFreeHost(hp);
   if (c->h_small) cudaFreeHost(c->h_small);
@@ -1983,9 +1955,12 @@ int xr_ctx_reserve(xr_ctx* c, int atoms, int systems, long long edges, long long
   if (!c || atoms < 1 || systems < 1 || edges < 0 || bonds < 0) return XR_EINPUT;
   cudaSetDevice(c->device);
   const long long chunks = (long long)systems + atoms / XR_CHUNK_ATOMS + 1;
+  // pinned host buffers too: a call within the reservation allocates and frees no page-locked memory
+  // (whose allocation stalls, and whose release waits for the whole device, other threads' work included)
   if (!ensure_atoms(c, atoms, systems) || !host_grow(&c->h_x, &c->ch_x, (size_t)atoms) ||
-      !host_grow(&c->h_guess, &c->ch_guess, (size_t)atoms) || !ensure_lists(c, edges, edges / 2, bonds) ||
-      !grow(c, &c->chunks, &c->cchunks, (size_t)chunks) ||
+      !host_grow(&c->h_guess, &c->ch_guess, (size_t)atoms) || !host_grow(&c->h_types, &c->ch_types, (size_t)atoms) ||
+      !host_grow(&c->h_sysof, &c->ch_sysof, (size_t)atoms) || !host_grow(&c->h_sysd, &c->ch_sysd, (size_t)systems) ||
+      !host_grow(&c->h_qsmall_p, &c->ch_qsmall_p, (size_t)systems) || !ensure_lists(c, edges, edges / 2, bonds) ||
       !grow(c, &c->chunk_part, &c->cchunk_part, (size_t)chunks * XR_PART_N) ||
       !grow(c, &c->outbuf, &c->coutbuf, result_layout(atoms, systems, bonds).end) ||
       !host_grow(&c->h_out, &c->ch_out, result_layout(atoms, systems, bonds).end) ||
@@ -2012,7 +1987,7 @@ long long xr_footprint_bytes(int atoms, int systems, long long edges, long long 
   if (atoms < 1 || systems < 1 || edges < 0 || bonds < 0) return -1;
   // the buffers of ensure_atoms, ensure_lists and xr_ctx_reserve, per element
   const long long per_atom = sizeof(double4_32a) + 2 * sizeof(int) + sizeof(int4) + 2 * sizeof(float4) + 4 * sizeof(int) +
-                             (AF_N + AJ_N + 8 + 4 + 3 + XR_QW_N + 8 + XR_ESUM_N) * sizeof(double) + 8 * sizeof(int);
+                             (AF_N + AJ_N + 8 + 4 + 3 + XR_QW_N + 8) * sizeof(double) + 8 * sizeof(int);
   const long long per_system = sizeof(int2) + 3 * sizeof(int) + sizeof(XrSystem) + 20 * sizeof(double);
   const long long per_edge = sizeof(int2) + 2 * sizeof(int) + sizeof(double) + sizeof(float) + sizeof(unsigned short);
   const long long per_pair = 3 * sizeof(int) + 6 * sizeof(double);
@@ -2021,7 +1996,7 @@ long long xr_footprint_bytes(int atoms, int systems, long long edges, long long 
   const long long per_cells = 4 * sizeof(int) + 2 * sizeof(int);  // cand_cnt, atom_cell, atom_slot, cell_atoms, cell_cnt
   const long long base = (long long)atoms * (per_atom + per_cells) + (long long)systems * (per_system + 64 * sizeof(int)) +
                          edges * (per_edge + sizeof(int2)) + (edges / 2) * per_pair + bonds * per_bond +
-                         chunks * (sizeof(int4) + XR_PART_N * sizeof(double));
+                         chunks * XR_PART_N * sizeof(double);
   const long long red = (long long)sizeof(double) * 4 * 8 * 2048;  // reduction scratch, at least this
   // grow()'s headroom (n + n/4 + 64 elements per buffer), rounded up by 2 %
   return (base + red) * 5 / 4 + (base + red) / 50 + 64ll * 64 * 16;

@@ -2162,27 +2162,18 @@ __global__ void k_pairs(XrWork w, XrFF ff0) {
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) pair_one(w, ff0, p);
 }
 
-// ------------------------------------------------------------------------------ Coulomb
-__global__ void k_coulomb(XrWork w) {
-  const int np = xr_num_pairs(w);
-  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < np; p += gridDim.x * blockDim.x) {
-    const int i = w.pair_i[p], j = w.edge[w.pair_edge[p]].x;
-    const double qq = C_ELE * w.q[i] * w.q[j];
-    w.p_ecoul[p] = qq * w.p_shield[p];
-    w.p_g[p] += qq * w.p_dshield[p];
-  }
-}
-
 // ------------------------------------------------------------------------ force assembly
-// Every radial sensitivity (vdW, Coulomb, bond-order chain) sits on its pair: dE/dx_j += G v/r,
-// dE/dx_i -= G v/r.
+// The pair's shielded Coulomb energy 332.06371 q_i q_j shield(r) is formed here, with the final
+// charges, and its dE/dr joins the pair's radial sensitivity (vdW, charge response, bond-order
+// chain): dE/dx_j += G v/r, dE/dx_i -= G v/r.
 __device__ inline void pair_force_one(const XrWork& w, int p) {
-  const double G = w.p_g[p];
-  if (G == 0.0) return;
   const int i = w.pair_i[p];
   const int2 ed = w.edge[w.pair_edge[p]];
   const int j = ed.x;
-  if (i == j) return;  // a self-image pair moves both ends together: no net force
+  const double qq = C_ELE * w.q[i] * w.q[j];
+  w.p_ecoul[p] = qq * w.p_shield[p];
+  const double G = w.p_g[p] + qq * w.p_dshield[p];
+  if (G == 0.0 || i == j) return;  // a self-image pair moves both ends together: no net force
   const XrSystem& S = w.sys[w.sys_of[i]];
   double v[3];
   edge_vector(S, w.x[i], w.x[j], (uint32_t)ed.y, v);
@@ -2199,65 +2190,58 @@ __global__ void k_pair_forces(XrWork w) {
 }
 
 // ------------------------------------------------------------------------ reductions
-// Energies land per item (pair, bond, atom). A warp per atom first folds its own pairs and half
-// bonds into per-atom component sums; fixed chunks of at most XR_CHUNK_ATOMS atoms of one system
-// are then summed by one block each, and one block per system adds its chunks in order. Every sum
-// has a fixed order, so energies, charges and dipoles are bitwise reproducible.
-#define ESUM(k, a) w.esum[(size_t)(k) * w.A + (a)]
-
-__global__ void k_energy_gather(XrWork w) {
-  const int lane = threadIdx.x & 31;
-  const int a = (int)((blockIdx.x * (unsigned)blockDim.x + threadIdx.x) >> 5);
-  if (a >= w.A) return;
-  const int L = w.A + 1;
-  double ev = 0, ec = 0, eb = 0, ec2 = 0, et = 0, eco = 0;
-  for (int p = w.cnt[1 * L + a] + lane; p < w.cnt[1 * L + a + 1]; p += 32) {
-    ev += w.p_evdw[p];
-    ec += w.p_ecoul[p];
-  }
-  for (int b = w.cnt[2 * L + a] + lane; b < w.cnt[2 * L + a + 1]; b += 32) {
-    eb += w.b_e[0 * w.cap_B + b];
-    ec2 += w.b_e[1 * w.cap_B + b];
-    et += w.b_e[2 * w.cap_B + b];
-    eco += w.b_e[3 * w.cap_B + b];
-  }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    ev += __shfl_xor_sync(0xffffffffu, ev, o);
-    ec += __shfl_xor_sync(0xffffffffu, ec, o);
-    eb += __shfl_xor_sync(0xffffffffu, eb, o);
-    ec2 += __shfl_xor_sync(0xffffffffu, ec2, o);
-    et += __shfl_xor_sync(0xffffffffu, et, o);
-    eco += __shfl_xor_sync(0xffffffffu, eco, o);
-  }
-  if (lane == 0) {
-    ESUM(C_BOND, a) = eb;
-    ESUM(C_ATOM, a) = AEV(1, a);
-    ESUM(C_LONE_PAIR, a) = AEV(0, a) + ec2;
-    ESUM(C_MOLECULE, a) = 0.0;
-    ESUM(C_ANGLE, a) = AEV(2, a);
-    ESUM(C_PENALTY, a) = AEV(3, a);
-    ESUM(C_ANGLE_CONJ, a) = AEV(4, a);
-    ESUM(C_HBOND, a) = AEV(5, a);
-    ESUM(C_TORSION, a) = et;
-    ESUM(C_CONJ, a) = eco;
-    ESUM(C_VDW, a) = ev;
-    ESUM(C_COULOMB, a) = ec;
-    ESUM(C_EFIELD, a) = 0.0;
-    ESUM(C_QEQ, a) = AEV(6, a);
-  }
-}
+// Energies land per item (pair, bond, atom). The atoms of each system are cut into fixed chunks of
+// at most XR_CHUNK_ATOMS, numbered in system order from XrSystem::chunk0; pairs and half bonds are
+// stored by their first atom, so a chunk's atoms own contiguous ranges of both, and one block sums
+// the chunk's pair, bond and atom terms directly. One block per system then adds its chunks in
+// order. Every sum has a fixed order that depends only on the system, so energies, charges and
+// dipoles are bitwise reproducible and the same whatever else a batch holds. The adds are FP64 (a
+// warp instruction takes 64 cycles of the FP64 pipe), so chunks are small enough to spread over the
+// SMs, and the block's partials are summed slot by slot (a few adds per lane, then five shuffles)
+// rather than each warp reducing all 23 slots.
+constexpr int kReduceThreads = 128;
 
 // Partial slots: 0..13 components, 14 mass, 15..17 mass * x, 18 charge, 19..21 charge * x, 22 finite.
-__global__ void k_reduce_chunk(XrWork w, XrFF ff) {
-  __shared__ double smem[XR_PART_N * 32];
-  const int4 ch = w.chunks[blockIdx.x];
-  const double* atab = atoms_of_system(ff, w.sys[ch.x]);
+__global__ void __launch_bounds__(kReduceThreads) k_reduce_chunk(XrWork w, XrFF ff) {
+  __shared__ double part[XR_PART_N][kReduceThreads];
+  // the chunk's system: the last one that starts at or before it (a system without atoms has no
+  // chunks and starts where the next one does)
+  const int chunk = blockIdx.x;
+  int lo = 0, hi = w.S - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (w.sys[mid].chunk0 <= chunk)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  const XrSystem& S = w.sys[lo];
+  const int a_beg = S.atom_off + (chunk - S.chunk0) * XR_CHUNK_ATOMS;
+  const int4 ch = make_int4(lo, a_beg, min(S.atom_off + S.natoms, a_beg + XR_CHUNK_ATOMS), 0);
+  const int L = w.A + 1, tid = threadIdx.x;
+  const double* atab = atoms_of_system(ff, S);
   double v[XR_PART_N];
+#pragma unroll
   for (int k = 0; k < XR_PART_N; ++k) v[k] = 0.0;
+  for (int p = w.cnt[1 * L + ch.y] + tid; p < w.cnt[1 * L + ch.z]; p += kReduceThreads) {
+    v[C_VDW] += w.p_evdw[p];
+    v[C_COULOMB] += w.p_ecoul[p];
+  }
+  for (int b = w.cnt[2 * L + ch.y] + tid; b < w.cnt[2 * L + ch.z]; b += kReduceThreads) {
+    v[C_BOND] += w.b_e[0 * w.cap_B + b];
+    v[C_LONE_PAIR] += w.b_e[1 * w.cap_B + b];
+    v[C_TORSION] += w.b_e[2 * w.cap_B + b];
+    v[C_CONJ] += w.b_e[3 * w.cap_B + b];
+  }
   double finite = 1.0;
-  for (int a = ch.y + threadIdx.x; a < ch.z; a += blockDim.x) {
-    for (int k = 0; k < XR_NCOMP; ++k) v[k] += ESUM(k, a);
+  for (int a = ch.y + tid; a < ch.z; a += kReduceThreads) {
+    v[C_LONE_PAIR] += AEV(0, a);
+    v[C_ATOM] += AEV(1, a);
+    v[C_ANGLE] += AEV(2, a);
+    v[C_PENALTY] += AEV(3, a);
+    v[C_ANGLE_CONJ] += AEV(4, a);
+    v[C_HBOND] += AEV(5, a);
+    v[C_QEQ] += AEV(6, a);
     const double m = atom_prm(atab, w.type[a], A_MASS);
     const double4_32a x = w.x[a];
     const double q = w.q[a];
@@ -2272,27 +2256,26 @@ __global__ void k_reduce_chunk(XrWork w, XrFF ff) {
     if (!(isfinite(q) && isfinite(w.f[3 * a]) && isfinite(w.f[3 * a + 1]) && isfinite(w.f[3 * a + 2]))) finite = 0.0;
   }
   v[22] = finite;
-  // block sum (finite combines by min)
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int k = 0; k < XR_PART_N; ++k)
-    for (int o = 16; o > 0; o >>= 1) {
-      const double y = __shfl_xor_sync(0xffffffffu, v[k], o);
-      v[k] = (k == 22) ? fmin(v[k], y) : v[k] + y;
-    }
-  if (lane == 0)
-    for (int k = 0; k < XR_PART_N; ++k) smem[k * 32 + wid] = v[k];
+#pragma unroll
+  for (int k = 0; k < XR_PART_N; ++k) part[k][tid] = v[k];
   __syncthreads();
-  if (threadIdx.x < XR_PART_N) {
-    const int k = threadIdx.x;
-    double s = k == 22 ? 1.0 : 0.0;
-    for (int q = 0; q < nw; ++q) s = (k == 22) ? fmin(s, smem[k * 32 + q]) : s + smem[k * 32 + q];
-    w.chunk_part[(size_t)blockIdx.x * XR_PART_N + k] = s;
+  // slot k by warp k % 4: four partials per lane in thread order, then the warp's butterfly (finite
+  // combines by min)
+  const int lane = tid & 31, wid = tid >> 5;
+  for (int k = wid; k < XR_PART_N; k += kReduceThreads / 32) {
+    double s = part[k][lane];
+    for (int t = lane + 32; t < kReduceThreads; t += 32) s = k == 22 ? fmin(s, part[k][t]) : s + part[k][t];
+    for (int o = 16; o > 0; o >>= 1) {
+      const double y = __shfl_xor_sync(0xffffffffu, s, o);
+      s = k == 22 ? fmin(s, y) : s + y;
+    }
+    if (lane == 0) w.chunk_part[(size_t)blockIdx.x * XR_PART_N + k] = s;
   }
 }
 
 __global__ void k_reduce_final(XrWork w) {
   const int s = blockIdx.x;
-  const int2 r = w.sys_chunks[s];
+  const int2 r = make_int2(w.sys[s].chunk0, w.sys[s].chunk0 + (w.sys[s].natoms + XR_CHUNK_ATOMS - 1) / XR_CHUNK_ATOMS);
   const int k = threadIdx.x;
   __shared__ double tot[XR_PART_N];
   if (k < XR_PART_N) {
@@ -2480,10 +2463,6 @@ int xr_launch_qeq(const XrWork& w, const XrFF& ff, cudaStream_t st, int nblocks,
 // stage 1: each pair's radial term -14.4 (lambda_i q_j + lambda_j q_i) dshield/dr.
 
 
-void xr_launch_coulomb(const XrWork& w, const XrFF& ff, cudaStream_t st) {
-  (void)ff;
-  if (w.nP > 0) k_coulomb<<<(w.nP + 255) / 256, 256, 0, st>>>(w);
-}
 
 void xr_launch_forces(const XrWork& w, const XrFF& ff, cudaStream_t st) {
   (void)ff;
@@ -2491,8 +2470,7 @@ void xr_launch_forces(const XrWork& w, const XrFF& ff, cudaStream_t st) {
 }
 
 void xr_launch_reduce(const XrWork& w, const XrFF& ff, cudaStream_t st) {
-  k_energy_gather<<<(w.A + 7) / 8, 256, 0, st>>>(w);
-  k_reduce_chunk<<<w.nchunks, 256, 0, st>>>(w, ff);
+  k_reduce_chunk<<<w.nchunks, kReduceThreads, 0, st>>>(w, ff);
   k_reduce_final<<<w.S, 32, 0, st>>>(w);
 }
 
