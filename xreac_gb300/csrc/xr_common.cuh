@@ -307,7 +307,7 @@ enum BJ { BJ_BO = 0, BJ_PI, BJ_PP, BJ_SIG, BJ_BO0, BJ_PI0, BJ_PP0, BJ_CI, BJ_CJ,
 
 #define XR_QW_N 12
 #define XR_PART_N 24
-#define XR_CHUNK_ATOMS 64
+#define XR_CHUNK_ATOMS 32
 
 // Kernel launchers (defined in the .cu files, called by the engine).
 void xr_launch_topology(const XrWork& w, cudaStream_t st);  // xr_launch_prep, then xr_launch_count

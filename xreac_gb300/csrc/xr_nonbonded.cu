@@ -2223,10 +2223,12 @@ __global__ void __launch_bounds__(kReduceThreads) k_reduce_chunk(XrWork w, XrFF 
   double v[XR_PART_N];
 #pragma unroll
   for (int k = 0; k < XR_PART_N; ++k) v[k] = 0.0;
+#pragma unroll 4
   for (int p = w.cnt[1 * L + ch.y] + tid; p < w.cnt[1 * L + ch.z]; p += kReduceThreads) {
     v[C_VDW] += w.p_evdw[p];
     v[C_COULOMB] += w.p_ecoul[p];
   }
+#pragma unroll 2
   for (int b = w.cnt[2 * L + ch.y] + tid; b < w.cnt[2 * L + ch.z]; b += kReduceThreads) {
     v[C_BOND] += w.b_e[0 * w.cap_B + b];
     v[C_LONE_PAIR] += w.b_e[1 * w.cap_B + b];
@@ -2273,18 +2275,25 @@ __global__ void __launch_bounds__(kReduceThreads) k_reduce_chunk(XrWork w, XrFF 
   }
 }
 
-__global__ void k_reduce_final(XrWork w) {
+// One block per system: warp k % 8 sums slot k over the system's chunks (a strided pass per lane in
+// chunk order, then the warp's butterfly).
+constexpr int kFinalThreads = 256;
+__global__ void __launch_bounds__(kFinalThreads) k_reduce_final(XrWork w) {
   const int s = blockIdx.x;
-  const int2 r = make_int2(w.sys[s].chunk0, w.sys[s].chunk0 + (w.sys[s].natoms + XR_CHUNK_ATOMS - 1) / XR_CHUNK_ATOMS);
-  const int k = threadIdx.x;
+  const int c0 = w.sys[s].chunk0, c1 = c0 + (w.sys[s].natoms + XR_CHUNK_ATOMS - 1) / XR_CHUNK_ATOMS;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, k = threadIdx.x;
   __shared__ double tot[XR_PART_N];
-  if (k < XR_PART_N) {
-    double acc = k == 22 ? 1.0 : 0.0;
-    for (int c = r.x; c < r.y; ++c) {
-      const double v = w.chunk_part[(size_t)c * XR_PART_N + k];
-      acc = (k == 22) ? fmin(acc, v) : acc + v;
+  for (int slot = wid; slot < XR_PART_N; slot += kFinalThreads / 32) {
+    double acc = slot == 22 ? 1.0 : 0.0;
+    for (int c = c0 + lane; c < c1; c += 32) {
+      const double v = w.chunk_part[(size_t)c * XR_PART_N + slot];
+      acc = slot == 22 ? fmin(acc, v) : acc + v;
     }
-    tot[k] = acc;
+    for (int o = 16; o > 0; o >>= 1) {
+      const double y = __shfl_xor_sync(0xffffffffu, acc, o);
+      acc = slot == 22 ? fmin(acc, y) : acc + y;
+    }
+    if (lane == 0) tot[slot] = acc;
   }
   __syncthreads();
   if (k == 0) {
@@ -2471,7 +2480,7 @@ void xr_launch_forces(const XrWork& w, const XrFF& ff, cudaStream_t st) {
 
 void xr_launch_reduce(const XrWork& w, const XrFF& ff, cudaStream_t st) {
   k_reduce_chunk<<<w.nchunks, kReduceThreads, 0, st>>>(w, ff);
-  k_reduce_final<<<w.S, 32, 0, st>>>(w);
+  k_reduce_final<<<w.S, kFinalThreads, 0, st>>>(w);
 }
 
 namespace {

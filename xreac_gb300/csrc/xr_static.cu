@@ -52,7 +52,6 @@ constexpr size_t kScratchBytes = kOffSys + align256(sizeof(XrSystem));
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 
 std::mutex g_setup_mutex;
-unsigned char* g_scratch_ptr[kMaxDevices] = {};
 thread_local const char* g_err = "";
 
 int fail(int code, const char* msg) {
@@ -60,19 +59,17 @@ int fail(int code, const char* msg) {
   return code;
 }
 
-// Device address of the scratch array on the current device, looked up once per device.
+// Device address of the scratch array on the current device, looked up on every call (a runtime table
+// lookup): a cached address would go stale after a device reset re-creates the primary context.
 int scratch_for_current_device(unsigned char** out) {
   int dev = -1;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
     return fail(XR_ECUDA, "no usable current CUDA device");
   std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (!g_scratch_ptr[dev]) {
-    void* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
-    if (e != cudaSuccess || !p) return fail(XR_ECUDA, "cudaGetSymbolAddress of the static scratch failed");
-    g_scratch_ptr[dev] = static_cast<unsigned char*>(p);
-  }
-  *out = g_scratch_ptr[dev];
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
+  if (e != cudaSuccess || !p) return fail(XR_ECUDA, "cudaGetSymbolAddress of the static scratch failed");
+  *out = static_cast<unsigned char*>(p);
   return XR_OK;
 }
 
