@@ -2194,8 +2194,8 @@ __global__ void k_pair_forces(XrWork w) {
 // at most XR_CHUNK_ATOMS, numbered in system order from XrSystem::chunk0; pairs and half bonds are
 // stored by their first atom, so a chunk's atoms own contiguous ranges of both, and one block sums
 // the chunk's pair, bond and atom terms directly. One block per system then adds its chunks in
-// order. Every sum has a fixed order that depends only on the system, so energies, charges and
-// dipoles are bitwise reproducible and the same whatever else a batch holds. The adds are FP64 (a
+// order. Every sum has a fixed order (the system's chunks, each in thread and lane order), so
+// energies, charges and dipoles are bitwise reproducible from call to call. The adds are FP64 (a
 // warp instruction takes 64 cycles of the FP64 pipe), so chunks are small enough to spread over the
 // SMs, and the block's partials are summed slot by slot (a few adds per lane, then five shuffles)
 // rather than each warp reducing all 23 slots.
