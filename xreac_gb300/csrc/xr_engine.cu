@@ -1960,7 +1960,9 @@ int xr_ctx_reserve(xr_ctx* c, int atoms, int systems, long long edges, long long
   if (!ensure_atoms(c, atoms, systems) || !host_grow(&c->h_x, &c->ch_x, (size_t)atoms) ||
       !host_grow(&c->h_guess, &c->ch_guess, (size_t)atoms) || !host_grow(&c->h_types, &c->ch_types, (size_t)atoms) ||
       !host_grow(&c->h_sysof, &c->ch_sysof, (size_t)atoms) || !host_grow(&c->h_sysd, &c->ch_sysd, (size_t)systems) ||
-      !host_grow(&c->h_qsmall_p, &c->ch_qsmall_p, (size_t)systems) || !ensure_lists(c, edges, edges / 2, bonds) ||
+      !host_grow(&c->h_qsmall_p, &c->ch_qsmall_p, (size_t)systems) ||
+      !host_grow(&c->h_qmap_p, &c->ch_qmap_p, (size_t)std::max(1, std::min(c->nsm * c->coop_per_sm, kQeqBlocks))) ||
+      !ensure_lists(c, edges, edges / 2, bonds) ||
       !grow(c, &c->chunk_part, &c->cchunk_part, (size_t)chunks * XR_PART_N) ||
       !grow(c, &c->outbuf, &c->coutbuf, result_layout(atoms, systems, bonds).end) ||
       !host_grow(&c->h_out, &c->ch_out, result_layout(atoms, systems, bonds).end) ||
