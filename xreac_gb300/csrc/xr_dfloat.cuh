@@ -62,13 +62,6 @@ __device__ inline xr_df xr_df_mul(xr_df a, xr_df b) {
   return xr_df_fast_two_sum(p, e);
 }
 
-__device__ inline xr_df xr_df_mul_f(xr_df a, float b) {
-  const float p = __fmul_rn(a.hi, b);
-  float e = __fmaf_rn(a.hi, b, -p);
-  e = __fmaf_rn(a.lo, b, e);
-  return xr_df_fast_two_sum(p, e);
-}
-
 // 2^(j/64) as (hi, lo), j = 0..63
 static __device__ const float2 xr_df_exp2_64[64] = {
     {0x1.0000000000000p+0f, 0x0.0p+0f}, {0x1.02c9a40000000p+0f, -0x1.887fa00000000p-28f},
