@@ -33,3 +33,9 @@ def test_package_never_imports_the_oracle():
     for path in (ROOT / "xreac_gb300").rglob("*.py"):
         text = path.read_text()
         assert "import oracle" not in text and "from oracle" not in text, path
+
+
+def test_integration_guide_lists_every_entry_point():
+    doc = (ROOT / "INTEGRATION.md").read_text()
+    missing = [n for n in declared_functions() if f"`{n}`" not in doc]
+    assert not missing, missing
